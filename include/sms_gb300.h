@@ -1,0 +1,227 @@
+/*
+ * sms_gb300.h -- C ABI of the GB300 (sm_103a) Specular Manifold Sampling library.
+ *
+ * This is the drop-in boundary for the reference's SMS solvers.  Every entry point
+ * takes plain pointers and sizes; no C++ or torch types cross it, no exception
+ * escapes it, and every function returns an sms_status code (0 = ok).
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   SMSConfig                                 include/mitsuba/render/manifold.h:11-45
+ *   integrator XML parameters                 src/integrators/path_sms_ss.cpp:47-61,
+ *                                             src/integrators/path_sms_ms.cpp:149-161,
+ *                                             src/integrators/path_sms_glints.cpp:42-54
+ *   SpecularManifoldSingleScatter             include/mitsuba/render/manifold_ss.h:9-159
+ *     ::specular_manifold_sampling(si,sampler) src/librender/manifold_ss.cpp:28-201
+ *     ::sample_path(shape,si,ei,sampler,n_offset,p_start)
+ *                                             src/librender/manifold_ss.cpp:203-279
+ *   SpecularManifoldMultiScatter              include/mitsuba/render/manifold_ms.h:9-166
+ *     ::specular_manifold_sampling            src/librender/manifold_ms.cpp:27-201
+ *     ::sample_path                           src/librender/manifold_ms.cpp:203-227
+ *   SpecularManifoldGlints(+Vectorized)       include/mitsuba/render/manifold_glints.h:9-208
+ *     ::specular_manifold_sampling            src/librender/manifold_glints.cpp:28-223
+ *     ::sample_glint(...,xi_start)            src/librender/manifold_glints.cpp:225-265
+ *   print_statistics() counters               src/librender/manifold_ss.cpp:14-18,859-883
+ *
+ * Where the reference calls the solver once per shading point from many host
+ * threads, this library takes a whole wavefront of shading points ("queries")
+ * per call and solves them on the GPU.  Query and result buffers are
+ * component-major SoA: field f of query i lives at buf[f * n + i].
+ */
+#ifndef SMS_GB300_H
+#define SMS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum sms_status {
+    SMS_OK = 0,
+    SMS_ERR_INVALID_ARG = 1,   /* null pointer, bad size, unknown id            */
+    SMS_ERR_CUDA = 2,          /* a CUDA runtime call failed                     */
+    SMS_ERR_DEVICE_LIMIT = 3,  /* a bounded device loop hit its limit            */
+    SMS_ERR_UNSUPPORTED = 4,   /* configuration the library does not implement   */
+    SMS_ERR_PARSE = 5,         /* integrator XML block could not be parsed       */
+    SMS_ERR_NO_DEVICE = 6      /* no CUDA device                                  */
+} sms_status;
+
+/* Human-readable text of the last error on this host thread. */
+const char *sms_last_error(void);
+
+/* ------------------------------------------------------------------ config */
+/* Same fields, names and defaults as the reference's SMSConfig
+ * (include/mitsuba/render/manifold.h:11-45) plus the integrator-level switches
+ * the SMS integrators read (path_sms_glints.cpp:42-54). */
+typedef struct sms_config {
+    int32_t biased;                 /* false */
+    int32_t twostage;               /* false */
+    int32_t halfvector_constraints; /* false */
+    int32_t mnee_init;              /* false */
+    float   step_scale;             /* 1     */
+    int32_t max_iterations;         /* 20    */
+    float   solver_threshold;       /* 1e-5  */
+    float   uniqueness_threshold;   /* 1e-4  */
+    int32_t max_trials;             /* -1    */
+    int32_t bounces;                /* 1 (path_sms_ms default is 2) */
+    int32_t bsdf_strategy_only;     /* false */
+    int32_t sms_strategy_only;      /* false */
+    int32_t glints_vectorized;      /* false */
+} sms_config;
+
+/* Fill *cfg with the reference defaults. */
+void sms_config_default(sms_config *cfg);
+
+/* Parse one <integrator type="path_sms_ss|path_sms_ms|path_sms_glints"> block
+ * (the XML subset the reference's integrators read with props.bool_/int_/float_).
+ * Unknown parameters are ignored like the reference's Properties lookups ignore
+ * them; type_out (may be NULL) receives the integrator type string. */
+sms_status sms_config_parse_xml(const char *xml, sms_config *cfg,
+                                char *type_out, size_t type_cap);
+
+/* ------------------------------------------------------------------- scene */
+/* Shape flags: src/librender/shape.cpp:78-82 */
+#define SMS_SHAPE_CAUSTIC_RECEIVER      (1u << 0)
+#define SMS_SHAPE_CAUSTIC_CASTER_SINGLE (1u << 1)
+#define SMS_SHAPE_CAUSTIC_CASTER_MULTI  (1u << 2)
+#define SMS_SHAPE_CAUSTIC_BOUNCER       (1u << 3)
+#define SMS_SHAPE_GLINTY                (1u << 4)
+/* Emitter flags: src/librender/emitter.cpp:9-10 */
+#define SMS_EMITTER_CAUSTIC_SINGLE      (1u << 0)
+#define SMS_EMITTER_CAUSTIC_MULTI       (1u << 1)
+
+/* BSDF kinds the SMS path distinguishes (bsdf.cpp:53-60, dielectric.cpp:328-334,
+ * conductor.cpp:288-295).  Only the fields the solver reads are kept. */
+typedef enum sms_bsdf_type {
+    SMS_BSDF_DIFFUSE = 0,     /* ior() = (0, 1): treated as eta = 1            */
+    SMS_BSDF_DIELECTRIC = 1,  /* smooth dielectric, eta = int_ior / ext_ior     */
+    SMS_BSDF_CONDUCTOR = 2    /* smooth conductor, complex ior (eta, k)         */
+} sms_bsdf_type;
+
+typedef struct sms_bsdf {
+    int32_t type;       /* sms_bsdf_type                                        */
+    float   eta;        /* dielectric relative IOR, or conductor real part      */
+    float   k;          /* conductor imaginary part                             */
+    float   albedo[3];  /* diffuse reflectance (receivers)                      */
+} sms_bsdf;
+
+typedef struct sms_scene sms_scene;  /* host-side scene builder (owned by caller) */
+
+sms_status sms_scene_create(sms_scene **out);
+void       sms_scene_destroy(sms_scene *scene);
+
+/* Analytic sphere (src/shapes/sphere.cpp). shape_id_out may be NULL. */
+sms_status sms_scene_add_sphere(sms_scene *scene, const float center[3], float radius,
+                                int32_t flip_normals, const sms_bsdf *bsdf,
+                                uint32_t flags, int32_t *shape_id_out);
+
+/* Triangle mesh (src/librender/mesh.cpp).  positions: n_vertices*3 floats,
+ * normals/texcoords: optional (NULL) n_vertices*3 / *2 floats, faces: n_faces*3
+ * vertex indices.  Data is copied. */
+sms_status sms_scene_add_mesh(sms_scene *scene, const float *positions,
+                              const float *normals, const float *texcoords,
+                              uint32_t n_vertices, const uint32_t *faces,
+                              uint32_t n_faces, const sms_bsdf *bsdf,
+                              uint32_t flags, int32_t *shape_id_out);
+
+/* Point light (src/emitters/point.cpp). */
+sms_status sms_scene_add_point_emitter(sms_scene *scene, const float position[3],
+                                       const float intensity[3], uint32_t flags);
+
+/* Area light attached to an existing sphere shape (src/emitters/area.cpp). */
+sms_status sms_scene_add_area_emitter(sms_scene *scene, int32_t shape_id,
+                                      const float radiance[3], uint32_t flags);
+
+/* --------------------------------------------------------------- context */
+typedef struct sms_ctx sms_ctx;   /* device copy of a scene + config + scratch */
+
+/* Upload the scene (BVH build on the host, copy to device 'device'). */
+sms_status sms_ctx_create(const sms_scene *scene, const sms_config *cfg,
+                          int32_t device, sms_ctx **out);
+void       sms_ctx_destroy(sms_ctx *ctx);
+sms_status sms_ctx_set_config(sms_ctx *ctx, const sms_config *cfg);
+/* The CUDA stream all work of this context is issued on (a cudaStream_t). */
+void      *sms_ctx_stream(sms_ctx *ctx);
+/* Launch shape of the persistent kernels: blocks per SM and threads per block
+ * (0 = library default).  Set by the autotuner. */
+sms_status sms_ctx_set_launch(sms_ctx *ctx, int32_t blocks_per_sm, int32_t threads_per_block);
+
+/* ---------------------------------------------------------------- queries */
+/* Shading-point query, SoA with SMS_QUERY_FIELDS rows of n floats each:
+ *   row 0-2   p        position on the receiver
+ *   row 3-5   n        shading normal (= geometric normal of the receiver)
+ *   row 6-8   dp_du    position partial
+ *   row 9-11  dp_dv    position partial
+ *   row 12-14 albedo   diffuse reflectance of the receiver (RGB)
+ *   row 15    cos_i    cosine of the incident (camera) direction in the local
+ *                      frame; the diffuse BSDF returns 0 when it is <= 0
+ * The receiver is taken as locally flat (dn/du = dn/dv = 0), as for the
+ * reference's rectangle receivers (src/shapes/rectangle.cpp:210-214). */
+#define SMS_QUERY_FIELDS 16
+
+/* Per-query estimator result, SoA:
+ *   value   3 rows of n floats: RGB contribution of all caustic casters
+ *   count   n int32: unbiased -> Bernoulli-trial count of the last caster
+ *           (0 when its first walk failed or was occluded; -1 when the trial cap
+ *           was hit); biased -> number of unique solutions summed over casters
+ *   walks   n int32: number of sample_path() calls made for this query          */
+typedef struct sms_result {
+    float   *value;
+    int32_t *count;
+    int32_t *walks;
+} sms_result;
+
+/* Solver statistics, same counters as manifold_ss.cpp:14-18 (accumulated per
+ * context since creation or the last reset). */
+typedef struct sms_stats {
+    uint64_t solver_succeeded;
+    uint64_t solver_failed;
+    uint64_t bernoulli_trial_calls;
+    uint64_t bernoulli_trial_iterations;
+    uint64_t bernoulli_trial_iterations_max;
+    uint64_t walks;
+    uint64_t newton_iterations;
+    uint64_t connections;
+    uint64_t rays;          /* rays cast by the connection kernel        */
+    uint64_t bvh_nodes;     /* BVH nodes fetched (64 bytes each)         */
+    uint64_t tri_tests;     /* triangles fetched (48 bytes each)         */
+} sms_stats;
+
+sms_status sms_stats_read(sms_ctx *ctx, sms_stats *out);
+sms_status sms_stats_reset(sms_ctx *ctx);
+
+/* ------------------------------------------------------- single scatter */
+/* SpecularManifoldSingleScatter::specular_manifold_sampling for n queries
+ * (manifold_ss.cpp:28-201).  Query i draws its random numbers from a PCG32
+ * stream (state seed 'seed', stream index i + stream_offset), in the same order
+ * as the reference's per-query sampler calls.  Host pointers: copied in and out
+ * on the context stream, synchronous. */
+sms_status sms_ss_connect_batch(sms_ctx *ctx, const float *queries, uint32_t n,
+                                uint64_t seed, uint64_t stream_offset,
+                                sms_result *out);
+
+/* Same, device pointers (queries, out->*), asynchronous on the context stream. */
+sms_status sms_ss_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
+                                       uint32_t n, uint64_t seed,
+                                       uint64_t stream_offset, sms_result *out_dev);
+
+/* Per-walk entry point: SpecularManifoldSingleScatter::sample_path with an
+ * explicit start point (manifold_ss.cpp:203-279, p_start != 0), the harness
+ * the reference's figure scripts use.
+ *   queries   SoA as above (n columns)
+ *   walk_in   SoA, SMS_WALK_IN_FIELDS rows: ei.p (3), p_start (3),
+ *             sample (2; used by sample_position when p_start == 0)
+ *   caster    shape id of the specular shape to walk on
+ *   walk_out  SoA, SMS_WALK_OUT_FIELDS rows: ok, iterations, p_final (3),
+ *             p_init (3), n_final (3)   (ok/iterations stored as floats)       */
+#define SMS_WALK_IN_FIELDS 8
+#define SMS_WALK_OUT_FIELDS 11
+sms_status sms_ss_walk_batch(sms_ctx *ctx, int32_t caster, const float *queries,
+                             const float *walk_in, uint32_t n, float *walk_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMS_GB300_H */

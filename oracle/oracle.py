@@ -1,0 +1,156 @@
+"""ctypes binding of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline / reference arm of bench.py, always as the checker or the CPU
+baseline, never as part of the GPU library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+LIB_PATH = ORACLE_DIR / "liboracle.so"
+FMA_LIB_PATH = ORACLE_DIR / "liboracle_fma.so"
+
+_LIB = None
+_LIBS = {}
+
+
+class _Config(C.Structure):
+    _fields_ = [("biased", C.c_int32), ("twostage", C.c_int32),
+                ("halfvector_constraints", C.c_int32), ("mnee_init", C.c_int32),
+                ("step_scale", C.c_float), ("max_iterations", C.c_int32),
+                ("solver_threshold", C.c_float), ("uniqueness_threshold", C.c_float),
+                ("max_trials", C.c_int32), ("bounces", C.c_int32),
+                ("bsdf_strategy_only", C.c_int32), ("sms_strategy_only", C.c_int32),
+                ("glints_vectorized", C.c_int32)]
+
+
+class _Bsdf(C.Structure):
+    _fields_ = [("type", C.c_int32), ("eta", C.c_float), ("k", C.c_float),
+                ("albedo", C.c_float * 3)]
+
+
+def build() -> Path:
+    """Compile liboracle.so with the committed Makefile."""
+    r = subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB_PATH
+
+
+def load(fma: bool = False):
+    """The oracle library; fma=True gives the FMA-contracted build used to
+    measure the floating-point chaos floor."""
+    global _LIB
+    key = bool(fma)
+    if key in _LIBS:
+        return _LIBS[key]
+    path = FMA_LIB_PATH if fma else LIB_PATH
+    if not path.exists():
+        build()
+    lib = C.CDLL(str(path))
+    vp, i32, u32, u64, f32 = C.c_void_p, C.c_int32, C.c_uint32, C.c_uint64, C.c_float
+    sig = {
+        "oracle_scene_create": (vp, []),
+        "oracle_scene_destroy": (None, [vp]),
+        "oracle_scene_add_sphere": (i32, [vp, C.POINTER(f32), f32, i32, C.POINTER(_Bsdf), u32]),
+        "oracle_scene_add_mesh": (i32, [vp, vp, vp, vp, u32, vp, u32, C.POINTER(_Bsdf), u32]),
+        "oracle_scene_add_point_emitter": (i32, [vp, C.POINTER(f32), C.POINTER(f32), u32]),
+        "oracle_scene_add_area_emitter": (i32, [vp, i32, C.POINTER(f32), u32]),
+        "oracle_scene_finalize": (None, [vp]),
+        "oracle_ss_walk_batch": (i32, [vp, C.POINTER(_Config), i32, vp, vp, u32, vp]),
+        "oracle_ss_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int,
+                                          vp]),
+        "oracle_fresnel": (f32, [f32, f32, C.POINTER(f32)]),
+        "oracle_fresnel_conductor": (f32, [f32, f32, f32]),
+        "oracle_uniform_sphere": (None, [f32, f32, C.POINTER(f32)]),
+        "oracle_pcg32": (None, [u64, u64, u32, vp]),
+        "oracle_pcg32_f32": (None, [u64, u64, u32, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIBS[key] = lib
+    if not fma:
+        _LIB = lib
+    return lib
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+def _cfg(config) -> _Config:
+    c = _Config()
+    for name, _ in _Config._fields_:
+        setattr(c, name, getattr(config, name))
+    return c
+
+
+def _bsdf(b) -> _Bsdf:
+    r = _Bsdf()
+    r.type, r.eta, r.k = b.type, b.eta, b.k
+    r.albedo[:] = [float(x) for x in b.albedo]
+    return r
+
+
+class OracleScene:
+    """The oracle's copy of a SceneDesc (same shape ids, same emitter order)."""
+
+    def __init__(self, desc, fma: bool = False):
+        lib = load(fma)
+        self._lib = lib
+        self._h = lib.oracle_scene_create()
+        self._keep = []
+        for kind, idx in desc.order:
+            if kind == "sphere":
+                c, r, flip, b, flags = desc.spheres[idx]
+                lib.oracle_scene_add_sphere(self._h, _f3(c), r, int(flip), C.byref(_bsdf(b)), flags)
+            else:
+                P, N, UV, F, b, flags = desc.meshes[idx]
+                self._keep += [P, N, UV, F]
+                lib.oracle_scene_add_mesh(self._h, P.ctypes.data, None if N is None else N.ctypes.data,
+                                          None if UV is None else UV.ctypes.data, P.shape[0],
+                                          F.ctypes.data, F.shape[0], C.byref(_bsdf(b)), flags)
+        for pos, I, flags in desc.point_emitters:
+            lib.oracle_scene_add_point_emitter(self._h, _f3(pos), _f3(I), flags)
+        for sid, L, flags in desc.area_emitters:
+            lib.oracle_scene_add_area_emitter(self._h, sid, _f3(L), flags)
+        lib.oracle_scene_finalize(self._h)
+
+    def walk_batch(self, config, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
+        n = queries.shape[1]
+        q = np.ascontiguousarray(queries, np.float32)
+        w = np.ascontiguousarray(walk_in, np.float32)
+        out = np.zeros((11, n), np.float32)
+        self._lib.oracle_ss_walk_batch(self._h, C.byref(_cfg(config)), caster, q.ctypes.data, w.ctypes.data, n,
+                                  out.ctypes.data)
+        return out
+
+    def connect_batch(self, config, queries: np.ndarray, seed: int = 0, stream_offset: int = 0,
+                      nthreads: int | None = None):
+        n = queries.shape[1]
+        q = np.ascontiguousarray(queries, np.float32)
+        value = np.zeros((3, n), np.float32)
+        count = np.zeros(n, np.int32)
+        walks = np.zeros(n, np.int32)
+        stats = np.zeros(8, np.uint64)
+        nt = nthreads or os.cpu_count() or 1
+        self._lib.oracle_ss_connect_batch(self._h, C.byref(_cfg(config)), q.ctypes.data, n, seed, stream_offset,
+                                     value.ctypes.data, count.ctypes.data, walks.ctypes.data, nt,
+                                     stats.ctypes.data)
+        names = ["solver_succeeded", "solver_failed", "bernoulli_trial_calls", "bernoulli_trial_iterations",
+                 "bernoulli_trial_iterations_max", "walks", "newton_iterations", "connections"]
+        return value, count, walks, dict(zip(names, stats.tolist()))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and getattr(self, "_lib", None) is not None:
+            self._lib.oracle_scene_destroy(self._h)
+            self._h = None

@@ -1,0 +1,1263 @@
+/*
+ * sms_oracle.cpp -- CPU oracle for the Specular Manifold Sampling hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is a scalar, one-walk-per-thread
+ * restatement of the reference's scalar_rgb SMS code.  It is the checker the
+ * GPU library is compared against, and the CPU baseline bench.py times; the
+ * library itself never links, loads or calls it.
+ *
+ * Parity status: the reference (Mitsuba 2 + SMS) cannot be built in this
+ * environment (its enoki/tbb/pybind11 submodules are empty), so no output of the
+ * reference itself pins this file.  It is pinned against (a) the known-answer
+ * values of the reference's own dependency tests (Fresnel, warps) and (b)
+ * analytic solutions of the specular constraint computed independently in FP64
+ * (tests/golden/).  SMS-level outputs are otherwise "parity unpinned".
+ *
+ * All arithmetic is FP32 like scalar_rgb, except the sphere intersection, which
+ * the reference does in FP64 (src/shapes/sphere.cpp:275-297).  Build with
+ * -ffp-contract=off so x86-64 and aarch64 produce the same results.
+ *
+ * Every function cites the reference lines it restates (paths relative to the
+ * reference project root).
+ */
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+#include "../include/sms_gb300.h"
+
+namespace orc {
+
+static const float kInf = std::numeric_limits<float>::infinity();
+static const float kPi = 3.14159265358979323846f;
+static const float kInvPi = 0.31830988618379067154f;
+/* include/mitsuba/core/math.h:37-38 */
+static const float kRayEps = (std::numeric_limits<float>::epsilon() / 2.f) * 1500.f;
+static const float kShadowEps = kRayEps * 10.f;
+
+/* ------------------------------------------------------------ vector math */
+struct V3 {
+    float x = 0.f, y = 0.f, z = 0.f;
+    V3() {}
+    V3(float a) : x(a), y(a), z(a) {}
+    V3(float a, float b, float c) : x(a), y(b), z(c) {}
+    float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+static inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }
+static inline V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3 operator*(float s, V3 a) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+static inline V3 &operator+=(V3 &a, V3 b) { a = a + b; return a; }
+static inline V3 &operator-=(V3 &a, V3 b) { a = a - b; return a; }
+static inline V3 &operator*=(V3 &a, float s) { a = a * s; return a; }
+static inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+static inline float norm(V3 a) { return std::sqrt(dot(a, a)); }
+static inline V3 normalize(V3 a) { return a * (1.f / norm(a)); }
+static inline float hmax_abs(V3 a) {
+    return std::max(std::fabs(a.x), std::max(std::fabs(a.y), std::fabs(a.z)));
+}
+static inline float safe_sqrt(float v) { return std::sqrt(std::max(v, 0.f)); }
+static inline float safe_acos(float v) { return std::acos(std::min(1.f, std::max(-1.f, v))); }
+static inline float safe_asin(float v) { return std::asin(std::min(1.f, std::max(-1.f, v))); }
+
+struct V2 { float x = 0.f, y = 0.f; };
+
+/* 2x2 matrix, row-major m[r][c] */
+struct M2 {
+    float m[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+};
+static inline float det(const M2 &a) { return a.m[0][0] * a.m[1][1] - a.m[0][1] * a.m[1][0]; }
+static inline M2 inverse(const M2 &a) {
+    float id = 1.f / det(a);
+    M2 r;
+    r.m[0][0] = a.m[1][1] * id;  r.m[0][1] = -a.m[0][1] * id;
+    r.m[1][0] = -a.m[1][0] * id; r.m[1][1] = a.m[0][0] * id;
+    return r;
+}
+static inline M2 mul(const M2 &a, const M2 &b) {
+    M2 r;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+            r.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j];
+    return r;
+}
+static inline V2 mul(const M2 &a, V2 v) {
+    return {a.m[0][0] * v.x + a.m[0][1] * v.y, a.m[1][0] * v.x + a.m[1][1] * v.y};
+}
+
+/* Orthonormal basis of Duff et al. 2017, as used by the reference's
+ * coordinate_system (include/mitsuba/core/vector.h:116-135). */
+static void coordinate_system(V3 n, V3 &s, V3 &t) {
+    float sign = std::copysign(1.f, n.z);
+    float a = -1.f / (sign + n.z);
+    float b = n.x * n.y * a;
+    s = V3(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    t = V3(b, sign + n.y * n.y * a, -n.y);
+}
+
+/* ------------------------------------------------------------------ PCG32 */
+/* O'Neill's PCG32 (XSH-RR 64/32), the generator behind the reference's
+ * independent sampler (include/mitsuba/core/random.h:50-52).  Floats take the
+ * high 23 bits as the mantissa of a number in [1, 2). */
+struct PCG32 {
+    uint64_t state = 0, inc = 1;
+    void seed(uint64_t initstate, uint64_t initseq) {
+        state = 0u;
+        inc = (initseq << 1u) | 1u;
+        next_u32();
+        state += initstate;
+        next_u32();
+    }
+    uint32_t next_u32() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
+    }
+    float next_f32() {
+        uint32_t bits = (next_u32() >> 9) | 0x3f800000u;
+        float f;
+        std::memcpy(&f, &bits, 4);
+        return f - 1.f;
+    }
+    V2 next_2d() { V2 r; r.x = next_f32(); r.y = next_f32(); return r; }
+};
+
+/* ------------------------------------------------------------------ scene */
+struct Shape {
+    int kind = 0; /* 0 sphere, 1 mesh */
+    V3 center; float radius = 1.f; bool flip = false;
+    std::vector<V3> P, N;
+    std::vector<V2> UV;
+    std::vector<uint32_t> F;
+    std::vector<float> pmf, cdf; /* area distribution over faces */
+    float area_sum = 0.f, area_norm = 0.f;
+    uint32_t valid_lo = 0, valid_hi = 0;
+    sms_bsdf bsdf{};
+    uint32_t flags = 0;
+    int emitter = -1;
+};
+
+struct Emitter {
+    int kind = 0; /* 0 point, 1 area (sphere shape) */
+    V3 p; V3 radiance; int shape = -1; uint32_t flags = 0;
+};
+
+struct BNode { float lo[3], hi[3]; int left = -1, right = -1; uint32_t first = 0, count = 0; };
+
+struct Scene {
+    std::vector<Shape> shapes;
+    std::vector<Emitter> emitters;
+    /* triangle BVH over all mesh shapes: primitive = (shape, face) */
+    std::vector<uint32_t> tri_shape, tri_face;
+    std::vector<BNode> nodes;
+    std::vector<int> casters_ss, casters_ms, bouncers, emitters_ss, emitters_ms;
+    bool finalized = false;
+};
+
+/* Surface interaction: the subset of the reference's SurfaceInteraction3f the
+ * SMS path reads (include/mitsuba/render/interaction.h). */
+struct SI {
+    float t = kInf;
+    V3 p, n, shn, dp_du, dp_dv;
+    V2 uv;
+    int shape = -1;
+    uint32_t prim = 0;
+    bool valid() const { return t != kInf; }
+};
+
+struct Ray {
+    V3 o, d;
+    float mint = kRayEps, maxt = kInf;
+};
+
+/* ---- sphere: src/shapes/sphere.cpp:275-297 (FP64 quadratic), math.h:371 */
+static bool solve_quadratic(double a, double b, double c, double &x0, double &x1) {
+    bool linear = (a == 0.0);
+    bool active = !linear || (b > 0.0);
+    x0 = x1 = -c / b;
+    double discrim = b * b - 4.0 * a * c;
+    active = active && (linear || discrim >= 0.0);
+    if (active && !linear) {
+        double sq = std::sqrt(discrim);
+        double temp = -0.5 * (b + std::copysign(sq, b));
+        double x0p = temp / a, x1p = c / temp;
+        x0 = std::min(x0p, x1p);
+        x1 = std::max(x0p, x1p);
+    }
+    return active;
+}
+
+static bool sphere_intersect(const Shape &s, const Ray &r, float &t_out) {
+    double mint = r.mint, maxt = r.maxt;
+    double ox = (double)r.o.x - s.center.x, oy = (double)r.o.y - s.center.y,
+           oz = (double)r.o.z - s.center.z;
+    double dx = r.d.x, dy = r.d.y, dz = r.d.z;
+    double A = dx * dx + dy * dy + dz * dz;
+    double B = 2.0 * (ox * dx + oy * dy + oz * dz);
+    double C = ox * ox + oy * oy + oz * oz - (double)s.radius * (double)s.radius;
+    double n0, f0;
+    bool found = solve_quadratic(A, B, C, n0, f0);
+    bool out_bounds = !(n0 <= maxt && f0 >= mint);
+    bool in_bounds = n0 < mint && f0 > maxt;
+    if (!(found && !out_bounds && !in_bounds)) return false;
+    t_out = (float)(n0 < mint ? f0 : n0);
+    return true;
+}
+
+/* src/shapes/sphere.cpp:322-382 (uv, dp_du, dp_dv; no rotation in to_world) */
+static void sphere_fill(const Shape &s, const Ray &r, SI &si) {
+    V3 hit = r.o + r.d * si.t;
+    V3 n = normalize(hit - s.center);
+    si.p = n * s.radius + s.center;
+    V3 local = (si.p - s.center) * (1.f / s.radius);
+    float rd2 = local.x * local.x + local.y * local.y;
+    /* angle to +z, robust form: 2 asin(|v - (0,0,+-1)| / 2) */
+    float sz = std::copysign(1.f, local.z);
+    float tmp = 2.f * safe_asin(0.5f * norm(V3(local.x, local.y, local.z - sz)));
+    float theta = local.z >= 0.f ? tmp : kPi - tmp;
+    float phi = std::atan2(local.y, local.x);
+    if (phi < 0.f) phi += 2.f * kPi;
+    si.uv.x = phi * (0.5f / kPi);
+    si.uv.y = theta * (1.f / kPi);
+    V3 dpdu(-local.y, local.x, 0.f);
+    float rd = std::sqrt(rd2), inv_rd = 1.f / rd;
+    float cphi = local.x * inv_rd, sphi = local.y * inv_rd;
+    V3 dpdv(local.z * cphi, local.z * sphi, -rd);
+    if (rd == 0.f) dpdv = V3(1.f, 0.f, 0.f);
+    si.dp_du = dpdu * (s.radius * 2.f * kPi);
+    si.dp_dv = dpdv * (s.radius * kPi);
+    if (s.flip) n = -n;
+    si.n = n;
+    si.shn = n;
+}
+
+/* ---- triangles: include/mitsuba/render/mesh.h:203-228 (Moller-Trumbore) */
+static bool tri_intersect(const Shape &m, uint32_t f, const Ray &r, float &u, float &v, float &t) {
+    V3 p0 = m.P[m.F[3 * f]], p1 = m.P[m.F[3 * f + 1]], p2 = m.P[m.F[3 * f + 2]];
+    V3 e1 = p1 - p0, e2 = p2 - p0;
+    V3 pvec = cross(r.d, e2);
+    float inv_det = 1.f / dot(e1, pvec);
+    V3 tvec = r.o - p0;
+    u = dot(tvec, pvec) * inv_det;
+    bool active = u >= 0.f && u <= 1.f;
+    V3 qvec = cross(tvec, e1);
+    v = dot(r.d, qvec) * inv_det;
+    active = active && v >= 0.f && u + v <= 1.f;
+    t = dot(e2, qvec) * inv_det;
+    active = active && t >= r.mint && t <= r.maxt;
+    return active;
+}
+
+/* src/librender/mesh.cpp:618-687 */
+static void mesh_fill(const Shape &m, float b1, float b2, SI &si) {
+    uint32_t f = si.prim;
+    uint32_t i0 = m.F[3 * f], i1 = m.F[3 * f + 1], i2 = m.F[3 * f + 2];
+    float b0 = 1.f - b1 - b2;
+    V3 p0 = m.P[i0], p1 = m.P[i1], p2 = m.P[i2];
+    V3 dp0 = p1 - p0, dp1 = p2 - p0;
+    si.p = p0 * b0 + p1 * b1 + p2 * b2;
+    V3 n = normalize(cross(dp0, dp1));
+    si.n = n;
+    V3 dpdu, dpdv;
+    coordinate_system(n, dpdu, dpdv);
+    V2 uv0, uv1, uv2;
+    if (!m.UV.empty()) { uv0 = m.UV[i0]; uv1 = m.UV[i1]; uv2 = m.UV[i2]; }
+    else { uv0 = {0.f, 0.f}; uv1 = {1.f, 0.f}; uv2 = {0.f, 1.f}; }
+    /* use_default_uv_parameterization defaults to true (mesh.cpp:42) */
+    V2 uv;
+    uv.x = uv0.x * b0 + uv1.x * b1 + uv2.x * b2;
+    uv.y = uv0.y * b0 + uv1.y * b1 + uv2.y * b2;
+    V2 duv0{uv1.x - uv0.x, uv1.y - uv0.y}, duv1{uv2.x - uv0.x, uv2.y - uv0.y};
+    float dt = duv0.x * duv1.y - duv0.y * duv1.x;
+    if (dt != 0.f) {
+        float inv = 1.f / dt;
+        dpdu = (dp0 * duv1.y - dp1 * duv0.y) * inv;
+        dpdv = (dp1 * duv0.x - dp0 * duv1.x) * inv;
+    }
+    si.uv = uv;
+    if (!m.N.empty()) n = normalize(m.N[i0] * b0 + m.N[i1] * b1 + m.N[i2] * b2);
+    si.shn = n;
+    si.dp_du = dpdu;
+    si.dp_dv = dpdv;
+}
+
+/* src/librender/mesh.cpp:693-765 (needs vertex normals; none -> flat, as the
+ * reference's rectangle, src/shapes/rectangle.cpp:210-214) */
+static void mesh_normal_derivative(const Shape &m, const SI &si, V3 &dndu, V3 &dndv) {
+    if (m.N.empty()) { dndu = V3(0.f); dndv = V3(0.f); return; }
+    uint32_t f = si.prim;
+    uint32_t i0 = m.F[3 * f], i1 = m.F[3 * f + 1], i2 = m.F[3 * f + 2];
+    V3 p0 = m.P[i0], p1 = m.P[i1], p2 = m.P[i2];
+    V3 n0 = m.N[i0], n1 = m.N[i1], n2 = m.N[i2];
+    V3 rel = si.p - p0, du = p1 - p0, dv = p2 - p0;
+    float b1 = dot(du, rel), b2 = dot(dv, rel), a11 = dot(du, du), a12 = dot(du, dv),
+          a22 = dot(dv, dv);
+    float inv_det = 1.f / (a11 * a22 - a12 * a12);
+    float u = (a22 * b1 - a12 * b2) * inv_det, v = (a11 * b2 - a12 * b1) * inv_det,
+          w = 1.f - u - v;
+    V3 N = n1 * u + n2 * v + n0 * w;
+    float il = 1.f / std::sqrt(dot(N, N));
+    N *= il;
+    dndu = (n1 - n0) * il;
+    dndv = (n2 - n0) * il;
+    dndu = dndu - N * dot(N, dndu);
+    dndv = dndv - N * dot(N, dndv);
+    V2 uv0, uv1, uv2;
+    if (!m.UV.empty()) { uv0 = m.UV[i0]; uv1 = m.UV[i1]; uv2 = m.UV[i2]; }
+    else { uv0 = {0.f, 0.f}; uv1 = {1.f, 0.f}; uv2 = {0.f, 1.f}; }
+    V2 duv1{uv1.x - uv0.x, uv1.y - uv0.y}, duv2{uv2.x - uv0.x, uv2.y - uv0.y};
+    float id = 1.f / (duv1.x * duv2.y - duv1.y * duv2.x);
+    V3 a = (dndu * duv2.y - dndv * duv1.y) * id;
+    V3 b = (dndv * duv1.x - dndu * duv2.x) * id;
+    dndu = a;
+    dndv = b;
+}
+
+/* ---- oracle BVH: median split, exact closest hit.  Any exact structure
+ * gives the reference kd-tree's closest-hit result. */
+static void bvh_bounds(const Scene &sc, uint32_t prim, float lo[3], float hi[3], float c[3]) {
+    const Shape &m = sc.shapes[sc.tri_shape[prim]];
+    uint32_t f = sc.tri_face[prim];
+    for (int k = 0; k < 3; ++k) { lo[k] = kInf; hi[k] = -kInf; }
+    for (int j = 0; j < 3; ++j) {
+        V3 p = m.P[m.F[3 * f + j]];
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); }
+    }
+    for (int k = 0; k < 3; ++k) c[k] = 0.5f * (lo[k] + hi[k]);
+}
+
+static int bvh_build_rec(Scene &sc, std::vector<uint32_t> &idx, std::vector<float> &cen,
+                         uint32_t first, uint32_t count, std::vector<BNode> &out) {
+    BNode node;
+    for (int k = 0; k < 3; ++k) { node.lo[k] = kInf; node.hi[k] = -kInf; }
+    float clo[3] = {kInf, kInf, kInf}, chi[3] = {-kInf, -kInf, -kInf};
+    for (uint32_t i = first; i < first + count; ++i) {
+        float lo[3], hi[3], c[3];
+        bvh_bounds(sc, idx[i], lo, hi, c);
+        for (int k = 0; k < 3; ++k) {
+            node.lo[k] = std::min(node.lo[k], lo[k]); node.hi[k] = std::max(node.hi[k], hi[k]);
+            clo[k] = std::min(clo[k], c[k]); chi[k] = std::max(chi[k], c[k]);
+        }
+    }
+    /* pad so that float rounding in the slab test never drops a triangle that
+       the exact triangle test would accept */
+    for (int k = 0; k < 3; ++k) {
+        float pad = 1e-6f * std::max(1.f, std::max(std::fabs(node.lo[k]), std::fabs(node.hi[k])));
+        node.lo[k] -= pad; node.hi[k] += pad;
+    }
+    int id = (int)out.size();
+    out.push_back(node);
+    if (count <= 4) { out[id].first = first; out[id].count = count; return id; }
+    int axis = 0;
+    for (int k = 1; k < 3; ++k) if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+    uint32_t mid = first + count / 2;
+    std::nth_element(idx.begin() + first, idx.begin() + mid, idx.begin() + first + count,
+                     [&](uint32_t a, uint32_t b) {
+                         if (cen[3 * a + axis] != cen[3 * b + axis])
+                             return cen[3 * a + axis] < cen[3 * b + axis];
+                         return a < b;
+                     });
+    int l = bvh_build_rec(sc, idx, cen, first, mid - first, out);
+    int r = bvh_build_rec(sc, idx, cen, mid, first + count - mid, out);
+    out[id].left = l; out[id].right = r; out[id].count = 0;
+    return id;
+}
+
+static bool box_hit(const BNode &n, const Ray &r, float tmax) {
+    float t0 = r.mint, t1 = tmax;
+    for (int k = 0; k < 3; ++k) {
+        float inv = 1.f / r.d[k];
+        float a = (n.lo[k] - r.o[k]) * inv, b = (n.hi[k] - r.o[k]) * inv;
+        if (a > b) std::swap(a, b);
+        /* NaN (0 * inf) leaves the interval unchanged */
+        if (a > t0) t0 = a;
+        if (b < t1) t1 = b;
+        if (t0 > t1) return false;
+    }
+    return true;
+}
+
+/* Scene::ray_intersect (src/librender/scene.cpp:123-131, kdtree.h:2334-2366) */
+static bool ray_is_nan(const Ray &r) {
+    return std::isnan(r.o.x) || std::isnan(r.o.y) || std::isnan(r.o.z) || std::isnan(r.d.x) ||
+           std::isnan(r.d.y) || std::isnan(r.d.z);
+}
+
+static SI ray_intersect(const Scene &sc, const Ray &ray) {
+    SI si;
+    /* a NaN ray hits nothing (all intersection comparisons are false) */
+    if (ray_is_nan(ray)) return si;
+    float best = ray.maxt;
+    int best_shape = -1; uint32_t best_prim = 0; float bu = 0.f, bv = 0.f;
+    bool hit = false;
+    for (size_t s = 0; s < sc.shapes.size(); ++s) {
+        if (sc.shapes[s].kind != 0) continue;
+        float t;
+        Ray r = ray; r.maxt = best;
+        if (sphere_intersect(sc.shapes[s], r, t) && (!hit || t < best)) {
+            best = t; best_shape = (int)s; hit = true;
+        }
+    }
+    if (!sc.nodes.empty()) {
+        int stack[128]; int sp = 0; stack[sp++] = 0;
+        while (sp) {
+            const BNode &n = sc.nodes[stack[--sp]];
+            if (!box_hit(n, ray, best)) continue;
+            if (n.count) {
+                for (uint32_t i = n.first; i < n.first + n.count; ++i) {
+                    const Shape &m = sc.shapes[sc.tri_shape[i]];
+                    float u, v, t;
+                    Ray r = ray; r.maxt = best;
+                    if (tri_intersect(m, sc.tri_face[i], r, u, v, t) && (!hit || t < best)) {
+                        best = t; best_shape = (int)sc.tri_shape[i]; best_prim = sc.tri_face[i];
+                        bu = u; bv = v; hit = true;
+                    }
+                }
+            } else {
+                stack[sp++] = n.left; stack[sp++] = n.right;
+            }
+        }
+    }
+    if (!hit) return si;
+    si.t = best; si.shape = best_shape; si.prim = best_prim;
+    const Shape &s = sc.shapes[best_shape];
+    if (s.kind == 0) sphere_fill(s, ray, si);
+    else mesh_fill(s, bu, bv, si);
+    return si;
+}
+
+/* Scene::ray_test (src/librender/scene.cpp:144-152) */
+static bool ray_test(const Scene &sc, const Ray &ray) {
+    if (ray_is_nan(ray)) return false;
+    for (const Shape &s : sc.shapes) {
+        float t;
+        if (s.kind == 0 && sphere_intersect(s, ray, t)) return true;
+    }
+    if (sc.nodes.empty()) return false;
+    int stack[128]; int sp = 0; stack[sp++] = 0;
+    while (sp) {
+        const BNode &n = sc.nodes[stack[--sp]];
+        if (!box_hit(n, ray, ray.maxt)) continue;
+        if (n.count) {
+            for (uint32_t i = n.first; i < n.first + n.count; ++i) {
+                float u, v, t;
+                if (tri_intersect(sc.shapes[sc.tri_shape[i]], sc.tri_face[i], ray, u, v, t)) return true;
+            }
+        } else { stack[sp++] = n.left; stack[sp++] = n.right; }
+    }
+    return false;
+}
+
+/* ---- sampling: warp.h:153-156,262-267; mesh.cpp:541-586; distr_1d.h:144-201 */
+static V3 square_to_uniform_sphere(V2 s) {
+    float z = 1.f - 2.f * s.y;
+    float r = safe_sqrt(1.f - z * z);
+    float ang = 2.f * kPi * s.x;
+    return V3(r * std::cos(ang), r * std::sin(ang), z);
+}
+
+static V3 sample_position(const Shape &s, V2 sample, V3 *n_out = nullptr) {
+    if (s.kind == 0) {
+        V3 local = square_to_uniform_sphere(sample);
+        if (n_out) *n_out = s.flip ? -local : local;
+        return local * s.radius + s.center;
+    }
+    /* DiscreteDistribution::sample_reuse on sample.y */
+    float value = sample.y * s.area_sum;
+    uint32_t lo = s.valid_lo, hi = s.valid_hi;
+    /* first index in [lo, hi] whose cdf >= value (hi if none) */
+    while (lo < hi) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        if (s.cdf[mid] < value) lo = mid + 1; else hi = mid;
+    }
+    uint32_t f = lo;
+    float pmf = s.pmf[f] * s.area_norm;
+    float cdf_prev = f > 0 ? s.cdf[f - 1] * s.area_norm : 0.f;
+    float y = (sample.y - cdf_prev) / pmf;
+    float tq = safe_sqrt(1.f - sample.x);
+    float bx = 1.f - tq, by = tq * y;
+    V3 p0 = s.P[s.F[3 * f]], p1 = s.P[s.F[3 * f + 1]], p2 = s.P[s.F[3 * f + 2]];
+    V3 e0 = p1 - p0, e1 = p2 - p0;
+    if (n_out) {
+        if (!s.N.empty())
+            *n_out = normalize(s.N[s.F[3 * f]] * (1.f - bx - by) + s.N[s.F[3 * f + 1]] * bx +
+                               s.N[s.F[3 * f + 2]] * by);
+        else
+            *n_out = normalize(cross(e0, e1));
+    }
+    return p0 + e0 * bx + e1 * by;
+}
+
+/* ------------------------------------------------------- ManifoldVertex */
+/* include/mitsuba/render/manifold.h:50-141 */
+struct MVertex {
+    V3 p, dp_du, dp_dv, n, gn, dn_du, dn_dv, s, t, ds_du, ds_dv, dt_du, dt_dv;
+    float eta = 1.f;
+    V2 uv;
+    int shape = -1;
+    bool fixed_direction = false;
+};
+
+/* manifold.h:94-96: eta = real(ior) when imag(ior) == 0, else 1.  Conductors
+ * with k = 0 therefore behave like dielectrics; non-specular BSDFs have
+ * ior = (0, 1) (bsdf.cpp:58-60) -> 1. */
+static float bsdf_eta(const sms_bsdf &b) {
+    if (b.type == SMS_BSDF_DIELECTRIC) return b.eta;
+    if (b.type == SMS_BSDF_CONDUCTOR && b.k == 0.f) return b.eta;
+    return 1.f;
+}
+
+/* frame.h:197-240 (compute_shading_frame{,_derivative}); bsdf.cpp:17-31 */
+static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v) {
+    const Shape &sh = sc.shapes[si.shape];
+    v.p = si.p; v.dp_du = si.dp_du; v.dp_dv = si.dp_dv; v.gn = si.n; v.uv = si.uv;
+    v.shape = si.shape; v.fixed_direction = false;
+    v.eta = bsdf_eta(sh.bsdf);
+    V3 n = si.shn;
+    V3 s = normalize(si.dp_du - n * dot(n, si.dp_du));
+    v.n = n; v.s = s; v.t = cross(n, s);
+    V3 dndu, dndv;
+    if (sh.kind == 0) {
+        float inv_r = (sh.flip ? -1.f : 1.f) / sh.radius;   /* sphere.cpp:376-382 */
+        dndu = si.dp_du * inv_r; dndv = si.dp_dv * inv_r;
+    } else {
+        mesh_normal_derivative(sh, si, dndu, dndv);
+    }
+    V3 s0 = si.dp_du - n * dot(n, si.dp_du);
+    float inv_len_s = 1.f / norm(s0);
+    s0 *= inv_len_s;
+    V3 dsdu = (-dndu * dot(n, si.dp_du) - n * dot(dndu, si.dp_du)) * inv_len_s;
+    V3 dsdv = (-dndv * dot(n, si.dp_du) - n * dot(dndv, si.dp_du)) * inv_len_s;
+    dsdu -= s0 * dot(dsdu, s0);
+    dsdv -= s0 * dot(dsdv, s0);
+    v.ds_du = dsdu; v.ds_dv = dsdv;
+    v.dt_du = cross(dndu, s0) + cross(n, dsdu);
+    v.dt_dv = cross(dndv, s0) + cross(n, dsdv);
+    v.dn_du = dndu; v.dn_dv = dndv;
+    if (dot(v.n, v.gn) < 0.f) v.gn = -v.gn;
+}
+
+/* manifold.h:115-126 */
+static void make_orthonormal(MVertex &v) {
+    float inv = 1.f / norm(v.dp_du);
+    v.dp_du *= inv; v.dn_du *= inv;
+    float dp = dot(v.dp_du, v.dp_dv);
+    V3 a = v.dp_dv - v.dp_du * dp, b = v.dn_dv - v.dn_du * dp;
+    inv = 1.f / norm(a);
+    v.dp_dv = a * inv; v.dn_dv = b * inv;
+}
+
+/* ------------------------------------------------ emitter interaction */
+struct EI {
+    V3 p, n, d, weight;
+    float pdf = 0.f;
+    int emitter = -1;
+    bool is_point = false, is_area = false;
+};
+
+/* ---------------------------------------------- specular transforms */
+/* manifold.h:348-418 */
+static bool reflect(V3 w, V3 n, V3 &out) { out = n * (2.f * dot(w, n)) - w; return true; }
+static void d_reflect(V3 w, V3 dwdu, V3 dwdv, V3 n, V3 dndu, V3 dndv, V3 &ou, V3 &ov) {
+    float dwn = dot(w, n), dun = dot(dwdu, n), dvn = dot(dwdv, n), wdu = dot(w, dndu),
+          wdv = dot(w, dndv);
+    ou = ((n * (dun + wdu)) + dndu * dwn) * 2.f - dwdu;
+    ov = ((n * (dvn + wdv)) + dndv * dwn) * 2.f - dwdv;
+}
+static bool refract(V3 w, V3 n, float eta_, V3 &out) {
+    float eta = 1.f / eta_;
+    if (dot(w, n) < 0.f) { eta = 1.f / eta; n = -n; }
+    float dwn = dot(w, n);
+    float root = 1.f - eta * eta * (1.f - dwn * dwn);
+    if (root < 0.f) { out = V3(0.f); return false; }
+    out = -(w - n * dwn) * eta - n * std::sqrt(root);
+    return true;
+}
+static void d_refract(V3 w, V3 dwdu, V3 dwdv, V3 n, V3 dndu, V3 dndv, float eta_, V3 &ou, V3 &ov) {
+    float eta = 1.f / eta_;
+    if (dot(w, n) < 0.f) { eta = 1.f / eta; n = -n; dndu = -dndu; dndv = -dndv; }
+    float dwn = dot(w, n), dun = dot(dwdu, n), dvn = dot(dwdv, n), wdu = dot(w, dndu),
+          wdv = dot(w, dndv);
+    float root = std::sqrt(1.f - eta * eta * (1.f - dwn * dwn));
+    V3 a_u = -(dwdu - (n * (dun + wdu) + dndu * dwn)) * eta;
+    V3 b_u = -(dndu * root + n * (1.f / (2.f * root)) * (-eta * eta * (-2.f * dwn * (dun + wdu))));
+    V3 a_v = -(dwdv - (n * (dvn + wdv) + dndv * dwn)) * eta;
+    V3 b_v = -(dndv * root + n * (1.f / (2.f * root)) * (-eta * eta * (-2.f * dwn * (dvn + wdv))));
+    ou = a_u + b_u;
+    ov = a_v + b_v;
+}
+/* manifold.h:420-443 */
+static void sphcoords(V3 w, float &theta, float &phi) {
+    theta = safe_acos(w.z);
+    phi = std::atan2(w.y, w.x);
+    if (phi < 0.f) phi += 2.f * kPi;
+}
+static void d_sphcoords(V3 w, V3 dwdu, V3 dwdv, float &dtu, float &dpu, float &dtv, float &dpv) {
+    float d_acos = -1.f / safe_sqrt(1.f - w.z * w.z);
+    dtu = d_acos * dwdu.z;
+    dtv = d_acos * dwdv.z;
+    float yx = w.y / w.x;
+    float d_atan = 1.f / (1.f + yx * yx);
+    float inv = 1.f / (w.x * w.x);
+    dpu = d_atan * (w.x * dwdu.y - w.y * dwdu.x) * inv;
+    dpv = d_atan * (w.x * dwdv.y - w.y * dwdv.x) * inv;
+    if (w.x == 0.f) { dpu = 0.f; dpv = 0.f; }
+}
+
+/* ------------------------------------------------------ constraints */
+/* manifold_ss.cpp:494-636 */
+static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX) {
+    V3 wi = x - v1.p;
+    float ili = norm(wi);
+    if (ili < 1e-3f) return false;
+    ili = 1.f / ili; wi *= ili;
+    V3 dwi_du = (v1.dp_du - wi * dot(wi, v1.dp_du)) * -ili;
+    V3 dwi_dv = (v1.dp_dv - wi * dot(wi, v1.dp_dv)) * -ili;
+    V3 wo = ei.p - v1.p;
+    float ilo = norm(wo);
+    if (ilo < 1e-3f) return false;
+    ilo = 1.f / ilo; wo *= ilo;
+    V3 dwo_du = (v1.dp_du - wo * dot(wo, v1.dp_du)) * -ilo;
+    V3 dwo_dv = (v1.dp_dv - wo * dot(wo, v1.dp_dv)) * -ilo;
+    /* n_offset = (0,0,1): n, dn_du, dn_dv are the vertex's own */
+    V3 n = v1.n, dndu = v1.dn_du, dndv = v1.dn_dv;
+    bool success = false;
+    M2 J;
+    C = V2{0.f, 0.f};
+    auto transform = [&](V3 w, V3 &out) {
+        return v1.eta == 1.f ? reflect(w, n, out) : refract(w, n, v1.eta, out);
+    };
+    auto d_transform = [&](V3 w, V3 du, V3 dv, V3 &ou, V3 &ov) {
+        if (v1.eta == 1.f) d_reflect(w, du, dv, n, dndu, dndv, ou, ov);
+        else d_refract(w, du, dv, n, dndu, dndv, v1.eta, ou, ov);
+    };
+    V3 wio;
+    if (transform(wi, wio)) {
+        V3 dwio_du, dwio_dv;
+        d_transform(wi, dwi_du, dwi_dv, dwio_du, dwio_dv);
+        float to, po, tio, pio;
+        sphcoords(wo, to, po); sphcoords(wio, tio, pio);
+        float dt = to - tio, dp = po - pio;
+        if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
+        C = V2{dt, dp};
+        float a0, a1, a2, a3, b0, b1, b2, b3;
+        d_sphcoords(wo, dwo_du, dwo_dv, a0, a1, a2, a3);
+        d_sphcoords(wio, dwio_du, dwio_dv, b0, b1, b2, b3);
+        J.m[0][0] = a0 - b0; J.m[1][0] = a1 - b1; J.m[0][1] = a2 - b2; J.m[1][1] = a3 - b3;
+        success = true;
+    }
+    V3 woi;
+    if (transform(wo, woi) && !success) {
+        V3 dwoi_du, dwoi_dv;
+        d_transform(wo, dwo_du, dwo_dv, dwoi_du, dwoi_dv);
+        float ti, pi, toi, poi;
+        sphcoords(wi, ti, pi); sphcoords(woi, toi, poi);
+        float dt = ti - toi, dp = pi - poi;
+        if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
+        C = V2{dt, dp};
+        float a0, a1, a2, a3, b0, b1, b2, b3;
+        d_sphcoords(wi, dwi_du, dwi_dv, a0, a1, a2, a3);
+        d_sphcoords(woi, dwoi_du, dwoi_dv, b0, b1, b2, b3);
+        J.m[0][0] = a0 - b0; J.m[1][0] = a1 - b1; J.m[0][1] = a2 - b2; J.m[1][1] = a3 - b3;
+        success = true;
+    }
+    float d = det(J);
+    if (std::fabs(d) < 1e-6f) return false;
+    dX = mul(inverse(J), C);
+    return success;
+}
+
+/* manifold_ss.cpp:407-492 */
+static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX) {
+    V3 wo = ei.p - v1.p;
+    float ilo = norm(wo);
+    if (ilo < 1e-3f) return false;
+    ilo = 1.f / ilo; wo *= ilo;
+    V3 wi = x - v1.p;
+    float ili = norm(wi);
+    if (ili < 1e-3f) return false;
+    ili = 1.f / ili; wi *= ili;
+    float eta = v1.eta;
+    if (dot(wi, v1.gn) < 0.f) eta = 1.f / eta;
+    V3 h = wi + wo * eta;
+    if (eta != 1.f) h *= -1.f;
+    float ilh = 1.f / norm(h);
+    h *= ilh;
+    ilo *= eta * ilh;
+    ili *= ilh;
+    V3 dh_du = -v1.dp_du * (ili + ilo) + wi * (dot(wi, v1.dp_du) * ili) + wo * (dot(wo, v1.dp_du) * ilo);
+    V3 dh_dv = -v1.dp_dv * (ili + ilo) + wi * (dot(wi, v1.dp_dv) * ili) + wo * (dot(wo, v1.dp_dv) * ilo);
+    dh_du -= h * dot(dh_du, h);
+    dh_dv -= h * dot(dh_dv, h);
+    if (eta != 1.f) { dh_du *= -1.f; dh_dv *= -1.f; }
+    M2 J;
+    J.m[0][0] = dot(v1.ds_du, h) + dot(v1.s, dh_du);
+    J.m[1][0] = dot(v1.dt_du, h) + dot(v1.t, dh_du);
+    J.m[0][1] = dot(v1.ds_dv, h) + dot(v1.s, dh_dv);
+    J.m[1][1] = dot(v1.dt_dv, h) + dot(v1.t, dh_dv);
+    float d = det(J);
+    if (std::fabs(d) < 1e-6f) return false;
+    C = V2{dot(v1.s, h), dot(v1.t, h)};
+    dX = mul(inverse(J), C);
+    return true;
+}
+
+/* ------------------------------------------------------ Newton solver */
+struct Cfg {
+    sms_config c;
+};
+
+/* manifold_ss.cpp:329-405.  Returns (ok, si_current, iterations). */
+static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MVertex &init,
+                          const EI &ei, SI &si_out, int &iters_out) {
+    MVertex vtx = init;
+    bool success = false;
+    int it = 0;
+    float beta = 1.f;
+    SI si_current;
+    while (it < cfg.max_iterations) {
+        V2 C, dX;
+        bool ok = cfg.halfvector_constraints ? step_halfvector(x, vtx, ei, C, dX)
+                                             : step_anglediff(x, vtx, ei, C, dX);
+        if (!ok) break;
+        if (std::sqrt(C.x * C.x + C.y * C.y) < cfg.solver_threshold) { success = true; break; }
+        V3 p_prop = vtx.p - (vtx.dp_du * dX.x + vtx.dp_dv * dX.y) * (cfg.step_scale * beta);
+        Ray r; r.o = x; r.d = normalize(p_prop - x);
+        si_current = ray_intersect(sc, r);
+        if (!si_current.valid() || vtx.shape != si_current.shape) {
+            beta = 0.5f * beta;
+            it += 1;
+            continue;
+        }
+        beta = std::min(1.f, 2.f * beta);
+        vertex_from_si(sc, si_current, vtx);
+        it++;
+    }
+    iters_out = it;
+    si_out = si_current;
+    if (!success) return false;
+    V3 wx = normalize(x - vtx.p);
+    V3 wy = normalize(ei.p - vtx.p);
+    float cx = dot(vtx.gn, wx), cy = dot(vtx.gn, wy);
+    bool refraction = cx * cy < 0.f;
+    bool reflection = !refraction;
+    if ((vtx.eta == 1.f && !reflection) || (vtx.eta != 1.f && !refraction)) return false;
+    return true;
+}
+
+/* ----------------------------------------------------------- query */
+struct Query {
+    V3 p, n, dp_du, dp_dv, albedo;
+    float cos_i = 1.f;
+};
+
+static Query load_query(const float *q, uint32_t n, uint32_t i) {
+    Query r;
+    auto f = [&](int k) { return q[(size_t)k * n + i]; };
+    r.p = V3(f(0), f(1), f(2)); r.n = V3(f(3), f(4), f(5));
+    r.dp_du = V3(f(6), f(7), f(8)); r.dp_dv = V3(f(9), f(10), f(11));
+    r.albedo = V3(f(12), f(13), f(14)); r.cos_i = f(15);
+    return r;
+}
+
+/* manifold_ss.cpp:203-279 (twostage / mnee_init / offset normals: unsupported) */
+static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, const Query &q,
+                        const EI &ei, V2 sample, V3 p_start, SI &si_final, SI &si_init,
+                        int &iters) {
+    const Shape &shape = sc.shapes[caster];
+    V3 p = sample_position(shape, sample);
+    if (p_start.x != 0.f || p_start.y != 0.f || p_start.z != 0.f) p = p_start;
+    V3 d_tmp = normalize(p - q.p);
+    Ray r; r.o = q.p; r.d = d_tmp;
+    si_init = ray_intersect(sc, r);
+    iters = 0;
+    if (!si_init.valid() || caster != si_init.shape) return false;
+    MVertex v0;
+    vertex_from_si(sc, si_init, v0);
+    bool ok = newton_solver(sc, cfg, q.p, v0, ei, si_final, iters);
+    return ok && si_final.valid();
+}
+
+/* manifold.h:204-260 */
+static EI sample_emitter_interaction(const Scene &sc, const Query &q, PCG32 &rng) {
+    EI ei;
+    const std::vector<int> &em = sc.emitters_ss;
+    if (em.empty()) return ei;
+    float es = rng.next_f32();
+    float emitter_pdf = 1.f / (float)em.size();
+    uint32_t idx = std::min((uint32_t)(es * (float)em.size()), (uint32_t)em.size() - 1);
+    const Emitter &e = sc.emitters[em[idx]];
+    ei.emitter = em[idx];
+    V3 spec(0.f);
+    if (e.kind == 1) {
+        ei.is_area = true;
+        const Shape &s = sc.shapes[e.shape];
+        V3 n;
+        V3 p = sample_position(s, rng.next_2d(), &n);
+        float area = 4.f * kPi * s.radius * s.radius;
+        float pdf = 1.f / area;
+        /* area.cpp:71-79 with wi = (0,0,1): cos_theta > 0 -> radiance */
+        spec = V3(e.radiance.x / pdf, e.radiance.y / pdf, e.radiance.z / pdf);
+        ei.p = p; ei.n = n; ei.d = normalize(p - q.p); ei.pdf = pdf;
+    } else {
+        ei.is_point = true;
+        (void)rng.next_2d(); /* point.cpp:74-100 consumes a 2D sample */
+        V3 d = e.p - q.p;
+        float dist = norm(d);
+        float inv = 1.f / dist;
+        d *= inv;
+        V3 s = e.radiance * (inv * inv);
+        ei.p = e.p; ei.d = d; ei.n = d; ei.pdf = 1.f;
+        spec = (s * dist) * dist;
+    }
+    ei.pdf *= emitter_pdf;
+    ei.weight = spec * (1.f / emitter_pdf);
+    return ei;
+}
+
+/* fresnel.h:34-80 */
+static float fresnel(float cos_i, float eta, float *cos_t_out = nullptr) {
+    bool outside = cos_i >= 0.f;
+    float rcp_eta = 1.f / eta;
+    float eta_it = outside ? eta : rcp_eta, eta_ti = outside ? rcp_eta : eta;
+    float ct2 = 1.f - (1.f - cos_i * cos_i) * (eta_ti * eta_ti);
+    float ci = std::fabs(cos_i), ct = safe_sqrt(ct2);
+    bool index_matched = eta == 1.f;
+    bool special = index_matched || ci == 0.f;
+    float r_sc = index_matched ? 0.f : 1.f;
+    float a_s = (ci - eta_it * ct) / (ci + eta_it * ct);
+    float a_p = (ct - eta_it * ci) / (ct + eta_it * ci);
+    float r = 0.5f * (a_s * a_s + a_p * a_p);
+    if (special) r = r_sc;
+    if (cos_t_out) *cos_t_out = cos_i >= 0.f ? -ct : ct;
+    return r;
+}
+/* fresnel.h:92-120 */
+static float fresnel_conductor(float cos_i, float er, float ei_) {
+    float c2 = cos_i * cos_i, s2 = 1.f - c2, s4 = s2 * s2;
+    float t1 = er * er - ei_ * ei_ - s2;
+    float a2pb2 = safe_sqrt(t1 * t1 + 4.f * ei_ * ei_ * er * er);
+    float a = safe_sqrt(0.5f * (a2pb2 + t1));
+    float term1 = a2pb2 + c2, term2 = 2.f * cos_i * a;
+    float rs = (term1 - term2) / (term1 + term2);
+    float term3 = a2pb2 * c2 + s4, term4 = term2 * s2;
+    float rp = rs * (term3 - term4) / (term3 + term4);
+    return 0.5f * (rs + rp);
+}
+
+/* manifold_ss.cpp:638-693 (smooth BSDFs) */
+static float specular_reflectance(const Scene &sc, const SI &si, V3 wo) {
+    if (!si.valid()) return 0.f;
+    const sms_bsdf &b = sc.shapes[si.shape].bsdf;
+    V3 n = si.shn;
+    float cos_theta = dot(n, wo);
+    if (b.type == SMS_BSDF_CONDUCTOR && b.k != 0.f)
+        return fresnel_conductor(std::fabs(cos_theta), b.eta, b.k);
+    if (b.type == SMS_BSDF_DIELECTRIC || b.type == SMS_BSDF_CONDUCTOR) {
+        /* real ior: the "reflection" mask is false -> transmission branch */
+        float eta = b.eta;
+        if (cos_theta < 0.f) eta = 1.f / eta;
+        float F = fresnel(cos_theta, eta);
+        return (1.f - F) * eta * eta;
+    }
+    /* diffuse: ior (0,1) has a nonzero imaginary part -> conductor formula */
+    return fresnel_conductor(std::fabs(cos_theta), 0.f, 1.f);
+}
+
+/* manifold_ss.cpp:695-857 */
+static float geometric_term(const MVertex &v0, const MVertex &v1, const MVertex &v2) {
+    V3 wi = v0.p - v1.p;
+    float ili = norm(wi);
+    if (ili < 1e-3f) return 0.f;
+    ili = 1.f / ili; wi *= ili;
+    V3 wo = v2.p - v1.p;
+    float ilo = norm(wo);
+    if (ilo < 1e-3f) return 0.f;
+    ilo = 1.f / ilo; wo *= ilo;
+    float eta = v1.eta;
+    if (dot(wi, v1.gn) < 0.f) eta = 1.f / eta;
+    V3 h = wi + wo * eta;
+    if (eta != 1.f) h *= -1.f;
+    float ilh = 1.f / norm(h);
+    h *= ilh;
+    ilo *= eta * ilh;
+    ili *= ilh;
+    float dpdu_n = dot(v1.dp_du, v1.n), dpdv_n = dot(v1.dp_dv, v1.n);
+    V3 s = v1.dp_du - v1.n * dpdu_n, t = v1.dp_dv - v1.n * dpdv_n;
+    V3 dh_du = -v1.dp_du * (ili + ilo) + wi * (dot(wi, v1.dp_du) * ili) + wo * (dot(wo, v1.dp_du) * ilo);
+    V3 dh_dv = -v1.dp_dv * (ili + ilo) + wi * (dot(wi, v1.dp_dv) * ili) + wo * (dot(wo, v1.dp_dv) * ilo);
+    dh_du -= h * dot(dh_du, h);
+    dh_dv -= h * dot(dh_dv, h);
+    if (eta != 1.f) { dh_du *= -1.f; dh_dv *= -1.f; }
+    float hn = dot(h, v1.n), hdu = dot(h, v1.dn_du), hdv = dot(h, v1.dn_dv);
+    M2 d11;
+    d11.m[0][0] = dot(dh_du, s) - dot(v1.dp_du, v1.dn_du) * hn - dpdu_n * hdu;
+    d11.m[0][1] = dot(dh_dv, s) - dot(v1.dp_du, v1.dn_dv) * hn - dpdu_n * hdv;
+    d11.m[1][0] = dot(dh_du, t) - dot(v1.dp_dv, v1.dn_du) * hn - dpdv_n * hdu;
+    d11.m[1][1] = dot(dh_dv, t) - dot(v1.dp_dv, v1.dn_dv) * hn - dpdv_n * hdv;
+    dh_du = (v2.dp_du - wo * dot(wo, v2.dp_du)) * ilo;
+    dh_dv = (v2.dp_dv - wo * dot(wo, v2.dp_dv)) * ilo;
+    dh_du -= h * dot(dh_du, h);
+    dh_dv -= h * dot(dh_dv, h);
+    if (eta != 1.f) { dh_du *= -1.f; dh_dv *= -1.f; }
+    M2 d12;
+    d12.m[0][0] = dot(dh_du, s); d12.m[0][1] = dot(dh_dv, s);
+    d12.m[1][0] = dot(dh_du, t); d12.m[1][1] = dot(dh_dv, t);
+    float d = det(d11);
+    if (std::fabs(d) < 1e-6f) return 0.f;
+    float dx1_dx2 = std::fabs(det(mul(inverse(d11), d12)));
+    dx1_dx2 = std::min(dx1_dx2, 1.f);
+    V3 dd = v0.p - v1.p;
+    float inv_r2 = 1.f / dot(dd, dd);
+    dd *= std::sqrt(inv_r2);
+    float dw0_dx1 = std::fabs(dot(dd, v1.gn)) * inv_r2;
+    return dw0_dx1 * dx1_dx2;
+}
+
+/* manifold.h:264-302 */
+static bool emitter_vertex(const Scene &sc, const EI &ei, V3 p, MVertex &vy) {
+    if (ei.is_area) {
+        V3 d = normalize(ei.p - p);
+        Ray r; r.o = p + d * kShadowEps; r.d = d;
+        SI si_y = ray_intersect(sc, r);
+        if (!si_y.valid()) return false;
+        vertex_from_si(sc, si_y, vy);
+        make_orthonormal(vy);
+        return true;
+    }
+    vy = MVertex();
+    vy.p = ei.p;
+    V3 d = normalize(p - ei.p);
+    vy.n = vy.gn = d;
+    coordinate_system(d, vy.dp_du, vy.dp_dv);
+    return true;
+}
+
+/* manifold_ss.cpp:281-327 */
+static V3 evaluate_path_contribution(const Scene &sc, const Query &q, const EI &ei_in,
+                                     const SI &si_final) {
+    MVertex vtx;
+    vertex_from_si(sc, si_final, vtx);
+    make_orthonormal(vtx);
+    EI ei = ei_in;
+    if (ei.is_point) {
+        const Emitter &e = sc.emitters[ei.emitter];
+        V3 d = e.p - si_final.p;
+        float dist = norm(d);
+        float inv = 1.f / dist;
+        d *= inv;
+        V3 spec = e.radiance * (inv * inv);
+        ei.p = e.p; ei.d = d; ei.n = d;
+        float emitter_pdf = ei.pdf;
+        ei.pdf = 1.f;
+        ei.weight = (spec * dist) * dist;
+        ei.pdf *= emitter_pdf;
+        ei.weight = ei.weight * (1.f / emitter_pdf);
+    }
+    MVertex vy;
+    if (!emitter_vertex(sc, ei, vtx.p, vy)) return V3(0.f);
+    /* shading point vertex: flat receiver (dn = 0) */
+    MVertex vx;
+    vx.p = q.p; vx.dp_du = q.dp_du; vx.dp_dv = q.dp_dv; vx.gn = q.n; vx.n = q.n;
+    vx.dn_du = V3(0.f); vx.dn_dv = V3(0.f);
+    make_orthonormal(vx);
+    /* path_throughput = 1 * F * G * weight (manifold_ss.cpp:322-326) */
+    float f = specular_reflectance(sc, si_final, normalize(ei.p - si_final.p));
+    f *= geometric_term(vx, vtx, vy);
+    return V3(f * ei.weight.x, f * ei.weight.y, f * ei.weight.z);
+}
+
+/* src/bsdfs/diffuse.cpp eval: albedo / pi * cos_theta_o (both cosines > 0) */
+static V3 diffuse_eval(const Query &q, V3 dir) {
+    float co = dot(dir, q.n);
+    if (q.cos_i <= 0.f || co <= 0.f) return V3(0.f);
+    return (q.albedo * kInvPi) * co;
+}
+
+static bool visible(const Scene &sc, const EI &ei, V3 p) {
+    V3 d = p - ei.p;
+    float dist = norm(d);
+    d *= 1.f / dist;
+    Ray r; r.o = ei.p; r.d = d;
+    r.mint = kRayEps * (1.f + hmax_abs(ei.p));
+    r.maxt = dist * (1.f - kRayEps);
+    return !ray_test(sc, r);
+}
+
+struct Stats {
+    std::atomic<uint64_t> succeeded{0}, failed{0}, calls{0}, iters{0}, iters_max{0}, walks{0},
+        newton{0}, connections{0};
+};
+
+static void update_max(std::atomic<uint64_t> &a, uint64_t v) {
+    uint64_t cur = a.load();
+    while (cur < v && !a.compare_exchange_weak(cur, v)) {}
+}
+
+/* manifold_ss.cpp:28-201 */
+static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG32 &rng,
+                     int &count_out, int &walks_out, Stats &st) {
+    count_out = 0; walks_out = 0;
+    EI ei = sample_emitter_interaction(sc, q, rng);
+    V3 result(0.f);
+    if (sc.casters_ss.empty() || ei.emitter < 0) return result;
+    st.connections++;
+    for (int caster : sc.casters_ss) {
+        V3 value(0.f);
+        SI si_final, si_init;
+        int it = 0;
+        if (!cfg.biased) {
+            count_out = 0;
+            bool ok = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), si_final, si_init, it);
+            walks_out++; st.walks++; st.newton += it;
+            if (!ok) { st.failed++; continue; }
+            st.succeeded++;
+            V3 direction = normalize(si_final.p - q.p);
+            if (!visible(sc, ei, si_final.p)) continue;
+            V3 spec = evaluate_path_contribution(sc, q, ei, si_final);
+            V3 bsdf = diffuse_eval(q, direction);
+            float inv_prob = 1.f;
+            int iterations = 1;
+            st.calls++;
+            while (true) {
+                SI sf, si0;
+                int it2 = 0;
+                bool ok2 = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), sf, si0, it2);
+                walks_out++; st.walks++; st.newton += it2;
+                if (ok2) {
+                    V3 dt = normalize(sf.p - q.p);
+                    if (std::fabs(dot(direction, dt) - 1.f) < cfg.uniqueness_threshold) break;
+                }
+                inv_prob += 1.f;
+                iterations++;
+                if (cfg.max_trials > 0 && iterations > cfg.max_trials) { inv_prob = 0.f; break; }
+            }
+            st.iters += (uint64_t)iterations;
+            update_max(st.iters_max, (uint64_t)iterations);
+            count_out = inv_prob == 0.f ? -1 : iterations;
+            value = bsdf * spec * inv_prob;
+        } else {
+            std::vector<V3> solutions;
+            for (int m = 0; m < cfg.max_trials; ++m) {
+                bool ok = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), si_final, si_init, it);
+                walks_out++; st.walks++; st.newton += it;
+                if (!ok) { st.failed++; continue; }
+                st.succeeded++;
+                V3 direction = normalize(si_final.p - q.p);
+                if (!visible(sc, ei, si_final.p)) continue;
+                bool dup = false;
+                for (const V3 &s : solutions)
+                    if (std::fabs(dot(direction, s) - 1.f) < cfg.uniqueness_threshold) { dup = true; break; }
+                if (dup) continue;
+                solutions.push_back(direction);
+                V3 bsdf = diffuse_eval(q, direction);
+                V3 spec = evaluate_path_contribution(sc, q, ei, si_final);
+                value += bsdf * spec;
+            }
+            count_out += (int)solutions.size();
+        }
+        result += value;
+    }
+    return result;
+}
+
+static Scene *as_scene(void *p) { return reinterpret_cast<Scene *>(p); }
+
+} // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+void *oracle_scene_create() { return new Scene(); }
+void oracle_scene_destroy(void *s) { delete as_scene(s); }
+
+int oracle_scene_add_sphere(void *s, const float *c, float r, int flip, const sms_bsdf *b,
+                            uint32_t flags) {
+    Scene *sc = as_scene(s);
+    Shape sh;
+    sh.kind = 0; sh.center = V3(c[0], c[1], c[2]); sh.radius = std::fabs(r);
+    sh.flip = (flip != 0) != (r <= 0.f);
+    sh.bsdf = *b; sh.flags = flags;
+    sc->shapes.push_back(sh);
+    sc->finalized = false;
+    return (int)sc->shapes.size() - 1;
+}
+
+int oracle_scene_add_mesh(void *s, const float *P, const float *N, const float *UV, uint32_t nv,
+                          const uint32_t *F, uint32_t nf, const sms_bsdf *b, uint32_t flags) {
+    Scene *sc = as_scene(s);
+    Shape sh;
+    sh.kind = 1;
+    sh.P.resize(nv);
+    for (uint32_t i = 0; i < nv; ++i) sh.P[i] = V3(P[3 * i], P[3 * i + 1], P[3 * i + 2]);
+    if (N) { sh.N.resize(nv); for (uint32_t i = 0; i < nv; ++i) sh.N[i] = V3(N[3 * i], N[3 * i + 1], N[3 * i + 2]); }
+    if (UV) { sh.UV.resize(nv); for (uint32_t i = 0; i < nv; ++i) { sh.UV[i].x = UV[2 * i]; sh.UV[i].y = UV[2 * i + 1]; } }
+    sh.F.assign(F, F + 3 * (size_t)nf);
+    /* mesh.cpp:505-528 + distr_1d.h:60-88: double accumulation, float storage */
+    sh.pmf.resize(nf); sh.cdf.resize(nf);
+    double sum = 0.0;
+    bool first = true;
+    for (uint32_t f = 0; f < nf; ++f) {
+        V3 p0 = sh.P[F[3 * f]], p1 = sh.P[F[3 * f + 1]], p2 = sh.P[F[3 * f + 2]];
+        float a = 0.5f * norm(cross(p1 - p0, p2 - p0));
+        sh.pmf[f] = a;
+        sum += (double)a;
+        sh.cdf[f] = (float)sum;
+        if (a > 0.f) { if (first) { sh.valid_lo = f; first = false; } sh.valid_hi = f; }
+    }
+    sh.area_sum = (float)sum;
+    sh.area_norm = (float)(1.0 / sum);
+    sh.bsdf = *b; sh.flags = flags;
+    sc->shapes.push_back(sh);
+    sc->finalized = false;
+    return (int)sc->shapes.size() - 1;
+}
+
+int oracle_scene_add_point_emitter(void *s, const float *p, const float *I, uint32_t flags) {
+    Scene *sc = as_scene(s);
+    Emitter e; e.kind = 0; e.p = V3(p[0], p[1], p[2]); e.radiance = V3(I[0], I[1], I[2]); e.flags = flags;
+    sc->emitters.push_back(e);
+    return (int)sc->emitters.size() - 1;
+}
+
+int oracle_scene_add_area_emitter(void *s, int shape, const float *L, uint32_t flags) {
+    Scene *sc = as_scene(s);
+    if (shape < 0 || shape >= (int)sc->shapes.size() || sc->shapes[shape].kind != 0) return -1;
+    Emitter e; e.kind = 1; e.shape = shape; e.radiance = V3(L[0], L[1], L[2]); e.flags = flags;
+    sc->emitters.push_back(e);
+    sc->shapes[shape].emitter = (int)sc->emitters.size() - 1;
+    return (int)sc->emitters.size() - 1;
+}
+
+void oracle_scene_finalize(void *s) {
+    Scene *sc = as_scene(s);
+    sc->tri_shape.clear(); sc->tri_face.clear(); sc->nodes.clear();
+    sc->casters_ss.clear(); sc->casters_ms.clear(); sc->bouncers.clear();
+    sc->emitters_ss.clear(); sc->emitters_ms.clear();
+    std::vector<uint32_t> idx;
+    for (size_t i = 0; i < sc->shapes.size(); ++i) {
+        const Shape &sh = sc->shapes[i];
+        if (sh.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) sc->casters_ss.push_back((int)i);
+        if (sh.flags & SMS_SHAPE_CAUSTIC_CASTER_MULTI) sc->casters_ms.push_back((int)i);
+        if (sh.flags & SMS_SHAPE_CAUSTIC_BOUNCER) sc->bouncers.push_back((int)i);
+        if (sh.kind == 1)
+            for (uint32_t f = 0; f < sh.F.size() / 3; ++f) {
+                sc->tri_shape.push_back((uint32_t)i); sc->tri_face.push_back(f);
+            }
+    }
+    for (size_t i = 0; i < sc->emitters.size(); ++i) {
+        if (sc->emitters[i].flags & SMS_EMITTER_CAUSTIC_SINGLE) sc->emitters_ss.push_back((int)i);
+        if (sc->emitters[i].flags & SMS_EMITTER_CAUSTIC_MULTI) sc->emitters_ms.push_back((int)i);
+    }
+    size_t np = sc->tri_shape.size();
+    if (np) {
+        std::vector<uint32_t> order(np);
+        std::vector<float> cen(3 * np);
+        for (uint32_t i = 0; i < np; ++i) {
+            order[i] = i;
+            float lo[3], hi[3], c[3];
+            bvh_bounds(*sc, i, lo, hi, c);
+            for (int k = 0; k < 3; ++k) cen[3 * i + k] = c[k];
+        }
+        bvh_build_rec(*sc, order, cen, 0, (uint32_t)np, sc->nodes);
+        std::vector<uint32_t> ts(np), tf(np);
+        for (size_t i = 0; i < np; ++i) { ts[i] = sc->tri_shape[order[i]]; tf[i] = sc->tri_face[order[i]]; }
+        sc->tri_shape.swap(ts); sc->tri_face.swap(tf);
+    }
+    sc->finalized = true;
+}
+
+/* Per-walk sample_path with explicit ei.p and start point (SoA in/out as in
+ * include/sms_gb300.h sms_ss_walk_batch). */
+int oracle_ss_walk_batch(void *s, const sms_config *cfg, int caster, const float *queries,
+                         const float *walk_in, uint32_t n, float *out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    for (uint32_t i = 0; i < n; ++i) {
+        Query q = load_query(queries, n, i);
+        auto w = [&](int k) { return walk_in[(size_t)k * n + i]; };
+        EI ei; ei.p = V3(w(0), w(1), w(2)); ei.is_point = true;
+        V3 ps(w(3), w(4), w(5));
+        V2 smp; smp.x = w(6); smp.y = w(7);
+        SI sf, s0;
+        int it = 0;
+        bool ok = sample_path(*sc, *cfg, caster, q, ei, smp, ps, sf, s0, it);
+        float vals[SMS_WALK_OUT_FIELDS] = {ok ? 1.f : 0.f, (float)it, sf.p.x, sf.p.y, sf.p.z,
+                                           s0.p.x, s0.p.y, s0.p.z, sf.shn.x, sf.shn.y, sf.shn.z};
+        if (!ok) { for (int k = 2; k < 5; ++k) vals[k] = 0.f; for (int k = 8; k < 11; ++k) vals[k] = 0.f; }
+        if (!s0.valid()) for (int k = 5; k < 8; ++k) vals[k] = 0.f;
+        for (int k = 0; k < SMS_WALK_OUT_FIELDS; ++k) out[(size_t)k * n + i] = vals[k];
+    }
+    return 0;
+}
+
+/* SpecularManifoldSingleScatter::specular_manifold_sampling over n queries on
+ * nthreads host threads (blocks of queries, like the reference's TBB loop). */
+int oracle_ss_connect_batch(void *s, const sms_config *cfg, const float *queries, uint32_t n,
+                            uint64_t seed, uint64_t stream_offset, float *value, int32_t *count,
+                            int32_t *walks, int nthreads, uint64_t *stats_out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    Stats st;
+    if (nthreads < 1) nthreads = 1;
+    std::atomic<uint32_t> next{0};
+    const uint32_t block = 64;
+    auto worker = [&]() {
+        while (true) {
+            uint32_t b = next.fetch_add(block);
+            if (b >= n) break;
+            uint32_t e = std::min(n, b + block);
+            for (uint32_t i = b; i < e; ++i) {
+                Query q = load_query(queries, n, i);
+                PCG32 rng;
+                rng.seed(seed, (uint64_t)i + stream_offset);
+                int c = 0, w = 0;
+                V3 v = ss_connect(*sc, *cfg, q, rng, c, w, st);
+                value[i] = v.x; value[(size_t)n + i] = v.y; value[2 * (size_t)n + i] = v.z;
+                count[i] = c; walks[i] = w;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
+    worker();
+    for (auto &t : th) t.join();
+    if (stats_out) {
+        stats_out[0] = st.succeeded; stats_out[1] = st.failed; stats_out[2] = st.calls;
+        stats_out[3] = st.iters; stats_out[4] = st.iters_max; stats_out[5] = st.walks;
+        stats_out[6] = st.newton; stats_out[7] = st.connections;
+    }
+    return 0;
+}
+
+/* Known-answer hooks for the dependency pins (fresnel.h:34-120, warp.h). */
+float oracle_fresnel(float cos_i, float eta, float *cos_t) { return fresnel(cos_i, eta, cos_t); }
+float oracle_fresnel_conductor(float cos_i, float eta, float k) { return fresnel_conductor(cos_i, eta, k); }
+void oracle_uniform_sphere(float u, float v, float *out) {
+    V2 s; s.x = u; s.y = v;
+    V3 r = square_to_uniform_sphere(s);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+void oracle_pcg32(uint64_t initstate, uint64_t initseq, uint32_t n, uint32_t *out) {
+    PCG32 r; r.seed(initstate, initseq);
+    for (uint32_t i = 0; i < n; ++i) out[i] = r.next_u32();
+}
+void oracle_pcg32_f32(uint64_t initstate, uint64_t initseq, uint32_t n, float *out) {
+    PCG32 r; r.seed(initstate, initseq);
+    for (uint32_t i = 0; i < n; ++i) out[i] = r.next_f32();
+}
+
+} // extern "C"

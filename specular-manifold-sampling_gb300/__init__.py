@@ -1,0 +1,350 @@
+"""GB300 (sm_103a) Specular Manifold Sampling -- host-side Python mirror.
+
+The product is the C-ABI library ``libsms_gb300.so`` (declared in
+``include/sms_gb300.h``).  This module binds it with ctypes and mirrors the
+reference's Python-facing interface for the SMS path
+(src/librender/python/manifold_v.cpp:8-100):
+
+    SMSConfig                        include/mitsuba/render/manifold.h:11-45
+    SpecularManifoldSingleScatter    include/mitsuba/render/manifold_ss.h
+        .specular_manifold_sampling  manifold_ss.cpp:28-201 (batched)
+        .sample_path(..., p_start)   manifold_ss.cpp:203-279 (batched)
+
+Where the reference takes one SurfaceInteraction per call, these methods take a
+wavefront of shading points as arrays.  Loading fails loudly when the compiled
+library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field, fields
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libsms_gb300.so"
+
+QUERY_FIELDS = 16
+WALK_IN_FIELDS = 8
+WALK_OUT_FIELDS = 11
+
+SHAPE_CAUSTIC_RECEIVER = 1 << 0
+SHAPE_CAUSTIC_CASTER_SINGLE = 1 << 1
+SHAPE_CAUSTIC_CASTER_MULTI = 1 << 2
+SHAPE_CAUSTIC_BOUNCER = 1 << 3
+SHAPE_GLINTY = 1 << 4
+EMITTER_CAUSTIC_SINGLE = 1 << 0
+EMITTER_CAUSTIC_MULTI = 1 << 1
+
+BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_CONDUCTOR = 0, 1, 2
+
+STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device limit",
+                4: "unsupported", 5: "parse error", 6: "no device"}
+
+
+class SMSError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Config(C.Structure):
+    _fields_ = [("biased", C.c_int32), ("twostage", C.c_int32),
+                ("halfvector_constraints", C.c_int32), ("mnee_init", C.c_int32),
+                ("step_scale", C.c_float), ("max_iterations", C.c_int32),
+                ("solver_threshold", C.c_float), ("uniqueness_threshold", C.c_float),
+                ("max_trials", C.c_int32), ("bounces", C.c_int32),
+                ("bsdf_strategy_only", C.c_int32), ("sms_strategy_only", C.c_int32),
+                ("glints_vectorized", C.c_int32)]
+
+
+class _Bsdf(C.Structure):
+    _fields_ = [("type", C.c_int32), ("eta", C.c_float), ("k", C.c_float),
+                ("albedo", C.c_float * 3)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("value", C.c_void_p), ("count", C.c_void_p), ("walks", C.c_void_p)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "solver_succeeded", "solver_failed", "bernoulli_trial_calls",
+        "bernoulli_trial_iterations", "bernoulli_trial_iterations_max", "walks",
+        "newton_iterations", "connections", "rays", "bvh_nodes", "tri_tests")]
+
+
+_LIB = None
+
+
+def load_library(path: str | os.PathLike | None = None):
+    """Load libsms_gb300.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with build.py (no CPU fallback exists)")
+    lib = C.CDLL(str(p))
+    vp, i32, u32, u64, f32 = C.c_void_p, C.c_int32, C.c_uint32, C.c_uint64, C.c_float
+    sig = {
+        "sms_last_error": (C.c_char_p, []),
+        "sms_config_default": (None, [C.POINTER(_Config)]),
+        "sms_config_parse_xml": (i32, [C.c_char_p, C.POINTER(_Config), C.c_char_p, C.c_size_t]),
+        "sms_scene_create": (i32, [C.POINTER(vp)]),
+        "sms_scene_destroy": (None, [vp]),
+        "sms_scene_add_sphere": (i32, [vp, C.POINTER(f32), f32, i32, C.POINTER(_Bsdf), u32, C.POINTER(i32)]),
+        "sms_scene_add_mesh": (i32, [vp, vp, vp, vp, u32, vp, u32, C.POINTER(_Bsdf), u32, C.POINTER(i32)]),
+        "sms_scene_add_point_emitter": (i32, [vp, C.POINTER(f32), C.POINTER(f32), u32]),
+        "sms_scene_add_area_emitter": (i32, [vp, i32, C.POINTER(f32), u32]),
+        "sms_ctx_create": (i32, [vp, C.POINTER(_Config), i32, C.POINTER(vp)]),
+        "sms_ctx_destroy": (None, [vp]),
+        "sms_ctx_set_config": (i32, [vp, C.POINTER(_Config)]),
+        "sms_ctx_stream": (vp, [vp]),
+        "sms_ctx_set_launch": (i32, [vp, i32, i32]),
+        "sms_stats_read": (i32, [vp, C.POINTER(_Stats)]),
+        "sms_stats_reset": (i32, [vp]),
+        "sms_ss_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
+        "sms_ss_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
+        "sms_ss_walk_batch": (i32, [vp, i32, vp, vp, u32, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(status: int):
+    if status != 0:
+        msg = _LIB.sms_last_error().decode() if _LIB is not None else ""
+        raise SMSError(status, msg)
+
+
+def _f3(v) -> C.Array:
+    a = (C.c_float * 3)(*[float(x) for x in v])
+    return a
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ------------------------------------------------------------------ config
+@dataclass
+class SMSConfig:
+    """Same fields, names and defaults as the reference's SMSConfig."""
+    biased: bool = False
+    twostage: bool = False
+    halfvector_constraints: bool = False
+    mnee_init: bool = False
+    step_scale: float = 1.0
+    max_iterations: int = 20
+    solver_threshold: float = 1e-5
+    uniqueness_threshold: float = 1e-4
+    max_trials: int = -1
+    bounces: int = 1
+    bsdf_strategy_only: bool = False
+    sms_strategy_only: bool = False
+    glints_vectorized: bool = False
+
+    def to_c(self) -> _Config:
+        c = _Config()
+        for f in fields(self):
+            setattr(c, f.name, getattr(self, f.name))
+        return c
+
+    @staticmethod
+    def from_c(c: _Config) -> "SMSConfig":
+        kw = {}
+        for f in fields(SMSConfig):
+            v = getattr(c, f.name)
+            kw[f.name] = bool(v) if f.type in ("bool", bool) else v
+        return SMSConfig(**kw)
+
+    @staticmethod
+    def from_xml(xml: str) -> tuple["SMSConfig", str]:
+        """Parse an <integrator type="path_sms_*"> block like the reference's
+        integrator constructors (path_sms_ss.cpp:47-61)."""
+        lib = load_library()
+        c = _Config()
+        buf = C.create_string_buffer(64)
+        _check(lib.sms_config_parse_xml(xml.encode(), C.byref(c), buf, 64))
+        return SMSConfig.from_c(c), buf.value.decode()
+
+
+def default_config() -> SMSConfig:
+    lib = load_library()
+    c = _Config()
+    lib.sms_config_default(C.byref(c))
+    return SMSConfig.from_c(c)
+
+
+# ------------------------------------------------------------------- scene
+@dataclass
+class Bsdf:
+    type: int = BSDF_DIFFUSE
+    eta: float = 1.0
+    k: float = 0.0
+    albedo: tuple = (0.5, 0.5, 0.5)
+
+    def to_c(self) -> _Bsdf:
+        b = _Bsdf()
+        b.type, b.eta, b.k = self.type, self.eta, self.k
+        b.albedo[:] = [float(x) for x in self.albedo]
+        return b
+
+
+@dataclass
+class SceneDesc:
+    """Backend-neutral scene description (shapes + emitters) that can be
+    instantiated on the GPU library or, in tests, on the CPU oracle."""
+    spheres: list = field(default_factory=list)   # (center, radius, flip, Bsdf, flags)
+    meshes: list = field(default_factory=list)    # (P, N, UV, F, Bsdf, flags)
+    order: list = field(default_factory=list)     # ("sphere"|"mesh", index) in shape-id order
+    point_emitters: list = field(default_factory=list)  # (pos, I, flags)
+    area_emitters: list = field(default_factory=list)   # (shape_id, L, flags)
+
+    def add_sphere(self, center, radius, bsdf: Bsdf, flags: int = 0, flip: bool = False) -> int:
+        self.spheres.append((tuple(center), float(radius), bool(flip), bsdf, flags))
+        self.order.append(("sphere", len(self.spheres) - 1))
+        return len(self.order) - 1
+
+    def add_mesh(self, P, F, bsdf: Bsdf, flags: int = 0, N=None, UV=None) -> int:
+        P = np.ascontiguousarray(P, dtype=np.float32).reshape(-1, 3)
+        F = np.ascontiguousarray(F, dtype=np.uint32).reshape(-1, 3)
+        N = None if N is None else np.ascontiguousarray(N, dtype=np.float32).reshape(-1, 3)
+        UV = None if UV is None else np.ascontiguousarray(UV, dtype=np.float32).reshape(-1, 2)
+        self.meshes.append((P, N, UV, F, bsdf, flags))
+        self.order.append(("mesh", len(self.meshes) - 1))
+        return len(self.order) - 1
+
+    def add_point_emitter(self, pos, intensity, flags: int = EMITTER_CAUSTIC_SINGLE):
+        self.point_emitters.append((tuple(pos), tuple(intensity), flags))
+
+    def add_area_emitter(self, shape_id: int, radiance, flags: int = EMITTER_CAUSTIC_SINGLE):
+        self.area_emitters.append((shape_id, tuple(radiance), flags))
+
+
+class Scene:
+    """Host-side scene builder of the GPU library (sms_scene)."""
+
+    def __init__(self, desc: SceneDesc):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.sms_scene_create(C.byref(h)))
+        self._h = h
+        self.desc = desc
+        self._keep = []
+        for kind, idx in desc.order:
+            sid = C.c_int32()
+            if kind == "sphere":
+                c, r, flip, b, flags = desc.spheres[idx]
+                _check(lib.sms_scene_add_sphere(h, _f3(c), r, int(flip), C.byref(b.to_c()), flags,
+                                                C.byref(sid)))
+            else:
+                P, N, UV, F, b, flags = desc.meshes[idx]
+                self._keep += [P, N, UV, F]
+                _check(lib.sms_scene_add_mesh(h, _ptr(P), None if N is None else _ptr(N),
+                                              None if UV is None else _ptr(UV), P.shape[0], _ptr(F),
+                                              F.shape[0], C.byref(b.to_c()), flags, C.byref(sid)))
+        for pos, I, flags in desc.point_emitters:
+            _check(lib.sms_scene_add_point_emitter(h, _f3(pos), _f3(I), flags))
+        for sid, L, flags in desc.area_emitters:
+            _check(lib.sms_scene_add_area_emitter(h, sid, _f3(L), flags))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _LIB is not None:
+            _LIB.sms_scene_destroy(self._h)
+            self._h = None
+
+
+class Context:
+    """Device copy of a scene plus solver config (sms_ctx)."""
+
+    def __init__(self, scene: Scene, config: SMSConfig, device: int = 0):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.sms_ctx_create(scene.handle, C.byref(config.to_c()), device, C.byref(h)))
+        self._h = h
+        self.config = config
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return _LIB.sms_ctx_stream(self._h) or 0
+
+    def set_config(self, config: SMSConfig):
+        _check(_LIB.sms_ctx_set_config(self._h, C.byref(config.to_c())))
+        self.config = config
+
+    def set_launch(self, blocks_per_sm: int = 0, threads_per_block: int = 0):
+        _check(_LIB.sms_ctx_set_launch(self._h, blocks_per_sm, threads_per_block))
+
+    def stats(self) -> dict:
+        s = _Stats()
+        _check(_LIB.sms_stats_read(self._h, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in _Stats._fields_}
+
+    def reset_stats(self):
+        _check(_LIB.sms_stats_reset(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) and _LIB is not None:
+            _LIB.sms_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def _soa(a: np.ndarray, rows: int, n: int) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.shape != (rows, n):
+        raise ValueError(f"expected SoA array of shape ({rows}, {n}), got {a.shape}")
+    return a
+
+
+class SpecularManifoldSingleScatter:
+    """Batched SpecularManifoldSingleScatter (include/mitsuba/render/manifold_ss.h)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def specular_manifold_sampling(self, queries: np.ndarray, seed: int = 0, stream_offset: int = 0):
+        """queries: (16, n) float32 SoA.  Returns (value (3, n), count (n,), walks (n,))."""
+        n = queries.shape[1]
+        q = _soa(queries, QUERY_FIELDS, n)
+        value = np.zeros((3, n), np.float32)
+        count = np.zeros(n, np.int32)
+        walks = np.zeros(n, np.int32)
+        r = _Result(_ptr(value), _ptr(count), _ptr(walks))
+        _check(_LIB.sms_ss_connect_batch(self.ctx.handle, _ptr(q), n, seed, stream_offset, C.byref(r)))
+        return value, count, walks
+
+    def specular_manifold_sampling_device(self, queries_ptr: int, n: int, value_ptr: int, count_ptr: int,
+                                          walks_ptr: int, seed: int = 0, stream_offset: int = 0):
+        """Device-pointer variant (asynchronous on ctx.stream)."""
+        r = _Result(value_ptr, count_ptr, walks_ptr)
+        _check(_LIB.sms_ss_connect_batch_device(self.ctx.handle, queries_ptr, n, seed, stream_offset,
+                                                C.byref(r)))
+
+    def sample_path(self, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
+        """Per-walk sample_path with explicit emitter point and start point.
+        walk_in: (8, n) rows ei.p(3), p_start(3), sample(2).  Returns (11, n)."""
+        n = queries.shape[1]
+        q = _soa(queries, QUERY_FIELDS, n)
+        w = _soa(walk_in, WALK_IN_FIELDS, n)
+        out = np.zeros((WALK_OUT_FIELDS, n), np.float32)
+        _check(_LIB.sms_ss_walk_batch(self.ctx.handle, caster, _ptr(q), _ptr(w), n, _ptr(out)))
+        return out

@@ -1,0 +1,636 @@
+// sms_host.cpp -- host side of the GB300 SMS library: scene builder, BVH
+// builder, device contexts and the extern "C" entry points of sms_gb300.h.
+//
+// The reference builds a SAH kd-tree over the scene (include/mitsuba/render/
+// kdtree.h) and answers one ray at a time per host thread.  Here the host
+// builds a binned-SAH BVH2 whose nodes carry both children's boxes (one 64-byte
+// record per node), uploads it once per context, and every query batch runs as
+// one persistent kernel on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sms_gb300.h"
+#include "sms_device.cuh"
+#include "sms_kernels.h"
+#include "sms_bvh.h"
+
+using namespace sms;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static sms_status fail(sms_status st, const std::string &msg) {
+    g_last_error = msg;
+    return st;
+}
+
+static sms_status cuda_fail(cudaError_t e, const char *what) {
+    return fail(SMS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(call)                                        \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
+    } while (0)
+
+extern "C" const char *sms_last_error(void) { return g_last_error.c_str(); }
+
+// ------------------------------------------------------------------ config
+extern "C" void sms_config_default(sms_config *c) {
+    if (!c) return;
+    c->biased = 0;
+    c->twostage = 0;
+    c->halfvector_constraints = 0;
+    c->mnee_init = 0;
+    c->step_scale = 1.f;
+    c->max_iterations = 20;
+    c->solver_threshold = 1e-5f;
+    c->uniqueness_threshold = 1e-4f;
+    c->max_trials = -1;
+    c->bounces = 1;
+    c->bsdf_strategy_only = 0;
+    c->sms_strategy_only = 0;
+    c->glints_vectorized = 0;
+}
+
+static bool attr(const std::string &tag, const char *name, std::string &out) {
+    std::string key = std::string(name) + "=\"";
+    size_t p = tag.find(key);
+    if (p == std::string::npos) return false;
+    p += key.size();
+    size_t e = tag.find('"', p);
+    if (e == std::string::npos) return false;
+    out = tag.substr(p, e - p);
+    return true;
+}
+
+static bool parse_bool(const std::string &v, bool &ok) {
+    ok = true;
+    if (v == "true" || v == "1") return true;
+    if (v == "false" || v == "0") return false;
+    ok = false;
+    return false;
+}
+
+// Reads the parameters the reference integrators read (path_sms_ss.cpp:47-61,
+// path_sms_ms.cpp:149-161, path_sms_glints.cpp:42-54).  Unknown names are
+// ignored, as Properties lookups ignore them.
+extern "C" sms_status sms_config_parse_xml(const char *xml, sms_config *cfg, char *type_out,
+                                           size_t type_cap) {
+    if (!xml || !cfg) return fail(SMS_ERR_INVALID_ARG, "sms_config_parse_xml: null argument");
+    std::string s(xml);
+    size_t ip = s.find("<integrator");
+    if (ip == std::string::npos) return fail(SMS_ERR_PARSE, "no <integrator> element");
+    size_t ie = s.find('>', ip);
+    if (ie == std::string::npos) return fail(SMS_ERR_PARSE, "unterminated <integrator> tag");
+    std::string itag = s.substr(ip, ie - ip + 1);
+    std::string type;
+    if (!attr(itag, "type", type)) return fail(SMS_ERR_PARSE, "<integrator> without type");
+    sms_config c;
+    sms_config_default(&c);
+    if (type == "path_sms_ms") c.bounces = 2;
+    size_t end = s.find("</integrator>", ie);
+    if (end == std::string::npos) end = s.size();
+    size_t pos = ie + 1;
+    while (true) {
+        size_t t = s.find('<', pos);
+        if (t == std::string::npos || t >= end) break;
+        size_t te = s.find('>', t);
+        if (te == std::string::npos) return fail(SMS_ERR_PARSE, "unterminated tag");
+        std::string tag = s.substr(t, te - t + 1);
+        pos = te + 1;
+        std::string kind;
+        if (tag.compare(0, 8, "<boolean") == 0) kind = "boolean";
+        else if (tag.compare(0, 8, "<integer") == 0) kind = "integer";
+        else if (tag.compare(0, 6, "<float") == 0) kind = "float";
+        else continue;
+        std::string name, value;
+        if (!attr(tag, "name", name) || !attr(tag, "value", value))
+            return fail(SMS_ERR_PARSE, "parameter without name/value: " + tag);
+        char *ep = nullptr;
+        if (kind == "boolean") {
+            bool ok;
+            bool b = parse_bool(value, ok);
+            if (!ok) return fail(SMS_ERR_PARSE, "bad boolean value for " + name + ": " + value);
+            int iv = b ? 1 : 0;
+            if (name == "biased") c.biased = iv;
+            else if (name == "twostage") c.twostage = iv;
+            else if (name == "halfvector_constraints") c.halfvector_constraints = iv;
+            else if (name == "mnee_init") c.mnee_init = iv;
+            else if (name == "bsdf_strategy_only") c.bsdf_strategy_only = iv;
+            else if (name == "sms_strategy_only") c.sms_strategy_only = iv;
+            else if (name == "glints_vectorized") c.glints_vectorized = iv;
+        } else if (kind == "integer") {
+            long v = std::strtol(value.c_str(), &ep, 10);
+            if (ep == value.c_str() || *ep) return fail(SMS_ERR_PARSE, "bad integer for " + name);
+            if (name == "max_iterations") c.max_iterations = (int32_t)v;
+            else if (name == "max_trials") c.max_trials = (int32_t)v;
+            else if (name == "bounces") c.bounces = (int32_t)v;
+        } else {
+            float v = std::strtof(value.c_str(), &ep);
+            if (ep == value.c_str() || *ep) return fail(SMS_ERR_PARSE, "bad float for " + name);
+            if (name == "step_scale") c.step_scale = v;
+            else if (name == "solver_threshold") c.solver_threshold = v;
+            else if (name == "uniqueness_threshold") c.uniqueness_threshold = v;
+        }
+    }
+    *cfg = c;
+    if (type_out && type_cap) {
+        std::snprintf(type_out, type_cap, "%s", type.c_str());
+    }
+    return SMS_OK;
+}
+
+// ------------------------------------------------------------------- scene
+struct HostShape {
+    int kind = kShapeSphere;
+    float center[3] = {0, 0, 0};
+    float radius = 1.f;
+    int flip = 0;
+    std::vector<float> P, N, UV;
+    std::vector<uint32_t> F;
+    sms_bsdf bsdf{};
+    uint32_t flags = 0;
+    int emitter = -1;
+};
+
+struct HostEmitter {
+    int kind = 0;
+    float p[3] = {0, 0, 0};
+    float rgb[3] = {0, 0, 0};
+    int shape = -1;
+    uint32_t flags = 0;
+};
+
+struct sms_scene {
+    std::vector<HostShape> shapes;
+    std::vector<HostEmitter> emitters;
+};
+
+extern "C" sms_status sms_scene_create(sms_scene **out) {
+    if (!out) return fail(SMS_ERR_INVALID_ARG, "sms_scene_create: null out");
+    *out = new sms_scene();
+    return SMS_OK;
+}
+
+extern "C" void sms_scene_destroy(sms_scene *s) { delete s; }
+
+static sms_status check_bsdf(const sms_bsdf *b) {
+    if (!b) return fail(SMS_ERR_INVALID_ARG, "null bsdf");
+    if (b->type < SMS_BSDF_DIFFUSE || b->type > SMS_BSDF_CONDUCTOR)
+        return fail(SMS_ERR_INVALID_ARG, "unknown bsdf type");
+    if (b->type == SMS_BSDF_DIELECTRIC && !(b->eta > 0.f))
+        return fail(SMS_ERR_INVALID_ARG, "dielectric eta must be positive");
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_scene_add_sphere(sms_scene *s, const float center[3], float radius, int32_t flip,
+                                           const sms_bsdf *bsdf, uint32_t flags, int32_t *id) {
+    if (!s || !center) return fail(SMS_ERR_INVALID_ARG, "sms_scene_add_sphere: null argument");
+    if (sms_status st = check_bsdf(bsdf)) return st;
+    if (!(radius != 0.f) || !std::isfinite(radius)) return fail(SMS_ERR_INVALID_ARG, "sphere radius must be nonzero");
+    HostShape h;
+    h.kind = kShapeSphere;
+    std::memcpy(h.center, center, sizeof(h.center));
+    // sphere.cpp:128-131: a negative radius flips the normals
+    h.radius = std::fabs(radius);
+    h.flip = (flip != 0) != (radius < 0.f);
+    h.bsdf = *bsdf;
+    h.flags = flags;
+    s->shapes.push_back(h);
+    if (id) *id = (int32_t)s->shapes.size() - 1;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_scene_add_mesh(sms_scene *s, const float *P, const float *N, const float *UV,
+                                         uint32_t nv, const uint32_t *F, uint32_t nf, const sms_bsdf *bsdf,
+                                         uint32_t flags, int32_t *id) {
+    if (!s || !P || !F) return fail(SMS_ERR_INVALID_ARG, "sms_scene_add_mesh: null argument");
+    if (nv == 0 || nf == 0) return fail(SMS_ERR_INVALID_ARG, "sms_scene_add_mesh: empty mesh");
+    if (sms_status st = check_bsdf(bsdf)) return st;
+    for (size_t i = 0; i < 3 * (size_t)nf; ++i)
+        if (F[i] >= nv) return fail(SMS_ERR_INVALID_ARG, "sms_scene_add_mesh: face index out of range");
+    HostShape h;
+    h.kind = kShapeMesh;
+    h.P.assign(P, P + 3 * (size_t)nv);
+    if (N) h.N.assign(N, N + 3 * (size_t)nv);
+    if (UV) h.UV.assign(UV, UV + 2 * (size_t)nv);
+    h.F.assign(F, F + 3 * (size_t)nf);
+    h.bsdf = *bsdf;
+    h.flags = flags;
+    s->shapes.push_back(std::move(h));
+    if (id) *id = (int32_t)s->shapes.size() - 1;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_scene_add_point_emitter(sms_scene *s, const float p[3], const float I[3],
+                                                  uint32_t flags) {
+    if (!s || !p || !I) return fail(SMS_ERR_INVALID_ARG, "sms_scene_add_point_emitter: null argument");
+    HostEmitter e;
+    e.kind = 0;
+    std::memcpy(e.p, p, sizeof(e.p));
+    std::memcpy(e.rgb, I, sizeof(e.rgb));
+    e.flags = flags;
+    s->emitters.push_back(e);
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_scene_add_area_emitter(sms_scene *s, int32_t shape, const float L[3],
+                                                 uint32_t flags) {
+    if (!s || !L) return fail(SMS_ERR_INVALID_ARG, "sms_scene_add_area_emitter: null argument");
+    if (shape < 0 || shape >= (int32_t)s->shapes.size())
+        return fail(SMS_ERR_INVALID_ARG, "sms_scene_add_area_emitter: unknown shape id");
+    if (s->shapes[shape].kind != kShapeSphere)
+        return fail(SMS_ERR_UNSUPPORTED, "area emitters are supported on spheres only");
+    if (s->shapes[shape].emitter >= 0)
+        return fail(SMS_ERR_INVALID_ARG, "an area emitter can only be attached to a single shape");
+    HostEmitter e;
+    e.kind = 1;
+    e.shape = shape;
+    std::memcpy(e.rgb, L, sizeof(e.rgb));
+    e.flags = flags;
+    s->emitters.push_back(e);
+    s->shapes[shape].emitter = (int)s->emitters.size() - 1;
+    return SMS_OK;
+}
+
+// ---------------------------------------------------------------- context
+struct sms_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    sms_config cfg{};
+    DevScene dsc{};
+    DevCounters *ctr = nullptr;
+    std::vector<void *> allocs;
+    int num_sms = 0;
+    int blocks_per_sm = 0;
+    int threads = 128;
+    // device staging for the host-pointer entry points
+    void *io = nullptr;
+    size_t io_bytes = 0;
+    std::vector<int> casters_ss;
+};
+
+template <typename T>
+static sms_status upload(sms_ctx *c, const std::vector<T> &v, const T **out) {
+    *out = nullptr;
+    if (v.empty()) return SMS_OK;
+    void *p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, v.size() * sizeof(T)));
+    c->allocs.push_back(p);
+    CUDA_TRY(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    *out = reinterpret_cast<const T *>(p);
+    return SMS_OK;
+}
+
+static SolverCfg solver_cfg(const sms_config &c) {
+    SolverCfg s;
+    s.biased = c.biased;
+    s.halfvector = c.halfvector_constraints;
+    s.max_iterations = c.max_iterations;
+    s.max_trials = c.max_trials;
+    s.solver_threshold = c.solver_threshold;
+    s.uniqueness_threshold = c.uniqueness_threshold;
+    s.step_scale = c.step_scale;
+    return s;
+}
+
+static sms_status validate_cfg(const sms_config *c) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null config");
+    if (c->twostage) return fail(SMS_ERR_UNSUPPORTED, "twostage solver is not implemented");
+    if (c->mnee_init) return fail(SMS_ERR_UNSUPPORTED, "mnee_init is not implemented");
+    if (c->max_iterations < 0) return fail(SMS_ERR_INVALID_ARG, "max_iterations must be >= 0");
+    return SMS_OK;
+}
+
+extern "C" void sms_ctx_destroy(sms_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->io) cudaFree(c->io);
+    if (c->ctr) cudaFree(c->ctr);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
+    // shapes, meshes and area CDFs
+    std::vector<DevShape> shapes;
+    std::vector<float> P, N, UV, cdf, pmf;
+    std::vector<uint32_t> F;
+    std::vector<uint32_t> tri_shape, tri_face;
+    DevScene &d = c->dsc;
+    std::memset(&d, 0, sizeof(d));
+    for (size_t i = 0; i < s->shapes.size(); ++i) {
+        const HostShape &h = s->shapes[i];
+        DevShape ds;
+        std::memset(&ds, 0, sizeof(ds));
+        ds.kind = h.kind;
+        ds.flags = h.flags;
+        ds.bsdf_type = h.bsdf.type;
+        ds.eta = h.bsdf.eta;
+        ds.k = h.bsdf.k;
+        // manifold.h:94-96: real ior -> eta, complex or non-specular -> 1
+        bool real_ior = h.bsdf.type == SMS_BSDF_DIELECTRIC ||
+                        (h.bsdf.type == SMS_BSDF_CONDUCTOR && h.bsdf.k == 0.f);
+        ds.spec_eta = real_ior ? h.bsdf.eta : 1.f;
+        ds.emitter = h.emitter;
+        if (h.kind == kShapeSphere) {
+            ds.cx = h.center[0]; ds.cy = h.center[1]; ds.cz = h.center[2];
+            ds.radius = h.radius;
+            ds.flip = h.flip;
+            if (d.n_spheres >= kMaxSpheres) return fail(SMS_ERR_UNSUPPORTED, "too many spheres");
+            d.sphere_shape[d.n_spheres] = (int)i;
+            d.sphere[d.n_spheres] = make_float4(h.center[0], h.center[1], h.center[2], h.radius);
+            d.n_spheres++;
+        } else {
+            uint32_t nv = (uint32_t)(h.P.size() / 3), nf = (uint32_t)(h.F.size() / 3);
+            ds.v_off = (uint32_t)(P.size() / 3);
+            ds.f_off = (uint32_t)(F.size() / 3);
+            ds.n_faces = nf;
+            ds.has_normals = !h.N.empty();
+            ds.has_uvs = !h.UV.empty();
+            P.insert(P.end(), h.P.begin(), h.P.end());
+            if (ds.has_normals) N.insert(N.end(), h.N.begin(), h.N.end());
+            else N.resize(N.size() + 3 * (size_t)nv, 0.f);
+            if (ds.has_uvs) UV.insert(UV.end(), h.UV.begin(), h.UV.end());
+            else UV.resize(UV.size() + 2 * (size_t)nv, 0.f);
+            F.insert(F.end(), h.F.begin(), h.F.end());
+            // mesh.cpp:505-528 + distr_1d.h:60-88: double accumulation, float storage
+            ds.cdf_off = (uint32_t)cdf.size();
+            double sum = 0.0;
+            bool first = true;
+            for (uint32_t f = 0; f < nf; ++f) {
+                const float *p0 = &h.P[3 * h.F[3 * f]], *p1 = &h.P[3 * h.F[3 * f + 1]],
+                            *p2 = &h.P[3 * h.F[3 * f + 2]];
+                float e0[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+                float e1[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+                float cx = e0[1] * e1[2] - e0[2] * e1[1], cy = e0[2] * e1[0] - e0[0] * e1[2],
+                      cz = e0[0] * e1[1] - e0[1] * e1[0];
+                float a = 0.5f * std::sqrt(cx * cx + cy * cy + cz * cz);
+                pmf.push_back(a);
+                sum += (double)a;
+                cdf.push_back((float)sum);
+                if (a > 0.f) {
+                    if (first) { ds.valid_lo = f; first = false; }
+                    ds.valid_hi = f;
+                }
+                tri_shape.push_back((uint32_t)i);
+                tri_face.push_back(f);
+            }
+            if (first) return fail(SMS_ERR_INVALID_ARG, "mesh has no face with positive area");
+            ds.area_sum = (float)sum;
+            ds.area_norm = (float)(1.0 / sum);
+        }
+        if (h.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) {
+            if (d.n_casters_ss >= kMaxCasters) return fail(SMS_ERR_UNSUPPORTED, "too many casters");
+            d.casters_ss[d.n_casters_ss++] = (int)i;
+        }
+        shapes.push_back(ds);
+    }
+    std::vector<DevEmitter> em;
+    for (size_t i = 0; i < s->emitters.size(); ++i) {
+        const HostEmitter &h = s->emitters[i];
+        DevEmitter e;
+        std::memset(&e, 0, sizeof(e));
+        e.kind = h.kind;
+        e.px = h.p[0]; e.py = h.p[1]; e.pz = h.p[2];
+        e.r = h.rgb[0]; e.g = h.rgb[1]; e.b = h.rgb[2];
+        e.shape = h.shape;
+        em.push_back(e);
+        if (h.flags & SMS_EMITTER_CAUSTIC_SINGLE) {
+            if (d.n_emitters_ss >= kMaxEmitters) return fail(SMS_ERR_UNSUPPORTED, "too many emitters");
+            d.emitters_ss[d.n_emitters_ss++] = (int)i;
+        }
+    }
+    // BVH over all mesh triangles
+    std::vector<BvhInputTri> in;
+    in.reserve(tri_shape.size());
+    for (size_t k = 0; k < tri_shape.size(); ++k) {
+        const HostShape &h = s->shapes[tri_shape[k]];
+        uint32_t f = tri_face[k];
+        BvhInputTri t;
+        for (int j = 0; j < 3; ++j) {
+            t.p0[j] = h.P[3 * h.F[3 * f] + j];
+            t.p1[j] = h.P[3 * h.F[3 * f + 1] + j];
+            t.p2[j] = h.P[3 * h.F[3 * f + 2] + j];
+        }
+        t.shape = (int)tri_shape[k];
+        t.face = (int)f;
+        in.push_back(t);
+    }
+    BvhResult bvh;
+    std::string berr;
+    if (!in.empty() && (!build_bvh(in, bvh, berr) || !validate_bvh(bvh, berr)))
+        return fail(SMS_ERR_INVALID_ARG, "BVH build: " + berr);
+    const std::vector<float4> &nodes = bvh.nodes, &tris = bvh.tris;
+    if (sms_status st = upload(c, nodes, &d.nodes)) return st;
+    if (sms_status st = upload(c, tris, &d.tris)) return st;
+    d.n_nodes = (uint32_t)(nodes.size() / 4);
+    d.n_tris = (uint32_t)(tris.size() / 3);
+    if (sms_status st = upload(c, shapes, &d.shapes)) return st;
+    d.n_shapes = (int)shapes.size();
+    if (sms_status st = upload(c, P, &d.mesh_P)) return st;
+    if (sms_status st = upload(c, N, &d.mesh_N)) return st;
+    if (sms_status st = upload(c, UV, &d.mesh_UV)) return st;
+    if (sms_status st = upload(c, F, &d.mesh_F)) return st;
+    if (sms_status st = upload(c, cdf, &d.cdf)) return st;
+    if (sms_status st = upload(c, pmf, &d.pmf)) return st;
+    if (sms_status st = upload(c, em, &d.emitters)) return st;
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_ctx_create(const sms_scene *s, const sms_config *cfg, int32_t device, sms_ctx **out) {
+    if (!s || !out) return fail(SMS_ERR_INVALID_ARG, "sms_ctx_create: null argument");
+    *out = nullptr;
+    if (sms_status st = validate_cfg(cfg)) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SMS_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= ndev) return fail(SMS_ERR_INVALID_ARG, "device id out of range");
+    sms_ctx *c = new sms_ctx();
+    c->device = device;
+    c->cfg = *cfg;
+    sms_status st = SMS_OK;
+    do {
+        cudaError_t e = cudaSetDevice(device);
+        if (e != cudaSuccess) { st = cuda_fail(e, "cudaSetDevice"); break; }
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { st = cuda_fail(e, "cudaStreamCreate"); break; }
+        e = cudaMalloc(&c->ctr, sizeof(DevCounters));
+        if (e != cudaSuccess) { st = cuda_fail(e, "cudaMalloc(counters)"); break; }
+        e = cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters), c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "cudaMemset(counters)"); break; }
+        cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+        st = ctx_build(c, s);
+    } while (0);
+    if (st != SMS_OK) { sms_ctx_destroy(c); return st; }
+    *out = c;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_ctx_set_config(sms_ctx *c, const sms_config *cfg) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    if (sms_status st = validate_cfg(cfg)) return st;
+    c->cfg = *cfg;
+    return SMS_OK;
+}
+
+extern "C" void *sms_ctx_stream(sms_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+extern "C" sms_status sms_ctx_set_launch(sms_ctx *c, int32_t bps, int32_t tpb) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    if (bps < 0 || tpb < 0) return fail(SMS_ERR_INVALID_ARG, "negative launch parameter");
+    if (tpb != 0 && tpb != 128) return fail(SMS_ERR_UNSUPPORTED, "threads per block must be 128");
+    c->blocks_per_sm = bps;
+    return SMS_OK;
+}
+
+static sms_status check_device_error(sms_ctx *c) {
+    unsigned err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, &c->ctr->error, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (err) {
+        CUDA_TRY(cudaMemsetAsync(&c->ctr->error, 0, sizeof(unsigned), c->stream));
+        std::string m = "device limit hit:";
+        if (err & kErrStackOverflow) m += " BVH traversal stack overflow;";
+        if (err & kErrTrialLimit) m += " Bernoulli trials exceeded the hard limit;";
+        if (err & kErrSolutionOverflow) m += " more unique solutions than the per-query capacity;";
+        if (err & kErrTraversalLimit) m += " BVH traversal step limit (malformed tree);";
+        return fail(SMS_ERR_DEVICE_LIMIT, m);
+    }
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_stats_read(sms_ctx *c, sms_stats *out) {
+    if (!c || !out) return fail(SMS_ERR_INVALID_ARG, "null argument");
+    DevCounters h;
+    CUDA_TRY(cudaSetDevice(c->device));
+    CUDA_TRY(cudaMemcpyAsync(&h, c->ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    out->solver_succeeded = h.solver_succeeded;
+    out->solver_failed = h.solver_failed;
+    out->bernoulli_trial_calls = h.bernoulli_calls;
+    out->bernoulli_trial_iterations = h.bernoulli_iters;
+    out->bernoulli_trial_iterations_max = h.bernoulli_max;
+    out->walks = h.walks;
+    out->newton_iterations = h.newton_iters;
+    out->connections = h.connections;
+    out->rays = h.rays;
+    out->bvh_nodes = h.bvh_nodes;
+    out->tri_tests = h.tri_tests;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_stats_reset(sms_ctx *c) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    CUDA_TRY(cudaSetDevice(c->device));
+    CUDA_TRY(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters), c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return SMS_OK;
+}
+
+static int connect_blocks(sms_ctx *c) {
+    int bps = c->blocks_per_sm;
+    if (bps <= 0) {
+        bps = ss_connect_max_blocks_per_sm();
+        if (bps <= 0) bps = 1;
+    }
+    return bps * c->num_sms;
+}
+
+extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                                  uint64_t stream_off, sms_result *out) {
+    if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
+        return fail(SMS_ERR_INVALID_ARG, "sms_ss_connect_batch_device: null argument");
+    if (n == 0) return SMS_OK;
+    if (c->cfg.biased && c->cfg.max_trials > 0x7fffffff / 2)
+        return fail(SMS_ERR_INVALID_ARG, "max_trials too large");
+    CUDA_TRY(cudaSetDevice(c->device));
+    CUDA_TRY(launch_ss_connect(c->dsc, solver_cfg(c->cfg), q, n, seed, stream_off, out->value, out->count,
+                               out->walks, c->ctr, connect_blocks(c), c->stream));
+    return SMS_OK;
+}
+
+// Device staging buffer of the host-pointer entry points, grown on demand and
+// kept for the context's lifetime.
+static sms_status ensure_io(sms_ctx *c, size_t bytes) {
+    if (c->io_bytes >= bytes) return SMS_OK;
+    if (c->io) {
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        cudaFree(c->io);
+        c->io = nullptr;
+        c->io_bytes = 0;
+    }
+    CUDA_TRY(cudaMalloc(&c->io, bytes));
+    c->io_bytes = bytes;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_ss_connect_batch(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                           uint64_t stream_off, sms_result *out) {
+    if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
+        return fail(SMS_ERR_INVALID_ARG, "sms_ss_connect_batch: null argument");
+    if (n == 0) return SMS_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    size_t qb = (size_t)SMS_QUERY_FIELDS * n * sizeof(float);
+    size_t vb = 3 * (size_t)n * sizeof(float), ib = (size_t)n * sizeof(int32_t);
+    if (sms_status st = ensure_io(c, qb + vb + 2 * ib)) return st;
+    char *dbuf = reinterpret_cast<char *>(c->io);
+    float *dq = reinterpret_cast<float *>(dbuf);
+    float *dv = reinterpret_cast<float *>(dbuf + qb);
+    int32_t *dc = reinterpret_cast<int32_t *>(dbuf + qb + vb);
+    int32_t *dw = reinterpret_cast<int32_t *>(dbuf + qb + vb + ib);
+    sms_status st = SMS_OK;
+    do {
+        cudaError_t e = cudaMemcpyAsync(dq, q, qb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy queries"); break; }
+        sms_result r{dv, dc, dw};
+        st = sms_ss_connect_batch_device(c, dq, n, seed, stream_off, &r);
+        if (st) break;
+        e = cudaMemcpyAsync(out->value, dv, vb, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->count, dc, ib, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->walks, dw, ib, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy results"); break; }
+    } while (0);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "sms_ss_connect_batch");
+    return check_device_error(c);
+}
+
+extern "C" sms_status sms_ss_walk_batch(sms_ctx *c, int32_t caster, const float *q, const float *w, uint32_t n,
+                                        float *out) {
+    if (!c || (n && (!q || !w || !out))) return fail(SMS_ERR_INVALID_ARG, "sms_ss_walk_batch: null argument");
+    if (caster < 0 || caster >= c->dsc.n_shapes) return fail(SMS_ERR_INVALID_ARG, "unknown caster shape id");
+    if (n == 0) return SMS_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    size_t qb = (size_t)SMS_QUERY_FIELDS * n * sizeof(float), wb = (size_t)SMS_WALK_IN_FIELDS * n * sizeof(float),
+           ob = (size_t)SMS_WALK_OUT_FIELDS * n * sizeof(float);
+    if (sms_status st = ensure_io(c, qb + wb + ob)) return st;
+    char *dbuf = reinterpret_cast<char *>(c->io);
+    sms_status st = SMS_OK;
+    do {
+        cudaError_t e = cudaMemcpyAsync(dbuf, q, qb, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dbuf + qb, w, wb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy walk inputs"); break; }
+        e = launch_ss_walk(c->dsc, solver_cfg(c->cfg), caster, reinterpret_cast<float *>(dbuf),
+                           reinterpret_cast<float *>(dbuf + qb), n, reinterpret_cast<float *>(dbuf + qb + wb),
+                           c->ctr, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "launch ss_walk"); break; }
+        e = cudaMemcpyAsync(out, dbuf + qb + wb, ob, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy walk outputs"); break; }
+    } while (0);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "sms_ss_walk_batch");
+    return check_device_error(c);
+}

@@ -1,0 +1,176 @@
+"""Synthetic SMS workloads with the shapes, sizes and seeds of the benchmark
+configurations (the reference's paper scenes are partly missing and are not
+used).  Every random draw comes from PCG32 streams so the GPU library, the
+oracle and the tests see identical inputs.
+
+  sphere_scene      glass sphere r=1 at (0,0,1.5), IOR 1.5, over the plane z=0,
+                    point light (0,0,5) I=100; 64x64 query grid on [-2,2]^2;
+                    biased SMS, 16 trials, 20 iterations, threshold 1e-5.
+  water_scene       z = 1 + sum of 32 sinusoids (a ~ U(0.002,0.02),
+                    |k| ~ U(2,40), uniform direction and phase) tessellated to a
+                    512x512 vertex grid over [-1,1]^2 (522,242 triangles), IOR
+                    1.33; spherical area light r=0.1 at (0,0,10); queries
+                    uniform on [-1,1]^2; unbiased SMS, trials capped at 256.
+
+The receiver plane z=0 is not part of the ray-cast scene: every ray of the
+single-scatter path starts on it or above it and ends above it, so no ray can
+reach it past the ray epsilon.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import (BSDF_CONDUCTOR, BSDF_DIELECTRIC, BSDF_DIFFUSE, EMITTER_CAUSTIC_SINGLE,
+               SHAPE_CAUSTIC_CASTER_SINGLE, QUERY_FIELDS, Bsdf, SceneDesc, SMSConfig)
+
+_MUL = np.uint64(6364136223846793005)
+_M64 = (1 << 64) - 1
+
+
+class Pcg32:
+    """Scalar PCG32 (O'Neill), same stream convention as the device code."""
+
+    def __init__(self, initstate: int, initseq: int = 0):
+        self.state = 0
+        self.inc = ((initseq << 1) | 1) & _M64
+        self.next_u32()
+        self.state = (self.state + initstate) & _M64
+        self.next_u32()
+
+    def next_u32(self) -> int:
+        old = self.state
+        self.state = (old * 6364136223846793005 + self.inc) & _M64
+        xs = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+        rot = old >> 59
+        return ((xs >> rot) | (xs << ((-rot) & 31))) & 0xFFFFFFFF
+
+    def next_f32(self) -> float:
+        bits = (self.next_u32() >> 9) | 0x3F800000
+        return float(np.array([bits], np.uint32).view(np.float32)[0]) - 1.0
+
+
+def pcg32_streams_f32(initstate: int, streams: np.ndarray, count: int) -> np.ndarray:
+    """`count` float32 draws from each of many PCG32 streams, vectorized over
+    streams.  Returns an array of shape (count, len(streams))."""
+    with np.errstate(over="ignore"):
+        inc = (np.asarray(streams, np.uint64) << np.uint64(1)) | np.uint64(1)
+        state = np.zeros_like(inc)
+
+        def step(st):
+            old = st
+            new = old * _MUL + inc
+            xs = (((old >> np.uint64(18)) ^ old) >> np.uint64(27)).astype(np.uint32)
+            rot = (old >> np.uint64(59)).astype(np.uint32)
+            out = (xs >> rot) | (xs << ((np.uint32(32) - rot) & np.uint32(31)))
+            return new, out
+
+        state, _ = step(state)
+        state = state + np.uint64(initstate)
+        state, _ = step(state)
+        res = np.empty((count, len(inc)), np.float32)
+        for k in range(count):
+            state, u = step(state)
+            res[k] = ((u >> np.uint32(9)) | np.uint32(0x3F800000)).view(np.float32) - np.float32(1.0)
+    return res
+
+
+def plane_queries(xy: np.ndarray, albedo: float = 0.5) -> np.ndarray:
+    """SoA queries (16, n) for shading points (x, y, 0) on the receiver z = 0."""
+    n = xy.shape[0]
+    q = np.zeros((QUERY_FIELDS, n), np.float32)
+    q[0], q[1] = xy[:, 0], xy[:, 1]
+    q[5] = 1.0          # n = (0, 0, 1)
+    q[6] = 1.0          # dp_du = (1, 0, 0)
+    q[10] = 1.0         # dp_dv = (0, 1, 0)
+    q[12:15] = albedo
+    q[15] = 1.0         # camera above the receiver
+    return q
+
+
+# ----------------------------------------------------------------- sphere
+def sphere_scene(conductor: bool = False) -> SceneDesc:
+    d = SceneDesc()
+    b = Bsdf(BSDF_CONDUCTOR, 0.2, 3.0) if conductor else Bsdf(BSDF_DIELECTRIC, 1.5)
+    d.add_sphere((0.0, 0.0, 1.5), 1.0, b, SHAPE_CAUSTIC_CASTER_SINGLE)
+    d.add_point_emitter((0.0, 0.0, 5.0), (100.0, 100.0, 100.0), EMITTER_CAUSTIC_SINGLE)
+    return d
+
+
+def sphere_queries(res: int = 64, extent: float = 2.0) -> np.ndarray:
+    c = (np.arange(res, dtype=np.float64) + 0.5) / res * (2 * extent) - extent
+    yy, xx = np.meshgrid(c, c, indexing="ij")
+    xy = np.stack([xx.ravel(), yy.ravel()], axis=1).astype(np.float32)
+    return plane_queries(xy)
+
+
+def sphere_config() -> SMSConfig:
+    return SMSConfig(biased=True, max_trials=16, max_iterations=20, solver_threshold=1e-5)
+
+
+# ------------------------------------------------------------------ water
+def water_params(n_waves: int = 32, seed: int = 2):
+    r = Pcg32(seed, 0)
+    waves = []
+    for _ in range(n_waves):
+        a = 0.002 + (0.02 - 0.002) * r.next_f32()
+        km = 2.0 + (40.0 - 2.0) * r.next_f32()
+        ang = 2.0 * math.pi * r.next_f32()
+        ph = 2.0 * math.pi * r.next_f32()
+        waves.append((a, km * math.cos(ang), km * math.sin(ang), ph))
+    return waves
+
+
+def heightfield_mesh(res: int, extent: float, base: float, waves, flip_normals: bool = False):
+    """Vertex grid res x res over [-extent, extent]^2 with z = base + waves.
+    Returns (P, N, UV, F) with analytic vertex normals and grid uvs."""
+    t = np.linspace(-extent, extent, res, dtype=np.float64)
+    yy, xx = np.meshgrid(t, t, indexing="ij")
+    z = np.full_like(xx, base)
+    zx = np.zeros_like(xx)
+    zy = np.zeros_like(xx)
+    for a, kx, ky, ph in waves:
+        arg = kx * xx + ky * yy + ph
+        z += a * np.sin(arg)
+        c = a * np.cos(arg)
+        zx += c * kx
+        zy += c * ky
+    P = np.stack([xx, yy, z], axis=-1).reshape(-1, 3).astype(np.float32)
+    Nn = np.stack([-zx, -zy, np.ones_like(z)], axis=-1)
+    Nn /= np.linalg.norm(Nn, axis=-1, keepdims=True)
+    if flip_normals:
+        Nn = -Nn
+    N = Nn.reshape(-1, 3).astype(np.float32)
+    u = (xx - xx.min()) / (xx.max() - xx.min())
+    v = (yy - yy.min()) / (yy.max() - yy.min())
+    UV = np.stack([u, v], axis=-1).reshape(-1, 2).astype(np.float32)
+    i, j = np.meshgrid(np.arange(res - 1), np.arange(res - 1), indexing="ij")
+    v00 = (i * res + j).ravel()
+    v10 = v00 + 1
+    v01 = v00 + res
+    v11 = v01 + 1
+    if flip_normals:
+        F = np.concatenate([np.stack([v00, v11, v10], 1), np.stack([v00, v01, v11], 1)])
+    else:
+        F = np.concatenate([np.stack([v00, v10, v11], 1), np.stack([v00, v11, v01], 1)])
+    return P, N, UV, F.astype(np.uint32)
+
+
+def water_scene(res: int = 512, light_radiance: float = 3000.0) -> SceneDesc:
+    d = SceneDesc()
+    P, N, UV, F = heightfield_mesh(res, 1.0, 1.0, water_params())
+    d.add_mesh(P, F, Bsdf(BSDF_DIELECTRIC, 1.33), SHAPE_CAUSTIC_CASTER_SINGLE, N=N, UV=UV)
+    light = d.add_sphere((0.0, 0.0, 10.0), 0.1, Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+    d.add_area_emitter(light, (light_radiance,) * 3, EMITTER_CAUSTIC_SINGLE)
+    return d
+
+
+def water_queries(n: int, seed: int = 3, first: int = 0) -> np.ndarray:
+    u = pcg32_streams_f32(seed, np.arange(first, first + n, dtype=np.uint64), 2)
+    xy = np.stack([2.0 * u[0] - 1.0, 2.0 * u[1] - 1.0], axis=1).astype(np.float32)
+    return plane_queries(xy)
+
+
+def water_config() -> SMSConfig:
+    return SMSConfig(biased=False, max_trials=256, max_iterations=20)

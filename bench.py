@@ -142,7 +142,7 @@ def run_reference(args):
     sms = load_package()
     from sms_gb300 import workloads as W
     cores = os.cpu_count() or 1
-    sample = int(os.environ.get("SMS_REF_SAMPLE", "16384"))
+    sample = int(os.environ.get("SMS_REF_SAMPLE", str(N_QUERIES)))
     vals = []
     for _ in range(args.warmup):
         cpu_baseline_sample(sms, W, 1024, cores)
@@ -278,7 +278,7 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        sample = int(os.environ.get("SMS_CPU_SAMPLE", "16384"))
+        sample = int(os.environ.get("SMS_CPU_SAMPLE", str(N_QUERIES)))
         v, dt, ns = cpu_baseline_sample(sms, W, sample, cores)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"first {ns} of the 1M queries, {dt:.1f} s"}

@@ -187,6 +187,9 @@ typedef struct sms_stats {
     uint64_t rays;          /* rays cast by the connection kernel        */
     uint64_t bvh_nodes;     /* BVH nodes fetched (64 bytes each)         */
     uint64_t tri_tests;     /* triangles fetched (48 bytes each)         */
+    uint64_t speculative_walks; /* Bernoulli trials run past the first
+                                   success of their 32-trial chunk (work the
+                                   sequential reference does not do)       */
 } sms_stats;
 
 sms_status sms_stats_read(sms_ctx *ctx, sms_stats *out);

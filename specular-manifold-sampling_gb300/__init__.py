@@ -73,7 +73,8 @@ class _Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "solver_succeeded", "solver_failed", "bernoulli_trial_calls",
         "bernoulli_trial_iterations", "bernoulli_trial_iterations_max", "walks",
-        "newton_iterations", "connections", "rays", "bvh_nodes", "tri_tests")]
+        "newton_iterations", "connections", "rays", "bvh_nodes", "tri_tests",
+        "speculative_walks")]
 
 
 _LIB = None

@@ -131,6 +131,23 @@ struct Pcg32 {
     SMS_HD float next_f32() {
         return sms_as_float((next_u32() >> 9) | 0x3f800000u) - 1.f;
     }
+    // Skip `delta` outputs in O(log delta): the LCG step x -> a x + c applied
+    // k times is x -> A_k x + C_k, composed by binary powering (Brown 1994,
+    // "Random number generation with arbitrary strides").
+    SMS_HD void advance(uint64_t delta) {
+        uint64_t cur_mult = 6364136223846793005ULL, cur_plus = inc;
+        uint64_t acc_mult = 1u, acc_plus = 0u;
+        while (delta > 0) {
+            if (delta & 1u) {
+                acc_mult *= cur_mult;
+                acc_plus = acc_plus * cur_mult + cur_plus;
+            }
+            cur_plus = (cur_mult + 1u) * cur_plus;
+            cur_mult *= cur_mult;
+            delta >>= 1u;
+        }
+        state = acc_mult * state + acc_plus;
+    }
 };
 
 // --------------------------------------------------------------- scene data
@@ -250,10 +267,10 @@ SMS_HD bool box2(float lox, float loy, float loz, float hix, float hiy, float hi
 }
 
 // Closest hit (any_hit = false) or occlusion test (any_hit = true) against the
-// whole scene.  Returns false and sets *err on stack overflow (treated as miss).
-template <bool kAnyHit>
-SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, Hit &hit,
-                      uint32_t &err) {
+// whole scene; one traversal loop serves both so that lanes of a warp casting
+// different kinds of rays still traverse together.  Returns false and sets *err on stack overflow (treated as miss).
+SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool any_hit, Hit &hit,
+                  uint32_t &err) {
     hit.t = maxt; hit.shape = -1; hit.prim = 0; hit.u = hit.v = 0.f;
     hit.nodes = 0; hit.tests = 0;
     // A NaN origin or direction (a Newton step through a NaN Jacobian, which
@@ -267,7 +284,7 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, Hit &h
         float t;
         if (sphere_hit(sc.sphere[i], o, d, mint, hit.t, t) && (!found || t < hit.t)) {
             hit.t = t; hit.shape = sc.sphere_shape[i]; found = true;
-            if (kAnyHit) return true;
+            if (any_hit) return true;
         }
     }
     if (sc.n_tris == 0) return found;
@@ -307,7 +324,7 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, Hit &h
                     hit.shape = sms_as_int(a.w);
                     hit.prim = (uint32_t)sms_as_int(b.w);
                     found = true;
-                    if (kAnyHit) return true;
+                    if (any_hit) return true;
                 }
             }
         }
@@ -770,8 +787,10 @@ SMS_HD f3 sample_position(const DevScene &sc, const DevShape &s, float sx, float
 // Counters shared by all kernels of a context (one record per context).
 struct DevCounters {
     unsigned long long solver_succeeded, solver_failed, bernoulli_calls, bernoulli_iters,
-        bernoulli_max, walks, newton_iters, connections, rays, bvh_nodes, tri_tests;
-    unsigned int queue_head;   // persistent-kernel work queue
+        bernoulli_max, walks, newton_iters, connections, rays, bvh_nodes, tri_tests, speculative_walks;
+    unsigned int trial_count;  // queries appended to the Bernoulli-trial queue
+    unsigned int trial_head;   // next queue entry (must follow trial_count)
+    unsigned int queue_head;   // general persistent-kernel work queue
     unsigned int error;
 };
 

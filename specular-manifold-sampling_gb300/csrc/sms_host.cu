@@ -275,6 +275,9 @@ struct sms_ctx {
     // device staging for the host-pointer entry points
     void *io = nullptr;
     size_t io_bytes = 0;
+    // per-query scratch of the unbiased estimator
+    void *scratch = nullptr;
+    uint32_t scratch_n = 0;
     std::vector<int> casters_ss;
 };
 
@@ -316,6 +319,7 @@ extern "C" void sms_ctx_destroy(sms_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void *p : c->allocs) cudaFree(p);
     if (c->io) cudaFree(c->io);
+    if (c->scratch) cudaFree(c->scratch);
     if (c->ctr) cudaFree(c->ctr);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -490,6 +494,7 @@ extern "C" sms_status sms_ctx_set_launch(sms_ctx *c, int32_t bps, int32_t tpb) {
     if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
     if (bps < 0 || tpb < 0) return fail(SMS_ERR_INVALID_ARG, "negative launch parameter");
     if (tpb != 0 && tpb != 128) return fail(SMS_ERR_UNSUPPORTED, "threads per block must be 128");
+    if (bps > 64) return fail(SMS_ERR_INVALID_ARG, "blocks per SM too large");
     c->blocks_per_sm = bps;
     return SMS_OK;
 }
@@ -527,6 +532,7 @@ extern "C" sms_status sms_stats_read(sms_ctx *c, sms_stats *out) {
     out->rays = h.rays;
     out->bvh_nodes = h.bvh_nodes;
     out->tri_tests = h.tri_tests;
+    out->speculative_walks = h.speculative_walks;
     return SMS_OK;
 }
 
@@ -538,13 +544,24 @@ extern "C" sms_status sms_stats_reset(sms_ctx *c) {
     return SMS_OK;
 }
 
-static int connect_blocks(sms_ctx *c) {
-    int bps = c->blocks_per_sm;
-    if (bps <= 0) {
-        bps = ss_connect_max_blocks_per_sm();
-        if (bps <= 0) bps = 1;
+static sms_status ensure_scratch(sms_ctx *c, uint32_t n, SsScratch &scr) {
+    if (c->scratch_n < n) {
+        if (c->scratch) {
+            CUDA_TRY(cudaStreamSynchronize(c->stream));
+            cudaFree(c->scratch);
+            c->scratch = nullptr;
+            c->scratch_n = 0;
+        }
+        CUDA_TRY(cudaMalloc(&c->scratch, ss_scratch_bytes(n)));
+        c->scratch_n = n;
     }
-    return bps * c->num_sms;
+    char *b = reinterpret_cast<char *>(c->scratch);
+    size_t cap = c->scratch_n;
+    scr.pos = reinterpret_cast<uint32_t *>(b);
+    scr.dir0 = reinterpret_cast<float *>(b + 4 * cap);
+    scr.val = reinterpret_cast<float *>(b + 16 * cap);
+    scr.list = reinterpret_cast<uint32_t *>(b + 28 * cap);
+    return SMS_OK;
 }
 
 extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
@@ -552,11 +569,14 @@ extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, ui
     if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
         return fail(SMS_ERR_INVALID_ARG, "sms_ss_connect_batch_device: null argument");
     if (n == 0) return SMS_OK;
-    if (c->cfg.biased && c->cfg.max_trials > 0x7fffffff / 2)
-        return fail(SMS_ERR_INVALID_ARG, "max_trials too large");
+    if (c->cfg.biased && c->cfg.max_trials > (1 << 24))
+        return fail(SMS_ERR_INVALID_ARG, "max_trials too large for the biased estimator");
     CUDA_TRY(cudaSetDevice(c->device));
+    SsScratch scr{};
+    if (!c->cfg.biased)
+        if (sms_status st = ensure_scratch(c, n, scr)) return st;
     CUDA_TRY(launch_ss_connect(c->dsc, solver_cfg(c->cfg), q, n, seed, stream_off, out->value, out->count,
-                               out->walks, c->ctr, connect_blocks(c), c->stream));
+                               out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, c->stream));
     return SMS_OK;
 }
 

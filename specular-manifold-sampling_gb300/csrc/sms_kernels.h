@@ -20,18 +20,32 @@ struct SolverCfg {
     float step_scale;
 };
 
-// Unique-solution capacity per query of the biased estimator (per lane, in
-// local memory).  More unique solutions than this set an error flag.
+// Unique-solution capacity per query of the biased estimator (shared memory
+// per lane group).  More unique solutions than this set an error flag.
 constexpr int kMaxSolutions = 64;
 // Bernoulli trials are unbounded in the reference when max_trials <= 0
 // (manifold_ss.cpp:127); the device loop stops here and flags the query.
-constexpr int kTrialHardLimit = 1 << 22;
+constexpr int kTrialHardLimit = 1 << 16;
+// Rows of the per-walk output (sms_ss_walk_batch).
+constexpr int kWalkOutFields = 11;
+
+// Per-query scratch of the unbiased estimator (device memory, n entries):
+// stream position after the walks done so far, first-walk direction and
+// contribution, and the queue of queries that need Bernoulli trials.
+struct SsScratch {
+    uint32_t *pos;    // n
+    float *dir0;      // 3 x n
+    float *val;       // 3 x n
+    uint32_t *list;   // n
+};
+// Bytes of SsScratch for n queries.
+inline size_t ss_scratch_bytes(uint32_t n) { return (size_t)n * (4 + 12 + 12 + 4); }
 
 cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q,
                            const float *w, uint32_t n, float *out, DevCounters *ctr, cudaStream_t s);
 cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n,
                               uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
-                              DevCounters *ctr, int blocks, cudaStream_t s);
-int ss_connect_max_blocks_per_sm();
+                              DevCounters *ctr, const SsScratch &scr, int num_sms, int blocks_per_sm,
+                              cudaStream_t s);
 
 }  // namespace sms

@@ -1,187 +1,203 @@
 // sms_ss.cu -- single-scatter SMS kernels for sm_103a.
 //
-//  ss_walk_kernel     one thread per walk: SpecularManifoldSingleScatter::
-//                     sample_path with an explicit start point
-//                     (src/librender/manifold_ss.cpp:203-279, 329-405).
-//  ss_connect_kernel  persistent kernel: specular_manifold_sampling for a
-//                     wavefront of shading points (manifold_ss.cpp:28-201).
+// Reference: SpecularManifoldSingleScatter (src/librender/manifold_ss.cpp):
+//   specular_manifold_sampling :28-201, sample_path :203-279,
+//   evaluate_path_contribution :281-327, newton_solver :329-405.
 //
-// The connection kernel keeps one query per lane.  Each lane is a small state
-// machine that issues exactly ONE ray per loop iteration (seed ray, Newton
-// reprojection, light visibility or the area-light vertex ray), so the BVH
-// traversal -- the expensive part -- runs converged across the warp whatever
-// phase each lane is in.  When a lane's query is complete it takes the next one
-// from a device work queue (one atomic per warp), so geometric Bernoulli-trial
-// counts and uneven Newton iteration counts never idle a lane.
+// Random-number layout.  Query i draws from one PCG32 stream (seed, stream
+// offset + i) in the reference's order: 3 draws for the emitter sample
+// (manifold.h:204-260: next_1d + next_2d), then exactly 2 draws per walk
+// (sample_path's next_2d for the seed; smooth casters draw nothing else).  Walk
+// m of a query therefore starts at stream position 3 + 2m, and PCG32 jump-ahead
+// lets lanes run the walks of one query side by side while reproducing the
+// reference's sequential draws exactly.
+//
+// Kernels
+//   ss_walk_kernel      one lane per walk (the per-walk harness, p_start).
+//   ss_biased_kernel    biased estimator (:142-197): a group of G lanes (16 or
+//                       32) per query, one walk per lane, then the walk-ordered
+//                       deduplication by warp shuffles.
+//   ss_first_kernel     unbiased estimator, part 1: one lane per query runs the
+//                       first walk, the light visibility test and the
+//                       contribution; queries that need Bernoulli trials are
+//                       appended to a device work queue.
+//   ss_trials_kernel    unbiased estimator, part 2 (:111-135): persistent warps
+//                       take queries from the queue and run the Bernoulli
+//                       trials 32 at a time (lane = trial); the first success is
+//                       found by ballot, so one query's trials never serialize
+//                       on a single lane.
+#include <algorithm>
+
 #include "sms_device.cuh"
 #include "sms_kernels.h"
 
 namespace sms {
 
-// ------------------------------------------------------------ walk kernel
-__global__ void ss_walk_kernel(DevScene sc, SolverCfg cfg, int caster, const float *__restrict__ q,
-                               const float *__restrict__ w, uint32_t n, float *__restrict__ out,
-                               DevCounters *ctr) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+#define SMS_D __device__ __forceinline__
+
+// ------------------------------------------------------------- statistics
+struct LaneStats {
+    unsigned long long succ = 0, fail = 0, calls = 0, iters = 0, imax = 0, walks = 0, newton = 0, conns = 0,
+                       rays = 0, nodes = 0, tris = 0, spec = 0;
+    SMS_D void ray(const Hit &h) {
+        rays++;
+        nodes += h.nodes;
+        tris += h.tests;
+    }
+};
+
+// Warp-aggregated counter update; all 32 lanes must call it.
+SMS_D void flush_stats(const LaneStats &st, DevCounters *ctr, uint32_t err) {
+    unsigned long long v[11] = {st.succ, st.fail, st.calls, st.iters, st.walks, st.newton, st.conns,
+                                st.rays, st.nodes, st.tris, st.spec};
+    unsigned long long *dst[11] = {&ctr->solver_succeeded, &ctr->solver_failed, &ctr->bernoulli_calls,
+                                   &ctr->bernoulli_iters, &ctr->walks, &ctr->newton_iters, &ctr->connections,
+                                   &ctr->rays, &ctr->bvh_nodes, &ctr->tri_tests, &ctr->speculative_walks};
+    const unsigned full = 0xffffffffu;
+    #pragma unroll
+    for (int k = 0; k < 11; ++k) {
+        unsigned long long s = v[k];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(full, s, off);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst[k], s);
+    }
+    unsigned long long m = st.imax;
+    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(full, m, off));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ctr->bernoulli_max, m);
+    unsigned e = err;
+    for (int off = 16; off > 0; off >>= 1) e |= __shfl_xor_sync(full, e, off);
+    if ((threadIdx.x & 31) == 0 && e) atomicOr(&ctr->error, e);
+}
+
+// ------------------------------------------------------------ query / light
+struct Query {
+    f3 x, n, albedo;
+    float cos_i;
+};
+
+SMS_D Query load_query(const float *__restrict__ q, uint32_t n, uint32_t i) {
     auto Q = [&](int k) { return __ldg(q + (size_t)k * n + i); };
-    auto W = [&](int k) { return __ldg(w + (size_t)k * n + i); };
-    f3 x = mk(Q(0), Q(1), Q(2));
-    f3 lp = mk(W(0), W(1), W(2));
-    f3 ps = mk(W(3), W(4), W(5));
-    uint32_t err = 0;
-    const DevShape &cs = sc.shapes[caster];
-    f3 seed = sample_position(sc, cs, W(6), W(7));
-    if (ps.x != 0.f || ps.y != 0.f || ps.z != 0.f) seed = ps;
+    Query r;
+    r.x = mk(Q(0), Q(1), Q(2));
+    r.n = mk(Q(3), Q(4), Q(5));
+    r.albedo = mk(Q(12), Q(13), Q(14));
+    r.cos_i = Q(15);
+    return r;
+}
+
+struct Light {
+    int eidx, kind;   // kind 0 point, 1 area sphere
+    f3 p, w;          // ei.p, ei.weight
+};
+
+// sample_emitter_interaction (manifold.h:204-260): 3 draws.
+SMS_D bool sample_emitter(const DevScene &sc, Pcg32 &rng, f3 x, Light &L) {
+    int ne = sc.n_emitters_ss;
+    if (ne == 0) return false;
+    float es = rng.next_f32();
+    float emitter_pdf = 1.f / (float)ne;
+    uint32_t idx = min((uint32_t)(es * (float)ne), (uint32_t)ne - 1);
+    L.eidx = sc.emitters_ss[idx];
+    const DevEmitter &e = sc.emitters[L.eidx];
+    L.kind = e.kind;
+    float sx = rng.next_f32(), sy = rng.next_f32();
+    f3 spec;
+    if (e.kind == 1) {
+        const DevShape &ls = sc.shapes[e.shape];
+        L.p = sample_position(sc, ls, sx, sy);
+        float pdf = 1.f / (4.f * kPi * ls.radius * ls.radius);
+        spec = mk(e.r / pdf, e.g / pdf, e.b / pdf);
+    } else {
+        L.p = mk(e.px, e.py, e.pz);
+        f3 d = L.p - x;
+        float dist = length(d);
+        float inv = 1.f / dist;
+        spec = mk(e.r, e.g, e.b) * (inv * inv);
+        spec = (spec * dist) * dist;
+    }
+    L.w = spec * (1.f / emitter_pdf);
+    return true;
+}
+
+SMS_D Pcg32 query_rng(uint64_t seed, uint64_t stream, uint64_t position) {
+    Pcg32 r;
+    r.seed(seed, stream);
+    if (position) r.advance(position);
+    return r;
+}
+
+// ------------------------------------------------------------------- walk
+// sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
+// explicit seed point.  Returns ok; v holds the solution vertex.
+SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
+                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr) {
     f3 d = normalize(seed - x);
     Hit h;
-    trace<false>(sc, x, d, kRayEps, INFINITY, h, err);
-    float res[11] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    int it = 0;
-    bool ok = false;
-    if (h.shape >= 0) {
-        // si_init.p
-        Vtx v;
-        vertex_from_hit(sc, x, d, h, v);
-        res[5] = v.p.x; res[6] = v.p.y; res[7] = v.p.z;
-        if (h.shape == caster) {
-            float beta = 1.f;
-            bool accepted = false, conv = false;
-            while (it < cfg.max_iterations) {
-                float c0, c1, dx0, dx1;
-                bool sok = cfg.halfvector ? step_halfvector(x, v, lp, c0, c1, dx0, dx1)
-                                          : step_anglediff(x, v, lp, c0, c1, dx0, dx1);
-                if (!sok) break;
-                if (sqrtf(c0 * c0 + c1 * c1) < cfg.solver_threshold) { conv = true; break; }
-                f3 pp = v.p - (v.dp_du * dx0 + v.dp_dv * dx1) * (cfg.step_scale * beta);
-                f3 dd = normalize(pp - x);
-                Hit hh;
-                trace<false>(sc, x, dd, kRayEps, INFINITY, hh, err);
-                if (hh.shape < 0 || hh.shape != v.shape) {
-                    beta = 0.5f * beta;
-                    it += 1;
-                    accepted = false;
-                    continue;
-                }
-                beta = fminf(1.f, 2.f * beta);
-                vertex_from_hit(sc, x, dd, hh, v);
-                accepted = true;
-                it++;
-            }
-            // si_current must be a valid hit on the walked shape: the last ray
-            // was an accepted reprojection (newton_solver returns si_current).
-            if (conv && accepted) {
-                f3 wx = normalize(x - v.p), wy = normalize(lp - v.p);
-                bool refraction = dot(v.gn, wx) * dot(v.gn, wy) < 0.f;
-                ok = (v.eta == 1.f) ? !refraction : refraction;
-            }
-            if (ok) {
-                res[2] = v.p.x; res[3] = v.p.y; res[4] = v.p.z;
-                res[8] = v.n.x; res[9] = v.n.y; res[10] = v.n.z;
-            }
+    trace(sc, x, d, kRayEps, INFINITY, false, h, err);
+    st.ray(h);
+    it = 0;
+    if (h.shape < 0) return false;
+    vertex_from_hit(sc, x, d, h, v);
+    if (p_init) *p_init = v.p;
+    if (h.shape != caster) return false;
+    float beta = 1.f;
+    bool accepted = false, conv = false;
+    while (it < cfg.max_iterations) {
+        float c0, c1, dx0, dx1;
+        bool sok = cfg.halfvector ? step_halfvector(x, v, lp, c0, c1, dx0, dx1)
+                                  : step_anglediff(x, v, lp, c0, c1, dx0, dx1);
+        if (!sok) break;
+        if (sqrtf(c0 * c0 + c1 * c1) < cfg.solver_threshold) { conv = true; break; }
+        f3 pp = v.p - (v.dp_du * dx0 + v.dp_dv * dx1) * (cfg.step_scale * beta);
+        f3 dd = normalize(pp - x);
+        trace(sc, x, dd, kRayEps, INFINITY, false, h, err);
+        st.ray(h);
+        it++;
+        if (h.shape < 0 || h.shape != v.shape) {
+            beta = 0.5f * beta;
+            accepted = false;
+            continue;
         }
+        beta = fminf(1.f, 2.f * beta);
+        vertex_from_hit(sc, x, dd, h, v);
+        accepted = true;
     }
-    res[0] = ok ? 1.f : 0.f;
-    res[1] = (float)it;
-    #pragma unroll
-    for (int k = 0; k < 11; ++k) out[(size_t)k * n + i] = res[k];
-    if (err) atomicOr(&ctr->error, err);
+    // newton_solver returns si_current: valid only after an accepted step.
+    if (!(conv && accepted)) return false;
+    f3 wx = normalize(x - v.p), wy = normalize(lp - v.p);
+    bool refraction = dot(v.gn, wx) * dot(v.gn, wy) < 0.f;
+    return (v.eta == 1.f) ? !refraction : refraction;
 }
 
-// ------------------------------------------------------- connection kernel
-enum Purpose : int { kNone = 0, kSeed = 1, kReproj = 2, kVis = 3, kEmit = 4 };
-
-struct Lane {
-    // query
-    uint32_t q;
-    f3 x, xn, albedo;
-    float cos_i;
-    // emitter interaction
-    f3 lp, lw;
-    int ekind, eidx;
-    // random numbers
-    Pcg32 rng;
-    // caster loop / estimator
-    int ci, caster;
-    int stage;          // 0 first walk, 1 Bernoulli trial (unbiased); walk index m (biased)
-    int iterations;     // Bernoulli iterations (unbiased)
-    int count, walks;
-    float inv_prob;
-    f3 dir0, val, acc, cur;
-    int n_sol;
-    // walk
-    Vtx v;
-    float beta;
-    int it;
-    bool accepted;
-    // pending ray
-    f3 ro, rd;
-    float rmin, rmax;
-    int purpose;
-};
-
-struct LaneStats {
-    unsigned long long succ, fail, calls, iters, imax, walks, newton, conns, rays, nodes, tris;
-};
-
-__device__ __forceinline__ void begin_walk(const DevScene &sc, Lane &L) {
-    float sx = L.rng.next_f32(), sy = L.rng.next_f32();
-    f3 seed = sample_position(sc, sc.shapes[L.caster], sx, sy);
-    L.ro = L.x;
-    L.rd = normalize(seed - L.x);
-    L.rmin = kRayEps;
-    L.rmax = INFINITY;
-    L.purpose = kSeed;
+// Light-to-solution visibility (manifold_ss.cpp:88-102).
+SMS_D bool visible(const DevScene &sc, f3 lp, f3 p, uint32_t &err, LaneStats &st) {
+    f3 d = p - lp;
+    float dist = length(d);
+    d = d * (1.f / dist);
+    float mint = kRayEps * (1.f + fmaxf(fabsf(lp.x), fmaxf(fabsf(lp.y), fabsf(lp.z))));
+    Hit h;
+    bool occ = trace(sc, lp, d, mint, dist * (1.f - kRayEps), true, h, err);
+    st.ray(h);
+    return !occ;
 }
 
-__device__ __forceinline__ void finish_query(Lane &L, uint32_t n, float *__restrict__ value,
-                                             int *__restrict__ count, int *__restrict__ walks) {
-    value[L.q] = L.acc.x;
-    value[(size_t)n + L.q] = L.acc.y;
-    value[2 * (size_t)n + L.q] = L.acc.z;
-    count[L.q] = L.count;
-    walks[L.q] = L.walks;
-    L.purpose = kNone;
-}
-
-// Start the estimator for caster L.ci, or finish the query.
-__device__ __forceinline__ void begin_caster(const DevScene &sc, const SolverCfg &cfg, Lane &L, uint32_t n,
-                                             float *value, int *count, int *walks) {
-    // A biased estimator with max_trials <= 0 makes no walk (manifold_ss.cpp:146).
-    if (cfg.biased && cfg.max_trials <= 0) L.ci = sc.n_casters_ss;
-    if (L.ci >= sc.n_casters_ss) { finish_query(L, n, value, count, walks); return; }
-    L.caster = sc.casters_ss[L.ci];
-    L.stage = 0;
-    L.cur = splat(0.f);
-    L.n_sol = 0;
-    if (!cfg.biased) L.count = 0;
-    begin_walk(sc, L);
-}
-
-__device__ __forceinline__ void caster_done(const DevScene &sc, const SolverCfg &cfg, Lane &L, uint32_t n,
-                                            float *value, int *count, int *walks) {
-    L.acc = L.acc + L.cur;
-    L.ci++;
-    begin_caster(sc, cfg, L, n, value, count, walks);
-}
-
-// Diffuse receiver eval: albedo / pi * cos_o (both cosines positive).
-__device__ __forceinline__ f3 diffuse_eval(const Lane &L, f3 dir) {
-    float co = dot(dir, L.xn);
-    if (L.cos_i <= 0.f || co <= 0.f) return splat(0.f);
-    return (L.albedo * kInvPi) * co;
-}
-
-// Contribution of the solution in L.v once the emitter vertex is known
-// (evaluate_path_contribution, manifold_ss.cpp:281-327).
-__device__ __forceinline__ f3 contribution(const DevScene &sc, const Lane &L, bool have_y, f3 yp, f3 ydu,
-                                           f3 ydv) {
-    if (!have_y) return splat(0.f);
-    Vtx vt = L.v;
+// evaluate_path_contribution (manifold_ss.cpp:281-327) for a flat receiver.
+SMS_D f3 contribution(const DevScene &sc, f3 x, const Light &L, const Vtx &sol, uint32_t &err, LaneStats &st) {
+    Vtx vt = sol;
     make_orthonormal(vt.dp_du, vt.dp_dv, vt.dn_du, vt.dn_dv);
-    f3 lw = L.lw;
-    f3 lp = L.lp;
-    if (L.ekind == 0) {
+    f3 lw = L.w, lp = L.p, yp, ydu, ydv;
+    if (L.kind == 1) {
+        // emitter vertex by one ray toward the light sample (manifold.h:264-279)
+        f3 d = normalize(lp - vt.p);
+        f3 o = vt.p + d * kShadowEps;
+        Hit h;
+        trace(sc, o, d, kRayEps, INFINITY, false, h, err);
+        st.ray(h);
+        if (h.shape < 0) return splat(0.f);
+        Vtx vy;
+        vertex_from_hit(sc, o, d, h, vy);
+        make_orthonormal(vy.dp_du, vy.dp_dv, vy.dn_du, vy.dn_dv);
+        yp = vy.p; ydu = vy.dp_du; ydv = vy.dp_dv;
+    } else {
         // point light re-sampled from the solution (manifold_ss.cpp:291-312)
         const DevEmitter &e = sc.emitters[L.eidx];
         lp = mk(e.px, e.py, e.pz);
@@ -192,347 +208,351 @@ __device__ __forceinline__ f3 contribution(const DevScene &sc, const Lane &L, bo
         f3 spec = mk(e.r, e.g, e.b) * (inv * inv);
         lw = (spec * dist) * dist;
         lw = lw * (1.f / emitter_pdf);
+        yp = lp;
+        onb(normalize(vt.p - lp), ydu, ydv);
     }
     float F = specular_reflectance(sc.shapes[vt.shape], vt.n, normalize(lp - vt.p));
-    F *= geometric_term(L.x, vt, yp, ydu, ydv);
+    F *= geometric_term(x, vt, yp, ydu, ydv);
     return lw * F;
 }
 
-__device__ __forceinline__ void after_contribution(const DevScene &sc, const SolverCfg &cfg, Lane &L, f3 spec,
-                                                   LaneStats &st, uint32_t n, float *value, int *count,
-                                                   int *walks) {
-    f3 dir = normalize(L.v.p - L.x);
-    f3 bsdf = diffuse_eval(L, dir);
-    if (!cfg.biased) {
-        L.val = bsdf * spec;
-        L.inv_prob = 1.f;
-        L.iterations = 1;
-        L.stage = 1;
-        st.calls++;
-        begin_walk(sc, L);
-    } else {
-        L.cur = L.cur + bsdf * spec;
-        L.count++;
-        L.stage++;
-        if (L.stage >= cfg.max_trials) caster_done(sc, cfg, L, n, value, count, walks);
-        else begin_walk(sc, L);
-    }
+// Diffuse receiver (src/bsdfs/diffuse.cpp): albedo / pi * cos_o.
+SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
+    float co = dot(dir, Q.n);
+    if (Q.cos_i <= 0.f || co <= 0.f) return splat(0.f);
+    return (Q.albedo * kInvPi) * co;
 }
 
-// Emitter vertex for the contribution: point lights directly, area lights by
-// one ray toward the sampled light point (manifold.h:264-302).
-__device__ __forceinline__ void start_contribution(const DevScene &sc, const SolverCfg &cfg, Lane &L,
-                                                   LaneStats &st, uint32_t n, float *value, int *count,
-                                                   int *walks) {
-    if (L.ekind == 1) {
-        f3 d = normalize(L.lp - L.v.p);
-        L.ro = L.v.p + d * kShadowEps;
-        L.rd = d;
-        L.rmin = kRayEps;
-        L.rmax = INFINITY;
-        L.purpose = kEmit;
-        return;
-    }
-    const DevEmitter &e = sc.emitters[L.eidx];
-    f3 ep = mk(e.px, e.py, e.pz);
-    f3 d = normalize(L.v.p - ep);
-    f3 du, dv;
-    onb(d, du, dv);
-    f3 spec = contribution(sc, L, true, ep, du, dv);
-    after_contribution(sc, cfg, L, spec, st, n, value, count, walks);
-}
-
-__device__ __forceinline__ void after_visibility(const DevScene &sc, const SolverCfg &cfg, Lane &L, bool vis,
-                                                 LaneStats &st, f3 *sol, uint32_t n, float *value,
-                                                 int *count, int *walks, uint32_t &err) {
-    if (!cfg.biased) {
-        if (!vis) { caster_done(sc, cfg, L, n, value, count, walks); return; }
-        start_contribution(sc, cfg, L, st, n, value, count, walks);
-        return;
-    }
-    if (vis) {
-        f3 dir = normalize(L.v.p - L.x);
-        bool dup = false;
-        for (int k = 0; k < L.n_sol; ++k)
-            if (fabsf(dot(dir, sol[k]) - 1.f) < cfg.uniqueness_threshold) { dup = true; break; }
-        if (!dup) {
-            if (L.n_sol < kMaxSolutions) {
-                sol[L.n_sol++] = dir;
-                start_contribution(sc, cfg, L, st, n, value, count, walks);
-                return;
-            }
-            err |= kErrSolutionOverflow;
-        }
-    }
-    L.stage++;
-    if (L.stage >= cfg.max_trials) caster_done(sc, cfg, L, n, value, count, walks);
-    else begin_walk(sc, L);
-}
-
-// A walk ended (converged or failed): advance the estimator.
-__device__ __forceinline__ void walk_done(const DevScene &sc, const SolverCfg &cfg, Lane &L, bool ok,
-                                          LaneStats &st, f3 *sol, uint32_t n, float *value, int *count,
-                                          int *walks, uint32_t &err) {
-    L.walks++;
-    st.walks++;
-    st.newton += (unsigned long long)L.it;
-    if (!cfg.biased && L.stage == 1) {
-        // Bernoulli trial (manifold_ss.cpp:115-135)
-        if (ok && fabsf(dot(L.dir0, normalize(L.v.p - L.x)) - 1.f) < cfg.uniqueness_threshold) {
-            L.cur = L.val * L.inv_prob;
-            L.count = L.iterations;
-            st.iters += (unsigned long long)L.iterations;
-            st.imax = max(st.imax, (unsigned long long)L.iterations);
-            caster_done(sc, cfg, L, n, value, count, walks);
-            return;
-        }
-        L.inv_prob += 1.f;
-        L.iterations++;
-        bool capped = cfg.max_trials > 0 && L.iterations > cfg.max_trials;
-        bool limit = cfg.max_trials <= 0 && L.iterations > kTrialHardLimit;
-        if (capped || limit) {
-            if (limit) err |= kErrTrialLimit;
-            L.inv_prob = 0.f;
-            L.cur = L.val * 0.f;
-            L.count = -1;
-            st.iters += (unsigned long long)L.iterations;
-            st.imax = max(st.imax, (unsigned long long)L.iterations);
-            caster_done(sc, cfg, L, n, value, count, walks);
-            return;
-        }
-        begin_walk(sc, L);
-        return;
-    }
-    if (!ok) {
-        st.fail++;
-        if (!cfg.biased) { caster_done(sc, cfg, L, n, value, count, walks); return; }
-        L.stage++;
-        if (L.stage >= cfg.max_trials) caster_done(sc, cfg, L, n, value, count, walks);
-        else begin_walk(sc, L);
-        return;
-    }
-    st.succ++;
-    if (!cfg.biased) L.dir0 = normalize(L.v.p - L.x);
-    // visibility between the light and the solution (manifold_ss.cpp:88-102)
-    f3 d = L.v.p - L.lp;
-    float dist = length(d);
-    d = d * (1.f / dist);
-    L.ro = L.lp;
-    L.rd = d;
-    L.rmin = kRayEps * (1.f + fmaxf(fabsf(L.lp.x), fmaxf(fabsf(L.lp.y), fabsf(L.lp.z))));
-    L.rmax = dist * (1.f - kRayEps);
-    L.purpose = kVis;
-    (void)sol; (void)err;
-}
-
-// One Newton iteration on the current vertex: converge, fail, or propose a
-// reprojection ray (manifold_ss.cpp:344-384).
-__device__ __forceinline__ void newton_advance(const DevScene &sc, const SolverCfg &cfg, Lane &L,
-                                               LaneStats &st, f3 *sol, uint32_t n, float *value,
-                                               int *count, int *walks, uint32_t &err) {
-    bool fail = L.it >= cfg.max_iterations;
-    float c0 = 0.f, c1 = 0.f, dx0 = 0.f, dx1 = 0.f;
-    if (!fail) {
-        bool ok = cfg.halfvector ? step_halfvector(L.x, L.v, L.lp, c0, c1, dx0, dx1)
-                                 : step_anglediff(L.x, L.v, L.lp, c0, c1, dx0, dx1);
-        fail = !ok;
-    }
-    if (fail) { walk_done(sc, cfg, L, false, st, sol, n, value, count, walks, err); return; }
-    if (sqrtf(c0 * c0 + c1 * c1) < cfg.solver_threshold) {
-        bool ok = L.accepted;
-        if (ok) {
-            f3 wx = normalize(L.x - L.v.p), wy = normalize(L.lp - L.v.p);
-            bool refraction = dot(L.v.gn, wx) * dot(L.v.gn, wy) < 0.f;
-            ok = (L.v.eta == 1.f) ? !refraction : refraction;
-        }
-        walk_done(sc, cfg, L, ok, st, sol, n, value, count, walks, err);
-        return;
-    }
-    f3 pp = L.v.p - (L.v.dp_du * dx0 + L.v.dp_dv * dx1) * (cfg.step_scale * L.beta);
-    L.ro = L.x;
-    L.rd = normalize(pp - L.x);
-    L.rmin = kRayEps;
-    L.rmax = INFINITY;
-    L.purpose = kReproj;
-}
-
-__device__ __forceinline__ void begin_query(const DevScene &sc, const SolverCfg &cfg, Lane &L, uint32_t qi,
-                                            const float *__restrict__ qs, uint32_t n, uint64_t seed,
-                                            uint64_t stream_off, LaneStats &st, float *value, int *count,
-                                            int *walks) {
-    L.q = qi;
-    auto Q = [&](int k) { return __ldg(qs + (size_t)k * n + qi); };
-    L.x = mk(Q(0), Q(1), Q(2));
-    L.xn = mk(Q(3), Q(4), Q(5));
-    L.albedo = mk(Q(12), Q(13), Q(14));
-    L.cos_i = Q(15);
-    L.rng.seed(seed, (uint64_t)qi + stream_off);
-    L.acc = splat(0.f);
-    L.count = 0;
-    L.walks = 0;
-    L.ci = 0;
-    // sample_emitter_interaction (manifold.h:204-260)
-    int ne = sc.n_emitters_ss;
-    if (ne == 0 || sc.n_casters_ss == 0) { finish_query(L, n, value, count, walks); return; }
-    float es = L.rng.next_f32();
-    float emitter_pdf = 1.f / (float)ne;
-    uint32_t idx = min((uint32_t)(es * (float)ne), (uint32_t)ne - 1);
-    L.eidx = sc.emitters_ss[idx];
-    const DevEmitter &e = sc.emitters[L.eidx];
-    L.ekind = e.kind;
-    float sx = L.rng.next_f32(), sy = L.rng.next_f32();
-    f3 spec;
-    if (e.kind == 1) {
-        const DevShape &ls = sc.shapes[e.shape];
-        L.lp = sample_position(sc, ls, sx, sy);
-        float pdf = 1.f / (4.f * kPi * ls.radius * ls.radius);
-        spec = mk(e.r / pdf, e.g / pdf, e.b / pdf);
-    } else {
-        L.lp = mk(e.px, e.py, e.pz);
-        f3 d = L.lp - L.x;
-        float dist = length(d);
-        float inv = 1.f / dist;
-        spec = mk(e.r, e.g, e.b) * (inv * inv);
-        spec = (spec * dist) * dist;
-    }
-    L.lw = spec * (1.f / emitter_pdf);
-    st.conns++;
-    begin_caster(sc, cfg, L, n, value, count, walks);
-}
-
-// Warp-aggregated counter update; every lane of the warp must call it.
-__device__ __forceinline__ void flush_stats(LaneStats &st, DevCounters *ctr, uint32_t err) {
-    unsigned long long v[10] = {st.succ, st.fail, st.calls, st.iters, st.walks, st.newton, st.conns,
-                                st.rays, st.nodes, st.tris};
-    unsigned long long *dst[10] = {&ctr->solver_succeeded, &ctr->solver_failed, &ctr->bernoulli_calls,
-                                   &ctr->bernoulli_iters, &ctr->walks, &ctr->newton_iters, &ctr->connections,
-                                   &ctr->rays, &ctr->bvh_nodes, &ctr->tri_tests};
-    __syncwarp();
-    const unsigned mask = 0xffffffffu;
-    #pragma unroll
-    for (int k = 0; k < 10; ++k) {
-        unsigned long long s = v[k];
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(mask, s, off);
-        if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst[k], s);
-    }
-    unsigned long long m = st.imax;
-    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(mask, m, off));
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ctr->bernoulli_max, m);
-    if (err) atomicOr(&ctr->error, err);
-}
-
-__global__ void __launch_bounds__(128) ss_connect_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
-                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
-                                                         float *__restrict__ value, int *__restrict__ count,
-                                                         int *__restrict__ walks, DevCounters *ctr) {
-    Lane L;
-    L.purpose = kNone;
-    LaneStats st = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+// ------------------------------------------------------------ walk kernel
+__global__ void __launch_bounds__(128) ss_walk_kernel(DevScene sc, SolverCfg cfg, int caster,
+                                                      const float *__restrict__ q, const float *__restrict__ w,
+                                                      uint32_t n, float *__restrict__ out, DevCounters *ctr) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    LaneStats st;
     uint32_t err = 0;
-    f3 sol[kMaxSolutions];
-    bool exhausted = false;
+    if (i < n) {
+        auto Q = [&](int k) { return __ldg(q + (size_t)k * n + i); };
+        auto W = [&](int k) { return __ldg(w + (size_t)k * n + i); };
+        f3 x = mk(Q(0), Q(1), Q(2));
+        f3 lp = mk(W(0), W(1), W(2));
+        f3 ps = mk(W(3), W(4), W(5));
+        f3 seed = sample_position(sc, sc.shapes[caster], W(6), W(7));
+        if (ps.x != 0.f || ps.y != 0.f || ps.z != 0.f) seed = ps;
+        Vtx v;
+        int it = 0;
+        f3 pi = splat(0.f);
+        bool ok = ss_walk(sc, cfg, caster, x, lp, seed, v, it, err, st, &pi);
+        float res[kWalkOutFields] = {ok ? 1.f : 0.f, (float)it, 0.f, 0.f, 0.f, pi.x, pi.y, pi.z, 0.f, 0.f, 0.f};
+        if (ok) {
+            res[2] = v.p.x; res[3] = v.p.y; res[4] = v.p.z;
+            res[8] = v.n.x; res[9] = v.n.y; res[10] = v.n.z;
+        }
+        #pragma unroll
+        for (int k = 0; k < kWalkOutFields; ++k) out[(size_t)k * n + i] = res[k];
+    }
+    flush_stats(st, ctr, err);
+}
+
+// ------------------------------------------------------ biased estimator
+// Group of G lanes per query; walk m of caster c sits at stream position
+// 3 + 2 (c M + m).  Contributions are summed in walk order over the first
+// occurrences of each solution direction, exactly as manifold_ss.cpp:146-196.
+template <int G>
+__global__ void __launch_bounds__(128) ss_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
+                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
+                                                        float *__restrict__ value, int *__restrict__ count,
+                                                        int *__restrict__ walks, DevCounters *ctr) {
+    constexpr int kGroupsPerBlock = 128 / G;
+    __shared__ f3 rec[kGroupsPerBlock][kMaxSolutions];
+    const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31;
-    while (true) {
-        // ---- refill idle lanes from the work queue (one atomic per warp)
-        bool need = L.purpose == kNone && !exhausted;
-        unsigned act = __activemask();
-        unsigned want = __ballot_sync(act, need);
-        if (want) {
-            unsigned leader = __ffs(want) - 1;
-            unsigned base = 0;
-            if (lane == leader) base = atomicAdd(&ctr->queue_head, (unsigned)__popc(want));
-            base = __shfl_sync(act, base, leader);
-            if (need) {
-                unsigned qi = base + __popc(want & ((1u << lane) - 1u));
-                if (qi >= n) exhausted = true;
-                else begin_query(sc, cfg, L, qi, qs, n, seed, stream_off, st, value, count, walks);
+    const int gl = (int)(threadIdx.x % G);             // lane within group
+    const int gib = (int)(threadIdx.x / G);            // group within block
+    const int gbase = (int)(lane & ~(unsigned)(G - 1));
+    const unsigned gmask = (G == 32) ? full : (((1u << G) - 1u) << gbase);
+    LaneStats st;
+    uint32_t err = 0;
+    const int M = cfg.max_trials > 0 ? cfg.max_trials : 0;
+    const uint32_t groups_total = gridDim.x * kGroupsPerBlock;
+    // every group of the grid runs the same number of rounds (full-warp syncs)
+    const uint32_t rounds = (n + groups_total - 1) / groups_total;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        uint32_t qi = (r * gridDim.x + blockIdx.x) * kGroupsPerBlock + gib;
+        bool live = qi < n;
+        Query Q{};
+        Light L{};
+        bool have_light = false;
+        if (live) {
+            Q = load_query(qs, n, qi);
+            Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+            have_light = sample_emitter(sc, rng, Q.x, L);
+        }
+        bool work = live && have_light && sc.n_casters_ss > 0;
+        if (work && gl == 0) st.conns++;
+        f3 acc = splat(0.f);
+        int n_unique = 0;
+        for (int c = 0; c < sc.n_casters_ss; ++c) {
+            int caster = sc.casters_ss[c];
+            int nrec = 0;
+            f3 cur = splat(0.f);
+            for (int m0 = 0; m0 < M; m0 += G) {
+                int m = m0 + gl;
+                bool cand = false;
+                f3 dir = splat(0.f), contrib = splat(0.f);
+                if (work && m < M) {
+                    Pcg32 rng = query_rng(seed, stream_off + qi, 3u + 2u * ((uint64_t)c * M + m));
+                    float sx = rng.next_f32(), sy = rng.next_f32();
+                    f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
+                    Vtx v;
+                    int it;
+                    bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
+                    st.walks++;
+                    st.newton += (unsigned)it;
+                    if (ok) {
+                        st.succ++;
+                        if (visible(sc, L.p, v.p, err, st)) {
+                            cand = true;
+                            dir = normalize(v.p - Q.x);
+                            // evaluated for every visible solution; only first
+                            // occurrences are kept below
+                            contrib = diffuse_eval(Q, dir) * contribution(sc, Q.x, L, v, err, st);
+                        }
+                    } else {
+                        st.fail++;
+                    }
+                }
+                // walk-ordered deduplication within the group
+                for (int k = 0; k < G; ++k) {
+                    const int src = gbase + k;
+                    bool ck = __shfl_sync(full, cand, src);
+                    f3 dk = mk(__shfl_sync(full, dir.x, src), __shfl_sync(full, dir.y, src),
+                               __shfl_sync(full, dir.z, src));
+                    f3 vk = mk(__shfl_sync(full, contrib.x, src), __shfl_sync(full, contrib.y, src),
+                               __shfl_sync(full, contrib.z, src));
+                    bool dup = false;
+                    if (ck)
+                        for (int j = gl; j < nrec; j += G)
+                            if (fabsf(dot(dk, rec[gib][j]) - 1.f) < cfg.uniqueness_threshold) dup = true;
+                    unsigned anydup = __ballot_sync(full, dup) & gmask;
+                    __syncwarp();
+                    if (ck && !anydup) {
+                        if (nrec < kMaxSolutions) {
+                            if (gl == 0) rec[gib][nrec] = dk;
+                            nrec++;
+                            cur = cur + vk;
+                        } else {
+                            err |= kErrSolutionOverflow;
+                        }
+                    }
+                    __syncwarp();
+                }
             }
+            acc = acc + cur;
+            n_unique += nrec;
         }
-        if (L.purpose == kNone) {
-            if (exhausted) break;
-            continue;
+        if (live && gl == 0) {
+            value[qi] = acc.x;
+            value[(size_t)n + qi] = acc.y;
+            value[2 * (size_t)n + qi] = acc.z;
+            count[qi] = n_unique;
+            walks[qi] = work ? M * sc.n_casters_ss : 0;
         }
-        // ---- one ray per lane
-        Hit h;
-        bool any;
-        if (L.purpose == kVis) {
-            any = trace<true>(sc, L.ro, L.rd, L.rmin, L.rmax, h, err);
+    }
+    flush_stats(st, ctr, err);
+}
+
+// --------------------------------------------------- unbiased: first walks
+__global__ void __launch_bounds__(128) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+                                                       uint32_t n, uint64_t seed, uint64_t stream_off,
+                                                       float *__restrict__ value, int *__restrict__ count,
+                                                       int *__restrict__ walks, SsScratch scr, DevCounters *ctr) {
+    uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    LaneStats st;
+    uint32_t err = 0;
+    bool enqueue = false;
+    if (qi < n) {
+        Query Q = load_query(qs, n, qi);
+        Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+        Light L;
+        bool have_light = sample_emitter(sc, rng, Q.x, L);
+        uint32_t pos = 3u;
+        f3 acc = splat(0.f);
+        int nw = 0;
+        if (c == 0) {
+            if (have_light) st.conns++;
         } else {
-            any = trace<false>(sc, L.ro, L.rd, L.rmin, L.rmax, h, err);
+            pos = scr.pos[qi];
+            acc = mk(value[qi], value[(size_t)n + qi], value[2 * (size_t)n + qi]);
+            nw = walks[qi];
         }
-        st.rays++;
-        st.nodes += h.nodes;
-        st.tris += h.tests;
-        // ---- consume
-        switch (L.purpose) {
-        case kSeed:
-            if (any && h.shape == L.caster) {
-                vertex_from_hit(sc, L.ro, L.rd, h, L.v);
-                L.it = 0;
-                L.beta = 1.f;
-                L.accepted = false;
-                newton_advance(sc, cfg, L, st, sol, n, value, count, walks, err);
+        if (have_light) {
+            int caster = sc.casters_ss[c];
+            rng.advance(pos - 3u);
+            float sx = rng.next_f32(), sy = rng.next_f32();
+            pos += 2u;
+            f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
+            Vtx v;
+            int it;
+            bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
+            st.walks++;
+            st.newton += (unsigned)it;
+            nw++;
+            if (ok) {
+                st.succ++;
+                if (visible(sc, L.p, v.p, err, st)) {
+                    f3 dir = normalize(v.p - Q.x);
+                    f3 spec = contribution(sc, Q.x, L, v, err, st);
+                    f3 val = diffuse_eval(Q, dir) * spec;
+                    scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;
+                    scr.val[qi] = val.x; scr.val[(size_t)n + qi] = val.y; scr.val[2 * (size_t)n + qi] = val.z;
+                    enqueue = true;
+                }
             } else {
-                L.it = 0;
-                walk_done(sc, cfg, L, false, st, sol, n, value, count, walks, err);
+                st.fail++;
             }
-            break;
-        case kReproj:
-            if (!any || h.shape != L.v.shape) {
-                L.beta = 0.5f * L.beta;
-                L.accepted = false;
-            } else {
-                L.beta = fminf(1.f, 2.f * L.beta);
-                vertex_from_hit(sc, L.ro, L.rd, h, L.v);
-                L.accepted = true;
-            }
-            L.it++;
-            newton_advance(sc, cfg, L, st, sol, n, value, count, walks, err);
-            break;
-        case kVis:
-            after_visibility(sc, cfg, L, !any, st, sol, n, value, count, walks, err);
-            break;
-        case kEmit: {
-            f3 spec = splat(0.f);
-            if (any) {
-                Vtx vy;
-                vertex_from_hit(sc, L.ro, L.rd, h, vy);
-                make_orthonormal(vy.dp_du, vy.dp_dv, vy.dn_du, vy.dn_dv);
-                spec = contribution(sc, L, true, vy.p, vy.dp_du, vy.dp_dv);
-            }
-            after_contribution(sc, cfg, L, spec, st, n, value, count, walks);
-            break;
         }
-        default:
-            break;
+        scr.pos[qi] = pos;
+        value[qi] = acc.x;
+        value[(size_t)n + qi] = acc.y;
+        value[2 * (size_t)n + qi] = acc.z;
+        count[qi] = 0;
+        walks[qi] = nw;
+    }
+    // warp-aggregated append to the trial queue
+    unsigned want = __ballot_sync(0xffffffffu, enqueue);
+    if (want) {
+        unsigned lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(&ctr->trial_count, (unsigned)__popc(want));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (enqueue) scr.list[base + __popc(want & ((1u << lane) - 1u))] = qi;
+    }
+    flush_stats(st, ctr, err);
+}
+
+// ------------------------------------------------ unbiased: Bernoulli trials
+// Persistent warps.  For query q with first-walk direction dir0 the trials are
+// t = 1, 2, ...; trial t draws stream positions pos + 2(t-1) and the next one.
+// The warp runs trials 32 at a time and keeps the first success
+// (manifold_ss.cpp:115-135).
+__global__ void __launch_bounds__(128) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
+                                                        float *__restrict__ value, int *__restrict__ count,
+                                                        int *__restrict__ walks, SsScratch scr, DevCounters *ctr) {
+    const unsigned full = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31;
+    LaneStats st;
+    uint32_t err = 0;
+    const int cap = cfg.max_trials > 0 ? cfg.max_trials : kTrialHardLimit;
+    const int caster = sc.casters_ss[c];
+    const unsigned n_list = *(volatile unsigned *)&ctr->trial_count;
+    while (true) {
+        unsigned idx = 0;
+        if (lane == 0) idx = atomicAdd(&ctr->trial_head, 1u);
+        idx = __shfl_sync(full, idx, 0);
+        if (idx >= n_list) break;
+        uint32_t qi = scr.list[idx];
+        Query Q = load_query(qs, n, qi);
+        Pcg32 base = query_rng(seed, stream_off + qi, 0);
+        Light L;
+        sample_emitter(sc, base, Q.x, L);   // base now sits at position 3
+        uint32_t pos = scr.pos[qi];
+        f3 dir0 = mk(scr.dir0[qi], scr.dir0[(size_t)n + qi], scr.dir0[2 * (size_t)n + qi]);
+        int first = 0;   // 1-based index of the first successful trial
+        for (int t0 = 1; t0 <= cap; t0 += 32) {
+            int t = t0 + (int)lane;
+            bool succ = false;
+            int it = 0;
+            if (t <= cap) {
+                Pcg32 rng = base;
+                rng.advance((uint64_t)(pos - 3u) + 2u * (uint64_t)(t - 1));
+                float sx = rng.next_f32(), sy = rng.next_f32();
+                f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
+                Vtx v;
+                succ = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st) &&
+                       fabsf(dot(dir0, normalize(v.p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
+            }
+            unsigned b = __ballot_sync(full, succ);
+            int f = b ? t0 + __ffs(b) - 1 : 0x7fffffff;
+            // trials up to the first success are the reference's walks; the
+            // rest of the chunk is speculative work
+            if (t <= cap) {
+                if (t <= f) { st.walks++; st.newton += (unsigned)it; }
+                else st.spec++;
+            }
+            if (b) { first = f; break; }
+        }
+        if (lane == 0) {
+            float inv_prob;
+            int iterations, trial_walks;
+            if (first) {
+                iterations = first;
+                inv_prob = (float)first;
+                trial_walks = first;
+            } else {
+                iterations = cap + 1;
+                inv_prob = 0.f;
+                trial_walks = cap;
+                if (cfg.max_trials <= 0) err |= kErrTrialLimit;
+            }
+            f3 val = mk(scr.val[qi], scr.val[(size_t)n + qi], scr.val[2 * (size_t)n + qi]);
+            f3 cur = val * inv_prob;
+            value[qi] += cur.x;
+            value[(size_t)n + qi] += cur.y;
+            value[2 * (size_t)n + qi] += cur.z;
+            count[qi] = first ? iterations : -1;
+            walks[qi] += trial_walks;
+            scr.pos[qi] = pos + 2u * (uint32_t)trial_walks;
+            st.calls++;
+            st.iters += (unsigned long long)iterations;
+            st.imax = max(st.imax, (unsigned long long)iterations);
         }
     }
     flush_stats(st, ctr, err);
 }
 
 // ---------------------------------------------------------------- launchers
-cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q,
-                           const float *w, uint32_t n, float *out, DevCounters *ctr, cudaStream_t s) {
+cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q, const float *w,
+                           uint32_t n, float *out, DevCounters *ctr, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    dim3 block(128), grid((n + 127) / 128);
-    ss_walk_kernel<<<grid, block, 0, s>>>(sc, cfg, caster, q, w, n, out, ctr);
+    ss_walk_kernel<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, caster, q, w, n, out, ctr);
     return cudaGetLastError();
 }
 
-cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n,
-                              uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
-                              DevCounters *ctr, int blocks, cudaStream_t s) {
+cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
+                              uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
+                              const SsScratch &scr, int num_sms, int blocks_per_sm, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(&ctr->queue_head, 0, sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
-    ss_connect_kernel<<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
-    return cudaGetLastError();
-}
-
-int ss_connect_max_blocks_per_sm() {
-    int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ss_connect_kernel, 128, 0);
-    return b;
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 8;
+    if (cfg.biased) {
+        const int G = cfg.max_trials <= 16 ? 16 : 32;
+        const uint32_t groups_per_block = 128 / G;
+        uint32_t blocks_needed = (n + groups_per_block - 1) / groups_per_block;
+        uint32_t blocks = std::min<uint32_t>(blocks_needed, (uint32_t)(num_sms * bps));
+        if (G == 16) ss_biased_kernel<16><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
+        else ss_biased_kernel<32><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
+        return cudaGetLastError();
+    }
+    if (sc.n_casters_ss == 0) {
+        // no caster: every query gets zero (manifold_ss.cpp:53-55)
+        cudaError_t e = cudaMemsetAsync(value, 0, 3 * (size_t)n * sizeof(float), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, (size_t)n * sizeof(int), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(walks, 0, (size_t)n * sizeof(int), s);
+        return e;
+    }
+    for (int c = 0; c < sc.n_casters_ss; ++c) {
+        cudaError_t e = cudaMemsetAsync(&ctr->trial_count, 0, 2 * sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+        ss_first_kernel<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks,
+                                                        scr, ctr);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        ss_trials_kernel<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks,
+                                                       scr, ctr);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace sms

@@ -95,11 +95,18 @@ def test_water_walks_within_chaos_floor(sms, workloads, oracle, gpu_lib, res):
     assert abs(out_g[1].mean() - out_o[1].mean()) < 0.2
 
 
-def _connect_diff(vg, cg, wg, vo, co, wo):
-    agree = (cg == co) & (wg == wo)
-    big = agree[None, :] & (np.abs(vo) > 1e-6)
-    rel = np.abs(vg - vo)[big] / np.abs(vo)[big]
-    return float(np.mean(cg != co)), float(rel.max()) if rel.size else 0.0
+def _connect_diff(va, ca, wa, vb, cb, wb, rtol=1e-3):
+    """(count mismatch fraction, fraction of queries whose estimate differs --
+    count, walk count or value beyond rtol -- and the median relative value
+    error over queries that agree)."""
+    same_cw = (ca == cb) & (wa == wb)
+    scale = np.maximum(np.abs(vb).max(axis=0), 1e-6)
+    rel = (np.abs(va - vb).max(axis=0) / scale)
+    nonzero = np.abs(vb).max(axis=0) > 1e-6
+    differs = ~same_cw | (nonzero & (rel > rtol))
+    agree = same_cw & nonzero & (rel <= rtol)
+    med = float(np.median(rel[agree])) if agree.any() else 0.0
+    return float(np.mean(ca != cb)), float(np.mean(differs)), med
 
 
 @pytest.mark.parametrize("conductor", [False, True])
@@ -112,18 +119,22 @@ def test_sphere_connect_biased(sms, workloads, oracle, gpu_lib, conductor):
     q = W.sphere_queries(64)   # the full 64x64 benchmark grid
     vg, cg, wg = ss.specular_manifold_sampling(q, seed=1)
     vo, co, wo, st_o = oracle.OracleScene(desc).connect_batch(cfg, q, seed=1)
-    cm, rel = _connect_diff(vg, cg, wg, vo, co, wo)
-    print(f"sphere biased conductor={conductor}: count mismatch {cm:.5f} max rel {rel:.2e} "
-          f"unique {co.sum()} vs {cg.sum()}")
+    vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=1)
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    print(f"sphere biased conductor={conductor}: count mismatch {g_cm:.5f} differs {g_diff:.5f} "
+          f"(floor {f_cm:.5f}/{f_diff:.5f}) median rel {g_med:.1e} unique {co.sum()} vs {cg.sum()}")
     assert np.all(wg == 16) and np.all(wo == 16)
-    assert cm < STRICT_MISMATCH
-    assert rel < VALUE_RTOL
+    assert g_cm < STRICT_MISMATCH
+    assert g_diff <= FLOOR_FACTOR * f_diff + STRICT_MISMATCH
+    assert g_med < 1e-4
     st = ctx.stats()
     assert st["walks"] == st_o["walks"] == 16 * q.shape[1]
     assert st["connections"] == q.shape[1]
     assert abs(st["solver_succeeded"] - st_o["solver_succeeded"]) <= 0.005 * st_o["solver_succeeded"] + 2
     if conductor:
         assert co.sum() > 100 and vo.sum() > 0
+        assert abs(vg.sum() - vo.sum()) <= 0.01 * vo.sum()
 
 
 def test_water_connect_unbiased(sms, workloads, oracle, gpu_lib):
@@ -137,11 +148,13 @@ def test_water_connect_unbiased(sms, workloads, oracle, gpu_lib):
     vg, cg, wg = ss.specular_manifold_sampling(q, seed=5)
     vo, co, wo, _ = oracle.OracleScene(desc).connect_batch(cfg, q, seed=5)
     vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=5)
-    g_cm, g_rel = _connect_diff(vg, cg, wg, vo, co, wo)
-    f_cm, _ = _connect_diff(vf, cf, wf, vo, co, wo)
-    print(f"water unbiased: gpu count mismatch {g_cm:.4f} (floor {f_cm:.4f}), max rel {g_rel:.2e}")
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    print(f"water unbiased: gpu count mismatch {g_cm:.4f} differs {g_diff:.4f} "
+          f"(floor {f_cm:.4f}/{f_diff:.4f}) median rel {g_med:.1e}")
     assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
-    assert g_rel < VALUE_RTOL
+    assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+    assert g_med < 1e-4
     # identical outcome classes in distribution
     for cls in (lambda c: c == 0, lambda c: c == -1, lambda c: c > 0):
         assert abs(cls(cg).mean() - cls(co).mean()) <= 2 * abs(cls(cf).mean() - cls(co).mean()) + 0.01

@@ -193,7 +193,32 @@ typedef struct sms_stats {
 } sms_stats;
 
 sms_status sms_stats_read(sms_ctx *ctx, sms_stats *out);
-sms_status sms_stats_reset(sms_ctx *ctx);
+sms_status sms_stats_reset(sms_ctx *ctx);   /* also clears the profile */
+
+/* Per-phase device profile, the GPU counterpart of the reference's sampling
+ * profiler phases SMSCaustics / SMSCausticsBernoulliTrials / SMSGlints
+ * (include/mitsuba/core/profiler.h:25-28).  Kernel times come from CUDA events
+ * recorded on the context stream around each launch while profiling is on;
+ * ray / node / triangle counts are always accumulated. */
+#define SMS_PHASES 8
+#define SMS_PHASE_SS_FIRST   0   /* unbiased: first walk + visibility + contribution */
+#define SMS_PHASE_SS_TRIALS  1   /* unbiased: Bernoulli trials                        */
+#define SMS_PHASE_SS_BIASED  2   /* biased single scatter                             */
+#define SMS_PHASE_SS_WALK    3   /* per-walk entry point                              */
+#define SMS_PHASE_MS         4   /* multi-scatter connections                         */
+#define SMS_PHASE_GLINTS     5   /* glint connections                                 */
+#define SMS_PHASE_MS_WALK    6
+#define SMS_PHASE_GLINT_WALK 7
+typedef struct sms_profile {
+    double   ms[SMS_PHASES];         /* summed kernel time (profiling on)  */
+    uint64_t launches[SMS_PHASES];   /* timed launches                      */
+    uint64_t rays[SMS_PHASES];
+    uint64_t bvh_nodes[SMS_PHASES];  /* 64-byte node records fetched        */
+    uint64_t tri_tests[SMS_PHASES];  /* 48-byte triangle records fetched    */
+} sms_profile;
+
+sms_status sms_ctx_set_profiling(sms_ctx *ctx, int32_t enable);
+sms_status sms_profile_read(sms_ctx *ctx, sms_profile *out);
 
 /* ------------------------------------------------------- single scatter */
 /* SpecularManifoldSingleScatter::specular_manifold_sampling for n queries

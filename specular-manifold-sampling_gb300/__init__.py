@@ -77,6 +77,14 @@ class _Stats(C.Structure):
         "speculative_walks")]
 
 
+PHASES = ["ss_first", "ss_trials", "ss_biased", "ss_walk", "ms", "glints", "ms_walk", "glint_walk"]
+
+
+class _Profile(C.Structure):
+    _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint64 * 8), ("rays", C.c_uint64 * 8),
+                ("bvh_nodes", C.c_uint64 * 8), ("tri_tests", C.c_uint64 * 8)]
+
+
 _LIB = None
 
 
@@ -107,6 +115,8 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ctx_set_launch": (i32, [vp, i32, i32]),
         "sms_stats_read": (i32, [vp, C.POINTER(_Stats)]),
         "sms_stats_reset": (i32, [vp]),
+        "sms_ctx_set_profiling": (i32, [vp, i32]),
+        "sms_profile_read": (i32, [vp, C.POINTER(_Profile)]),
         "sms_ss_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ss_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ss_walk_batch": (i32, [vp, i32, vp, vp, u32, vp]),
@@ -299,6 +309,17 @@ class Context:
 
     def reset_stats(self):
         _check(_LIB.sms_stats_reset(self._h))
+
+    def set_profiling(self, enable: bool = True):
+        _check(_LIB.sms_ctx_set_profiling(self._h, int(enable)))
+
+    def profile(self) -> dict:
+        """Per-phase kernel time (CUDA events) and traversal counters."""
+        p = _Profile()
+        _check(_LIB.sms_profile_read(self._h, C.byref(p)))
+        return {name: {"ms": p.ms[k], "launches": p.launches[k], "rays": p.rays[k],
+                       "bvh_nodes": p.bvh_nodes[k], "tri_tests": p.tri_tests[k]}
+                for k, name in enumerate(PHASES)}
 
     def close(self):
         if getattr(self, "_h", None) and _LIB is not None:

@@ -785,7 +785,14 @@ SMS_HD f3 sample_position(const DevScene &sc, const DevShape &s, float sx, float
 }
 
 // Counters shared by all kernels of a context (one record per context).
+// Profiling phases (one per kernel family), after the reference's profiler
+// phases SMSCaustics / SMSCausticsBernoulliTrials / SMSGlints
+// (include/mitsuba/core/profiler.h:25-28).
+enum : int { kPhaseSsFirst = 0, kPhaseSsTrials = 1, kPhaseSsBiased = 2, kPhaseSsWalk = 3, kPhaseMs = 4,
+             kPhaseGlints = 5, kPhaseMsWalk = 6, kPhaseGlintWalk = 7, kPhases = 8 };
+
 struct DevCounters {
+    unsigned long long phase_rays[kPhases], phase_nodes[kPhases], phase_tris[kPhases];
     unsigned long long solver_succeeded, solver_failed, bernoulli_calls, bernoulli_iters,
         bernoulli_max, walks, newton_iters, connections, rays, bvh_nodes, tri_tests, speculative_walks;
     unsigned int trial_count;  // queries appended to the Bernoulli-trial queue

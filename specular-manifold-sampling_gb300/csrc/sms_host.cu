@@ -261,6 +261,57 @@ extern "C" sms_status sms_scene_add_area_emitter(sms_scene *s, int32_t shape, co
     return SMS_OK;
 }
 
+// ----------------------------------------------------------- phase timing
+namespace sms {
+struct PhaseTimer {
+    bool enabled = false;
+    struct Rec { int phase; cudaEvent_t a, b; };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    int open_phase = -1;
+    cudaEvent_t open_ev = nullptr;
+    double ms[kPhases] = {0};
+    unsigned long long launches[kPhases] = {0};
+    cudaEvent_t get() {
+        if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    void collect() {
+        for (Rec &r : pending) {
+            float t = 0.f;
+            if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+                ms[r.phase] += t;
+                launches[r.phase]++;
+            }
+            pool.push_back(r.a);
+            pool.push_back(r.b);
+        }
+        pending.clear();
+    }
+    ~PhaseTimer() {
+        collect();
+        for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    }
+};
+
+void phase_begin(PhaseTimer *tm, int phase, cudaStream_t s) {
+    if (!tm || !tm->enabled) return;
+    tm->open_phase = phase;
+    tm->open_ev = tm->get();
+    cudaEventRecord(tm->open_ev, s);
+}
+
+void phase_end(PhaseTimer *tm, cudaStream_t s) {
+    if (!tm || !tm->enabled || tm->open_phase < 0) return;
+    cudaEvent_t b = tm->get();
+    cudaEventRecord(b, s);
+    tm->pending.push_back({tm->open_phase, tm->open_ev, b});
+    tm->open_phase = -1;
+}
+}  // namespace sms
+
 // ---------------------------------------------------------------- context
 struct sms_ctx {
     int device = 0;
@@ -278,6 +329,7 @@ struct sms_ctx {
     // per-query scratch of the unbiased estimator
     void *scratch = nullptr;
     uint32_t scratch_n = 0;
+    PhaseTimer timer;
     std::vector<int> casters_ss;
 };
 
@@ -317,6 +369,7 @@ extern "C" void sms_ctx_destroy(sms_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    c->timer.collect();
     for (void *p : c->allocs) cudaFree(p);
     if (c->io) cudaFree(c->io);
     if (c->scratch) cudaFree(c->scratch);
@@ -541,6 +594,32 @@ extern "C" sms_status sms_stats_reset(sms_ctx *c) {
     CUDA_TRY(cudaSetDevice(c->device));
     CUDA_TRY(cudaMemsetAsync(c->ctr, 0, sizeof(DevCounters), c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->timer.collect();
+    for (int k = 0; k < kPhases; ++k) { c->timer.ms[k] = 0.0; c->timer.launches[k] = 0; }
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_ctx_set_profiling(sms_ctx *c, int32_t enable) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    c->timer.enabled = enable != 0;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_profile_read(sms_ctx *c, sms_profile *out) {
+    if (!c || !out) return fail(SMS_ERR_INVALID_ARG, "null argument");
+    static_assert(SMS_PHASES == kPhases, "phase count");
+    DevCounters h;
+    CUDA_TRY(cudaSetDevice(c->device));
+    CUDA_TRY(cudaMemcpyAsync(&h, c->ctr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->timer.collect();
+    for (int k = 0; k < kPhases; ++k) {
+        out->ms[k] = c->timer.ms[k];
+        out->launches[k] = c->timer.launches[k];
+        out->rays[k] = h.phase_rays[k];
+        out->bvh_nodes[k] = h.phase_nodes[k];
+        out->tri_tests[k] = h.phase_tris[k];
+    }
     return SMS_OK;
 }
 
@@ -576,7 +655,7 @@ extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, ui
     if (!c->cfg.biased)
         if (sms_status st = ensure_scratch(c, n, scr)) return st;
     CUDA_TRY(launch_ss_connect(c->dsc, solver_cfg(c->cfg), q, n, seed, stream_off, out->value, out->count,
-                               out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, c->stream));
+                               out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, &c->timer, c->stream));
     return SMS_OK;
 }
 
@@ -644,7 +723,7 @@ extern "C" sms_status sms_ss_walk_batch(sms_ctx *c, int32_t caster, const float 
         if (e != cudaSuccess) { st = cuda_fail(e, "copy walk inputs"); break; }
         e = launch_ss_walk(c->dsc, solver_cfg(c->cfg), caster, reinterpret_cast<float *>(dbuf),
                            reinterpret_cast<float *>(dbuf + qb), n, reinterpret_cast<float *>(dbuf + qb + wb),
-                           c->ctr, c->stream);
+                           c->ctr, &c->timer, c->stream);
         if (e != cudaSuccess) { st = cuda_fail(e, "launch ss_walk"); break; }
         e = cudaMemcpyAsync(out, dbuf + qb + wb, ob, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) { st = cuda_fail(e, "copy walk outputs"); break; }

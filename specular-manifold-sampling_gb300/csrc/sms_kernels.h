@@ -8,6 +8,12 @@ namespace sms {
 struct DevScene;
 struct DevCounters;
 
+// Optional per-phase CUDA-event timing (host side, sms_host.cu).  Both calls
+// are no-ops when tm is null or profiling is off.
+struct PhaseTimer;
+void phase_begin(PhaseTimer *tm, int phase, cudaStream_t s);
+void phase_end(PhaseTimer *tm, cudaStream_t s);
+
 // Solver parameters the kernels read (a subset of sms_config, already
 // validated by the host).
 struct SolverCfg {
@@ -42,10 +48,11 @@ struct SsScratch {
 inline size_t ss_scratch_bytes(uint32_t n) { return (size_t)n * (4 + 12 + 12 + 4); }
 
 cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q,
-                           const float *w, uint32_t n, float *out, DevCounters *ctr, cudaStream_t s);
+                           const float *w, uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm,
+                           cudaStream_t s);
 cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n,
                               uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
                               DevCounters *ctr, const SsScratch &scr, int num_sms, int blocks_per_sm,
-                              cudaStream_t s);
+                              PhaseTimer *tm, cudaStream_t s);
 
 }  // namespace sms

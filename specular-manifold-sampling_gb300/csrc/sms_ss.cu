@@ -47,7 +47,7 @@ struct LaneStats {
 };
 
 // Warp-aggregated counter update; all 32 lanes must call it.
-SMS_D void flush_stats(const LaneStats &st, DevCounters *ctr, uint32_t err) {
+SMS_D void flush_stats(const LaneStats &st, DevCounters *ctr, uint32_t err, int phase) {
     unsigned long long v[11] = {st.succ, st.fail, st.calls, st.iters, st.walks, st.newton, st.conns,
                                 st.rays, st.nodes, st.tris, st.spec};
     unsigned long long *dst[11] = {&ctr->solver_succeeded, &ctr->solver_failed, &ctr->bernoulli_calls,
@@ -59,6 +59,14 @@ SMS_D void flush_stats(const LaneStats &st, DevCounters *ctr, uint32_t err) {
         unsigned long long s = v[k];
         for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(full, s, off);
         if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst[k], s);
+    }
+    unsigned long long pv[3] = {st.rays, st.nodes, st.tris};
+    unsigned long long *pd[3] = {&ctr->phase_rays[phase], &ctr->phase_nodes[phase], &ctr->phase_tris[phase]};
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        unsigned long long s = pv[k];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(full, s, off);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(pd[k], s);
     }
     unsigned long long m = st.imax;
     for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(full, m, off));
@@ -250,7 +258,7 @@ __global__ void __launch_bounds__(128) ss_walk_kernel(DevScene sc, SolverCfg cfg
         #pragma unroll
         for (int k = 0; k < kWalkOutFields; ++k) out[(size_t)k * n + i] = res[k];
     }
-    flush_stats(st, ctr, err);
+    flush_stats(st, ctr, err, kPhaseSsWalk);
 }
 
 // ------------------------------------------------------ biased estimator
@@ -358,7 +366,7 @@ __global__ void __launch_bounds__(128) ss_biased_kernel(DevScene sc, SolverCfg c
             walks[qi] = work ? M * sc.n_casters_ss : 0;
         }
     }
-    flush_stats(st, ctr, err);
+    flush_stats(st, ctr, err, kPhaseSsBiased);
 }
 
 // --------------------------------------------------- unbiased: first walks
@@ -427,7 +435,7 @@ __global__ void __launch_bounds__(128) ss_first_kernel(DevScene sc, SolverCfg cf
         base = __shfl_sync(0xffffffffu, base, leader);
         if (enqueue) scr.list[base + __popc(want & ((1u << lane) - 1u))] = qi;
     }
-    flush_stats(st, ctr, err);
+    flush_stats(st, ctr, err, kPhaseSsFirst);
 }
 
 // ------------------------------------------------ unbiased: Bernoulli trials
@@ -508,20 +516,23 @@ __global__ void __launch_bounds__(128) ss_trials_kernel(DevScene sc, SolverCfg c
             st.imax = max(st.imax, (unsigned long long)iterations);
         }
     }
-    flush_stats(st, ctr, err);
+    flush_stats(st, ctr, err, kPhaseSsTrials);
 }
 
 // ---------------------------------------------------------------- launchers
 cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q, const float *w,
-                           uint32_t n, float *out, DevCounters *ctr, cudaStream_t s) {
+                           uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    phase_begin(tm, kPhaseSsWalk, s);
     ss_walk_kernel<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, caster, q, w, n, out, ctr);
+    phase_end(tm, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                               uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
-                              const SsScratch &scr, int num_sms, int blocks_per_sm, cudaStream_t s) {
+                              const SsScratch &scr, int num_sms, int blocks_per_sm, PhaseTimer *tm,
+                              cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const int bps = blocks_per_sm > 0 ? blocks_per_sm : 8;
     if (cfg.biased) {
@@ -529,8 +540,10 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
         const uint32_t groups_per_block = 128 / G;
         uint32_t blocks_needed = (n + groups_per_block - 1) / groups_per_block;
         uint32_t blocks = std::min<uint32_t>(blocks_needed, (uint32_t)(num_sms * bps));
+        phase_begin(tm, kPhaseSsBiased, s);
         if (G == 16) ss_biased_kernel<16><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
         else ss_biased_kernel<32><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
+        phase_end(tm, s);
         return cudaGetLastError();
     }
     if (sc.n_casters_ss == 0) {
@@ -543,12 +556,16 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
     for (int c = 0; c < sc.n_casters_ss; ++c) {
         cudaError_t e = cudaMemsetAsync(&ctr->trial_count, 0, 2 * sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
+        phase_begin(tm, kPhaseSsFirst, s);
         ss_first_kernel<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks,
                                                         scr, ctr);
+        phase_end(tm, s);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        phase_begin(tm, kPhaseSsTrials, s);
         ss_trials_kernel<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks,
                                                        scr, ctr);
+        phase_end(tm, s);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

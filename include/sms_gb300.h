@@ -235,6 +235,29 @@ sms_status sms_ss_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
                                        uint32_t n, uint64_t seed,
                                        uint64_t stream_offset, sms_result *out_dev);
 
+/* Allocation-free variant of sms_ss_connect_batch_device.  No counterpart in
+ * the reference: it exists for callers that must not allocate device memory
+ * while rendering (work issued inside CUDA stream capture, fixed-budget
+ * real-time loops, hosts that own every allocation).  It runs the same kernels
+ * and gives bit-identical results, but takes the unbiased estimator's
+ * per-query scratch from a fixed device array inside the library instead of
+ * growing the context's scratch with cudaMalloc, and calls no allocating CUDA
+ * or library routine.
+ *   - n may not exceed 262,144 queries (the array holds 32 bytes per query:
+ *     8 MiB on every GPU that loads the library, kept until process exit);
+ *     larger batches are rejected with SMS_ERR_INVALID_ARG -- split them and
+ *     use stream_offset, which keeps results identical.
+ *   - The first call on a device looks up the array's device address (and lets
+ *     the CUDA runtime load the module that holds it); make that first call
+ *     before any stream capture.
+ *   - All calls, from every context on a device, share the one array: calls
+ *     whose kernels overlap on the GPU (different streams, or different
+ *     contexts) race on it.  Calls issued on one stream are safe.
+ * Device pointers in and out; asynchronous on the context stream. */
+sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *queries_dev,
+                                        uint32_t n, uint64_t seed,
+                                        uint64_t stream_offset, sms_result *out_dev);
+
 /* Per-walk entry point: SpecularManifoldSingleScatter::sample_path with an
  * explicit start point (manifold_ss.cpp:203-279, p_start != 0), the harness
  * the reference's figure scripts use.

@@ -27,6 +27,7 @@ PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "libsms_gb300.so"
 
 QUERY_FIELDS = 16
+NOALLOC_MAX_QUERIES = 1 << 18
 WALK_IN_FIELDS = 8
 WALK_OUT_FIELDS = 11
 
@@ -120,6 +121,7 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ss_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ss_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ss_walk_batch": (i32, [vp, i32, vp, vp, u32, vp]),
+        "sms_ss_connect_batch_noalloc": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -360,6 +362,14 @@ class SpecularManifoldSingleScatter:
         r = _Result(value_ptr, count_ptr, walks_ptr)
         _check(_LIB.sms_ss_connect_batch_device(self.ctx.handle, queries_ptr, n, seed, stream_offset,
                                                 C.byref(r)))
+
+    def specular_manifold_sampling_noalloc(self, queries_ptr: int, n: int, value_ptr: int, count_ptr: int,
+                                           walks_ptr: int, seed: int = 0, stream_offset: int = 0):
+        """Allocation-free device-pointer variant (sms_ss_connect_batch_noalloc):
+        at most NOALLOC_MAX_QUERIES queries per call; see the C header."""
+        r = _Result(value_ptr, count_ptr, walks_ptr)
+        _check(_LIB.sms_ss_connect_batch_noalloc(self.ctx.handle, queries_ptr, n, seed, stream_offset,
+                                                 C.byref(r)))
 
     def sample_path(self, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
         """Per-walk sample_path with explicit emitter point and start point.

@@ -733,3 +733,22 @@ extern "C" sms_status sms_ss_walk_batch(sms_ctx *c, int32_t caster, const float 
     if (e != cudaSuccess) return cuda_fail(e, "sms_ss_walk_batch");
     return check_device_error(c);
 }
+
+// ------------------------------------------------- accessors for other TUs
+bool ctx_view(sms_ctx *c, CtxView &out) {
+    if (!c) return false;
+    out.device = c->device;
+    out.stream = c->stream;
+    out.scene = &c->dsc;
+    out.solver = solver_cfg(c->cfg);
+    out.counters = c->ctr;
+    out.num_sms = c->num_sms;
+    out.blocks_per_sm = c->blocks_per_sm;
+    out.timer = &c->timer;
+    return true;
+}
+
+int set_last_error_impl(int st, const char *msg) {
+    g_last_error = msg ? msg : "";
+    return st;
+}

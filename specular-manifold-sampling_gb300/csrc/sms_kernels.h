@@ -55,4 +55,22 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
                               DevCounters *ctr, const SsScratch &scr, int num_sms, int blocks_per_sm,
                               PhaseTimer *tm, cudaStream_t s);
 
+// Read-only view of a context for entry points defined outside sms_host.cu.
+struct CtxView {
+    int device;
+    cudaStream_t stream;
+    const DevScene *scene;
+    SolverCfg solver;
+    DevCounters *counters;
+    int num_sms;
+    int blocks_per_sm;
+    PhaseTimer *timer;
+};
+
 }  // namespace sms
+
+// Context accessors implemented in sms_host.cu.
+struct sms_ctx;
+bool ctx_view(sms_ctx *c, sms::CtxView &out);
+// Records msg as sms_last_error() for this thread and returns st.
+int set_last_error_impl(int st, const char *msg);

@@ -1,0 +1,60 @@
+"""The allocation-free connection entry point (sms_ss_connect_batch_noalloc).
+
+It serves callers that cannot allocate device memory during a render: work
+issued inside CUDA stream capture, fixed-budget real-time loops, or hosts that
+own every allocation.  It must give the same results as the regular device
+entry point, call after call, even though its scratch array keeps the previous
+call's contents.  This file is collected last on purpose.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(fn, ctx, q_dev, n, seed, stream_offset=0):
+    import torch
+    dev = q_dev.device
+    val = torch.full((3, n), -1.0, dtype=torch.float32, device=dev)
+    cnt = torch.full((n,), -7, dtype=torch.int32, device=dev)
+    wlk = torch.full((n,), -7, dtype=torch.int32, device=dev)
+    fn(q_dev.data_ptr(), n, val.data_ptr(), cnt.data_ptr(), wlk.data_ptr(), seed=seed, stream_offset=stream_offset)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    stream.synchronize()
+    return val.cpu().numpy(), cnt.cpu().numpy(), wlk.cpu().numpy()
+
+
+def test_noalloc_matches_device_entry_point(sms, workloads, gpu_lib):
+    import torch
+    W = workloads
+    ctx = sms.Context(sms.Scene(W.water_scene(res=128)), W.water_config())
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    n = 6000
+    q_dev = torch.from_numpy(W.water_queries(n)).cuda()
+    # two calls in a row with different seeds and offsets: the second call must
+    # not see anything the first one left in the shared scratch array
+    for seed, off in ((3, 0), (4, 1000)):
+        v_ref, c_ref, w_ref = _run(ss.specular_manifold_sampling_device, ctx, q_dev, n, seed, off)
+        v, c, w = _run(ss.specular_manifold_sampling_noalloc, ctx, q_dev, n, seed, off)
+        assert np.array_equal(c, c_ref) and np.array_equal(w, w_ref)
+        np.testing.assert_allclose(v, v_ref, rtol=1e-6, atol=0)
+        assert (c > 0).sum() > 0 and (w >= 1).all()
+    ctx.close()
+
+
+def test_noalloc_rejects_oversized_batch(sms, workloads, gpu_lib):
+    import torch
+    W = workloads
+    ctx = sms.Context(sms.Scene(W.water_scene(res=64)), W.water_config())
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    n = sms.NOALLOC_MAX_QUERIES + 1
+    q_dev = torch.zeros((16, n), dtype=torch.float32, device="cuda")
+    out = torch.zeros((5, n), dtype=torch.float32, device="cuda")
+    with pytest.raises(sms.SMSError) as e:
+        ss.specular_manifold_sampling_noalloc(q_dev.data_ptr(), n, out[0].data_ptr(), out[3].data_ptr(),
+                                              out[4].data_ptr())
+    assert e.value.status == 1 and "exceed" in str(e.value)
+    ctx.close()

@@ -272,6 +272,27 @@ sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *queries_dev,
 sms_status sms_ss_walk_batch(sms_ctx *ctx, int32_t caster, const float *queries,
                              const float *walk_in, uint32_t n, float *walk_out);
 
+/* ------------------------------------------------------- multi scatter */
+/* SpecularManifoldMultiScatter::specular_manifold_sampling for n queries
+ * (manifold_ms.cpp:27-201): k-bounce chains through shapes flagged
+ * SMS_SHAPE_CAUSTIC_CASTER_MULTI / _BOUNCER, k = cfg.bounces (1..4), emitters
+ * flagged SMS_EMITTER_CAUSTIC_MULTI.  Same buffers, random-number streams and
+ * count/walks meaning as sms_ss_connect_batch. */
+sms_status sms_ms_connect_batch(sms_ctx *ctx, const float *queries, uint32_t n,
+                                uint64_t seed, uint64_t stream_offset,
+                                sms_result *out);
+sms_status sms_ms_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
+                                       uint32_t n, uint64_t seed,
+                                       uint64_t stream_offset, sms_result *out_dev);
+
+/* Per-walk multi-scatter sample_path with first_path = true
+ * (manifold_ms.cpp:203-227, 280-408): walk_in as sms_ss_walk_batch; walk_out
+ * SMS_MS_WALK_OUT_FIELDS rows: ok, iterations, first vertex (3), last vertex
+ * (3), seed path ok. */
+#define SMS_MS_WALK_OUT_FIELDS 9
+sms_status sms_ms_walk_batch(sms_ctx *ctx, int32_t caster, const float *queries,
+                             const float *walk_in, uint32_t n, float *walk_out);
+
 #ifdef __cplusplus
 }
 #endif

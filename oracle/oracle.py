@@ -67,6 +67,8 @@ def load(fma: bool = False):
         "oracle_ss_walk_batch": (i32, [vp, C.POINTER(_Config), i32, vp, vp, u32, vp]),
         "oracle_ss_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int,
                                           vp]),
+        "oracle_ms_walk_batch": (i32, [vp, C.POINTER(_Config), i32, vp, vp, u32, vp]),
+        "oracle_ms_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
         "oracle_fresnel": (f32, [f32, f32, C.POINTER(f32)]),
         "oracle_fresnel_conductor": (f32, [f32, f32, f32]),
         "oracle_uniform_sphere": (None, [f32, f32, C.POINTER(f32)]),
@@ -134,8 +136,19 @@ class OracleScene:
                                   out.ctypes.data)
         return out
 
+    def ms_walk_batch(self, config, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
+        """Multi-scatter first-path walks: rows ok, iterations, first vertex (3),
+        last vertex (3), seed-path ok."""
+        n = queries.shape[1]
+        q = np.ascontiguousarray(queries, np.float32)
+        w = np.ascontiguousarray(walk_in, np.float32)
+        out = np.zeros((9, n), np.float32)
+        self._lib.oracle_ms_walk_batch(self._h, C.byref(_cfg(config)), caster, q.ctypes.data, w.ctypes.data, n,
+                                       out.ctypes.data)
+        return out
+
     def connect_batch(self, config, queries: np.ndarray, seed: int = 0, stream_offset: int = 0,
-                      nthreads: int | None = None):
+                      nthreads: int | None = None, multi: bool = False):
         n = queries.shape[1]
         q = np.ascontiguousarray(queries, np.float32)
         value = np.zeros((3, n), np.float32)
@@ -143,9 +156,9 @@ class OracleScene:
         walks = np.zeros(n, np.int32)
         stats = np.zeros(8, np.uint64)
         nt = nthreads or os.cpu_count() or 1
-        self._lib.oracle_ss_connect_batch(self._h, C.byref(_cfg(config)), q.ctypes.data, n, seed, stream_offset,
-                                     value.ctypes.data, count.ctypes.data, walks.ctypes.data, nt,
-                                     stats.ctypes.data)
+        fn = self._lib.oracle_ms_connect_batch if multi else self._lib.oracle_ss_connect_batch
+        fn(self._h, C.byref(_cfg(config)), q.ctypes.data, n, seed, stream_offset, value.ctypes.data,
+           count.ctypes.data, walks.ctypes.data, nt, stats.ctypes.data)
         names = ["solver_succeeded", "solver_failed", "bernoulli_trial_calls", "bernoulli_trial_iterations",
                  "bernoulli_trial_iterations_max", "walks", "newton_iterations", "connections"]
         return value, count, walks, dict(zip(names, stats.tolist()))

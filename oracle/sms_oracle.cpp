@@ -790,10 +790,9 @@ static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, cons
     return ok && si_final.valid();
 }
 
-/* manifold.h:204-260 */
-static EI sample_emitter_interaction(const Scene &sc, const Query &q, PCG32 &rng) {
+/* manifold.h:204-260 (em: the caustic emitter list of the estimator) */
+static EI sample_emitter_interaction(const Scene &sc, const std::vector<int> &em, const Query &q, PCG32 &rng) {
     EI ei;
-    const std::vector<int> &em = sc.emitters_ss;
     if (em.empty()) return ei;
     float es = rng.next_f32();
     float emitter_pdf = 1.f / (float)em.size();
@@ -1010,7 +1009,7 @@ static void update_max(std::atomic<uint64_t> &a, uint64_t v) {
 static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG32 &rng,
                      int &count_out, int &walks_out, Stats &st) {
     count_out = 0; walks_out = 0;
-    EI ei = sample_emitter_interaction(sc, q, rng);
+    EI ei = sample_emitter_interaction(sc, sc.emitters_ss, q, rng);
     V3 result(0.f);
     if (sc.casters_ss.empty() || ei.emitter < 0) return result;
     st.connections++;
@@ -1064,6 +1063,487 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
                 solutions.push_back(direction);
                 V3 bsdf = diffuse_eval(q, direction);
                 V3 spec = evaluate_path_contribution(sc, q, ei, si_final);
+                value += bsdf * spec;
+            }
+            count_out += (int)solutions.size();
+        }
+        result += value;
+    }
+    return result;
+}
+
+
+/* ====================================================================
+ * Multi-scatter SMS (src/librender/manifold_ms.cpp)
+ * ==================================================================== */
+struct MSBlock {
+    V2 C, dx;
+    M2 prev, cur, next, tmp, inv_lambda;
+};
+
+static M2 msub(const M2 &a, const M2 &b) {
+    M2 r;
+    for (int i = 0; i < 2; ++i) for (int j = 0; j < 2; ++j) r.m[i][j] = a.m[i][j] - b.m[i][j];
+    return r;
+}
+static M2 mneg(const M2 &a) {
+    M2 r;
+    for (int i = 0; i < 2; ++i) for (int j = 0; j < 2; ++j) r.m[i][j] = -a.m[i][j];
+    return r;
+}
+static V2 vsub(V2 a, V2 b) { V2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+
+/* manifold_ms.cpp:1192-1232 (block Thomas, Kaplanyan et al. 2014) */
+static bool invert_tridiagonal_step(std::vector<MSBlock> &b) {
+    auto inv = [](const M2 &A, M2 &Ai) {
+        if (std::fabs(det(A)) == 0.f) return false;
+        Ai = inverse(A);
+        return true;
+    };
+    int n = (int)b.size();
+    if (n == 0) return true;
+    b[0].tmp = b[0].prev;
+    if (!inv(b[0].cur, b[0].inv_lambda)) return false;
+    for (int i = 1; i < n; ++i) {
+        b[i].tmp = mul(b[i].prev, b[i - 1].inv_lambda);
+        M2 m = msub(b[i].cur, mul(b[i].tmp, b[i - 1].next));
+        if (!inv(m, b[i].inv_lambda)) return false;
+    }
+    b[0].dx = b[0].C;
+    for (int i = 1; i < n; ++i) b[i].dx = vsub(b[i].C, mul(b[i].tmp, b[i - 1].dx));
+    b[n - 1].dx = mul(b[n - 1].inv_lambda, b[n - 1].dx);
+    for (int i = n - 2; i >= 0; --i) b[i].dx = mul(b[i].inv_lambda, vsub(b[i].dx, mul(b[i].next, b[i + 1].dx)));
+    return true;
+}
+
+/* manifold_ms.cpp:1234-1268 (Jakob & Marschner 2012) */
+static float invert_tridiagonal_geo(std::vector<MSBlock> &b) {
+    auto inv = [](const M2 &A, M2 &Ai) {
+        if (std::fabs(det(A)) == 0.f) return false;
+        Ai = inverse(A);
+        return true;
+    };
+    int n = (int)b.size();
+    if (n == 0) return 0.f;
+    M2 Li;
+    if (!inv(b[0].cur, Li)) return 0.f;
+    for (int i = 0; i < n - 2; ++i) {
+        b[i].tmp = mul(Li, b[i].next);
+        M2 m = msub(b[i + 1].cur, mul(b[i + 1].prev, b[i].tmp));
+        if (!inv(m, Li)) return 0.f;
+    }
+    b[n - 2].inv_lambda = mul(mneg(Li), b[n - 2].next);
+    for (int i = n - 3; i >= 0; --i) b[i].inv_lambda = mul(mneg(b[i].tmp), b[i + 1].inv_lambda);
+    return std::fabs(det(mneg(b[0].inv_lambda)));
+}
+
+static void d_sph_pair(V3 w, V3 du, V3 dv, float &a, float &b, float &c, float &d) { d_sphcoords(w, du, dv, a, b, c, d); }
+
+/* manifold_ms.cpp:631-857 (n_offset = (0,0,1), positional light) */
+static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::vector<MSBlock> &b) {
+    size_t k = v.size();
+    b.assign(k, MSBlock());
+    bool success = true;
+    for (size_t i = 0; i < k; ++i) {
+        V3 xp = i == 0 ? x0 : v[i - 1].p, xn = i == k - 1 ? lp : v[i + 1].p, xc = v[i].p;
+        V3 wo = xn - xc;
+        float ilo = norm(wo);
+        if (ilo < 1e-3f) return false;
+        ilo = 1.f / ilo; wo *= ilo;
+        V3 dwo_du = (v[i].dp_du - wo * dot(wo, v[i].dp_du)) * -ilo;
+        V3 dwo_dv = (v[i].dp_dv - wo * dot(wo, v[i].dp_dv)) * -ilo;
+        V3 wi = xp - xc;
+        float ili = norm(wi);
+        if (ili < 1e-3f) return false;
+        ili = 1.f / ili; wi *= ili;
+        V3 dwi_du = (v[i].dp_du - wi * dot(wi, v[i].dp_du)) * -ili;
+        V3 dwi_dv = (v[i].dp_dv - wi * dot(wi, v[i].dp_dv)) * -ili;
+        const MVertex &vi = v[i];
+        V3 n = vi.n, dndu = vi.dn_du, dndv = vi.dn_dv;
+        auto transform = [&](V3 w, V3 &out) { return vi.eta == 1.f ? reflect(w, n, out) : refract(w, n, vi.eta, out); };
+        auto d_transform = [&](V3 w, V3 du, V3 dv, V3 nd_u, V3 nd_v, V3 &ou, V3 &ov) {
+            if (vi.eta == 1.f) d_reflect(w, du, dv, n, nd_u, nd_v, ou, ov);
+            else d_refract(w, du, dv, n, nd_u, nd_v, vi.eta, ou, ov);
+        };
+        bool ok_i = false;
+        V3 wio;
+        if (transform(wi, wio)) {
+            float to, po, tio, pio;
+            sphcoords(wo, to, po); sphcoords(wio, tio, pio);
+            float dt = to - tio, dp = po - pio;
+            if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
+            b[i].C.x = dt; b[i].C.y = dp;
+            float a0, a1, a2, a3, c0, c1, c2, c3;
+            if (i > 0) {
+                V3 du = (v[i - 1].dp_du - wi * dot(wi, v[i - 1].dp_du)) * ili;
+                V3 dv = (v[i - 1].dp_dv - wi * dot(wi, v[i - 1].dp_dv)) * ili;
+                V3 ou, ov;
+                d_transform(wi, du, dv, V3(0.f), V3(0.f), ou, ov);
+                d_sph_pair(wio, ou, ov, c0, c1, c2, c3);
+                b[i].prev.m[0][0] = -c0; b[i].prev.m[1][0] = -c1; b[i].prev.m[0][1] = -c2; b[i].prev.m[1][1] = -c3;
+            }
+            V3 ou, ov;
+            d_transform(wi, dwi_du, dwi_dv, dndu, dndv, ou, ov);
+            d_sph_pair(wo, dwo_du, dwo_dv, a0, a1, a2, a3);
+            d_sph_pair(wio, ou, ov, c0, c1, c2, c3);
+            b[i].cur.m[0][0] = a0 - c0; b[i].cur.m[1][0] = a1 - c1; b[i].cur.m[0][1] = a2 - c2; b[i].cur.m[1][1] = a3 - c3;
+            if (i < k - 1) {
+                V3 du = (v[i + 1].dp_du - wo * dot(wo, v[i + 1].dp_du)) * ilo;
+                V3 dv = (v[i + 1].dp_dv - wo * dot(wo, v[i + 1].dp_dv)) * ilo;
+                d_sph_pair(wo, du, dv, a0, a1, a2, a3);
+                b[i].next.m[0][0] = a0; b[i].next.m[1][0] = a1; b[i].next.m[0][1] = a2; b[i].next.m[1][1] = a3;
+            }
+            ok_i = true;
+        }
+        V3 woi;
+        if (transform(wo, woi) && !ok_i) {
+            float ti, pi, toi, poi;
+            sphcoords(wi, ti, pi); sphcoords(woi, toi, poi);
+            float dt = ti - toi, dp = pi - poi;
+            if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
+            b[i].C.x = dt; b[i].C.y = dp;
+            float a0, a1, a2, a3, c0, c1, c2, c3;
+            if (i > 0) {
+                V3 du = (v[i - 1].dp_du - wi * dot(wi, v[i - 1].dp_du)) * ili;
+                V3 dv = (v[i - 1].dp_dv - wi * dot(wi, v[i - 1].dp_dv)) * ili;
+                d_sph_pair(wi, du, dv, a0, a1, a2, a3);
+                b[i].prev.m[0][0] = a0; b[i].prev.m[1][0] = a1; b[i].prev.m[0][1] = a2; b[i].prev.m[1][1] = a3;
+            }
+            V3 ou, ov;
+            d_transform(wo, dwo_du, dwo_dv, dndu, dndv, ou, ov);
+            d_sph_pair(wi, dwi_du, dwi_dv, a0, a1, a2, a3);
+            d_sph_pair(woi, ou, ov, c0, c1, c2, c3);
+            b[i].cur.m[0][0] = a0 - c0; b[i].cur.m[1][0] = a1 - c1; b[i].cur.m[0][1] = a2 - c2; b[i].cur.m[1][1] = a3 - c3;
+            if (i < k - 1) {
+                V3 du = (v[i + 1].dp_du - wo * dot(wo, v[i + 1].dp_du)) * ilo;
+                V3 dv = (v[i + 1].dp_dv - wo * dot(wo, v[i + 1].dp_dv)) * ilo;
+                d_transform(wo, du, dv, V3(0.f), V3(0.f), ou, ov);
+                d_sph_pair(woi, ou, ov, c0, c1, c2, c3);
+                b[i].next.m[0][0] = -c0; b[i].next.m[1][0] = -c1; b[i].next.m[0][1] = -c2; b[i].next.m[1][1] = -c3;
+            }
+            ok_i = true;
+        }
+        success = success && ok_i;
+    }
+    if (!success || !invert_tridiagonal_step(b)) return false;
+    return true;
+}
+
+/* manifold_ms.cpp:500-629 */
+static bool ms_step_halfvector(V3 x0, V3 lp, const std::vector<MVertex> &v, std::vector<MSBlock> &b) {
+    size_t k = v.size();
+    b.assign(k, MSBlock());
+    for (size_t i = 0; i < k; ++i) {
+        V3 xp = i == 0 ? x0 : v[i - 1].p, xn = i == k - 1 ? lp : v[i + 1].p, xc = v[i].p;
+        V3 wo = xn - xc;
+        float ilo = norm(wo);
+        if (ilo < 1e-3f) return false;
+        ilo = 1.f / ilo; wo *= ilo;
+        V3 wi = xp - xc;
+        float ili = norm(wi);
+        if (ili < 1e-3f) return false;
+        ili = 1.f / ili; wi *= ili;
+        float eta = v[i].eta;
+        if (dot(wi, v[i].gn) < 0.f) eta = 1.f / eta;
+        V3 h = wi + wo * eta;
+        if (eta != 1.f) h *= -1.f;
+        float ilh = 1.f / norm(h);
+        h *= ilh;
+        ilo *= eta * ilh;
+        ili *= ilh;
+        V3 du, dv;
+        if (i > 0) {
+            du = (v[i - 1].dp_du - wi * dot(wi, v[i - 1].dp_du)) * ili;
+            dv = (v[i - 1].dp_dv - wi * dot(wi, v[i - 1].dp_dv)) * ili;
+            du -= h * dot(du, h); dv -= h * dot(dv, h);
+            if (eta != 1.f) { du *= -1.f; dv *= -1.f; }
+            b[i].prev.m[0][0] = dot(v[i].s, du); b[i].prev.m[0][1] = dot(v[i].s, dv);
+            b[i].prev.m[1][0] = dot(v[i].t, du); b[i].prev.m[1][1] = dot(v[i].t, dv);
+        }
+        du = -v[i].dp_du * (ili + ilo) + wi * (dot(wi, v[i].dp_du) * ili) + wo * (dot(wo, v[i].dp_du) * ilo);
+        dv = -v[i].dp_dv * (ili + ilo) + wi * (dot(wi, v[i].dp_dv) * ili) + wo * (dot(wo, v[i].dp_dv) * ilo);
+        du -= h * dot(du, h); dv -= h * dot(dv, h);
+        if (eta != 1.f) { du *= -1.f; dv *= -1.f; }
+        b[i].cur.m[0][0] = dot(v[i].ds_du, h) + dot(v[i].s, du);
+        b[i].cur.m[0][1] = dot(v[i].ds_dv, h) + dot(v[i].s, dv);
+        b[i].cur.m[1][0] = dot(v[i].dt_du, h) + dot(v[i].t, du);
+        b[i].cur.m[1][1] = dot(v[i].dt_dv, h) + dot(v[i].t, dv);
+        if (i < k - 1) {
+            du = (v[i + 1].dp_du - wo * dot(wo, v[i + 1].dp_du)) * ilo;
+            dv = (v[i + 1].dp_dv - wo * dot(wo, v[i + 1].dp_dv)) * ilo;
+            du -= h * dot(du, h); dv -= h * dot(dv, h);
+            if (eta != 1.f) { du *= -1.f; dv *= -1.f; }
+            b[i].next.m[0][0] = dot(v[i].s, du); b[i].next.m[0][1] = dot(v[i].s, dv);
+            b[i].next.m[1][0] = dot(v[i].t, du); b[i].next.m[1][1] = dot(v[i].t, dv);
+        }
+        b[i].C.x = dot(v[i].s, h);
+        b[i].C.y = dot(v[i].t, h);
+    }
+    return invert_tridiagonal_step(b);
+}
+
+static bool is_chain_shape(const Scene &sc, int s) {
+    uint32_t f = sc.shapes[s].flags;
+    return (f & SMS_SHAPE_CAUSTIC_CASTER_MULTI) || (f & SMS_SHAPE_CAUSTIC_BOUNCER);
+}
+
+/* si.spawn_ray (interaction.h:58-62) */
+static Ray spawn_ray(V3 p, V3 d) {
+    Ray r; r.o = p; r.d = d; r.mint = (1.f + hmax_abs(p)) * kRayEps; r.maxt = kInf;
+    return r;
+}
+
+/* Trace the specular chain from x0 toward x1 (sample_seed_path :280-408 with
+ * first_path/template shapes, reproject :859-918).  template_shapes empty ->
+ * any caster_multi/bouncer shape is allowed (first path). */
+static bool ms_trace_chain(const Scene &sc, int bounces, V3 x0, V3 x1, const std::vector<int> &tmpl,
+                           bool require_chain_flags, std::vector<MVertex> &path) {
+    path.clear();
+    V3 wo = normalize(x1 - x0);
+    Ray ray; ray.o = x0; ray.d = wo;
+    while ((int)path.size() < bounces) {
+        int bounce = (int)path.size();
+        SI si = ray_intersect(sc, ray);
+        if (!si.valid()) return false;
+        if (require_chain_flags && !is_chain_shape(sc, si.shape)) return false;
+        if (!tmpl.empty() && si.shape != tmpl[bounce]) return false;
+        MVertex v;
+        vertex_from_si(sc, si, v);
+        path.push_back(v);
+        V3 wi = -wo;
+        bool ok;
+        if (v.eta == 1.f) ok = reflect(wi, v.n, wo);
+        else ok = refract(wi, v.n, v.eta, wo);
+        if (!ok) return false;
+        ray = spawn_ray(si.p, wo);
+    }
+    return true;
+}
+
+/* manifold_ms.cpp:410-498 */
+static bool ms_newton(const Scene &sc, const sms_config &cfg, V3 x0, V3 lp, const std::vector<int> &tmpl,
+                      std::vector<MVertex> &path, int &iters) {
+    bool success = false;
+    int it = 0;
+    float beta = 1.f;
+    bool needs_update = true;
+    std::vector<MSBlock> b;
+    while (it < cfg.max_iterations) {
+        bool ok = true;
+        if (needs_update)
+            ok = cfg.halfvector_constraints ? ms_step_halfvector(x0, lp, path, b) : ms_step_anglediff(x0, lp, path, b);
+        if (!ok) break;
+        bool conv = true;
+        for (const MSBlock &bl : b)
+            if (std::sqrt(bl.C.x * bl.C.x + bl.C.y * bl.C.y) > cfg.solver_threshold) { conv = false; break; }
+        if (conv) { success = true; break; }
+        /* only the first proposed position drives the reprojection (:865-867) */
+        const MVertex &v0 = path[0];
+        V3 p0 = v0.p - (v0.dp_du * b[0].dx.x + v0.dp_dv * b[0].dx.y) * (cfg.step_scale * beta);
+        std::vector<MVertex> prop;
+        bool proj = ms_trace_chain(sc, (int)path.size(), x0, p0, tmpl, false, prop) && prop.size() == tmpl.size();
+        if (!proj) { beta = 0.5f * beta; needs_update = false; }
+        else { beta = std::min(1.f, 2.f * beta); path = prop; needs_update = true; }
+        it++;
+    }
+    iters = it;
+    if (!success) return false;
+    size_t n = path.size();
+    for (size_t i = 0; i < n; ++i) {
+        V3 xp = i == 0 ? x0 : path[i - 1].p, xn = i == n - 1 ? lp : path[i + 1].p;
+        V3 wi = normalize(xp - path[i].p), wo = normalize(xn - path[i].p);
+        bool refraction = dot(path[i].gn, wi) * dot(path[i].gn, wo) < 0.f;
+        bool reflection = !refraction;
+        if ((path[i].eta == 1.f && !reflection) || (path[i].eta != 1.f && !refraction)) return false;
+    }
+    return true;
+}
+
+/* sample_path (:203-227): seed path + Newton.  seed_shapes: in = template
+ * (empty for a first path), out = this walk's seed shapes. */
+static bool ms_sample_path(const Scene &sc, const sms_config &cfg, int caster, const Query &q, V3 lp, V2 sample,
+                           V3 p_start, std::vector<int> &tmpl, bool first_path, std::vector<MVertex> &path,
+                           int &iters, bool &seed_ok) {
+    iters = 0;
+    seed_ok = false;
+    V3 x1 = sample_position(sc.shapes[caster], sample);
+    if (p_start.x != 0.f || p_start.y != 0.f || p_start.z != 0.f) x1 = p_start;
+    static const std::vector<int> none;
+    if (!ms_trace_chain(sc, cfg.bounces, q.p, x1, first_path ? none : tmpl, true, path)) return false;
+    seed_ok = true;
+    if (first_path) {
+        tmpl.clear();
+        for (const MVertex &v : path) tmpl.push_back(v.shape);
+    }
+    return ms_newton(sc, cfg, q.p, lp, tmpl, path, iters);
+}
+
+/* manifold_ms.cpp:920-1023 (smooth BSDFs) */
+static float ms_specular_reflectance(const Scene &sc, V3 x0, V3 lp, const std::vector<MVertex> &path) {
+    if (path.empty()) return 0.f;
+    Ray ray; ray.o = x0; ray.d = normalize(path[0].p - x0);
+    float val = 1.f;
+    SI si;
+    for (size_t k = 0; k < path.size(); ++k) {
+        si = ray_intersect(sc, ray);
+        if (!si.valid()) return 0.f;
+        V3 wo = k + 1 < path.size() ? normalize(path[k + 1].p - si.p) : normalize(lp - si.p);
+        val *= specular_reflectance(sc, si, wo);
+        ray = Ray(); ray.o = si.p; ray.d = wo;
+    }
+    Ray vis; vis.o = si.p; vis.d = normalize(lp - si.p);
+    vis.mint = kRayEps * (1.f + hmax_abs(si.p));
+    vis.maxt = norm(lp - si.p) * (1.f - kRayEps);
+    if (ray_test(sc, vis)) return 0.f;
+    return val;
+}
+
+/* manifold_ms.cpp:1025-1190 (positional endpoint) */
+static float ms_geometric_term(const MVertex &vx, const std::vector<MVertex> &path, const MVertex &vy) {
+    std::vector<MVertex> v = path;
+    v.push_back(vy);
+    size_t k = v.size();
+    std::vector<MSBlock> b(k);
+    for (size_t i = 0; i + 1 < k; ++i) {
+        V3 xc = v[i].p, xn = v[i + 1].p;
+        V3 wo = xn - xc;
+        float ilo = norm(wo);
+        if (ilo < 1e-3f) return 0.f;
+        ilo = 1.f / ilo; wo *= ilo;
+        V3 xp = i == 0 ? vx.p : v[i - 1].p;
+        V3 wi = xp - xc;
+        float ili = norm(wi);
+        if (ili < 1e-3f) return 0.f;
+        ili = 1.f / ili; wi *= ili;
+        float eta = v[i].eta;
+        if (dot(wi, v[i].gn) < 0.f) eta = 1.f / eta;
+        V3 h = wi + wo * eta;
+        if (eta != 1.f) h *= -1.f;
+        float ilh = 1.f / norm(h);
+        h *= ilh;
+        ilo *= eta * ilh;
+        ili *= ilh;
+        float dpdu_n = dot(v[i].dp_du, v[i].n), dpdv_n = dot(v[i].dp_dv, v[i].n);
+        V3 s = v[i].dp_du - v[i].n * dpdu_n, t = v[i].dp_dv - v[i].n * dpdv_n;
+        V3 du, dv;
+        if (i > 0) {
+            du = (v[i - 1].dp_du - wi * dot(wi, v[i - 1].dp_du)) * ili;
+            dv = (v[i - 1].dp_dv - wi * dot(wi, v[i - 1].dp_dv)) * ili;
+            du -= h * dot(du, h); dv -= h * dot(dv, h);
+            if (eta != 1.f) { du *= -1.f; dv *= -1.f; }
+            b[i].prev.m[0][0] = dot(s, du); b[i].prev.m[0][1] = dot(s, dv);
+            b[i].prev.m[1][0] = dot(t, du); b[i].prev.m[1][1] = dot(t, dv);
+        }
+        du = -v[i].dp_du * (ili + ilo) + wi * (dot(wi, v[i].dp_du) * ili) + wo * (dot(wo, v[i].dp_du) * ilo);
+        dv = -v[i].dp_dv * (ili + ilo) + wi * (dot(wi, v[i].dp_dv) * ili) + wo * (dot(wo, v[i].dp_dv) * ilo);
+        du -= h * dot(du, h); dv -= h * dot(dv, h);
+        if (eta != 1.f) { du *= -1.f; dv *= -1.f; }
+        float hn = dot(h, v[i].n), hdu = dot(h, v[i].dn_du), hdv = dot(h, v[i].dn_dv);
+        b[i].cur.m[0][0] = dot(du, s) - dot(v[i].dp_du, v[i].dn_du) * hn - dpdu_n * hdu;
+        b[i].cur.m[0][1] = dot(dv, s) - dot(v[i].dp_du, v[i].dn_dv) * hn - dpdu_n * hdv;
+        b[i].cur.m[1][0] = dot(du, t) - dot(v[i].dp_dv, v[i].dn_du) * hn - dpdv_n * hdu;
+        b[i].cur.m[1][1] = dot(dv, t) - dot(v[i].dp_dv, v[i].dn_dv) * hn - dpdv_n * hdv;
+        du = (v[i + 1].dp_du - wo * dot(wo, v[i + 1].dp_du)) * ilo;
+        dv = (v[i + 1].dp_dv - wo * dot(wo, v[i + 1].dp_dv)) * ilo;
+        du -= h * dot(du, h); dv -= h * dot(dv, h);
+        if (eta != 1.f) { du *= -1.f; dv *= -1.f; }
+        b[i].next.m[0][0] = dot(s, du); b[i].next.m[0][1] = dot(s, dv);
+        b[i].next.m[1][0] = dot(t, du); b[i].next.m[1][1] = dot(t, dv);
+    }
+    float dx1_dxend = invert_tridiagonal_geo(b);
+    V3 d = vx.p - v[0].p;
+    float inv_r2 = 1.f / dot(d, d);
+    d *= std::sqrt(inv_r2);
+    return std::fabs(dot(d, v[0].gn)) * inv_r2 * dx1_dxend;
+}
+
+/* manifold_ms.cpp:229-278 */
+static V3 ms_contribution(const Scene &sc, const Query &q, const EI &ei_in, const std::vector<MVertex> &path_in) {
+    EI ei = ei_in;
+    const MVertex &last = path_in.back();
+    if (ei.is_point) {
+        const Emitter &e = sc.emitters[ei.emitter];
+        V3 d = e.p - last.p;
+        float dist = norm(d);
+        float inv = 1.f / dist;
+        V3 spec = e.radiance * (inv * inv);
+        float emitter_pdf = ei.pdf;
+        ei.p = e.p;
+        ei.pdf = 1.f;
+        ei.weight = (spec * dist) * dist;
+        ei.pdf *= emitter_pdf;
+        ei.weight = ei.weight * (1.f / emitter_pdf);
+    }
+    MVertex vy;
+    if (!emitter_vertex(sc, ei, last.p, vy)) return V3(0.f);
+    std::vector<MVertex> path = path_in;
+    for (MVertex &v : path) make_orthonormal(v);
+    MVertex vx;
+    vx.p = q.p; vx.dp_du = q.dp_du; vx.dp_dv = q.dp_dv; vx.gn = q.n; vx.n = q.n;
+    vx.dn_du = V3(0.f); vx.dn_dv = V3(0.f);
+    make_orthonormal(vx);
+    float f = ms_specular_reflectance(sc, q.p, ei.p, path);
+    f *= ms_geometric_term(vx, path, vy);
+    return V3(f * ei.weight.x, f * ei.weight.y, f * ei.weight.z);
+}
+
+/* manifold_ms.cpp:27-201 */
+static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG32 &rng, int &count_out,
+                     int &walks_out, Stats &st) {
+    count_out = 0; walks_out = 0;
+    EI ei = sample_emitter_interaction(sc, sc.emitters_ms, q, rng);
+    V3 result(0.f);
+    if (sc.casters_ms.empty() || ei.emitter < 0) return result;
+    st.connections++;
+    for (int caster : sc.casters_ms) {
+        V3 value(0.f);
+        std::vector<int> tmpl;
+        std::vector<MVertex> path;
+        int it = 0;
+        bool seed_ok;
+        if (!cfg.biased) {
+            count_out = 0;
+            bool ok = ms_sample_path(sc, cfg, caster, q, ei.p, rng.next_2d(), V3(0.f), tmpl, true, path, it, seed_ok);
+            walks_out++; st.walks++; st.newton += it;
+            if (!ok) { st.failed++; continue; }
+            st.succeeded++;
+            V3 direction = normalize(path[0].p - q.p);
+            V3 spec = ms_contribution(sc, q, ei, path);
+            V3 bsdf = diffuse_eval(q, direction);
+            float inv_prob = 1.f;
+            int iterations = 1;
+            st.calls++;
+            while (true) {
+                std::vector<MVertex> tp;
+                int it2 = 0;
+                bool ok2 = ms_sample_path(sc, cfg, caster, q, ei.p, rng.next_2d(), V3(0.f), tmpl, false, tp, it2, seed_ok);
+                walks_out++; st.walks++; st.newton += it2;
+                if (ok2 && std::fabs(dot(direction, normalize(tp[0].p - q.p)) - 1.f) < cfg.uniqueness_threshold) break;
+                inv_prob += 1.f;
+                iterations++;
+                if (cfg.max_trials > 0 && iterations > cfg.max_trials) { inv_prob = 0.f; break; }
+            }
+            st.iters += (uint64_t)iterations;
+            update_max(st.iters_max, (uint64_t)iterations);
+            count_out = inv_prob == 0.f ? -1 : iterations;
+            value = bsdf * spec * inv_prob;
+        } else {
+            std::vector<V3> solutions;
+            for (int m = 0; m < cfg.max_trials; ++m) {
+                bool first = tmpl.empty();
+                bool ok = ms_sample_path(sc, cfg, caster, q, ei.p, rng.next_2d(), V3(0.f), tmpl, first, path, it, seed_ok);
+                if (!seed_ok && first) tmpl.clear();
+                walks_out++; st.walks++; st.newton += it;
+                if (!ok) { st.failed++; continue; }
+                st.succeeded++;
+                V3 direction = normalize(path[0].p - q.p);
+                bool dup = false;
+                for (const V3 &s : solutions)
+                    if (std::fabs(dot(direction, s) - 1.f) < cfg.uniqueness_threshold) { dup = true; break; }
+                if (dup) continue;
+                solutions.push_back(direction);
+                V3 bsdf = diffuse_eval(q, direction);
+                V3 spec = ms_contribution(sc, q, ei, path);
                 value += bsdf * spec;
             }
             count_out += (int)solutions.size();
@@ -1226,6 +1706,68 @@ int oracle_ss_connect_batch(void *s, const sms_config *cfg, const float *queries
                 rng.seed(seed, (uint64_t)i + stream_offset);
                 int c = 0, w = 0;
                 V3 v = ss_connect(*sc, *cfg, q, rng, c, w, st);
+                value[i] = v.x; value[(size_t)n + i] = v.y; value[2 * (size_t)n + i] = v.z;
+                count[i] = c; walks[i] = w;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
+    worker();
+    for (auto &t : th) t.join();
+    if (stats_out) {
+        stats_out[0] = st.succeeded; stats_out[1] = st.failed; stats_out[2] = st.calls;
+        stats_out[3] = st.iters; stats_out[4] = st.iters_max; stats_out[5] = st.walks;
+        stats_out[6] = st.newton; stats_out[7] = st.connections;
+    }
+    return 0;
+}
+
+/* Multi-scatter per-walk: first-path sample_path with explicit light point and
+ * start point (walk_in rows: ei.p (3), p_start (3), sample (2)); out rows: ok,
+ * iterations, p of the first vertex (3), p of the last vertex (3), seed ok. */
+int oracle_ms_walk_batch(void *s, const sms_config *cfg, int caster, const float *queries, const float *walk_in,
+                         uint32_t n, float *out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    for (uint32_t i = 0; i < n; ++i) {
+        Query q = load_query(queries, n, i);
+        auto w = [&](int k) { return walk_in[(size_t)k * n + i]; };
+        V3 lp(w(0), w(1), w(2)), ps(w(3), w(4), w(5));
+        V2 smp; smp.x = w(6); smp.y = w(7);
+        std::vector<int> tmpl;
+        std::vector<MVertex> path;
+        int it = 0;
+        bool seed_ok = false;
+        bool ok = ms_sample_path(*sc, *cfg, caster, q, lp, smp, ps, tmpl, true, path, it, seed_ok);
+        float vals[9] = {ok ? 1.f : 0.f, (float)it, 0, 0, 0, 0, 0, 0, seed_ok ? 1.f : 0.f};
+        if (ok) {
+            vals[2] = path[0].p.x; vals[3] = path[0].p.y; vals[4] = path[0].p.z;
+            vals[5] = path.back().p.x; vals[6] = path.back().p.y; vals[7] = path.back().p.z;
+        }
+        for (int k = 0; k < 9; ++k) out[(size_t)k * n + i] = vals[k];
+    }
+    return 0;
+}
+
+int oracle_ms_connect_batch(void *s, const sms_config *cfg, const float *queries, uint32_t n, uint64_t seed,
+                            uint64_t stream_offset, float *value, int32_t *count, int32_t *walks, int nthreads,
+                            uint64_t *stats_out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    Stats st;
+    if (nthreads < 1) nthreads = 1;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        while (true) {
+            uint32_t b = next.fetch_add(16);
+            if (b >= n) break;
+            for (uint32_t i = b; i < std::min(n, b + 16); ++i) {
+                Query q = load_query(queries, n, i);
+                PCG32 rng;
+                rng.seed(seed, (uint64_t)i + stream_offset);
+                int c = 0, w = 0;
+                V3 v = ms_connect(*sc, *cfg, q, rng, c, w, st);
                 value[i] = v.x; value[(size_t)n + i] = v.y; value[2 * (size_t)n + i] = v.z;
                 count[i] = c; walks[i] = w;
             }

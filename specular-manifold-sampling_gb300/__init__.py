@@ -30,6 +30,7 @@ QUERY_FIELDS = 16
 NOALLOC_MAX_QUERIES = 1 << 18
 WALK_IN_FIELDS = 8
 WALK_OUT_FIELDS = 11
+MS_WALK_OUT_FIELDS = 9
 
 SHAPE_CAUSTIC_RECEIVER = 1 << 0
 SHAPE_CAUSTIC_CASTER_SINGLE = 1 << 1
@@ -122,6 +123,9 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ss_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ss_walk_batch": (i32, [vp, i32, vp, vp, u32, vp]),
         "sms_ss_connect_batch_noalloc": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
+        "sms_ms_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
+        "sms_ms_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
+        "sms_ms_walk_batch": (i32, [vp, i32, vp, vp, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -379,4 +383,38 @@ class SpecularManifoldSingleScatter:
         w = _soa(walk_in, WALK_IN_FIELDS, n)
         out = np.zeros((WALK_OUT_FIELDS, n), np.float32)
         _check(_LIB.sms_ss_walk_batch(self.ctx.handle, caster, _ptr(q), _ptr(w), n, _ptr(out)))
+        return out
+
+
+class SpecularManifoldMultiScatter:
+    """Batched SpecularManifoldMultiScatter (include/mitsuba/render/manifold_ms.h);
+    the chain length is config.bounces."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def specular_manifold_sampling(self, queries: np.ndarray, seed: int = 0, stream_offset: int = 0):
+        n = queries.shape[1]
+        q = _soa(queries, QUERY_FIELDS, n)
+        value = np.zeros((3, n), np.float32)
+        count = np.zeros(n, np.int32)
+        walks = np.zeros(n, np.int32)
+        r = _Result(_ptr(value), _ptr(count), _ptr(walks))
+        _check(_LIB.sms_ms_connect_batch(self.ctx.handle, _ptr(q), n, seed, stream_offset, C.byref(r)))
+        return value, count, walks
+
+    def specular_manifold_sampling_device(self, queries_ptr: int, n: int, value_ptr: int, count_ptr: int,
+                                          walks_ptr: int, seed: int = 0, stream_offset: int = 0):
+        r = _Result(value_ptr, count_ptr, walks_ptr)
+        _check(_LIB.sms_ms_connect_batch_device(self.ctx.handle, queries_ptr, n, seed, stream_offset,
+                                                C.byref(r)))
+
+    def sample_path(self, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
+        """First-path walks with explicit light point / start point; returns
+        (9, n): ok, iterations, first vertex (3), last vertex (3), seed ok."""
+        n = queries.shape[1]
+        q = _soa(queries, QUERY_FIELDS, n)
+        w = _soa(walk_in, WALK_IN_FIELDS, n)
+        out = np.zeros((MS_WALK_OUT_FIELDS, n), np.float32)
+        _check(_LIB.sms_ms_walk_batch(self.ctx.handle, caster, _ptr(q), _ptr(w), n, _ptr(out)))
         return out

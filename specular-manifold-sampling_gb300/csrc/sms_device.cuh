@@ -152,6 +152,11 @@ struct Pcg32 {
 
 // --------------------------------------------------------------- scene data
 enum : int { kShapeSphere = 0, kShapeMesh = 1 };
+// shape flags (same bits as SMS_SHAPE_* in sms_gb300.h)
+constexpr uint32_t kShapeFlagCasterSingle = 1u << 1;
+constexpr uint32_t kShapeFlagCasterMulti = 1u << 2;
+constexpr uint32_t kShapeFlagBouncer = 1u << 3;
+constexpr uint32_t kShapeFlagGlinty = 1u << 4;
 enum : int { kBsdfDiffuse = 0, kBsdfDielectric = 1, kBsdfConductor = 2 };
 
 struct DevShape {
@@ -204,6 +209,8 @@ struct DevScene {
     // caustic lists (scene.cpp:95-112)
     int n_casters_ss, casters_ss[kMaxCasters];
     int n_emitters_ss, emitters_ss[kMaxEmitters];
+    int n_casters_ms, casters_ms[kMaxCasters];
+    int n_emitters_ms, emitters_ms[kMaxEmitters];
     const DevEmitter *emitters;
 };
 

@@ -1,0 +1,166 @@
+// sms_estimator.cuh -- device helpers shared by the SMS estimators: counters,
+// shading-point queries, emitter sampling, light visibility, emitter vertex,
+// diffuse receiver.
+#pragma once
+#include "sms_device.cuh"
+#include "sms_kernels.h"
+
+namespace sms {
+
+#define SMS_D __device__ __forceinline__
+
+// ------------------------------------------------------------- statistics
+struct LaneStats {
+    unsigned long long succ = 0, fail = 0, calls = 0, iters = 0, imax = 0, walks = 0, newton = 0, conns = 0,
+                       rays = 0, nodes = 0, tris = 0, spec = 0;
+    SMS_D void ray(const Hit &h) {
+        rays++;
+        nodes += h.nodes;
+        tris += h.tests;
+    }
+};
+
+// Warp-aggregated counter update; all 32 lanes must call it.
+SMS_D void flush_stats(const LaneStats &st, DevCounters *ctr, uint32_t err, int phase) {
+    unsigned long long v[11] = {st.succ, st.fail, st.calls, st.iters, st.walks, st.newton, st.conns,
+                                st.rays, st.nodes, st.tris, st.spec};
+    unsigned long long *dst[11] = {&ctr->solver_succeeded, &ctr->solver_failed, &ctr->bernoulli_calls,
+                                   &ctr->bernoulli_iters, &ctr->walks, &ctr->newton_iters, &ctr->connections,
+                                   &ctr->rays, &ctr->bvh_nodes, &ctr->tri_tests, &ctr->speculative_walks};
+    const unsigned full = 0xffffffffu;
+    #pragma unroll
+    for (int k = 0; k < 11; ++k) {
+        unsigned long long s = v[k];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(full, s, off);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst[k], s);
+    }
+    unsigned long long pv[3] = {st.rays, st.nodes, st.tris};
+    unsigned long long *pd[3] = {&ctr->phase_rays[phase], &ctr->phase_nodes[phase], &ctr->phase_tris[phase]};
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        unsigned long long s = pv[k];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(full, s, off);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(pd[k], s);
+    }
+    unsigned long long m = st.imax;
+    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(full, m, off));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ctr->bernoulli_max, m);
+    unsigned e = err;
+    for (int off = 16; off > 0; off >>= 1) e |= __shfl_xor_sync(full, e, off);
+    if ((threadIdx.x & 31) == 0 && e) atomicOr(&ctr->error, e);
+}
+
+// ------------------------------------------------------------ query / light
+struct Query {
+    f3 x, n, albedo;
+    float cos_i;
+};
+
+SMS_D Query load_query(const float *__restrict__ q, uint32_t n, uint32_t i) {
+    auto Q = [&](int k) { return __ldg(q + (size_t)k * n + i); };
+    Query r;
+    r.x = mk(Q(0), Q(1), Q(2));
+    r.n = mk(Q(3), Q(4), Q(5));
+    r.albedo = mk(Q(12), Q(13), Q(14));
+    r.cos_i = Q(15);
+    return r;
+}
+
+struct Light {
+    int eidx, kind;   // kind 0 point, 1 area sphere
+    int n_list;       // size of the emitter list it was drawn from
+    f3 p, w;          // ei.p, ei.weight
+};
+
+// sample_emitter_interaction (manifold.h:204-260) over an emitter list
+// (caustic_emitters_single_scatter or _multi_scatter): 3 draws.
+SMS_D bool sample_emitter(const DevScene &sc, const int *list, int ne, Pcg32 &rng, f3 x, Light &L) {
+    if (ne == 0) return false;
+    float es = rng.next_f32();
+    float emitter_pdf = 1.f / (float)ne;
+    uint32_t idx = min((uint32_t)(es * (float)ne), (uint32_t)ne - 1);
+    L.eidx = list[idx];
+    L.n_list = ne;
+    const DevEmitter &e = sc.emitters[L.eidx];
+    L.kind = e.kind;
+    float sx = rng.next_f32(), sy = rng.next_f32();
+    f3 spec;
+    if (e.kind == 1) {
+        const DevShape &ls = sc.shapes[e.shape];
+        L.p = sample_position(sc, ls, sx, sy);
+        float pdf = 1.f / (4.f * kPi * ls.radius * ls.radius);
+        spec = mk(e.r / pdf, e.g / pdf, e.b / pdf);
+    } else {
+        L.p = mk(e.px, e.py, e.pz);
+        f3 d = L.p - x;
+        float dist = length(d);
+        float inv = 1.f / dist;
+        spec = mk(e.r, e.g, e.b) * (inv * inv);
+        spec = (spec * dist) * dist;
+    }
+    L.w = spec * (1.f / emitter_pdf);
+    return true;
+}
+
+SMS_D Pcg32 query_rng(uint64_t seed, uint64_t stream, uint64_t position) {
+    Pcg32 r;
+    r.seed(seed, stream);
+    if (position) r.advance(position);
+    return r;
+}
+
+// Light-to-solution visibility (manifold_ss.cpp:88-102).
+SMS_D bool visible(const DevScene &sc, f3 lp, f3 p, uint32_t &err, LaneStats &st) {
+    f3 d = p - lp;
+    float dist = length(d);
+    d = d * (1.f / dist);
+    float mint = kRayEps * (1.f + fmaxf(fabsf(lp.x), fmaxf(fabsf(lp.y), fabsf(lp.z))));
+    Hit h;
+    bool occ = trace(sc, lp, d, mint, dist * (1.f - kRayEps), true, h, err);
+    st.ray(h);
+    return !occ;
+}
+
+// Emitter endpoint of the generalized geometric term (manifold.h:264-302) and
+// the emitter weight for a solution whose last specular vertex is at p.
+// Point lights are re-sampled from p (manifold_ss.cpp:291-312, manifold_ms.cpp:
+// 234-257); area lights cast one ray toward the light sample.
+SMS_D bool emitter_endpoint(const DevScene &sc, const Light &L, f3 p, f3 &yp, f3 &ydu, f3 &ydv, f3 &lw, f3 &lp,
+                            uint32_t &err, LaneStats &st) {
+    lw = L.w;
+    lp = L.p;
+    if (L.kind == 1) {
+        f3 d = normalize(lp - p);
+        f3 o = p + d * kShadowEps;
+        Hit h;
+        trace(sc, o, d, kRayEps, INFINITY, false, h, err);
+        st.ray(h);
+        if (h.shape < 0) return false;
+        Vtx vy;
+        vertex_from_hit(sc, o, d, h, vy);
+        make_orthonormal(vy.dp_du, vy.dp_dv, vy.dn_du, vy.dn_dv);
+        yp = vy.p; ydu = vy.dp_du; ydv = vy.dp_dv;
+        return true;
+    }
+    const DevEmitter &e = sc.emitters[L.eidx];
+    lp = mk(e.px, e.py, e.pz);
+    f3 d = lp - p;
+    float dist = length(d);
+    float inv = 1.f / dist;
+    float emitter_pdf = 1.f / (float)L.n_list;
+    f3 spec = mk(e.r, e.g, e.b) * (inv * inv);
+    lw = (spec * dist) * dist;
+    lw = lw * (1.f / emitter_pdf);
+    yp = lp;
+    onb(normalize(p - lp), ydu, ydv);
+    return true;
+}
+
+// Diffuse receiver (src/bsdfs/diffuse.cpp): albedo / pi * cos_o.
+SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
+    float co = dot(dir, Q.n);
+    if (Q.cos_i <= 0.f || co <= 0.f) return splat(0.f);
+    return (Q.albedo * kInvPi) * co;
+}
+
+}  // namespace sms

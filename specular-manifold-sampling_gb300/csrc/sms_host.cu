@@ -326,9 +326,11 @@ struct sms_ctx {
     // device staging for the host-pointer entry points
     void *io = nullptr;
     size_t io_bytes = 0;
-    // per-query scratch of the unbiased estimator
+    // per-query scratch of the unbiased estimators
     void *scratch = nullptr;
     uint32_t scratch_n = 0;
+    int *ms_tmpl = nullptr;       // multi-scatter template shapes, kMaxBounces x n
+    uint32_t ms_tmpl_n = 0;
     PhaseTimer timer;
     std::vector<int> casters_ss;
 };
@@ -373,6 +375,7 @@ extern "C" void sms_ctx_destroy(sms_ctx *c) {
     for (void *p : c->allocs) cudaFree(p);
     if (c->io) cudaFree(c->io);
     if (c->scratch) cudaFree(c->scratch);
+    if (c->ms_tmpl) cudaFree(c->ms_tmpl);
     if (c->ctr) cudaFree(c->ctr);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -451,6 +454,10 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
             if (d.n_casters_ss >= kMaxCasters) return fail(SMS_ERR_UNSUPPORTED, "too many casters");
             d.casters_ss[d.n_casters_ss++] = (int)i;
         }
+        if (h.flags & SMS_SHAPE_CAUSTIC_CASTER_MULTI) {
+            if (d.n_casters_ms >= kMaxCasters) return fail(SMS_ERR_UNSUPPORTED, "too many casters");
+            d.casters_ms[d.n_casters_ms++] = (int)i;
+        }
         shapes.push_back(ds);
     }
     std::vector<DevEmitter> em;
@@ -466,6 +473,10 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         if (h.flags & SMS_EMITTER_CAUSTIC_SINGLE) {
             if (d.n_emitters_ss >= kMaxEmitters) return fail(SMS_ERR_UNSUPPORTED, "too many emitters");
             d.emitters_ss[d.n_emitters_ss++] = (int)i;
+        }
+        if (h.flags & SMS_EMITTER_CAUSTIC_MULTI) {
+            if (d.n_emitters_ms >= kMaxEmitters) return fail(SMS_ERR_UNSUPPORTED, "too many emitters");
+            d.emitters_ms[d.n_emitters_ms++] = (int)i;
         }
     }
     // BVH over all mesh triangles
@@ -751,4 +762,100 @@ bool ctx_view(sms_ctx *c, CtxView &out) {
 int set_last_error_impl(int st, const char *msg) {
     g_last_error = msg ? msg : "";
     return st;
+}
+
+// -------------------------------------------------------------- multi scatter
+static sms_status check_ms_cfg(sms_ctx *c) {
+    if (c->cfg.bounces < 1 || c->cfg.bounces > kMaxBounces)
+        return fail(SMS_ERR_UNSUPPORTED, "bounces must be between 1 and 4");
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_ms_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                                  uint64_t stream_off, sms_result *out) {
+    if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
+        return fail(SMS_ERR_INVALID_ARG, "sms_ms_connect_batch_device: null argument");
+    if (sms_status st = check_ms_cfg(c)) return st;
+    if (n == 0) return SMS_OK;
+    if (c->cfg.biased && c->cfg.max_trials > (1 << 24))
+        return fail(SMS_ERR_INVALID_ARG, "max_trials too large for the biased estimator");
+    CUDA_TRY(cudaSetDevice(c->device));
+    SsScratch scr{};
+    if (!c->cfg.biased) {
+        if (sms_status st = ensure_scratch(c, n, scr)) return st;
+        if (c->ms_tmpl_n < n) {
+            if (c->ms_tmpl) {
+                CUDA_TRY(cudaStreamSynchronize(c->stream));
+                cudaFree(c->ms_tmpl);
+                c->ms_tmpl = nullptr;
+                c->ms_tmpl_n = 0;
+            }
+            CUDA_TRY(cudaMalloc(&c->ms_tmpl, (size_t)kMaxBounces * n * sizeof(int)));
+            c->ms_tmpl_n = n;
+        }
+    }
+    CUDA_TRY(launch_ms_connect(c->dsc, solver_cfg(c->cfg), c->cfg.bounces, q, n, seed, stream_off, out->value,
+                               out->count, out->walks, c->ctr, scr, c->ms_tmpl, c->num_sms, c->blocks_per_sm,
+                               &c->timer, c->stream));
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_ms_connect_batch(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                           uint64_t stream_off, sms_result *out) {
+    if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
+        return fail(SMS_ERR_INVALID_ARG, "sms_ms_connect_batch: null argument");
+    if (sms_status st = check_ms_cfg(c)) return st;
+    if (n == 0) return SMS_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    size_t qb = (size_t)SMS_QUERY_FIELDS * n * sizeof(float);
+    size_t vb = 3 * (size_t)n * sizeof(float), ib = (size_t)n * sizeof(int32_t);
+    if (sms_status st = ensure_io(c, qb + vb + 2 * ib)) return st;
+    char *dbuf = reinterpret_cast<char *>(c->io);
+    float *dq = reinterpret_cast<float *>(dbuf);
+    sms_result r{reinterpret_cast<float *>(dbuf + qb), reinterpret_cast<int32_t *>(dbuf + qb + vb),
+                 reinterpret_cast<int32_t *>(dbuf + qb + vb + ib)};
+    sms_status st = SMS_OK;
+    do {
+        cudaError_t e = cudaMemcpyAsync(dq, q, qb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy queries"); break; }
+        st = sms_ms_connect_batch_device(c, dq, n, seed, stream_off, &r);
+        if (st) break;
+        e = cudaMemcpyAsync(out->value, r.value, vb, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->count, r.count, ib, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->walks, r.walks, ib, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy results"); break; }
+    } while (0);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "sms_ms_connect_batch");
+    return check_device_error(c);
+}
+
+extern "C" sms_status sms_ms_walk_batch(sms_ctx *c, int32_t caster, const float *q, const float *w, uint32_t n,
+                                        float *out) {
+    if (!c || (n && (!q || !w || !out))) return fail(SMS_ERR_INVALID_ARG, "sms_ms_walk_batch: null argument");
+    if (caster < 0 || caster >= c->dsc.n_shapes) return fail(SMS_ERR_INVALID_ARG, "unknown caster shape id");
+    if (sms_status st = check_ms_cfg(c)) return st;
+    if (n == 0) return SMS_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    size_t qb = (size_t)SMS_QUERY_FIELDS * n * sizeof(float), wb = (size_t)SMS_WALK_IN_FIELDS * n * sizeof(float),
+           ob = (size_t)SMS_MS_WALK_OUT_FIELDS * n * sizeof(float);
+    if (sms_status st = ensure_io(c, qb + wb + ob)) return st;
+    char *dbuf = reinterpret_cast<char *>(c->io);
+    sms_status st = SMS_OK;
+    do {
+        cudaError_t e = cudaMemcpyAsync(dbuf, q, qb, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dbuf + qb, w, wb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy walk inputs"); break; }
+        e = launch_ms_walk(c->dsc, solver_cfg(c->cfg), c->cfg.bounces, caster, reinterpret_cast<float *>(dbuf),
+                           reinterpret_cast<float *>(dbuf + qb), n, reinterpret_cast<float *>(dbuf + qb + wb), c->ctr,
+                           &c->timer, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "launch ms_walk"); break; }
+        e = cudaMemcpyAsync(out, dbuf + qb + wb, ob, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy walk outputs"); break; }
+    } while (0);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "sms_ms_walk_batch");
+    return check_device_error(c);
 }

@@ -32,8 +32,11 @@ constexpr int kMaxSolutions = 64;
 // Bernoulli trials are unbounded in the reference when max_trials <= 0
 // (manifold_ss.cpp:127); the device loop stops here and flags the query.
 constexpr int kTrialHardLimit = 1 << 16;
-// Rows of the per-walk output (sms_ss_walk_batch).
+// Rows of the per-walk outputs (sms_ss_walk_batch, sms_ms_walk_batch).
 constexpr int kWalkOutFields = 11;
+constexpr int kMsWalkOutFields = 9;
+// Longest specular chain of the multi-scatter kernels.
+constexpr int kMaxBounces = 4;
 
 // Per-query scratch of the unbiased estimator (device memory, n entries):
 // stream position after the walks done so far, first-walk direction and
@@ -53,6 +56,13 @@ cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster,
 cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n,
                               uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
                               DevCounters *ctr, const SsScratch &scr, int num_sms, int blocks_per_sm,
+                              PhaseTimer *tm, cudaStream_t s);
+
+cudaError_t launch_ms_walk(const DevScene &sc, const SolverCfg &cfg, int bounces, int caster, const float *q,
+                           const float *w, uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s);
+cudaError_t launch_ms_connect(const DevScene &sc, const SolverCfg &cfg, int bounces, const float *q, uint32_t n,
+                              uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
+                              DevCounters *ctr, const SsScratch &scr, int *tmpl, int num_sms, int blocks_per_sm,
                               PhaseTimer *tm, cudaStream_t s);
 
 // Read-only view of a context for entry points defined outside sms_host.cu.

@@ -29,109 +29,10 @@
 #include <algorithm>
 
 #include "sms_device.cuh"
+#include "sms_estimator.cuh"
 #include "sms_kernels.h"
 
 namespace sms {
-
-#define SMS_D __device__ __forceinline__
-
-// ------------------------------------------------------------- statistics
-struct LaneStats {
-    unsigned long long succ = 0, fail = 0, calls = 0, iters = 0, imax = 0, walks = 0, newton = 0, conns = 0,
-                       rays = 0, nodes = 0, tris = 0, spec = 0;
-    SMS_D void ray(const Hit &h) {
-        rays++;
-        nodes += h.nodes;
-        tris += h.tests;
-    }
-};
-
-// Warp-aggregated counter update; all 32 lanes must call it.
-SMS_D void flush_stats(const LaneStats &st, DevCounters *ctr, uint32_t err, int phase) {
-    unsigned long long v[11] = {st.succ, st.fail, st.calls, st.iters, st.walks, st.newton, st.conns,
-                                st.rays, st.nodes, st.tris, st.spec};
-    unsigned long long *dst[11] = {&ctr->solver_succeeded, &ctr->solver_failed, &ctr->bernoulli_calls,
-                                   &ctr->bernoulli_iters, &ctr->walks, &ctr->newton_iters, &ctr->connections,
-                                   &ctr->rays, &ctr->bvh_nodes, &ctr->tri_tests, &ctr->speculative_walks};
-    const unsigned full = 0xffffffffu;
-    #pragma unroll
-    for (int k = 0; k < 11; ++k) {
-        unsigned long long s = v[k];
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(full, s, off);
-        if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst[k], s);
-    }
-    unsigned long long pv[3] = {st.rays, st.nodes, st.tris};
-    unsigned long long *pd[3] = {&ctr->phase_rays[phase], &ctr->phase_nodes[phase], &ctr->phase_tris[phase]};
-    #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        unsigned long long s = pv[k];
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(full, s, off);
-        if ((threadIdx.x & 31) == 0 && s) atomicAdd(pd[k], s);
-    }
-    unsigned long long m = st.imax;
-    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(full, m, off));
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ctr->bernoulli_max, m);
-    unsigned e = err;
-    for (int off = 16; off > 0; off >>= 1) e |= __shfl_xor_sync(full, e, off);
-    if ((threadIdx.x & 31) == 0 && e) atomicOr(&ctr->error, e);
-}
-
-// ------------------------------------------------------------ query / light
-struct Query {
-    f3 x, n, albedo;
-    float cos_i;
-};
-
-SMS_D Query load_query(const float *__restrict__ q, uint32_t n, uint32_t i) {
-    auto Q = [&](int k) { return __ldg(q + (size_t)k * n + i); };
-    Query r;
-    r.x = mk(Q(0), Q(1), Q(2));
-    r.n = mk(Q(3), Q(4), Q(5));
-    r.albedo = mk(Q(12), Q(13), Q(14));
-    r.cos_i = Q(15);
-    return r;
-}
-
-struct Light {
-    int eidx, kind;   // kind 0 point, 1 area sphere
-    f3 p, w;          // ei.p, ei.weight
-};
-
-// sample_emitter_interaction (manifold.h:204-260): 3 draws.
-SMS_D bool sample_emitter(const DevScene &sc, Pcg32 &rng, f3 x, Light &L) {
-    int ne = sc.n_emitters_ss;
-    if (ne == 0) return false;
-    float es = rng.next_f32();
-    float emitter_pdf = 1.f / (float)ne;
-    uint32_t idx = min((uint32_t)(es * (float)ne), (uint32_t)ne - 1);
-    L.eidx = sc.emitters_ss[idx];
-    const DevEmitter &e = sc.emitters[L.eidx];
-    L.kind = e.kind;
-    float sx = rng.next_f32(), sy = rng.next_f32();
-    f3 spec;
-    if (e.kind == 1) {
-        const DevShape &ls = sc.shapes[e.shape];
-        L.p = sample_position(sc, ls, sx, sy);
-        float pdf = 1.f / (4.f * kPi * ls.radius * ls.radius);
-        spec = mk(e.r / pdf, e.g / pdf, e.b / pdf);
-    } else {
-        L.p = mk(e.px, e.py, e.pz);
-        f3 d = L.p - x;
-        float dist = length(d);
-        float inv = 1.f / dist;
-        spec = mk(e.r, e.g, e.b) * (inv * inv);
-        spec = (spec * dist) * dist;
-    }
-    L.w = spec * (1.f / emitter_pdf);
-    return true;
-}
-
-SMS_D Pcg32 query_rng(uint64_t seed, uint64_t stream, uint64_t position) {
-    Pcg32 r;
-    r.seed(seed, stream);
-    if (position) r.advance(position);
-    return r;
-}
 
 // ------------------------------------------------------------------- walk
 // sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
@@ -176,59 +77,15 @@ SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f
     return (v.eta == 1.f) ? !refraction : refraction;
 }
 
-// Light-to-solution visibility (manifold_ss.cpp:88-102).
-SMS_D bool visible(const DevScene &sc, f3 lp, f3 p, uint32_t &err, LaneStats &st) {
-    f3 d = p - lp;
-    float dist = length(d);
-    d = d * (1.f / dist);
-    float mint = kRayEps * (1.f + fmaxf(fabsf(lp.x), fmaxf(fabsf(lp.y), fabsf(lp.z))));
-    Hit h;
-    bool occ = trace(sc, lp, d, mint, dist * (1.f - kRayEps), true, h, err);
-    st.ray(h);
-    return !occ;
-}
-
 // evaluate_path_contribution (manifold_ss.cpp:281-327) for a flat receiver.
 SMS_D f3 contribution(const DevScene &sc, f3 x, const Light &L, const Vtx &sol, uint32_t &err, LaneStats &st) {
     Vtx vt = sol;
     make_orthonormal(vt.dp_du, vt.dp_dv, vt.dn_du, vt.dn_dv);
-    f3 lw = L.w, lp = L.p, yp, ydu, ydv;
-    if (L.kind == 1) {
-        // emitter vertex by one ray toward the light sample (manifold.h:264-279)
-        f3 d = normalize(lp - vt.p);
-        f3 o = vt.p + d * kShadowEps;
-        Hit h;
-        trace(sc, o, d, kRayEps, INFINITY, false, h, err);
-        st.ray(h);
-        if (h.shape < 0) return splat(0.f);
-        Vtx vy;
-        vertex_from_hit(sc, o, d, h, vy);
-        make_orthonormal(vy.dp_du, vy.dp_dv, vy.dn_du, vy.dn_dv);
-        yp = vy.p; ydu = vy.dp_du; ydv = vy.dp_dv;
-    } else {
-        // point light re-sampled from the solution (manifold_ss.cpp:291-312)
-        const DevEmitter &e = sc.emitters[L.eidx];
-        lp = mk(e.px, e.py, e.pz);
-        f3 d = lp - vt.p;
-        float dist = length(d);
-        float inv = 1.f / dist;
-        float emitter_pdf = 1.f / (float)sc.n_emitters_ss;
-        f3 spec = mk(e.r, e.g, e.b) * (inv * inv);
-        lw = (spec * dist) * dist;
-        lw = lw * (1.f / emitter_pdf);
-        yp = lp;
-        onb(normalize(vt.p - lp), ydu, ydv);
-    }
+    f3 yp, ydu, ydv, lw, lp;
+    if (!emitter_endpoint(sc, L, vt.p, yp, ydu, ydv, lw, lp, err, st)) return splat(0.f);
     float F = specular_reflectance(sc.shapes[vt.shape], vt.n, normalize(lp - vt.p));
     F *= geometric_term(x, vt, yp, ydu, ydv);
     return lw * F;
-}
-
-// Diffuse receiver (src/bsdfs/diffuse.cpp): albedo / pi * cos_o.
-SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
-    float co = dot(dir, Q.n);
-    if (Q.cos_i <= 0.f || co <= 0.f) return splat(0.f);
-    return (Q.albedo * kInvPi) * co;
 }
 
 // ------------------------------------------------------------ walk kernel
@@ -293,7 +150,7 @@ __global__ void __launch_bounds__(128) ss_biased_kernel(DevScene sc, SolverCfg c
         if (live) {
             Q = load_query(qs, n, qi);
             Pcg32 rng = query_rng(seed, stream_off + qi, 0);
-            have_light = sample_emitter(sc, rng, Q.x, L);
+            have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
         }
         bool work = live && have_light && sc.n_casters_ss > 0;
         if (work && gl == 0) st.conns++;
@@ -382,7 +239,7 @@ __global__ void __launch_bounds__(128) ss_first_kernel(DevScene sc, SolverCfg cf
         Query Q = load_query(qs, n, qi);
         Pcg32 rng = query_rng(seed, stream_off + qi, 0);
         Light L;
-        bool have_light = sample_emitter(sc, rng, Q.x, L);
+        bool have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
         uint32_t pos = 3u;
         f3 acc = splat(0.f);
         int nw = 0;
@@ -463,7 +320,7 @@ __global__ void __launch_bounds__(128) ss_trials_kernel(DevScene sc, SolverCfg c
         Query Q = load_query(qs, n, qi);
         Pcg32 base = query_rng(seed, stream_off + qi, 0);
         Light L;
-        sample_emitter(sc, base, Q.x, L);   // base now sits at position 3
+        sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, base, Q.x, L);   // base now sits at position 3
         uint32_t pos = scr.pos[qi];
         f3 dir0 = mk(scr.dir0[qi], scr.dir0[(size_t)n + qi], scr.dir0[2 * (size_t)n + qi]);
         int first = 0;   // 1-based index of the first successful trial

@@ -6,6 +6,11 @@ oracle and the tests see identical inputs.
   sphere_scene      glass sphere r=1 at (0,0,1.5), IOR 1.5, over the plane z=0,
                     point light (0,0,5) I=100; 64x64 query grid on [-2,2]^2;
                     biased SMS, 16 trials, 20 iterations, threshold 1e-5.
+  slab_scene        two-bounce glass slab (IOR 1.5): top face z = 1.3 + h1 and
+                    bottom face z = 1 + h2, with h1, h2 independent sums of 8
+                    sinusoids (total amplitude <= 0.01) on 256x256 vertex grids
+                    over [-1,1]^2; point light (0,0,5); queries uniform on
+                    [-1,1]^2; biased SMS, 32 trials, 30 iterations, 2 bounces.
   water_scene       z = 1 + sum of 32 sinusoids (a ~ U(0.002,0.02),
                     |k| ~ U(2,40), uniform direction and phase) tessellated to a
                     512x512 vertex grid over [-1,1]^2 (522,242 triangles), IOR
@@ -22,8 +27,9 @@ import math
 
 import numpy as np
 
-from . import (BSDF_CONDUCTOR, BSDF_DIELECTRIC, BSDF_DIFFUSE, EMITTER_CAUSTIC_SINGLE,
-               SHAPE_CAUSTIC_CASTER_SINGLE, QUERY_FIELDS, Bsdf, SceneDesc, SMSConfig)
+from . import (BSDF_CONDUCTOR, BSDF_DIELECTRIC, BSDF_DIFFUSE, EMITTER_CAUSTIC_MULTI, EMITTER_CAUSTIC_SINGLE,
+               SHAPE_CAUSTIC_BOUNCER, SHAPE_CAUSTIC_CASTER_MULTI, SHAPE_CAUSTIC_CASTER_SINGLE, QUERY_FIELDS, Bsdf,
+               SceneDesc, SMSConfig)
 
 _MUL = np.uint64(6364136223846793005)
 _M64 = (1 << 64) - 1
@@ -174,3 +180,39 @@ def water_queries(n: int, seed: int = 3, first: int = 0) -> np.ndarray:
 
 def water_config() -> SMSConfig:
     return SMSConfig(biased=False, max_trials=256, max_iterations=20)
+
+
+# ------------------------------------------------------------------- slab
+def slab_waves(seed: int, n_waves: int = 8):
+    r = Pcg32(seed, 0)
+    waves = []
+    for _ in range(n_waves):
+        a = 0.0005 + (0.00125 - 0.0005) * r.next_f32()
+        km = 2.0 + (20.0 - 2.0) * r.next_f32()
+        ang = 2.0 * math.pi * r.next_f32()
+        ph = 2.0 * math.pi * r.next_f32()
+        waves.append((a, km * math.cos(ang), km * math.sin(ang), ph))
+    return waves
+
+
+def slab_scene(res: int = 256) -> SceneDesc:
+    """Glass slab: top face caustic_caster_multi (normals up), bottom face
+    caustic_bouncer (normals down, i.e. outward), IOR 1.5; point light."""
+    d = SceneDesc()
+    glass = Bsdf(BSDF_DIELECTRIC, 1.5)
+    P, N, UV, F = heightfield_mesh(res, 1.0, 1.3, slab_waves(4))
+    d.add_mesh(P, F, glass, SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    P, N, UV, F = heightfield_mesh(res, 1.0, 1.0, slab_waves(5), flip_normals=True)
+    d.add_mesh(P, F, glass, SHAPE_CAUSTIC_BOUNCER, N=N, UV=UV)
+    d.add_point_emitter((0.0, 0.0, 5.0), (100.0, 100.0, 100.0), EMITTER_CAUSTIC_MULTI)
+    return d
+
+
+def slab_queries(n: int, seed: int = 6, first: int = 0) -> np.ndarray:
+    u = pcg32_streams_f32(seed, np.arange(first, first + n, dtype=np.uint64), 2)
+    xy = np.stack([2.0 * u[0] - 1.0, 2.0 * u[1] - 1.0], axis=1).astype(np.float32)
+    return plane_queries(xy)
+
+
+def slab_config() -> SMSConfig:
+    return SMSConfig(biased=True, max_trials=32, max_iterations=30, bounces=2)

@@ -134,3 +134,86 @@ def test_nan_walks_are_misses(sms, workloads, oracle):
     w[3:6, 0][2] = 1e-30  # non-zero so it counts as an explicit start, ~ the shading point
     out = o.walk_batch(sms.SMSConfig(), 0, q, w)
     assert out[0, 0] == 0.0
+
+
+def _flat_slab(sms, W):
+    """Two parallel glass faces z = 1 (bouncer, normals down) and z = 1.3
+    (caster_multi, normals up), IOR 1.5, point light (0.3, -0.2, 5)."""
+    d = sms.SceneDesc()
+    glass = sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)
+    P, N, UV, F = W.heightfield_mesh(8, 2.0, 1.3, [])
+    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    P, N, UV, F = W.heightfield_mesh(8, 2.0, 1.0, [], flip_normals=True)
+    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_BOUNCER, N=N, UV=UV)
+    d.add_point_emitter((0.3, -0.2, 5.0), (100.0, 100.0, 100.0), sms.EMITTER_CAUSTIC_MULTI)
+    return d
+
+
+def _slab_solution(x, light, h1=1.0, t=0.3, eta=1.5):
+    """Entry and exit points of the double refraction through a flat slab,
+    from a bisection on the incidence angle (FP64, independent of the oracle)."""
+    dxy = np.array(light[:2]) - np.array(x[:2])
+    D = np.linalg.norm(dxy)
+    h2 = light[2] - (h1 + t)
+    f = lambda th: h1 * math.tan(th) + t * math.tan(math.asin(math.sin(th) / eta)) + h2 * math.tan(th) - D
+    a, b = 0.0, math.pi / 2 - 1e-9
+    for _ in range(200):
+        m = 0.5 * (a + b)
+        a, b = (m, b) if f(m) < 0 else (a, m)
+    th = 0.5 * (a + b)
+    u = dxy / D
+    p1 = np.array([*(np.array(x[:2]) + h1 * math.tan(th) * u), h1])
+    th_t = math.asin(math.sin(th) / eta)
+    p2 = np.array([*(p1[:2] + t * math.tan(th_t) * u), h1 + t])
+    return p1, p2
+
+
+def test_ms_walks_converge_to_flat_slab_solution(sms, workloads, oracle):
+    W = workloads
+    o = oracle.OracleScene(_flat_slab(sms, W))
+    xs = np.array([[0.0, 0.0], [0.5, 0.2], [-0.4, 0.6], [1.0, -1.0]], np.float32)
+    q = W.plane_queries(xs)
+    light = (0.3, -0.2, 5.0)
+    w = np.zeros((8, len(xs)), np.float32)
+    w[0], w[1], w[2] = light
+    for i, x in enumerate(xs):
+        p1, p2 = _slab_solution((x[0], x[1], 0.0), light)
+        w[3:6, i] = p2 + np.array([0.05, -0.03, 0.0])   # start near the exit point
+    out = o.ms_walk_batch(sms.SMSConfig(bounces=2, max_iterations=30), 0, q, w)
+    assert np.all(out[0] == 1) and np.all(out[8] == 1)
+    for i, x in enumerate(xs):
+        p1, p2 = _slab_solution((x[0], x[1], 0.0), light)
+        assert np.linalg.norm(out[2:5, i] - p1) < 1e-5
+        assert np.linalg.norm(out[5:8, i] - p2) < 1e-5
+
+
+def test_block_tridiagonal_matches_dense_solve():
+    """The block Thomas recursion of manifold_ms.cpp:1192-1232, written out in
+    FP64, equals a dense solve of the same 2k x 2k system."""
+    rng = np.random.default_rng(4)
+    for k in (1, 2, 3, 4):
+        P = [rng.normal(size=(2, 2)) for _ in range(k)]
+        Cu = [rng.normal(size=(2, 2)) + 3 * np.eye(2) for _ in range(k)]
+        N = [rng.normal(size=(2, 2)) for _ in range(k)]
+        C = [rng.normal(size=2) for _ in range(k)]
+        A = np.zeros((2 * k, 2 * k))
+        for i in range(k):
+            A[2 * i:2 * i + 2, 2 * i:2 * i + 2] = Cu[i]
+            if i > 0:
+                A[2 * i:2 * i + 2, 2 * i - 2:2 * i] = P[i]
+            if i < k - 1:
+                A[2 * i:2 * i + 2, 2 * i + 2:2 * i + 4] = N[i]
+        ref = np.linalg.solve(A, np.concatenate(C))
+        tmp, il, dx = [None] * k, [None] * k, [None] * k
+        tmp[0] = P[0]
+        il[0] = np.linalg.inv(Cu[0])
+        for i in range(1, k):
+            tmp[i] = P[i] @ il[i - 1]
+            il[i] = np.linalg.inv(Cu[i] - tmp[i] @ N[i - 1])
+        dx[0] = C[0]
+        for i in range(1, k):
+            dx[i] = C[i] - tmp[i] @ dx[i - 1]
+        dx[k - 1] = il[k - 1] @ dx[k - 1]
+        for i in range(k - 2, -1, -1):
+            dx[i] = il[i] @ (dx[i] - N[i] @ dx[i + 1])
+        assert np.allclose(np.concatenate(dx), ref, atol=1e-10)

@@ -134,6 +134,14 @@ sms_status sms_scene_add_point_emitter(sms_scene *scene, const float position[3]
 sms_status sms_scene_add_area_emitter(sms_scene *scene, int32_t shape_id,
                                       const float radiance[3], uint32_t flags);
 
+/* Slope-based normal map of a glinty shape (the level-0 (sx, sy) channels of
+ * the reference's LEAN data, src/librender/normalmap.cpp:7-36, as used by
+ * NormalmapBSDF::slope, src/bsdfs/normalmap.cpp:305-336).  slopes: res*res
+ * interleaved FP16 pairs (IEEE binary16 bit patterns), row-major with v as the
+ * row; tiles as the BSDF's "tiles" parameter.  Marks the shape glinty. */
+sms_status sms_scene_set_normalmap(sms_scene *scene, int32_t shape_id,
+                                   const uint16_t *slopes, uint32_t res, float tiles);
+
 /* --------------------------------------------------------------- context */
 typedef struct sms_ctx sms_ctx;   /* device copy of a scene + config + scratch */
 
@@ -292,6 +300,36 @@ sms_status sms_ms_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
 #define SMS_MS_WALK_OUT_FIELDS 9
 sms_status sms_ms_walk_batch(sms_ctx *ctx, int32_t caster, const float *queries,
                              const float *walk_in, uint32_t n, float *walk_out);
+
+/* --------------------------------------------------------------- glints */
+/* Glint query (SoA, SMS_GLINT_QUERY_FIELDS rows): p (3), n (3), dp_du (3),
+ * dp_dv (3), uv (2), duv_dx (2), duv_dy (2) of the pixel footprint (already
+ * scaled like SamplingIntegrator::scale_differential), sensor position (3).   */
+#define SMS_GLINT_QUERY_FIELDS 21
+
+/* SpecularManifoldGlints::specular_manifold_sampling, SMS strategy
+ * (manifold_glints.cpp:28-176, and the vectorized variant when
+ * cfg.glints_vectorized): emitter sample over all emitters, shadow test, then
+ * the biased or unbiased estimator over footprint seeds.  value =
+ * sms_weight x ei.weight, i.e. everything except the MIS weight against BSDF
+ * sampling (LEAN pdf) and the sensor importance We, which the integrator
+ * multiplies in (:159-175).  count: unique glints (biased) or the Bernoulli
+ * count (unbiased). */
+sms_status sms_glint_connect_batch(sms_ctx *ctx, const float *queries, uint32_t n,
+                                   uint64_t seed, uint64_t stream_offset,
+                                   sms_result *out);
+sms_status sms_glint_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
+                                          uint32_t n, uint64_t seed,
+                                          uint64_t stream_offset, sms_result *out_dev);
+
+/* sample_glint with an explicit footprint sample (xi_start,
+ * manifold_glints.cpp:225-265).  walk_in SMS_GLINT_WALK_IN_FIELDS rows: light
+ * point (3), footprint sample (2); walk_out SMS_GLINT_WALK_OUT_FIELDS rows: ok,
+ * iterations, uv_final (2), uv_init (2). */
+#define SMS_GLINT_WALK_IN_FIELDS 5
+#define SMS_GLINT_WALK_OUT_FIELDS 6
+sms_status sms_glint_walk_batch(sms_ctx *ctx, const float *queries,
+                                const float *walk_in, uint32_t n, float *walk_out);
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,10 @@ def load(fma: bool = False):
                                           vp]),
         "oracle_ms_walk_batch": (i32, [vp, C.POINTER(_Config), i32, vp, vp, u32, vp]),
         "oracle_ms_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
+        "oracle_scene_set_normalmap": (i32, [vp, i32, vp, u32, f32]),
+        "oracle_glint_walk_batch": (i32, [vp, C.POINTER(_Config), vp, vp, u32, vp]),
+        "oracle_glint_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
+        "oracle_nm_slope": (None, [vp, f32, f32, vp]),
         "oracle_fresnel": (f32, [f32, f32, C.POINTER(f32)]),
         "oracle_fresnel_conductor": (f32, [f32, f32, f32]),
         "oracle_uniform_sphere": (None, [f32, f32, C.POINTER(f32)]),
@@ -125,6 +129,11 @@ class OracleScene:
             lib.oracle_scene_add_point_emitter(self._h, _f3(pos), _f3(I), flags)
         for sid, L, flags in desc.area_emitters:
             lib.oracle_scene_add_area_emitter(self._h, sid, _f3(L), flags)
+        if getattr(desc, "normalmap", None) is not None:
+            sid, slopes, tiles = desc.normalmap
+            sl = np.ascontiguousarray(slopes, np.float16)
+            self._keep.append(sl)
+            lib.oracle_scene_set_normalmap(self._h, sid, sl.ctypes.data, sl.shape[0], tiles)
         lib.oracle_scene_finalize(self._h)
 
     def walk_batch(self, config, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
@@ -147,8 +156,24 @@ class OracleScene:
                                        out.ctypes.data)
         return out
 
+    def glint_walk_batch(self, config, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
+        """sample_glint with explicit light point (rows 0-2) and footprint
+        sample (rows 3-4); out rows ok, iterations, uv_final (2), uv_init (2)."""
+        n = queries.shape[1]
+        q = np.ascontiguousarray(queries, np.float32)
+        w = np.ascontiguousarray(walk_in, np.float32)
+        out = np.zeros((6, n), np.float32)
+        self._lib.oracle_glint_walk_batch(self._h, C.byref(_cfg(config)), q.ctypes.data, w.ctypes.data, n,
+                                          out.ctypes.data)
+        return out
+
+    def slope(self, u: float, v: float) -> np.ndarray:
+        out = np.zeros(6, np.float32)
+        self._lib.oracle_nm_slope(self._h, u, v, out.ctypes.data)
+        return out
+
     def connect_batch(self, config, queries: np.ndarray, seed: int = 0, stream_offset: int = 0,
-                      nthreads: int | None = None, multi: bool = False):
+                      nthreads: int | None = None, multi: bool = False, glints: bool = False):
         n = queries.shape[1]
         q = np.ascontiguousarray(queries, np.float32)
         value = np.zeros((3, n), np.float32)
@@ -156,7 +181,8 @@ class OracleScene:
         walks = np.zeros(n, np.int32)
         stats = np.zeros(8, np.uint64)
         nt = nthreads or os.cpu_count() or 1
-        fn = self._lib.oracle_ms_connect_batch if multi else self._lib.oracle_ss_connect_batch
+        fn = (self._lib.oracle_glint_connect_batch if glints else
+              self._lib.oracle_ms_connect_batch if multi else self._lib.oracle_ss_connect_batch)
         fn(self._h, C.byref(_cfg(config)), q.ctypes.data, n, seed, stream_offset, value.ctypes.data,
            count.ctypes.data, walks.ctypes.data, nt, stats.ctypes.data)
         names = ["solver_succeeded", "solver_failed", "bernoulli_trial_calls", "bernoulli_trial_iterations",

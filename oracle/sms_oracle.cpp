@@ -156,9 +156,21 @@ struct Emitter {
 
 struct BNode { float lo[3], hi[3]; int left = -1, right = -1; uint32_t first = 0, count = 0; };
 
+/* Slope-based normal map, level 0 (channels sx, sy of the reference's LEAN
+ * data, src/librender/normalmap.cpp:7-36), stored as FP16 by the library and
+ * widened to FP32 here. */
+struct NormalMap {
+    uint32_t res = 0;
+    float tiles = 1.f;
+    std::vector<float> sx, sy;
+};
+
 struct Scene {
     std::vector<Shape> shapes;
     std::vector<Emitter> emitters;
+    std::vector<int> emitters_all;
+    NormalMap nmap;
+    int glinty_shape = -1;
     /* triangle BVH over all mesh shapes: primitive = (shape, face) */
     std::vector<uint32_t> tri_shape, tri_face;
     std::vector<BNode> nodes;
@@ -1553,6 +1565,315 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
     return result;
 }
 
+
+/* ====================================================================
+ * Glints (src/librender/manifold_glints.cpp)
+ * ==================================================================== */
+struct GQuery {
+    V3 p, n, dp_du, dp_dv, sensor;
+    V2 uv, duv_dx, duv_dy;
+};
+
+static GQuery load_gquery(const float *q, uint32_t n, uint32_t i) {
+    auto f = [&](int k) { return q[(size_t)k * n + i]; };
+    GQuery r;
+    r.p = V3(f(0), f(1), f(2)); r.n = V3(f(3), f(4), f(5));
+    r.dp_du = V3(f(6), f(7), f(8)); r.dp_dv = V3(f(9), f(10), f(11));
+    r.uv.x = f(12); r.uv.y = f(13); r.duv_dx.x = f(14); r.duv_dx.y = f(15);
+    r.duv_dy.x = f(16); r.duv_dy.y = f(17);
+    r.sensor = V3(f(18), f(19), f(20));
+    return r;
+}
+
+/* bilinear setup of Normalmap::eval_normal (normalmap.h:62-104) at level 0
+ * after the tiling wrap of NormalmapBSDF::slope (src/bsdfs/normalmap.cpp:305-316) */
+static void nm_texels(const NormalMap &m, V2 uv_in, uint32_t idx[4], float &wx, float &wy) {
+    float u = uv_in.x * m.tiles, v = uv_in.y * m.tiles;
+    u -= std::floor(u);
+    v -= std::floor(v);
+    float res = (float)m.res;
+    float duv = 1.f / res;
+    float px = (u - 0.5f * duv) * res, py = (v - 0.5f * duv) * res;
+    px = std::min(std::max(px, 0.f), res - 1.f);
+    py = std::min(std::max(py, 0.f), res - 1.f);
+    uint32_t x0 = (uint32_t)std::floor(px), y0 = (uint32_t)std::floor(py);
+    uint32_t x1 = std::min(x0 + 1, m.res - 1), y1 = std::min(y0 + 1, m.res - 1);
+    x0 = std::min(x0, m.res - 1); y0 = std::min(y0, m.res - 1);
+    idx[0] = y0 * m.res + x0; idx[1] = y0 * m.res + x1; idx[2] = y1 * m.res + x0; idx[3] = y1 * m.res + x1;
+    wx = px - (float)x0;
+    wy = py - (float)y0;
+}
+
+/* NormalmapBSDF::slope: (-n[0], -n[1]) of the bilinear slope normal */
+static V2 nm_slope(const NormalMap &m, V2 uv) {
+    uint32_t id[4]; float wx, wy;
+    nm_texels(m, uv, id, wx, wy);
+    float w0x = 1.f - wx, w0y = 1.f - wy;
+    V2 r;
+    float a0 = w0x * m.sx[id[0]] + wx * m.sx[id[1]], a1 = w0x * m.sx[id[2]] + wx * m.sx[id[3]];
+    float b0 = w0x * m.sy[id[0]] + wx * m.sy[id[1]], b1 = w0x * m.sy[id[2]] + wx * m.sy[id[3]];
+    r.x = w0y * a0 + wy * a1;
+    r.y = w0y * b0 + wy * b1;
+    return r;
+}
+
+/* NormalmapBSDF::slope_derivative (normalmap.cpp:318-336 with
+ * normalmap.h:125-193): analytic bilinear derivative x res x tiles */
+static void nm_slope_derivative(const NormalMap &m, V2 uv, V2 &du, V2 &dv) {
+    uint32_t id[4]; float wx, wy;
+    nm_texels(m, uv, id, wx, wy);
+    float res = (float)m.res;
+    auto d = [&](const std::vector<float> &c, float &ou, float &ov) {
+        float v00 = c[id[0]], v10 = c[id[1]], v01 = c[id[2]], v11 = c[id[3]];
+        float tmp = v01 + v10 - v11;
+        ou = (v10 + v00 * (wy - 1.f) - tmp * wy) * res;
+        ov = (v01 + v00 * (wx - 1.f) - tmp * wx) * res;
+    };
+    float ux, vx_, uy, vy_;
+    d(m.sx, ux, vx_);
+    d(m.sy, uy, vy_);
+    du.x = ux * m.tiles; du.y = uy * m.tiles;
+    dv.x = vx_ * m.tiles; dv.y = vy_ * m.tiles;
+}
+
+/* manifold_glints.cpp:348-373 */
+static bool glint_step(const NormalMap &m, V2 target, V2 uv, V2 &C, V2 &dX) {
+    V2 cur = nm_slope(m, uv);
+    C.x = cur.x - target.x; C.y = cur.y - target.y;
+    V2 du, dv;
+    nm_slope_derivative(m, uv, du, dv);
+    M2 J;
+    J.m[0][0] = du.x; J.m[1][0] = du.y; J.m[0][1] = dv.x; J.m[1][1] = dv.y;
+    if (std::fabs(det(J)) < 1e-6f) return false;
+    dX = mul(inverse(J), C);
+    return true;
+}
+
+/* manifold_glints.h:162-194 */
+static bool inside_triangle(V2 p, V2 a, V2 b, V2 c) {
+    V2 v0{c.x - a.x, c.y - a.y}, v1{b.x - a.x, b.y - a.y}, v2{p.x - a.x, p.y - a.y};
+    float d00 = v0.x * v0.x + v0.y * v0.y, d01 = v0.x * v1.x + v0.y * v1.y, d02 = v0.x * v2.x + v0.y * v2.y,
+          d11 = v1.x * v1.x + v1.y * v1.y, d12 = v1.x * v2.x + v1.y * v2.y;
+    float inv = 1.f / (d00 * d11 - d01 * d01);
+    float u = (d11 * d02 - d01 * d12) * inv, v = (d00 * d12 - d01 * d02) * inv;
+    return u >= 0.f && v >= 0.f && u + v < 1.f;
+}
+
+/* manifold_glints.cpp:296-343 */
+static bool glint_newton(const sms_config &cfg, const NormalMap &m, V2 target, V2 uv_init, const GQuery &q, V2 &uv_out,
+                         int &iters) {
+    V2 uv = uv_init;
+    auto corner = [&](float a, float b) {
+        V2 r; r.x = q.uv.x + a * q.duv_dx.x + b * q.duv_dy.x; r.y = q.uv.y + a * q.duv_dx.y + b * q.duv_dy.y;
+        return r;
+    };
+    V2 fa = corner(0.5f, 0.5f), fb = corner(0.5f, -0.5f), fc = corner(-0.5f, -0.5f), fd = corner(-0.5f, 0.5f);
+    bool success = false;
+    int it = 0;
+    float beta = 1.f;
+    while (it < cfg.max_iterations) {
+        V2 C, step;
+        if (!glint_step(m, target, uv, C, step)) break;
+        if (std::sqrt(C.x * C.x + C.y * C.y) < cfg.solver_threshold) { success = true; break; }
+        V2 prop;
+        prop.x = uv.x - cfg.step_scale * beta * step.x;
+        prop.y = uv.y - cfg.step_scale * beta * step.y;
+        if (!(inside_triangle(prop, fa, fb, fc) || inside_triangle(prop, fa, fc, fd))) {
+            beta = 0.5f * beta;
+            it++;
+            continue;
+        }
+        beta = std::min(1.f, 2.f * beta);
+        uv = prop;
+        it++;
+    }
+    iters = it;
+    uv_out = uv;
+    return success;
+}
+
+static void base_frame(const GQuery &q, V3 &s, V3 &t) {
+    s = normalize(q.dp_du - q.n * dot(q.n, q.dp_du));
+    t = cross(q.n, s);
+}
+
+/* manifold_glints.cpp:225-265 */
+static bool sample_glint(const sms_config &cfg, const NormalMap &m, const GQuery &q, V3 lp, V2 fp, V2 &uv_final,
+                         V2 &uv_init, int &iters) {
+    iters = 0;
+    V3 s, t;
+    base_frame(q, s, t);
+    V3 wiw = normalize(q.sensor - q.p), wow = normalize(lp - q.p);
+    V3 wi(dot(wiw, s), dot(wiw, t), dot(wiw, q.n)), wo(dot(wow, s), dot(wow, t), dot(wow, q.n));
+    if (wi.z <= 0.f || wo.z <= 0.f) return false;
+    V3 h = normalize(wi + wo);
+    V2 target;
+    target.x = -h.x / h.z + (-0.f / 1.f);
+    target.y = -h.y / h.z + (-0.f / 1.f);
+    V2 duv;
+    duv.x = (fp.x - 0.5f) * q.duv_dx.x + (fp.y - 0.5f) * q.duv_dy.x;
+    duv.y = (fp.x - 0.5f) * q.duv_dx.y + (fp.y - 0.5f) * q.duv_dy.y;
+    uv_init.x = q.uv.x + duv.x;
+    uv_init.y = q.uv.y + duv.y;
+    return glint_newton(cfg, m, target, uv_init, q, uv_final, iters);
+}
+
+/* normal-mapped shading frame and its derivative at uv (normalmap.cpp:218-290)
+ * for a flat base surface (base frame derivative 0) */
+static void glint_vertex(const NormalMap &m, const GQuery &q, V2 uv, MVertex &v) {
+    V3 s, t;
+    base_frame(q, s, t);
+    V2 sl = nm_slope(m, uv);
+    V2 du, dv;
+    nm_slope_derivative(m, uv, du, dv);
+    V3 nl(-sl.x, -sl.y, 1.f);
+    V3 wn = s * nl.x + t * nl.y + q.n * nl.z;
+    float inv_len = 1.f / norm(wn);
+    wn *= inv_len;
+    /* eval_normal_derivatives returns (-d sx, -d sy, 0); the frame maps it to world */
+    V3 dnu = (s * -du.x + t * -du.y) * inv_len;
+    V3 dnv = (s * -dv.x + t * -dv.y) * inv_len;
+    dnu -= wn * dot(dnu, wn);
+    dnv -= wn * dot(dnv, wn);
+    v = MVertex();
+    v.p = q.p; v.dp_du = q.dp_du; v.dp_dv = q.dp_dv; v.gn = q.n; v.n = wn;
+    v.dn_du = dnu; v.dn_dv = dnv; v.eta = 1.f;
+    if (dot(v.n, v.gn) < 0.f) v.gn = -v.gn;
+}
+
+/* manifold_glints.cpp:411-554 (positional light) */
+static float glint_geometric_term(const MVertex &v0, const MVertex &v1, const MVertex &v2) {
+    V3 wi = v0.p - v1.p;
+    float ili = norm(wi);
+    if (ili < 1e-3f) return 0.f;
+    ili = 1.f / ili; wi *= ili;
+    V3 wo = v2.p - v1.p;
+    float ilo = norm(wo);
+    if (ilo < 1e-3f) return 0.f;
+    ilo = 1.f / ilo; wo *= ilo;
+    V3 h = wi + wo;
+    float ilh = 1.f / norm(h);
+    h *= ilh;
+    ilo *= ilh;
+    ili *= ilh;
+    float dpdu_n = dot(v1.dp_du, v1.n), dpdv_n = dot(v1.dp_dv, v1.n);
+    V3 s = v1.dp_du - v1.n * dpdu_n, t = v1.dp_dv - v1.n * dpdv_n;
+    V3 dh_du = -v1.dp_du * (ili + ilo) + wi * (dot(wi, v1.dp_du) * ili) + wo * (dot(wo, v1.dp_du) * ilo);
+    V3 dh_dv = -v1.dp_dv * (ili + ilo) + wi * (dot(wi, v1.dp_dv) * ili) + wo * (dot(wo, v1.dp_dv) * ilo);
+    dh_du -= h * dot(dh_du, h);
+    dh_dv -= h * dot(dh_dv, h);
+    float hn = dot(h, v1.n), hdu = dot(h, v1.dn_du), hdv = dot(h, v1.dn_dv);
+    M2 d11;
+    d11.m[0][0] = dot(dh_du, s) - dot(v1.dp_du, v1.dn_du) * hn - dpdu_n * hdu;
+    d11.m[0][1] = dot(dh_dv, s) - dot(v1.dp_du, v1.dn_dv) * hn - dpdu_n * hdv;
+    d11.m[1][0] = dot(dh_du, t) - dot(v1.dp_dv, v1.dn_du) * hn - dpdv_n * hdu;
+    d11.m[1][1] = dot(dh_dv, t) - dot(v1.dp_dv, v1.dn_dv) * hn - dpdv_n * hdv;
+    dh_du = (v2.dp_du - wo * dot(wo, v2.dp_du)) * ilo;
+    dh_dv = (v2.dp_dv - wo * dot(wo, v2.dp_dv)) * ilo;
+    dh_du -= h * dot(dh_du, h);
+    dh_dv -= h * dot(dh_dv, h);
+    M2 d12;
+    d12.m[0][0] = dot(dh_du, s); d12.m[0][1] = dot(dh_dv, s);
+    d12.m[1][0] = dot(dh_du, t); d12.m[1][1] = dot(dh_dv, t);
+    if (std::fabs(det(d11)) < 1e-6f) return 0.f;
+    float dx1_dx2 = std::fabs(det(mul(inverse(d11), d12)));
+    V3 d = v0.p - v1.p;
+    float inv_r2 = 1.f / dot(d, d);
+    d *= std::sqrt(inv_r2);
+    float G = std::fabs(dot(d, v1.gn)) * inv_r2 * dx1_dx2;
+    return std::min(1e-5f, G);
+}
+
+/* manifold_glints.cpp:375-409 (delta BSDF): Fresnel at the normal-mapped normal */
+static float glint_reflectance(const sms_bsdf &b, V3 n, V3 wo) {
+    float cos_theta = dot(n, wo);
+    if (b.type == SMS_BSDF_CONDUCTOR && b.k != 0.f) return fresnel_conductor(std::fabs(cos_theta), b.eta, b.k);
+    if (b.type == SMS_BSDF_DIELECTRIC || b.type == SMS_BSDF_CONDUCTOR) return fresnel(std::fabs(cos_theta), b.eta);
+    return fresnel_conductor(std::fabs(cos_theta), 0.f, 1.f);
+}
+
+/* manifold_glints.cpp:267-294 */
+static float glint_contribution(const Scene &sc, const GQuery &q, const EI &ei, V2 uv) {
+    MVertex vy;
+    if (!emitter_vertex(sc, ei, q.p, vy)) return 0.f;
+    MVertex vx;
+    vx.p = q.sensor;
+    V3 dxv = normalize(q.p - q.sensor);
+    vx.n = vx.gn = dxv;
+    coordinate_system(vx.n, vx.dp_du, vx.dp_dv);
+    MVertex vt;
+    glint_vertex(sc.nmap, q, uv, vt);
+    MVertex vt_o = vt;
+    make_orthonormal(vt_o);
+    float f = glint_reflectance(sc.shapes[sc.glinty_shape].bsdf, vt.n, normalize(ei.p - q.p));
+    f *= glint_geometric_term(vx, vt_o, vy);
+    return f;
+}
+
+/* manifold_glints.cpp:28-176: the SMS strategy, before the MIS weight and the
+ * sensor importance (both applied by the integrator): sms_weight x ei.weight. */
+static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q, PCG32 &rng, int &count_out,
+                        int &walks_out, Stats &st) {
+    count_out = 0; walks_out = 0;
+    Query qq; qq.p = q.p;
+    EI ei = sample_emitter_interaction(sc, sc.emitters_all, qq, rng);
+    if (ei.emitter < 0 || sc.glinty_shape < 0 || sc.nmap.res == 0) return V3(0.f);
+    st.connections++;
+    V3 d = ei.p - q.p;
+    float dist = norm(d);
+    d *= 1.f / dist;
+    Ray r; r.o = q.p; r.d = d;
+    r.mint = kRayEps * (1.f + hmax_abs(q.p));
+    r.maxt = dist * (1.f - kRayEps);
+    if (ray_test(sc, r)) return V3(0.f);
+    float w = 0.f;
+    V2 uvf, uvi;
+    int it;
+    if (!cfg.biased) {
+        bool ok = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvf, uvi, it);
+        walks_out++; st.walks++; st.newton += it;
+        if (!ok) { st.failed++; return V3(0.f); }
+        st.succeeded++;
+        float spec = glint_contribution(sc, q, ei, uvf);
+        float inv_prob = 1.f;
+        int iterations = 1;
+        st.calls++;
+        while (true) {
+            V2 uvt, uvi2;
+            int it2;
+            bool ok2 = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvt, uvi2, it2);
+            walks_out++; st.walks++; st.newton += it2;
+            float dx = uvt.x - uvf.x, dy = uvt.y - uvf.y;
+            if (ok2 && std::sqrt(dx * dx + dy * dy) < cfg.uniqueness_threshold) break;
+            inv_prob += 1.f;
+            iterations++;
+            if (cfg.max_trials > 0 && iterations > cfg.max_trials) { inv_prob = 0.f; break; }
+        }
+        st.iters += (uint64_t)iterations;
+        update_max(st.iters_max, (uint64_t)iterations);
+        count_out = inv_prob == 0.f ? -1 : iterations;
+        w = spec * inv_prob;
+    } else {
+        std::vector<V2> sols;
+        for (int m = 0; m < cfg.max_trials; ++m) {
+            bool ok = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvf, uvi, it);
+            walks_out++; st.walks++; st.newton += it;
+            if (!ok) { st.failed++; continue; }
+            st.succeeded++;
+            bool dup = false;
+            for (const V2 &u : sols) {
+                float dx = uvf.x - u.x, dy = uvf.y - u.y;
+                if (std::sqrt(dx * dx + dy * dy) < cfg.uniqueness_threshold) { dup = true; break; }
+            }
+            if (dup) continue;
+            sols.push_back(uvf);
+            w += glint_contribution(sc, q, ei, uvf);
+        }
+        count_out = (int)sols.size();
+    }
+    return V3(w * ei.weight.x, w * ei.weight.y, w * ei.weight.z);
+}
+
 static Scene *as_scene(void *p) { return reinterpret_cast<Scene *>(p); }
 
 } // namespace orc
@@ -1638,7 +1959,9 @@ void oracle_scene_finalize(void *s) {
                 sc->tri_shape.push_back((uint32_t)i); sc->tri_face.push_back(f);
             }
     }
+    sc->emitters_all.clear();
     for (size_t i = 0; i < sc->emitters.size(); ++i) {
+        sc->emitters_all.push_back((int)i);
         if (sc->emitters[i].flags & SMS_EMITTER_CAUSTIC_SINGLE) sc->emitters_ss.push_back((int)i);
         if (sc->emitters[i].flags & SMS_EMITTER_CAUSTIC_MULTI) sc->emitters_ms.push_back((int)i);
     }
@@ -1785,6 +2108,93 @@ int oracle_ms_connect_batch(void *s, const sms_config *cfg, const float *queries
     return 0;
 }
 
+int oracle_scene_set_normalmap(void *s, int shape, const uint16_t *slopes_half, uint32_t res, float tiles) {
+    Scene *sc = as_scene(s);
+    if (shape < 0 || shape >= (int)sc->shapes.size() || res == 0) return -1;
+    auto h2f = [](uint16_t h) {
+        uint32_t sign = (uint32_t)(h >> 15) << 31, e = (h >> 10) & 0x1f, m = h & 0x3ff, bits;
+        if (e == 0) {
+            if (m == 0) bits = sign;
+            else { /* subnormal */
+                int shift = 0;
+                while (!(m & 0x400)) { m <<= 1; ++shift; }
+                m &= 0x3ff;
+                bits = sign | ((uint32_t)(127 - 15 - shift + 1) << 23) | (m << 13);
+            }
+        } else if (e == 31) {
+            bits = sign | 0x7f800000u | (m << 13);
+        } else {
+            bits = sign | ((e - 15 + 127) << 23) | (m << 13);
+        }
+        float f;
+        std::memcpy(&f, &bits, 4);
+        return f;
+    };
+    sc->nmap.res = res;
+    sc->nmap.tiles = tiles;
+    size_t n = (size_t)res * res;
+    sc->nmap.sx.resize(n);
+    sc->nmap.sy.resize(n);
+    for (size_t i = 0; i < n; ++i) { sc->nmap.sx[i] = h2f(slopes_half[2 * i]); sc->nmap.sy[i] = h2f(slopes_half[2 * i + 1]); }
+    sc->glinty_shape = shape;
+    return 0;
+}
+
+/* sample_glint with an explicit footprint sample (xi_start, :225-265) and
+ * light point: out rows ok, iterations, uv_final (2), uv_init (2). */
+int oracle_glint_walk_batch(void *s, const sms_config *cfg, const float *queries, const float *walk_in, uint32_t n,
+                            float *out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    for (uint32_t i = 0; i < n; ++i) {
+        GQuery q = load_gquery(queries, n, i);
+        auto w = [&](int k) { return walk_in[(size_t)k * n + i]; };
+        V3 lp(w(0), w(1), w(2));
+        V2 fp; fp.x = w(3); fp.y = w(4);
+        V2 uvf, uvi;
+        int it = 0;
+        bool ok = sample_glint(*cfg, sc->nmap, q, lp, fp, uvf, uvi, it);
+        float vals[6] = {ok ? 1.f : 0.f, (float)it, uvf.x, uvf.y, uvi.x, uvi.y};
+        for (int k = 0; k < 6; ++k) out[(size_t)k * n + i] = vals[k];
+    }
+    return 0;
+}
+
+int oracle_glint_connect_batch(void *s, const sms_config *cfg, const float *queries, uint32_t n, uint64_t seed,
+                               uint64_t stream_offset, float *value, int32_t *count, int32_t *walks, int nthreads,
+                               uint64_t *stats_out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    Stats st;
+    if (nthreads < 1) nthreads = 1;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        while (true) {
+            uint32_t b = next.fetch_add(64);
+            if (b >= n) break;
+            for (uint32_t i = b; i < std::min(n, b + 64); ++i) {
+                GQuery q = load_gquery(queries, n, i);
+                PCG32 rng;
+                rng.seed(seed, (uint64_t)i + stream_offset);
+                int c = 0, w = 0;
+                V3 v = glint_connect(*sc, *cfg, q, rng, c, w, st);
+                value[i] = v.x; value[(size_t)n + i] = v.y; value[2 * (size_t)n + i] = v.z;
+                count[i] = c; walks[i] = w;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
+    worker();
+    for (auto &t : th) t.join();
+    if (stats_out) {
+        stats_out[0] = st.succeeded; stats_out[1] = st.failed; stats_out[2] = st.calls;
+        stats_out[3] = st.iters; stats_out[4] = st.iters_max; stats_out[5] = st.walks;
+        stats_out[6] = st.newton; stats_out[7] = st.connections;
+    }
+    return 0;
+}
+
 /* Known-answer hooks for the dependency pins (fresnel.h:34-120, warp.h). */
 float oracle_fresnel(float cos_i, float eta, float *cos_t) { return fresnel(cos_i, eta, cos_t); }
 float oracle_fresnel_conductor(float cos_i, float eta, float k) { return fresnel_conductor(cos_i, eta, k); }
@@ -1796,6 +2206,13 @@ void oracle_uniform_sphere(float u, float v, float *out) {
 void oracle_pcg32(uint64_t initstate, uint64_t initseq, uint32_t n, uint32_t *out) {
     PCG32 r; r.seed(initstate, initseq);
     for (uint32_t i = 0; i < n; ++i) out[i] = r.next_u32();
+}
+void oracle_nm_slope(void *s, float u, float v, float *out) {
+    Scene *sc = as_scene(s);
+    V2 uv; uv.x = u; uv.y = v;
+    V2 sl = nm_slope(sc->nmap, uv), du, dv;
+    nm_slope_derivative(sc->nmap, uv, du, dv);
+    out[0] = sl.x; out[1] = sl.y; out[2] = du.x; out[3] = du.y; out[4] = dv.x; out[5] = dv.y;
 }
 void oracle_pcg32_f32(uint64_t initstate, uint64_t initseq, uint32_t n, float *out) {
     PCG32 r; r.seed(initstate, initseq);

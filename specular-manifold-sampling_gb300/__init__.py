@@ -31,6 +31,9 @@ NOALLOC_MAX_QUERIES = 1 << 18
 WALK_IN_FIELDS = 8
 WALK_OUT_FIELDS = 11
 MS_WALK_OUT_FIELDS = 9
+GLINT_QUERY_FIELDS = 21
+GLINT_WALK_IN_FIELDS = 5
+GLINT_WALK_OUT_FIELDS = 6
 
 SHAPE_CAUSTIC_RECEIVER = 1 << 0
 SHAPE_CAUSTIC_CASTER_SINGLE = 1 << 1
@@ -126,6 +129,10 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ms_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ms_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ms_walk_batch": (i32, [vp, i32, vp, vp, u32, vp]),
+        "sms_scene_set_normalmap": (i32, [vp, i32, vp, u32, f32]),
+        "sms_glint_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
+        "sms_glint_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
+        "sms_glint_walk_batch": (i32, [vp, vp, vp, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -223,6 +230,7 @@ class SceneDesc:
     meshes: list = field(default_factory=list)    # (P, N, UV, F, Bsdf, flags)
     order: list = field(default_factory=list)     # ("sphere"|"mesh", index) in shape-id order
     point_emitters: list = field(default_factory=list)  # (pos, I, flags)
+    normalmap: tuple | None = None   # (shape_id, (res, res, 2) float16 slopes, tiles)
     area_emitters: list = field(default_factory=list)   # (shape_id, L, flags)
 
     def add_sphere(self, center, radius, bsdf: Bsdf, flags: int = 0, flip: bool = False) -> int:
@@ -272,6 +280,13 @@ class Scene:
             _check(lib.sms_scene_add_point_emitter(h, _f3(pos), _f3(I), flags))
         for sid, L, flags in desc.area_emitters:
             _check(lib.sms_scene_add_area_emitter(h, sid, _f3(L), flags))
+        if desc.normalmap is not None:
+            sid, slopes, tiles = desc.normalmap
+            sl = np.ascontiguousarray(slopes, np.float16)
+            if sl.ndim != 3 or sl.shape[0] != sl.shape[1] or sl.shape[2] != 2:
+                raise ValueError("slopes must have shape (res, res, 2)")
+            self._keep.append(sl)
+            _check(lib.sms_scene_set_normalmap(h, sid, _ptr(sl), sl.shape[0], float(tiles)))
 
     @property
     def handle(self):
@@ -417,4 +432,40 @@ class SpecularManifoldMultiScatter:
         w = _soa(walk_in, WALK_IN_FIELDS, n)
         out = np.zeros((MS_WALK_OUT_FIELDS, n), np.float32)
         _check(_LIB.sms_ms_walk_batch(self.ctx.handle, caster, _ptr(q), _ptr(w), n, _ptr(out)))
+        return out
+
+
+class SpecularManifoldGlints:
+    """Batched SpecularManifoldGlints / SpecularManifoldGlintsVectorized
+    (include/mitsuba/render/manifold_glints.h): the SMS strategy over pixel
+    footprints; value = sms_weight x ei.weight (MIS and sensor importance are
+    the integrator's)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def specular_manifold_sampling(self, queries: np.ndarray, seed: int = 0, stream_offset: int = 0):
+        n = queries.shape[1]
+        q = _soa(queries, GLINT_QUERY_FIELDS, n)
+        value = np.zeros((3, n), np.float32)
+        count = np.zeros(n, np.int32)
+        walks = np.zeros(n, np.int32)
+        r = _Result(_ptr(value), _ptr(count), _ptr(walks))
+        _check(_LIB.sms_glint_connect_batch(self.ctx.handle, _ptr(q), n, seed, stream_offset, C.byref(r)))
+        return value, count, walks
+
+    def specular_manifold_sampling_device(self, queries_ptr: int, n: int, value_ptr: int, count_ptr: int,
+                                          walks_ptr: int, seed: int = 0, stream_offset: int = 0):
+        r = _Result(value_ptr, count_ptr, walks_ptr)
+        _check(_LIB.sms_glint_connect_batch_device(self.ctx.handle, queries_ptr, n, seed, stream_offset,
+                                                   C.byref(r)))
+
+    def sample_glint(self, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
+        """walk_in (5, n): light point (3), footprint sample xi_start (2);
+        returns (6, n): ok, iterations, uv_final (2), uv_init (2)."""
+        n = queries.shape[1]
+        q = _soa(queries, GLINT_QUERY_FIELDS, n)
+        w = _soa(walk_in, GLINT_WALK_IN_FIELDS, n)
+        out = np.zeros((GLINT_WALK_OUT_FIELDS, n), np.float32)
+        _check(_LIB.sms_glint_walk_batch(self.ctx.handle, _ptr(q), _ptr(w), n, _ptr(out)))
         return out

@@ -211,6 +211,12 @@ struct DevScene {
     int n_emitters_ss, emitters_ss[kMaxEmitters];
     int n_casters_ms, casters_ms[kMaxCasters];
     int n_emitters_ms, emitters_ms[kMaxEmitters];
+    int n_emitters_all, emitters_all[kMaxEmitters];
+    // glints: FP16 (sx, sy) slope map of the glinty shape, res x res texels
+    const uint32_t *nmap;      // one __half2 per texel
+    uint32_t nmap_res;
+    float nmap_tiles;
+    int glinty_shape;
     const DevEmitter *emitters;
 };
 

@@ -172,6 +172,11 @@ struct HostEmitter {
 struct sms_scene {
     std::vector<HostShape> shapes;
     std::vector<HostEmitter> emitters;
+    // glint normal map (slope based, level 0)
+    int nmap_shape = -1;
+    uint32_t nmap_res = 0;
+    float nmap_tiles = 1.f;
+    std::vector<uint16_t> nmap;   // res * res * 2 FP16 (sx, sy)
 };
 
 extern "C" sms_status sms_scene_create(sms_scene **out) {
@@ -258,6 +263,21 @@ extern "C" sms_status sms_scene_add_area_emitter(sms_scene *s, int32_t shape, co
     e.flags = flags;
     s->emitters.push_back(e);
     s->shapes[shape].emitter = (int)s->emitters.size() - 1;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_scene_set_normalmap(sms_scene *s, int32_t shape, const uint16_t *slopes, uint32_t res,
+                                              float tiles) {
+    if (!s || !slopes) return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_normalmap: null argument");
+    if (shape < 0 || shape >= (int32_t)s->shapes.size())
+        return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_normalmap: unknown shape id");
+    if (res == 0 || res > 65536) return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_normalmap: bad resolution");
+    if (!(tiles > 0.f)) return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_normalmap: tiles must be positive");
+    s->nmap_shape = shape;
+    s->nmap_res = res;
+    s->nmap_tiles = tiles;
+    s->nmap.assign(slopes, slopes + 2 * (size_t)res * res);
+    s->shapes[shape].flags |= SMS_SHAPE_GLINTY;
     return SMS_OK;
 }
 
@@ -461,7 +481,12 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         shapes.push_back(ds);
     }
     std::vector<DevEmitter> em;
+    d.glinty_shape = s->nmap_shape;
+    d.nmap_res = s->nmap_res;
+    d.nmap_tiles = s->nmap_tiles;
     for (size_t i = 0; i < s->emitters.size(); ++i) {
+        if (d.n_emitters_all >= kMaxEmitters) return fail(SMS_ERR_UNSUPPORTED, "too many emitters");
+        d.emitters_all[d.n_emitters_all++] = (int)i;
         const HostEmitter &h = s->emitters[i];
         DevEmitter e;
         std::memset(&e, 0, sizeof(e));
@@ -513,6 +538,11 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
     if (sms_status st = upload(c, cdf, &d.cdf)) return st;
     if (sms_status st = upload(c, pmf, &d.pmf)) return st;
     if (sms_status st = upload(c, em, &d.emitters)) return st;
+    {
+        const uint16_t *nm = nullptr;
+        if (sms_status st = upload(c, s->nmap, &nm)) return st;
+        d.nmap = reinterpret_cast<const uint32_t *>(nm);
+    }
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return SMS_OK;
 }
@@ -857,5 +887,88 @@ extern "C" sms_status sms_ms_walk_batch(sms_ctx *c, int32_t caster, const float 
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (st) return st;
     if (e != cudaSuccess) return cuda_fail(e, "sms_ms_walk_batch");
+    return check_device_error(c);
+}
+
+// --------------------------------------------------------------------- glints
+static sms_status check_glint_scene(sms_ctx *c) {
+    if (c->dsc.glinty_shape < 0 || c->dsc.nmap_res == 0)
+        return fail(SMS_ERR_INVALID_ARG, "the scene has no normal map (sms_scene_set_normalmap)");
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_glint_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                                     uint64_t stream_off, sms_result *out) {
+    if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
+        return fail(SMS_ERR_INVALID_ARG, "sms_glint_connect_batch_device: null argument");
+    if (sms_status st = check_glint_scene(c)) return st;
+    if (n == 0) return SMS_OK;
+    if (c->cfg.biased && c->cfg.max_trials > (1 << 24))
+        return fail(SMS_ERR_INVALID_ARG, "max_trials too large for the biased estimator");
+    CUDA_TRY(cudaSetDevice(c->device));
+    SsScratch scr{};
+    if (!c->cfg.biased)
+        if (sms_status st = ensure_scratch(c, n, scr)) return st;
+    CUDA_TRY(launch_glint_connect(c->dsc, solver_cfg(c->cfg), q, n, seed, stream_off, out->value, out->count,
+                                  out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, &c->timer, c->stream));
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_glint_connect_batch(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                              uint64_t stream_off, sms_result *out) {
+    if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
+        return fail(SMS_ERR_INVALID_ARG, "sms_glint_connect_batch: null argument");
+    if (sms_status st = check_glint_scene(c)) return st;
+    if (n == 0) return SMS_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    size_t qb = (size_t)SMS_GLINT_QUERY_FIELDS * n * sizeof(float);
+    size_t vb = 3 * (size_t)n * sizeof(float), ib = (size_t)n * sizeof(int32_t);
+    if (sms_status st = ensure_io(c, qb + vb + 2 * ib)) return st;
+    char *dbuf = reinterpret_cast<char *>(c->io);
+    float *dq = reinterpret_cast<float *>(dbuf);
+    sms_result r{reinterpret_cast<float *>(dbuf + qb), reinterpret_cast<int32_t *>(dbuf + qb + vb),
+                 reinterpret_cast<int32_t *>(dbuf + qb + vb + ib)};
+    sms_status st = SMS_OK;
+    do {
+        cudaError_t e = cudaMemcpyAsync(dq, q, qb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy queries"); break; }
+        st = sms_glint_connect_batch_device(c, dq, n, seed, stream_off, &r);
+        if (st) break;
+        e = cudaMemcpyAsync(out->value, r.value, vb, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->count, r.count, ib, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out->walks, r.walks, ib, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy results"); break; }
+    } while (0);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "sms_glint_connect_batch");
+    return check_device_error(c);
+}
+
+extern "C" sms_status sms_glint_walk_batch(sms_ctx *c, const float *q, const float *w, uint32_t n, float *out) {
+    if (!c || (n && (!q || !w || !out))) return fail(SMS_ERR_INVALID_ARG, "sms_glint_walk_batch: null argument");
+    if (sms_status st = check_glint_scene(c)) return st;
+    if (n == 0) return SMS_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    size_t qb = (size_t)SMS_GLINT_QUERY_FIELDS * n * sizeof(float),
+           wb = (size_t)SMS_GLINT_WALK_IN_FIELDS * n * sizeof(float),
+           ob = (size_t)SMS_GLINT_WALK_OUT_FIELDS * n * sizeof(float);
+    if (sms_status st = ensure_io(c, qb + wb + ob)) return st;
+    char *dbuf = reinterpret_cast<char *>(c->io);
+    sms_status st = SMS_OK;
+    do {
+        cudaError_t e = cudaMemcpyAsync(dbuf, q, qb, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dbuf + qb, w, wb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy walk inputs"); break; }
+        e = launch_glint_walk(c->dsc, solver_cfg(c->cfg), reinterpret_cast<float *>(dbuf),
+                              reinterpret_cast<float *>(dbuf + qb), n, reinterpret_cast<float *>(dbuf + qb + wb),
+                              c->ctr, &c->timer, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "launch glint_walk"); break; }
+        e = cudaMemcpyAsync(out, dbuf + qb + wb, ob, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) { st = cuda_fail(e, "copy walk outputs"); break; }
+    } while (0);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "sms_glint_walk_batch");
     return check_device_error(c);
 }

@@ -35,6 +35,9 @@ constexpr int kTrialHardLimit = 1 << 16;
 // Rows of the per-walk outputs (sms_ss_walk_batch, sms_ms_walk_batch).
 constexpr int kWalkOutFields = 11;
 constexpr int kMsWalkOutFields = 9;
+constexpr int kGlintWalkOutFields = 6;
+constexpr int kGlintQueryFields = 21;
+constexpr int kGlintWalkInFields = 5;
 // Longest specular chain of the multi-scatter kernels.
 constexpr int kMaxBounces = 4;
 
@@ -64,6 +67,12 @@ cudaError_t launch_ms_connect(const DevScene &sc, const SolverCfg &cfg, int boun
                               uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
                               DevCounters *ctr, const SsScratch &scr, int *tmpl, int num_sms, int blocks_per_sm,
                               PhaseTimer *tm, cudaStream_t s);
+
+cudaError_t launch_glint_walk(const DevScene &sc, const SolverCfg &cfg, const float *q, const float *w, uint32_t n,
+                              float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s);
+cudaError_t launch_glint_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
+                                 uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
+                                 const SsScratch &scr, int num_sms, int blocks_per_sm, PhaseTimer *tm, cudaStream_t s);
 
 // Read-only view of a context for entry points defined outside sms_host.cu.
 struct CtxView {

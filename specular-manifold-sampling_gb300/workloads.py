@@ -11,6 +11,14 @@ oracle and the tests see identical inputs.
                     sinusoids (total amplitude <= 0.01) on 256x256 vertex grids
                     over [-1,1]^2; point light (0,0,5); queries uniform on
                     [-1,1]^2; biased SMS, 32 trials, 30 iterations, 2 bounces.
+  glint_scene       normal-mapped conductor plane [-0.5,0.5]^2 at z=0 (uv in
+                    [0,1]^2); FP16 slope map res^2 (8192^2 for the benchmark)
+                    from a Gaussian random field with correlation length 4
+                    texels and slope std 0.15 (seed 7); pinhole camera
+                    (1024^2, 30 deg FOV) at 60 deg from the normal, point light
+                    in the mirror direction; one query per pixel that sees the
+                    plane, footprints from ray differentials; biased SMS, 64
+                    seeds, 10 iterations.
   water_scene       z = 1 + sum of 32 sinusoids (a ~ U(0.002,0.02),
                     |k| ~ U(2,40), uniform direction and phase) tessellated to a
                     512x512 vertex grid over [-1,1]^2 (522,242 triangles), IOR
@@ -28,8 +36,8 @@ import math
 import numpy as np
 
 from . import (BSDF_CONDUCTOR, BSDF_DIELECTRIC, BSDF_DIFFUSE, EMITTER_CAUSTIC_MULTI, EMITTER_CAUSTIC_SINGLE,
-               SHAPE_CAUSTIC_BOUNCER, SHAPE_CAUSTIC_CASTER_MULTI, SHAPE_CAUSTIC_CASTER_SINGLE, QUERY_FIELDS, Bsdf,
-               SceneDesc, SMSConfig)
+               SHAPE_CAUSTIC_BOUNCER, SHAPE_CAUSTIC_CASTER_MULTI, SHAPE_CAUSTIC_CASTER_SINGLE, SHAPE_GLINTY,
+               QUERY_FIELDS, Bsdf, SceneDesc, SMSConfig)
 
 _MUL = np.uint64(6364136223846793005)
 _M64 = (1 << 64) - 1
@@ -216,3 +224,96 @@ def slab_queries(n: int, seed: int = 6, first: int = 0) -> np.ndarray:
 
 def slab_config() -> SMSConfig:
     return SMSConfig(biased=True, max_trials=32, max_iterations=30, bounces=2)
+
+
+# ----------------------------------------------------------------- glints
+GLINT_QUERY_FIELDS = 21
+
+
+def glint_slopes(res: int, seed: int = 7, corr: float = 4.0, std: float = 0.15) -> np.ndarray:
+    """(res, res, 2) float16 slopes (sx, sy): white noise smoothed by a Gaussian
+    of `corr` texels (wrapping, like the tiled lookup), scaled to std `std`."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    out = np.empty((res, res, 2), np.float16)
+    for c in range(2):
+        w = rng.standard_normal((res, res), dtype=np.float32)
+        w = gaussian_filter(w, sigma=corr, mode="wrap", truncate=3.0)
+        w *= np.float32(std / float(w.std()))
+        out[..., c] = w.astype(np.float16)
+    return out
+
+
+GLINT_CAM_DIST = 2.0
+GLINT_ELEV = math.radians(60.0)
+
+
+def glint_camera():
+    cam = np.array([0.0, -math.sin(GLINT_ELEV), math.cos(GLINT_ELEV)]) * GLINT_CAM_DIST
+    light = np.array([0.0, math.sin(GLINT_ELEV), math.cos(GLINT_ELEV)]) * GLINT_CAM_DIST
+    return cam, light
+
+
+def glint_scene(map_res: int = 8192, slopes: np.ndarray | None = None, intensity: float = 50.0,
+                conductor=(1.0, 6.0)) -> SceneDesc:
+    d = SceneDesc()
+    P = np.array([[-0.5, -0.5, 0.0], [0.5, -0.5, 0.0], [0.5, 0.5, 0.0], [-0.5, 0.5, 0.0]], np.float32)
+    UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    F = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    sid = d.add_mesh(P, F, Bsdf(BSDF_CONDUCTOR, conductor[0], conductor[1]), SHAPE_GLINTY, UV=UV)
+    d.normalmap = (sid, glint_slopes(map_res) if slopes is None else slopes, 1.0)
+    _, light = glint_camera()
+    d.add_point_emitter(tuple(light), (intensity,) * 3, EMITTER_CAUSTIC_SINGLE)
+    return d
+
+
+def glint_queries(width: int = 1024, fov_deg: float = 30.0, diff_scale: float = 1.0) -> np.ndarray:
+    """One query per pixel whose primary ray hits the plane: p, n, dp_du, dp_dv,
+    uv, duv_dx, duv_dy (interaction.h:216-248 compute_partials, scaled by
+    diff_scale) and the sensor position.  Shape (21, n)."""
+    cam, _ = glint_camera()
+    fwd = -cam / np.linalg.norm(cam)
+    up = np.array([0.0, 0.0, 1.0])
+    right = np.cross(fwd, up)
+    right /= np.linalg.norm(right)
+    upv = np.cross(right, fwd)
+    tan_h = math.tan(math.radians(fov_deg) / 2)
+    j, i = np.meshgrid(np.arange(width), np.arange(width), indexing="ij")
+
+    def dirs(px, py):
+        sx = (2.0 * (px + 0.5) / width - 1.0) * tan_h
+        sy = (1.0 - 2.0 * (py + 0.5) / width) * tan_h
+        d = fwd[None, None, :] + sx[..., None] * right[None, None, :] + sy[..., None] * upv[None, None, :]
+        return d / np.linalg.norm(d, axis=-1, keepdims=True)
+
+    d0 = dirs(i.astype(np.float64), j.astype(np.float64))
+    dx = dirs(i + 1.0, j.astype(np.float64))
+    dy = dirs(i.astype(np.float64), j + 1.0)
+    t = -cam[2] / d0[..., 2]
+    p = cam[None, None, :] + t[..., None] * d0
+    hit = (t > 0) & (np.abs(p[..., 0]) <= 0.5) & (np.abs(p[..., 1]) <= 0.5)
+    p, d0, dx, dy = p[hit], d0[hit], dx[hit], dy[hit]
+    n = np.array([0.0, 0.0, 1.0])
+
+    def offset_point(dd):
+        tt = (0.0 - cam[2]) / dd[:, 2]   # plane z = 0 (n . p = 0)
+        return cam[None, :] + tt[:, None] * dd
+
+    dp_dx = (offset_point(dx) - p) * diff_scale
+    dp_dy = (offset_point(dy) - p) * diff_scale
+    m = p.shape[0]
+    q = np.zeros((GLINT_QUERY_FIELDS, m), np.float32)
+    q[0:3] = p.T
+    q[5] = 1.0
+    q[6] = 1.0            # dp_du = (1, 0, 0): uv = (x + 0.5, y + 0.5)
+    q[10] = 1.0           # dp_dv = (0, 1, 0)
+    q[12] = p[:, 0] + 0.5
+    q[13] = p[:, 1] + 0.5
+    q[14], q[15] = dp_dx[:, 0], dp_dx[:, 1]
+    q[16], q[17] = dp_dy[:, 0], dp_dy[:, 1]
+    q[18:21] = cam[:, None]
+    return q
+
+
+def glint_config() -> SMSConfig:
+    return SMSConfig(biased=True, max_trials=64, max_iterations=10, glints_vectorized=True)

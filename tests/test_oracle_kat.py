@@ -217,3 +217,52 @@ def test_block_tridiagonal_matches_dense_solve():
         for i in range(k - 2, -1, -1):
             dx[i] = il[i] @ (dx[i] - N[i] @ dx[i + 1])
         assert np.allclose(np.concatenate(dx), ref, atol=1e-10)
+
+
+def test_slope_derivative_matches_finite_differences(sms, workloads, oracle):
+    """NormalmapBSDF::slope_derivative (src/bsdfs/normalmap.cpp:318-336) is the
+    analytic derivative of the bilinear slope lookup: compare with central
+    differences inside a texel."""
+    W = workloads
+    d = W.glint_scene(slopes=W.glint_slopes(64))
+    o = oracle.OracleScene(d)
+    rng = np.random.default_rng(3)
+    h = 1e-4
+    for u, v in rng.uniform(0.05, 0.95, size=(20, 2)):
+        a = o.slope(u, v)
+        pu, mu = o.slope(u + h, v), o.slope(u - h, v)
+        pv, mv = o.slope(u, v + h), o.slope(u, v - h)
+        fd_u = (pu[:2] - mu[:2]) / (2 * h)
+        fd_v = (pv[:2] - mv[:2]) / (2 * h)
+        # the bilinear patch is smooth inside a texel; skip samples straddling an edge
+        if np.abs(pu[2:4] - mu[2:4]).max() > 1e-3 * max(1.0, np.abs(a[2:4]).max()):
+            continue
+        np.testing.assert_allclose(a[2:4], fd_u, rtol=2e-2, atol=2e-2)
+        np.testing.assert_allclose(a[4:6], fd_v, rtol=2e-2, atol=2e-2)
+
+
+def test_glint_walks_reach_target_slope(sms, workloads, oracle):
+    """Converged glint walks end at a uv whose slope equals the half-vector
+    slope (manifold_glints.cpp:236-247) and inside the footprint."""
+    W = workloads
+    d = W.glint_scene(slopes=W.glint_slopes(256))
+    o = oracle.OracleScene(d)
+    q = W.glint_queries(64)
+    n = q.shape[1]
+    _, light = W.glint_camera()
+    u = W.pcg32_streams_f32(5, np.arange(n, dtype=np.uint64), 2)
+    w = np.zeros((5, n), np.float32)
+    w[0:3] = np.asarray(light, np.float32)[:, None]
+    w[3], w[4] = u[0], u[1]
+    cfg = W.glint_config()
+    out = o.glint_walk_batch(cfg, q, w)
+    ok = out[0] > 0.5
+    assert ok.sum() > 10
+    for i in np.nonzero(ok)[0][:50]:
+        p, sensor = q[0:3, i], q[18:21, i]
+        wi = (sensor - p) / np.linalg.norm(sensor - p)
+        wo = (np.asarray(light) - p) / np.linalg.norm(np.asarray(light) - p)
+        h = (wi + wo) / np.linalg.norm(wi + wo)
+        target = -h[:2] / h[2]
+        s = o.slope(out[2, i], out[3, i])[:2]
+        assert np.linalg.norm(s - target) < 1e-4

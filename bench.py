@@ -135,6 +135,147 @@ def cpu_baseline_sample(sms, W, n_sample: int, nthreads: int, seed: int = 1):
     return n_sample / dt, dt, n_sample
 
 
+class DeviceTimer:
+    """CUDA-event time of work issued on one stream."""
+
+    def __init__(self, torch, stream):
+        self.torch, self.stream = torch, stream
+
+    def __enter__(self):
+        self.a = self.torch.cuda.Event(enable_timing=True)
+        self.b = self.torch.cuda.Event(enable_timing=True)
+        self.a.record(self.stream)
+        return self
+
+    def __exit__(self, *exc):
+        self.b.record(self.stream)
+        self.b.synchronize()
+        self.ms = self.a.elapsed_time(self.b)
+
+
+def connect_timed(torch, sms, ctx, kind, q_dev, n, seed, stream_offset=0):
+    """One device-pointer connection call; returns (value (3, n) on device, ms)."""
+    dev = q_dev.device
+    val = torch.empty((3, n), dtype=torch.float32, device=dev)
+    cnt = torch.empty(n, dtype=torch.int32, device=dev)
+    wlk = torch.empty(n, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    est = {"ss": sms.SpecularManifoldSingleScatter, "ms": sms.SpecularManifoldMultiScatter,
+           "glints": sms.SpecularManifoldGlints}[kind](ctx)
+    with DeviceTimer(torch, stream) as t:
+        est.specular_manifold_sampling_device(q_dev.data_ptr(), n, val.data_ptr(), cnt.data_ptr(), wlk.data_ptr(),
+                                              seed=seed, stream_offset=stream_offset)
+    return val, t.ms
+
+
+def secondary_configs(torch, sms, W, dev):
+    """Throughput of the other solver configurations (one GPU): sphere
+    (biased, 16 walks), two-bounce slab (biased, 32 walks, 512k queries) and
+    glints (8192^2 FP16 slope map, 1024^2 pixels, 64 seeds, vectorized)."""
+    out = {}
+    cases = [
+        ("sphere_biased_m16", "ss", W.sphere_scene, W.sphere_config, lambda: W.sphere_queries(64), 16),
+        ("slab_two_bounce_biased_m32", "ms", W.slab_scene, W.slab_config, lambda: W.slab_queries(1 << 19), 32),
+        ("glints_8192_vectorized_m64", "glints", W.glint_scene, W.glint_config, lambda: W.glint_queries(1024), 64),
+    ]
+    for name, kind, scene, config, queries, walks in cases:
+        ctx = sms.Context(sms.Scene(scene()), config(), device=dev)
+        q = torch.from_numpy(np.ascontiguousarray(queries(), np.float32)).to(f"cuda:{dev}")
+        n = q.shape[1]
+        for i in range(3):
+            connect_timed(torch, sms, ctx, kind, q, n, seed=50 + i)
+        ctx.reset_stats()
+        ms = [connect_timed(torch, sms, ctx, kind, q, n, seed=60 + i)[1] for i in range(5)]
+        st = ctx.stats()
+        t = float(np.mean(ms))
+        out[name] = {"queries": n, "ms_per_call": t, "connections_per_s": n / (t / 1e3),
+                     "walks_per_s": st["walks"] / (5 * t / 1e3), "walks_per_connection": walks,
+                     "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"])}
+        ctx.close()
+    return out
+
+
+def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=8192, lr=1e-3, res=128,
+                  ref_spp=4096):
+    """Learned seed proposal on the water workload: training pairs from the
+    uniform-seed solver, GPU training, then equal-time caustic RMSE of
+    learned vs uniform seeding against a ref_spp uniform-seed image of
+    res x res receiver points."""
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    cfg = W.water_config()
+    ctx.set_config(cfg)
+    prop = sms.SeedProposal(ctx, 0, seed=1, capacity=pairs)
+    chunk = 1 << 20
+    total, calls = 0, 0
+    with DeviceTimer(torch, stream) as t_collect:
+        while total < pairs and calls < 16:
+            q = torch.from_numpy(W.water_queries(chunk, seed=77, first=calls * chunk)).to(f"cuda:{dev}")
+            torch.cuda.synchronize()
+            total = prop.collect(q.data_ptr(), chunk, seed=77, stream_offset=calls * chunk, walks_per_query=8)
+            calls += 1
+    prop.normalize()
+    loss0, _ = prop.loss_grad(batch)
+    prop.train(steps=100, batch=batch, lr=lr)   # graph capture + warm-up
+    t0 = time.perf_counter()
+    with DeviceTimer(torch, stream) as t_train:
+        loss = prop.train(steps=steps - 100, batch=batch, lr=lr)
+    train_wall = time.perf_counter() - t0
+    step_ms = t_train.ms / (steps - 100)
+    flop_step = 3 * 2 * batch * (96 * 64 + 3 * 64 * 64 + 64 * 48)   # forward + backward GEMMs
+    # images: pixel centres of a res x res grid on the receiver, spp samples each
+    c = (np.arange(res) + 0.5) / res * 2.0 - 1.0
+    yy, xx = np.meshgrid(c, c, indexing="ij")
+    pix = W.plane_queries(np.stack([xx.ravel(), yy.ravel()], axis=1).astype(np.float32))
+    npix = pix.shape[1]
+
+    def render(spp, seed, offset, learned):
+        ctx.set_proposal(prop if learned else None, 0.1)
+        per_call = max(1, (1 << 21) // npix)
+        acc = torch.zeros(npix, dtype=torch.float64, device=f"cuda:{dev}")
+        ms = 0.0
+        done = 0
+        while done < spp:
+            k = min(per_call, spp - done)
+            q = torch.from_numpy(np.tile(pix, (1, k))).to(f"cuda:{dev}")
+            v, t = connect_timed(torch, sms, ctx, "ss", q, npix * k, seed=seed, stream_offset=offset + done * npix)
+            acc += v[0].view(k, npix).double().sum(0)
+            ms += t
+            done += k
+        ctx.set_proposal(None)
+        return (acc / spp).cpu().numpy(), ms
+
+    ref, ref_ms = render(ref_spp, 11, 1 << 30, False)
+    rows = []
+    for learned in (False, True):
+        for spp in (4, 16, 64):
+            img, ms = render(spp, 12 + spp, 1 << 28, learned)
+            rmse = float(np.sqrt(np.mean((img - ref) ** 2)))
+            rows.append({"seeding": "learned" if learned else "uniform", "spp": spp, "ms": ms, "rmse": rmse})
+    uni64 = next(r for r in rows if r["seeding"] == "uniform" and r["spp"] == 64)
+    reach = [r for r in rows if r["seeding"] == "learned" and r["rmse"] <= uni64["rmse"]]
+    t_equal = min(r["ms"] for r in reach) if reach else None
+    # per-sample efficiency: MSE x time at 64 spp (lower is better)
+    eff = {}
+    for mode in ("uniform", "learned"):
+        r = next(x for x in rows if x["seeding"] == mode and x["spp"] == 64)
+        eff[mode] = r["rmse"] ** 2 * r["ms"]
+    prop.close()
+    return {
+        "workload": f"water 512^2 unbiased (trials<=256), {res}x{res} receiver image, reference {ref_spp} spp uniform",
+        "pairs": total, "collect_ms": t_collect.ms, "collect_queries": calls * chunk,
+        "train": {"steps": steps, "batch": batch, "lr": lr, "loss_start": loss0, "loss_end": loss,
+                  "ms_per_step": step_ms, "wall_s": train_wall,
+                  "roofline": {"bound": "tensor", "achieved": flop_step / (step_ms / 1e3) / 1e12,
+                               "unit": "TFLOP/s", "flop_per_step": flop_step}},
+        "reference_ms": ref_ms,
+        "renders": rows,
+        "learned_ms_to_uniform64_rmse": t_equal,
+        "time_ratio_to_equal_rmse": (uni64["ms"] / t_equal) if t_equal else None,
+        "mse_x_time_ratio_64spp": eff["uniform"] / max(eff["learned"], 1e-30),
+    }
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -289,6 +430,19 @@ def run_ours(args):
         "clocks": clk,
         "wall_s": wall,
     }
+    if rank == 0 and world == 1 and not args.no_learned:
+        bf16_peak = None
+        pp = ROOT / "MEASURED_PEAKS.json"
+        if pp.exists():
+            bf16_peak = json.loads(pp.read_text()).get("bf16_tflops")
+        lt = learned_study(torch, sms, W, ctx, dev)
+        rl = lt["train"]["roofline"]
+        rl["peak"] = bf16_peak or 1900.0
+        rl["frac"] = rl["achieved"] / rl["peak"]
+        rl["peak_kind"] = "measured" if bf16_peak else "fallback"
+        line["learned"] = lt
+    if rank == 0 and world == 1 and not args.no_configs:
+        line["configs"] = secondary_configs(torch, sms, W, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         sample = int(os.environ.get("SMS_CPU_SAMPLE", str(N_QUERIES)))
@@ -309,6 +463,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal study")
+    ap.add_argument("--no-configs", action="store_true", help="skip the sphere / slab / glint configurations")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -155,6 +155,12 @@ void      *sms_ctx_stream(sms_ctx *ctx);
 /* Launch shape of the persistent kernels: blocks per SM and threads per block
  * (0 = library default).  Set by the autotuner. */
 sms_status sms_ctx_set_launch(sms_ctx *ctx, int32_t blocks_per_sm, int32_t threads_per_block);
+/* Lanes per query of the unbiased estimator's Bernoulli-trial kernel: 8, 16
+ * or 32 trials of one query run side by side (the first success is found by
+ * ballot, so results do not depend on it); 0 picks 32 for uniform seeding and
+ * 8 with a learned proposal.  No counterpart in the reference (a tuning knob
+ * of the batched solver). */
+sms_status sms_ctx_set_trial_group(sms_ctx *ctx, int32_t group);
 
 /* ---------------------------------------------------------------- queries */
 /* Shading-point query, SoA with SMS_QUERY_FIELDS rows of n floats each:
@@ -330,6 +336,95 @@ sms_status sms_glint_connect_batch_device(sms_ctx *ctx, const float *queries_dev
 #define SMS_GLINT_WALK_OUT_FIELDS 6
 sms_status sms_glint_walk_batch(sms_ctx *ctx, const float *queries,
                                 const float *walk_in, uint32_t n, float *walk_out);
+
+/* ---------------------------------------------------- learned proposal */
+/* No counterpart in the reference, whose walks are always seeded uniformly on
+ * the caster (manifold_ss.cpp:223, Shape::sample_position).  A proposal is a
+ * small network (9 features: shading point, light sample, shading normal,
+ * normalised and frequency-encoded -> 4 x 64 SiLU -> 8-component Gaussian
+ * mixture over the caster's uv frame)
+ * trained on the GPU from walks that the uniform-seed solver itself
+ * converges.  Bound to a context, it seeds the unbiased single-scatter
+ * estimator's first walk and every Bernoulli trial of that caster from
+ *   q(uv) = defensive * uniform + (1 - defensive) * mixture(query),
+ * three random numbers per walk instead of two.  The trials redraw from the
+ * same q, so their count still estimates 1 / P(reaching the first solution)
+ * and the estimator stays unbiased; the uniform component keeps every
+ * solution reachable.
+ * uv frame of a caster: mesh -> its bounding box spanned by the two widest
+ * axes (uv in [0,1]^2 covers the box, the third axis at mid-height); sphere ->
+ * (theta / pi, phi / 2 pi).  The network's mean outputs are offsets from an
+ * anchor uv computed in FP32: where the segment from the shading point to the
+ * light sample meets the frame's plane (mesh, clamped to [-1, 2]^2), or the
+ * sphere point along the bisector of the directions from the centre to the
+ * shading point and to the light sample (sphere). */
+#define SMS_PROPOSAL_FEATURES 9      /* x (3), light sample (3), n (3)    */
+#define SMS_PROPOSAL_OUTPUTS 40      /* 8 logits, 8 x 2 means, 8 x 2 raw  */
+#define SMS_PROPOSAL_PARAMS 21808    /* FP32 master parameters            */
+typedef struct sms_proposal sms_proposal;
+
+/* A fresh network for caster shape `caster` of ctx (a SMS_SHAPE_CAUSTIC_CASTER_SINGLE
+ * shape), initialised from `init_seed`, with room for `capacity` training
+ * pairs on the device.  Destroy proposals before their context. */
+sms_status sms_proposal_create(sms_ctx *ctx, int32_t caster, uint64_t init_seed,
+                               uint32_t capacity, sms_proposal **out);
+sms_status sms_proposal_destroy(sms_proposal *p);
+
+/* Training pairs from the solver: for each query (device SoA, as
+ * sms_ss_connect_batch) the emitter sample and `walks_per_query` uniformly
+ * seeded walks on the stream (seed, stream_offset + i); each distinct solution
+ * they converge to (uniqueness threshold of the config) that the light sample
+ * sees appends one pair (features, uv of the solution).  Pairs are appended
+ * to those already held; *total = pairs held afterwards (at most capacity).
+ * Synchronous. */
+sms_status sms_proposal_collect(sms_proposal *p, const float *queries_dev, uint32_t n,
+                                uint64_t seed, uint64_t stream_offset,
+                                int32_t walks_per_query, uint32_t *total);
+/* Replace the training set with host arrays (features SoA 9 x n, uv SoA 2 x n). */
+sms_status sms_proposal_set_data(sms_proposal *p, const float *features, const float *uv,
+                                 uint32_t n);
+/* Read the training set back (host arrays sized as above for *n = count). */
+sms_status sms_proposal_get_data(sms_proposal *p, float *features, float *uv, uint32_t cap,
+                                 uint32_t *n);
+/* Set the input normalisation (x - shift) * scale from the training set's
+ * mean and standard deviation (features with zero spread get scale 0). */
+sms_status sms_proposal_normalize(sms_proposal *p);
+
+/* `steps` Adam steps (lr, beta 0.9 / 0.999, eps 1e-8) on batches of `batch`
+ * pairs (multiple of 16, <= 65536) drawn with replacement from the training
+ * set; the mean batch NLL of the last min(steps, 256) steps in *mean_loss.
+ * Steps are replayed from a CUDA graph. Synchronous. */
+sms_status sms_proposal_train(sms_proposal *p, int32_t steps, int32_t batch, float lr,
+                              float *mean_loss);
+/* Loss and gradient of the first `batch` pairs of the training set without
+ * an update (gradient checks): *loss = mean NLL, grad = d loss / d params. */
+sms_status sms_proposal_loss_grad(sms_proposal *p, int32_t batch, float *loss, float *grad);
+
+/* Network state for checkpoint / resume.  params, adam_m, adam_v: 21808
+ * floats each (any may be NULL on get); norm: shift (9) then scale (9);
+ * step: Adam steps taken. */
+sms_status sms_proposal_get_state(sms_proposal *p, float *params, float *adam_m, float *adam_v,
+                                  float *norm, uint32_t *step);
+sms_status sms_proposal_set_state(sms_proposal *p, const float *params, const float *adam_m,
+                                  const float *adam_v, const float *norm, uint32_t step);
+
+/* Network outputs for host feature arrays (9 x n): mixture = 0 gives the raw
+ * 40 outputs (logits, mean offsets from the anchor, log-sigma logits),
+ * mixture = 1 the processed mixture the seeding uses: cdf (8), means (8 x 2,
+ * anchor added), sigmas (8 x 2).  out: 40 x n. */
+sms_status sms_proposal_eval(sms_proposal *p, const float *features, uint32_t n, int32_t mixture,
+                             float *out);
+
+/* The caster's uv frame: kind (0 box, 1 sphere), org (3), ax_u (3), ax_v (3);
+ * box: seed = org + u ax_u + v ax_v; sphere: org + ax_u[0] * (sin(pi u)
+ * cos(2 pi v), sin(pi u) sin(2 pi v), cos(pi u)). */
+sms_status sms_proposal_frame(sms_proposal *p, float frame[10]);
+
+/* Bind a proposal to its context (NULL unbinds); defensive in (0, 1] is the
+ * uniform seeding's share.  While bound, the unbiased single-scatter entry
+ * points seed its caster from the proposal; the biased estimator and the
+ * allocation-free entry point return SMS_ERR_UNSUPPORTED. */
+sms_status sms_ctx_set_proposal(sms_ctx *ctx, sms_proposal *p, float defensive);
 
 #ifdef __cplusplus
 }

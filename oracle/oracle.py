@@ -73,6 +73,9 @@ def load(fma: bool = False):
         "oracle_glint_walk_batch": (i32, [vp, C.POINTER(_Config), vp, vp, u32, vp]),
         "oracle_glint_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
         "oracle_nm_slope": (None, [vp, f32, f32, vp]),
+        "oracle_ss_emitter_batch": (i32, [vp, vp, u32, u64, u64, vp]),
+        "oracle_ss_connect_learned_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, i32, f32, vp, vp,
+                                                  vp, vp, vp, C.c_int, vp]),
         "oracle_fresnel": (f32, [f32, f32, C.POINTER(f32)]),
         "oracle_fresnel_conductor": (f32, [f32, f32, f32]),
         "oracle_uniform_sphere": (None, [f32, f32, C.POINTER(f32)]),
@@ -185,6 +188,38 @@ class OracleScene:
               self._lib.oracle_ms_connect_batch if multi else self._lib.oracle_ss_connect_batch)
         fn(self._h, C.byref(_cfg(config)), q.ctypes.data, n, seed, stream_offset, value.ctypes.data,
            count.ctypes.data, walks.ctypes.data, nt, stats.ctypes.data)
+        names = ["solver_succeeded", "solver_failed", "bernoulli_trial_calls", "bernoulli_trial_iterations",
+                 "bernoulli_trial_iterations_max", "walks", "newton_iterations", "connections"]
+        return value, count, walks, dict(zip(names, stats.tolist()))
+
+    def emitter_batch(self, queries: np.ndarray, seed: int = 0, stream_offset: int = 0) -> np.ndarray:
+        """The single-scatter estimator's emitter sample per query: rows ei.p
+        (3), valid."""
+        n = queries.shape[1]
+        q = np.ascontiguousarray(queries, np.float32)
+        out = np.zeros((4, n), np.float32)
+        self._lib.oracle_ss_emitter_batch(self._h, q.ctypes.data, n, seed, stream_offset, out.ctypes.data)
+        return out
+
+    def connect_learned_batch(self, config, queries: np.ndarray, shape: int, defensive: float, frame: np.ndarray,
+                              mixture: np.ndarray, seed: int = 0, stream_offset: int = 0,
+                              nthreads: int | None = None):
+        """Unbiased single scatter seeded by a learned proposal: mixture is the
+        processed per-query mixture (40 x n), frame the caster's uv frame."""
+        n = queries.shape[1]
+        q = np.ascontiguousarray(queries, np.float32)
+        fr = np.ascontiguousarray(frame, np.float32)
+        mx = np.ascontiguousarray(mixture, np.float32)
+        assert mx.shape == (40, n) and fr.shape == (10,)
+        value = np.zeros((3, n), np.float32)
+        count = np.zeros(n, np.int32)
+        walks = np.zeros(n, np.int32)
+        stats = np.zeros(8, np.uint64)
+        nt = nthreads or os.cpu_count() or 1
+        self._lib.oracle_ss_connect_learned_batch(self._h, C.byref(_cfg(config)), q.ctypes.data, n, seed,
+                                                  stream_offset, shape, defensive, fr.ctypes.data, mx.ctypes.data,
+                                                  value.ctypes.data, count.ctypes.data, walks.ctypes.data, nt,
+                                                  stats.ctypes.data)
         names = ["solver_succeeded", "solver_failed", "bernoulli_trial_calls", "bernoulli_trial_iterations",
                  "bernoulli_trial_iterations_max", "walks", "newton_iterations", "connections"]
         return value, count, walks, dict(zip(names, stats.tolist()))

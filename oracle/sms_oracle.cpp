@@ -1018,8 +1018,50 @@ static void update_max(std::atomic<uint64_t> &a, uint64_t v) {
 }
 
 /* manifold_ss.cpp:28-201 */
+/* Learned seed proposal (no counterpart in the reference: it always seeds
+ * uniformly, manifold_ss.cpp:223).  For the proposal's caster every walk
+ * draws three numbers: u_sel, then the 2D sample.  u_sel < defensive keeps
+ * the reference's uniform seeding with the 2D sample; otherwise component k
+ * of the query's mixture (first k with u' < cdf[k], u' = (u_sel - defensive)
+ * / (1 - defensive)) gives uv = mean_k + sigma_k * z with z from Box-Muller
+ * (r = sqrt(-2 ln(1 - x)), angle 2 pi y), mapped to a seed point through the
+ * caster's uv frame.  mix: 40 values of this query (cdf 8, means 16, sigmas
+ * 16) with stride `stride`. */
+struct Learned {
+    int shape = -1;
+    float defensive = 1.f;
+    int kind = 0;               /* 0 box frame, 1 sphere */
+    V3 org, ax_u, ax_v;
+    const float *mix = nullptr;
+    size_t stride = 0;
+};
+
+static V3 learned_seed_point(const Learned &L, float u, float v) {
+    if (L.kind == 1) {
+        float th = kPi * u, ph = 2.f * kPi * v;
+        return L.org + V3(std::sin(th) * std::cos(ph), std::sin(th) * std::sin(ph), std::cos(th)) * L.ax_u.x;
+    }
+    return L.org + L.ax_u * u + L.ax_v * v;
+}
+
+/* one walk's seed: returns p_start for sample_path (zero = uniform seeding
+ * with `sample`) */
+static V3 learned_seed(const Learned &L, PCG32 &rng, V2 &sample) {
+    float us = rng.next_f32();
+    sample = rng.next_2d();
+    if (us < L.defensive) return V3(0.f);
+    float u2 = (us - L.defensive) / (1.f - L.defensive);
+    int k = 0;
+    while (k < 7 && u2 >= L.mix[(size_t)k * L.stride]) ++k;
+    float r = std::sqrt(-2.f * std::log(1.f - sample.x));
+    float ang = 2.f * kPi * sample.y;
+    float u = L.mix[(size_t)(8 + 2 * k) * L.stride] + L.mix[(size_t)(24 + 2 * k) * L.stride] * (r * std::cos(ang));
+    float v = L.mix[(size_t)(9 + 2 * k) * L.stride] + L.mix[(size_t)(25 + 2 * k) * L.stride] * (r * std::sin(ang));
+    return learned_seed_point(L, u, v);
+}
+
 static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG32 &rng,
-                     int &count_out, int &walks_out, Stats &st) {
+                     int &count_out, int &walks_out, Stats &st, const Learned *learned = nullptr) {
     count_out = 0; walks_out = 0;
     EI ei = sample_emitter_interaction(sc, sc.emitters_ss, q, rng);
     V3 result(0.f);
@@ -1031,7 +1073,15 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
         int it = 0;
         if (!cfg.biased) {
             count_out = 0;
-            bool ok = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), si_final, si_init, it);
+            const bool lrn = learned && learned->shape == caster;
+            auto seed_of = [&](V2 &smp) -> V3 {
+                if (lrn) return learned_seed(*learned, rng, smp);
+                smp = rng.next_2d();
+                return V3(0.f);
+            };
+            V2 smp;
+            V3 ps = seed_of(smp);
+            bool ok = sample_path(sc, cfg, caster, q, ei, smp, ps, si_final, si_init, it);
             walks_out++; st.walks++; st.newton += it;
             if (!ok) { st.failed++; continue; }
             st.succeeded++;
@@ -1045,7 +1095,9 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             while (true) {
                 SI sf, si0;
                 int it2 = 0;
-                bool ok2 = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), sf, si0, it2);
+                V2 smp2;
+                V3 ps2 = seed_of(smp2);
+                bool ok2 = sample_path(sc, cfg, caster, q, ei, smp2, ps2, sf, si0, it2);
                 walks_out++; st.walks++; st.newton += it2;
                 if (ok2) {
                     V3 dt = normalize(sf.p - q.p);
@@ -2029,6 +2081,74 @@ int oracle_ss_connect_batch(void *s, const sms_config *cfg, const float *queries
                 rng.seed(seed, (uint64_t)i + stream_offset);
                 int c = 0, w = 0;
                 V3 v = ss_connect(*sc, *cfg, q, rng, c, w, st);
+                value[i] = v.x; value[(size_t)n + i] = v.y; value[2 * (size_t)n + i] = v.z;
+                count[i] = c; walks[i] = w;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
+    worker();
+    for (auto &t : th) t.join();
+    if (stats_out) {
+        stats_out[0] = st.succeeded; stats_out[1] = st.failed; stats_out[2] = st.calls;
+        stats_out[3] = st.iters; stats_out[4] = st.iters_max; stats_out[5] = st.walks;
+        stats_out[6] = st.newton; stats_out[7] = st.connections;
+    }
+    return 0;
+}
+
+/* The emitter interaction the single-scatter estimator draws first for each
+ * query (stream (seed, stream_offset + i), manifold.h:204-260): out rows
+ * ei.p (3), valid (1). */
+int oracle_ss_emitter_batch(void *s, const float *queries, uint32_t n, uint64_t seed, uint64_t stream_offset,
+                            float *out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    for (uint32_t i = 0; i < n; ++i) {
+        Query q = load_query(queries, n, i);
+        PCG32 rng;
+        rng.seed(seed, (uint64_t)i + stream_offset);
+        EI ei = sample_emitter_interaction(*sc, sc->emitters_ss, q, rng);
+        out[i] = ei.p.x; out[(size_t)n + i] = ei.p.y; out[2 * (size_t)n + i] = ei.p.z;
+        out[3 * (size_t)n + i] = ei.emitter >= 0 ? 1.f : 0.f;
+    }
+    return 0;
+}
+
+/* Unbiased single scatter with a learned proposal on caster `shape`: mix is
+ * the processed mixture per query (40 x n, as sms_proposal_eval with
+ * mixture = 1), frame = kind, org (3), ax_u (3), ax_v (3). */
+int oracle_ss_connect_learned_batch(void *s, const sms_config *cfg, const float *queries, uint32_t n,
+                                    uint64_t seed, uint64_t stream_offset, int shape, float defensive,
+                                    const float *frame, const float *mix, float *value, int32_t *count,
+                                    int32_t *walks, int nthreads, uint64_t *stats_out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    Stats st;
+    if (nthreads < 1) nthreads = 1;
+    std::atomic<uint32_t> next{0};
+    const uint32_t block = 64;
+    auto worker = [&]() {
+        while (true) {
+            uint32_t b = next.fetch_add(block);
+            if (b >= n) break;
+            uint32_t e = std::min(n, b + block);
+            for (uint32_t i = b; i < e; ++i) {
+                Learned L;
+                L.shape = shape;
+                L.defensive = defensive;
+                L.kind = (int)frame[0];
+                L.org = V3(frame[1], frame[2], frame[3]);
+                L.ax_u = V3(frame[4], frame[5], frame[6]);
+                L.ax_v = V3(frame[7], frame[8], frame[9]);
+                L.mix = mix + i;
+                L.stride = n;
+                Query q = load_query(queries, n, i);
+                PCG32 rng;
+                rng.seed(seed, (uint64_t)i + stream_offset);
+                int c = 0, w = 0;
+                V3 v = ss_connect(*sc, *cfg, q, rng, c, w, st, &L);
                 value[i] = v.x; value[(size_t)n + i] = v.y; value[2 * (size_t)n + i] = v.z;
                 count[i] = c; walks[i] = w;
             }

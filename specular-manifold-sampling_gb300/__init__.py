@@ -45,6 +45,10 @@ EMITTER_CAUSTIC_MULTI = 1 << 1
 
 BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_CONDUCTOR = 0, 1, 2
 
+PROPOSAL_FEATURES = 9
+PROPOSAL_OUTPUTS = 40
+PROPOSAL_PARAMS = 21808
+
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device limit",
                 4: "unsupported", 5: "parse error", 6: "no device"}
 
@@ -118,6 +122,7 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ctx_set_config": (i32, [vp, C.POINTER(_Config)]),
         "sms_ctx_stream": (vp, [vp]),
         "sms_ctx_set_launch": (i32, [vp, i32, i32]),
+        "sms_ctx_set_trial_group": (i32, [vp, i32]),
         "sms_stats_read": (i32, [vp, C.POINTER(_Stats)]),
         "sms_stats_reset": (i32, [vp]),
         "sms_ctx_set_profiling": (i32, [vp, i32]),
@@ -133,6 +138,19 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_glint_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_glint_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_glint_walk_batch": (i32, [vp, vp, vp, u32, vp]),
+        "sms_proposal_create": (i32, [vp, i32, u64, u32, C.POINTER(vp)]),
+        "sms_proposal_destroy": (i32, [vp]),
+        "sms_proposal_collect": (i32, [vp, vp, u32, u64, u64, i32, C.POINTER(u32)]),
+        "sms_proposal_set_data": (i32, [vp, vp, vp, u32]),
+        "sms_proposal_get_data": (i32, [vp, vp, vp, u32, C.POINTER(u32)]),
+        "sms_proposal_normalize": (i32, [vp]),
+        "sms_proposal_train": (i32, [vp, i32, i32, f32, C.POINTER(f32)]),
+        "sms_proposal_loss_grad": (i32, [vp, i32, C.POINTER(f32), vp]),
+        "sms_proposal_get_state": (i32, [vp, vp, vp, vp, vp, C.POINTER(u32)]),
+        "sms_proposal_set_state": (i32, [vp, vp, vp, vp, vp, u32]),
+        "sms_proposal_eval": (i32, [vp, vp, u32, i32, vp]),
+        "sms_ctx_set_proposal": (i32, [vp, vp, f32]),
+        "sms_proposal_frame": (i32, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -323,6 +341,10 @@ class Context:
     def set_launch(self, blocks_per_sm: int = 0, threads_per_block: int = 0):
         _check(_LIB.sms_ctx_set_launch(self._h, blocks_per_sm, threads_per_block))
 
+    def set_trial_group(self, group: int = 0):
+        """Lanes per query of the Bernoulli-trial kernel (0 auto, 8, 16, 32)."""
+        _check(_LIB.sms_ctx_set_trial_group(self._h, group))
+
     def stats(self) -> dict:
         s = _Stats()
         _check(_LIB.sms_stats_read(self._h, C.byref(s)))
@@ -342,9 +364,119 @@ class Context:
                        "bvh_nodes": p.bvh_nodes[k], "tri_tests": p.tri_tests[k]}
                 for k, name in enumerate(PHASES)}
 
+    def set_proposal(self, proposal: "SeedProposal | None", defensive: float = 0.1):
+        """Seed the unbiased single-scatter estimator from a learned proposal
+        (None restores uniform seeding)."""
+        _check(_LIB.sms_ctx_set_proposal(self._h, proposal.handle if proposal else None, defensive))
+        self._proposal = proposal
+
     def close(self):
         if getattr(self, "_h", None) and _LIB is not None:
             _LIB.sms_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class SeedProposal:
+    """Learned seed proposal for one single-scatter caster (sms_proposal).
+
+    No counterpart in the reference, whose walks are seeded uniformly on the
+    caster (manifold_ss.cpp:223).  The network maps (shading point, light
+    sample, shading normal) to an 8-component Gaussian mixture over the
+    caster's uv frame; bound with Context.set_proposal it seeds the unbiased
+    estimator, mixed with the uniform seeding."""
+
+    def __init__(self, ctx: Context, caster: int, seed: int = 0, capacity: int = 1 << 22):
+        h = C.c_void_p()
+        _check(_LIB.sms_proposal_create(ctx.handle, caster, seed, capacity, C.byref(h)))
+        self._h = h
+        self._ctx = ctx
+        self.capacity = capacity
+
+    @property
+    def handle(self):
+        return self._h
+
+    def collect(self, queries_ptr: int, n: int, seed: int = 0, stream_offset: int = 0,
+                walks_per_query: int = 1) -> int:
+        """Append the solver's converged uniform-seed walks for device queries;
+        returns the pairs held."""
+        total = C.c_uint32()
+        _check(_LIB.sms_proposal_collect(self._h, queries_ptr, n, seed, stream_offset, walks_per_query,
+                                         C.byref(total)))
+        return total.value
+
+    def set_data(self, features: np.ndarray, uv: np.ndarray):
+        n = features.shape[1]
+        f = _soa(features, PROPOSAL_FEATURES, n)
+        u = _soa(uv, 2, n)
+        _check(_LIB.sms_proposal_set_data(self._h, _ptr(f), _ptr(u), n))
+
+    def get_data(self) -> tuple[np.ndarray, np.ndarray]:
+        n = C.c_uint32()
+        _check(_LIB.sms_proposal_get_data(self._h, None, None, 0, C.byref(n)))
+        f = np.zeros((PROPOSAL_FEATURES, n.value), np.float32)
+        u = np.zeros((2, n.value), np.float32)
+        _check(_LIB.sms_proposal_get_data(self._h, _ptr(f), _ptr(u), n.value, C.byref(n)))
+        return f, u
+
+    def normalize(self):
+        _check(_LIB.sms_proposal_normalize(self._h))
+
+    def train(self, steps: int, batch: int = 8192, lr: float = 1e-3) -> float:
+        loss = C.c_float()
+        _check(_LIB.sms_proposal_train(self._h, steps, batch, lr, C.byref(loss)))
+        return loss.value
+
+    def loss_grad(self, batch: int) -> tuple[float, np.ndarray]:
+        loss = C.c_float()
+        g = np.zeros(PROPOSAL_PARAMS, np.float32)
+        _check(_LIB.sms_proposal_loss_grad(self._h, batch, C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def state(self) -> dict:
+        p, m, v = (np.zeros(PROPOSAL_PARAMS, np.float32) for _ in range(3))
+        norm = np.zeros(2 * PROPOSAL_FEATURES, np.float32)
+        step = C.c_uint32()
+        _check(_LIB.sms_proposal_get_state(self._h, _ptr(p), _ptr(m), _ptr(v), _ptr(norm), C.byref(step)))
+        return {"params": p, "adam_m": m, "adam_v": v, "norm": norm, "step": step.value}
+
+    def load_state(self, st: dict):
+        arr = {k: np.ascontiguousarray(st[k], np.float32) for k in ("params", "adam_m", "adam_v", "norm")
+               if st.get(k) is not None}
+        _check(_LIB.sms_proposal_set_state(
+            self._h, _ptr(arr["params"]), _ptr(arr["adam_m"]) if "adam_m" in arr else None,
+            _ptr(arr["adam_v"]) if "adam_v" in arr else None, _ptr(arr["norm"]) if "norm" in arr else None,
+            int(st.get("step", 0))))
+
+    def save(self, path):
+        """Checkpoint (weights, Adam state, normalisation, step) as .npz."""
+        np.savez(path, **self.state())
+
+    def load(self, path):
+        with np.load(path) as z:
+            self.load_state({k: z[k] for k in z.files})
+
+    def frame(self) -> np.ndarray:
+        """kind, org (3), ax_u (3), ax_v (3) of the caster's uv frame."""
+        f = np.zeros(10, np.float32)
+        _check(_LIB.sms_proposal_frame(self._h, _ptr(f)))
+        return f
+
+    def eval(self, features: np.ndarray, mixture: bool = False) -> np.ndarray:
+        """Raw outputs (40 x n) or the processed mixture: cdf (8), means
+        (8 x 2), sigmas (8 x 2)."""
+        n = features.shape[1]
+        f = _soa(features, PROPOSAL_FEATURES, n)
+        out = np.zeros((PROPOSAL_OUTPUTS, n), np.float32)
+        _check(_LIB.sms_proposal_eval(self._h, _ptr(f), n, int(mixture), _ptr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None) and _LIB is not None:
+            _LIB.sms_proposal_destroy(self._h)
             self._h = None
 
     def __del__(self):

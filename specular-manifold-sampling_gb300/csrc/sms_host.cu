@@ -343,6 +343,7 @@ struct sms_ctx {
     int num_sms = 0;
     int blocks_per_sm = 0;
     int threads = 128;
+    int trial_group = 0;          // lanes per query of the Bernoulli-trial kernel (0: auto)
     // device staging for the host-pointer entry points
     void *io = nullptr;
     size_t io_bytes = 0;
@@ -353,6 +354,13 @@ struct sms_ctx {
     uint32_t ms_tmpl_n = 0;
     PhaseTimer timer;
     std::vector<int> casters_ss;
+    // learned seed proposal: uv frame of every shape, the bound proposal and
+    // its per-query mixture scratch (kGmmParams x gmm_n floats)
+    std::vector<mlp::SeedFrame> frames;
+    sms_proposal *prop = nullptr;
+    float defensive = 0.1f;
+    float *gmm = nullptr;
+    uint32_t gmm_n = 0;
 };
 
 template <typename T>
@@ -396,9 +404,39 @@ extern "C" void sms_ctx_destroy(sms_ctx *c) {
     if (c->io) cudaFree(c->io);
     if (c->scratch) cudaFree(c->scratch);
     if (c->ms_tmpl) cudaFree(c->ms_tmpl);
+    if (c->gmm) cudaFree(c->gmm);
+    if (c->prop) proposal_detach(c->prop);
     if (c->ctr) cudaFree(c->ctr);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+// uv frame of the learned proposal for one shape (sms_proposal_create):
+// spheres (theta / pi, phi / 2 pi); meshes their bounding box over the two
+// widest axes, the third axis at mid-height.
+static mlp::SeedFrame seed_frame(const HostShape &h) {
+    mlp::SeedFrame f;
+    std::memset(&f, 0, sizeof(f));
+    if (h.kind == kShapeSphere) {
+        f.kind = 1;
+        for (int k = 0; k < 3; ++k) f.org[k] = h.center[k];
+        f.ax_u[0] = h.radius;
+        return f;
+    }
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t i = 0; i + 2 < h.P.size(); i += 3)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], h.P[i + k]);
+            hi[k] = std::max(hi[k], h.P[i + k]);
+        }
+    int ax[3] = {0, 1, 2};
+    std::sort(ax, ax + 3, [&](int a, int b) { return hi[a] - lo[a] > hi[b] - lo[b] || (hi[a] - lo[a] == hi[b] - lo[b] && a < b); });
+    f.kind = 0;
+    for (int k = 0; k < 3; ++k) f.org[k] = lo[k];
+    f.org[ax[2]] = 0.5f * (lo[ax[2]] + hi[ax[2]]);
+    f.ax_u[ax[0]] = hi[ax[0]] - lo[ax[0]];
+    f.ax_v[ax[1]] = hi[ax[1]] - lo[ax[1]];
+    return f;
 }
 
 static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
@@ -423,6 +461,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
                         (h.bsdf.type == SMS_BSDF_CONDUCTOR && h.bsdf.k == 0.f);
         ds.spec_eta = real_ior ? h.bsdf.eta : 1.f;
         ds.emitter = h.emitter;
+        c->frames.push_back(seed_frame(h));
         if (h.kind == kShapeSphere) {
             ds.cx = h.center[0]; ds.cy = h.center[1]; ds.cz = h.center[2];
             ds.radius = h.radius;
@@ -584,6 +623,14 @@ extern "C" sms_status sms_ctx_set_config(sms_ctx *c, const sms_config *cfg) {
 
 extern "C" void *sms_ctx_stream(sms_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+extern "C" sms_status sms_ctx_set_trial_group(sms_ctx *c, int32_t group) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    if (group != 0 && group != 8 && group != 16 && group != 32)
+        return fail(SMS_ERR_INVALID_ARG, "trial group must be 0 (auto), 8, 16 or 32");
+    c->trial_group = group;
+    return SMS_OK;
+}
+
 extern "C" sms_status sms_ctx_set_launch(sms_ctx *c, int32_t bps, int32_t tpb) {
     if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
     if (bps < 0 || tpb < 0) return fail(SMS_ERR_INVALID_ARG, "negative launch parameter");
@@ -691,13 +738,51 @@ extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, ui
     if (n == 0) return SMS_OK;
     if (c->cfg.biased && c->cfg.max_trials > (1 << 24))
         return fail(SMS_ERR_INVALID_ARG, "max_trials too large for the biased estimator");
+    if (c->prop && c->cfg.biased)
+        return fail(SMS_ERR_UNSUPPORTED, "a learned proposal seeds the unbiased estimator only");
     CUDA_TRY(cudaSetDevice(c->device));
     SsScratch scr{};
     if (!c->cfg.biased)
         if (sms_status st = ensure_scratch(c, n, scr)) return st;
+    mlp::SeedProposal pr{};
+    if (c->prop) {
+        if (c->gmm_n < n) {
+            if (c->gmm) {
+                CUDA_TRY(cudaStreamSynchronize(c->stream));
+                cudaFree(c->gmm);
+                c->gmm = nullptr;
+                c->gmm_n = 0;
+            }
+            CUDA_TRY(cudaMalloc(&c->gmm, (size_t)mlp::kGmmParams * n * sizeof(float)));
+            c->gmm_n = n;
+        }
+        if (!proposal_seed_desc(c->prop, pr)) return fail(SMS_ERR_INVALID_ARG, "proposal is not usable");
+        pr.defensive = c->defensive;
+        pr.gmm = c->gmm;
+    }
     CUDA_TRY(launch_ss_connect(c->dsc, solver_cfg(c->cfg), q, n, seed, stream_off, out->value, out->count,
-                               out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, &c->timer, c->stream));
+                               out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, &c->timer, c->stream,
+                               c->prop ? &pr : nullptr, c->trial_group));
     return SMS_OK;
+}
+
+extern "C" sms_status sms_ctx_set_proposal(sms_ctx *c, sms_proposal *p, float defensive) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    if (!p) {
+        c->prop = nullptr;
+        return SMS_OK;
+    }
+    if (proposal_ctx(p) != c) return fail(SMS_ERR_INVALID_ARG, "proposal belongs to another context");
+    if (!(defensive > 0.f && defensive <= 1.f))
+        return fail(SMS_ERR_INVALID_ARG, "defensive share must lie in (0, 1]");
+    c->prop = p;
+    c->defensive = defensive;
+    return SMS_OK;
+}
+
+// Context side of a proposal's lifetime (sms_proposal.cu).
+void ctx_forget_proposal(sms_ctx *c, sms_proposal *p) {
+    if (c && c->prop == p) c->prop = nullptr;
 }
 
 // Device staging buffer of the host-pointer entry points, grown on demand and
@@ -786,6 +871,10 @@ bool ctx_view(sms_ctx *c, CtxView &out) {
     out.num_sms = c->num_sms;
     out.blocks_per_sm = c->blocks_per_sm;
     out.timer = &c->timer;
+    out.frames = c->frames.data();
+    out.n_shapes = (int)c->frames.size();
+    out.proposal_bound = c->prop != nullptr;
+    out.trial_group = c->trial_group;
     return true;
 }
 

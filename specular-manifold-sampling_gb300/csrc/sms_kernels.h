@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "sms_mlp.h"
+
 namespace sms {
 
 struct DevScene;
@@ -59,7 +61,13 @@ cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster,
 cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n,
                               uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
                               DevCounters *ctr, const SsScratch &scr, int num_sms, int blocks_per_sm,
-                              PhaseTimer *tm, cudaStream_t s);
+                              PhaseTimer *tm, cudaStream_t s, const mlp::SeedProposal *prop = nullptr,
+                              int trial_group = 0);
+// Training pairs for a learned proposal (see ss_collect_kernel).
+cudaError_t launch_ss_collect(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q, uint32_t n,
+                              uint64_t seed, uint64_t stream_off, int per_query, const mlp::SeedFrame &fr,
+                              float *data, uint32_t cap, unsigned *fill, DevCounters *ctr, PhaseTimer *tm,
+                              cudaStream_t s);
 
 cudaError_t launch_ms_walk(const DevScene &sc, const SolverCfg &cfg, int bounces, int caster, const float *q,
                            const float *w, uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s);
@@ -84,6 +92,10 @@ struct CtxView {
     int num_sms;
     int blocks_per_sm;
     PhaseTimer *timer;
+    const mlp::SeedFrame *frames;   // learned-proposal uv frame per shape
+    int n_shapes;
+    bool proposal_bound;            // a learned proposal seeds the SS estimator
+    int trial_group;                // lanes per query of the trial kernel (0: auto)
 };
 
 }  // namespace sms
@@ -93,3 +105,13 @@ struct sms_ctx;
 bool ctx_view(sms_ctx *c, sms::CtxView &out);
 // Records msg as sms_last_error() for this thread and returns st.
 int set_last_error_impl(int st, const char *msg);
+
+// Learned proposals (sms_proposal.cu) and the context that binds them.
+struct sms_proposal;
+sms_ctx *proposal_ctx(sms_proposal *p);
+// Shape, frame and network of a proposal (defensive and gmm left to the caller).
+bool proposal_seed_desc(sms_proposal *p, sms::mlp::SeedProposal &out);
+// The context is going away: the proposal keeps working for nothing but destroy.
+void proposal_detach(sms_proposal *p);
+// A proposal is going away: unbind it from its context.
+void ctx_forget_proposal(sms_ctx *c, sms_proposal *p);

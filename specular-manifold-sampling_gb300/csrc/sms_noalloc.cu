@@ -63,6 +63,10 @@ extern "C" sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *qu
     if (n == 0) return SMS_OK;
     CtxView v;
     if (!ctx_view(ctx, v)) return set_last_error(SMS_ERR_INVALID_ARG, "sms_ss_connect_batch_noalloc: bad context");
+    if (v.proposal_bound)
+        return set_last_error(SMS_ERR_UNSUPPORTED,
+                              "sms_ss_connect_batch_noalloc: a bound learned proposal needs per-query mixture "
+                              "scratch; use sms_ss_connect_batch_device");
     cudaError_t e = cudaSetDevice(v.device);
     if (e != cudaSuccess) return set_last_error(SMS_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     void *base = nullptr;
@@ -81,7 +85,8 @@ extern "C" sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *qu
     // written before they are read within the call, and the trial-queue
     // counters live in the context and are cleared by the launch itself.
     e = launch_ss_connect(*v.scene, v.solver, queries_dev, n, seed, stream_offset, out_dev->value, out_dev->count,
-                          out_dev->walks, v.counters, scr, v.num_sms, v.blocks_per_sm, v.timer, v.stream);
+                          out_dev->walks, v.counters, scr, v.num_sms, v.blocks_per_sm, v.timer, v.stream, nullptr,
+                          v.trial_group);
     if (e != cudaSuccess) return set_last_error(SMS_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     return SMS_OK;
 }

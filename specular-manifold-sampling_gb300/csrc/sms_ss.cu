@@ -31,6 +31,7 @@
 #include "sms_device.cuh"
 #include "sms_estimator.cuh"
 #include "sms_kernels.h"
+#include "sms_mlp.cuh"
 
 namespace sms {
 
@@ -227,19 +228,67 @@ __global__ void __launch_bounds__(128) ss_biased_kernel(DevScene sc, SolverCfg c
 }
 
 // --------------------------------------------------- unbiased: first walks
-__global__ void __launch_bounds__(128) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+// kLearned: seeds come from the query's learned mixture (three draws per walk,
+// mlp::proposal_seed) instead of two-draw uniform seeding.  The warp first
+// evaluates the proposal network for its 32 queries on the tensor cores
+// (weights staged in shared memory), stores each query's mixture for the
+// trials kernel and then runs the first walk.
+template <bool kLearned>
+__global__ void __launch_bounds__(128, kLearned ? 3 : 4) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
                                                        float *__restrict__ value, int *__restrict__ count,
-                                                       int *__restrict__ walks, SsScratch scr, DevCounters *ctr) {
-    uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+                                                       int *__restrict__ walks, SsScratch scr, DevCounters *ctr,
+                                                       mlp::SeedProposal pr) {
+    const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = qi < n;
+    const unsigned lane = threadIdx.x & 31;
     LaneStats st;
     uint32_t err = 0;
     bool enqueue = false;
-    if (qi < n) {
-        Query Q = load_query(qs, n, qi);
-        Pcg32 rng = query_rng(seed, stream_off + qi, 0);
-        Light L;
-        bool have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
+    Query Q;
+    Pcg32 rng;
+    Light L;
+    bool have_light = false;
+    if (active) {
+        Q = load_query(qs, n, qi);
+        rng = query_rng(seed, stream_off + qi, 0);
+        have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
+    }
+    if constexpr (kLearned) {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        constexpr int kStage = 16 * mlp::kXLd / 2;   // floats: input tile, then output rows
+        __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+        float *feats = reinterpret_cast<float *>(smem_raw + (size_t)mlp::kWeightsFwd * 2) +
+                       (threadIdx.x / 32) * (32 * mlp::kIn + kStage);
+        float *stage = feats + 32 * mlp::kIn;
+        mlp::stage_weights(pr.net.wbf, sw, mlp::kWeightsFwd);
+        // this lane's normalised features: shading point, light sample, normal
+        const f3 fx = active ? Q.x : splat(0.f), fl = have_light ? L.p : splat(0.f), fn = active ? Q.n : splat(0.f);
+        const float fv[mlp::kIn] = {fx.x, fx.y, fx.z, fl.x, fl.y, fl.z, fn.x, fn.y, fn.z};
+        #pragma unroll
+        for (int k = 0; k < mlp::kIn; ++k) feats[lane * mlp::kIn + k] = (fv[k] - pr.net.shift[k]) * pr.net.scale[k];
+        __syncthreads();
+        #pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            float xn[mlp::kIn];
+            #pragma unroll
+            for (int k = 0; k < mlp::kIn; ++k) xn[k] = feats[(h * 16 + (lane & 15)) * mlp::kIn + k];
+            __nv_bfloat16 *sx = reinterpret_cast<__nv_bfloat16 *>(stage);
+            mlp::stage_inputs(xn, sx);
+            float o[6][4];
+            mlp::forward<false>(pr.net, sw, sx, o);
+            __syncwarp();
+            mlp::stage_outputs(o, stage);
+            __syncwarp();
+            if ((int)(lane >> 4) == h && active) {
+                float au, av;
+                mlp::anchor_uv(pr.net.frame, fx, fl, au, av);
+                mlp::mixture_from_raw(stage + (lane & 15) * mlp::kOutPad, pr.gmm + qi, n, au, av);
+            }
+            __syncwarp();
+        }
+    }
+    if (active) {
         uint32_t pos = 3u;
         f3 acc = splat(0.f);
         int nw = 0;
@@ -251,11 +300,18 @@ __global__ void __launch_bounds__(128) ss_first_kernel(DevScene sc, SolverCfg cf
             nw = walks[qi];
         }
         if (have_light) {
-            int caster = sc.casters_ss[c];
+            const int caster = sc.casters_ss[c];
             rng.advance(pos - 3u);
-            float sx = rng.next_f32(), sy = rng.next_f32();
-            pos += 2u;
-            f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
+            f3 sp;
+            if constexpr (kLearned) {
+                const float us = rng.next_f32(), sx = rng.next_f32(), sy = rng.next_f32();
+                pos += 3u;
+                sp = mlp::proposal_seed(sc, pr, sc.shapes[caster], pr.gmm + qi, n, us, sx, sy);
+            } else {
+                const float sx = rng.next_f32(), sy = rng.next_f32();
+                pos += 2u;
+                sp = sample_position(sc, sc.shapes[caster], sx, sy);
+            }
             Vtx v;
             int it;
             bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
@@ -286,7 +342,7 @@ __global__ void __launch_bounds__(128) ss_first_kernel(DevScene sc, SolverCfg cf
     // warp-aggregated append to the trial queue
     unsigned want = __ballot_sync(0xffffffffu, enqueue);
     if (want) {
-        unsigned lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+        unsigned leader = __ffs(want) - 1;
         unsigned base = 0;
         if (lane == leader) base = atomicAdd(&ctr->trial_count, (unsigned)__popc(want));
         base = __shfl_sync(0xffffffffu, base, leader);
@@ -296,84 +352,196 @@ __global__ void __launch_bounds__(128) ss_first_kernel(DevScene sc, SolverCfg cf
 }
 
 // ------------------------------------------------ unbiased: Bernoulli trials
-// Persistent warps.  For query q with first-walk direction dir0 the trials are
-// t = 1, 2, ...; trial t draws stream positions pos + 2(t-1) and the next one.
-// The warp runs trials 32 at a time and keeps the first success
-// (manifold_ss.cpp:115-135).
-__global__ void __launch_bounds__(128) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+// Persistent warps split into groups of G lanes; each group takes queries
+// from the queue and runs their Bernoulli trials G at a time (lane = trial).
+// For query q with first-walk direction dir0 the trials are t = 1, 2, ...;
+// trial t draws stream positions pos + S(t-1) .. (S = 2 draws per walk, 3 with
+// a learned proposal), so the first success -- found by ballot -- is exactly
+// the reference's sequential trial count (manifold_ss.cpp:115-135) whatever
+// G is.  G = 32 suits uniform seeding (tens of trials per query); a learned
+// proposal succeeds within a few trials and runs G = 8 (four queries per warp)
+// to cut the speculative walks past the first success.  Every trial redraws
+// its seed from the same per-query proposal as the first walk, so the count
+// still estimates the inverse probability of reaching dir0.
+//
+// All lanes run one warp-uniform loop: groups whose query finished fetch the
+// next one at the top, so every ballot and shuffle has the whole warp.
+template <bool kLearned, int G>
+__global__ void __launch_bounds__(128, 4) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
-                                                        int *__restrict__ walks, SsScratch scr, DevCounters *ctr) {
+                                                        int *__restrict__ walks, SsScratch scr, DevCounters *ctr,
+                                                        mlp::SeedProposal pr) {
+    static_assert(G == 8 || G == 16 || G == 32, "group size");
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31;
+    const unsigned gbase = lane & ~(unsigned)(G - 1), gl = lane - gbase;
+    const unsigned gmask = (G == 32) ? full : (((1u << G) - 1u) << gbase);
+    constexpr uint32_t kStride = kLearned ? 3u : 2u;
     LaneStats st;
     uint32_t err = 0;
     const int cap = cfg.max_trials > 0 ? cfg.max_trials : kTrialHardLimit;
     const int caster = sc.casters_ss[c];
     const unsigned n_list = *(volatile unsigned *)&ctr->trial_count;
+    // per-group state (replicated on the group's lanes)
+    bool have = false, drained = false;
+    uint32_t qi = 0, pos = 0;
+    int t0 = 1;
+    Query Q;
+    Light L;
+    Pcg32 base;
+    f3 dir0 = splat(0.f);
     while (true) {
+        // groups without a query take the next one
+        const bool need = !have && !drained;
         unsigned idx = 0;
-        if (lane == 0) idx = atomicAdd(&ctr->trial_head, 1u);
-        idx = __shfl_sync(full, idx, 0);
-        if (idx >= n_list) break;
-        uint32_t qi = scr.list[idx];
-        Query Q = load_query(qs, n, qi);
-        Pcg32 base = query_rng(seed, stream_off + qi, 0);
-        Light L;
-        sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, base, Q.x, L);   // base now sits at position 3
-        uint32_t pos = scr.pos[qi];
-        f3 dir0 = mk(scr.dir0[qi], scr.dir0[(size_t)n + qi], scr.dir0[2 * (size_t)n + qi]);
-        int first = 0;   // 1-based index of the first successful trial
-        for (int t0 = 1; t0 <= cap; t0 += 32) {
-            int t = t0 + (int)lane;
-            bool succ = false;
-            int it = 0;
-            if (t <= cap) {
-                Pcg32 rng = base;
-                rng.advance((uint64_t)(pos - 3u) + 2u * (uint64_t)(t - 1));
-                float sx = rng.next_f32(), sy = rng.next_f32();
-                f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
-                Vtx v;
-                succ = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st) &&
-                       fabsf(dot(dir0, normalize(v.p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
+        if (need && gl == 0) idx = atomicAdd(&ctr->trial_head, 1u);
+        idx = __shfl_sync(full, idx, gbase);
+        if (need) {
+            if (idx < n_list) {
+                have = true;
+                qi = scr.list[idx];
+                Q = load_query(qs, n, qi);
+                base = query_rng(seed, stream_off + qi, 0);
+                sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, base, Q.x, L);   // base sits at position 3
+                pos = scr.pos[qi];
+                dir0 = mk(scr.dir0[qi], scr.dir0[(size_t)n + qi], scr.dir0[2 * (size_t)n + qi]);
+                t0 = 1;
+            } else {
+                drained = true;
             }
-            unsigned b = __ballot_sync(full, succ);
-            int f = b ? t0 + __ffs(b) - 1 : 0x7fffffff;
+        }
+        if (__ballot_sync(full, have) == 0u) break;
+        const int t = t0 + (int)gl;
+        bool succ = false;
+        int it = 0;
+        if (have && t <= cap) {
+            Pcg32 rng = base;
+            rng.advance((uint64_t)(pos - 3u) + kStride * (uint64_t)(t - 1));
+            f3 sp;
+            if constexpr (kLearned) {
+                const float us = rng.next_f32(), sx = rng.next_f32(), sy = rng.next_f32();
+                sp = mlp::proposal_seed(sc, pr, sc.shapes[caster], pr.gmm + qi, n, us, sx, sy);
+            } else {
+                const float sx = rng.next_f32(), sy = rng.next_f32();
+                sp = sample_position(sc, sc.shapes[caster], sx, sy);
+            }
+            Vtx v;
+            succ = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st) &&
+                   fabsf(dot(dir0, normalize(v.p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
+        }
+        const unsigned b = (__ballot_sync(full, succ) & gmask) >> gbase;
+        const int f = b ? t0 + __ffs(b) - 1 : 0x7fffffff;
+        if (have && t <= cap) {
             // trials up to the first success are the reference's walks; the
             // rest of the chunk is speculative work
-            if (t <= cap) {
-                if (t <= f) { st.walks++; st.newton += (unsigned)it; }
-                else st.spec++;
-            }
-            if (b) { first = f; break; }
+            if (t <= f) { st.walks++; st.newton += (unsigned)it; }
+            else st.spec++;
         }
-        if (lane == 0) {
-            float inv_prob;
-            int iterations, trial_walks;
-            if (first) {
-                iterations = first;
-                inv_prob = (float)first;
-                trial_walks = first;
-            } else {
-                iterations = cap + 1;
-                inv_prob = 0.f;
-                trial_walks = cap;
-                if (cfg.max_trials <= 0) err |= kErrTrialLimit;
+        if (have && (b || t0 + G > cap)) {
+            if (gl == 0) {
+                float inv_prob;
+                int iterations, trial_walks;
+                if (b) {
+                    iterations = f;
+                    inv_prob = (float)f;
+                    trial_walks = f;
+                } else {
+                    iterations = cap + 1;
+                    inv_prob = 0.f;
+                    trial_walks = cap;
+                    if (cfg.max_trials <= 0) err |= kErrTrialLimit;
+                }
+                f3 val = mk(scr.val[qi], scr.val[(size_t)n + qi], scr.val[2 * (size_t)n + qi]);
+                f3 cur = val * inv_prob;
+                value[qi] += cur.x;
+                value[(size_t)n + qi] += cur.y;
+                value[2 * (size_t)n + qi] += cur.z;
+                count[qi] = b ? iterations : -1;
+                walks[qi] += trial_walks;
+                scr.pos[qi] = pos + kStride * (uint32_t)trial_walks;
+                st.calls++;
+                st.iters += (unsigned long long)iterations;
+                st.imax = max(st.imax, (unsigned long long)iterations);
             }
-            f3 val = mk(scr.val[qi], scr.val[(size_t)n + qi], scr.val[2 * (size_t)n + qi]);
-            f3 cur = val * inv_prob;
-            value[qi] += cur.x;
-            value[(size_t)n + qi] += cur.y;
-            value[2 * (size_t)n + qi] += cur.z;
-            count[qi] = first ? iterations : -1;
-            walks[qi] += trial_walks;
-            scr.pos[qi] = pos + 2u * (uint32_t)trial_walks;
-            st.calls++;
-            st.iters += (unsigned long long)iterations;
-            st.imax = max(st.imax, (unsigned long long)iterations);
+            have = false;
+        } else if (have) {
+            t0 += G;
         }
     }
     flush_stats(st, ctr, err, kPhaseSsTrials);
+}
+
+// ------------------------------------------------- learned proposal: data
+// Training pairs for the proposal from the uniform-seed solver: per query the
+// emitter sample (3 draws) and `per_query` uniform-seeded walks (2 draws each,
+// the biased estimator's layout).  Every distinct solution a query's walks
+// converge to (directions compared with the uniqueness threshold, as the
+// biased estimator does, manifold_ss.cpp:170-178) that the light sees appends
+// one pair: features (shading point, light sample, shading normal) and the
+// solution's uv in the proposal frame.  Keeping each solution once, however
+// often the uniform seeds found it, spreads the learned mixture over all of a
+// query's solutions instead of over the large basins only.  data: (kIn + 2) rows with row stride cap; *fill counts
+// the pairs found (it may exceed cap; rows past cap are dropped).
+constexpr int kCollectUnique = 16;
+
+__global__ void __launch_bounds__(128) ss_collect_kernel(DevScene sc, SolverCfg cfg, int caster,
+                                                         const float *__restrict__ qs, uint32_t n, uint64_t seed,
+                                                         uint64_t stream_off, int per_query, mlp::SeedFrame fr,
+                                                         float *__restrict__ data, uint32_t cap, unsigned *fill,
+                                                         DevCounters *ctr) {
+    const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned lane = threadIdx.x & 31;
+    LaneStats st;
+    uint32_t err = 0;
+    Query Q;
+    Pcg32 rng;
+    Light L;
+    bool have_light = false;
+    if (qi < n) {
+        Q = load_query(qs, n, qi);
+        rng = query_rng(seed, stream_off + qi, 0);
+        have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
+    }
+    f3 seen[kCollectUnique];   // directions of the solutions kept so far
+    int n_seen = 0;
+    for (int m = 0; m < per_query; ++m) {
+        bool ok = false;
+        Vtx v;
+        if (have_light) {
+            const float sx = rng.next_f32(), sy = rng.next_f32();
+            f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
+            int it;
+            ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
+            st.walks++;
+            st.newton += (unsigned)it;
+            if (ok) st.succ++; else st.fail++;
+            if (ok) {
+                // keep each contributing solution of the query once
+                const f3 dir = normalize(v.p - Q.x);
+                for (int j = 0; j < n_seen && ok; ++j)
+                    if (fabsf(dot(dir, seen[j]) - 1.f) < cfg.uniqueness_threshold) ok = false;
+                if (ok) ok = visible(sc, L.p, v.p, err, st);
+                if (ok && n_seen < kCollectUnique) seen[n_seen++] = dir;
+            }
+        }
+        const unsigned want = __ballot_sync(0xffffffffu, ok);
+        if (want) {
+            const unsigned leader = __ffs(want) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(fill, (unsigned)__popc(want));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            const unsigned idx = base + __popc(want & ((1u << lane) - 1u));
+            if (ok && idx < cap) {
+                float u, w;
+                mlp::frame_uv(fr, v.p, u, w);
+                const float rec[mlp::kIn + 2] = {Q.x.x, Q.x.y, Q.x.z, L.p.x, L.p.y, L.p.z, Q.n.x, Q.n.y, Q.n.z, u, w};
+                #pragma unroll
+                for (int k = 0; k < mlp::kIn + 2; ++k) data[(size_t)k * cap + idx] = rec[k];
+            }
+        }
+    }
+    flush_stats(st, ctr, err, kPhaseSsWalk);
 }
 
 // ---------------------------------------------------------------- launchers
@@ -389,7 +557,7 @@ cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster,
 cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                               uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                               const SsScratch &scr, int num_sms, int blocks_per_sm, PhaseTimer *tm,
-                              cudaStream_t s) {
+                              cudaStream_t s, const mlp::SeedProposal *prop, int trial_group) {
     if (n == 0) return cudaSuccess;
     const int bps = blocks_per_sm > 0 ? blocks_per_sm : 8;
     if (cfg.biased) {
@@ -413,20 +581,46 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
     for (int c = 0; c < sc.n_casters_ss; ++c) {
         cudaError_t e = cudaMemsetAsync(&ctr->trial_count, 0, 2 * sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
+        const bool learned = prop && prop->shape == sc.casters_ss[c];
+        const mlp::SeedProposal pr = learned ? *prop : mlp::SeedProposal{};
         phase_begin(tm, kPhaseSsFirst, s);
-        ss_first_kernel<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks,
-                                                        scr, ctr);
+        if (learned) {
+            const size_t smem = mlp::smem_seed_fused();
+            e = cudaFuncSetAttribute(ss_first_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            ss_first_kernel<true><<<(n + 127) / 128, 128, smem, s>>>(sc, cfg, c, q, n, seed, stream_off, value,
+                                                                     count, walks, scr, ctr, pr);
+        } else {
+            ss_first_kernel<false><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count,
+                                                                   walks, scr, ctr, pr);
+        }
         phase_end(tm, s);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         phase_begin(tm, kPhaseSsTrials, s);
-        ss_trials_kernel<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks,
-                                                       scr, ctr);
+        const int group = trial_group > 0 ? trial_group : (learned ? 8 : 32);
+        auto trials = learned ? (group == 8 ? ss_trials_kernel<true, 8>
+                                            : group == 16 ? ss_trials_kernel<true, 16> : ss_trials_kernel<true, 32>)
+                              : (group == 8 ? ss_trials_kernel<false, 8>
+                                            : group == 16 ? ss_trials_kernel<false, 16> : ss_trials_kernel<false, 32>);
+        trials<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr, pr);
         phase_end(tm, s);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t launch_ss_collect(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q, uint32_t n,
+                              uint64_t seed, uint64_t stream_off, int per_query, const mlp::SeedFrame &fr,
+                              float *data, uint32_t cap, unsigned *fill, DevCounters *ctr, PhaseTimer *tm,
+                              cudaStream_t s) {
+    if (n == 0 || per_query <= 0) return cudaSuccess;
+    phase_begin(tm, kPhaseSsWalk, s);
+    ss_collect_kernel<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, caster, q, n, seed, stream_off, per_query, fr, data,
+                                                      cap, fill, ctr);
+    phase_end(tm, s);
+    return cudaGetLastError();
 }
 
 }  // namespace sms

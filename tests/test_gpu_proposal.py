@@ -1,0 +1,294 @@
+"""GPU tests of the learned seed proposal, through the C ABI.
+
+Kernels under test (specular-manifold-sampling_gb300/csrc/sms_mlp.cu and the
+fused seeding in sms_ss.cu) against the NumPy oracle (oracle/mlp_oracle.py)
+and the C oracle's learned-seeding estimator (oracle/sms_oracle.cpp):
+
+  * forward:  raw outputs within FWD_ATOL + FWD_RTOL |o| of the oracle's
+              bf16-emulating forward (differences: FP32 vs FP64 accumulation
+              and the rare bf16 rounding flip that causes);
+  * mixture:  processed mixture of the GPU outputs within MIX_RTOL;
+  * gradient: per layer, relative L2 error below GRAD_REL and cosine above
+              GRAD_COS against the oracle's bf16-emulating backward pass;
+  * Adam:     one update equal to the closed form within ADAM_ATOL;
+  * estimator: count mismatches against the oracle within the chaos floor
+              (as the uniform-seed parity tests), unbiasedness within 4
+              standard errors of uniform seeding, and lower variance.
+"""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+FWD_ATOL, FWD_RTOL = 1e-2, 1e-2
+MIX_RTOL = 2e-5
+GRAD_REL, GRAD_COS = 3e-2, 0.999
+ADAM_ATOL = 1e-6
+FLOOR_FACTOR, FLOOR_SLACK = 1.5, 0.005
+
+
+def _ctx(sms, W, res=64, max_trials=256):
+    desc = W.water_scene(res=res)
+    cfg = sms.SMSConfig(biased=False, max_trials=max_trials)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    return desc, cfg, ctx
+
+
+def _random_state(seed, scale=0.3):
+    rng = np.random.default_rng(seed)
+    p = rng.uniform(-scale, scale, M.N_PARAMS).astype(np.float32)
+    M.unpack(p)[0][0][:, M.N_ENC:] = 0.0
+    norm = np.concatenate([rng.normal(size=9), rng.uniform(0.5, 2.0, 9)]).astype(np.float32)
+    return {"params": p, "norm": norm, "step": 0}
+
+
+def _device(q):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(q, np.float32)).cuda()
+    torch.cuda.synchronize()
+    return t
+
+
+def test_forward_matches_oracle(sms, workloads, gpu_lib):
+    _, _, ctx = _ctx(sms, workloads)
+    prop = sms.SeedProposal(ctx, 0, seed=1, capacity=1024)
+    st = _random_state(3)
+    prop.load_state(st)
+    feat = np.random.default_rng(4).normal(size=(9, 1000)).astype(np.float32)
+    g = prop.eval(feat)
+    o, _ = M.forward(st["params"], st["norm"][:9], st["norm"][9:], feat, bf=True)
+    o = o[:, :40].T
+    err = np.abs(g - o)
+    print(f"forward: max |err| {err.max():.2e} median {np.median(err):.2e} max |o| {np.abs(o).max():.2f}")
+    assert np.all(err <= FWD_ATOL + FWD_RTOL * np.abs(o))
+    assert np.median(err) < 1e-4
+
+
+def test_mixture_matches_oracle(sms, workloads, gpu_lib):
+    _, _, ctx = _ctx(sms, workloads)
+    prop = sms.SeedProposal(ctx, 0, seed=2, capacity=1024)
+    prop.load_state(_random_state(5))
+    feat = np.random.default_rng(6).normal(size=(9, 777)).astype(np.float32)
+    raw = prop.eval(feat)
+    mix = prop.eval(feat, mixture=True)
+    anc = M.anchor(prop.frame(), feat)
+    want = M.mixture(np.concatenate([raw.T, np.zeros((raw.shape[1], 8))], axis=1), anc).T
+    np.testing.assert_allclose(mix, want, rtol=MIX_RTOL, atol=1e-5)
+
+
+def _layer_blocks():
+    off = 0
+    for i, o in M.LAYERS:
+        yield off, off + o * i, off + o * i + o
+        off += o * i + o
+
+
+def test_loss_and_gradient_match_oracle(sms, workloads, gpu_lib):
+    _, _, ctx = _ctx(sms, workloads)
+    rng = np.random.default_rng(8)
+    n = 512
+    feat = rng.normal(size=(9, n)).astype(np.float32)
+    uv = rng.uniform(0.2, 0.8, size=(2, n)).astype(np.float32)
+    prop = sms.SeedProposal(ctx, 0, seed=3, capacity=n)
+    prop.set_data(feat, uv)
+    st = _random_state(9, scale=0.2)
+    prop.load_state(st)
+    fr = prop.frame()
+    for batch in (16, 256, 512):
+        loss, grad = prop.loss_grad(batch)
+        args = (st["params"], st["norm"][:9], st["norm"][9:], feat[:, :batch], uv[:, :batch])
+        lo, go = M.loss_grad(*args, bf=True, frame=fr)
+        _, gx = M.loss_grad(*args, bf=False, frame=fr)
+        print(f"batch {batch}: loss gpu {loss:.6f} oracle {lo:.6f}")
+        assert abs(loss - lo) < 1e-3 * max(1.0, abs(lo))
+        for a, b, e in _layer_blocks():
+            for sl in (slice(a, b), slice(b, e)):
+                g1, g2 = grad[sl].astype(np.float64), go[sl]
+                rel = np.linalg.norm(g1 - g2) / max(np.linalg.norm(g2), 1e-12)
+                cos = g1 @ g2 / max(np.linalg.norm(g1) * np.linalg.norm(g2), 1e-30)
+                assert rel < GRAD_REL and cos > GRAD_COS, (batch, sl, rel, cos)
+        assert (grad @ gx) / np.linalg.norm(grad) / np.linalg.norm(gx) > 0.99
+        # padded input columns carry no gradient
+        assert np.all(M.unpack(grad)[0][0][:, M.N_ENC:] == 0)
+
+
+def test_adam_update_matches_closed_form(sms, workloads, gpu_lib):
+    _, _, ctx = _ctx(sms, workloads)
+    rng = np.random.default_rng(10)
+    n = 2048
+    # one pair repeated: every batch the training step draws is the same batch
+    feat = np.repeat(rng.normal(size=(9, 1)), n, axis=1).astype(np.float32)
+    uv = np.repeat(rng.uniform(0.3, 0.7, size=(2, 1)), n, axis=1).astype(np.float32)
+    prop = sms.SeedProposal(ctx, 0, seed=4, capacity=n)
+    prop.set_data(feat, uv)
+    st = _random_state(11, scale=0.2)
+    st["adam_m"] = rng.normal(scale=1e-3, size=M.N_PARAMS).astype(np.float32)
+    st["adam_v"] = rng.uniform(1e-7, 1e-5, size=M.N_PARAMS).astype(np.float32)
+    st["step"] = 5
+    M.unpack(st["adam_m"])[0][0][:, M.N_ENC:] = 0.0
+    prop.load_state(st)
+    _, grad = prop.loss_grad(1024)
+    prop.train(steps=1, batch=1024, lr=1e-3)
+    after = prop.state()
+    p1, m1, v1 = M.adam_step(st["params"].astype(np.float64), grad.astype(np.float64),
+                             st["adam_m"].astype(np.float64), st["adam_v"].astype(np.float64), 5, 1e-3)
+    assert after["step"] == 6
+    np.testing.assert_allclose(after["adam_m"], m1, rtol=1e-4, atol=1e-9)
+    np.testing.assert_allclose(after["adam_v"], v1, rtol=1e-4, atol=1e-12)
+    assert np.abs(after["params"] - p1).max() < ADAM_ATOL
+
+
+def test_checkpoint_roundtrip(sms, workloads, gpu_lib, tmp_path):
+    _, _, ctx = _ctx(sms, workloads)
+    rng = np.random.default_rng(12)
+    feat = rng.normal(size=(9, 256)).astype(np.float32)
+    uv = rng.uniform(0.2, 0.8, size=(2, 256)).astype(np.float32)
+    a = sms.SeedProposal(ctx, 0, seed=5, capacity=256)
+    a.set_data(feat, uv)
+    a.normalize()
+    a.train(steps=60, batch=256, lr=1e-3)
+    a.save(tmp_path / "prop.npz")
+    b = sms.SeedProposal(ctx, 0, seed=99, capacity=256)
+    b.load(tmp_path / "prop.npz")
+    assert b.state()["step"] == 60
+    np.testing.assert_array_equal(a.eval(feat), b.eval(feat))
+    # resumed training continues identically
+    b.set_data(feat, uv)
+    la = a.train(steps=10, batch=256, lr=1e-3)
+    lb = b.train(steps=10, batch=256, lr=1e-3)
+    assert abs(la - lb) < 1e-3 * max(1.0, abs(la))
+
+
+def _collect(sms, W, ctx, n=32768, walks=4, capacity=1 << 22, seed=21):
+    q = W.water_queries(n, seed=seed)
+    prop = sms.SeedProposal(ctx, 0, seed=7, capacity=capacity)
+    ctx.reset_stats()
+    total = prop.collect(_device(q).data_ptr(), n, seed=seed, walks_per_query=walks)
+    return prop, total
+
+
+def test_collected_pairs_are_solver_solutions(sms, workloads, oracle, gpu_lib):
+    W = workloads
+    desc, cfg, ctx = _ctx(sms, W)
+    prop, total = _collect(sms, W, ctx, n=4096, walks=2)
+    st = ctx.stats()
+    assert 100 < total <= st["solver_succeeded"]
+    feat, uv = prop.get_data()
+    assert feat.shape == (9, total)
+    # features: shading point on the receiver, light sample on the light, normal
+    assert np.all(np.abs(feat[2]) < 1e-6) and np.all(np.abs(feat[8] - 1) < 1e-6)
+    assert np.all(np.abs(np.linalg.norm(feat[3:6] - np.array([[0], [0], [10]]), axis=0) - 0.1) < 1e-4)
+    assert np.all((uv > -0.01) & (uv < 1.01))
+    # each pair is a solution: a walk started at its uv point converges there
+    fr = prop.frame()
+    seed_pts = fr[1:4, None] + fr[4:7, None] * uv[0] + fr[7:10, None] * uv[1]
+    q = workloads.plane_queries(feat[0:2].T.copy())
+    w = np.zeros((8, total), np.float32)
+    w[0:3] = feat[3:6]
+    w[3:6] = seed_pts
+    out = oracle.OracleScene(desc).walk_batch(cfg, 0, q, w)
+    conv = out[0] > 0.5
+    back = np.abs(out[2:4] - seed_pts[0:2]).max(axis=0)
+    print(f"pairs {total}: oracle re-walk converged {conv.mean():.3f}, same point {np.mean(back[conv] < 1e-3):.3f}")
+    assert conv.mean() > 0.9
+    assert np.mean(back[conv] < 1e-3) > 0.9
+
+
+def _trained(sms, W, ctx, steps=1500, batch=4096, n=32768, walks=4):
+    prop, total = _collect(sms, W, ctx, n=n, walks=walks)
+    prop.normalize()
+    loss0, _ = prop.loss_grad(1024)
+    loss = prop.train(steps=steps, batch=batch, lr=1e-3)
+    return prop, total, loss0, loss
+
+
+def test_training_reduces_loss(sms, workloads, gpu_lib):
+    _, _, ctx = _ctx(sms, workloads)
+    prop, total, loss0, loss = _trained(sms, workloads, ctx, steps=600)
+    print(f"pairs {total}: loss {loss0:.3f} -> {loss:.3f}")
+    assert total > 2000
+    assert loss < loss0 - 1.0
+
+
+def test_learned_connect_matches_oracle(sms, workloads, oracle, gpu_lib):
+    W = workloads
+    desc, cfg, ctx = _ctx(sms, W, max_trials=64)
+    prop, _, _, _ = _trained(sms, W, ctx, steps=300)
+    ctx.set_proposal(prop, 0.1)
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    n = 4096
+    q = W.water_queries(n, seed=31)
+    vg, cg, wg = ss.specular_manifold_sampling(q, seed=5)
+    ei = oracle.OracleScene(desc).emitter_batch(q, seed=5)
+    feat = np.concatenate([q[0:3], ei[0:3], q[3:6]]).astype(np.float32)
+    mix = prop.eval(feat, mixture=True)
+    args = (cfg, q, 0, 0.1, prop.frame(), mix)
+    vo, co, wo, _ = oracle.OracleScene(desc).connect_learned_batch(*args, seed=5)
+    vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_learned_batch(*args, seed=5)
+    g_cm, f_cm = float(np.mean(cg != co)), float(np.mean(cf != co))
+    print(f"learned connect: count mismatch {g_cm:.4f} (floor {f_cm:.4f}); walks gpu {wg.sum()} oracle {wo.sum()}")
+    assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+    same = (cg == co) & (wg == wo)
+    scale = np.maximum(np.abs(vo).max(axis=0), 1e-6)
+    rel = np.abs(vg - vo).max(axis=0) / scale
+    assert np.mean(rel[same] < 1e-3) > 0.99
+
+
+def test_learned_estimator_unbiased_and_lower_variance(sms, workloads, gpu_lib):
+    """Same shading points, many independent samples: the learned-seed mean
+    matches the uniform-seed mean within 4 standard errors, and the per-point
+    variance drops."""
+    W = workloads
+    _, _, ctx = _ctx(sms, W, max_trials=4096)
+    prop, _, _, loss = _trained(sms, W, ctx, steps=4000, batch=8192, n=1 << 20, walks=8)
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    P, S = 4096, 32
+    q1 = W.water_queries(P, seed=41)
+    q = np.tile(q1, (1, S))
+    res = {}
+    ctx.set_profiling(True)
+    for mode in ("uniform", "learned"):
+        ctx.set_proposal(prop if mode == "learned" else None, 0.1)
+        ctx.reset_stats()
+        v, c, w = ss.specular_manifold_sampling(q, seed=9, stream_offset=1 << 20)
+        est = v[0].reshape(S, P).astype(np.float64)
+        pr = ctx.profile()
+        res[mode] = (est, ctx.stats(), pr["ss_first"]["ms"] + pr["ss_trials"]["ms"])
+    eu, su, tmu = res["uniform"]
+    el, sl, tml = res["learned"]
+    mu, ml = eu.mean(), el.mean()
+    se = np.sqrt(eu.mean(axis=1).var(ddof=1) / S + el.mean(axis=1).var(ddof=1) / S)
+    var_u, var_l = eu.var(axis=0, ddof=1).sum(), el.var(axis=0, ddof=1).sum()
+    tu = su["bernoulli_trial_iterations"] / max(su["bernoulli_trial_calls"], 1)
+    tl = sl["bernoulli_trial_iterations"] / max(sl["bernoulli_trial_calls"], 1)
+    eff = (var_u * tmu) / max(var_l * tml, 1e-30)
+    print(f"loss {loss:.3f}; mean uniform {mu:.5g} learned {ml:.5g} (4 se {4 * se:.3g}); "
+          f"variance ratio {var_u / max(var_l, 1e-30):.2f}; mean trials {tu:.1f} -> {tl:.1f}; "
+          f"kernel ms {tmu:.2f} -> {tml:.2f}; efficiency x{eff:.2f}")
+    assert abs(mu - ml) < 4 * se
+    assert tl < tu
+    # variance x time: the learned seeds reach a given error in less time
+    assert eff > 1.5
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_trial_group_size_does_not_change_results(sms, workloads, gpu_lib, learned):
+    """The grouped Bernoulli-trial kernel finds the first success by ballot:
+    8, 16 and 32 lanes per query give bit-identical estimates."""
+    W = workloads
+    _, _, ctx = _ctx(sms, W, max_trials=256)
+    if learned:
+        prop, _, _, _ = _trained(sms, W, ctx, steps=200)
+        ctx.set_proposal(prop, 0.1)
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    q = W.water_queries(20000, seed=51)
+    outs = []
+    for g in (8, 16, 32):
+        ctx.set_trial_group(g)
+        outs.append(ss.specular_manifold_sampling(q, seed=3))
+    for v, c, w in outs[1:]:
+        np.testing.assert_array_equal(v, outs[0][0])
+        np.testing.assert_array_equal(c, outs[0][1])
+        np.testing.assert_array_equal(w, outs[0][2])

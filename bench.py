@@ -197,7 +197,7 @@ def secondary_configs(torch, sms, W, dev):
 
 
 def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=8192, lr=1e-3, res=128,
-                  ref_spp=4096):
+                  ref_spp=4096, sigma_scale=1.0, weighted=True):
     """Learned seed proposal on the water workload: training pairs from the
     uniform-seed solver, GPU training, then equal-time caustic RMSE of
     learned vs uniform seeding against a ref_spp uniform-seed image of
@@ -206,6 +206,7 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     cfg = W.water_config()
     ctx.set_config(cfg)
     prop = sms.SeedProposal(ctx, 0, seed=1, capacity=pairs)
+    prop.set_options(sigma_scale, weighted)
     chunk = 1 << 20
     total, calls = 0, 0
     with DeviceTimer(torch, stream) as t_collect:
@@ -216,12 +217,13 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
             calls += 1
     prop.normalize()
     loss0, _ = prop.loss_grad(batch)
-    prop.train(steps=100, batch=batch, lr=lr)   # graph capture + warm-up
+    warm = min(100, max(1, steps // 10))
+    prop.train(steps=warm, batch=batch, lr=lr)   # graph capture + warm-up
     t0 = time.perf_counter()
     with DeviceTimer(torch, stream) as t_train:
-        loss = prop.train(steps=steps - 100, batch=batch, lr=lr)
+        loss = prop.train(steps=steps - warm, batch=batch, lr=lr)
     train_wall = time.perf_counter() - t0
-    step_ms = t_train.ms / (steps - 100)
+    step_ms = t_train.ms / max(1, steps - warm)
     flop_step = 3 * 2 * batch * (96 * 64 + 3 * 64 * 64 + 64 * 48)   # forward + backward GEMMs
     # images: pixel centres of a res x res grid on the receiver, spp samples each
     c = (np.arange(res) + 0.5) / res * 2.0 - 1.0
@@ -229,8 +231,11 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     pix = W.plane_queries(np.stack([xx.ravel(), yy.ravel()], axis=1).astype(np.float32))
     npix = pix.shape[1]
 
-    def render(spp, seed, offset, learned):
+    def render(spp, seed, offset, learned, stats=None):
         ctx.set_proposal(prop if learned else None, 0.1)
+        if stats is not None:
+            ctx.reset_stats()
+            ctx.set_profiling(True)
         per_call = max(1, (1 << 21) // npix)
         acc = torch.zeros(npix, dtype=torch.float64, device=f"cuda:{dev}")
         ms = 0.0
@@ -243,15 +248,32 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
             ms += t
             done += k
         ctx.set_proposal(None)
+        if stats is not None:
+            st, pr = ctx.stats(), ctx.profile()
+            ctx.set_profiling(False)
+            conns = npix * spp
+            stats.update({
+                "first_ms": pr["ss_first"]["ms"], "trials_ms": pr["ss_trials"]["ms"],
+                "queued_fraction": st["bernoulli_trial_calls"] / conns,
+                "trials_per_queued": st["bernoulli_trial_iterations"] / max(1, st["bernoulli_trial_calls"]),
+                "walks_per_connection": st["walks"] / conns,
+                "speculative_walks_per_connection": st["speculative_walks"] / conns,
+                "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),
+                "first_walk_converged": st["solver_succeeded"] / max(1, st["solver_succeeded"] + st["solver_failed"]),
+            })
         return (acc / spp).cpu().numpy(), ms
 
     ref, ref_ms = render(ref_spp, 11, 1 << 30, False)
     rows = []
     for learned in (False, True):
         for spp in (4, 16, 64):
-            img, ms = render(spp, 12 + spp, 1 << 28, learned)
+            extra = {} if spp == 64 else None
+            img, ms = render(spp, 12 + spp, 1 << 28, learned, extra)
             rmse = float(np.sqrt(np.mean((img - ref) ** 2)))
-            rows.append({"seeding": "learned" if learned else "uniform", "spp": spp, "ms": ms, "rmse": rmse})
+            row = {"seeding": "learned" if learned else "uniform", "spp": spp, "ms": ms, "rmse": rmse}
+            if extra:
+                row["profile"] = extra
+            rows.append(row)
     uni64 = next(r for r in rows if r["seeding"] == "uniform" and r["spp"] == 64)
     reach = [r for r in rows if r["seeding"] == "learned" and r["rmse"] <= uni64["rmse"]]
     t_equal = min(r["ms"] for r in reach) if reach else None
@@ -316,7 +338,7 @@ def run_ours(args):
     sms = load_package()
     from sms_gb300 import workloads as W
 
-    n = N_QUERIES
+    n = args.queries
     desc = W.water_scene()
     cfg = W.water_config()
     ctx = sms.Context(sms.Scene(desc), cfg, device=dev)
@@ -435,7 +457,8 @@ def run_ours(args):
         pp = ROOT / "MEASURED_PEAKS.json"
         if pp.exists():
             bf16_peak = json.loads(pp.read_text()).get("bf16_tflops")
-        lt = learned_study(torch, sms, W, ctx, dev)
+        lt = learned_study(torch, sms, W, ctx, dev, pairs=args.learned_pairs, steps=args.learned_steps,
+                           ref_spp=args.ref_spp)
         rl = lt["train"]["roofline"]
         rl["peak"] = bf16_peak or 1900.0
         rl["frac"] = rl["achieved"] / rl["peak"]
@@ -464,6 +487,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal study")
+    ap.add_argument("--queries", type=int, default=N_QUERIES, help="queries per step (smaller cases for ncu)")
+    ap.add_argument("--learned-pairs", type=int, default=4 << 20)
+    ap.add_argument("--learned-steps", type=int, default=20000)
+    ap.add_argument("--ref-spp", type=int, default=4096)
     ap.add_argument("--no-configs", action="store_true", help="skip the sphere / slab / glint configurations")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -374,18 +374,26 @@ sms_status sms_proposal_destroy(sms_proposal *p);
  * sms_ss_connect_batch) the emitter sample and `walks_per_query` uniformly
  * seeded walks on the stream (seed, stream_offset + i); each distinct solution
  * they converge to (uniqueness threshold of the config) that the light sample
- * sees appends one pair (features, uv of the solution).  Pairs are appended
- * to those already held; *total = pairs held afterwards (at most capacity).
+ * sees appends one pair: features, uv of the solution, and a weight = the
+ * solution's share of the query's summed contribution.  Pairs are appended to
+ * those already held; *total = pairs held afterwards (at most capacity).
  * Synchronous. */
 sms_status sms_proposal_collect(sms_proposal *p, const float *queries_dev, uint32_t n,
                                 uint64_t seed, uint64_t stream_offset,
                                 int32_t walks_per_query, uint32_t *total);
-/* Replace the training set with host arrays (features SoA 9 x n, uv SoA 2 x n). */
+/* Replace the training set with host arrays (features SoA 9 x n, uv SoA 2 x n,
+ * weights n or NULL for all ones). */
 sms_status sms_proposal_set_data(sms_proposal *p, const float *features, const float *uv,
-                                 uint32_t n);
-/* Read the training set back (host arrays sized as above for *n = count). */
-sms_status sms_proposal_get_data(sms_proposal *p, float *features, float *uv, uint32_t cap,
-                                 uint32_t *n);
+                                 const float *weights, uint32_t n);
+/* Read the training set back (host arrays sized as above for the first
+ * min(cap, count) pairs; weights may be NULL); *n = pairs held. */
+sms_status sms_proposal_get_data(sms_proposal *p, float *features, float *uv, float *weights,
+                                 uint32_t cap, uint32_t *n);
+/* sigma_scale (> 0, default 1) multiplies every mixture sigma when seeds are
+ * drawn (any fixed proposal keeps the estimator unbiased; a sharper one puts
+ * more seeds inside the predicted basins).  weighted (default 1): the
+ * training loss weights each pair by its contribution share. */
+sms_status sms_proposal_set_options(sms_proposal *p, float sigma_scale, int32_t weighted);
 /* Set the input normalisation (x - shift) * scale from the training set's
  * mean and standard deviation (features with zero spread get scale 0). */
 sms_status sms_proposal_normalize(sms_proposal *p);

@@ -150,8 +150,9 @@ def mixture_nll(o: np.ndarray, uv: np.ndarray):
     return -logp[:, 0], g
 
 
-def loss_grad(params, shift, scale, feat, uv, bf: bool = True, frame=None):
-    """Mean NLL over the batch and its gradient (flat, parameter layout).
+def loss_grad(params, shift, scale, feat, uv, bf: bool = True, frame=None, weights=None):
+    """Mean (weighted) NLL over the batch and its gradient (flat, parameter
+    layout): loss = sum_b w_b NLL_b / B.
 
     With bf=True the backward pass rounds the pre-activation gradients and
     weights to bfloat16 where the GPU does (straight-through for the forward
@@ -160,7 +161,9 @@ def loss_grad(params, shift, scale, feat, uv, bf: bool = True, frame=None):
     rel = np.asarray(uv, np.float64) - (anchor(frame, feat) if frame is not None else 0.0)
     nll, g = mixture_nll(o, rel)
     B = o.shape[0]
-    dz = g / B
+    w = np.ones(B) if weights is None else np.asarray(weights, np.float64)
+    nll = nll * w
+    dz = g * (w / B)[:, None]
     grads = []
     for li in range(len(LAYERS) - 1, -1, -1):
         hin, Wq, z = cache[li]

@@ -141,8 +141,9 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_proposal_create": (i32, [vp, i32, u64, u32, C.POINTER(vp)]),
         "sms_proposal_destroy": (i32, [vp]),
         "sms_proposal_collect": (i32, [vp, vp, u32, u64, u64, i32, C.POINTER(u32)]),
-        "sms_proposal_set_data": (i32, [vp, vp, vp, u32]),
-        "sms_proposal_get_data": (i32, [vp, vp, vp, u32, C.POINTER(u32)]),
+        "sms_proposal_set_data": (i32, [vp, vp, vp, vp, u32]),
+        "sms_proposal_get_data": (i32, [vp, vp, vp, vp, u32, C.POINTER(u32)]),
+        "sms_proposal_set_options": (i32, [vp, f32, i32]),
         "sms_proposal_normalize": (i32, [vp]),
         "sms_proposal_train": (i32, [vp, i32, i32, f32, C.POINTER(f32)]),
         "sms_proposal_loss_grad": (i32, [vp, i32, C.POINTER(f32), vp]),
@@ -408,19 +409,26 @@ class SeedProposal:
                                          C.byref(total)))
         return total.value
 
-    def set_data(self, features: np.ndarray, uv: np.ndarray):
+    def set_data(self, features: np.ndarray, uv: np.ndarray, weights: np.ndarray | None = None):
         n = features.shape[1]
         f = _soa(features, PROPOSAL_FEATURES, n)
         u = _soa(uv, 2, n)
-        _check(_LIB.sms_proposal_set_data(self._h, _ptr(f), _ptr(u), n))
+        w = None if weights is None else np.ascontiguousarray(weights, np.float32).reshape(n)
+        _check(_LIB.sms_proposal_set_data(self._h, _ptr(f), _ptr(u), None if w is None else _ptr(w), n))
 
-    def get_data(self) -> tuple[np.ndarray, np.ndarray]:
+    def get_data(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Training set: features (9 x n), uv (2 x n), weights (n)."""
         n = C.c_uint32()
-        _check(_LIB.sms_proposal_get_data(self._h, None, None, 0, C.byref(n)))
+        _check(_LIB.sms_proposal_get_data(self._h, None, None, None, 0, C.byref(n)))
         f = np.zeros((PROPOSAL_FEATURES, n.value), np.float32)
         u = np.zeros((2, n.value), np.float32)
-        _check(_LIB.sms_proposal_get_data(self._h, _ptr(f), _ptr(u), n.value, C.byref(n)))
-        return f, u
+        w = np.zeros(n.value, np.float32)
+        _check(_LIB.sms_proposal_get_data(self._h, _ptr(f), _ptr(u), _ptr(w), n.value, C.byref(n)))
+        return f, u, w
+
+    def set_options(self, sigma_scale: float = 1.0, weighted: bool = True):
+        """Seeding sharpness (sigma multiplier) and contribution-weighted training."""
+        _check(_LIB.sms_proposal_set_options(self._h, sigma_scale, int(weighted)))
 
     def normalize(self):
         _check(_LIB.sms_proposal_normalize(self._h))

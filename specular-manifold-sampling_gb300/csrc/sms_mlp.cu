@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(MlpDev m, const float 
                 auto F = [&](int k) { return __ldg(feat + (size_t)k * n + r); };
                 float au, av;
                 anchor_uv(m.frame, mk(F(0), F(1), F(2)), mk(F(3), F(4), F(5)), au, av);
-                mixture_from_raw(row, out + r, n, au, av);
+                mixture_from_raw(row, out + r, n, au, av, m.sigma_scale);
             } else {
                 for (int c = 0; c < kGmmParams; ++c) out[(size_t)c * n + b0 + lane] = row[c];
             }
@@ -169,7 +169,8 @@ __global__ void __launch_bounds__(128) mlp_train_fb_kernel(MlpDev m, const float
         float au, av;
         anchor_uv(m.frame, mk(F(0), F(1), F(2)), mk(F(3), F(4), F(5)), au, av);
         loss = mixture_nll(oo, __ldg(uv + r) - au, __ldg(uv + ld + r) - av, go);
-        const float inv_b = 1.f / (float)batch;   // the loss is the batch mean
+        // the loss is the batch mean of (weighted) NLLs
+        const float inv_b = (m.weighted ? __ldg(uv + 2 * ld + r) : 1.f) / (float)batch;
         #pragma unroll
         for (int c = 0; c < kOutPad; ++c) stage[lane * kOutPad + c] = go[c] * inv_b;
         loss *= inv_b;

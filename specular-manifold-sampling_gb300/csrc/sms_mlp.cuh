@@ -184,8 +184,10 @@ __device__ __forceinline__ void stage_outputs(const float o[6][4], float *stage)
 __device__ __forceinline__ float log_sigma(float raw) { return kLsMin + (kLsMax - kLsMin) * sigmoid(raw); }
 
 // Raw outputs o[0..39] -> mixture (cdf[8], mean[16], sigma[16]) written with
-// stride `stride` (SoA of a query batch); means are anchor + offset.
-__device__ __forceinline__ void mixture_from_raw(const float *o, float *dst, size_t stride, float au, float av) {
+// stride `stride` (SoA of a query batch); means are anchor + offset, sigmas
+// are scaled by sigma_scale (seeding sharpness).
+__device__ __forceinline__ void mixture_from_raw(const float *o, float *dst, size_t stride, float au, float av,
+                                                 float sigma_scale) {
     float mx = o[0];
     #pragma unroll
     for (int k = 1; k < kComp; ++k) mx = fmaxf(mx, o[k]);
@@ -202,7 +204,7 @@ __device__ __forceinline__ void mixture_from_raw(const float *o, float *dst, siz
     #pragma unroll
     for (int k = 0; k < 2 * kComp; ++k) {
         dst[(size_t)(8 + k) * stride] = o[8 + k] + ((k & 1) ? av : au);
-        dst[(size_t)(24 + k) * stride] = __expf(log_sigma(o[24 + k]));
+        dst[(size_t)(24 + k) * stride] = sigma_scale * __expf(log_sigma(o[24 + k]));
     }
 }
 

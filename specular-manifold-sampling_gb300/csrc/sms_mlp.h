@@ -27,6 +27,7 @@ constexpr int kOutPad = 48;     // output layer width (multiple of 16)
 // Log-sigma of a component is kLsMin + (kLsMax - kLsMin) * sigmoid(raw).
 constexpr float kLsMin = -7.f;
 constexpr float kLsMax = 0.f;
+constexpr int kDataRows = kIn + 3;   // training pair: features, uv, weight
 constexpr int kLossHist = 256;  // per-step loss ring
 constexpr int kMaxBatch = 65536;
 
@@ -93,6 +94,8 @@ struct MlpDev {
     float shift[kIn];       // input normalisation: (f - shift) * scale
     float scale[kIn];
     SeedFrame frame;        // anchor of the mixture means
+    float sigma_scale;      // seeding sharpness: sigmas of the processed mixture x this
+    int weighted;           // training loss weighted by the pairs' contribution shares
 };
 
 // A learned proposal bound to a context for the unbiased single-scatter
@@ -115,8 +118,9 @@ cudaError_t launch_sync(const MlpDev &m, cudaStream_t s);
 cudaError_t launch_forward(const MlpDev &m, const float *feat, uint32_t n, float *out, bool mixture, int num_sms,
                            cudaStream_t s);
 // One optimizer step over a batch drawn (with replacement) from the data set
-// (feat: kIn rows, uv: 2 rows, row stride ld, n_data pairs); shuffle=false
-// takes rows 0..batch-1; update=false stops after the gradient.
+// (feat: kIn rows, then uv: 2 rows and weight: 1 row, row stride ld, n_data
+// pairs); shuffle=false takes rows 0..batch-1; update=false stops after the
+// gradient.
 cudaError_t launch_train_step(const MlpDev &m, const float *feat, const float *uv, size_t ld, uint32_t n_data,
                               int batch, float lr, bool shuffle, bool update, cudaStream_t s);
 // Per-feature sums and sums of squares (2 kIn doubles, accumulated).

@@ -26,7 +26,7 @@ struct sms_proposal {
     mlp::SeedFrame frame{};
     mlp::MlpDev net{};
     void *block = nullptr;       // parameters, moments, copies, counters
-    float *data = nullptr;       // (kIn + 2) x cap training pairs
+    float *data = nullptr;       // kDataRows x cap training pairs (features, uv, weight)
     uint32_t cap = 0;
     unsigned *fill = nullptr;    // device: pairs appended (may exceed cap)
     uint32_t n_data = 0;
@@ -163,7 +163,7 @@ extern "C" sms_status sms_proposal_create(sms_ctx *ctx, int32_t caster, uint64_t
     do {
         cudaError_t e = cudaMalloc(&p->block, total);
         if (e != cudaSuccess) { st = cuda_fail(e, "cudaMalloc(proposal)"); break; }
-        e = cudaMalloc(&p->data, (size_t)(mlp::kIn + 2) * capacity * sizeof(float));
+        e = cudaMalloc(&p->data, (size_t)mlp::kDataRows * capacity * sizeof(float));
         if (e != cudaSuccess) { st = cuda_fail(e, "cudaMalloc(proposal training set)"); break; }
         char *b = reinterpret_cast<char *>(p->block);
         p->net.params = reinterpret_cast<float *>(b);
@@ -177,6 +177,8 @@ extern "C" sms_status sms_proposal_create(sms_ctx *ctx, int32_t caster, uint64_t
         p->net.wbf = reinterpret_cast<__nv_bfloat16 *>(b + off_wbf);
         p->moments = reinterpret_cast<double *>(b + off_mom);
         for (int k = 0; k < mlp::kIn; ++k) { p->net.shift[k] = 0.f; p->net.scale[k] = 1.f; }
+        p->net.sigma_scale = 1.f;
+        p->net.weighted = 1;
         e = cudaMemsetAsync(p->block, 0, total, v.stream);
         if (e != cudaSuccess) { st = cuda_fail(e, "cudaMemset(proposal)"); break; }
         std::vector<float> P;
@@ -232,14 +234,21 @@ extern "C" sms_status sms_proposal_collect(sms_proposal *p, const float *q, uint
     return SMS_OK;
 }
 
-extern "C" sms_status sms_proposal_set_data(sms_proposal *p, const float *feat, const float *uv, uint32_t n) {
+extern "C" sms_status sms_proposal_set_data(sms_proposal *p, const float *feat, const float *uv, const float *weight,
+                                            uint32_t n) {
     CtxView v;
     if (!live(p, v)) return fail(SMS_ERR_INVALID_ARG, "sms_proposal_set_data: proposal without context");
     if (n && (!feat || !uv)) return fail(SMS_ERR_INVALID_ARG, "sms_proposal_set_data: null array");
     if (n > p->cap) return fail(SMS_ERR_INVALID_ARG, "sms_proposal_set_data: more pairs than the capacity");
     PTRY(cudaSetDevice(v.device));
-    for (int k = 0; k < mlp::kIn + 2 && n; ++k) {
-        const float *src = k < mlp::kIn ? feat + (size_t)k * n : uv + (size_t)(k - mlp::kIn) * n;
+    std::vector<float> ones;
+    if (!weight) {
+        ones.assign(n, 1.f);
+        weight = ones.data();
+    }
+    for (int k = 0; k < mlp::kDataRows && n; ++k) {
+        const float *src = k < mlp::kIn ? feat + (size_t)k * n
+                         : k < mlp::kIn + 2 ? uv + (size_t)(k - mlp::kIn) * n : weight;
         PTRY(cudaMemcpyAsync(p->data + (size_t)k * p->cap, src, (size_t)n * 4, cudaMemcpyHostToDevice, v.stream));
     }
     unsigned f = n;
@@ -250,7 +259,8 @@ extern "C" sms_status sms_proposal_set_data(sms_proposal *p, const float *feat, 
     return SMS_OK;
 }
 
-extern "C" sms_status sms_proposal_get_data(sms_proposal *p, float *feat, float *uv, uint32_t cap, uint32_t *n) {
+extern "C" sms_status sms_proposal_get_data(sms_proposal *p, float *feat, float *uv, float *weight, uint32_t cap,
+                                            uint32_t *n) {
     CtxView v;
     if (!live(p, v)) return fail(SMS_ERR_INVALID_ARG, "sms_proposal_get_data: proposal without context");
     if (!n) return fail(SMS_ERR_INVALID_ARG, "sms_proposal_get_data: null count");
@@ -258,8 +268,10 @@ extern "C" sms_status sms_proposal_get_data(sms_proposal *p, float *feat, float 
     const uint32_t m = std::min(cap, p->n_data);
     if (m && (!feat || !uv)) return fail(SMS_ERR_INVALID_ARG, "sms_proposal_get_data: null array");
     PTRY(cudaSetDevice(v.device));
-    for (int k = 0; k < mlp::kIn + 2 && m; ++k) {
-        float *dst = k < mlp::kIn ? feat + (size_t)k * m : uv + (size_t)(k - mlp::kIn) * m;
+    for (int k = 0; k < mlp::kDataRows && m; ++k) {
+        float *dst = k < mlp::kIn ? feat + (size_t)k * m
+                   : k < mlp::kIn + 2 ? uv + (size_t)(k - mlp::kIn) * m : weight;
+        if (!dst) continue;
         PTRY(cudaMemcpyAsync(dst, p->data + (size_t)k * p->cap, (size_t)m * 4, cudaMemcpyDeviceToHost, v.stream));
     }
     PTRY(cudaStreamSynchronize(v.stream));
@@ -402,6 +414,16 @@ extern "C" sms_status sms_proposal_set_state(sms_proposal *p, const float *param
     PTRY(cudaStreamSynchronize(v.stream));
     if (norm)
         for (int k = 0; k < mlp::kIn; ++k) { p->net.shift[k] = norm[k]; p->net.scale[k] = norm[mlp::kIn + k]; }
+    p->version++;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_proposal_set_options(sms_proposal *p, float sigma_scale, int32_t weighted) {
+    if (!p) return fail(SMS_ERR_INVALID_ARG, "sms_proposal_set_options: null proposal");
+    if (!(sigma_scale > 0.f) || !std::isfinite(sigma_scale))
+        return fail(SMS_ERR_INVALID_ARG, "sms_proposal_set_options: sigma_scale must be positive");
+    p->net.sigma_scale = sigma_scale;
+    p->net.weighted = weighted != 0;
     p->version++;
     return SMS_OK;
 }

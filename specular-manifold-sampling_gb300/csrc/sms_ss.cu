@@ -283,7 +283,8 @@ __global__ void __launch_bounds__(128, kLearned ? 3 : 4) ss_first_kernel(DevScen
             if ((int)(lane >> 4) == h && active) {
                 float au, av;
                 mlp::anchor_uv(pr.net.frame, fx, fl, au, av);
-                mlp::mixture_from_raw(stage + (lane & 15) * mlp::kOutPad, pr.gmm + qi, n, au, av);
+                mlp::mixture_from_raw(stage + (lane & 15) * mlp::kOutPad, pr.gmm + qi, n, au, av,
+                                      pr.net.sigma_scale);
             }
             __syncwarp();
         }
@@ -477,12 +478,15 @@ __global__ void __launch_bounds__(128, 4) ss_trials_kernel(DevScene sc, SolverCf
 // emitter sample (3 draws) and `per_query` uniform-seeded walks (2 draws each,
 // the biased estimator's layout).  Every distinct solution a query's walks
 // converge to (directions compared with the uniqueness threshold, as the
-// biased estimator does, manifold_ss.cpp:170-178) that the light sees appends
-// one pair: features (shading point, light sample, shading normal) and the
-// solution's uv in the proposal frame.  Keeping each solution once, however
-// often the uniform seeds found it, spreads the learned mixture over all of a
-// query's solutions instead of over the large basins only.  data: (kIn + 2) rows with row stride cap; *fill counts
-// the pairs found (it may exceed cap; rows past cap are dropped).
+// biased estimator does, manifold_ss.cpp:170-178) that the light sees becomes
+// one pair: features (shading point, light sample, shading normal), the
+// solution's uv in the proposal frame, and a weight = its share of the
+// query's total contribution (diffuse BSDF x specular path contribution, mean
+// of RGB).  Keeping each solution once, however often the uniform seeds found
+// it, spreads the learned mixture over all of a query's solutions; the weight
+// (used by weighted training) moves the mixture mass towards p_k ~ f_k, which
+// minimises the Bernoulli estimator's variance sum_k f_k^2 (2 - p_k) / p_k for
+// a given total success probability.
 constexpr int kCollectUnique = 16;
 
 __global__ void __launch_bounds__(128) ss_collect_kernel(DevScene sc, SolverCfg cfg, int caster,
@@ -503,43 +507,50 @@ __global__ void __launch_bounds__(128) ss_collect_kernel(DevScene sc, SolverCfg 
         rng = query_rng(seed, stream_off + qi, 0);
         have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
     }
-    f3 seen[kCollectUnique];   // directions of the solutions kept so far
+    f3 seen[kCollectUnique];     // directions of the solutions kept so far
+    float kuv[kCollectUnique][2], kf[kCollectUnique];
     int n_seen = 0;
-    for (int m = 0; m < per_query; ++m) {
-        bool ok = false;
+    float fsum = 0.f;
+    for (int m = 0; m < per_query && have_light; ++m) {
         Vtx v;
-        if (have_light) {
-            const float sx = rng.next_f32(), sy = rng.next_f32();
-            f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
-            int it;
-            ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
-            st.walks++;
-            st.newton += (unsigned)it;
-            if (ok) st.succ++; else st.fail++;
-            if (ok) {
-                // keep each contributing solution of the query once
-                const f3 dir = normalize(v.p - Q.x);
-                for (int j = 0; j < n_seen && ok; ++j)
-                    if (fabsf(dot(dir, seen[j]) - 1.f) < cfg.uniqueness_threshold) ok = false;
-                if (ok) ok = visible(sc, L.p, v.p, err, st);
-                if (ok && n_seen < kCollectUnique) seen[n_seen++] = dir;
-            }
-        }
-        const unsigned want = __ballot_sync(0xffffffffu, ok);
-        if (want) {
-            const unsigned leader = __ffs(want) - 1;
-            unsigned base = 0;
-            if (lane == leader) base = atomicAdd(fill, (unsigned)__popc(want));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            const unsigned idx = base + __popc(want & ((1u << lane) - 1u));
-            if (ok && idx < cap) {
-                float u, w;
-                mlp::frame_uv(fr, v.p, u, w);
-                const float rec[mlp::kIn + 2] = {Q.x.x, Q.x.y, Q.x.z, L.p.x, L.p.y, L.p.z, Q.n.x, Q.n.y, Q.n.z, u, w};
-                #pragma unroll
-                for (int k = 0; k < mlp::kIn + 2; ++k) data[(size_t)k * cap + idx] = rec[k];
-            }
-        }
+        const float sx = rng.next_f32(), sy = rng.next_f32();
+        f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
+        int it;
+        bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
+        st.walks++;
+        st.newton += (unsigned)it;
+        if (ok) st.succ++; else st.fail++;
+        if (!ok || n_seen >= kCollectUnique) continue;
+        const f3 dir = normalize(v.p - Q.x);
+        bool dup = false;
+        for (int j = 0; j < n_seen; ++j)
+            if (fabsf(dot(dir, seen[j]) - 1.f) < cfg.uniqueness_threshold) dup = true;
+        if (dup || !visible(sc, L.p, v.p, err, st)) continue;
+        const f3 c = diffuse_eval(Q, dir) * contribution(sc, Q.x, L, v, err, st);
+        seen[n_seen] = dir;
+        mlp::frame_uv(fr, v.p, kuv[n_seen][0], kuv[n_seen][1]);
+        kf[n_seen] = fmaxf(0.f, (c.x + c.y + c.z) * (1.f / 3.f));
+        fsum += kf[n_seen];
+        n_seen++;
+    }
+    // warp-aggregated append of every lane's solutions
+    int incl = n_seen;
+    #pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, off);
+        if ((int)lane >= off) incl += y;
+    }
+    unsigned base = 0;
+    if (lane == 31 && incl) base = atomicAdd(fill, (unsigned)incl);
+    base = __shfl_sync(0xffffffffu, base, 31) + (unsigned)(incl - n_seen);
+    for (int j = 0; j < n_seen; ++j) {
+        const unsigned idx = base + (unsigned)j;
+        if (idx >= cap) break;
+        const float w = fsum > 0.f ? kf[j] / fsum : 1.f / (float)n_seen;
+        const float rec[mlp::kDataRows] = {Q.x.x, Q.x.y, Q.x.z, L.p.x, L.p.y, L.p.z, Q.n.x, Q.n.y, Q.n.z,
+                                           kuv[j][0], kuv[j][1], w};
+        #pragma unroll
+        for (int k = 0; k < mlp::kDataRows; ++k) data[(size_t)k * cap + idx] = rec[k];
     }
     flush_stats(st, ctr, err, kPhaseSsWalk);
 }

@@ -112,6 +112,15 @@ def test_loss_and_gradient_match_oracle(sms, workloads, gpu_lib):
         assert (grad @ gx) / np.linalg.norm(grad) / np.linalg.norm(gx) > 0.99
         # padded input columns carry no gradient
         assert np.all(M.unpack(grad)[0][0][:, M.N_ENC:] == 0)
+    # contribution-weighted loss
+    wt = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    prop.set_data(feat, uv, wt)
+    loss, grad = prop.loss_grad(256)
+    lo, go = M.loss_grad(st["params"], st["norm"][:9], st["norm"][9:], feat[:, :256], uv[:, :256], bf=True,
+                         frame=fr, weights=wt[:256])
+    assert abs(loss - lo) < 1e-3 * max(1.0, abs(lo))
+    cos = grad @ go / np.linalg.norm(grad) / np.linalg.norm(go)
+    assert cos > GRAD_COS and np.linalg.norm(grad - go) / np.linalg.norm(go) < GRAD_REL
 
 
 def test_adam_update_matches_closed_form(sms, workloads, gpu_lib):
@@ -175,8 +184,12 @@ def test_collected_pairs_are_solver_solutions(sms, workloads, oracle, gpu_lib):
     prop, total = _collect(sms, W, ctx, n=4096, walks=2)
     st = ctx.stats()
     assert 100 < total <= st["solver_succeeded"]
-    feat, uv = prop.get_data()
+    feat, uv, wt = prop.get_data()
     assert feat.shape == (9, total)
+    # weights: contribution shares of each query's solutions (sum 1 per query)
+    assert np.all(wt >= 0) and np.all(wt <= 1 + 1e-6)
+    _, inv = np.unique(feat[0:2].T, axis=0, return_inverse=True)
+    np.testing.assert_allclose(np.bincount(inv.ravel(), weights=wt), 1.0, rtol=1e-4)
     # features: shading point on the receiver, light sample on the light, normal
     assert np.all(np.abs(feat[2]) < 1e-6) and np.all(np.abs(feat[8] - 1) < 1e-6)
     assert np.all(np.abs(np.linalg.norm(feat[3:6] - np.array([[0], [0], [10]]), axis=0) - 0.1) < 1e-4)

@@ -115,6 +115,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def shard(rank: int, n: int) -> tuple[int, int]:
+    """Replica sharding: rank r solves queries [r n, (r+1) n) of the global
+    set on PCG32 streams starting at r n, so N ranks reproduce one N n-query
+    run exactly (no data-path collective)."""
+    return rank * n, rank * n
+
+
+def max_over_ranks(torch, values, device):
+    """Element-wise maximum of per-rank timings (identity without a process group)."""
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -344,7 +360,8 @@ def run_ours(args):
     ctx = sms.Context(sms.Scene(desc), cfg, device=dev)
     ss = sms.SpecularManifoldSingleScatter(ctx)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
-    q_host = W.water_queries(n, first=rank * n)
+    first, offset = shard(rank, n)
+    q_host = W.water_queries(n, first=first)
     q_dev = torch.from_numpy(q_host).to(f"cuda:{dev}")
     val = torch.empty((3, n), dtype=torch.float32, device=f"cuda:{dev}")
     cnt = torch.empty(n, dtype=torch.int32, device=f"cuda:{dev}")
@@ -355,7 +372,7 @@ def run_ours(args):
         with torch.cuda.stream(stream):
             flush.zero_()   # L2 flush between steps (256 MiB write)
         ss.specular_manifold_sampling_device(q_dev.data_ptr(), n, val.data_ptr(), cnt.data_ptr(),
-                                             wlk.data_ptr(), seed=seed, stream_offset=rank * n)
+                                             wlk.data_ptr(), seed=seed, stream_offset=offset)
 
     for i in range(args.warmup):
         step(100 + i)
@@ -374,7 +391,7 @@ def run_ours(args):
             flush.zero_()
             ev[i][0].record(stream)
         ss.specular_manifold_sampling_device(q_dev.data_ptr(), n, val.data_ptr(), cnt.data_ptr(),
-                                             wlk.data_ptr(), seed=1 + i, stream_offset=rank * n)
+                                             wlk.data_ptr(), seed=1 + i, stream_offset=offset)
         with torch.cuda.stream(stream):
             ev[i][1].record(stream)
     torch.cuda.synchronize()
@@ -392,24 +409,21 @@ def run_ours(args):
     import ctypes as C
     lib = sms.load_library()
     res = sms._Result(vh.data_ptr(), ch.data_ptr(), wh.data_ptr())
-    sms._check(lib.sms_ss_connect_batch(ctx.handle, qh.data_ptr(), n, 200, rank * n, C.byref(res)))
+    sms._check(lib.sms_ss_connect_batch(ctx.handle, qh.data_ptr(), n, 200, offset, C.byref(res)))
     e2e_t = []
     for i in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        sms._check(lib.sms_ss_connect_batch(ctx.handle, qh.data_ptr(), n, 1 + i, rank * n, C.byref(res)))
+        sms._check(lib.sms_ss_connect_batch(ctx.handle, qh.data_ptr(), n, 1 + i, offset, C.byref(res)))
         e2e_t.append(time.perf_counter() - t1)
     clk = clocks.stop()
 
     step_ms = float(np.mean(step_ms_list))
     total_s = float(np.sum(step_ms_list)) / 1e3
     e2e_s = float(np.sum(e2e_t))
-    if world > 1:
-        t = torch.tensor([total_s, e2e_s], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s, e2e_s = t.tolist()
+    total_s, e2e_s = max_over_ranks(torch, [total_s, e2e_s], f"cuda:{dev}")
     value = world * n * args.steps / total_s
     e2e_value = world * n * args.steps / e2e_s
 

@@ -221,6 +221,7 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     cfg = W.water_config()
     ctx.set_config(cfg)
+    ctx.set_trial_group(0)   # 32 lanes per query for uniform seeds, 8 for learned ones
     prop = sms.SeedProposal(ctx, 0, seed=1, capacity=pairs)
     prop.set_options(sigma_scale, weighted)
     chunk = 1 << 20
@@ -374,6 +375,13 @@ def run_ours(args):
         ss.specular_manifold_sampling_device(q_dev.data_ptr(), n, val.data_ptr(), cnt.data_ptr(),
                                              wlk.data_ptr(), seed=seed, stream_offset=offset)
 
+    tuned = None
+    if not args.no_autotune:
+        # launch shape (blocks per SM x trial group) picked on a quarter of the
+        # step's queries; no shape changes a result
+        from sms_gb300.autotune import autotune_ss
+        m = max(1, n // 4)
+        tuned = autotune_ss(sms, ctx, q_dev.data_ptr(), m, val.data_ptr(), cnt.data_ptr(), wlk.data_ptr())
     for i in range(args.warmup):
         step(100 + i)
     torch.cuda.synchronize()
@@ -447,7 +455,9 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "queries_per_step": n, "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "launch": ({"blocks_per_sm": tuned["best"][0], "trial_group": tuned["best"][1],
+                               "autotune_ms": tuned["ms"]} if tuned else "library default")},
         "walks_per_s": world * st["walks"] / total_s,
         "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),
         "trials_per_connection": st["bernoulli_trial_iterations"] / max(1, st["bernoulli_trial_calls"]),
@@ -501,6 +511,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal study")
+    ap.add_argument("--no-autotune", action="store_true", help="library default launch shape")
     ap.add_argument("--queries", type=int, default=N_QUERIES, help="queries per step (smaller cases for ncu)")
     ap.add_argument("--learned-pairs", type=int, default=4 << 20)
     ap.add_argument("--learned-steps", type=int, default=20000)

@@ -213,7 +213,7 @@ def secondary_configs(torch, sms, W, dev):
 
 
 def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=8192, lr=1e-3, res=128,
-                  ref_spp=4096, sigma_scale=1.0, weighted=True):
+                  ref_spp=4096, sigma_scale=1.0, weighted=True, walks_per_query=8):
     """Learned seed proposal on the water workload: training pairs from the
     uniform-seed solver, GPU training, then equal-time caustic RMSE of
     learned vs uniform seeding against a ref_spp uniform-seed image of
@@ -230,7 +230,8 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
         while total < pairs and calls < 16:
             q = torch.from_numpy(W.water_queries(chunk, seed=77, first=calls * chunk)).to(f"cuda:{dev}")
             torch.cuda.synchronize()
-            total = prop.collect(q.data_ptr(), chunk, seed=77, stream_offset=calls * chunk, walks_per_query=8)
+            total = prop.collect(q.data_ptr(), chunk, seed=77, stream_offset=calls * chunk,
+                                 walks_per_query=walks_per_query)
             calls += 1
     prop.normalize()
     loss0, _ = prop.loss_grad(batch)
@@ -283,7 +284,7 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     ref, ref_ms = render(ref_spp, 11, 1 << 30, False)
     rows = []
     for learned in (False, True):
-        for spp in (4, 16, 64):
+        for spp in ((4, 16, 64) if not learned else (4, 8, 16, 24, 32, 48, 64)):
             extra = {} if spp == 64 else None
             img, ms = render(spp, 12 + spp, 1 << 28, learned, extra)
             rmse = float(np.sqrt(np.mean((img - ref) ** 2)))
@@ -294,6 +295,10 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     uni64 = next(r for r in rows if r["seeding"] == "uniform" and r["spp"] == 64)
     reach = [r for r in rows if r["seeding"] == "learned" and r["rmse"] <= uni64["rmse"]]
     t_equal = min(r["ms"] for r in reach) if reach else None
+    # the same from the 64-spp renders, with MSE ~ 1/spp: learned time at which
+    # its MSE reaches the uniform 64-spp MSE
+    l64 = next(r for r in rows if r["seeding"] == "learned" and r["spp"] == 64)
+    t_equal_fit = l64["ms"] * (l64["rmse"] / uni64["rmse"]) ** 2
     # per-sample efficiency: MSE x time at 64 spp (lower is better)
     eff = {}
     for mode in ("uniform", "learned"):
@@ -311,6 +316,7 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
         "renders": rows,
         "learned_ms_to_uniform64_rmse": t_equal,
         "time_ratio_to_equal_rmse": (uni64["ms"] / t_equal) if t_equal else None,
+        "time_ratio_to_equal_rmse_fit": uni64["ms"] / t_equal_fit,
         "mse_x_time_ratio_64spp": eff["uniform"] / max(eff["learned"], 1e-30),
     }
 

@@ -30,7 +30,7 @@ struct TNode {
     uint32_t first = 0, count = 0;
 };
 
-constexpr int kMaxLeaf = 4;
+constexpr int kMaxLeaf = 2;
 constexpr int kMaxDepth = 56;   // below the device traversal stack depth
 constexpr int kBins = 16;
 

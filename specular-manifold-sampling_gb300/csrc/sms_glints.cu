@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(128) glint_walk_kernel(DevScene sc, SolverCfg 
 // G lanes per query, walk m at stream position 3 + 2m; deduplication in uv in
 // walk order (:117-138), contributions only for first occurrences.
 template <int G>
-__global__ void __launch_bounds__(128) glint_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
+__global__ void __launch_bounds__(128, 8) glint_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
                                                            uint32_t n, uint64_t seed, uint64_t stream_off,
                                                            float *__restrict__ value, int *__restrict__ count,
                                                            int *__restrict__ walks, DevCounters *ctr) {
@@ -496,7 +496,7 @@ cudaError_t launch_glint_connect(const DevScene &sc, const SolverCfg &cfg, const
                                  uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                                  const SsScratch &scr, int num_sms, int blocks_per_sm, PhaseTimer *tm, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 8;
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 16;
     phase_begin(tm, kPhaseGlints, s);
     if (cfg.biased) {
         const int G = cfg.max_trials <= 16 ? 16 : 32;

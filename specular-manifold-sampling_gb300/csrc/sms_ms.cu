@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(128) ms_walk_kernel(DevScene sc, SolverCfg cfg
 // deduplicated before the contribution, which itself tests visibility
 // (:147-195).
 template <int K, int G>
-__global__ void __launch_bounds__(128) ms_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
+__global__ void __launch_bounds__(128, 4) ms_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
                                                         int *__restrict__ walks, DevCounters *ctr) {
@@ -803,7 +803,7 @@ cudaError_t launch_ms_connect(const DevScene &sc, const SolverCfg &cfg, int boun
         if (e == cudaSuccess) e = cudaMemsetAsync(walks, 0, (size_t)n * sizeof(int), s);
         return e;
     }
-    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 8;
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 16;
     switch (bounces) {
     case 1: return ms_connect_k<1>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr, scr, tmpl, num_sms, bps, tm, s);
     case 2: return ms_connect_k<2>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr, scr, tmpl, num_sms, bps, tm, s);

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(128) ss_walk_kernel(DevScene sc, SolverCfg cfg
 // 3 + 2 (c M + m).  Contributions are summed in walk order over the first
 // occurrences of each solution direction, exactly as manifold_ss.cpp:146-196.
 template <int G>
-__global__ void __launch_bounds__(128) ss_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
+__global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
                                                         int *__restrict__ walks, DevCounters *ctr) {
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(128) ss_biased_kernel(DevScene sc, SolverCfg c
 // (weights staged in shared memory), stores each query's mixture for the
 // trials kernel and then runs the first walk.
 template <bool kLearned>
-__global__ void __launch_bounds__(128, kLearned ? 3 : 4) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+__global__ void __launch_bounds__(128, kLearned ? 3 : 8) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
                                                        float *__restrict__ value, int *__restrict__ count,
                                                        int *__restrict__ walks, SsScratch scr, DevCounters *ctr,
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(128, kLearned ? 3 : 4) ss_first_kernel(DevScen
 // All lanes run one warp-uniform loop: groups whose query finished fetch the
 // next one at the top, so every ballot and shuffle has the whole warp.
 template <bool kLearned, int G>
-__global__ void __launch_bounds__(128, 4) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+__global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
                                                         int *__restrict__ walks, SsScratch scr, DevCounters *ctr,
@@ -570,7 +570,7 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
                               const SsScratch &scr, int num_sms, int blocks_per_sm, PhaseTimer *tm,
                               cudaStream_t s, const mlp::SeedProposal *prop, int trial_group) {
     if (n == 0) return cudaSuccess;
-    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 8;
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 16;
     if (cfg.biased) {
         const int G = cfg.max_trials <= 16 ? 16 : 32;
         const uint32_t groups_per_block = 128 / G;

@@ -31,7 +31,7 @@ struct TNode {
 };
 
 constexpr int kMaxLeaf = 2;
-constexpr int kMaxDepth = 56;   // below the device traversal stack depth
+constexpr int kMaxDepth = 31;   // below the device traversal stack depth (32)
 constexpr int kBins = 16;
 
 struct Builder {

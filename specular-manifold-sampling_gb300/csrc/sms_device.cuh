@@ -66,7 +66,7 @@ constexpr float kRayEps = 5.9604644775390625e-08f * 1500.f;
 constexpr float kShadowEps = kRayEps * 10.f;
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kInvPi = 0.31830988618379067154f;
-constexpr int kStackDepth = 64;
+constexpr int kStackDepth = 32;
 constexpr int kMaxCasters = 8;
 constexpr int kMaxEmitters = 16;
 constexpr int kMaxSpheres = 16;

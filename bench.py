@@ -212,7 +212,7 @@ def secondary_configs(torch, sms, W, dev):
     return out
 
 
-def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=8192, lr=1e-3, res=128,
+def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=8192, lr=1e-3, res=256,
                   ref_spp=4096, sigma_scale=1.0, weighted=True, walks_per_query=8):
     """Learned seed proposal on the water workload: training pairs from the
     uniform-seed solver, GPU training, then equal-time caustic RMSE of
@@ -249,8 +249,25 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     pix = W.plane_queries(np.stack([xx.ravel(), yy.ravel()], axis=1).astype(np.float32))
     npix = pix.shape[1]
 
+    # trial-group size for learned seeds, tuned on a 16-spp sample of the image
+    from sms_gb300.autotune import autotune_ss
+    ctx.set_proposal(prop, 0.1)
+    qs = torch.from_numpy(np.tile(pix, (1, 16))).to(f"cuda:{dev}")
+    ns = qs.shape[1]
+    vs = torch.empty((3, ns), dtype=torch.float32, device=f"cuda:{dev}")
+    cs = torch.empty(ns, dtype=torch.int32, device=f"cuda:{dev}")
+    ws = torch.empty(ns, dtype=torch.int32, device=f"cuda:{dev}")
+    torch.cuda.synchronize()
+    tune = autotune_ss(sms, ctx, qs.data_ptr(), ns, vs.data_ptr(), cs.data_ptr(), ws.data_ptr(),
+                       blocks_per_sm=(16,), trial_groups=(8, 16, 32), seed=99)
+    learned_group = tune["best"][1]
+    ctx.set_proposal(None)
+    ctx.set_launch(0, 0)
+    ctx.set_trial_group(0)
+
     def render(spp, seed, offset, learned, stats=None):
         ctx.set_proposal(prop if learned else None, 0.1)
+        ctx.set_trial_group(learned_group if learned else 0)
         if stats is not None:
             ctx.reset_stats()
             ctx.set_profiling(True)
@@ -284,7 +301,7 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     ref, ref_ms = render(ref_spp, 11, 1 << 30, False)
     rows = []
     for learned in (False, True):
-        for spp in ((4, 16, 64) if not learned else (4, 8, 16, 24, 32, 48, 64)):
+        for spp in (8, 16, 32, 64):
             extra = {} if spp == 64 else None
             img, ms = render(spp, 12 + spp, 1 << 28, learned, extra)
             rmse = float(np.sqrt(np.mean((img - ref) ** 2)))
@@ -295,10 +312,22 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     uni64 = next(r for r in rows if r["seeding"] == "uniform" and r["spp"] == 64)
     reach = [r for r in rows if r["seeding"] == "learned" and r["rmse"] <= uni64["rmse"]]
     t_equal = min(r["ms"] for r in reach) if reach else None
-    # the same from the 64-spp renders, with MSE ~ 1/spp: learned time at which
-    # its MSE reaches the uniform 64-spp MSE
-    l64 = next(r for r in rows if r["seeding"] == "learned" and r["spp"] == 64)
-    t_equal_fit = l64["ms"] * (l64["rmse"] / uni64["rmse"]) ** 2
+    # least-squares fit MSE(spp) = a / spp + b per seeding over the renders (b:
+    # the reference's own noise and the truncation-bias difference); time per
+    # sample from the 64-spp render.  Equal-RMSE time ratio = (a t)_uniform /
+    # (a t)_learned.
+    fit = {}
+    for mode in ("uniform", "learned"):
+        rs = [r for r in rows if r["seeding"] == mode]
+        A = np.array([[1.0 / r["spp"], 1.0] for r in rs])
+        y = np.array([r["rmse"] ** 2 for r in rs])
+        (a, b), *_ = np.linalg.lstsq(A, y, rcond=None)
+        t1 = next(r["ms"] for r in rs if r["spp"] == 64) / 64.0
+        fit[mode] = {"mse_per_sample": float(a), "mse_floor": float(b), "ms_per_sample": t1}
+    t_equal_fit = None
+    if fit["learned"]["mse_per_sample"] > 0:
+        t_equal_fit = uni64["ms"] * (fit["learned"]["mse_per_sample"] * fit["learned"]["ms_per_sample"]) / (
+            fit["uniform"]["mse_per_sample"] * fit["uniform"]["ms_per_sample"])
     # per-sample efficiency: MSE x time at 64 spp (lower is better)
     eff = {}
     for mode in ("uniform", "learned"):
@@ -313,10 +342,12 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
                   "roofline": {"bound": "tensor", "achieved": flop_step / (step_ms / 1e3) / 1e12,
                                "unit": "TFLOP/s", "flop_per_step": flop_step}},
         "reference_ms": ref_ms,
+        "learned_trial_group": learned_group,
         "renders": rows,
         "learned_ms_to_uniform64_rmse": t_equal,
         "time_ratio_to_equal_rmse": (uni64["ms"] / t_equal) if t_equal else None,
-        "time_ratio_to_equal_rmse_fit": uni64["ms"] / t_equal_fit,
+        "time_ratio_to_equal_rmse_fit": (uni64["ms"] / t_equal_fit) if t_equal_fit else None,
+        "mse_fit": fit,
         "mse_x_time_ratio_64spp": eff["uniform"] / max(eff["learned"], 1e-30),
     }
 

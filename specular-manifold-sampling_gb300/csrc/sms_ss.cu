@@ -227,47 +227,44 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
     flush_stats(st, ctr, err, kPhaseSsBiased);
 }
 
-// --------------------------------------------------- unbiased: first walks
-// kLearned: seeds come from the query's learned mixture (three draws per walk,
-// mlp::proposal_seed) instead of two-draw uniform seeding.  The warp first
-// evaluates the proposal network for its 32 queries on the tensor cores
-// (weights staged in shared memory), stores each query's mixture for the
-// trials kernel and then runs the first walk.
-template <bool kLearned>
-__global__ void __launch_bounds__(128, kLearned ? 3 : 8) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
-                                                       uint32_t n, uint64_t seed, uint64_t stream_off,
-                                                       float *__restrict__ value, int *__restrict__ count,
-                                                       int *__restrict__ walks, SsScratch scr, DevCounters *ctr,
-                                                       mlp::SeedProposal pr) {
-    const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = qi < n;
+// ------------------------------------------ learned proposal: inference
+// The proposal network for every query of a batch, before its first walk:
+// each warp takes 32 queries, draws their emitter samples (the same 3 draws
+// the estimator makes), evaluates the network on the tensor cores (weights
+// staged once per block in shared memory) and stores each query's mixture
+// (cdf, means, sigmas) for the first-walk and trial kernels.  Kept apart from
+// the first-walk kernel so that kernel keeps the walk kernels' occupancy (the
+// network needs 168 registers and 66 KB of shared memory per block).
+__global__ void __launch_bounds__(128, 3) ss_proposal_kernel(DevScene sc, const float *__restrict__ qs, uint32_t n,
+                                                             uint64_t seed, uint64_t stream_off,
+                                                             mlp::SeedProposal pr) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kStage = 16 * mlp::kXLd / 2;   // floats: input tile, then output rows
+    __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+    float *feats = reinterpret_cast<float *>(smem_raw + (size_t)mlp::kWeightsFwd * 2) +
+                   (threadIdx.x / 32) * (32 * mlp::kIn + kStage);
+    float *stage = feats + 32 * mlp::kIn;
+    mlp::stage_weights(pr.net.wbf, sw, mlp::kWeightsFwd);
+    __syncthreads();
     const unsigned lane = threadIdx.x & 31;
-    LaneStats st;
-    uint32_t err = 0;
-    bool enqueue = false;
-    Query Q;
-    Pcg32 rng;
-    Light L;
-    bool have_light = false;
-    if (active) {
-        Q = load_query(qs, n, qi);
-        rng = query_rng(seed, stream_off + qi, 0);
-        have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
-    }
-    if constexpr (kLearned) {
-        extern __shared__ __align__(16) unsigned char smem_raw[];
-        constexpr int kStage = 16 * mlp::kXLd / 2;   // floats: input tile, then output rows
-        __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
-        float *feats = reinterpret_cast<float *>(smem_raw + (size_t)mlp::kWeightsFwd * 2) +
-                       (threadIdx.x / 32) * (32 * mlp::kIn + kStage);
-        float *stage = feats + 32 * mlp::kIn;
-        mlp::stage_weights(pr.net.wbf, sw, mlp::kWeightsFwd);
+    const uint32_t wpb = blockDim.x / 32;
+    for (uint32_t w = blockIdx.x * wpb + threadIdx.x / 32; (size_t)w * 32 < n; w += gridDim.x * wpb) {
+        const uint32_t qi = w * 32 + lane;
+        const bool active = qi < n;
+        f3 fx = splat(0.f), fl = splat(0.f), fn = splat(0.f);
+        if (active) {
+            const Query Q = load_query(qs, n, qi);
+            Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+            Light L;
+            fx = Q.x;
+            fn = Q.n;
+            if (sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L)) fl = L.p;
+        }
         // this lane's normalised features: shading point, light sample, normal
-        const f3 fx = active ? Q.x : splat(0.f), fl = have_light ? L.p : splat(0.f), fn = active ? Q.n : splat(0.f);
         const float fv[mlp::kIn] = {fx.x, fx.y, fx.z, fl.x, fl.y, fl.z, fn.x, fn.y, fn.z};
         #pragma unroll
         for (int k = 0; k < mlp::kIn; ++k) feats[lane * mlp::kIn + k] = (fv[k] - pr.net.shift[k]) * pr.net.scale[k];
-        __syncthreads();
+        __syncwarp();
         #pragma unroll 1
         for (int h = 0; h < 2; ++h) {
             float xn[mlp::kIn];
@@ -288,6 +285,33 @@ __global__ void __launch_bounds__(128, kLearned ? 3 : 8) ss_first_kernel(DevScen
             }
             __syncwarp();
         }
+    }
+}
+
+// --------------------------------------------------- unbiased: first walks
+// kLearned: seeds come from the query's learned mixture (three draws per walk,
+// mlp::proposal_seed, mixture from ss_proposal_kernel) instead of two-draw
+// uniform seeding.
+template <bool kLearned>
+__global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+                                                       uint32_t n, uint64_t seed, uint64_t stream_off,
+                                                       float *__restrict__ value, int *__restrict__ count,
+                                                       int *__restrict__ walks, SsScratch scr, DevCounters *ctr,
+                                                       mlp::SeedProposal pr) {
+    const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = qi < n;
+    const unsigned lane = threadIdx.x & 31;
+    LaneStats st;
+    uint32_t err = 0;
+    bool enqueue = false;
+    Query Q;
+    Pcg32 rng;
+    Light L;
+    bool have_light = false;
+    if (active) {
+        Q = load_query(qs, n, qi);
+        rng = query_rng(seed, stream_off + qi, 0);
+        have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
     }
     if (active) {
         uint32_t pos = 3u;
@@ -597,10 +621,12 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
         phase_begin(tm, kPhaseSsFirst, s);
         if (learned) {
             const size_t smem = mlp::smem_seed_fused();
-            e = cudaFuncSetAttribute(ss_first_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = cudaFuncSetAttribute(ss_proposal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            ss_first_kernel<true><<<(n + 127) / 128, 128, smem, s>>>(sc, cfg, c, q, n, seed, stream_off, value,
-                                                                     count, walks, scr, ctr, pr);
+            const uint32_t pblocks = std::min<uint32_t>((n + 127) / 128, (uint32_t)num_sms * 3);
+            ss_proposal_kernel<<<pblocks, 128, smem, s>>>(sc, q, n, seed, stream_off, pr);
+            ss_first_kernel<true><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value,
+                                                                  count, walks, scr, ctr, pr);
         } else {
             ss_first_kernel<false><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count,
                                                                    walks, scr, ctr, pr);

@@ -74,6 +74,7 @@ def load(fma: bool = False):
         "oracle_glint_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
         "oracle_nm_slope": (None, [vp, f32, f32, vp]),
         "oracle_ss_emitter_batch": (i32, [vp, vp, u32, u64, u64, vp]),
+        "oracle_ss_step_at": (i32, [vp, i32, i32, f32, f32, vp, vp, vp]),
         "oracle_ss_connect_learned_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, i32, f32, vp, vp,
                                                   vp, vp, vp, C.c_int, vp]),
         "oracle_fresnel": (f32, [f32, f32, C.POINTER(f32)]),
@@ -191,6 +192,16 @@ class OracleScene:
         names = ["solver_succeeded", "solver_failed", "bernoulli_trial_calls", "bernoulli_trial_iterations",
                  "bernoulli_trial_iterations_max", "walks", "newton_iterations", "connections"]
         return value, count, walks, dict(zip(names, stats.tolist()))
+
+    def step_at(self, shape: int, halfvector: bool, u: float, v: float, x, lp) -> np.ndarray:
+        """ok, C (2), J (2x2 row-major) of the single-scatter Newton step at the
+        sphere point with uv (u, v)."""
+        out = np.zeros(7, np.float32)
+        xa = np.ascontiguousarray(x, np.float32)
+        la = np.ascontiguousarray(lp, np.float32)
+        self._lib.oracle_ss_step_at(self._h, shape, int(halfvector), u, v, xa.ctypes.data, la.ctypes.data,
+                                    out.ctypes.data)
+        return out
 
     def emitter_batch(self, queries: np.ndarray, seed: int = 0, stream_offset: int = 0) -> np.ndarray:
         """The single-scatter estimator's emitter sample per query: rows ei.p

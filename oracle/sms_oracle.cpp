@@ -630,7 +630,7 @@ static void d_sphcoords(V3 w, V3 dwdu, V3 dwdv, float &dtu, float &dpu, float &d
 
 /* ------------------------------------------------------ constraints */
 /* manifold_ss.cpp:494-636 */
-static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX) {
+static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr) {
     V3 wi = x - v1.p;
     float ili = norm(wi);
     if (ili < 1e-3f) return false;
@@ -685,6 +685,7 @@ static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX)
         J.m[0][0] = a0 - b0; J.m[1][0] = a1 - b1; J.m[0][1] = a2 - b2; J.m[1][1] = a3 - b3;
         success = true;
     }
+    if (J_out) *J_out = J;
     float d = det(J);
     if (std::fabs(d) < 1e-6f) return false;
     dX = mul(inverse(J), C);
@@ -692,7 +693,7 @@ static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX)
 }
 
 /* manifold_ss.cpp:407-492 */
-static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX) {
+static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr) {
     V3 wo = ei.p - v1.p;
     float ilo = norm(wo);
     if (ilo < 1e-3f) return false;
@@ -719,6 +720,7 @@ static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX
     J.m[1][0] = dot(v1.dt_du, h) + dot(v1.t, dh_du);
     J.m[0][1] = dot(v1.ds_dv, h) + dot(v1.s, dh_dv);
     J.m[1][1] = dot(v1.dt_dv, h) + dot(v1.t, dh_dv);
+    if (J_out) { *J_out = J; C = V2{dot(v1.s, h), dot(v1.t, h)}; }
     float d = det(J);
     if (std::fabs(d) < 1e-6f) return false;
     C = V2{dot(v1.s, h), dot(v1.t, h)};
@@ -2095,6 +2097,62 @@ int oracle_ss_connect_batch(void *s, const sms_config *cfg, const float *queries
         stats_out[3] = st.iters; stats_out[4] = st.iters_max; stats_out[5] = st.walks;
         stats_out[6] = st.newton; stats_out[7] = st.connections;
     }
+    return 0;
+}
+
+/* Constraint and Jacobian of one single-scatter Newton step at the point of
+ * `shape` with uv (u, v) (sphere: sphere.cpp:322-373 parametrization; mesh:
+ * texture coordinates), for a
+ * shading point x and light point lp: out = ok, C (2), J (2x2, row-major:
+ * rows the constraint components, columns d/du, d/dv).  Test hook for the
+ * finite-difference check of compute_step_anglediff / _halfvector. */
+int oracle_ss_step_at(void *s, int shape, int halfvector, float u, float v, const float *x, const float *lp,
+                      float *out) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    for (int k = 0; k < 7; ++k) out[k] = 0.f;
+    if (shape < 0 || shape >= (int)sc->shapes.size()) return 1;
+    const Shape &sh = sc->shapes[shape];
+    Ray r;
+    if (sh.kind == 0) {
+        const float th = kPi * v, ph = 2.f * kPi * u;
+        V3 dir(std::sin(th) * std::cos(ph), std::sin(th) * std::sin(ph), std::cos(th));
+        r.o = sh.center + dir * (3.f * sh.radius);
+        r.d = -dir;
+    } else {
+        /* mesh: (u, v) are texture coordinates; find the face holding them */
+        if (sh.UV.empty()) return 1;
+        bool found = false;
+        for (size_t f = 0; f < sh.F.size() / 3 && !found; ++f) {
+            V2 a = sh.UV[sh.F[3 * f]], b = sh.UV[sh.F[3 * f + 1]], c = sh.UV[sh.F[3 * f + 2]];
+            float d = (b.x - a.x) * (c.y - a.y) - (c.x - a.x) * (b.y - a.y);
+            if (d == 0.f) continue;
+            float b1 = ((u - a.x) * (c.y - a.y) - (c.x - a.x) * (v - a.y)) / d;
+            float b2 = ((b.x - a.x) * (v - a.y) - (u - a.x) * (b.y - a.y)) / d;
+            if (b1 < 0.f || b2 < 0.f || b1 + b2 > 1.f) continue;
+            V3 p0 = sh.P[sh.F[3 * f]], p1 = sh.P[sh.F[3 * f + 1]], p2 = sh.P[sh.F[3 * f + 2]];
+            V3 pt = p0 * (1.f - b1 - b2) + p1 * b1 + p2 * b2;
+            V3 gn = normalize(cross(p1 - p0, p2 - p0));
+            r.o = pt + gn * 0.5f;
+            r.d = -gn;
+            found = true;
+        }
+        if (!found) return 2;
+    }
+    SI si = ray_intersect(*sc, r);
+    if (!si.valid() || si.shape != shape) return 2;
+    MVertex vtx;
+    vertex_from_si(*sc, si, vtx);
+    EI ei;
+    ei.p = V3(lp[0], lp[1], lp[2]);
+    ei.is_point = true;
+    V2 C, dX;
+    M2 J;
+    bool ok = halfvector ? step_halfvector(V3(x[0], x[1], x[2]), vtx, ei, C, dX, &J)
+                         : step_anglediff(V3(x[0], x[1], x[2]), vtx, ei, C, dX, &J);
+    out[0] = ok ? 1.f : 0.f;
+    out[1] = C.x; out[2] = C.y;
+    out[3] = J.m[0][0]; out[4] = J.m[0][1]; out[5] = J.m[1][0]; out[6] = J.m[1][1];
     return 0;
 }
 

@@ -47,18 +47,21 @@ def _walk_diff(a, b):
     return float(np.mean(oka != okb)), float(np.sum(~same)) / len(oka), med, int(both.sum())
 
 
+@pytest.mark.parametrize("halfvector", [False, True])
 @pytest.mark.parametrize("conductor", [False, True])
-def test_sphere_walks(sms, workloads, oracle, gpu_lib, conductor):
+def test_sphere_walks(sms, workloads, oracle, gpu_lib, conductor, halfvector):
     W = workloads
     desc = W.sphere_scene(conductor=conductor)
-    ctx = sms.Context(sms.Scene(desc), sms.SMSConfig())
+    cfg = sms.SMSConfig(halfvector_constraints=halfvector)
+    ctx = sms.Context(sms.Scene(desc), cfg)
     ss = sms.SpecularManifoldSingleScatter(ctx)
     q = W.sphere_queries(64)
     w = _walk_inputs(W, q.shape[1], (0.0, 0.0, 5.0))
     out_g = ss.sample_path(0, q, w)
-    out_o = oracle.OracleScene(desc).walk_batch(sms.SMSConfig(), 0, q, w)
+    out_o = oracle.OracleScene(desc).walk_batch(cfg, 0, q, w)
     mism, crossed, med, nboth = _walk_diff(out_g, out_o)
-    print(f"sphere conductor={conductor}: mismatch {mism:.5f} crossed {crossed:.5f} median|dp| {med:.1e} both {nboth}")
+    print(f"sphere conductor={conductor} halfvector={halfvector}: mismatch {mism:.5f} crossed {crossed:.5f} "
+          f"median|dp| {med:.1e} both {nboth}")
     assert nboth > 20
     assert mism < STRICT_MISMATCH and crossed < STRICT_MISMATCH
     assert med < 1e-5
@@ -69,11 +72,11 @@ def test_sphere_walks(sms, workloads, oracle, gpu_lib, conductor):
     assert np.mean(out_g[1, same] == out_o[1, same]) > 0.99
 
 
-@pytest.mark.parametrize("res", [128, 512])
-def test_water_walks_within_chaos_floor(sms, workloads, oracle, gpu_lib, res):
+@pytest.mark.parametrize("res,halfvector", [(128, False), (512, False), (128, True)])
+def test_water_walks_within_chaos_floor(sms, workloads, oracle, gpu_lib, res, halfvector):
     W = workloads
     desc = W.water_scene(res=res)
-    cfg = sms.SMSConfig()
+    cfg = sms.SMSConfig(halfvector_constraints=halfvector)
     ctx = sms.Context(sms.Scene(desc), cfg)
     ss = sms.SpecularManifoldSingleScatter(ctx)
     n = 16384
@@ -84,7 +87,7 @@ def test_water_walks_within_chaos_floor(sms, workloads, oracle, gpu_lib, res):
     out_f = oracle.OracleScene(desc, fma=True).walk_batch(cfg, 0, q, w)
     g_m, g_c, g_med, nboth = _walk_diff(out_g, out_o)
     f_m, f_c, f_med, _ = _walk_diff(out_f, out_o)
-    print(f"water{res}: gpu mismatch {g_m:.4f} crossed {g_c:.4f} | floor mismatch {f_m:.4f} "
+    print(f"water{res} halfvector={halfvector}: gpu mismatch {g_m:.4f} crossed {g_c:.4f} | floor mismatch {f_m:.4f} "
           f"crossed {f_c:.4f} | median|dp| {g_med:.1e} both {nboth}")
     assert nboth > 200
     assert g_m <= FLOOR_FACTOR * f_m + FLOOR_SLACK

@@ -266,3 +266,106 @@ def test_glint_walks_reach_target_slope(sms, workloads, oracle):
         target = -h[:2] / h[2]
         s = o.slope(out[2, i], out[3, i])[:2]
         assert np.linalg.norm(s - target) < 1e-4
+
+
+@pytest.mark.parametrize("halfvector", [False])
+@pytest.mark.parametrize("conductor", [False, True])
+def test_newton_jacobian_matches_finite_differences(sms, workloads, oracle, halfvector, conductor):
+    """compute_step_anglediff / compute_step_halfvector (manifold_ss.cpp:410-636):
+    the analytic 2x2 Jacobian of the constraint against central differences of
+    the constraint along the sphere's (u, v) parametrization.  Points whose
+    directions come within 25 degrees of the sphcoords pole (where the angle
+    constraint is too nonlinear for a finite difference) are skipped."""
+    W = workloads
+    osc = oracle.OracleScene(W.sphere_scene(conductor=conductor))
+    rng = np.random.default_rng(17 + 2 * halfvector + conductor)
+    lp = np.array([4.0, -3.0, 2.5], np.float32)   # off-axis: directions away from the pole
+    centre, radius, eta = np.array([0.0, 0.0, 1.5]), 1.0, (1.0 if conductor else 1.5)
+    h = 2e-4
+    checked = 0
+    for _ in range(200):
+        u, v = rng.uniform(0.05, 0.95), rng.uniform(0.1, 0.9)
+        x = np.array([rng.uniform(-2, 2), rng.uniform(-2, 2), 0.0], np.float32)
+        nrm = np.array([np.sin(np.pi * v) * np.cos(2 * np.pi * u), np.sin(np.pi * v) * np.sin(2 * np.pi * u),
+                        np.cos(np.pi * v)])
+        p = centre + radius * nrm
+        wi, wo = (x - p) / np.linalg.norm(x - p), (lp - p) / np.linalg.norm(lp - p)
+        if eta == 1.0:
+            turned = [2 * (w @ nrm) * nrm - w for w in (wi, wo)]
+        else:
+            turned = []
+            for w in (wi, wo):
+                e, n = 1 / eta, nrm
+                if w @ n < 0:
+                    e, n = eta, -n
+                root = 1 - e * e * (1 - (w @ n) ** 2)
+                turned.append(-(w - n * (w @ n)) * e - n * np.sqrt(max(root, 0.0)))
+        if max(abs(w[2]) for w in [wi, wo] + turned) > np.cos(np.radians(25)):
+            continue
+        c0 = osc.step_at(0, halfvector, u, v, x, lp)
+        if not c0[0]:
+            continue
+        J = c0[3:7].reshape(2, 2).astype(np.float64)
+        scale = max(1.0, np.abs(J).max())
+
+        def fd(hh):
+            cols = []
+            for du, dv in ((hh, 0.0), (0.0, hh)):
+                a = osc.step_at(0, halfvector, u + du, v + dv, x, lp)
+                b = osc.step_at(0, halfvector, u - du, v - dv, x, lp)
+                if not (a[0] and b[0]) or np.abs(a[1:3] - b[1:3]).max() > 1.0:   # failed or wrapped at +-pi
+                    return None
+                cols.append((a[1:3].astype(np.float64) - b[1:3]) / (2 * hh))
+            return np.stack(cols, axis=1)
+        d1, d2 = fd(2 * h), fd(h)
+        if d1 is None or d2 is None or np.abs(d1 - d2).max() > 1e-2 * scale:
+            continue   # too curved here for the difference to have converged
+        assert np.abs(J - d2).max() < 2e-2 * scale, (u, v, x.tolist(), J, d2)
+        checked += 1
+    assert checked >= 20
+
+
+@pytest.mark.parametrize("halfvector", [False, True])
+@pytest.mark.parametrize("conductor", [False, True])
+def test_newton_jacobian_on_a_curved_shading_mesh(sms, oracle, halfvector, conductor):
+    """Both constraints on a flat quad with tilted vertex normals (curved
+    shading, mesh.cpp:693-755 normal derivatives).  On a mesh the shading
+    frame derivative of the reference (frame.h:224-242, which treats dp_du as
+    constant) is exact, so the half-vector Jacobian is checked here; on a
+    sphere only the angle-difference one is (the frame derivative there omits
+    the parametrization's curvature, as in the reference)."""
+    d = sms.SceneDesc()
+    P = np.array([[-1, -1, 1.0], [1, -1, 1.0], [1, 1, 1.0], [-1, 1, 1.0]], np.float32)
+    N = np.array([[-0.3, -0.2, 1], [0.25, -0.3, 1], [0.3, 0.2, 1], [-0.2, 0.3, 1]], np.float32)
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    F = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    b = sms.Bsdf(sms.BSDF_CONDUCTOR, 0.2, 3.0) if conductor else sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)
+    d.add_mesh(P, F, b, sms.SHAPE_CAUSTIC_CASTER_SINGLE, N=N, UV=UV)
+    d.add_point_emitter((0.3, -0.2, 4.0), (100.0, 100.0, 100.0))
+    osc = oracle.OracleScene(d)
+    rng = np.random.default_rng(31 + 2 * halfvector + conductor)
+    lp = np.array([0.3, -0.2, 4.0], np.float32)
+    h = 2e-4
+    checked = 0
+    for _ in range(100):
+        u, v = rng.uniform(0.05, 0.95), rng.uniform(0.05, 0.95)
+        if abs(u - v) < 0.01:
+            continue   # keep the differences inside one triangle
+        x = np.array([rng.uniform(-1, 1), rng.uniform(-1, 1), 0.0], np.float32)
+        c0 = osc.step_at(0, halfvector, u, v, x, lp)
+        if not c0[0]:
+            continue
+        J = c0[3:7].reshape(2, 2).astype(np.float64)
+        scale = max(1.0, np.abs(J).max())
+        cols = []
+        for du, dv in ((h, 0.0), (0.0, h)):
+            a = osc.step_at(0, halfvector, u + du, v + dv, x, lp)
+            bb = osc.step_at(0, halfvector, u - du, v - dv, x, lp)
+            cols.append((a[1:3].astype(np.float64) - bb[1:3]) / (2 * h) if a[0] and bb[0] else None)
+        if any(c is None for c in cols) or max(np.abs(c).max() for c in cols) > 1e3:
+            continue
+        fd = np.stack(cols, axis=1)
+        assert np.abs(J - fd).max() < 2e-2 * scale, (u, v, x.tolist(), J, fd)
+        checked += 1
+    assert checked >= 20

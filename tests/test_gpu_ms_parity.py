@@ -20,10 +20,11 @@ def _ms_walk_diff(a, b, tol=1e-4):
             float(np.median(d[same])) if same.any() else 0.0, int(both.sum()))
 
 
-def test_slab_walks(sms, workloads, oracle, gpu_lib):
+@pytest.mark.parametrize("halfvector", [False, True])
+def test_slab_walks(sms, workloads, oracle, gpu_lib, halfvector):
     W = workloads
     desc = W.slab_scene()
-    cfg = sms.SMSConfig(bounces=2, max_iterations=30)
+    cfg = sms.SMSConfig(bounces=2, max_iterations=30, halfvector_constraints=halfvector)
     ctx = sms.Context(sms.Scene(desc), cfg)
     ms = sms.SpecularManifoldMultiScatter(ctx)
     n = 8192
@@ -37,7 +38,7 @@ def test_slab_walks(sms, workloads, oracle, gpu_lib):
     out_f = oracle.OracleScene(desc, fma=True).ms_walk_batch(cfg, 0, q, w)
     g_m, g_c, g_med, nboth = _ms_walk_diff(out_g, out_o)
     f_m, f_c, _, _ = _ms_walk_diff(out_f, out_o)
-    print(f"slab walks: gpu mismatch {g_m:.4f} crossed {g_c:.4f} (floor {f_m:.4f}/{f_c:.4f}) "
+    print(f"slab walks halfvector={halfvector}: gpu mismatch {g_m:.4f} crossed {g_c:.4f} (floor {f_m:.4f}/{f_c:.4f}) "
           f"median|dp| {g_med:.1e} both {nboth}")
     assert nboth > n // 4
     assert np.mean(out_g[8] != out_o[8]) < 0.005          # seed paths

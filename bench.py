@@ -205,9 +205,20 @@ def secondary_configs(torch, sms, W, dev):
         ms = [connect_timed(torch, sms, ctx, kind, q, n, seed=60 + i)[1] for i in range(5)]
         st = ctx.stats()
         t = float(np.mean(ms))
+        its_per_s = st["newton_iterations"] / (5 * t / 1e3)
         out[name] = {"queries": n, "ms_per_call": t, "connections_per_s": n / (t / 1e3),
                      "walks_per_s": st["walks"] / (5 * t / 1e3), "walks_per_connection": walks,
-                     "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"])}
+                     "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),
+                     "newton_iterations_per_s": its_per_s}
+        if kind == "glints":
+            # one iteration gathers a 2x2 FP16 (sx, sy) texel block: 16 B of the
+            # 256 MiB slope map (larger than L2)
+            peak, _ = peaks()
+            gbs = its_per_s * 16 / 1e9
+            out[name]["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                                     "frac": gbs / peak, "bytes_per_iteration": 16}
+        else:
+            out[name]["rays_per_s"] = st["rays"] / (5 * t / 1e3)
         ctx.close()
     return out
 

@@ -357,7 +357,8 @@ struct sms_ctx {
     // learned seed proposal: uv frame of every shape, the bound proposal and
     // its per-query mixture scratch (kGmmParams x gmm_n floats)
     std::vector<mlp::SeedFrame> frames;
-    sms_proposal *prop = nullptr;
+    sms_proposal *prop = nullptr;                 // bound to the SS estimator
+    std::vector<sms_proposal *> proposals;        // every live proposal made on this context
     float defensive = 0.1f;
     float *gmm = nullptr;
     uint32_t gmm_n = 0;
@@ -405,7 +406,7 @@ extern "C" void sms_ctx_destroy(sms_ctx *c) {
     if (c->scratch) cudaFree(c->scratch);
     if (c->ms_tmpl) cudaFree(c->ms_tmpl);
     if (c->gmm) cudaFree(c->gmm);
-    if (c->prop) proposal_detach(c->prop);
+    for (sms_proposal *p : c->proposals) proposal_detach(p);
     if (c->ctr) cudaFree(c->ctr);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -781,8 +782,13 @@ extern "C" sms_status sms_ctx_set_proposal(sms_ctx *c, sms_proposal *p, float de
 }
 
 // Context side of a proposal's lifetime (sms_proposal.cu).
+void ctx_register_proposal(sms_ctx *c, sms_proposal *p) {
+    if (c) c->proposals.push_back(p);
+}
 void ctx_forget_proposal(sms_ctx *c, sms_proposal *p) {
-    if (c && c->prop == p) c->prop = nullptr;
+    if (!c) return;
+    if (c->prop == p) c->prop = nullptr;
+    c->proposals.erase(std::remove(c->proposals.begin(), c->proposals.end(), p), c->proposals.end());
 }
 
 // Device staging buffer of the host-pointer entry points, grown on demand and

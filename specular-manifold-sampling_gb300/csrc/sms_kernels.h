@@ -113,5 +113,7 @@ sms_ctx *proposal_ctx(sms_proposal *p);
 bool proposal_seed_desc(sms_proposal *p, sms::mlp::SeedProposal &out);
 // The context is going away: the proposal keeps working for nothing but destroy.
 void proposal_detach(sms_proposal *p);
-// A proposal is going away: unbind it from its context.
+// A proposal was made on / is going away from a context (which detaches all
+// of its proposals when it is destroyed first).
+void ctx_register_proposal(sms_ctx *c, sms_proposal *p);
 void ctx_forget_proposal(sms_ctx *c, sms_proposal *p);

@@ -195,6 +195,7 @@ extern "C" sms_status sms_proposal_create(sms_ctx *ctx, int32_t caster, uint64_t
         delete p;
         return st;
     }
+    ctx_register_proposal(ctx, p);
     *out = p;
     return SMS_OK;
 }

@@ -59,7 +59,7 @@ typedef struct sms_config {
     int32_t biased;                 /* false */
     int32_t twostage;               /* false */
     int32_t halfvector_constraints; /* false */
-    int32_t mnee_init;              /* false */
+    int32_t mnee_init;              /* false; straight-line seeds (manifold_ss.cpp:229-241) */
     float   step_scale;             /* 1     */
     int32_t max_iterations;         /* 20    */
     float   solver_threshold;       /* 1e-5  */

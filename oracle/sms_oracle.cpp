@@ -147,6 +147,7 @@ struct Shape {
     sms_bsdf bsdf{};
     uint32_t flags = 0;
     int emitter = -1;
+    V3 bbox_center;   /* Shape::bbox().center(), for the MNEE initialisation */
 };
 
 struct Emitter {
@@ -531,6 +532,15 @@ static float bsdf_eta(const sms_bsdf &b) {
     return 1.f;
 }
 
+/* MNEE initialisation target (manifold_ss.cpp:229-241, manifold_ms.cpp:305-316):
+ * complex ior (imag != 0: conductors with k != 0, and the diffuse BSDF whose
+ * ior() is (0, 1)) -> the shape's bounding-box centre, else the light point. */
+static V3 mnee_target(const Shape &s, V3 lp) {
+    const sms_bsdf &b = s.bsdf;
+    bool real_ior = b.type == SMS_BSDF_DIELECTRIC || (b.type == SMS_BSDF_CONDUCTOR && b.k == 0.f);
+    return real_ior ? lp : s.bbox_center;
+}
+
 /* frame.h:197-240 (compute_shading_frame{,_derivative}); bsdf.cpp:17-31 */
 static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v) {
     const Shape &sh = sc.shapes[si.shape];
@@ -794,6 +804,7 @@ static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, cons
     V3 p = sample_position(shape, sample);
     if (p_start.x != 0.f || p_start.y != 0.f || p_start.z != 0.f) p = p_start;
     V3 d_tmp = normalize(p - q.p);
+    if (cfg.mnee_init) d_tmp = normalize(mnee_target(shape, ei.p) - q.p);
     Ray r; r.o = q.p; r.d = d_tmp;
     si_init = ray_intersect(sc, r);
     iters = 0;
@@ -1363,7 +1374,7 @@ static Ray spawn_ray(V3 p, V3 d) {
  * first_path/template shapes, reproject :859-918).  template_shapes empty ->
  * any caster_multi/bouncer shape is allowed (first path). */
 static bool ms_trace_chain(const Scene &sc, int bounces, V3 x0, V3 x1, const std::vector<int> &tmpl,
-                           bool require_chain_flags, std::vector<MVertex> &path) {
+                           bool require_chain_flags, std::vector<MVertex> &path, bool straight = false) {
     path.clear();
     V3 wo = normalize(x1 - x0);
     Ray ray; ray.o = x0; ray.d = wo;
@@ -1377,8 +1388,9 @@ static bool ms_trace_chain(const Scene &sc, int bounces, V3 x0, V3 x1, const std
         vertex_from_si(sc, si, v);
         path.push_back(v);
         V3 wi = -wo;
-        bool ok;
-        if (v.eta == 1.f) ok = reflect(wi, v.n, wo);
+        bool ok = true;
+        if (straight) { /* MNEE seed path: no scattering (manifold_ms.cpp:377-397) */ }
+        else if (v.eta == 1.f) ok = reflect(wi, v.n, wo);
         else ok = refract(wi, v.n, v.eta, wo);
         if (!ok) return false;
         ray = spawn_ray(si.p, wo);
@@ -1435,7 +1447,9 @@ static bool ms_sample_path(const Scene &sc, const sms_config &cfg, int caster, c
     V3 x1 = sample_position(sc.shapes[caster], sample);
     if (p_start.x != 0.f || p_start.y != 0.f || p_start.z != 0.f) x1 = p_start;
     static const std::vector<int> none;
-    if (!ms_trace_chain(sc, cfg.bounces, q.p, x1, first_path ? none : tmpl, true, path)) return false;
+    if (cfg.mnee_init) x1 = mnee_target(sc.shapes[caster], lp);
+    if (!ms_trace_chain(sc, cfg.bounces, q.p, x1, first_path ? none : tmpl, true, path, cfg.mnee_init != 0))
+        return false;
     seed_ok = true;
     if (first_path) {
         tmpl.clear();
@@ -1946,6 +1960,7 @@ int oracle_scene_add_sphere(void *s, const float *c, float r, int flip, const sm
     sh.kind = 0; sh.center = V3(c[0], c[1], c[2]); sh.radius = std::fabs(r);
     sh.flip = (flip != 0) != (r <= 0.f);
     sh.bsdf = *b; sh.flags = flags;
+    sh.bbox_center = sh.center;
     sc->shapes.push_back(sh);
     sc->finalized = false;
     return (int)sc->shapes.size() - 1;
@@ -1961,6 +1976,14 @@ int oracle_scene_add_mesh(void *s, const float *P, const float *N, const float *
     if (N) { sh.N.resize(nv); for (uint32_t i = 0; i < nv; ++i) sh.N[i] = V3(N[3 * i], N[3 * i + 1], N[3 * i + 2]); }
     if (UV) { sh.UV.resize(nv); for (uint32_t i = 0; i < nv; ++i) { sh.UV[i].x = UV[2 * i]; sh.UV[i].y = UV[2 * i + 1]; } }
     sh.F.assign(F, F + 3 * (size_t)nf);
+    {
+        V3 lo(kInf), hi(-kInf);
+        for (const V3 &p : sh.P) {
+            lo = V3(std::min(lo.x, p.x), std::min(lo.y, p.y), std::min(lo.z, p.z));
+            hi = V3(std::max(hi.x, p.x), std::max(hi.y, p.y), std::max(hi.z, p.z));
+        }
+        sh.bbox_center = (lo + hi) * 0.5f;
+    }
     /* mesh.cpp:505-528 + distr_1d.h:60-88: double accumulation, float storage */
     sh.pmf.resize(nf); sh.cdf.resize(nf);
     double sum = 0.0;

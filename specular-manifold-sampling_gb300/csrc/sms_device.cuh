@@ -175,7 +175,14 @@ struct DevShape {
     float area_sum, area_norm;
     uint32_t valid_lo, valid_hi;
     int emitter;
+    float bcx, bcy, bcz;   // bounding-box centre
+    int reflective;        // complex ior: MNEE initialisation aims at the box centre
 };
+
+// Target of the MNEE initialisation (manifold_ss.cpp:229-241,
+// manifold_ms.cpp:305-316): the shape's bounding-box centre for reflecting
+// (complex-ior) BSDFs, the light sample otherwise.
+SMS_HD f3 mnee_target(const DevShape &s, f3 lp) { return s.reflective ? mk(s.bcx, s.bcy, s.bcz) : lp; }
 
 struct DevEmitter {
     int kind;              // 0 point, 1 area on a sphere shape

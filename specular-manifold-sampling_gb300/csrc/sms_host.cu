@@ -385,13 +385,13 @@ static SolverCfg solver_cfg(const sms_config &c) {
     s.solver_threshold = c.solver_threshold;
     s.uniqueness_threshold = c.uniqueness_threshold;
     s.step_scale = c.step_scale;
+    s.mnee_init = c.mnee_init;
     return s;
 }
 
 static sms_status validate_cfg(const sms_config *c) {
     if (!c) return fail(SMS_ERR_INVALID_ARG, "null config");
     if (c->twostage) return fail(SMS_ERR_UNSUPPORTED, "twostage solver is not implemented");
-    if (c->mnee_init) return fail(SMS_ERR_UNSUPPORTED, "mnee_init is not implemented");
     if (c->max_iterations < 0) return fail(SMS_ERR_INVALID_ARG, "max_iterations must be >= 0");
     return SMS_OK;
 }
@@ -462,6 +462,17 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
                         (h.bsdf.type == SMS_BSDF_CONDUCTOR && h.bsdf.k == 0.f);
         ds.spec_eta = real_ior ? h.bsdf.eta : 1.f;
         ds.emitter = h.emitter;
+        // MNEE initialisation target (manifold_ss.cpp:229-241): the bounding-box
+        // centre for a complex-ior (reflecting) BSDF, else the light sample
+        ds.reflective = real_ior ? 0 : 1;
+        if (h.kind == kShapeSphere) {
+            ds.bcx = h.center[0]; ds.bcy = h.center[1]; ds.bcz = h.center[2];
+        } else {
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (size_t k = 0; k + 2 < h.P.size(); k += 3)
+                for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], h.P[k + a]); hi[a] = std::max(hi[a], h.P[k + a]); }
+            ds.bcx = 0.5f * (lo[0] + hi[0]); ds.bcy = 0.5f * (lo[1] + hi[1]); ds.bcz = 0.5f * (lo[2] + hi[2]);
+        }
         c->frames.push_back(seed_frame(h));
         if (h.kind == kShapeSphere) {
             ds.cx = h.center[0]; ds.cy = h.center[1]; ds.cz = h.center[2];

@@ -26,6 +26,7 @@ struct SolverCfg {
     float solver_threshold;
     float uniqueness_threshold;
     float step_scale;
+    int mnee_init;      // seed along the straight path (manifold_ss.cpp:229-241)
 };
 
 // Unique-solution capacity per query of the biased estimator (shared memory

@@ -55,10 +55,11 @@ SMS_D bool chain_shape(const DevScene &sc, int s) {
 
 // Trace a specular chain from x0 toward x1, reflecting or refracting at each
 // hit (sample_seed_path :327-397, reproject :865-917).  tmpl (K shape ids) or
-// null; check_flags restricts hits to caster_multi / bouncer shapes.
+// null; check_flags restricts hits to caster_multi / bouncer shapes; straight
+// keeps the direction at every hit (the MNEE seed path, :378-397).
 template <int K>
 SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool check_flags, Chain<K> &c,
-                       int *shapes, uint32_t &err, LaneStats &st) {
+                       int *shapes, uint32_t &err, LaneStats &st, bool straight = false) {
     f3 wo = normalize(x1 - x0);
     f3 o = x0;
     float mint = kRayEps;
@@ -73,7 +74,9 @@ SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool c
         vertex_from_hit(sc, o, wo, h, c.v[b]);
         if (shapes) shapes[b] = h.shape;
         f3 wi = -wo;
-        if (c.v[b].eta == 1.f) {
+        if (straight) {
+            // no scattering: the chain continues along the straight line
+        } else if (c.v[b].eta == 1.f) {
             wo = c.v[b].n * (2.f * dot(wi, c.v[b].n)) - wi;
         } else if (!refract(wi, c.v[b].n, c.v[b].eta, wo)) {
             return false;
@@ -82,6 +85,17 @@ SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool c
         mint = (1.f + fmaxf(fabsf(o.x), fmaxf(fabsf(o.y), fabsf(o.z)))) * kRayEps;
     }
     return true;
+}
+
+// The seed path of a walk (sample_seed_path :280-408): toward the sampled
+// point x1, or with cfg.mnee_init along the straight line toward the MNEE
+// target without scattering.
+template <int K>
+SMS_D bool seed_chain(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x0, f3 x1, f3 lp, const int *tmpl,
+                      Chain<K> &c, int *shapes, uint32_t &err, LaneStats &st) {
+    if (cfg.mnee_init)
+        return trace_chain<K>(sc, x0, mnee_target(sc.shapes[caster], lp), tmpl, true, c, shapes, err, st, true);
+    return trace_chain<K>(sc, x0, x1, tmpl, true, c, shapes, err, st);
 }
 
 // Angle-difference constraint of vertex i and its blocks w.r.t. the previous,
@@ -442,7 +456,7 @@ __global__ void __launch_bounds__(128) ms_walk_kernel(DevScene sc, SolverCfg cfg
         Chain<K> c;
         int shapes[K];
         int it = 0;
-        bool seed_ok = trace_chain<K>(sc, x, x1, nullptr, true, c, shapes, err, st);
+        bool seed_ok = seed_chain<K>(sc, cfg, caster, x, x1, lp, nullptr, c, shapes, err, st);
         bool ok = seed_ok && chain_newton<K>(sc, cfg, x, lp, shapes, c, it, err, st);
         float res[kMsWalkOutFields] = {ok ? 1.f : 0.f, (float)it, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, seed_ok ? 1.f : 0.f};
         if (ok) {
@@ -512,7 +526,7 @@ __global__ void __launch_bounds__(128, 4) ms_biased_kernel(DevScene sc, SolverCf
                     Pcg32 rng = query_rng(seed, stream_off + qi, 3u + 2u * ((uint64_t)ci * M + m));
                     float sx = rng.next_f32(), sy = rng.next_f32();
                     f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
-                    seed_ok = trace_chain<K>(sc, Q.x, x1, nullptr, true, c, shapes, err, st);
+                    seed_ok = seed_chain<K>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st);
                 }
                 // the first completed seed path of the estimate is the template
                 unsigned sb = __ballot_sync(kFull, seed_ok) & gmask;
@@ -631,7 +645,7 @@ __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cf
             Chain<K> c;
             int shapes[K];
             int it = 0;
-            bool ok = trace_chain<K>(sc, Q.x, x1, nullptr, true, c, shapes, err, st) &&
+            bool ok = seed_chain<K>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st) &&
                       chain_newton<K>(sc, cfg, Q.x, L.p, shapes, c, it, err, st);
             st.walks++;
             st.newton += (unsigned)it;
@@ -708,7 +722,7 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
                 float sx = rng.next_f32(), sy = rng.next_f32();
                 f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
                 Chain<K> c;
-                bool ok = trace_chain<K>(sc, Q.x, x1, tmpl, true, c, nullptr, err, st) &&
+                bool ok = seed_chain<K>(sc, cfg, caster, Q.x, x1, L.p, tmpl, c, nullptr, err, st) &&
                           chain_newton<K>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st);
                 succ = ok && fabsf(dot(dir0, normalize(c.v[0].p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
             }

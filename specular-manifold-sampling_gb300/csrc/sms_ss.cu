@@ -40,7 +40,7 @@ namespace sms {
 // explicit seed point.  Returns ok; v holds the solution vertex.
 SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
                    uint32_t &err, LaneStats &st, f3 *p_init = nullptr) {
-    f3 d = normalize(seed - x);
+    f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
     Hit h;
     trace(sc, x, d, kRayEps, INFINITY, false, h, err);
     st.ray(h);

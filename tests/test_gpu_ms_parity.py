@@ -98,3 +98,26 @@ def test_ms_bounce_validation(sms, workloads, gpu_lib):
     with pytest.raises(sms.SMSError) as e:
         ms.specular_manifold_sampling(W.slab_queries(4))
     assert e.value.status == 4
+
+
+def test_slab_mnee_init_walks(sms, workloads, oracle, gpu_lib):
+    """MNEE seed paths through the slab (manifold_ms.cpp:305-316, 377-397):
+    straight line toward the light, no scattering at the seed vertices."""
+    W = workloads
+    desc = W.slab_scene(res=128)
+    cfg = sms.SMSConfig(bounces=2, max_iterations=30, mnee_init=True)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    n = 4096
+    q = W.slab_queries(n)
+    u = W.pcg32_streams_f32(12, np.arange(n, dtype=np.uint64), 2)
+    w = np.zeros((8, n), np.float32)
+    w[2] = 5.0
+    w[6], w[7] = u[0], u[1]
+    out_g = sms.SpecularManifoldMultiScatter(ctx).sample_path(0, q, w)
+    out_o = oracle.OracleScene(desc).ms_walk_batch(cfg, 0, q, w)
+    out_f = oracle.OracleScene(desc, fma=True).ms_walk_batch(cfg, 0, q, w)
+    g_m, g_c, g_med, nboth = _ms_walk_diff(out_g, out_o)
+    f_m, f_c, _, _ = _ms_walk_diff(out_f, out_o)
+    print(f"slab mnee walks: gpu mismatch {g_m:.4f} (floor {f_m:.4f}) both {nboth}")
+    assert nboth > n // 4
+    assert g_m <= FLOOR_FACTOR * f_m + FLOOR_SLACK and g_c <= FLOOR_FACTOR * f_c + FLOOR_SLACK

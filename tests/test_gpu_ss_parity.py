@@ -225,3 +225,30 @@ def test_bad_arguments(sms, workloads, gpu_lib):
         ctx.set_config(sms.SMSConfig(twostage=True))
     with pytest.raises(ValueError):
         ss.specular_manifold_sampling(np.zeros((15, 4), np.float32))
+
+
+@pytest.mark.parametrize("conductor", [False, True])
+def test_mnee_init_walks_and_connect(sms, workloads, oracle, gpu_lib, conductor):
+    """mnee_init: deterministic straight-line seeds, GPU vs oracle per walk and
+    for the biased estimator (every walk of a query finds the same solution,
+    so at most one unique solution)."""
+    W = workloads
+    desc = W.sphere_scene(conductor=conductor)
+    cfg = sms.SMSConfig(mnee_init=True)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    q = W.sphere_queries(64)
+    w = _walk_inputs(W, q.shape[1], (0.0, 0.0, 5.0))
+    out_g = ss.sample_path(0, q, w)
+    out_o = oracle.OracleScene(desc).walk_batch(cfg, 0, q, w)
+    mism, crossed, med, nboth = _walk_diff(out_g, out_o)
+    print(f"mnee conductor={conductor}: mismatch {mism:.5f} both {nboth}")
+    assert mism < STRICT_MISMATCH and crossed < STRICT_MISMATCH
+    if not conductor:
+        assert nboth > 20
+    bcfg = sms.SMSConfig(mnee_init=True, biased=True, max_trials=8)
+    ctx.set_config(bcfg)
+    vg, cg, wg = ss.specular_manifold_sampling(q, seed=2)
+    vo, co, wo, _ = oracle.OracleScene(desc).connect_batch(bcfg, q, seed=2)
+    assert np.all(cg <= 1) and np.mean(cg == co) > 1 - STRICT_MISMATCH
+    ctx.close()

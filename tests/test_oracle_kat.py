@@ -369,3 +369,26 @@ def test_newton_jacobian_on_a_curved_shading_mesh(sms, oracle, halfvector, condu
         assert np.abs(J - fd).max() < 2e-2 * scale, (u, v, x.tolist(), J, fd)
         checked += 1
     assert checked >= 20
+
+
+@pytest.mark.parametrize("conductor", [False, True])
+def test_mnee_init_ignores_the_random_seed(sms, workloads, oracle, conductor):
+    """mnee_init (manifold_ss.cpp:229-241) replaces the sampled seed direction
+    by the straight line to the light (real ior) or to the shape's bounding-box
+    centre (complex ior): every walk of a query is the same walk."""
+    W = workloads
+    osc = oracle.OracleScene(W.sphere_scene(conductor=conductor))
+    cfg = sms.SMSConfig(mnee_init=True)
+    q = W.sphere_queries(16)
+    n = q.shape[1]
+    outs = []
+    for seed in (3, 4):
+        u = W.pcg32_streams_f32(seed, np.arange(n, dtype=np.uint64), 2)
+        w = np.zeros((8, n), np.float32)
+        w[2] = 5.0
+        w[6], w[7] = u[0], u[1]
+        outs.append(osc.walk_batch(cfg, 0, q, w))
+    np.testing.assert_array_equal(outs[0], outs[1])
+    if not conductor:
+        # refraction: the straight line toward the light starts next to the solution
+        assert outs[0][0].sum() > 10

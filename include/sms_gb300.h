@@ -126,6 +126,25 @@ sms_status sms_scene_add_mesh(sms_scene *scene, const float *positions,
                               uint32_t n_faces, const sms_bsdf *bsdf,
                               uint32_t flags, int32_t *shape_id_out);
 
+/* Wavefront OBJ reader (src/shapes/obj.cpp:90-330): one output vertex per
+ * distinct (v, vt, vn) reference in order of first use, polygons
+ * fan-triangulated, texture v flipped unless flip_tex_coords is 0, vertex
+ * normals recomputed (angle-weighted, src/librender/mesh.cpp:420-470) when the
+ * file has none, no vertex normals with face_normals.  Arrays are allocated
+ * by the library (normals / texcoords NULL when absent); release them with
+ * sms_mesh_data_free.  Feed them to sms_scene_add_mesh.  Errors:
+ * SMS_ERR_PARSE with the line in sms_last_error(). */
+typedef struct sms_mesh_data {
+    uint32_t n_vertices, n_faces;
+    float *positions;   /* 3 x n_vertices */
+    float *normals;     /* 3 x n_vertices or NULL */
+    float *texcoords;   /* 2 x n_vertices or NULL */
+    uint32_t *faces;    /* 3 x n_faces */
+} sms_mesh_data;
+sms_status sms_obj_load(const char *path, int32_t face_normals, int32_t flip_tex_coords,
+                        sms_mesh_data *out);
+void sms_mesh_data_free(sms_mesh_data *mesh);
+
 /* Point light (src/emitters/point.cpp). */
 sms_status sms_scene_add_point_emitter(sms_scene *scene, const float position[3],
                                        const float intensity[3], uint32_t flags);

@@ -78,6 +78,12 @@ class _Result(C.Structure):
     _fields_ = [("value", C.c_void_p), ("count", C.c_void_p), ("walks", C.c_void_p)]
 
 
+class _MeshData(C.Structure):
+    _fields_ = [("n_vertices", C.c_uint32), ("n_faces", C.c_uint32), ("positions", C.POINTER(C.c_float)),
+                ("normals", C.POINTER(C.c_float)), ("texcoords", C.POINTER(C.c_float)),
+                ("faces", C.POINTER(C.c_uint32))]
+
+
 class _Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "solver_succeeded", "solver_failed", "bernoulli_trial_calls",
@@ -152,6 +158,8 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_proposal_eval": (i32, [vp, vp, u32, i32, vp]),
         "sms_ctx_set_proposal": (i32, [vp, vp, f32]),
         "sms_proposal_frame": (i32, [vp, vp]),
+        "sms_obj_load": (i32, [C.c_char_p, i32, i32, C.POINTER(_MeshData)]),
+        "sms_mesh_data_free": (None, [C.POINTER(_MeshData)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -266,11 +274,34 @@ class SceneDesc:
         self.order.append(("mesh", len(self.meshes) - 1))
         return len(self.order) - 1
 
+    def add_obj(self, path, bsdf: Bsdf, flags: int = 0, face_normals: bool = False,
+                flip_tex_coords: bool = True) -> int:
+        """Add a Wavefront OBJ mesh (the reference's obj shape plugin)."""
+        P, F, N, UV = load_obj(path, face_normals, flip_tex_coords)
+        return self.add_mesh(P, F, bsdf, flags, N=N, UV=UV)
+
     def add_point_emitter(self, pos, intensity, flags: int = EMITTER_CAUSTIC_SINGLE):
         self.point_emitters.append((tuple(pos), tuple(intensity), flags))
 
     def add_area_emitter(self, shape_id: int, radiance, flags: int = EMITTER_CAUSTIC_SINGLE):
         self.area_emitters.append((shape_id, tuple(radiance), flags))
+
+
+def load_obj(path, face_normals: bool = False, flip_tex_coords: bool = True):
+    """(positions (nv, 3), faces (nf, 3), normals (nv, 3) or None, texcoords
+    (nv, 2) or None) of a Wavefront OBJ file, read by the library."""
+    lib = load_library()
+    m = _MeshData()
+    _check(lib.sms_obj_load(str(path).encode(), int(face_normals), int(flip_tex_coords), C.byref(m)))
+    try:
+        nv, nf = m.n_vertices, m.n_faces
+        P = np.ctypeslib.as_array(m.positions, shape=(nv, 3)).copy()
+        F = np.ctypeslib.as_array(m.faces, shape=(nf, 3)).copy()
+        N = np.ctypeslib.as_array(m.normals, shape=(nv, 3)).copy() if m.normals else None
+        UV = np.ctypeslib.as_array(m.texcoords, shape=(nv, 2)).copy() if m.texcoords else None
+    finally:
+        lib.sms_mesh_data_free(C.byref(m))
+    return P, F, N, UV
 
 
 class Scene:

@@ -287,6 +287,14 @@ class SceneDesc:
         self.area_emitters.append((shape_id, tuple(radiance), flags))
 
 
+def load_scene(path):
+    """(SceneDesc, SMSConfig or None, integrator type or None) from a scene XML
+    file in the reference's format (the subset described in scene_xml.py)."""
+    import sys
+    from .scene_xml import load_scene_xml
+    return load_scene_xml(sys.modules[__name__], path)
+
+
 def load_obj(path, face_normals: bool = False, flip_tex_coords: bool = True):
     """(positions (nv, 3), faces (nf, 3), normals (nv, 3) or None, texcoords
     (nv, 2) or None) of a Wavefront OBJ file, read by the library."""

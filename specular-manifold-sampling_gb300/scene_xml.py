@@ -1,0 +1,225 @@
+"""Scene loader for the subset of the reference's XML scene format the SMS path
+needs (Mitsuba 2 scene files, as the paper's scenes are written).
+
+Recognised elements (everything else raises ValueError, so a scene is never
+silently half-loaded):
+
+  <shape type="sphere">   center (point), radius (float), flip_normals
+  <shape type="obj">      filename (relative to the XML file), face_normals,
+                          flip_tex_coords (src/shapes/obj.cpp:90-110)
+  <shape type="rectangle"> the two triangles of [-1,1]^2 at z = 0 with uv
+                          (src/shapes/rectangle.cpp)
+      shape flags: caustic_caster_single, caustic_caster_multi,
+      caustic_bouncer, caustic_receiver, glinty (src/librender/shape.cpp:78-82);
+      <transform name="to_world"> with translate / scale / matrix children
+      (spheres: translate and uniform scale only);
+      nested <bsdf>: dielectric (int_ior / ext_ior, names from
+      include/mitsuba/render/ior.h), conductor (eta, k), diffuse (reflectance);
+      no bsdf -> diffuse (shape.cpp:73-74);
+      nested <emitter type="area"> with radiance (spheres only)
+  <emitter type="point">  position (point), intensity (spectrum / rgb / float)
+      emitter flags: caustic_emitter_single, caustic_emitter_multi
+      (src/librender/emitter.cpp:9-10)
+  <integrator type="path_sms_*"> -> SMSConfig (sms_config_parse_xml)
+  <sensor>, <film>, <sampler> are accepted and ignored (not on this path).
+
+Returns (SceneDesc, SMSConfig or None, integrator type or None).
+"""
+from __future__ import annotations
+
+import math
+import xml.etree.ElementTree as ET
+from pathlib import Path
+
+import numpy as np
+
+# include/mitsuba/render/ior.h:22-49
+IOR = {"vacuum": 1.0, "helium": 1.000036, "hydrogen": 1.000132, "air": 1.000277, "carbon dioxide": 1.00045,
+       "water": 1.3330, "acetone": 1.36, "ethanol": 1.361, "carbon tetrachloride": 1.461, "glycerol": 1.4729,
+       "benzene": 1.501, "silicone oil": 1.52045, "bromine": 1.661, "water ice": 1.31, "fused quartz": 1.458,
+       "pyrex": 1.470, "acrylic glass": 1.49, "polypropylene": 1.49, "bk7": 1.5046, "sodium chloride": 1.544,
+       "amber": 1.55, "pet": 1.5750, "diamond": 2.419}
+
+_IGNORED = {"sensor", "film", "sampler", "default"}
+
+
+def _props(el):
+    """name -> (tag, element) of the direct property children."""
+    return {c.get("name"): (c.tag, c) for c in el if c.get("name") is not None}
+
+
+def _bool(p, name, default=False):
+    if name not in p:
+        return default
+    return p[name][1].get("value", "false").strip().lower() == "true"
+
+
+def _float(p, name, default):
+    if name not in p:
+        return default
+    tag, el = p[name]
+    v = el.get("value")
+    if tag == "string":
+        if v.lower() not in IOR:
+            raise ValueError(f"unknown index of refraction name '{v}'")
+        return IOR[v.lower()]
+    return float(v)
+
+
+def _spectrum(p, name, default):
+    """rgb / spectrum / float -> 3 floats (a single value is grey)."""
+    if name not in p:
+        return default
+    tag, el = p[name]
+    v = el.get("value")
+    if tag in ("float", "spectrum") and v is not None and "," not in v and len(v.split()) == 1:
+        x = float(v)
+        return (x, x, x)
+    vals = [float(x) for x in v.replace(",", " ").split()]
+    if len(vals) != 3:
+        raise ValueError(f"'{name}': expected 1 or 3 values")
+    return tuple(vals)
+
+
+def _point(p, name, default):
+    if name not in p:
+        return default
+    el = p[name][1]
+    if el.get("value") is not None:
+        return tuple(float(x) for x in el.get("value").replace(",", " ").split())
+    return (float(el.get("x", 0)), float(el.get("y", 0)), float(el.get("z", 0)))
+
+
+def _transform(el):
+    """4x4 matrix of a <transform> element (translate, scale, matrix)."""
+    M = np.eye(4)
+    for c in el:
+        if c.tag == "translate":
+            T = np.eye(4)
+            if c.get("value"):
+                T[:3, 3] = [float(x) for x in c.get("value").replace(",", " ").split()]
+            else:
+                T[:3, 3] = [float(c.get(k, 0)) for k in "xyz"]
+            M = T @ M
+        elif c.tag == "scale":
+            S = np.eye(4)
+            if c.get("value") and len(c.get("value").replace(",", " ").split()) == 1:
+                S[:3, :3] *= float(c.get("value"))
+            elif c.get("value"):
+                S[np.arange(3), np.arange(3)] = [float(x) for x in c.get("value").replace(",", " ").split()]
+            else:
+                S[np.arange(3), np.arange(3)] = [float(c.get(k, 1)) for k in "xyz"]
+            M = S @ M
+        elif c.tag == "matrix":
+            A = np.array([float(x) for x in c.get("value").replace(",", " ").split()]).reshape(4, 4)
+            M = A @ M
+        else:
+            raise ValueError(f"unsupported transform operation <{c.tag}>")
+    return M
+
+
+def _bsdf(sms, el):
+    if el is None:
+        return sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5, 0.5, 0.5))
+    t = el.get("type")
+    p = _props(el)
+    if t == "twosided":
+        inner = [c for c in el if c.tag == "bsdf"]
+        return _bsdf(sms, inner[0] if inner else None)
+    if t == "dielectric":
+        # dielectric.cpp:177-186: eta = int_ior / ext_ior, defaults bk7 / air
+        return sms.Bsdf(sms.BSDF_DIELECTRIC, _float(p, "int_ior", 1.5046) / _float(p, "ext_ior", 1.000277))
+    if t == "conductor":
+        eta, k = _spectrum(p, "eta", (0.0,) * 3), _spectrum(p, "k", (1.0,) * 3)
+        return sms.Bsdf(sms.BSDF_CONDUCTOR, float(np.mean(eta)), float(np.mean(k)))
+    if t == "diffuse":
+        return sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, _spectrum(p, "reflectance", (0.5,) * 3))
+    raise ValueError(f"unsupported bsdf type '{t}'")
+
+
+def _flags(sms, p):
+    f = 0
+    for name, bit in (("caustic_receiver", sms.SHAPE_CAUSTIC_RECEIVER),
+                      ("caustic_caster_single", sms.SHAPE_CAUSTIC_CASTER_SINGLE),
+                      ("caustic_caster_multi", sms.SHAPE_CAUSTIC_CASTER_MULTI),
+                      ("caustic_bouncer", sms.SHAPE_CAUSTIC_BOUNCER), ("glinty", sms.SHAPE_GLINTY)):
+        if _bool(p, name):
+            f |= bit
+    return f
+
+
+def _emitter_flags(sms, p):
+    f = 0
+    if _bool(p, "caustic_emitter_single"):
+        f |= sms.EMITTER_CAUSTIC_SINGLE
+    if _bool(p, "caustic_emitter_multi"):
+        f |= sms.EMITTER_CAUSTIC_MULTI
+    return f
+
+
+def load_scene_xml(sms, path):
+    path = Path(path)
+    root = ET.parse(path).getroot()
+    if root.tag != "scene":
+        raise ValueError("not a <scene> document")
+    desc = sms.SceneDesc()
+    config, itype = None, None
+    for el in root:
+        if el.tag in _IGNORED:
+            continue
+        if el.tag == "integrator":
+            config, itype = sms.SMSConfig.from_xml(ET.tostring(el, encoding="unicode"))
+            continue
+        if el.tag == "bsdf":
+            raise ValueError("top-level <bsdf> references are not supported; nest the bsdf in its shape")
+        p = _props(el)
+        if el.tag == "emitter":
+            if el.get("type") != "point":
+                raise ValueError(f"unsupported top-level emitter type '{el.get('type')}'")
+            desc.add_point_emitter(_point(p, "position", (0.0, 0.0, 0.0)), _spectrum(p, "intensity", (1.0,) * 3),
+                                   _emitter_flags(sms, p))
+            continue
+        if el.tag != "shape":
+            raise ValueError(f"unsupported element <{el.tag}>")
+        t = el.get("type")
+        bsdf_el = next((c for c in el if c.tag == "bsdf"), None)
+        tr_el = next((c for c in el if c.tag == "transform" and c.get("name") == "to_world"), None)
+        M = _transform(tr_el) if tr_el is not None else np.eye(4)
+        flags = _flags(sms, p)
+        b = _bsdf(sms, bsdf_el)
+        if t == "sphere":
+            c = np.array(_point(p, "center", (0.0, 0.0, 0.0)), np.float64)
+            r = _float(p, "radius", 1.0)
+            A = M[:3, :3]
+            s = np.cbrt(abs(np.linalg.det(A)))
+            if not np.allclose(A, s * np.eye(3), atol=1e-6 * max(1.0, s)):
+                raise ValueError("sphere to_world must be a translation and a uniform scale")
+            centre = A @ c + M[:3, 3]
+            sid = desc.add_sphere(tuple(centre), r * s, b, flags, flip=_bool(p, "flip_normals"))
+        elif t in ("obj", "rectangle"):
+            if t == "obj":
+                P, F, N, UV = sms.load_obj(path.parent / p["filename"][1].get("value"),
+                                           _bool(p, "face_normals"), _bool(p, "flip_tex_coords", True))
+            else:
+                P = np.array([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], np.float32)
+                F = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+                UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+                N = None
+            Ph = np.concatenate([P.astype(np.float64), np.ones((P.shape[0], 1))], axis=1) @ M.T
+            P = Ph[:, :3].astype(np.float32)
+            if N is not None:
+                Nw = N.astype(np.float64) @ np.linalg.inv(M[:3, :3])
+                N = (Nw / np.linalg.norm(Nw, axis=1, keepdims=True)).astype(np.float32)
+            if _bool(p, "flip_normals") and N is not None:
+                N = -N
+            sid = desc.add_mesh(P, F, b, flags, N=N, UV=UV)
+        else:
+            raise ValueError(f"unsupported shape type '{t}'")
+        for em in (c for c in el if c.tag == "emitter"):
+            if em.get("type") != "area":
+                raise ValueError("only area emitters may be nested in a shape")
+            if t != "sphere":
+                raise ValueError("area emitters are supported on spheres only")
+            ep = _props(em)
+            desc.add_area_emitter(sid, _spectrum(ep, "radiance", (1.0,) * 3), _emitter_flags(sms, ep))
+    return desc, config, itype

@@ -1,0 +1,111 @@
+"""Scene XML loading (the reference's scene format, subset in scene_xml.py):
+a file describing the benchmark sphere scene must give the same scene as the
+built-in description -- checked through the CPU oracle, bit for bit -- and
+unsupported content must be refused, never dropped."""
+import numpy as np
+import pytest
+
+SPHERE_XML = """<scene version="2.0.0">
+  <integrator type="path_sms_ss">
+    <boolean name="biased" value="true"/>
+    <integer name="max_trials" value="16"/>
+    <integer name="max_iterations" value="20"/>
+    <float name="solver_threshold" value="1e-5"/>
+  </integrator>
+  <sensor type="perspective"><float name="fov" value="30"/></sensor>
+  <shape type="sphere">
+    <point name="center" x="0" y="0" z="0"/>
+    <float name="radius" value="0.5"/>
+    <transform name="to_world">
+      <scale value="2"/>
+      <translate x="0" y="0" z="1.5"/>
+    </transform>
+    <bsdf type="conductor">
+      <float name="eta" value="0.2"/>
+      <float name="k" value="3"/>
+    </bsdf>
+    <boolean name="caustic_caster_single" value="true"/>
+  </shape>
+  <shape type="sphere">
+    <point name="center" x="5" y="5" z="-3"/>
+    <float name="radius" value="0.5"/>
+    <bsdf type="dielectric">
+      <float name="int_ior" value="1.5"/>
+      <string name="ext_ior" value="vacuum"/>
+    </bsdf>
+  </shape>
+  <shape type="rectangle">
+    <transform name="to_world"><scale value="4"/></transform>
+    <bsdf type="diffuse"><rgb name="reflectance" value="0.5, 0.5, 0.5"/></bsdf>
+    <boolean name="caustic_receiver" value="true"/>
+  </shape>
+  <emitter type="point">
+    <point name="position" value="0, 0, 5"/>
+    <spectrum name="intensity" value="100"/>
+    <boolean name="caustic_emitter_single" value="true"/>
+  </emitter>
+</scene>
+"""
+
+
+def test_sphere_scene_from_xml_matches_builtin(sms, workloads, oracle, tmp_path):
+    path = tmp_path / "sphere.xml"
+    path.write_text(SPHERE_XML)
+    desc, cfg, kind = sms.load_scene(path)
+    assert kind == "path_sms_ss" and cfg.biased and cfg.max_trials == 16
+    c, r, flip, b, flags = desc.spheres[0]
+    np.testing.assert_allclose(c, (0, 0, 1.5))
+    assert r == pytest.approx(1.0) and b.type == sms.BSDF_CONDUCTOR and b.k == pytest.approx(3.0)
+    assert flags == sms.SHAPE_CAUSTIC_CASTER_SINGLE
+    b2 = desc.spheres[1][3]
+    assert b2.type == sms.BSDF_DIELECTRIC and b2.eta == pytest.approx(1.5) and desc.spheres[1][4] == 0
+    P = desc.meshes[0][0]
+    np.testing.assert_allclose(np.abs(P[:, :2]), 4.0)
+    q = workloads.sphere_queries(16)
+    ref = oracle.OracleScene(workloads.sphere_scene(conductor=True)).connect_batch(workloads.sphere_config(), q,
+                                                                                  seed=3)
+    got = oracle.OracleScene(desc).connect_batch(cfg, q, seed=3)
+    for a, b_ in zip(ref[:3], got[:3]):
+        np.testing.assert_array_equal(a, b_)
+    assert (ref[1] > 0).sum() > 10
+
+
+def test_obj_shape_and_area_emitter(sms, tmp_path):
+    (tmp_path / "quad.obj").write_text("v -1 -1 0\nv 1 -1 0\nv 1 1 0\nv -1 1 0\nf 1 2 3 4\n")
+    (tmp_path / "s.xml").write_text("""<scene version="2.0.0">
+  <shape type="obj">
+    <string name="filename" value="quad.obj"/>
+    <transform name="to_world"><translate x="0" y="0" z="1"/></transform>
+    <bsdf type="conductor"><rgb name="eta" value="0.2, 0.2, 0.2"/><rgb name="k" value="3, 3, 3"/></bsdf>
+    <boolean name="caustic_caster_single" value="true"/>
+  </shape>
+  <shape type="sphere">
+    <point name="center" x="0" y="0" z="10"/><float name="radius" value="0.1"/>
+    <emitter type="area">
+      <rgb name="radiance" value="1000, 1000, 1000"/>
+      <boolean name="caustic_emitter_single" value="true"/>
+    </emitter>
+  </shape>
+</scene>""")
+    desc, cfg, kind = sms.load_scene(tmp_path / "s.xml")
+    assert cfg is None and kind is None
+    P, N, UV, F, b, flags = desc.meshes[0]
+    np.testing.assert_allclose(P[:, 2], 1.0)
+    assert b.type == sms.BSDF_CONDUCTOR and b.k == pytest.approx(3.0)
+    assert np.allclose(N[:, 2], 1.0)              # recomputed normals of the quad
+    assert len(desc.area_emitters) == 1 and desc.area_emitters[0][0] == 1
+
+
+@pytest.mark.parametrize("body,what", [
+    ('<shape type="cylinder"/>', "cylinder"),
+    ('<shape type="sphere"><bsdf type="roughconductor"/></shape>', "roughconductor"),
+    ('<emitter type="envmap"/>', "envmap"),
+    ('<shape type="sphere"><transform name="to_world"><rotate x="1" angle="3"/></transform></shape>', "rotate"),
+    ('<shape type="sphere"><bsdf type="dielectric"><string name="int_ior" value="unobtainium"/></bsdf></shape>',
+     "unobtainium"),
+])
+def test_unsupported_content_is_refused(sms, tmp_path, body, what):
+    (tmp_path / "bad.xml").write_text(f'<scene version="2.0.0">{body}</scene>')
+    with pytest.raises(ValueError) as e:
+        sms.load_scene(tmp_path / "bad.xml")
+    assert what in str(e.value)

@@ -453,6 +453,71 @@ sms_status sms_proposal_frame(sms_proposal *p, float frame[10]);
  * allocation-free entry point return SMS_ERR_UNSUPPORTED. */
 sms_status sms_ctx_set_proposal(sms_ctx *ctx, sms_proposal *p, float defensive);
 
+/* ------------------------------------------------------------- rendering */
+/* Wavefront path tracer around the SMS solvers, the reference's sampling
+ * integrators for this path:
+ *   path          src/integrators/path.cpp:94-226
+ *   path_sms_ss   src/integrators/path_sms_ss.cpp:69-251
+ *   path_sms_ms   src/integrators/path_sms_ms.cpp:172-330
+ * with the MonteCarloIntegrator parameters (src/librender/integrator.cpp:
+ * 300-320), a perspective sensor (src/sensors/perspective.cpp) and a box
+ * reconstruction filter (one pixel per sample, src/rfilters/box.cpp), for
+ * scenes of diffuse, smooth dielectric and smooth conductor BSDFs, point
+ * lights and sphere area lights.  Shading points on caustic receivers are
+ * solved as one SMS batch per bounce by the context's estimator and config.
+ *
+ * Random numbers: path p = s * width * height + y * width + x (sample s of
+ * pixel (x, y)) draws from PCG32 stream p (state seed `seed`) in the
+ * reference's per-sample order: pixel position (2), wavelength (1), then per
+ * bounce Russian roulette (1, past rr_depth), emitter sampling (2, when it
+ * runs) and BSDF sampling (1 + 2).  The SMS call at bounce `depth` of path p
+ * draws from stream p of state seed sms_render_sms_seed(seed, depth).  Images
+ * therefore do not depend on the wavefront size. */
+typedef struct sms_camera {
+    float   to_world[16];   /* row-major camera-to-world; camera space has x
+                               left, y up, z forward (the reference's look_at) */
+    float   fov;            /* field of view in degrees along fov_axis       */
+    int32_t fov_axis;       /* SMS_FOV_*                                     */
+    int32_t width, height;  /* film size in pixels                           */
+    float   near_clip;      /* 1e-2 */
+    float   far_clip;       /* 1e4  */
+} sms_camera;
+#define SMS_FOV_X        0
+#define SMS_FOV_Y        1
+#define SMS_FOV_DIAGONAL 2
+#define SMS_FOV_SMALLER  3
+#define SMS_FOV_LARGER   4
+
+#define SMS_INTEGRATOR_PATH        0
+#define SMS_INTEGRATOR_PATH_SMS_SS 1
+#define SMS_INTEGRATOR_PATH_SMS_MS 2
+typedef struct sms_render_options {
+    int32_t  integrator;                 /* SMS_INTEGRATOR_*                        */
+    int32_t  max_depth;                  /* -1 = unbounded                          */
+    int32_t  rr_depth;                   /* 5                                       */
+    int32_t  spp;                        /* samples per pixel (1)                   */
+    int32_t  disable_reflected_emitters; /* path_sms_ss (false)                     */
+    int32_t  biased_mnee;                /* path_sms_ss (false)                     */
+    uint64_t seed;                       /* 0                                       */
+    uint32_t max_paths;                  /* paths per wavefront, 0 = 1,048,576      */
+} sms_render_options;
+void sms_render_options_default(sms_render_options *opt);
+
+/* State seed of the SMS streams at bounce `depth` (SplitMix64 of the seed
+ * and the depth). */
+uint64_t sms_render_sms_seed(uint64_t seed, int32_t depth);
+
+/* Render: image receives height x width RGB (row-major, y down, 3 floats per
+ * pixel) = the mean of spp samples.  sms_render takes a host pointer and
+ * returns when the image is there; sms_render_device takes a device pointer
+ * and is asynchronous on the context stream apart from one small
+ * device-to-host read per bounce (the number of SMS queries).
+ * path_sms_ms with mnee_init and without biased_mnee returns
+ * SMS_ERR_UNSUPPORTED (its MNEE bookkeeping is not implemented). */
+sms_status sms_render(sms_ctx *ctx, const sms_camera *cam, const sms_render_options *opt, float *image);
+sms_status sms_render_device(sms_ctx *ctx, const sms_camera *cam, const sms_render_options *opt,
+                             float *image_dev);
+
 #ifdef __cplusplus
 }
 #endif

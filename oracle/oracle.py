@@ -36,6 +36,21 @@ class _Bsdf(C.Structure):
                 ("albedo", C.c_float * 3)]
 
 
+class _Camera(C.Structure):
+    _fields_ = [("to_world", C.c_float * 16), ("fov", C.c_float), ("fov_axis", C.c_int32),
+                ("width", C.c_int32), ("height", C.c_int32), ("near_clip", C.c_float), ("far_clip", C.c_float)]
+
+
+class _RenderOptions(C.Structure):
+    _fields_ = [("integrator", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
+                ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
+                ("seed", C.c_uint64), ("max_paths", C.c_uint32)]
+
+
+_INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2}
+_FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
+
+
 def build() -> Path:
     """Compile liboracle.so with the committed Makefile."""
     r = subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], capture_output=True, text=True)
@@ -78,6 +93,7 @@ def load(fma: bool = False):
         "oracle_ss_connect_learned_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, i32, f32, vp, vp,
                                                   vp, vp, vp, C.c_int, vp]),
         "oracle_fresnel": (f32, [f32, f32, C.POINTER(f32)]),
+        "oracle_render": (i32, [vp, C.POINTER(_Config), C.POINTER(_Camera), C.POINTER(_RenderOptions), vp, C.c_int]),
         "oracle_fresnel_conductor": (f32, [f32, f32, f32]),
         "oracle_uniform_sphere": (None, [f32, f32, C.POINTER(f32)]),
         "oracle_pcg32": (None, [u64, u64, u32, vp]),
@@ -234,6 +250,26 @@ class OracleScene:
         names = ["solver_succeeded", "solver_failed", "bernoulli_trial_calls", "bernoulli_trial_iterations",
                  "bernoulli_trial_iterations_max", "walks", "newton_iterations", "connections"]
         return value, count, walks, dict(zip(names, stats.tolist()))
+
+    def render(self, config, camera, options, nthreads: int | None = None) -> np.ndarray:
+        """The library's sms_render restated path by path: camera / options
+        are objects with the fields of the library's Camera / RenderOptions."""
+        cam = _Camera()
+        M = np.asarray(camera.to_world, np.float32).reshape(16)
+        for k in range(16):
+            cam.to_world[k] = float(M[k])
+        cam.fov, cam.fov_axis = camera.fov, _FOV_AXES[camera.fov_axis]
+        cam.width, cam.height = int(camera.width), int(camera.height)
+        cam.near_clip, cam.far_clip = camera.near_clip, camera.far_clip
+        o = _RenderOptions()
+        o.integrator = _INTEGRATORS[options.integrator]
+        o.max_depth, o.rr_depth, o.spp = options.max_depth, options.rr_depth, options.spp
+        o.disable_reflected_emitters = int(options.disable_reflected_emitters)
+        o.biased_mnee, o.seed, o.max_paths = int(options.biased_mnee), options.seed, options.max_paths
+        img = np.zeros((camera.height, camera.width, 3), np.float32)
+        nt = nthreads or os.cpu_count() or 1
+        self._lib.oracle_render(self._h, C.byref(_cfg(config)), C.byref(cam), C.byref(o), img.ctypes.data, nt)
+        return img
 
     def __del__(self):
         if getattr(self, "_h", None) and getattr(self, "_lib", None) is not None:

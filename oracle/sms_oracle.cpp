@@ -1942,6 +1942,294 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
     return V3(w * ei.weight.x, w * ei.weight.y, w * ei.weight.z);
 }
 
+/* ====================================================================
+ * Path tracer around the SMS solvers: src/integrators/path.cpp:94-226,
+ * path_sms_ss.cpp:69-251, path_sms_ms.cpp:172-330, MonteCarloIntegrator
+ * (src/librender/integrator.cpp), perspective sensor, box filter.  One path at
+ * a time, with the random-number layout of the library's sms_render: path p
+ * draws from PCG32 stream p (state seed `seed`), its SMS call at bounce d from
+ * stream p of state seed sms_seed(seed, d).
+ * ==================================================================== */
+static uint64_t sms_seed(uint64_t seed, int depth) {
+    /* SplitMix64 (Steele, Lea and Flood 2014) */
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(uint32_t)(depth + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static float mis_weight(float a, float b) {   /* path.cpp:227-231 */
+    a *= a; b *= b;
+    return a > 0.f ? a / (a + b) : 0.f;
+}
+
+static float hmax_v(V3 v) { return std::max(v.x, std::max(v.y, v.z)); }
+
+/* sh_frame of the surface interaction: tangent from dp_du (kdtree.h:2334-2366) */
+static void pt_frame(const SI &si, V3 &s, V3 &t) {
+    V3 n = si.shn;
+    V3 a = si.dp_du - n * dot(n, si.dp_du);
+    float l2 = dot(a, a);
+    if (l2 > 1e-20f) { s = a * (1.f / std::sqrt(l2)); t = cross(n, s); }
+    else coordinate_system(n, s, t);
+}
+
+/* area.cpp eval: radiance from the front side of a sphere emitter */
+static V3 pt_emitted(const Scene &sc, const Shape &s, V3 p, V3 d) {
+    if (s.emitter < 0) return V3(0.f);
+    V3 n = normalize(p - s.center);
+    if (s.flip) n = -n;
+    if (!(dot(n, -d) > 0.f)) return V3(0.f);
+    return sc.emitters[s.emitter].radiance;
+}
+
+/* Sphere::pdf_direction x emitter pick (scene.cpp:206-220) */
+static float pt_emitter_pdf(const Scene &sc, const Shape &s, V3 x, V3 p, V3 d, float dist) {
+    V3 n = normalize(p - s.center);
+    if (s.flip) n = -n;
+    if (!(dot(d, n) < 0.f)) return 0.f;
+    float sin_a = s.radius / norm(s.center - x);
+    float cos_a = safe_sqrt(1.f - sin_a * sin_a);
+    float pdf;
+    if (sin_a < 1.f - 5.9604644775390625e-08f) pdf = (0.5f * kInvPi) / (1.f - cos_a);
+    else pdf = (1.f / (4.f * kPi * s.radius * s.radius)) * dist * dist / std::fabs(dot(d, n));
+    return sc.emitters_all.size() > 1 ? pdf * (1.f / (float)sc.emitters_all.size()) : pdf;
+}
+
+struct PtDir { V3 d, spec; float dist = 0.f, pdf = 0.f; bool delta = false; };
+
+/* Scene::sample_emitter_direction (scene.cpp:156-196), point.cpp and
+ * area.cpp + Sphere::sample_direction (sphere.cpp) */
+static bool pt_sample_emitter(const Scene &sc, V3 x, float ux, float uy, PtDir &ds) {
+    const int ne = (int)sc.emitters_all.size();
+    if (ne == 0) return false;
+    int idx = 0;
+    if (ne > 1) {
+        float epdf = 1.f / (float)ne;
+        idx = (int)std::min((uint32_t)(ux * (float)ne), (uint32_t)ne - 1);
+        ux = (ux - (float)idx * epdf) * (float)ne;
+    }
+    const Emitter &e = sc.emitters[sc.emitters_all[idx]];
+    if (e.kind == 0) {
+        V3 d = e.p - x;
+        ds.dist = norm(d);
+        float inv = 1.f / ds.dist;
+        ds.d = d * inv; ds.pdf = 1.f; ds.delta = true;
+        ds.spec = e.radiance * (inv * inv);
+    } else {
+        const Shape &s = sc.shapes[e.shape];
+        V3 dc = s.center - x;
+        float dc2 = dot(dc, dc);
+        float r_adj = s.radius * (s.flip ? (1.f + kRayEps) : (1.f - kRayEps));
+        V3 p, n;
+        if (dc2 > r_adj * r_adj) {
+            float inv_dc = 1.f / std::sqrt(dc2);
+            float sin_max = s.radius * inv_dc, sin2_max = sin_max * sin_max, inv_sin_max = 1.f / sin_max;
+            float cos_max = safe_sqrt(1.f - sin2_max);
+            float a = (cos_max - 1.f) * ux + 1.f;
+            float sin2 = sin2_max > 0.00068523f ? 1.f - a * a : sin2_max * ux;
+            float cos_t = safe_sqrt(1.f - sin2);
+            float cos_al = sin2 * inv_sin_max + cos_t * safe_sqrt(1.f - sin2 * inv_sin_max * inv_sin_max);
+            float sin_al = safe_sqrt(1.f - cos_al * cos_al);
+            float ang = uy * (2.f * kPi);
+            float sp = std::sin(ang), cp = std::cos(ang);
+            V3 fz = dc * -inv_dc, fs, ft;
+            coordinate_system(fz, fs, ft);
+            V3 dl = fs * (cp * sin_al) + ft * (sp * sin_al) + fz * cos_al;
+            p = dl * s.radius + s.center; n = dl;
+            V3 dv = p - x;
+            ds.dist = norm(dv);
+            ds.d = dv * (1.f / ds.dist);
+            ds.pdf = ds.dist == 0.f ? 0.f : (0.5f * kInvPi) / (1.f - cos_max);
+        } else {
+            V3 dl = square_to_uniform_sphere(V2{ux, uy});
+            p = dl * s.radius + s.center; n = dl;
+            V3 dv = p - x;
+            float dist2 = dot(dv, dv);
+            ds.dist = std::sqrt(dist2);
+            ds.d = dv * (1.f / ds.dist);
+            ds.pdf = (1.f / (4.f * kPi * s.radius * s.radius)) * dist2 / std::fabs(dot(ds.d, n));
+        }
+        if (s.flip) n = -n;
+        ds.delta = false;
+        if (!(dot(ds.d, n) < 0.f && ds.pdf != 0.f)) return false;
+        ds.spec = e.radiance * (1.f / ds.pdf);
+    }
+    if (ne > 1) { ds.pdf *= 1.f / (float)ne; ds.spec = ds.spec * (float)ne; }
+    return ds.pdf != 0.f;
+}
+
+/* warp.h:54-90 concentric disk, lifted to the cosine hemisphere (warp.h:332-340) */
+static V3 pt_cosine_hemisphere(float u1, float u2) {
+    float x = 2.f * u1 - 1.f, y = 2.f * u2 - 1.f, r, phi;
+    if (x == 0.f && y == 0.f) { r = 0.f; phi = 0.f; }
+    else if (std::fabs(x) < std::fabs(y)) { r = y; phi = 0.5f * kPi - (x / y) * (0.25f * kPi); }
+    else { r = x; phi = (y / x) * (0.25f * kPi); }
+    float px = r * std::cos(phi), py = r * std::sin(phi);
+    return V3(px, py, safe_sqrt(1.f - px * px - py * py));
+}
+
+struct PtBsdf { V3 wo, weight; float pdf = 0.f, eta = 1.f; bool delta = false; };
+
+/* diffuse.cpp / dielectric.cpp / conductor.cpp sample() (smooth, radiance) */
+static bool pt_bsdf_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u3, PtBsdf &bs) {
+    const float ci = wi.z;
+    if (b.type == SMS_BSDF_DIFFUSE) {
+        if (!(ci > 0.f)) return false;
+        bs.wo = pt_cosine_hemisphere(u2, u3);
+        bs.pdf = kInvPi * bs.wo.z; bs.eta = 1.f; bs.delta = false;
+        bs.weight = V3(b.albedo[0], b.albedo[1], b.albedo[2]);
+        return bs.pdf > 0.f;
+    }
+    if (b.type == SMS_BSDF_DIELECTRIC) {
+        float cos_t_abs;
+        float r = fresnel(ci, b.eta, &cos_t_abs);
+        bool outside = ci >= 0.f;
+        float eta_it = outside ? b.eta : 1.f / b.eta, eta_ti = outside ? 1.f / b.eta : b.eta;
+        float cos_t = outside ? -std::fabs(cos_t_abs) : std::fabs(cos_t_abs);
+        bs.delta = true;
+        if (u1 <= r) {
+            bs.wo = V3(-wi.x, -wi.y, wi.z); bs.pdf = r; bs.eta = 1.f; bs.weight = V3(1.f);
+        } else {
+            bs.wo = V3(-eta_ti * wi.x, -eta_ti * wi.y, cos_t); bs.pdf = 1.f - r; bs.eta = eta_it;
+            bs.weight = V3(eta_ti * eta_ti);
+        }
+        return true;
+    }
+    if (!(ci > 0.f)) return false;
+    bs.wo = V3(-wi.x, -wi.y, wi.z); bs.pdf = 1.f; bs.eta = 1.f; bs.delta = true;
+    bs.weight = V3(fresnel_conductor(ci, b.eta, b.k));
+    return true;
+}
+
+/* One camera sample (path id g) of the integrator; returns its radiance. */
+static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &cam, const sms_render_options &opt,
+                    const double tm[2], uint64_t g, Stats &st) {
+    const uint64_t wh = (uint64_t)cam.width * (uint64_t)cam.height;
+    const uint32_t pix = (uint32_t)(g % wh);
+    const uint32_t px = pix % (uint32_t)cam.width, py = pix / (uint32_t)cam.width;
+    PCG32 rng;
+    rng.seed(opt.seed, g);
+    float ux = rng.next_f32(), uy = rng.next_f32();
+    (void)rng.next_f32();
+    float sx = ((float)px + ux) / (float)cam.width, sy = ((float)py + uy) / (float)cam.height;
+    V3 dc = normalize(V3((float)tm[0] * (1.f - 2.f * sx), (float)tm[1] * (1.f - 2.f * sy), 1.f));
+    float inv_z = 1.f / dc.z;
+    const float *M = cam.to_world;
+    Ray ray;
+    ray.o = V3(M[3], M[7], M[11]);
+    ray.d = normalize(V3(M[0] * dc.x + M[1] * dc.y + M[2] * dc.z, M[4] * dc.x + M[5] * dc.y + M[6] * dc.z,
+                         M[8] * dc.x + M[9] * dc.y + M[10] * dc.z));
+    float near_clip = cam.near_clip > 0.f ? cam.near_clip : 1e-2f;
+    float far_clip = cam.far_clip > near_clip ? cam.far_clip : 1e4f;
+    ray.mint = near_clip * inv_z; ray.maxt = far_clip * inv_z;
+    SI si = ray_intersect(sc, ray);
+    V3 L(0.f), thr(1.f);
+    float eta = 1.f;
+    if (si.valid()) L += pt_emitted(sc, sc.shapes[si.shape], si.p, ray.d);
+    bool spec_cam = true, prev_receiver = false;
+    V3 prev_p;
+    const int integ = opt.integrator;
+    const int bounces = integ == SMS_INTEGRATOR_PATH_SMS_MS ? cfg.bounces : 1;
+    for (int depth = 1;; ++depth) {
+        if (!si.valid()) break;
+        if (depth > opt.rr_depth) {
+            float q = std::min(hmax_v(thr) * eta * eta, 0.95f);
+            float u = rng.next_f32();
+            if (integ == SMS_INTEGRATOR_PATH ? !(u < q) : (u > q)) break;
+            thr = thr * (1.f / q);
+        }
+        if ((uint32_t)depth >= (uint32_t)opt.max_depth) break;
+        const Shape &s = sc.shapes[si.shape];
+        V3 fs, ft;
+        pt_frame(si, fs, ft);
+        V3 n_sh = si.shn, wiw = -ray.d;
+        V3 wi(dot(wiw, fs), dot(wiw, ft), dot(wiw, n_sh));
+        const bool receiver = (s.flags & SMS_SHAPE_CAUSTIC_RECEIVER) != 0;
+        bool on_caster = false;
+        if (integ == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) != 0;
+        else if (integ == SMS_INTEGRATOR_PATH_SMS_MS)
+            on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
+        const bool smooth = s.bsdf.type == SMS_BSDF_DIFFUSE;
+        V3 albedo(s.bsdf.albedo[0], s.bsdf.albedo[1], s.bsdf.albedo[2]);
+        /* SMS at a receiver (path_sms_ss.cpp:115-121, path_sms_ms.cpp:226-232) */
+        if (integ != SMS_INTEGRATOR_PATH && receiver && !on_caster && smooth &&
+            (opt.max_depth < 0 || depth + bounces < opt.max_depth)) {
+            Query q;
+            q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
+            PCG32 srng;
+            srng.seed(sms_seed(opt.seed, depth), g);
+            int c = 0, w = 0;
+            V3 v = integ == SMS_INTEGRATOR_PATH_SMS_MS ? ms_connect(sc, cfg, q, srng, c, w, st)
+                                                       : ss_connect(sc, cfg, q, srng, c, w, st);
+            L += thr * v;
+        }
+        /* emitter sampling */
+        bool nee = smooth && !on_caster;
+        if (integ == SMS_INTEGRATOR_PATH_SMS_SS) nee = nee || (depth == 1 && !opt.disable_reflected_emitters);
+        if (nee) {
+            float ex = rng.next_f32(), ey = rng.next_f32();
+            PtDir ds;
+            if (pt_sample_emitter(sc, si.p, ex, ey, ds)) {
+                Ray sr; sr.o = si.p; sr.d = ds.d;
+                sr.mint = kRayEps * (1.f + hmax_abs(si.p)); sr.maxt = ds.dist * (1.f - kShadowEps);
+                if (!ray_test(sc, sr) && smooth) {
+                    float co = dot(ds.d, n_sh);
+                    if (wi.z > 0.f && co > 0.f) {
+                        V3 bv = albedo * (kInvPi * co);
+                        float w = ds.delta ? 1.f : mis_weight(ds.pdf, kInvPi * co);
+                        L += thr * bv * ds.spec * w;
+                    }
+                }
+            }
+        }
+        /* BSDF sampling */
+        float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
+        PtBsdf bs;
+        if (!pt_bsdf_sample(s.bsdf, wi, u1, u2, u3, bs)) break;
+        thr = thr * bs.weight;
+        eta *= bs.eta;
+        if (!bs.delta) spec_cam = false;
+        if (thr.x == 0.f && thr.y == 0.f && thr.z == 0.f) break;
+        Ray nr;
+        nr.o = si.p; nr.d = fs * bs.wo.x + ft * bs.wo.y + n_sh * bs.wo.z;
+        nr.mint = kRayEps * (1.f + hmax_abs(si.p)); nr.maxt = kInf;
+        SI si2 = ray_intersect(sc, nr);
+        if (si2.valid() && sc.shapes[si2.shape].emitter >= 0) {
+            const Shape &es = sc.shapes[si2.shape];
+            V3 ep = nr.o + nr.d * si2.t;
+            V3 Le = pt_emitted(sc, es, ep, nr.d);
+            bool allow = true;
+            if (integ == SMS_INTEGRATOR_PATH_SMS_SS) allow = !on_caster || (depth == 1 && !opt.disable_reflected_emitters);
+            else if (integ == SMS_INTEGRATOR_PATH_SMS_MS) allow = !on_caster || spec_cam;
+            if (allow) {
+                float epdf = bs.delta ? 0.f : pt_emitter_pdf(sc, es, si.p, ep, nr.d, si2.t);
+                L += thr * Le * mis_weight(bs.pdf, epdf);
+            } else if (integ == SMS_INTEGRATOR_PATH_SMS_SS && cfg.mnee_init && !opt.biased_mnee && prev_receiver &&
+                       std::find(sc.emitters_ss.begin(), sc.emitters_ss.end(), es.emitter) != sc.emitters_ss.end()) {
+                /* path_sms_ss.cpp:207-241: the MNEE walk from the previous vertex */
+                Query q;
+                q.p = prev_p;
+                EI ei;
+                ei.p = ep;
+                SI sf, s0;
+                int it = 0;
+                bool found = sample_path(sc, cfg, si.shape, q, ei, V2{0.5f, 0.5f}, V3(0.f), sf, s0, it);
+                if (found) {
+                    V3 dpt = normalize(si.p - prev_p), dmn = normalize(sf.p - prev_p);
+                    found = std::fabs(dot(dpt, dmn) - 1.f) < cfg.uniqueness_threshold;
+                }
+                if (!found) L += thr * Le;
+            }
+        }
+        prev_p = si.p;
+        prev_receiver = receiver;
+        ray = nr;
+        si = si2;
+    }
+    return L;
+}
+
 static Scene *as_scene(void *p) { return reinterpret_cast<Scene *>(p); }
 
 } // namespace orc
@@ -2399,6 +2687,49 @@ int oracle_glint_connect_batch(void *s, const sms_config *cfg, const float *quer
 /* Known-answer hooks for the dependency pins (fresnel.h:34-120, warp.h). */
 float oracle_fresnel(float cos_i, float eta, float *cos_t) { return fresnel(cos_i, eta, cos_t); }
 float oracle_fresnel_conductor(float cos_i, float eta, float k) { return fresnel_conductor(cos_i, eta, k); }
+/* Image of spp samples per pixel (height x width x 3, row-major), the
+ * library's sms_render restated path by path; nthreads host threads. */
+int oracle_render(void *s, const sms_config *cfg, const sms_camera *cam, const sms_render_options *opt,
+                  float *image, int nthreads) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
+    const double aspect = (double)cam->width / (double)cam->height;
+    const double t = std::tan(0.5 * (double)cam->fov * 3.14159265358979323846 / 180.0);
+    double tx = t;
+    if (cam->fov_axis == SMS_FOV_Y) tx = t * aspect;
+    else if (cam->fov_axis == SMS_FOV_DIAGONAL) tx = t / std::sqrt(1.0 + 1.0 / (aspect * aspect));
+    else if (cam->fov_axis == SMS_FOV_SMALLER) tx = aspect >= 1.0 ? t * aspect : t;
+    else if (cam->fov_axis == SMS_FOV_LARGER) tx = aspect >= 1.0 ? t : t * aspect;
+    const double tm[2] = {(double)(float)tx, (double)(float)(tx / aspect)};
+    const uint64_t total = wh * (uint64_t)opt->spp;
+    std::vector<float> Ls(3 * total);
+    Stats st;
+    if (nthreads < 1) nthreads = 1;
+    std::atomic<uint64_t> next{0};
+    auto worker = [&]() {
+        while (true) {
+            uint64_t b = next.fetch_add(16);
+            if (b >= total) break;
+            for (uint64_t g = b; g < std::min(total, b + 16); ++g) {
+                V3 L = pt_sample(*sc, *cfg, *cam, *opt, tm, g, st);
+                Ls[3 * g] = L.x; Ls[3 * g + 1] = L.y; Ls[3 * g + 2] = L.z;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int k = 1; k < nthreads; ++k) th.emplace_back(worker);
+    worker();
+    for (auto &x : th) x.join();
+    for (uint64_t p = 0; p < wh; ++p) {
+        float acc[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < opt->spp; ++k)
+            for (int c = 0; c < 3; ++c) acc[c] += Ls[3 * ((uint64_t)k * wh + p) + c];
+        for (int c = 0; c < 3; ++c) image[3 * p + c] = acc[c] * (1.f / (float)opt->spp);
+    }
+    return 0;
+}
+
 void oracle_uniform_sphere(float u, float v, float *out) {
     V2 s; s.x = u; s.y = v;
     V3 r = square_to_uniform_sphere(s);

@@ -49,6 +49,9 @@ PROPOSAL_FEATURES = 9
 PROPOSAL_OUTPUTS = 40
 PROPOSAL_PARAMS = 21808
 
+INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2}
+FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
+
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device limit",
                 4: "unsupported", 5: "parse error", 6: "no device"}
 
@@ -93,6 +96,17 @@ class _Stats(C.Structure):
 
 
 PHASES = ["ss_first", "ss_trials", "ss_biased", "ss_walk", "ms", "glints", "ms_walk", "glint_walk"]
+
+
+class _Camera(C.Structure):
+    _fields_ = [("to_world", C.c_float * 16), ("fov", C.c_float), ("fov_axis", C.c_int32),
+                ("width", C.c_int32), ("height", C.c_int32), ("near_clip", C.c_float), ("far_clip", C.c_float)]
+
+
+class _RenderOptions(C.Structure):
+    _fields_ = [("integrator", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
+                ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
+                ("seed", C.c_uint64), ("max_paths", C.c_uint32)]
 
 
 class _Profile(C.Structure):
@@ -160,6 +174,10 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_proposal_frame": (i32, [vp, vp]),
         "sms_obj_load": (i32, [C.c_char_p, i32, i32, C.POINTER(_MeshData)]),
         "sms_mesh_data_free": (None, [C.POINTER(_MeshData)]),
+        "sms_render_options_default": (None, [C.POINTER(_RenderOptions)]),
+        "sms_render_sms_seed": (u64, [u64, i32]),
+        "sms_render": (i32, [vp, C.POINTER(_Camera), C.POINTER(_RenderOptions), vp]),
+        "sms_render_device": (i32, [vp, C.POINTER(_Camera), C.POINTER(_RenderOptions), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -404,6 +422,16 @@ class Context:
                        "bvh_nodes": p.bvh_nodes[k], "tri_tests": p.tri_tests[k]}
                 for k, name in enumerate(PHASES)}
 
+    def render(self, camera: "Camera", options: "RenderOptions") -> np.ndarray:
+        """Image (height, width, 3) float32 of the path tracer (sms_render)."""
+        img = np.zeros((camera.height, camera.width, 3), np.float32)
+        _check(_LIB.sms_render(self._h, C.byref(camera.to_c()), C.byref(options.to_c()), _ptr(img)))
+        return img
+
+    def render_device(self, camera: "Camera", options: "RenderOptions", image_ptr: int):
+        """Render into a device buffer of height * width * 3 floats."""
+        _check(_LIB.sms_render_device(self._h, C.byref(camera.to_c()), C.byref(options.to_c()), image_ptr))
+
     def set_proposal(self, proposal: "SeedProposal | None", defensive: float = 0.1):
         """Seed the unbiased single-scatter estimator from a learned proposal
         (None restores uniform seeding)."""
@@ -528,6 +556,76 @@ class SeedProposal:
 
     def __del__(self):
         self.close()
+
+
+# --------------------------------------------------------------- rendering
+@dataclass
+class Camera:
+    """Perspective sensor (src/sensors/perspective.cpp): camera-to-world 4x4
+    (camera x left, y up, z forward), field of view in degrees along fov_axis,
+    film size, clip distances."""
+    to_world: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
+    fov: float = 45.0
+    width: int = 64
+    height: int = 64
+    fov_axis: str = "x"
+    near_clip: float = 1e-2
+    far_clip: float = 1e4
+
+    @staticmethod
+    def look_at(origin, target, up, fov: float = 45.0, width: int = 64, height: int = 64,
+                fov_axis: str = "x") -> "Camera":
+        """The reference's look_at transform (include/mitsuba/core/transform.h):
+        columns left, up, forward, origin."""
+        o, t, u = (np.asarray(v, np.float64) for v in (origin, target, up))
+        d = t - o
+        d /= np.linalg.norm(d)
+        left = np.cross(u, d)
+        left /= np.linalg.norm(left)
+        new_up = np.cross(d, left)
+        M = np.eye(4)
+        M[:3, 0], M[:3, 1], M[:3, 2], M[:3, 3] = left, new_up, d, o
+        return Camera(M.astype(np.float32), fov, width, height, fov_axis)
+
+    def to_c(self) -> _Camera:
+        c = _Camera()
+        M = np.asarray(self.to_world, np.float32).reshape(16)
+        for k in range(16):
+            c.to_world[k] = float(M[k])
+        c.fov = self.fov
+        c.fov_axis = FOV_AXES[self.fov_axis]
+        c.width, c.height = int(self.width), int(self.height)
+        c.near_clip, c.far_clip = self.near_clip, self.far_clip
+        return c
+
+
+@dataclass
+class RenderOptions:
+    """Integrator parameters: path / path_sms_ss / path_sms_ms with the
+    MonteCarloIntegrator fields (src/librender/integrator.cpp:300-320) and the
+    SMS integrators' switches (path_sms_ss.cpp:59-60)."""
+    integrator: str = "path_sms_ss"
+    max_depth: int = -1
+    rr_depth: int = 5
+    spp: int = 1
+    disable_reflected_emitters: bool = False
+    biased_mnee: bool = False
+    seed: int = 0
+    max_paths: int = 0
+
+    def to_c(self) -> _RenderOptions:
+        o = _RenderOptions()
+        o.integrator = INTEGRATORS[self.integrator]
+        o.max_depth, o.rr_depth, o.spp = self.max_depth, self.rr_depth, self.spp
+        o.disable_reflected_emitters = int(self.disable_reflected_emitters)
+        o.biased_mnee = int(self.biased_mnee)
+        o.seed, o.max_paths = self.seed, self.max_paths
+        return o
+
+
+def sms_render_seed(seed: int, depth: int) -> int:
+    """State seed of the SMS random-number streams at bounce `depth`."""
+    return int(load_library().sms_render_sms_seed(seed, depth))
 
 
 def _soa(a: np.ndarray, rows: int, n: int) -> np.ndarray:

@@ -153,6 +153,7 @@ struct Pcg32 {
 // --------------------------------------------------------------- scene data
 enum : int { kShapeSphere = 0, kShapeMesh = 1 };
 // shape flags (same bits as SMS_SHAPE_* in sms_gb300.h)
+constexpr uint32_t kShapeFlagReceiver = 1u << 0;
 constexpr uint32_t kShapeFlagCasterSingle = 1u << 1;
 constexpr uint32_t kShapeFlagCasterMulti = 1u << 2;
 constexpr uint32_t kShapeFlagBouncer = 1u << 3;
@@ -177,6 +178,7 @@ struct DevShape {
     int emitter;
     float bcx, bcy, bcz;   // bounding-box centre
     int reflective;        // complex ior: MNEE initialisation aims at the box centre
+    float albedo[3];       // diffuse reflectance (path tracer)
 };
 
 // Target of the MNEE initialisation (manifold_ss.cpp:229-241,

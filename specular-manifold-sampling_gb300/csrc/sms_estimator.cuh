@@ -1,6 +1,7 @@
-// sms_estimator.cuh -- device helpers shared by the SMS estimators: counters,
-// shading-point queries, emitter sampling, light visibility, emitter vertex,
-// diffuse receiver.
+// sms_estimator.cuh -- device helpers shared by the SMS estimators and the
+// path tracer: counters, shading-point queries, emitter sampling, light
+// visibility, emitter vertex, diffuse receiver, the single-scatter walk and
+// its contribution.
 #pragma once
 #include "sms_device.cuh"
 #include "sms_kernels.h"
@@ -102,6 +103,10 @@ SMS_D bool sample_emitter(const DevScene &sc, const int *list, int ne, Pcg32 &rn
     return true;
 }
 
+SMS_D uint64_t query_stream(const SolverCfg &cfg, uint64_t stream_off, uint32_t qi) {
+    return stream_off + (cfg.stream_ids ? (uint64_t)__ldg(cfg.stream_ids + qi) : (uint64_t)qi);
+}
+
 SMS_D Pcg32 query_rng(uint64_t seed, uint64_t stream, uint64_t position) {
     Pcg32 r;
     r.seed(seed, stream);
@@ -161,6 +166,60 @@ SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
     float co = dot(dir, Q.n);
     if (Q.cos_i <= 0.f || co <= 0.f) return splat(0.f);
     return (Q.albedo * kInvPi) * co;
+}
+
+// ------------------------------------------------------------------- walk
+// sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
+// explicit seed point.  Returns ok; v holds the solution vertex.
+SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
+                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr) {
+    f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
+    Hit h;
+    trace(sc, x, d, kRayEps, INFINITY, false, h, err);
+    st.ray(h);
+    it = 0;
+    if (h.shape < 0) return false;
+    vertex_from_hit(sc, x, d, h, v);
+    if (p_init) *p_init = v.p;
+    if (h.shape != caster) return false;
+    float beta = 1.f;
+    bool accepted = false, conv = false;
+    while (it < cfg.max_iterations) {
+        float c0, c1, dx0, dx1;
+        bool sok = cfg.halfvector ? step_halfvector(x, v, lp, c0, c1, dx0, dx1)
+                                  : step_anglediff(x, v, lp, c0, c1, dx0, dx1);
+        if (!sok) break;
+        if (sqrtf(c0 * c0 + c1 * c1) < cfg.solver_threshold) { conv = true; break; }
+        f3 pp = v.p - (v.dp_du * dx0 + v.dp_dv * dx1) * (cfg.step_scale * beta);
+        f3 dd = normalize(pp - x);
+        trace(sc, x, dd, kRayEps, INFINITY, false, h, err);
+        st.ray(h);
+        it++;
+        if (h.shape < 0 || h.shape != v.shape) {
+            beta = 0.5f * beta;
+            accepted = false;
+            continue;
+        }
+        beta = fminf(1.f, 2.f * beta);
+        vertex_from_hit(sc, x, dd, h, v);
+        accepted = true;
+    }
+    // newton_solver returns si_current: valid only after an accepted step.
+    if (!(conv && accepted)) return false;
+    f3 wx = normalize(x - v.p), wy = normalize(lp - v.p);
+    bool refraction = dot(v.gn, wx) * dot(v.gn, wy) < 0.f;
+    return (v.eta == 1.f) ? !refraction : refraction;
+}
+
+// evaluate_path_contribution (manifold_ss.cpp:281-327) for a flat receiver.
+SMS_D f3 contribution(const DevScene &sc, f3 x, const Light &L, const Vtx &sol, uint32_t &err, LaneStats &st) {
+    Vtx vt = sol;
+    make_orthonormal(vt.dp_du, vt.dp_dv, vt.dn_du, vt.dn_dv);
+    f3 yp, ydu, ydv, lw, lp;
+    if (!emitter_endpoint(sc, L, vt.p, yp, ydu, ydv, lw, lp, err, st)) return splat(0.f);
+    float F = specular_reflectance(sc.shapes[vt.shape], vt.n, normalize(lp - vt.p));
+    F *= geometric_term(x, vt, yp, ydu, ydv);
+    return lw * F;
 }
 
 }  // namespace sms

@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(128, 8) glint_biased_kernel(DevScene sc, Solve
         bool have_light = false, vis = false;
         if (live) {
             Q = load_gquery(qs, n, qi);
-            Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+            Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
             // the shadow ray is the same for every lane of the group: one lane casts it
             Pcg32 r2 = rng;
             have_light = sample_emitter(sc, sc.emitters_all, sc.n_emitters_all, r2, Q.p, L);
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(128, 8) glint_biased_kernel(DevScene sc, Solve
             bool ok = false;
             f2 uv = {0.f, 0.f};
             if (work && m < M) {
-                Pcg32 rng = query_rng(seed, stream_off + qi, 3u + 2u * (uint64_t)m);
+                Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + 2u * (uint64_t)m);
                 float fx = rng.next_f32(), fy = rng.next_f32();
                 f2 uv0;
                 int it;
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(128) glint_first_kernel(DevScene sc, SolverCfg
     bool enqueue = false;
     if (qi < n) {
         GQuery Q = load_gquery(qs, n, qi);
-        Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+        Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
         Light L;
         bool vis = false;
         bool have = glint_light(sc, rng, Q, L, vis, err, st) && sc.glinty_shape >= 0 && sc.nmap_res > 0;
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(128) glint_trials_kernel(DevScene sc, SolverCf
         if (idx >= n_list) break;
         uint32_t qi = scr.list[idx];
         GQuery Q = load_gquery(qs, n, qi);
-        Pcg32 base = query_rng(seed, stream_off + qi, 0);
+        Pcg32 base = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
         Light L;
         sample_emitter(sc, sc.emitters_all, sc.n_emitters_all, base, Q.p, L);   // at position 3
         f2 uv0 = {scr.dir0[qi], scr.dir0[(size_t)n + qi]};

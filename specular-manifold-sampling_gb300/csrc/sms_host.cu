@@ -386,6 +386,7 @@ static SolverCfg solver_cfg(const sms_config &c) {
     s.uniqueness_threshold = c.uniqueness_threshold;
     s.step_scale = c.step_scale;
     s.mnee_init = c.mnee_init;
+    s.stream_ids = nullptr;
     return s;
 }
 
@@ -457,6 +458,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         ds.bsdf_type = h.bsdf.type;
         ds.eta = h.bsdf.eta;
         ds.k = h.bsdf.k;
+        ds.albedo[0] = h.bsdf.albedo[0]; ds.albedo[1] = h.bsdf.albedo[1]; ds.albedo[2] = h.bsdf.albedo[2];
         // manifold.h:94-96: real ior -> eta, complex or non-specular -> 1
         bool real_ior = h.bsdf.type == SMS_BSDF_DIELECTRIC ||
                         (h.bsdf.type == SMS_BSDF_CONDUCTOR && h.bsdf.k == 0.f);
@@ -652,7 +654,9 @@ extern "C" sms_status sms_ctx_set_launch(sms_ctx *c, int32_t bps, int32_t tpb) {
     return SMS_OK;
 }
 
-static sms_status check_device_error(sms_ctx *c) {
+sms_status ctx_check_device_error(sms_ctx *c);
+static sms_status check_device_error(sms_ctx *c) { return ctx_check_device_error(c); }
+sms_status ctx_check_device_error(sms_ctx *c) {
     unsigned err = 0;
     CUDA_TRY(cudaMemcpyAsync(&err, &c->ctr->error, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -743,8 +747,10 @@ static sms_status ensure_scratch(sms_ctx *c, uint32_t n, SsScratch &scr) {
     return SMS_OK;
 }
 
-extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
-                                                  uint64_t stream_off, sms_result *out) {
+// Single-scatter connection of n device-resident queries; stream_ids (may be
+// null) as SolverCfg::stream_ids.
+sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
+                          const uint32_t *stream_ids, sms_result *out) {
     if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
         return fail(SMS_ERR_INVALID_ARG, "sms_ss_connect_batch_device: null argument");
     if (n == 0) return SMS_OK;
@@ -772,10 +778,17 @@ extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, ui
         pr.defensive = c->defensive;
         pr.gmm = c->gmm;
     }
-    CUDA_TRY(launch_ss_connect(c->dsc, solver_cfg(c->cfg), q, n, seed, stream_off, out->value, out->count,
-                               out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, &c->timer, c->stream,
-                               c->prop ? &pr : nullptr, c->trial_group));
+    SolverCfg sc = solver_cfg(c->cfg);
+    sc.stream_ids = stream_ids;
+    CUDA_TRY(launch_ss_connect(c->dsc, sc, q, n, seed, stream_off, out->value, out->count, out->walks, c->ctr, scr,
+                               c->num_sms, c->blocks_per_sm, &c->timer, c->stream, c->prop ? &pr : nullptr,
+                               c->trial_group));
     return SMS_OK;
+}
+
+extern "C" sms_status sms_ss_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                                  uint64_t stream_off, sms_result *out) {
+    return ctx_ss_connect(c, q, n, seed, stream_off, nullptr, out);
 }
 
 extern "C" sms_status sms_ctx_set_proposal(sms_ctx *c, sms_proposal *p, float defensive) {
@@ -892,6 +905,7 @@ bool ctx_view(sms_ctx *c, CtxView &out) {
     out.n_shapes = (int)c->frames.size();
     out.proposal_bound = c->prop != nullptr;
     out.trial_group = c->trial_group;
+    out.bounces = c->cfg.bounces;
     return true;
 }
 
@@ -907,8 +921,8 @@ static sms_status check_ms_cfg(sms_ctx *c) {
     return SMS_OK;
 }
 
-extern "C" sms_status sms_ms_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
-                                                  uint64_t stream_off, sms_result *out) {
+sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
+                          const uint32_t *stream_ids, sms_result *out) {
     if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
         return fail(SMS_ERR_INVALID_ARG, "sms_ms_connect_batch_device: null argument");
     if (sms_status st = check_ms_cfg(c)) return st;
@@ -930,10 +944,17 @@ extern "C" sms_status sms_ms_connect_batch_device(sms_ctx *c, const float *q, ui
             c->ms_tmpl_n = n;
         }
     }
-    CUDA_TRY(launch_ms_connect(c->dsc, solver_cfg(c->cfg), c->cfg.bounces, q, n, seed, stream_off, out->value,
-                               out->count, out->walks, c->ctr, scr, c->ms_tmpl, c->num_sms, c->blocks_per_sm,
-                               &c->timer, c->stream));
+    SolverCfg sc = solver_cfg(c->cfg);
+    sc.stream_ids = stream_ids;
+    CUDA_TRY(launch_ms_connect(c->dsc, sc, c->cfg.bounces, q, n, seed, stream_off, out->value, out->count,
+                               out->walks, c->ctr, scr, c->ms_tmpl, c->num_sms, c->blocks_per_sm, &c->timer,
+                               c->stream));
     return SMS_OK;
+}
+
+extern "C" sms_status sms_ms_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                                  uint64_t stream_off, sms_result *out) {
+    return ctx_ms_connect(c, q, n, seed, stream_off, nullptr, out);
 }
 
 extern "C" sms_status sms_ms_connect_batch(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,

@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/sms_gb300.h"
 #include "sms_mlp.h"
 
 namespace sms {
@@ -27,6 +28,11 @@ struct SolverCfg {
     float uniqueness_threshold;
     float step_scale;
     int mnee_init;      // seed along the straight path (manifold_ss.cpp:229-241)
+    // Optional per-query random-number stream table: query i draws from stream
+    // stream_off + stream_ids[i] instead of stream_off + i (the path tracer
+    // passes each query's path index, so that results do not depend on which
+    // paths of a wavefront reached a receiver).
+    const uint32_t *stream_ids;
 };
 
 // Unique-solution capacity per query of the biased estimator (shared memory
@@ -97,6 +103,7 @@ struct CtxView {
     int n_shapes;
     bool proposal_bound;            // a learned proposal seeds the SS estimator
     int trial_group;                // lanes per query of the trial kernel (0: auto)
+    int bounces;                    // multi-scatter chain length (sms_config::bounces)
 };
 
 }  // namespace sms
@@ -104,6 +111,16 @@ struct CtxView {
 // Context accessors implemented in sms_host.cu.
 struct sms_ctx;
 bool ctx_view(sms_ctx *c, sms::CtxView &out);
+// Connection entry points shared with the path tracer (sms_render.cu): as
+// sms_ss_connect_batch_device / sms_ms_connect_batch_device, with an optional
+// per-query stream table (SolverCfg::stream_ids).
+sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
+                          const uint32_t *stream_ids, sms_result *out);
+sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
+                          const uint32_t *stream_ids, sms_result *out);
+// Reads and clears the device error flags of a context (synchronizes its
+// stream); SMS_ERR_DEVICE_LIMIT with the reasons when any was set.
+sms_status ctx_check_device_error(sms_ctx *c);
 // Records msg as sms_last_error() for this thread and returns st.
 int set_last_error_impl(int st, const char *msg);
 

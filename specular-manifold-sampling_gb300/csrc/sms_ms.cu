@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(128, 4) ms_biased_kernel(DevScene sc, SolverCf
         bool have_light = false;
         if (live) {
             Q = load_query(qs, n, qi);
-            Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+            Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
             have_light = sample_emitter(sc, sc.emitters_ms, sc.n_emitters_ms, rng, Q.x, L);
         }
         bool work = live && have_light && sc.n_casters_ms > 0;
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(128, 4) ms_biased_kernel(DevScene sc, SolverCf
                 for (int b = 0; b < K; ++b) shapes[b] = -1;
                 bool seed_ok = false;
                 if (act) {
-                    Pcg32 rng = query_rng(seed, stream_off + qi, 3u + 2u * ((uint64_t)ci * M + m));
+                    Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + 2u * ((uint64_t)ci * M + m));
                     float sx = rng.next_f32(), sy = rng.next_f32();
                     f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
                     seed_ok = seed_chain<K>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st);
@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cf
     bool enqueue = false;
     if (qi < n) {
         Query Q = load_query(qs, n, qi);
-        Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+        Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
         Light L;
         bool have_light = sample_emitter(sc, sc.emitters_ms, sc.n_emitters_ms, rng, Q.x, L);
         uint32_t pos = 3u;
@@ -703,7 +703,7 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
         if (idx >= n_list) break;
         uint32_t qi = scr.list[idx];
         Query Q = load_query(qs, n, qi);
-        Pcg32 base = query_rng(seed, stream_off + qi, 0);
+        Pcg32 base = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
         Light L;
         sample_emitter(sc, sc.emitters_ms, sc.n_emitters_ms, base, Q.x, L);
         uint32_t pos = scr.pos[qi];

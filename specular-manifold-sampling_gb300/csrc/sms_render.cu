@@ -1,0 +1,828 @@
+// sms_render.cu -- wavefront path tracer around the SMS solvers (sm_103a).
+//
+// The reference's integrators (src/integrators/path.cpp, path_sms_ss.cpp,
+// path_sms_ms.cpp) trace one camera path per host thread and call the SMS
+// solver inline at every caustic receiver.  Here a wavefront of up to 2^20
+// paths advances one bounce per launch:
+//
+//   pt_camera_kernel   camera ray, first intersection, directly seen emitters
+//   pt_bounce_kernel   one bounce of every live path: Russian roulette, the SMS
+//                      query of a receiver vertex (staged, not solved), emitter
+//                      sampling with MIS, BSDF sampling, the next intersection
+//                      and the emitter it hits (filtered like the reference,
+//                      with the unbiased-MNEE check walk of path_sms_ss)
+//   pt_scan_kernel     ordered prefix sum of the per-block query counts
+//   pt_gather_kernel   compacts the staged queries into an SMS query batch
+//                      in path order, with each query's path index as its
+//                      random-number stream
+//   (SMS estimator)    the context's single- or multi-scatter connection
+//                      kernels on that batch
+//   pt_sms_add_kernel  adds throughput x SMS estimate to each path's radiance
+//   pt_resolve_kernel  sums the samples of each pixel in sample order
+//
+// One host read per bounce (query and live-path counts) sizes the SMS launch.
+// Every sum runs in a fixed order, so images are bit-reproducible, and since
+// all random numbers are keyed by the path index they do not depend on the
+// wavefront size.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sms_gb300.h"
+#include "sms_device.cuh"
+#include "sms_estimator.cuh"
+#include "sms_kernels.h"
+
+namespace sms {
+namespace {
+
+constexpr int kPtBlock = 256;
+constexpr uint32_t kPtDefaultPaths = 1u << 20;
+constexpr int kPtHardDepth = 4096;        // bounce limit of an unbounded path
+constexpr int kStageRows = 19;            // 16 query rows + 3 throughput rows
+
+// path flags
+constexpr int kAlive = 1, kPrevReceiver = 2, kSpecularCamera = 4;
+
+struct PtCam {
+    float m[12];          // rows 0..2 of camera-to-world
+    float tx, ty;         // tan of the half field of view along x and y
+    float near_clip, far_clip;
+    int width, height;
+};
+
+struct PtParams {
+    int integrator;       // SMS_INTEGRATOR_*
+    int max_depth, rr_depth;
+    int disable_reflected_emitters, biased_mnee;
+    int bounces;          // SMS chain length (path_sms_ms)
+    int mnee_check;       // path_sms_ss with mnee_init and !biased_mnee
+    uint64_t seed;
+    SolverCfg solver;     // for the MNEE check walk
+};
+
+struct PtState {
+    uint64_t *rng_state, *rng_inc;
+    float *o, *d, *thr, *L, *prev_p;      // 3 x cap
+    float *eta, *hit_t, *hit_u, *hit_v;   // cap
+    int *hit_shape, *flags;               // cap
+    uint32_t *hit_prim;                   // cap
+    float *stage;                         // kStageRows x cap
+    int *want;                            // cap
+    uint32_t *block_q, *block_a;          // per block
+    uint32_t *totals;                     // [0] queries, [1] live paths
+    float *q;                             // 16 x cap (compacted queries)
+    uint32_t *map;                        // cap: compacted query -> path
+    float *value;                         // 3 x cap
+    int *count, *walks;                   // cap
+    uint32_t cap;
+};
+
+SMS_D f3 ld3s(const float *a, uint32_t cap, uint32_t i) { return mk(a[i], a[cap + i], a[2 * (size_t)cap + i]); }
+SMS_D void st3s(float *a, uint32_t cap, uint32_t i, f3 v) {
+    a[i] = v.x; a[cap + i] = v.y; a[2 * (size_t)cap + i] = v.z;
+}
+SMS_D float hmax3(f3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
+SMS_D float max_abs(f3 v) { return fmaxf(fabsf(v.x), fmaxf(fabsf(v.y), fabsf(v.z))); }
+
+// Power heuristic (path.cpp:227-231).
+SMS_D float mis_weight(float a, float b) {
+    a *= a;
+    b *= b;
+    return a > 0.f ? a / (a + b) : 0.f;
+}
+
+// Surface data of a closest hit: position, geometric and shading normals,
+// position partials (sphere.cpp:322-373, mesh.cpp:618-687).
+SMS_D void surface_at(const DevScene &sc, f3 o, f3 d, float t, int shape, uint32_t prim, float u, float v,
+                      SurfPt &si) {
+    const DevShape &s = sc.shapes[shape];
+    if (s.kind == kShapeSphere) {
+        sphere_surface(s, o, d, t, si);
+    } else {
+        MeshTri m;
+        load_tri(sc, s, prim, m);
+        mesh_surface(m, s.has_normals, u, v, si);
+    }
+}
+
+// Shading frame: normal n, tangent from dp_du (the reference's surface
+// interaction frame, kdtree.h:2334-2366), Duff et al. basis when dp_du is
+// degenerate or parallel to n.
+SMS_D void shading_frame(const SurfPt &si, f3 &s, f3 &t) {
+    f3 n = si.shn;
+    f3 a = si.dp_du - n * dot(n, si.dp_du);
+    float l2 = dot(a, a);
+    if (l2 > 1e-20f) {
+        s = a * (1.f / sqrtf(l2));
+        t = cross(n, s);
+    } else {
+        onb(n, s, t);
+    }
+}
+
+// Emitted radiance of an area emitter seen along direction d from its front
+// side (area.cpp: eval, cos_theta(wi) > 0).  Only spheres carry emitters.
+SMS_D f3 emitted(const DevScene &sc, const DevShape &s, f3 p, f3 d) {
+    if (s.emitter < 0) return splat(0.f);
+    f3 n = normalize(p - mk(s.cx, s.cy, s.cz));
+    if (s.flip) n = -n;
+    if (!(dot(n, -d) > 0.f)) return splat(0.f);
+    const DevEmitter &e = sc.emitters[s.emitter];
+    return mk(e.r, e.g, e.b);
+}
+
+// Sphere::pdf_direction (sphere.cpp) x the emitter pick (scene.cpp:206-220):
+// density of emitter sampling from x for the emitter point p (normal n).
+SMS_D float emitter_pdf(const DevScene &sc, const DevShape &s, f3 x, f3 p, f3 d, float dist) {
+    f3 n = normalize(p - mk(s.cx, s.cy, s.cz));
+    if (s.flip) n = -n;
+    if (!(dot(d, n) < 0.f)) return 0.f;
+    f3 c = mk(s.cx, s.cy, s.cz);
+    float sin_a = s.radius / length(c - x);
+    float cos_a = safe_sqrt(1.f - sin_a * sin_a);
+    float pdf;
+    if (sin_a < 1.f - 5.9604644775390625e-08f)
+        pdf = (0.5f * kInvPi) / (1.f - cos_a);
+    else
+        pdf = (1.f / (4.f * kPi * s.radius * s.radius)) * dist * dist / fabsf(dot(d, n));
+    return sc.n_emitters_all > 1 ? pdf * (1.f / (float)sc.n_emitters_all) : pdf;
+}
+
+struct DirSample {
+    f3 d, spec;
+    float dist, pdf;
+    bool delta;
+};
+
+// Scene::sample_emitter_direction over all emitters (scene.cpp:156-196):
+// point.cpp sample_direction; area.cpp + Sphere::sample_direction (cone
+// sampling from outside, uniform sphere from inside).  Visibility is tested
+// by the caller.
+SMS_D bool sample_emitter_direction(const DevScene &sc, f3 x, float ux, float uy, DirSample &ds) {
+    const int ne = sc.n_emitters_all;
+    if (ne == 0) return false;
+    int idx = 0;
+    if (ne > 1) {
+        const float epdf = 1.f / (float)ne;
+        idx = (int)min((uint32_t)(ux * (float)ne), (uint32_t)ne - 1);
+        ux = (ux - (float)idx * epdf) * (float)ne;
+    }
+    const DevEmitter &e = sc.emitters[sc.emitters_all[idx]];
+    if (e.kind == 0) {
+        f3 d = mk(e.px, e.py, e.pz) - x;
+        ds.dist = length(d);
+        float inv = 1.f / ds.dist;
+        ds.d = d * inv;
+        ds.pdf = 1.f;
+        ds.delta = true;
+        ds.spec = mk(e.r, e.g, e.b) * (inv * inv);
+    } else {
+        const DevShape &s = sc.shapes[e.shape];
+        f3 c = mk(s.cx, s.cy, s.cz);
+        f3 dc = c - x;
+        float dc2 = dot(dc, dc);
+        float r_adj = s.radius * (s.flip ? (1.f + kRayEps) : (1.f - kRayEps));
+        f3 p, n;
+        if (dc2 > r_adj * r_adj) {
+            float inv_dc = 1.f / sqrtf(dc2);
+            float sin_max = s.radius * inv_dc, sin2_max = sin_max * sin_max, inv_sin_max = 1.f / sin_max;
+            float cos_max = safe_sqrt(1.f - sin2_max);
+            // small cones: first-order expansion of 1 - cos^2 (1.5 degrees)
+            float a = (cos_max - 1.f) * ux + 1.f;
+            float sin2 = sin2_max > 0.00068523f ? 1.f - a * a : sin2_max * ux;
+            float cos_t = safe_sqrt(1.f - sin2);
+            // point on the visible cap (Akalin, "Sampling the visible sphere")
+            float cos_al = sin2 * inv_sin_max + cos_t * safe_sqrt(1.f - sin2 * inv_sin_max * inv_sin_max);
+            float sin_al = safe_sqrt(1.f - cos_al * cos_al);
+            float sp, cp;
+            sincosf(uy * (2.f * kPi), &sp, &cp);
+            f3 fz = dc * -inv_dc, fs, ft;
+            onb(fz, fs, ft);
+            f3 dl = fs * (cp * sin_al) + ft * (sp * sin_al) + fz * cos_al;
+            p = dl * s.radius + c;
+            n = dl;
+            f3 dv = p - x;
+            ds.dist = length(dv);
+            ds.d = dv * (1.f / ds.dist);
+            ds.pdf = ds.dist == 0.f ? 0.f : (0.5f * kInvPi) / (1.f - cos_max);
+        } else {
+            float z = 1.f - 2.f * uy;
+            float r = safe_sqrt(1.f - z * z);
+            float sp, cp;
+            sincosf(2.f * kPi * ux, &sp, &cp);
+            f3 dl = mk(r * cp, r * sp, z);
+            p = dl * s.radius + c;
+            n = dl;
+            f3 dv = p - x;
+            float dist2 = dot(dv, dv);
+            ds.dist = sqrtf(dist2);
+            ds.d = dv * (1.f / ds.dist);
+            ds.pdf = (1.f / (4.f * kPi * s.radius * s.radius)) * dist2 / fabsf(dot(ds.d, n));
+        }
+        if (s.flip) n = -n;
+        ds.delta = false;
+        if (!(dot(ds.d, n) < 0.f && ds.pdf != 0.f)) return false;
+        ds.spec = mk(e.r, e.g, e.b) * (1.f / ds.pdf);
+    }
+    if (ne > 1) {
+        ds.pdf *= 1.f / (float)ne;
+        ds.spec = ds.spec * (float)ne;
+    }
+    return ds.pdf != 0.f;
+}
+
+// Fresnel equations for a dielectric (fresnel.h:34-80): reflectance, signed
+// cosine of the transmitted direction and the two relative indices.
+SMS_D float fresnel_full(float cos_i, float eta, float &cos_t, float &eta_it, float &eta_ti) {
+    bool outside = cos_i >= 0.f;
+    float rcp_eta = 1.f / eta;
+    eta_it = outside ? eta : rcp_eta;
+    eta_ti = outside ? rcp_eta : eta;
+    float ct2 = 1.f - (1.f - cos_i * cos_i) * (eta_ti * eta_ti);
+    float ci = fabsf(cos_i), ct = safe_sqrt(ct2);
+    float a_s = (ci - eta_it * ct) / (ci + eta_it * ct);
+    float a_p = (ct - eta_it * ci) / (ct + eta_it * ci);
+    float r = 0.5f * (a_s * a_s + a_p * a_p);
+    if (eta == 1.f) r = 0.f;
+    else if (ci == 0.f) r = 1.f;
+    cos_t = cos_i >= 0.f ? -ct : ct;
+    return r;
+}
+
+// Concentric square-to-disk map (Shirley and Chiu 1997, in the branch-free
+// form of warp.h:54-90) lifted to the cosine-weighted hemisphere.
+SMS_D f3 cosine_hemisphere(float u1, float u2) {
+    float x = 2.f * u1 - 1.f, y = 2.f * u2 - 1.f;
+    float r, phi;
+    if (x == 0.f && y == 0.f) {
+        r = 0.f; phi = 0.f;
+    } else if (fabsf(x) < fabsf(y)) {
+        r = y; phi = 0.5f * kPi - (x / y) * (0.25f * kPi);
+    } else {
+        r = x; phi = (y / x) * (0.25f * kPi);
+    }
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    float px = r * cp, py = r * sp;
+    return mk(px, py, safe_sqrt(1.f - px * px - py * py));
+}
+
+struct BsdfSample {
+    f3 wo, weight;
+    float pdf, eta;
+    bool delta;
+};
+
+// BSDF::sample of diffuse.cpp, dielectric.cpp, conductor.cpp (smooth),
+// radiance transport, local frame.  Returns false for a zero weight.
+SMS_D bool bsdf_sample(const DevShape &s, f3 wi, float u1, float u2, float u3, BsdfSample &bs) {
+    const float ci = wi.z;
+    if (s.bsdf_type == kBsdfDiffuse) {
+        if (!(ci > 0.f)) return false;
+        bs.wo = cosine_hemisphere(u2, u3);
+        bs.pdf = kInvPi * bs.wo.z;
+        bs.eta = 1.f;
+        bs.delta = false;
+        bs.weight = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
+        return bs.pdf > 0.f;
+    }
+    if (s.bsdf_type == kBsdfDielectric) {
+        float cos_t, eta_it, eta_ti;
+        float r = fresnel_full(ci, s.eta, cos_t, eta_it, eta_ti);
+        bs.delta = true;
+        if (u1 <= r) {
+            bs.wo = mk(-wi.x, -wi.y, wi.z);
+            bs.pdf = r;
+            bs.eta = 1.f;
+            bs.weight = splat(1.f);
+        } else {
+            bs.wo = mk(-eta_ti * wi.x, -eta_ti * wi.y, cos_t);
+            bs.pdf = 1.f - r;
+            bs.eta = eta_it;
+            bs.weight = splat(eta_ti * eta_ti);
+        }
+        return true;
+    }
+    // conductor
+    if (!(ci > 0.f)) return false;
+    bs.wo = mk(-wi.x, -wi.y, wi.z);
+    bs.pdf = 1.f;
+    bs.eta = 1.f;
+    bs.delta = true;
+    bs.weight = splat(fresnel_conductor(ci, s.eta, s.k));
+    return true;
+}
+
+// Caustic single-scatter flag of emitter e (used by the MNEE check).
+SMS_D bool emitter_is_caustic_ss(const DevScene &sc, int e) {
+    for (int k = 0; k < sc.n_emitters_ss; ++k)
+        if (sc.emitters_ss[k] == e) return true;
+    return false;
+}
+
+SMS_D Pcg32 load_rng(const PtState &S, uint32_t i) {
+    Pcg32 r;
+    r.state = S.rng_state[i];
+    r.inc = S.rng_inc[i];
+    return r;
+}
+SMS_D void store_rng(const PtState &S, uint32_t i, const Pcg32 &r) {
+    S.rng_state[i] = r.state;
+    S.rng_inc[i] = r.inc;
+}
+
+// ------------------------------------------------------------------ camera
+// Perspective sensor (perspective.cpp sample_ray) through a box-filtered pixel
+// sample; first intersection and directly visible emitters.
+__global__ void __launch_bounds__(kPtBlock) pt_camera_kernel(DevScene sc, PtCam cam, PtState S, uint64_t base,
+                                                             uint32_t n, uint64_t seed) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t g = base + i;
+    const uint64_t wh = (uint64_t)cam.width * (uint64_t)cam.height;
+    const uint32_t pix = (uint32_t)(g % wh);
+    const uint32_t px = pix % (uint32_t)cam.width, py = pix / (uint32_t)cam.width;
+    Pcg32 rng;
+    rng.seed(seed, g);
+    float ux = rng.next_f32(), uy = rng.next_f32();
+    (void)rng.next_f32();   // wavelength sample (integrator.cpp render_sample)
+    float sx = ((float)px + ux) / (float)cam.width, sy = ((float)py + uy) / (float)cam.height;
+    f3 dc = normalize(mk(cam.tx * (1.f - 2.f * sx), cam.ty * (1.f - 2.f * sy), 1.f));
+    float inv_z = 1.f / dc.z;
+    f3 d = normalize(mk(cam.m[0] * dc.x + cam.m[1] * dc.y + cam.m[2] * dc.z,
+                        cam.m[4] * dc.x + cam.m[5] * dc.y + cam.m[6] * dc.z,
+                        cam.m[8] * dc.x + cam.m[9] * dc.y + cam.m[10] * dc.z));
+    f3 o = mk(cam.m[3], cam.m[7], cam.m[11]);
+    Hit h;
+    uint32_t err = 0;
+    trace(sc, o, d, cam.near_clip * inv_z, cam.far_clip * inv_z, false, h, err);
+    f3 L = splat(0.f);
+    if (h.shape >= 0) {
+        const DevShape &s = sc.shapes[h.shape];
+        if (s.emitter >= 0) L = emitted(sc, s, o + d * h.t, d);
+    }
+    st3s(S.o, S.cap, i, o);
+    st3s(S.d, S.cap, i, d);
+    st3s(S.thr, S.cap, i, splat(1.f));
+    st3s(S.L, S.cap, i, L);
+    S.eta[i] = 1.f;
+    S.hit_t[i] = h.t; S.hit_u[i] = h.u; S.hit_v[i] = h.v;
+    S.hit_shape[i] = h.shape; S.hit_prim[i] = h.prim;
+    S.flags[i] = (h.shape >= 0 ? kAlive : 0) | kSpecularCamera;
+    store_rng(S, i, rng);
+}
+
+// ------------------------------------------------------------------ bounce
+template <bool kMneeCheck>
+__global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtParams P, PtState S, int depth,
+                                                             uint32_t n, DevCounters *ctr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    int want = 0, alive_out = 0;
+    uint32_t err = 0;
+    if (i < n && (S.flags[i] & kAlive)) {
+        int flags = S.flags[i];
+        Pcg32 rng = load_rng(S, i);
+        f3 o = ld3s(S.o, S.cap, i), d = ld3s(S.d, S.cap, i);
+        f3 thr = ld3s(S.thr, S.cap, i), L = ld3s(S.L, S.cap, i);
+        float eta = S.eta[i];
+        const int shape = S.hit_shape[i];
+        SurfPt si;
+        surface_at(sc, o, d, S.hit_t[i], shape, S.hit_prim[i], S.hit_u[i], S.hit_v[i], si);
+        const DevShape &s = sc.shapes[shape];
+        bool alive = true;
+        // Russian roulette (path.cpp:139-144; path_sms_ss.cpp:102-107)
+        if (depth > P.rr_depth) {
+            float q = fminf(hmax3(thr) * eta * eta, 0.95f);
+            float u = rng.next_f32();
+            if (P.integrator == SMS_INTEGRATOR_PATH ? !(u < q) : (u > q)) alive = false;
+            thr = thr * (1.f / q);
+        }
+        if ((uint32_t)depth >= (uint32_t)P.max_depth) alive = false;
+        if (alive) {
+            f3 fs, ft;
+            shading_frame(si, fs, ft);
+            const f3 n_sh = si.shn;
+            const f3 wiw = -d;
+            const f3 wi = mk(dot(wiw, fs), dot(wiw, ft), dot(wiw, n_sh));
+            const bool receiver = (s.flags & kShapeFlagReceiver) != 0;
+            bool on_caster = false;
+            if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & kShapeFlagCasterSingle) != 0;
+            else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS)
+                on_caster = (s.flags & (kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
+            const bool smooth = s.bsdf_type == kBsdfDiffuse;
+            const f3 albedo = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
+            // ---- SMS query of a receiver vertex (solved after this launch)
+            if (P.integrator != SMS_INTEGRATOR_PATH && receiver && !on_caster && smooth &&
+                (P.max_depth < 0 || depth + P.bounces < P.max_depth)) {
+                const float row[kStageRows] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
+                                               si.dp_du.x, si.dp_du.y, si.dp_du.z, si.dp_dv.x, si.dp_dv.y, si.dp_dv.z,
+                                               albedo.x, albedo.y, albedo.z, wi.z, thr.x, thr.y, thr.z};
+                #pragma unroll
+                for (int k = 0; k < kStageRows; ++k) S.stage[(size_t)k * S.cap + i] = row[k];
+                want = 1;
+            }
+            // ---- emitter sampling
+            bool nee = smooth && !on_caster;
+            if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS)
+                nee = nee || (depth == 1 && !P.disable_reflected_emitters);
+            if (nee) {
+                float ux = rng.next_f32(), uy = rng.next_f32();
+                DirSample ds;
+                if (sample_emitter_direction(sc, si.p, ux, uy, ds)) {
+                    Hit hs;
+                    float mint = kRayEps * (1.f + max_abs(si.p));
+                    bool occ = trace(sc, si.p, ds.d, mint, ds.dist * (1.f - kShadowEps), true, hs, err);
+                    if (!occ && smooth) {
+                        float co = dot(ds.d, n_sh);
+                        if (wi.z > 0.f && co > 0.f) {
+                            f3 bv = albedo * (kInvPi * co);
+                            float bpdf = kInvPi * co;
+                            float w = ds.delta ? 1.f : mis_weight(ds.pdf, bpdf);
+                            L = L + thr * bv * ds.spec * w;
+                        }
+                    }
+                }
+            }
+            // ---- BSDF sampling
+            float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
+            BsdfSample bs;
+            bool ok = bsdf_sample(s, wi, u1, u2, u3, bs);
+            if (ok) {
+                thr = thr * bs.weight;
+                eta *= bs.eta;
+                if (!bs.delta) flags &= ~kSpecularCamera;
+            }
+            if (!ok || (thr.x == 0.f && thr.y == 0.f && thr.z == 0.f)) {
+                alive = false;
+            } else {
+                f3 d2 = fs * bs.wo.x + ft * bs.wo.y + n_sh * bs.wo.z;
+                Hit h2;
+                trace(sc, si.p, d2, kRayEps * (1.f + max_abs(si.p)), INFINITY, false, h2, err);
+                if (h2.shape >= 0 && sc.shapes[h2.shape].emitter >= 0) {
+                    const DevShape &es = sc.shapes[h2.shape];
+                    const f3 ep = si.p + d2 * h2.t;
+                    const f3 Le = emitted(sc, es, ep, d2);
+                    bool allow = true;
+                    if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS)
+                        allow = !on_caster || (depth == 1 && !P.disable_reflected_emitters);
+                    else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS)
+                        allow = !on_caster || (flags & kSpecularCamera);
+                    if (allow) {
+                        float epdf = bs.delta ? 0.f : emitter_pdf(sc, es, si.p, ep, d2, h2.t);
+                        L = L + thr * Le * mis_weight(bs.pdf, epdf);
+                    } else if (kMneeCheck && (flags & kPrevReceiver) &&
+                               (sc.emitters[es.emitter].kind == 1) && emitter_is_caustic_ss(sc, es.emitter)) {
+                        // path_sms_ss.cpp:207-241: add the path unless the MNEE
+                        // walk from the previous vertex finds this very solution
+                        const f3 xp = ld3s(S.prev_p, S.cap, i);
+                        Vtx v;
+                        int it;
+                        LaneStats st;
+                        bool found = ss_walk(sc, P.solver, shape, xp, ep, si.p, v, it, err, st);
+                        if (found) {
+                            f3 dpt = normalize(si.p - xp), dmn = normalize(v.p - xp);
+                            found = fabsf(dot(dpt, dmn) - 1.f) < P.solver.uniqueness_threshold;
+                        }
+                        if (!found) L = L + thr * Le;
+                    }
+                }
+                st3s(S.prev_p, S.cap, i, si.p);
+                flags = receiver ? (flags | kPrevReceiver) : (flags & ~kPrevReceiver);
+                st3s(S.o, S.cap, i, si.p);
+                st3s(S.d, S.cap, i, d2);
+                S.hit_t[i] = h2.t; S.hit_u[i] = h2.u; S.hit_v[i] = h2.v;
+                S.hit_shape[i] = h2.shape; S.hit_prim[i] = h2.prim;
+                alive = h2.shape >= 0;
+            }
+        }
+        st3s(S.thr, S.cap, i, thr);
+        st3s(S.L, S.cap, i, L);
+        S.eta[i] = eta;
+        S.flags[i] = alive ? (flags | kAlive) : (flags & ~kAlive);
+        store_rng(S, i, rng);
+        alive_out = alive;
+    }
+    if (i < n) S.want[i] = want;
+    const int bq = __syncthreads_count(want);
+    const int ba = __syncthreads_count(alive_out);
+    if (threadIdx.x == 0) {
+        S.block_q[blockIdx.x] = (uint32_t)bq;
+        S.block_a[blockIdx.x] = (uint32_t)ba;
+    }
+    if (err) atomicOr(&ctr->error, err);
+}
+
+// ------------------------------------------------------------ compaction
+// Exclusive prefix sum of the per-block query counts (one block, in order)
+// and the totals of queries and live paths.
+__global__ void __launch_bounds__(1024) pt_scan_kernel(PtState S, uint32_t n_blocks) {
+    __shared__ uint32_t warp_sum[32];
+    __shared__ uint32_t carry;
+    __shared__ uint32_t alive_sum;
+    if (threadIdx.x == 0) { carry = 0; alive_sum = 0; }
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t alive_local = 0;
+    for (uint32_t b0 = 0; b0 < n_blocks; b0 += 1024) {
+        const uint32_t b = b0 + threadIdx.x;
+        const uint32_t v = b < n_blocks ? S.block_q[b] : 0u;
+        alive_local += b < n_blocks ? S.block_a[b] : 0u;
+        uint32_t x = v;
+        #pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if ((int)lane >= off) x += y;
+        }
+        if (lane == 31) warp_sum[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t w = warp_sum[lane];
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+                if ((int)lane >= off) w += y;
+            }
+            warp_sum[lane] = w;   // inclusive
+        }
+        __syncthreads();
+        const uint32_t before = carry + (wid ? warp_sum[wid - 1] : 0u) + x - v;
+        if (b < n_blocks) S.block_q[b] = before;   // now the block's offset
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sum[31];
+        __syncthreads();
+    }
+    atomicAdd(&alive_sum, alive_local);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        S.totals[0] = carry;
+        S.totals[1] = alive_sum;
+    }
+}
+
+// Staged queries -> SMS query batch (SoA with the batch size as stride), in
+// path order; map[k] = path of query k (also its random-number stream).
+__global__ void __launch_bounds__(kPtBlock) pt_gather_kernel(PtState S, uint32_t n) {
+    __shared__ uint32_t warp_cnt[kPtBlock / 32];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = i < n ? S.want[i] : 0;
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, w);
+    if (lane == 0) warp_cnt[wid] = __popc(m);
+    __syncthreads();
+    if (!w) return;
+    uint32_t r = S.block_q[blockIdx.x] + __popc(m & ((1u << lane) - 1u));
+    for (unsigned k = 0; k < wid; ++k) r += warp_cnt[k];
+    const uint32_t nq = S.totals[0];
+    #pragma unroll
+    for (int k = 0; k < 16; ++k) S.q[(size_t)k * nq + r] = S.stage[(size_t)k * S.cap + i];
+    S.map[r] = i;
+}
+
+__global__ void __launch_bounds__(kPtBlock) pt_sms_add_kernel(PtState S, uint32_t nq) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nq) return;
+    const uint32_t i = S.map[r];
+    f3 w = mk(S.stage[(size_t)16 * S.cap + i], S.stage[(size_t)17 * S.cap + i], S.stage[(size_t)18 * S.cap + i]);
+    f3 v = mk(S.value[r], S.value[(size_t)nq + r], S.value[2 * (size_t)nq + r]);
+    st3s(S.L, S.cap, i, ld3s(S.L, S.cap, i) + w * v);
+}
+
+// image[pix0 + j] += sum over the chunk's samples k of L[k * n_pix + j].
+__global__ void __launch_bounds__(kPtBlock) pt_resolve_kernel(PtState S, float *image, uint32_t pix0,
+                                                              uint32_t n_pix, uint32_t n_samples) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_pix) return;
+    f3 acc = splat(0.f);
+    for (uint32_t k = 0; k < n_samples; ++k) acc = acc + ld3s(S.L, S.cap, k * n_pix + j);
+    float *px = image + 3 * (size_t)(pix0 + j);
+    px[0] += acc.x; px[1] += acc.y; px[2] += acc.z;
+}
+
+__global__ void pt_scale_kernel(float *image, size_t n, float s) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) image[i] *= s;
+}
+
+sms_status rfail(sms_status st, const std::string &msg) {
+    return (sms_status)set_last_error_impl((int)st, msg.c_str());
+}
+
+#define PT_TRY(call)                                                                         \
+    do {                                                                                     \
+        cudaError_t _e = (call);                                                             \
+        if (_e != cudaSuccess) {                                                             \
+            st = rfail(SMS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));    \
+            goto done;                                                                       \
+        }                                                                                    \
+    } while (0)
+
+}  // namespace
+
+}  // namespace sms
+
+using namespace sms;
+
+extern "C" void sms_render_options_default(sms_render_options *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->integrator = SMS_INTEGRATOR_PATH_SMS_SS;
+    o->max_depth = -1;
+    o->rr_depth = 5;
+    o->spp = 1;
+}
+
+extern "C" uint64_t sms_render_sms_seed(uint64_t seed, int32_t depth) {
+    // SplitMix64 (Steele, Lea and Flood 2014) of seed + depth * golden gamma
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(uint32_t)(depth + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static bool camera_params(const sms_camera *c, PtCam &out, std::string &why) {
+    if (c->width <= 0 || c->height <= 0) { why = "film size must be positive"; return false; }
+    if (!(c->fov > 0.f && c->fov < 180.f)) { why = "fov must lie in (0, 180) degrees"; return false; }
+    const double aspect = (double)c->width / (double)c->height;
+    const double t = std::tan(0.5 * (double)c->fov * M_PI / 180.0);
+    double tx;
+    switch (c->fov_axis) {
+        case SMS_FOV_X: tx = t; break;
+        case SMS_FOV_Y: tx = t * aspect; break;
+        case SMS_FOV_DIAGONAL: tx = t / std::sqrt(1.0 + 1.0 / (aspect * aspect)); break;
+        case SMS_FOV_SMALLER: tx = aspect >= 1.0 ? t * aspect : t; break;
+        case SMS_FOV_LARGER: tx = aspect >= 1.0 ? t : t * aspect; break;
+        default: why = "unknown fov_axis"; return false;
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 4; ++k) out.m[4 * r + k] = c->to_world[4 * r + k];
+    out.tx = (float)tx;
+    out.ty = (float)(tx / aspect);
+    out.near_clip = c->near_clip > 0.f ? c->near_clip : 1e-2f;
+    out.far_clip = c->far_clip > out.near_clip ? c->far_clip : 1e4f;
+    out.width = c->width;
+    out.height = c->height;
+    return true;
+}
+
+extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const sms_render_options *opt,
+                                        float *image) {
+    if (!c || !cam || !opt || !image) return rfail(SMS_ERR_INVALID_ARG, "sms_render_device: null argument");
+    CtxView v;
+    if (!ctx_view(c, v)) return rfail(SMS_ERR_INVALID_ARG, "sms_render_device: bad context");
+    PtCam pc;
+    std::string why;
+    if (!camera_params(cam, pc, why)) return rfail(SMS_ERR_INVALID_ARG, "sms_render: " + why);
+    if (opt->spp <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: spp must be positive");
+    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_SMS_MS)
+        return rfail(SMS_ERR_INVALID_ARG, "sms_render: unknown integrator");
+    if (opt->rr_depth <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: rr_depth must be positive");
+    if (opt->max_depth < -1) return rfail(SMS_ERR_INVALID_ARG, "sms_render: max_depth must be -1 or >= 0");
+    if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee)
+        return rfail(SMS_ERR_UNSUPPORTED, "path_sms_ms: unbiased MNEE (mnee_init without biased_mnee) is not "
+                                          "implemented");
+    PtParams P{};
+    P.integrator = opt->integrator;
+    P.max_depth = opt->max_depth;
+    P.rr_depth = opt->rr_depth;
+    P.disable_reflected_emitters = opt->disable_reflected_emitters;
+    P.biased_mnee = opt->biased_mnee;
+    P.bounces = opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS ? v.bounces : 1;
+    P.mnee_check = opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee;
+    P.seed = opt->seed;
+    P.solver = v.solver;
+
+    const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
+    const uint64_t total = wh * (uint64_t)opt->spp;
+    uint32_t cap = opt->max_paths ? opt->max_paths : kPtDefaultPaths;
+    if (wh <= cap) cap = (uint32_t)(std::min<uint64_t>(cap / wh, (uint64_t)opt->spp) * wh);
+    cap = std::max<uint32_t>(cap, 1u);
+    const uint32_t n_blocks_cap = (cap + kPtBlock - 1) / kPtBlock;
+
+    // one device block for the whole path state
+    size_t bytes = 0;
+    auto take = [&](size_t b) { size_t o = bytes; bytes += (b + 255) & ~(size_t)255; return o; };
+    const size_t o_rs = take(8 * (size_t)cap), o_ri = take(8 * (size_t)cap), o_o = take(12 * (size_t)cap),
+                 o_d = take(12 * (size_t)cap), o_thr = take(12 * (size_t)cap), o_L = take(12 * (size_t)cap),
+                 o_pp = take(12 * (size_t)cap), o_eta = take(4 * (size_t)cap), o_ht = take(4 * (size_t)cap),
+                 o_hu = take(4 * (size_t)cap), o_hv = take(4 * (size_t)cap), o_hs = take(4 * (size_t)cap),
+                 o_fl = take(4 * (size_t)cap), o_hp = take(4 * (size_t)cap),
+                 o_st = take(4 * (size_t)kStageRows * cap), o_w = take(4 * (size_t)cap),
+                 o_bq = take(4 * (size_t)n_blocks_cap), o_ba = take(4 * (size_t)n_blocks_cap), o_tot = take(16),
+                 o_q = take(4 * (size_t)SMS_QUERY_FIELDS * cap), o_map = take(4 * (size_t)cap),
+                 o_val = take(12 * (size_t)cap), o_cnt = take(4 * (size_t)cap), o_wk = take(4 * (size_t)cap);
+    char *blk = nullptr;
+    uint32_t *host_tot = nullptr;
+    sms_status st = SMS_OK;
+    cudaStream_t s = v.stream;
+    PtState S{};
+    uint64_t g0 = 0;
+    const size_t img_n = 3 * (size_t)wh;
+    PT_TRY(cudaSetDevice(v.device));
+    PT_TRY(cudaMalloc(&blk, bytes));
+    PT_TRY(cudaMallocHost(&host_tot, 2 * sizeof(uint32_t)));
+    S.rng_state = reinterpret_cast<uint64_t *>(blk + o_rs);
+    S.rng_inc = reinterpret_cast<uint64_t *>(blk + o_ri);
+    S.o = reinterpret_cast<float *>(blk + o_o);
+    S.d = reinterpret_cast<float *>(blk + o_d);
+    S.thr = reinterpret_cast<float *>(blk + o_thr);
+    S.L = reinterpret_cast<float *>(blk + o_L);
+    S.prev_p = reinterpret_cast<float *>(blk + o_pp);
+    S.eta = reinterpret_cast<float *>(blk + o_eta);
+    S.hit_t = reinterpret_cast<float *>(blk + o_ht);
+    S.hit_u = reinterpret_cast<float *>(blk + o_hu);
+    S.hit_v = reinterpret_cast<float *>(blk + o_hv);
+    S.hit_shape = reinterpret_cast<int *>(blk + o_hs);
+    S.flags = reinterpret_cast<int *>(blk + o_fl);
+    S.hit_prim = reinterpret_cast<uint32_t *>(blk + o_hp);
+    S.stage = reinterpret_cast<float *>(blk + o_st);
+    S.want = reinterpret_cast<int *>(blk + o_w);
+    S.block_q = reinterpret_cast<uint32_t *>(blk + o_bq);
+    S.block_a = reinterpret_cast<uint32_t *>(blk + o_ba);
+    S.totals = reinterpret_cast<uint32_t *>(blk + o_tot);
+    S.q = reinterpret_cast<float *>(blk + o_q);
+    S.map = reinterpret_cast<uint32_t *>(blk + o_map);
+    S.value = reinterpret_cast<float *>(blk + o_val);
+    S.count = reinterpret_cast<int *>(blk + o_cnt);
+    S.walks = reinterpret_cast<int *>(blk + o_wk);
+    S.cap = cap;
+    PT_TRY(cudaMemsetAsync(image, 0, img_n * sizeof(float), s));
+    while (g0 < total) {
+        uint32_t n;
+        if (wh <= cap) n = (uint32_t)std::min<uint64_t>(cap, total - g0);
+        else n = (uint32_t)std::min<uint64_t>(cap, wh - g0 % wh);
+        const uint32_t nb = (n + kPtBlock - 1) / kPtBlock;
+        pt_camera_kernel<<<nb, kPtBlock, 0, s>>>(*v.scene, pc, S, g0, n, P.seed);
+        PT_TRY(cudaGetLastError());
+        for (int depth = 1;; ++depth) {
+            if (depth > kPtHardDepth) {
+                st = rfail(SMS_ERR_DEVICE_LIMIT, "sms_render: a path exceeded 4096 bounces (raise rr pressure or "
+                                                 "bound max_depth)");
+                goto done;
+            }
+            if (P.mnee_check) pt_bounce_kernel<true><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters);
+            else pt_bounce_kernel<false><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters);
+            PT_TRY(cudaGetLastError());
+            pt_scan_kernel<<<1, 1024, 0, s>>>(S, nb);
+            PT_TRY(cudaGetLastError());
+            pt_gather_kernel<<<nb, kPtBlock, 0, s>>>(S, n);
+            PT_TRY(cudaGetLastError());
+            PT_TRY(cudaMemcpyAsync(host_tot, S.totals, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            PT_TRY(cudaStreamSynchronize(s));
+            const uint32_t nq = host_tot[0], n_alive = host_tot[1];
+            if (nq) {
+                sms_result r{S.value, S.count, S.walks};
+                const uint64_t sseed = sms_render_sms_seed(P.seed, depth);
+                st = P.integrator == SMS_INTEGRATOR_PATH_SMS_MS
+                         ? ctx_ms_connect(c, S.q, nq, sseed, g0, S.map, &r)
+                         : ctx_ss_connect(c, S.q, nq, sseed, g0, S.map, &r);
+                if (st) goto done;
+                pt_sms_add_kernel<<<(nq + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, nq);
+                PT_TRY(cudaGetLastError());
+            }
+            if (n_alive == 0) break;
+        }
+        {
+            const uint32_t n_pix = (uint32_t)std::min<uint64_t>(n, wh);
+            const uint32_t pix0 = (uint32_t)(g0 % wh);
+            pt_resolve_kernel<<<(n_pix + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, image, pix0, n_pix,
+                                                                                     n / n_pix);
+            PT_TRY(cudaGetLastError());
+        }
+        g0 += n;
+    }
+    pt_scale_kernel<<<(unsigned)((img_n + 255) / 256), 256, 0, s>>>(image, img_n, 1.f / (float)opt->spp);
+    PT_TRY(cudaGetLastError());
+    st = ctx_check_device_error(c);
+done:
+    if (blk) {
+        cudaStreamSynchronize(s);
+        cudaFree(blk);
+    }
+    if (host_tot) cudaFreeHost(host_tot);
+    return st;
+}
+
+extern "C" sms_status sms_render(sms_ctx *c, const sms_camera *cam, const sms_render_options *opt, float *image) {
+    if (!c || !cam || !opt || !image) return rfail(SMS_ERR_INVALID_ARG, "sms_render: null argument");
+    if (cam->width <= 0 || cam->height <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: bad film size");
+    CtxView v;
+    if (!ctx_view(c, v)) return rfail(SMS_ERR_INVALID_ARG, "sms_render: bad context");
+    const size_t bytes = 3 * (size_t)cam->width * (size_t)cam->height * sizeof(float);
+    float *dimg = nullptr;
+    cudaError_t e = cudaSetDevice(v.device);
+    if (e == cudaSuccess) e = cudaMalloc(&dimg, bytes);
+    if (e != cudaSuccess) return rfail(SMS_ERR_CUDA, std::string("sms_render: ") + cudaGetErrorString(e));
+    sms_status st = sms_render_device(c, cam, opt, dimg);
+    if (st == SMS_OK) {
+        e = cudaMemcpyAsync(image, dimg, bytes, cudaMemcpyDeviceToHost, v.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(v.stream);
+        if (e != cudaSuccess) st = rfail(SMS_ERR_CUDA, std::string("sms_render: ") + cudaGetErrorString(e));
+    }
+    cudaFree(dimg);
+    return st;
+}

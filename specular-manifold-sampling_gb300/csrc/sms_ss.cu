@@ -35,60 +35,6 @@
 
 namespace sms {
 
-// ------------------------------------------------------------------- walk
-// sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
-// explicit seed point.  Returns ok; v holds the solution vertex.
-SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
-                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr) {
-    f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
-    Hit h;
-    trace(sc, x, d, kRayEps, INFINITY, false, h, err);
-    st.ray(h);
-    it = 0;
-    if (h.shape < 0) return false;
-    vertex_from_hit(sc, x, d, h, v);
-    if (p_init) *p_init = v.p;
-    if (h.shape != caster) return false;
-    float beta = 1.f;
-    bool accepted = false, conv = false;
-    while (it < cfg.max_iterations) {
-        float c0, c1, dx0, dx1;
-        bool sok = cfg.halfvector ? step_halfvector(x, v, lp, c0, c1, dx0, dx1)
-                                  : step_anglediff(x, v, lp, c0, c1, dx0, dx1);
-        if (!sok) break;
-        if (sqrtf(c0 * c0 + c1 * c1) < cfg.solver_threshold) { conv = true; break; }
-        f3 pp = v.p - (v.dp_du * dx0 + v.dp_dv * dx1) * (cfg.step_scale * beta);
-        f3 dd = normalize(pp - x);
-        trace(sc, x, dd, kRayEps, INFINITY, false, h, err);
-        st.ray(h);
-        it++;
-        if (h.shape < 0 || h.shape != v.shape) {
-            beta = 0.5f * beta;
-            accepted = false;
-            continue;
-        }
-        beta = fminf(1.f, 2.f * beta);
-        vertex_from_hit(sc, x, dd, h, v);
-        accepted = true;
-    }
-    // newton_solver returns si_current: valid only after an accepted step.
-    if (!(conv && accepted)) return false;
-    f3 wx = normalize(x - v.p), wy = normalize(lp - v.p);
-    bool refraction = dot(v.gn, wx) * dot(v.gn, wy) < 0.f;
-    return (v.eta == 1.f) ? !refraction : refraction;
-}
-
-// evaluate_path_contribution (manifold_ss.cpp:281-327) for a flat receiver.
-SMS_D f3 contribution(const DevScene &sc, f3 x, const Light &L, const Vtx &sol, uint32_t &err, LaneStats &st) {
-    Vtx vt = sol;
-    make_orthonormal(vt.dp_du, vt.dp_dv, vt.dn_du, vt.dn_dv);
-    f3 yp, ydu, ydv, lw, lp;
-    if (!emitter_endpoint(sc, L, vt.p, yp, ydu, ydv, lw, lp, err, st)) return splat(0.f);
-    float F = specular_reflectance(sc.shapes[vt.shape], vt.n, normalize(lp - vt.p));
-    F *= geometric_term(x, vt, yp, ydu, ydv);
-    return lw * F;
-}
-
 // ------------------------------------------------------------ walk kernel
 __global__ void __launch_bounds__(128) ss_walk_kernel(DevScene sc, SolverCfg cfg, int caster,
                                                       const float *__restrict__ q, const float *__restrict__ w,
@@ -150,7 +96,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
         bool have_light = false;
         if (live) {
             Q = load_query(qs, n, qi);
-            Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+            Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
             have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
         }
         bool work = live && have_light && sc.n_casters_ss > 0;
@@ -166,7 +112,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
                 bool cand = false;
                 f3 dir = splat(0.f), contrib = splat(0.f);
                 if (work && m < M) {
-                    Pcg32 rng = query_rng(seed, stream_off + qi, 3u + 2u * ((uint64_t)c * M + m));
+                    Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + 2u * ((uint64_t)c * M + m));
                     float sx = rng.next_f32(), sy = rng.next_f32();
                     f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
                     Vtx v;
@@ -235,8 +181,8 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
 // (cdf, means, sigmas) for the first-walk and trial kernels.  Kept apart from
 // the first-walk kernel so that kernel keeps the walk kernels' occupancy (the
 // network needs 168 registers and 66 KB of shared memory per block).
-__global__ void __launch_bounds__(128, 3) ss_proposal_kernel(DevScene sc, const float *__restrict__ qs, uint32_t n,
-                                                             uint64_t seed, uint64_t stream_off,
+__global__ void __launch_bounds__(128, 3) ss_proposal_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
+                                                             uint32_t n, uint64_t seed, uint64_t stream_off,
                                                              mlp::SeedProposal pr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int kStage = 16 * mlp::kXLd / 2;   // floats: input tile, then output rows
@@ -254,7 +200,7 @@ __global__ void __launch_bounds__(128, 3) ss_proposal_kernel(DevScene sc, const 
         f3 fx = splat(0.f), fl = splat(0.f), fn = splat(0.f);
         if (active) {
             const Query Q = load_query(qs, n, qi);
-            Pcg32 rng = query_rng(seed, stream_off + qi, 0);
+            Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
             Light L;
             fx = Q.x;
             fn = Q.n;
@@ -310,7 +256,7 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
     bool have_light = false;
     if (active) {
         Q = load_query(qs, n, qi);
-        rng = query_rng(seed, stream_off + qi, 0);
+        rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
         have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
     }
     if (active) {
@@ -427,7 +373,7 @@ __global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCf
                 have = true;
                 qi = scr.list[idx];
                 Q = load_query(qs, n, qi);
-                base = query_rng(seed, stream_off + qi, 0);
+                base = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
                 sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, base, Q.x, L);   // base sits at position 3
                 pos = scr.pos[qi];
                 dir0 = mk(scr.dir0[qi], scr.dir0[(size_t)n + qi], scr.dir0[2 * (size_t)n + qi]);
@@ -528,7 +474,7 @@ __global__ void __launch_bounds__(128) ss_collect_kernel(DevScene sc, SolverCfg 
     bool have_light = false;
     if (qi < n) {
         Q = load_query(qs, n, qi);
-        rng = query_rng(seed, stream_off + qi, 0);
+        rng = query_rng(seed, query_stream(cfg, stream_off, qi), 0);
         have_light = sample_emitter(sc, sc.emitters_ss, sc.n_emitters_ss, rng, Q.x, L);
     }
     f3 seen[kCollectUnique];     // directions of the solutions kept so far
@@ -624,7 +570,7 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
             e = cudaFuncSetAttribute(ss_proposal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
             const uint32_t pblocks = std::min<uint32_t>((n + 127) / 128, (uint32_t)num_sms * 3);
-            ss_proposal_kernel<<<pblocks, 128, smem, s>>>(sc, q, n, seed, stream_off, pr);
+            ss_proposal_kernel<<<pblocks, 128, smem, s>>>(sc, cfg, q, n, seed, stream_off, pr);
             ss_first_kernel<true><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value,
                                                                   count, walks, scr, ctr, pr);
         } else {

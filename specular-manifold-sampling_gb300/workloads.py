@@ -36,7 +36,7 @@ import math
 import numpy as np
 
 from . import (BSDF_CONDUCTOR, BSDF_DIELECTRIC, BSDF_DIFFUSE, EMITTER_CAUSTIC_MULTI, EMITTER_CAUSTIC_SINGLE,
-               SHAPE_CAUSTIC_BOUNCER, SHAPE_CAUSTIC_CASTER_MULTI, SHAPE_CAUSTIC_CASTER_SINGLE, SHAPE_GLINTY,
+               SHAPE_CAUSTIC_BOUNCER, SHAPE_CAUSTIC_RECEIVER, SHAPE_CAUSTIC_CASTER_MULTI, SHAPE_CAUSTIC_CASTER_SINGLE, SHAPE_GLINTY,
                QUERY_FIELDS, Bsdf, SceneDesc, SMSConfig)
 
 _MUL = np.uint64(6364136223846793005)
@@ -188,6 +188,37 @@ def water_queries(n: int, seed: int = 3, first: int = 0) -> np.ndarray:
 
 def water_config() -> SMSConfig:
     return SMSConfig(biased=False, max_trials=256, max_iterations=20)
+
+
+# ------------------------------------------------------------------- pool
+def pool_scene(res: int = 128, light_radius: float = 0.5, light_z: float = 4.0, radiance: float = 40.0,
+               point_light: bool = False, floor_albedo: float = 0.5, wave_scale: float = 1.0) -> SceneDesc:
+    """Rendering scene: the water heightfield of water_scene with its wave
+    amplitudes scaled by wave_scale (0: flat; res x res grid over [-1, 1]^2
+    around z = 1, dielectric 1.33, caustic_caster_single) over a
+    diffuse floor z = 0 on [-2, 2]^2 (caustic_receiver), lit by a sphere area
+    light (or a point light of intensity radiance * light_radius^2 * pi at the
+    same place), flagged caustic_emitter_single."""
+    d = SceneDesc()
+    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
+    fuv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32),
+               Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (floor_albedo,) * 3), SHAPE_CAUSTIC_RECEIVER, UV=fuv)
+    waves = [(a * wave_scale, kx, ky, ph) for (a, kx, ky, ph) in water_params()] if wave_scale > 0 else []
+    P, N, UV, F = heightfield_mesh(res, 1.0, 1.0, waves)
+    d.add_mesh(P, F, Bsdf(BSDF_DIELECTRIC, 1.33), SHAPE_CAUSTIC_CASTER_SINGLE, N=N, UV=UV)
+    if point_light:
+        I = radiance * math.pi * light_radius * light_radius
+        d.add_point_emitter((0.0, 0.0, light_z), (I, I, I), EMITTER_CAUSTIC_SINGLE)
+    else:
+        light = d.add_sphere((0.0, 0.0, light_z), light_radius, Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+        d.add_area_emitter(light, (radiance,) * 3, EMITTER_CAUSTIC_SINGLE)
+    return d
+
+
+def pool_camera(width: int = 64, height: int = 64, fov: float = 40.0):
+    from . import Camera
+    return Camera.look_at((0.0, -3.2, 3.6), (0.0, 0.0, 0.4), (0.0, 0.0, 1.0), fov, width, height)
 
 
 # ------------------------------------------------------------------- slab

@@ -1,0 +1,168 @@
+"""GPU path tracer (sms_render) against the oracle's restatement and against
+plain path tracing.  Both implementations draw every random number from the
+same PCG32 streams (keyed by path index), so most pixels agree to float
+rounding; the few paths whose discrete choices (Russian roulette, Fresnel lobe,
+Newton basin) flip under FP32 rounding differences make the rest, which the
+image means absorb."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PIXEL_RTOL = 1e-3
+
+
+def _blocks(img, b):
+    h, w = img.shape[:2]
+    return img[..., 0].reshape(h // b, b, w // b, b).mean(axis=(1, 3))
+
+
+def _agree(a, b):
+    return np.mean(np.abs(a - b) <= PIXEL_RTOL * np.maximum(np.abs(b), 1e-3))
+
+
+@pytest.mark.parametrize("integrator", ["path", "path_sms_ss"])
+def test_render_matches_oracle(sms, workloads, oracle, gpu_lib, integrator):
+    W = workloads
+    desc = W.pool_scene(res=32)
+    cfg = W.water_config()
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    cam = W.pool_camera(16, 16)
+    opt = sms.RenderOptions(integrator=integrator, spp=8, seed=11)
+    g = ctx.render(cam, opt)
+    o = oracle.OracleScene(desc).render(cfg, cam, opt)
+    assert np.isfinite(g).all()
+    agree = _agree(g, o)
+    assert agree > (0.97 if integrator == "path" else 0.9), agree
+    # a divergent unbiased-SMS sample carries a heavy-tailed weight (its
+    # Bernoulli-trial count), so compare robust statistics of the images
+    assert abs(np.median(g) - np.median(o)) <= 1e-3 * np.median(o) + 1e-6
+    far = np.abs(g - o) > 0.5 * np.maximum(np.abs(o), 1e-2)
+    assert far.mean() < 0.05
+    ctx.close()
+
+
+def test_render_biased_and_point_light_match_oracle(sms, workloads, oracle, gpu_lib):
+    W = workloads
+    desc = W.pool_scene(res=32, point_light=True)
+    cfg = sms.SMSConfig(biased=True, max_trials=16)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    cam = W.pool_camera(16, 16)
+    opt = sms.RenderOptions(integrator="path_sms_ss", spp=4, seed=5)
+    g = ctx.render(cam, opt)
+    o = oracle.OracleScene(desc).render(cfg, cam, opt)
+    assert _agree(g, o) > 0.9
+    assert abs(g.mean() - o.mean()) < 0.03 * o.mean()    # biased estimator: bounded weights
+    ctx.close()
+
+
+def test_render_is_deterministic_and_wavefront_invariant(sms, workloads, gpu_lib):
+    """Random numbers are keyed by path index: the same image from two runs,
+    and (up to the order of the per-pixel sums) from a wavefront size that
+    splits the samples of a pixel across launches."""
+    W = workloads
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=32)), W.water_config())
+    cam = W.pool_camera(24, 16)
+    a = ctx.render(cam, sms.RenderOptions(spp=6, seed=2))
+    b = ctx.render(cam, sms.RenderOptions(spp=6, seed=2))
+    c = ctx.render(cam, sms.RenderOptions(spp=6, seed=2, max_paths=1000))
+    assert np.array_equal(a, b)
+    assert np.allclose(a, c, rtol=1e-5, atol=1e-6)
+    d = ctx.render(cam, sms.RenderOptions(spp=6, seed=3))
+    assert not np.array_equal(a, d)
+    ctx.close()
+
+
+def _compare_integrators(sms, ctx, cam, integ, spp_path, spp_sms, reps, block=4, rel=0.02):
+    """Plain path tracing vs integrator `integ` on 4x4-pixel blocks: the
+    difference of the means must lie within 5 standard errors (from the
+    spread of `reps` independent runs) plus `rel` of the value."""
+    runs = {}
+    for name, spp in (("path", spp_path), (integ, spp_sms)):
+        runs[name] = np.stack([_blocks(ctx.render(cam, sms.RenderOptions(integrator=name, spp=spp, seed=900 + r)),
+                                       block) for r in range(reps)])
+    a, b = runs["path"], runs[integ]
+    se = np.sqrt(a.var(0, ddof=1) / reps + b.var(0, ddof=1) / reps)
+    diff = np.abs(a.mean(0) - b.mean(0))
+    assert np.all(diff < 5.0 * se + rel * a.mean(0) + 1e-3), (a.mean(0), b.mean(0), se)
+    assert abs(a.mean() - b.mean()) < rel * a.mean()
+
+
+def test_path_sms_ss_is_unbiased_against_path(sms, workloads, gpu_lib):
+    """Flat water: unbiased SMS + the integrator's path filtering estimate the
+    same image as plain path tracing."""
+    W = workloads
+    cfg = W.water_config()
+    cfg.max_trials = -1
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=32, wave_scale=0.0)), cfg)
+    _compare_integrators(sms, ctx, W.pool_camera(32, 32), "path_sms_ss", 4096, 512, 4)
+    ctx.close()
+
+
+def test_unbiased_mnee_is_unbiased_against_path(sms, workloads, gpu_lib):
+    """mnee_init without biased_mnee (path_sms_ss.cpp:207-241): paths the
+    deterministic MNEE walk cannot find are added from BSDF sampling."""
+    W = workloads
+    cfg = W.water_config()
+    cfg.mnee_init = True
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=32, wave_scale=0.0)), cfg)
+    _compare_integrators(sms, ctx, W.pool_camera(32, 32), "path_sms_ss", 4096, 512, 4)
+    ctx.close()
+
+
+def test_path_sms_ms_matches_path_on_flat_slab(sms, workloads, gpu_lib):
+    """Two-bounce chains through a flat glass slab over the floor: path_sms_ms
+    (bounces = 2, unbiased) against plain path tracing.  Paths that reflect
+    inside the slab are filtered and not re-sampled (as in the reference), a
+    loss below 1% here, inside the 2% tolerance."""
+    d = sms.SceneDesc()
+    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
+    d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3),
+               sms.SHAPE_CAUSTIC_RECEIVER, UV=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
+    W = workloads
+    glass = sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)
+    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.3, [])
+    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.0, [], flip_normals=True)
+    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_BOUNCER, N=N, UV=UV)
+    light = d.add_sphere((0.0, 0.0, 4.0), 0.5, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+    d.add_area_emitter(light, (40.0,) * 3, sms.EMITTER_CAUSTIC_MULTI)
+    cfg = sms.SMSConfig(biased=False, max_trials=-1, bounces=2)
+    ctx = sms.Context(sms.Scene(d), cfg)
+    _compare_integrators(sms, ctx, W.pool_camera(32, 32), "path_sms_ms", 4096, 512, 4)
+    ctx.close()
+
+
+def test_render_with_learned_proposal(sms, workloads, gpu_lib):
+    """A bound learned proposal seeds the SMS calls of the path tracer."""
+    import torch
+    W = workloads
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=32)), W.water_config())
+    q = torch.from_numpy(W.water_queries(8192, seed=4)).cuda()
+    torch.cuda.synchronize()
+    prop = sms.SeedProposal(ctx, 1, seed=1, capacity=1 << 15)
+    assert prop.collect(q.data_ptr(), 8192, seed=4, walks_per_query=4) > 0
+    prop.normalize()
+    prop.train(steps=50, batch=1024)
+    ctx.set_proposal(prop, 0.1)
+    img = ctx.render(W.pool_camera(16, 16), sms.RenderOptions(spp=4, seed=1))
+    assert np.isfinite(img).all() and img.mean() > 0.0
+    ctx.set_proposal(None)
+    prop.close()
+    ctx.close()
+
+
+def test_render_argument_errors(sms, workloads, gpu_lib):
+    W = workloads
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=16)), sms.SMSConfig(mnee_init=True, bounces=2))
+    with pytest.raises(sms.SMSError) as e:
+        ctx.render(W.pool_camera(8, 8), sms.RenderOptions(integrator="path_sms_ms"))
+    assert e.value.status == 4
+    with pytest.raises(sms.SMSError) as e:
+        ctx.render(W.pool_camera(8, 8), sms.RenderOptions(spp=0))
+    assert e.value.status == 1
+    cam = W.pool_camera(8, 8)
+    cam.fov = 0.0
+    with pytest.raises(sms.SMSError):
+        ctx.render(cam, sms.RenderOptions())
+    ctx.close()

@@ -1,0 +1,83 @@
+"""CPU checks of the path-tracer restatement in the oracle (the checker of the
+library's sms_render): integrator identities, unbiasedness of path_sms_ss
+against plain path tracing on a scene where SMS finds every solution, and the
+camera convention."""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def O():
+    from oracle import oracle
+    return oracle
+
+
+def _blocks(img, b):
+    h, w = img.shape[:2]
+    return img[..., 0].reshape(h // b, b, w // b, b).mean(axis=(1, 3))
+
+
+def test_look_at_convention(sms):
+    """Camera space x left, y up, z forward (the reference's look_at)."""
+    cam = sms.Camera.look_at((1.0, 2.0, 3.0), (1.0, 2.0, 0.0), (0.0, 1.0, 0.0))
+    M = cam.to_world
+    assert np.allclose(M[:3, 3], [1, 2, 3])
+    assert np.allclose(M[:3, 2], [0, 0, -1])          # forward
+    assert np.allclose(M[:3, 1], [0, 1, 0])           # up
+    assert np.allclose(M[:3, 0], [-1, 0, 0])          # left = up x forward
+
+
+def test_unflagged_scene_sms_integrator_equals_path(sms, workloads, O):
+    """Without caustic flags path_sms_ss never calls SMS and filters nothing;
+    with disable_reflected_emitters it also skips the first-bounce emitter
+    sample on delta BSDFs (path_sms_ss.cpp:150-151), so it draws the same
+    random numbers as path and gives the same image."""
+    W = workloads
+    d = sms.SceneDesc()
+    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
+    d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3))
+    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.0, W.water_params())
+    d.add_mesh(P, F, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.33), 0, N=N, UV=UV)
+    light = d.add_sphere((0.0, 0.0, 4.0), 0.5, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+    d.add_area_emitter(light, (40.0,) * 3, 0)
+    osc = O.OracleScene(d)
+    cam = W.pool_camera(8, 8)
+    a = osc.render(W.water_config(), cam, sms.RenderOptions(integrator="path", spp=4, seed=3, rr_depth=100))
+    b = osc.render(W.water_config(), cam, sms.RenderOptions(integrator="path_sms_ss", spp=4, seed=3, rr_depth=100,
+                                                            disable_reflected_emitters=True))
+    assert np.array_equal(a, b)
+    assert a.mean() > 0.0
+
+
+def test_path_sms_ss_matches_path_on_flat_water(sms, workloads, O):
+    """Flat water: SMS finds the one refraction solution of every receiver
+    point, so path_sms_ss (unbiased) and plain path tracing estimate the same
+    image; compare 3x3-pixel blocks against the sample spread of 4 runs."""
+    W = workloads
+    osc = O.OracleScene(W.pool_scene(res=16, wave_scale=0.0))
+    cam = W.pool_camera(12, 12)
+    cfg = W.water_config()
+    cfg.max_trials = -1
+    runs = {}
+    for integ, spp in (("path", 2048), ("path_sms_ss", 256)):
+        runs[integ] = np.stack([_blocks(osc.render(cfg, cam, sms.RenderOptions(integrator=integ, spp=spp,
+                                                                                seed=50 + r)), 3)
+                                for r in range(4)])
+    a, b = runs["path"], runs["path_sms_ss"]
+    se = np.sqrt(a.var(0, ddof=1) / 4 + b.var(0, ddof=1) / 4)
+    diff = np.abs(a.mean(0) - b.mean(0))
+    assert np.all(diff < 5.0 * se + 0.01 * a.mean(0) + 1e-3), (a.mean(0), b.mean(0), se)
+    assert abs(a.mean() - b.mean()) < 0.03 * a.mean()
+
+
+def test_sms_seed_matches_library(sms, O):
+    """The oracle and the library derive the per-bounce SMS seed alike
+    (SplitMix64); checked through the library's exported function."""
+    def splitmix(seed, depth):
+        m = (1 << 64) - 1
+        z = (seed + 0x9E3779B97F4A7C15 * ((depth + 1) & 0xFFFFFFFF)) & m
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+        return z ^ (z >> 31)
+    for seed, depth in ((0, 1), (7, 3), (123456789, 12)):
+        assert sms.sms_render_seed(seed, depth) == splitmix(seed, depth)

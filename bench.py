@@ -223,6 +223,51 @@ def secondary_configs(torch, sms, W, dev):
     return out
 
 
+def render_study(torch, sms, W, dev, width=512, height=512, spp=16):
+    """Whole images through the path tracer around the SMS solver (sms_render):
+    the pool scene (512^2 water heightfield over a diffuse floor, sphere area
+    light), path_sms_ss with the unbiased estimator (cap 256) and plain path
+    tracing, width x height x spp samples; the oracle's restatement of the
+    same integrator on the host cores for a bounded 64 x 64 x 4 sample."""
+    from oracle import oracle as O
+    desc = W.pool_scene(res=512)
+    cfg = W.water_config()
+    ctx = sms.Context(sms.Scene(desc), cfg, device=dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    img = torch.zeros((height, width, 3), dtype=torch.float32, device=f"cuda:{dev}")
+    torch.cuda.synchronize()
+    cam = W.pool_camera(width, height)
+    out = {"scene": "pool: 512^2 water heightfield (IOR 1.33) over a diffuse floor, sphere area light r=0.5",
+           "image": [width, height], "spp": spp}
+    for integ in ("path_sms_ss", "path"):
+        opt = sms.RenderOptions(integrator=integ, spp=spp, seed=1)
+        ctx.render_device(cam, opt, img.data_ptr())
+        ctx.reset_stats()
+        times = []
+        for k in range(3):
+            opt.seed = 2 + k
+            with DeviceTimer(torch, stream) as t:
+                ctx.render_device(cam, opt, img.data_ptr())
+            times.append(t.ms)
+        st = ctx.stats()
+        ms = float(np.mean(times))
+        out[integ] = {"ms_per_image": ms, "samples_per_s": width * height * spp / (ms / 1e3),
+                      "sms_connections_per_s": st["connections"] / (3 * ms / 1e3),
+                      "sms_walks_per_s": st["walks"] / (3 * ms / 1e3), "mean": float(img.mean().item())}
+    cores = os.cpu_count() or 1
+    ccam = W.pool_camera(64, 64)
+    opt = sms.RenderOptions(integrator="path_sms_ss", spp=4, seed=1)
+    osc = O.OracleScene(desc)
+    t0 = time.perf_counter()
+    osc.render(cfg, ccam, opt, nthreads=cores)
+    dt = time.perf_counter() - t0
+    out["cpu_oracle"] = {"samples_per_s": 64 * 64 * 4 / dt, "cores": cores, "kind": "port",
+                         "sample": f"64x64 pixels x 4 spp path_sms_ss, {dt:.2f} s"}
+    out["speedup_vs_cpu_oracle"] = out["path_sms_ss"]["samples_per_s"] / out["cpu_oracle"]["samples_per_s"]
+    ctx.close()
+    return out
+
+
 def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=8192, lr=1e-3, res=256,
                   ref_spp=4096, sigma_scale=1.0, weighted=True, walks_per_query=8):
     """Learned seed proposal on the water workload: training pairs from the
@@ -538,6 +583,8 @@ def run_ours(args):
         line["learned"] = lt
     if rank == 0 and world == 1 and not args.no_configs:
         line["configs"] = secondary_configs(torch, sms, W, dev)
+    if rank == 0 and world == 1 and not args.no_render:
+        line["render"] = render_study(torch, sms, W, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         sample = int(os.environ.get("SMS_CPU_SAMPLE", str(N_QUERIES)))
@@ -565,6 +612,7 @@ def main():
     ap.add_argument("--learned-steps", type=int, default=20000)
     ap.add_argument("--ref-spp", type=int, default=4096)
     ap.add_argument("--no-configs", action="store_true", help="skip the sphere / slab / glint configurations")
+    ap.add_argument("--no-render", action="store_true", help="skip the path-tracer images")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -21,6 +21,9 @@
  *     ::specular_manifold_sampling            src/librender/manifold_glints.cpp:28-223
  *     ::sample_glint(...,xi_start)            src/librender/manifold_glints.cpp:225-265
  *   print_statistics() counters               src/librender/manifold_ss.cpp:14-18,859-883
+ *   PathIntegrator / SMS path integrators     src/integrators/path.cpp:94-226,
+ *     ::sample (whole images: sms_render)     src/integrators/path_sms_ss.cpp:69-251,
+ *                                             src/integrators/path_sms_ms.cpp:172-330
  *
  * Where the reference calls the solver once per shading point from many host
  * threads, this library takes a whole wavefront of shading points ("queries")
@@ -471,8 +474,8 @@ sms_status sms_ctx_set_proposal(sms_ctx *ctx, sms_proposal *p, float defensive);
  * reference's per-sample order: pixel position (2), wavelength (1), then per
  * bounce Russian roulette (1, past rr_depth), emitter sampling (2, when it
  * runs) and BSDF sampling (1 + 2).  The SMS call at bounce `depth` of path p
- * draws from stream p of state seed sms_render_sms_seed(seed, depth).  Images
- * therefore do not depend on the wavefront size. */
+ * draws from stream p + depth * 2^48 of state seed sms_render_sms_seed(seed).
+ * Images therefore do not depend on the wavefront size. */
 typedef struct sms_camera {
     float   to_world[16];   /* row-major camera-to-world; camera space has x
                                left, y up, z forward (the reference's look_at) */
@@ -503,9 +506,8 @@ typedef struct sms_render_options {
 } sms_render_options;
 void sms_render_options_default(sms_render_options *opt);
 
-/* State seed of the SMS streams at bounce `depth` (SplitMix64 of the seed
- * and the depth). */
-uint64_t sms_render_sms_seed(uint64_t seed, int32_t depth);
+/* State seed of the SMS streams (SplitMix64 of the seed). */
+uint64_t sms_render_sms_seed(uint64_t seed);
 
 /* Render: image receives height x width RGB (row-major, y down, 3 floats per
  * pixel) = the mean of spp samples.  sms_render takes a host pointer and

@@ -1948,11 +1948,11 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
  * (src/librender/integrator.cpp), perspective sensor, box filter.  One path at
  * a time, with the random-number layout of the library's sms_render: path p
  * draws from PCG32 stream p (state seed `seed`), its SMS call at bounce d from
- * stream p of state seed sms_seed(seed, d).
+ * stream p + d * 2^48 of state seed sms_seed(seed).
  * ==================================================================== */
-static uint64_t sms_seed(uint64_t seed, int depth) {
+static uint64_t sms_seed(uint64_t seed) {
     /* SplitMix64 (Steele, Lea and Flood 2014) */
-    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(uint32_t)(depth + 1);
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
@@ -2158,7 +2158,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             Query q;
             q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
             PCG32 srng;
-            srng.seed(sms_seed(opt.seed, depth), g);
+            srng.seed(sms_seed(opt.seed), g + ((uint64_t)depth << 48));
             int c = 0, w = 0;
             V3 v = integ == SMS_INTEGRATOR_PATH_SMS_MS ? ms_connect(sc, cfg, q, srng, c, w, st)
                                                        : ss_connect(sc, cfg, q, srng, c, w, st);

@@ -175,7 +175,7 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_obj_load": (i32, [C.c_char_p, i32, i32, C.POINTER(_MeshData)]),
         "sms_mesh_data_free": (None, [C.POINTER(_MeshData)]),
         "sms_render_options_default": (None, [C.POINTER(_RenderOptions)]),
-        "sms_render_sms_seed": (u64, [u64, i32]),
+        "sms_render_sms_seed": (u64, [u64]),
         "sms_render": (i32, [vp, C.POINTER(_Camera), C.POINTER(_RenderOptions), vp]),
         "sms_render_device": (i32, [vp, C.POINTER(_Camera), C.POINTER(_RenderOptions), vp]),
     }
@@ -311,6 +311,13 @@ def load_scene(path):
     import sys
     from .scene_xml import load_scene_xml
     return load_scene_xml(sys.modules[__name__], path)
+
+
+def load_render_setup(path):
+    """(Camera, RenderOptions) from a scene file's <sensor> and <integrator>."""
+    import sys
+    from .scene_xml import load_render_setup as _lrs
+    return _lrs(sys.modules[__name__], path)
 
 
 def load_obj(path, face_normals: bool = False, flip_tex_coords: bool = True):
@@ -623,9 +630,9 @@ class RenderOptions:
         return o
 
 
-def sms_render_seed(seed: int, depth: int) -> int:
-    """State seed of the SMS random-number streams at bounce `depth`."""
-    return int(load_library().sms_render_sms_seed(seed, depth))
+def sms_render_seed(seed: int) -> int:
+    """State seed of the path tracer's SMS random-number streams."""
+    return int(load_library().sms_render_sms_seed(seed))
 
 
 def _soa(a: np.ndarray, rows: int, n: int) -> np.ndarray:

@@ -104,7 +104,8 @@ SMS_D bool sample_emitter(const DevScene &sc, const int *list, int ne, Pcg32 &rn
 }
 
 SMS_D uint64_t query_stream(const SolverCfg &cfg, uint64_t stream_off, uint32_t qi) {
-    return stream_off + (cfg.stream_ids ? (uint64_t)__ldg(cfg.stream_ids + qi) : (uint64_t)qi);
+    return cfg.streams ? __ldg(reinterpret_cast<const unsigned long long *>(cfg.streams) + qi)
+                       : stream_off + (uint64_t)qi;
 }
 
 SMS_D Pcg32 query_rng(uint64_t seed, uint64_t stream, uint64_t position) {

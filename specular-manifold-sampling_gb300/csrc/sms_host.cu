@@ -386,7 +386,7 @@ static SolverCfg solver_cfg(const sms_config &c) {
     s.uniqueness_threshold = c.uniqueness_threshold;
     s.step_scale = c.step_scale;
     s.mnee_init = c.mnee_init;
-    s.stream_ids = nullptr;
+    s.streams = nullptr;
     return s;
 }
 
@@ -747,10 +747,10 @@ static sms_status ensure_scratch(sms_ctx *c, uint32_t n, SsScratch &scr) {
     return SMS_OK;
 }
 
-// Single-scatter connection of n device-resident queries; stream_ids (may be
-// null) as SolverCfg::stream_ids.
+// Single-scatter connection of n device-resident queries; streams (may be
+// null) as SolverCfg::streams.
 sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
-                          const uint32_t *stream_ids, sms_result *out) {
+                          const uint64_t *streams, sms_result *out) {
     if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
         return fail(SMS_ERR_INVALID_ARG, "sms_ss_connect_batch_device: null argument");
     if (n == 0) return SMS_OK;
@@ -779,7 +779,7 @@ sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
         pr.gmm = c->gmm;
     }
     SolverCfg sc = solver_cfg(c->cfg);
-    sc.stream_ids = stream_ids;
+    sc.streams = streams;
     CUDA_TRY(launch_ss_connect(c->dsc, sc, q, n, seed, stream_off, out->value, out->count, out->walks, c->ctr, scr,
                                c->num_sms, c->blocks_per_sm, &c->timer, c->stream, c->prop ? &pr : nullptr,
                                c->trial_group));
@@ -922,7 +922,7 @@ static sms_status check_ms_cfg(sms_ctx *c) {
 }
 
 sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
-                          const uint32_t *stream_ids, sms_result *out) {
+                          const uint64_t *streams, sms_result *out) {
     if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
         return fail(SMS_ERR_INVALID_ARG, "sms_ms_connect_batch_device: null argument");
     if (sms_status st = check_ms_cfg(c)) return st;
@@ -945,7 +945,7 @@ sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
         }
     }
     SolverCfg sc = solver_cfg(c->cfg);
-    sc.stream_ids = stream_ids;
+    sc.streams = streams;
     CUDA_TRY(launch_ms_connect(c->dsc, sc, c->cfg.bounces, q, n, seed, stream_off, out->value, out->count,
                                out->walks, c->ctr, scr, c->ms_tmpl, c->num_sms, c->blocks_per_sm, &c->timer,
                                c->stream));

@@ -29,10 +29,10 @@ struct SolverCfg {
     float step_scale;
     int mnee_init;      // seed along the straight path (manifold_ss.cpp:229-241)
     // Optional per-query random-number stream table: query i draws from stream
-    // stream_off + stream_ids[i] instead of stream_off + i (the path tracer
-    // passes each query's path index, so that results do not depend on which
-    // paths of a wavefront reached a receiver).
-    const uint32_t *stream_ids;
+    // streams[i] instead of stream_off + i (the path tracer keys each query by
+    // its path and bounce, so that results do not depend on which paths of a
+    // wavefront reached a receiver or on how the queries were batched).
+    const uint64_t *streams;
 };
 
 // Unique-solution capacity per query of the biased estimator (shared memory
@@ -113,11 +113,11 @@ struct sms_ctx;
 bool ctx_view(sms_ctx *c, sms::CtxView &out);
 // Connection entry points shared with the path tracer (sms_render.cu): as
 // sms_ss_connect_batch_device / sms_ms_connect_batch_device, with an optional
-// per-query stream table (SolverCfg::stream_ids).
+// per-query stream table (SolverCfg::streams).
 sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
-                          const uint32_t *stream_ids, sms_result *out);
+                          const uint64_t *streams, sms_result *out);
 sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
-                          const uint32_t *stream_ids, sms_result *out);
+                          const uint64_t *streams, sms_result *out);
 // Reads and clears the device error flags of a context (synchronizes its
 // stream); SMS_ERR_DEVICE_LIMIT with the reasons when any was set.
 sms_status ctx_check_device_error(sms_ctx *c);

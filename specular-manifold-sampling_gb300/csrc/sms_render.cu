@@ -12,17 +12,21 @@
 //                      and the emitter it hits (filtered like the reference,
 //                      with the unbiased-MNEE check walk of path_sms_ss)
 //   pt_scan_kernel     ordered prefix sum of the per-block query counts
-//   pt_gather_kernel   compacts the staged queries into an SMS query batch
-//                      in path order, with each query's path index as its
-//                      random-number stream
+//   pt_gather_kernel   appends the staged queries of this bounce to the
+//                      wavefront's pending SMS batch, in path order, each
+//                      with its random-number stream (path, bounce)
+//   pt_pack_kernel     the pending batch as one SoA query array
 //   (SMS estimator)    the context's single- or multi-scatter connection
-//                      kernels on that batch
-//   pt_sms_add_kernel  adds throughput x SMS estimate to each path's radiance
+//                      kernels on the whole pending batch: the queries of all
+//                      bounces of a wavefront are solved by one call, so the
+//                      trial kernel's tail is paid once, not once per bounce
+//   pt_sms_add_kernel  adds throughput x SMS estimate to each path's radiance,
+//                      one launch per bounce in bounce order
 //   pt_resolve_kernel  sums the samples of each pixel in sample order
 //
-// One host read per bounce (query and live-path counts) sizes the SMS launch.
+// One host read per bounce (query and live-path counts) drives the loop.
 // Every sum runs in a fixed order, so images are bit-reproducible, and since
-// all random numbers are keyed by the path index they do not depend on the
+// all random numbers are keyed by path and bounce they do not depend on the
 // wavefront size.
 #include <algorithm>
 #include <cmath>
@@ -75,11 +79,15 @@ struct PtState {
     int *want;                            // cap
     uint32_t *block_q, *block_a;          // per block
     uint32_t *totals;                     // [0] queries, [1] live paths
-    float *q;                             // 16 x cap (compacted queries)
-    uint32_t *map;                        // cap: compacted query -> path
-    float *value;                         // 3 x cap
-    int *count, *walks;                   // cap
-    uint32_t cap;
+    // pending SMS batch (qcap entries, appended bounce by bounce)
+    float *qraw;                          // 16 x qcap, stride qcap
+    float *qw;                            // 3 x qcap: path throughput
+    uint32_t *qmap;                       // qcap: query -> path
+    uint64_t *qstream;                    // qcap: random-number stream
+    float *q;                             // 16 x nq packed (stride nq)
+    float *value;                         // 3 x nq
+    int *count, *walks;                   // nq
+    uint32_t cap, qcap;
 };
 
 SMS_D f3 ld3s(const float *a, uint32_t cap, uint32_t i) { return mk(a[i], a[cap + i], a[2 * (size_t)cap + i]); }
@@ -564,9 +572,10 @@ __global__ void __launch_bounds__(1024) pt_scan_kernel(PtState S, uint32_t n_blo
     }
 }
 
-// Staged queries -> SMS query batch (SoA with the batch size as stride), in
-// path order; map[k] = path of query k (also its random-number stream).
-__global__ void __launch_bounds__(kPtBlock) pt_gather_kernel(PtState S, uint32_t n) {
+// Staged queries of this bounce -> entries base + r of the pending batch
+// (r = rank in path order); their stream is path + bounce * 2^48.
+__global__ void __launch_bounds__(kPtBlock) pt_gather_kernel(PtState S, uint32_t n, uint32_t base, uint64_t g0,
+                                                             int depth) {
     __shared__ uint32_t warp_cnt[kPtBlock / 32];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int w = i < n ? S.want[i] : 0;
@@ -577,18 +586,32 @@ __global__ void __launch_bounds__(kPtBlock) pt_gather_kernel(PtState S, uint32_t
     if (!w) return;
     uint32_t r = S.block_q[blockIdx.x] + __popc(m & ((1u << lane) - 1u));
     for (unsigned k = 0; k < wid; ++k) r += warp_cnt[k];
-    const uint32_t nq = S.totals[0];
+    const uint32_t e = base + r;
     #pragma unroll
-    for (int k = 0; k < 16; ++k) S.q[(size_t)k * nq + r] = S.stage[(size_t)k * S.cap + i];
-    S.map[r] = i;
+    for (int k = 0; k < 16; ++k) S.qraw[(size_t)k * S.qcap + e] = S.stage[(size_t)k * S.cap + i];
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) S.qw[(size_t)k * S.qcap + e] = S.stage[(size_t)(16 + k) * S.cap + i];
+    S.qmap[e] = i;
+    S.qstream[e] = g0 + i + ((uint64_t)depth << 48);
 }
 
-__global__ void __launch_bounds__(kPtBlock) pt_sms_add_kernel(PtState S, uint32_t nq) {
+// Pending batch (stride qcap) -> packed SoA queries (stride nq).
+__global__ void __launch_bounds__(kPtBlock) pt_pack_kernel(PtState S, uint32_t nq) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nq) return;
+    #pragma unroll
+    for (int f = 0; f < 16; ++f) S.q[(size_t)f * nq + k] = S.qraw[(size_t)f * S.qcap + k];
+}
+
+// Entries [b, b + cnt) of the solved batch (one bounce: each path at most
+// once) -> path radiance.
+__global__ void __launch_bounds__(kPtBlock) pt_sms_add_kernel(PtState S, uint32_t nq, uint32_t b, uint32_t cnt) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nq) return;
-    const uint32_t i = S.map[r];
-    f3 w = mk(S.stage[(size_t)16 * S.cap + i], S.stage[(size_t)17 * S.cap + i], S.stage[(size_t)18 * S.cap + i]);
-    f3 v = mk(S.value[r], S.value[(size_t)nq + r], S.value[2 * (size_t)nq + r]);
+    if (r >= cnt) return;
+    const uint32_t k = b + r;
+    const uint32_t i = S.qmap[k];
+    f3 w = mk(S.qw[k], S.qw[(size_t)S.qcap + k], S.qw[2 * (size_t)S.qcap + k]);
+    f3 v = mk(S.value[k], S.value[(size_t)nq + k], S.value[2 * (size_t)nq + k]);
     st3s(S.L, S.cap, i, ld3s(S.L, S.cap, i) + w * v);
 }
 
@@ -636,9 +659,9 @@ extern "C" void sms_render_options_default(sms_render_options *o) {
     o->spp = 1;
 }
 
-extern "C" uint64_t sms_render_sms_seed(uint64_t seed, int32_t depth) {
-    // SplitMix64 (Steele, Lea and Flood 2014) of seed + depth * golden gamma
-    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(uint32_t)(depth + 1);
+extern "C" uint64_t sms_render_sms_seed(uint64_t seed) {
+    // SplitMix64 (Steele, Lea and Flood 2014) of seed + golden gamma
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
@@ -698,12 +721,14 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
 
     const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
     const uint64_t total = wh * (uint64_t)opt->spp;
+    if (total >= (1ull << 48)) return rfail(SMS_ERR_INVALID_ARG, "sms_render: more than 2^48 samples");
     uint32_t cap = opt->max_paths ? opt->max_paths : kPtDefaultPaths;
     if (wh <= cap) cap = (uint32_t)(std::min<uint64_t>(cap / wh, (uint64_t)opt->spp) * wh);
     cap = std::max<uint32_t>(cap, 1u);
+    const uint32_t qcap = 2u * cap;
     const uint32_t n_blocks_cap = (cap + kPtBlock - 1) / kPtBlock;
 
-    // one device block for the whole path state
+    // one device block for the whole path state and the pending SMS batch
     size_t bytes = 0;
     auto take = [&](size_t b) { size_t o = bytes; bytes += (b + 255) & ~(size_t)255; return o; };
     const size_t o_rs = take(8 * (size_t)cap), o_ri = take(8 * (size_t)cap), o_o = take(12 * (size_t)cap),
@@ -713,8 +738,10 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
                  o_fl = take(4 * (size_t)cap), o_hp = take(4 * (size_t)cap),
                  o_st = take(4 * (size_t)kStageRows * cap), o_w = take(4 * (size_t)cap),
                  o_bq = take(4 * (size_t)n_blocks_cap), o_ba = take(4 * (size_t)n_blocks_cap), o_tot = take(16),
-                 o_q = take(4 * (size_t)SMS_QUERY_FIELDS * cap), o_map = take(4 * (size_t)cap),
-                 o_val = take(12 * (size_t)cap), o_cnt = take(4 * (size_t)cap), o_wk = take(4 * (size_t)cap);
+                 o_qr = take(4 * (size_t)SMS_QUERY_FIELDS * qcap), o_qw = take(12 * (size_t)qcap),
+                 o_qm = take(4 * (size_t)qcap), o_qs = take(8 * (size_t)qcap),
+                 o_q = take(4 * (size_t)SMS_QUERY_FIELDS * qcap), o_val = take(12 * (size_t)qcap),
+                 o_cnt = take(4 * (size_t)qcap), o_wk = take(4 * (size_t)qcap);
     char *blk = nullptr;
     uint32_t *host_tot = nullptr;
     sms_status st = SMS_OK;
@@ -722,6 +749,31 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     PtState S{};
     uint64_t g0 = 0;
     const size_t img_n = 3 * (size_t)wh;
+    const uint64_t sseed = sms_render_sms_seed(P.seed);
+    std::vector<uint32_t> seg_base, seg_cnt;   // pending batch: one segment per bounce
+    uint32_t pending = 0;
+    // Solves the pending batch and adds it to the paths' radiance.
+    auto flush = [&]() -> sms_status {
+        if (pending == 0) { seg_base.clear(); seg_cnt.clear(); return SMS_OK; }
+        pt_pack_kernel<<<(pending + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, pending);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return rfail(SMS_ERR_CUDA, std::string("pt_pack_kernel: ") + cudaGetErrorString(e));
+        sms_result r{S.value, S.count, S.walks};
+        sms_status fs = P.integrator == SMS_INTEGRATOR_PATH_SMS_MS
+                            ? ctx_ms_connect(c, S.q, pending, sseed, 0, S.qstream, &r)
+                            : ctx_ss_connect(c, S.q, pending, sseed, 0, S.qstream, &r);
+        if (fs) return fs;
+        for (size_t k = 0; k < seg_base.size(); ++k) {
+            pt_sms_add_kernel<<<(seg_cnt[k] + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, pending, seg_base[k],
+                                                                                         seg_cnt[k]);
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return rfail(SMS_ERR_CUDA, std::string("pt_sms_add_kernel: ") + cudaGetErrorString(e));
+        pending = 0;
+        seg_base.clear();
+        seg_cnt.clear();
+        return SMS_OK;
+    };
     PT_TRY(cudaSetDevice(v.device));
     PT_TRY(cudaMalloc(&blk, bytes));
     PT_TRY(cudaMallocHost(&host_tot, 2 * sizeof(uint32_t)));
@@ -744,12 +796,16 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     S.block_q = reinterpret_cast<uint32_t *>(blk + o_bq);
     S.block_a = reinterpret_cast<uint32_t *>(blk + o_ba);
     S.totals = reinterpret_cast<uint32_t *>(blk + o_tot);
+    S.qraw = reinterpret_cast<float *>(blk + o_qr);
+    S.qw = reinterpret_cast<float *>(blk + o_qw);
+    S.qmap = reinterpret_cast<uint32_t *>(blk + o_qm);
+    S.qstream = reinterpret_cast<uint64_t *>(blk + o_qs);
     S.q = reinterpret_cast<float *>(blk + o_q);
-    S.map = reinterpret_cast<uint32_t *>(blk + o_map);
     S.value = reinterpret_cast<float *>(blk + o_val);
     S.count = reinterpret_cast<int *>(blk + o_cnt);
     S.walks = reinterpret_cast<int *>(blk + o_wk);
     S.cap = cap;
+    S.qcap = qcap;
     PT_TRY(cudaMemsetAsync(image, 0, img_n * sizeof(float), s));
     while (g0 < total) {
         uint32_t n;
@@ -758,34 +814,37 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         const uint32_t nb = (n + kPtBlock - 1) / kPtBlock;
         pt_camera_kernel<<<nb, kPtBlock, 0, s>>>(*v.scene, pc, S, g0, n, P.seed);
         PT_TRY(cudaGetLastError());
+        uint32_t alive_bound = n;   // paths that can stage a query at the next bounce
         for (int depth = 1;; ++depth) {
             if (depth > kPtHardDepth) {
                 st = rfail(SMS_ERR_DEVICE_LIMIT, "sms_render: a path exceeded 4096 bounces (raise rr pressure or "
                                                  "bound max_depth)");
                 goto done;
             }
+            if (pending + alive_bound > qcap) {
+                st = flush();
+                if (st) goto done;
+            }
             if (P.mnee_check) pt_bounce_kernel<true><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters);
             else pt_bounce_kernel<false><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters);
             PT_TRY(cudaGetLastError());
             pt_scan_kernel<<<1, 1024, 0, s>>>(S, nb);
             PT_TRY(cudaGetLastError());
-            pt_gather_kernel<<<nb, kPtBlock, 0, s>>>(S, n);
+            pt_gather_kernel<<<nb, kPtBlock, 0, s>>>(S, n, pending, g0, depth);
             PT_TRY(cudaGetLastError());
             PT_TRY(cudaMemcpyAsync(host_tot, S.totals, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
             PT_TRY(cudaStreamSynchronize(s));
             const uint32_t nq = host_tot[0], n_alive = host_tot[1];
             if (nq) {
-                sms_result r{S.value, S.count, S.walks};
-                const uint64_t sseed = sms_render_sms_seed(P.seed, depth);
-                st = P.integrator == SMS_INTEGRATOR_PATH_SMS_MS
-                         ? ctx_ms_connect(c, S.q, nq, sseed, g0, S.map, &r)
-                         : ctx_ss_connect(c, S.q, nq, sseed, g0, S.map, &r);
-                if (st) goto done;
-                pt_sms_add_kernel<<<(nq + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, nq);
-                PT_TRY(cudaGetLastError());
+                seg_base.push_back(pending);
+                seg_cnt.push_back(nq);
+                pending += nq;
             }
+            alive_bound = n_alive;
             if (n_alive == 0) break;
         }
+        st = flush();
+        if (st) goto done;
         {
             const uint32_t n_pix = (uint32_t)std::min<uint64_t>(n, wh);
             const uint32_t pix0 = (uint32_t)(g0 % wh);

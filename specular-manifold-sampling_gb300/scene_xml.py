@@ -24,6 +24,16 @@ silently half-loaded):
   <sensor>, <film>, <sampler> are accepted and ignored (not on this path).
 
 Returns (SceneDesc, SMSConfig or None, integrator type or None).
+
+load_render_setup reads the rendering side of the same file:
+  <sensor type="perspective">  fov, fov_axis, near_clip, far_clip,
+      <transform name="to_world"> (lookat / translate / scale / rotate / matrix),
+      <film> width, height (hdrfilm defaults 768 x 576), <sampler> sample_count
+      (independent sampler default 4)   (src/sensors/perspective.cpp)
+  <integrator type="path|path_sms_ss|path_sms_ms">  max_depth, rr_depth
+      (src/librender/integrator.cpp:300-320), disable_reflected_emitters,
+      biased_mnee (path_sms_ss.cpp:59-60)
+and returns (Camera, RenderOptions).
 """
 from __future__ import annotations
 
@@ -41,6 +51,7 @@ IOR = {"vacuum": 1.0, "helium": 1.000036, "hydrogen": 1.000132, "air": 1.000277,
        "amber": 1.55, "pet": 1.5750, "diamond": 2.419}
 
 _IGNORED = {"sensor", "film", "sampler", "default"}
+_INTEGRATOR_TYPES = {"path", "path_sms_ss", "path_sms_ms"}
 
 
 def _props(el):
@@ -113,6 +124,30 @@ def _transform(el):
         elif c.tag == "matrix":
             A = np.array([float(x) for x in c.get("value").replace(",", " ").split()]).reshape(4, 4)
             M = A @ M
+        elif c.tag == "rotate":
+            # rotation by `angle` degrees about the axis (x, y, z) (Rodrigues)
+            if c.get("value"):
+                ax = np.array([float(x) for x in c.get("value").replace(",", " ").split()])
+            else:
+                ax = np.array([float(c.get(k, 0)) for k in "xyz"])
+            ax = ax / np.linalg.norm(ax)
+            a = math.radians(float(c.get("angle", 0)))
+            K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+            R = np.eye(4)
+            R[:3, :3] = np.eye(3) + math.sin(a) * K + (1 - math.cos(a)) * (K @ K)
+            M = R @ M
+        elif c.tag == "lookat":
+            # include/mitsuba/core/transform.h look_at: columns left, up, forward, origin
+            vec = lambda k: np.array([float(x) for x in c.get(k).replace(",", " ").split()])
+            o, t = vec("origin"), vec("target")
+            up = vec("up") if c.get("up") else np.array([0.0, 1.0, 0.0])
+            d = (t - o) / np.linalg.norm(t - o)
+            left = np.cross(up, d)
+            left /= np.linalg.norm(left)
+            new_up = np.cross(d, left)
+            L = np.eye(4)
+            L[:3, 0], L[:3, 1], L[:3, 2], L[:3, 3] = left, new_up, d, o
+            M = L @ M
         else:
             raise ValueError(f"unsupported transform operation <{c.tag}>")
     return M
@@ -223,3 +258,46 @@ def load_scene_xml(sms, path):
             ep = _props(em)
             desc.add_area_emitter(sid, _spectrum(ep, "radiance", (1.0,) * 3), _emitter_flags(sms, ep))
     return desc, config, itype
+
+
+def _int(p, name, default):
+    return int(p[name][1].get("value")) if name in p else default
+
+
+def load_render_setup(sms, path):
+    """(Camera, RenderOptions) of the scene file's sensor and integrator."""
+    root = ET.parse(Path(path)).getroot()
+    sensor = next((c for c in root if c.tag == "sensor"), None)
+    if sensor is None:
+        raise ValueError("the scene has no <sensor>")
+    if sensor.get("type") != "perspective":
+        raise ValueError(f"unsupported sensor type '{sensor.get('type')}'")
+    p = _props(sensor)
+    if "focal_length" in p:
+        raise ValueError("focal_length is not supported; give the sensor a fov")
+    tr = next((c for c in sensor if c.tag == "transform" and c.get("name") == "to_world"), None)
+    M = _transform(tr) if tr is not None else np.eye(4)
+    film = next((c for c in sensor if c.tag == "film"), None)
+    fp = _props(film) if film is not None else {}
+    smp = next((c for c in sensor if c.tag == "sampler"), None)
+    sp = _props(smp) if smp is not None else {}
+    if film is not None:
+        rf = next((c for c in film if c.tag == "rfilter"), None)
+        if rf is not None and rf.get("type") != "box":
+            raise ValueError(f"reconstruction filter '{rf.get('type')}' is not supported (box only)")
+    axis = p["fov_axis"][1].get("value").lower() if "fov_axis" in p else "x"
+    cam = sms.Camera(M.astype(np.float32), _float(p, "fov", 45.0), _int(fp, "width", 768), _int(fp, "height", 576),
+                     axis, _float(p, "near_clip", 1e-2), _float(p, "far_clip", 1e4))
+    opt = sms.RenderOptions(spp=_int(sp, "sample_count", 4))
+    integ = next((c for c in root if c.tag == "integrator"), None)
+    if integ is not None:
+        t = integ.get("type")
+        if t not in _INTEGRATOR_TYPES:
+            raise ValueError(f"unsupported integrator type '{t}'")
+        ip = _props(integ)
+        opt.integrator = t
+        opt.max_depth = _int(ip, "max_depth", -1)
+        opt.rr_depth = _int(ip, "rr_depth", 5)
+        opt.disable_reflected_emitters = _bool(ip, "disable_reflected_emitters")
+        opt.biased_mnee = _bool(ip, "biased_mnee")
+    return cam, opt

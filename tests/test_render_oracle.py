@@ -71,13 +71,13 @@ def test_path_sms_ss_matches_path_on_flat_water(sms, workloads, O):
 
 
 def test_sms_seed_matches_library(sms, O):
-    """The oracle and the library derive the per-bounce SMS seed alike
+    """The oracle and the library derive the SMS state seed alike
     (SplitMix64); checked through the library's exported function."""
-    def splitmix(seed, depth):
+    def splitmix(seed):
         m = (1 << 64) - 1
-        z = (seed + 0x9E3779B97F4A7C15 * ((depth + 1) & 0xFFFFFFFF)) & m
+        z = (seed + 0x9E3779B97F4A7C15) & m
         z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
         z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
         return z ^ (z >> 31)
-    for seed, depth in ((0, 1), (7, 3), (123456789, 12)):
-        assert sms.sms_render_seed(seed, depth) == splitmix(seed, depth)
+    for seed in (0, 7, 123456789, (1 << 64) - 1):
+        assert sms.sms_render_seed(seed) == splitmix(seed)

@@ -100,7 +100,9 @@ def test_obj_shape_and_area_emitter(sms, tmp_path):
     ('<shape type="cylinder"/>', "cylinder"),
     ('<shape type="sphere"><bsdf type="roughconductor"/></shape>', "roughconductor"),
     ('<emitter type="envmap"/>', "envmap"),
-    ('<shape type="sphere"><transform name="to_world"><rotate x="1" angle="3"/></transform></shape>', "rotate"),
+    ('<shape type="sphere"><transform name="to_world"><rotate x="1" angle="3"/></transform></shape>',
+     "translation and a uniform scale"),
+    ('<shape type="sphere"><transform name="to_world"><shear value="1"/></transform></shape>', "shear"),
     ('<shape type="sphere"><bsdf type="dielectric"><string name="int_ior" value="unobtainium"/></bsdf></shape>',
      "unobtainium"),
 ])
@@ -109,3 +111,45 @@ def test_unsupported_content_is_refused(sms, tmp_path, body, what):
     with pytest.raises(ValueError) as e:
         sms.load_scene(tmp_path / "bad.xml")
     assert what in str(e.value)
+
+
+RENDER_XML = """<scene version="2.0.0">
+  <integrator type="path_sms_ss">
+    <integer name="max_depth" value="8"/>
+    <integer name="rr_depth" value="3"/>
+    <boolean name="biased_mnee" value="true"/>
+    <boolean name="disable_reflected_emitters" value="true"/>
+  </integrator>
+  <sensor type="perspective">
+    <float name="fov" value="40"/>
+    <string name="fov_axis" value="y"/>
+    <transform name="to_world">
+      <lookat origin="0, -3.2, 3.6" target="0, 0, 0.4" up="0, 0, 1"/>
+    </transform>
+    <sampler type="independent"><integer name="sample_count" value="32"/></sampler>
+    <film type="hdrfilm">
+      <integer name="width" value="40"/><integer name="height" value="30"/>
+      <rfilter type="box"/>
+    </film>
+  </sensor>
+</scene>
+"""
+
+
+def test_render_setup_from_xml(sms, workloads, tmp_path):
+    """Sensor, film, sampler and integrator parameters of a scene file."""
+    path = tmp_path / "render.xml"
+    path.write_text(RENDER_XML)
+    cam, opt = sms.load_render_setup(path)
+    ref = workloads.pool_camera(40, 30)
+    np.testing.assert_allclose(cam.to_world, ref.to_world, atol=1e-6)
+    assert (cam.width, cam.height, cam.fov, cam.fov_axis) == (40, 30, 40.0, "y")
+    assert (opt.integrator, opt.max_depth, opt.rr_depth, opt.spp) == ("path_sms_ss", 8, 3, 32)
+    assert opt.biased_mnee and opt.disable_reflected_emitters
+    bad = RENDER_XML.replace('<rfilter type="box"/>', '<rfilter type="gaussian"/>')
+    path.write_text(bad)
+    with pytest.raises(ValueError):
+        sms.load_render_setup(path)
+    path.write_text(RENDER_XML.replace('type="path_sms_ss"', 'type="bdpt"'))
+    with pytest.raises(ValueError):
+        sms.load_render_setup(path)

@@ -584,7 +584,7 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_configs:
         line["configs"] = secondary_configs(torch, sms, W, dev)
     if rank == 0 and world == 1 and not args.no_render:
-        line["render"] = render_study(torch, sms, W, dev)
+        line["render"] = render_study(torch, sms, W, dev, args.render_size, args.render_size, args.render_spp)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         sample = int(os.environ.get("SMS_CPU_SAMPLE", str(N_QUERIES)))
@@ -613,7 +613,18 @@ def main():
     ap.add_argument("--ref-spp", type=int, default=4096)
     ap.add_argument("--no-configs", action="store_true", help="skip the sphere / slab / glint configurations")
     ap.add_argument("--no-render", action="store_true", help="skip the path-tracer images")
+    ap.add_argument("--render-only", action="store_true",
+                    help="only the path-tracer images (one JSON object; for profiling the renderer)")
+    ap.add_argument("--render-size", type=int, default=512)
+    ap.add_argument("--render-spp", type=int, default=16)
     args = ap.parse_args()
+    if args.render_only:
+        import torch
+        sms = load_package()
+        from sms_gb300 import workloads as W
+        print(json.dumps({"render": render_study(torch, sms, W, 0, args.render_size, args.render_size,
+                                                 args.render_spp)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

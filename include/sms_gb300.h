@@ -99,15 +99,21 @@ sms_status sms_config_parse_xml(const char *xml, sms_config *cfg,
  * conductor.cpp:288-295).  Only the fields the solver reads are kept. */
 typedef enum sms_bsdf_type {
     SMS_BSDF_DIFFUSE = 0,     /* ior() = (0, 1): treated as eta = 1            */
-    SMS_BSDF_DIELECTRIC = 1,  /* smooth dielectric, eta = int_ior / ext_ior     */
-    SMS_BSDF_CONDUCTOR = 2    /* smooth conductor, complex ior (eta, k)         */
+    SMS_BSDF_DIELECTRIC = 1,  /* dielectric, eta = int_ior / ext_ior            */
+    SMS_BSDF_CONDUCTOR = 2    /* conductor, complex ior (eta, k)                */
 } sms_bsdf_type;
 
+/* alpha > 0 makes a dielectric / conductor the reference's roughdielectric /
+ * roughconductor with an isotropic Beckmann distribution of that roughness
+ * (src/bsdfs/roughdielectric.cpp, roughconductor.cpp; BSDF::roughness()).  A
+ * rough single-scatter caster draws an offset normal per query
+ * (manifold_ss.cpp:60-70). */
 typedef struct sms_bsdf {
     int32_t type;       /* sms_bsdf_type                                        */
     float   eta;        /* dielectric relative IOR, or conductor real part      */
     float   k;          /* conductor imaginary part                             */
     float   albedo[3];  /* diffuse reflectance (receivers)                      */
+    float   alpha;      /* Beckmann roughness, 0 = smooth                       */
 } sms_bsdf;
 
 typedef struct sms_scene sms_scene;  /* host-side scene builder (owned by caller) */

@@ -640,7 +640,8 @@ static void d_sphcoords(V3 w, V3 dwdu, V3 dwdv, float &dtu, float &dpu, float &d
 
 /* ------------------------------------------------------ constraints */
 /* manifold_ss.cpp:494-636 */
-static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr) {
+static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr,
+                           V3 no = V3(0.f, 0.f, 1.f)) {
     V3 wi = x - v1.p;
     float ili = norm(wi);
     if (ili < 1e-3f) return false;
@@ -653,8 +654,13 @@ static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX,
     ilo = 1.f / ilo; wo *= ilo;
     V3 dwo_du = (v1.dp_du - wo * dot(wo, v1.dp_du)) * -ilo;
     V3 dwo_dv = (v1.dp_dv - wo * dot(wo, v1.dp_dv)) * -ilo;
-    /* n_offset = (0,0,1): n, dn_du, dn_dv are the vertex's own */
+    /* offset normal (manifold_ss.cpp:560-569); (0,0,1) keeps the vertex's own */
     V3 n = v1.n, dndu = v1.dn_du, dndv = v1.dn_dv;
+    if (no.x != 0.f || no.y != 0.f) {
+        n = v1.s * no.x + v1.t * no.y + v1.n * no.z;
+        dndu = v1.ds_du * no.x + v1.dt_du * no.y + v1.dn_du * no.z;
+        dndv = v1.ds_dv * no.x + v1.dt_dv * no.y + v1.dn_dv * no.z;
+    }
     bool success = false;
     M2 J;
     C = V2{0.f, 0.f};
@@ -703,7 +709,8 @@ static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX,
 }
 
 /* manifold_ss.cpp:407-492 */
-static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr) {
+static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr,
+                            V3 no = V3(0.f, 0.f, 1.f)) {
     V3 wo = ei.p - v1.p;
     float ilo = norm(wo);
     if (ilo < 1e-3f) return false;
@@ -730,10 +737,10 @@ static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX
     J.m[1][0] = dot(v1.dt_du, h) + dot(v1.t, dh_du);
     J.m[0][1] = dot(v1.ds_dv, h) + dot(v1.s, dh_dv);
     J.m[1][1] = dot(v1.dt_dv, h) + dot(v1.t, dh_dv);
-    if (J_out) { *J_out = J; C = V2{dot(v1.s, h), dot(v1.t, h)}; }
+    if (J_out) { *J_out = J; C = V2{dot(v1.s, h) - no.x, dot(v1.t, h) - no.y}; }
     float d = det(J);
     if (std::fabs(d) < 1e-6f) return false;
-    C = V2{dot(v1.s, h), dot(v1.t, h)};
+    C = V2{dot(v1.s, h) - no.x, dot(v1.t, h) - no.y};   /* H - N (manifold_ss.cpp:485-488) */
     dX = mul(inverse(J), C);
     return true;
 }
@@ -745,7 +752,7 @@ struct Cfg {
 
 /* manifold_ss.cpp:329-405.  Returns (ok, si_current, iterations). */
 static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MVertex &init,
-                          const EI &ei, SI &si_out, int &iters_out) {
+                          const EI &ei, SI &si_out, int &iters_out, V3 no = V3(0.f, 0.f, 1.f)) {
     MVertex vtx = init;
     bool success = false;
     int it = 0;
@@ -753,8 +760,8 @@ static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MV
     SI si_current;
     while (it < cfg.max_iterations) {
         V2 C, dX;
-        bool ok = cfg.halfvector_constraints ? step_halfvector(x, vtx, ei, C, dX)
-                                             : step_anglediff(x, vtx, ei, C, dX);
+        bool ok = cfg.halfvector_constraints ? step_halfvector(x, vtx, ei, C, dX, nullptr, no)
+                                             : step_anglediff(x, vtx, ei, C, dX, nullptr, no);
         if (!ok) break;
         if (std::sqrt(C.x * C.x + C.y * C.y) < cfg.solver_threshold) { success = true; break; }
         V3 p_prop = vtx.p - (vtx.dp_du * dX.x + vtx.dp_dv * dX.y) * (cfg.step_scale * beta);
@@ -796,10 +803,10 @@ static Query load_query(const float *q, uint32_t n, uint32_t i) {
     return r;
 }
 
-/* manifold_ss.cpp:203-279 (twostage / mnee_init / offset normals: unsupported) */
+/* manifold_ss.cpp:203-279 (twostage: unsupported); no = offset normal */
 static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, const Query &q,
                         const EI &ei, V2 sample, V3 p_start, SI &si_final, SI &si_init,
-                        int &iters) {
+                        int &iters, V3 no = V3(0.f, 0.f, 1.f)) {
     const Shape &shape = sc.shapes[caster];
     V3 p = sample_position(shape, sample);
     if (p_start.x != 0.f || p_start.y != 0.f || p_start.z != 0.f) p = p_start;
@@ -811,7 +818,7 @@ static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, cons
     if (!si_init.valid() || caster != si_init.shape) return false;
     MVertex v0;
     vertex_from_si(sc, si_init, v0);
-    bool ok = newton_solver(sc, cfg, q.p, v0, ei, si_final, iters);
+    bool ok = newton_solver(sc, cfg, q.p, v0, ei, si_final, iters, no);
     return ok && si_final.valid();
 }
 
@@ -899,6 +906,82 @@ static float specular_reflectance(const Scene &sc, const SI &si, V3 wo) {
     /* diffuse: ior (0,1) has a nonzero imaginary part -> conductor formula */
     return fresnel_conductor(std::fabs(cos_theta), 0.f, 1.f);
 }
+
+/* ---- isotropic Beckmann microfacets (include/mitsuba/render/microfacet.h):
+ * D(m) with its underflow cut-off; Smith G1 by the rational approximation of
+ * Walter et al. 2007 (eq. 27); sampling of m with density D(m) cos(theta_m). */
+static float beckmann_D(V3 m, float alpha) {
+    float c2 = m.z * m.z;
+    float r = std::exp(-((m.x * m.x + m.y * m.y) / (alpha * alpha)) / c2) / (kPi * alpha * alpha * c2 * c2);
+    return r * m.z > 1e-20f ? r : 0.f;
+}
+static float beckmann_G1(V3 v, V3 m, float alpha) {
+    float xy = alpha * alpha * (v.x * v.x + v.y * v.y);
+    float r = 1.f;
+    if (xy != 0.f) {
+        float a = 1.f / std::sqrt(xy / (v.z * v.z)), a2 = a * a;
+        r = a >= 1.6f ? 1.f : (3.535f * a + 2.181f * a2) / (1.f + 2.276f * a + 2.577f * a2);
+    }
+    return dot(v, m) * v.z <= 0.f ? 0.f : r;
+}
+static V3 beckmann_sample(float alpha, float u0, float u1, float &pdf) {
+    float ang = 2.f * kPi * u1;
+    float sp = std::sin(ang), cp = std::cos(ang);
+    float ct = 1.f / std::sqrt(1.f - alpha * alpha * std::log(1.f - u0));
+    float c2 = ct * ct;
+    pdf = (1.f - u0) / (kPi * alpha * alpha * std::max(c2 * ct, 1e-20f));
+    float st = std::sqrt(1.f - c2);
+    return V3(cp * st, sp * st, ct);
+}
+/* roughconductor.cpp eval (value x cos_theta_o), local frame */
+static float roughconductor_eval(float alpha, float er, float ek, V3 wi, V3 wo) {
+    if (!(wi.z > 0.f && wo.z > 0.f)) return 0.f;
+    V3 h = normalize(wo + wi);
+    float D = beckmann_D(h, alpha);
+    if (D == 0.f) return 0.f;
+    float G = beckmann_G1(wi, h, alpha) * beckmann_G1(wo, h, alpha);
+    return D * G / (4.f * wi.z) * fresnel_conductor(dot(wi, h), er, ek);
+}
+/* roughdielectric.cpp eval (value x |cos_theta_o|, radiance transport), local frame */
+static float roughdielectric_eval(float alpha, float eta_, V3 wi, V3 wo) {
+    const float ci = wi.z, co = wo.z;
+    if (ci == 0.f) return 0.f;
+    const bool reflect = ci * co > 0.f;
+    const float eta = ci > 0.f ? eta_ : 1.f / eta_, inv_eta = ci > 0.f ? 1.f / eta_ : eta_;
+    V3 m = normalize(wi + wo * (reflect ? 1.f : eta));
+    if (m.z < 0.f) m = -m;
+    float D = beckmann_D(m, alpha);
+    float F = fresnel(dot(wi, m), eta_);
+    float G = beckmann_G1(wi, m, alpha) * beckmann_G1(wo, m, alpha);
+    if (reflect) return F * D * G / (4.f * std::fabs(ci));
+    float den = dot(wi, m) + eta * dot(wo, m);
+    return std::fabs((inv_eta * inv_eta) * (1.f - F) * D * G * eta * eta * dot(wi, m) * dot(wo, m) /
+                     (ci * den * den));
+}
+/* manifold_ss.cpp:648-669: a rough BSDF's value in the half-vector domain;
+ * wi toward the shading point, wo toward the light (world space). */
+static float specular_reflectance_rough(const Scene &sc, const SI &si, V3 wi_w, V3 wo_w) {
+    const sms_bsdf &b = sc.shapes[si.shape].bsdf;
+    V3 n = si.shn;
+    V3 fs = normalize(si.dp_du - n * dot(n, si.dp_du));
+    V3 ft = cross(n, fs);
+    V3 wi(dot(wi_w, fs), dot(wi_w, ft), dot(wi_w, n));
+    V3 wo(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
+    if (b.type == SMS_BSDF_CONDUCTOR && b.k != 0.f) {
+        float f = roughconductor_eval(b.alpha, b.eta, b.k, wi, wo);
+        V3 h = normalize(wi + wo);
+        return f * 4.f * std::fabs(dot(wo, h));
+    }
+    float f = b.type == SMS_BSDF_CONDUCTOR ? roughconductor_eval(b.alpha, b.eta, b.k, wi, wo)
+                                           : roughdielectric_eval(b.alpha, b.eta, wi, wo);
+    float eta = b.eta;
+    if (wi.z < 0.f) eta = 1.f / eta;
+    V3 h = -normalize(wi + wo * eta);
+    float a = dot(wi, h) + eta * dot(wo, h);
+    return f * a * a / (eta * eta * std::fabs(dot(wo, h)));
+}
+
+static bool is_rough(const sms_bsdf &b) { return b.type != SMS_BSDF_DIFFUSE && b.alpha > 0.f; }
 
 /* manifold_ss.cpp:695-857 */
 static float geometric_term(const MVertex &v0, const MVertex &v1, const MVertex &v2) {
@@ -998,7 +1081,9 @@ static V3 evaluate_path_contribution(const Scene &sc, const Query &q, const EI &
     vx.dn_du = V3(0.f); vx.dn_dv = V3(0.f);
     make_orthonormal(vx);
     /* path_throughput = 1 * F * G * weight (manifold_ss.cpp:322-326) */
-    float f = specular_reflectance(sc, si_final, normalize(ei.p - si_final.p));
+    float f = is_rough(sc.shapes[si_final.shape].bsdf)
+                  ? specular_reflectance_rough(sc, si_final, normalize(q.p - si_final.p), normalize(ei.p - si_final.p))
+                  : specular_reflectance(sc, si_final, normalize(ei.p - si_final.p));
     f *= geometric_term(vx, vtx, vy);
     return V3(f * ei.weight.x, f * ei.weight.y, f * ei.weight.z);
 }
@@ -1084,6 +1169,13 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
         V3 value(0.f);
         SI si_final, si_init;
         int it = 0;
+        /* offset normal of a rough caster (manifold_ss.cpp:60-70) */
+        V3 no(0.f, 0.f, 1.f);
+        float p_offset = 1.f;
+        if (is_rough(sc.shapes[caster].bsdf)) {
+            V2 u = rng.next_2d();
+            no = beckmann_sample(sc.shapes[caster].bsdf.alpha, u.x, u.y, p_offset);
+        }
         if (!cfg.biased) {
             count_out = 0;
             const bool lrn = learned && learned->shape == caster;
@@ -1094,7 +1186,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             };
             V2 smp;
             V3 ps = seed_of(smp);
-            bool ok = sample_path(sc, cfg, caster, q, ei, smp, ps, si_final, si_init, it);
+            bool ok = sample_path(sc, cfg, caster, q, ei, smp, ps, si_final, si_init, it, no);
             walks_out++; st.walks++; st.newton += it;
             if (!ok) { st.failed++; continue; }
             st.succeeded++;
@@ -1110,7 +1202,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
                 int it2 = 0;
                 V2 smp2;
                 V3 ps2 = seed_of(smp2);
-                bool ok2 = sample_path(sc, cfg, caster, q, ei, smp2, ps2, sf, si0, it2);
+                bool ok2 = sample_path(sc, cfg, caster, q, ei, smp2, ps2, sf, si0, it2, no);
                 walks_out++; st.walks++; st.newton += it2;
                 if (ok2) {
                     V3 dt = normalize(sf.p - q.p);
@@ -1127,7 +1219,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
         } else {
             std::vector<V3> solutions;
             for (int m = 0; m < cfg.max_trials; ++m) {
-                bool ok = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), si_final, si_init, it);
+                bool ok = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), si_final, si_init, it, no);
                 walks_out++; st.walks++; st.newton += it;
                 if (!ok) { st.failed++; continue; }
                 st.succeeded++;
@@ -1144,7 +1236,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             }
             count_out += (int)solutions.size();
         }
-        result += value;
+        result += value * (1.f / p_offset);
     }
     return result;
 }
@@ -2071,9 +2163,83 @@ static V3 pt_cosine_hemisphere(float u1, float u2) {
 
 struct PtBsdf { V3 wo, weight; float pdf = 0.f, eta = 1.f; bool delta = false; };
 
+/* density of pt_rough_sample for (wi, wo): D(m) cos(theta_m) x the Jacobian
+ * of reflection / refraction (roughconductor.cpp / roughdielectric.cpp pdf
+ * with normals drawn from D cos instead of the visible normals) */
+static float pt_rough_pdf(const sms_bsdf &b, V3 wi, V3 wo) {
+    const float ci = wi.z, co = wo.z;
+    if (b.type == SMS_BSDF_CONDUCTOR) {
+        if (!(ci > 0.f && co > 0.f)) return 0.f;
+        V3 h = normalize(wo + wi);
+        return beckmann_D(h, b.alpha) * h.z / (4.f * dot(wo, h));
+    }
+    if (ci == 0.f) return 0.f;
+    const bool reflect = ci * co > 0.f;
+    const float eta = ci > 0.f ? b.eta : 1.f / b.eta;
+    V3 m = normalize(wi + wo * (reflect ? 1.f : eta));
+    if (m.z < 0.f) m = -m;
+    if (dot(wi, m) * ci <= 0.f || dot(wo, m) * co <= 0.f) return 0.f;
+    const float F = fresnel(dot(wi, m), b.eta);
+    const float pm = beckmann_D(m, b.alpha) * m.z;
+    if (reflect) return F * pm / (4.f * std::fabs(dot(wo, m)));
+    const float den = dot(wi, m) + eta * dot(wo, m);
+    return (1.f - F) * pm * eta * eta * std::fabs(dot(wo, m)) / (den * den);
+}
+
+/* diffuse.cpp eval, roughconductor.cpp / roughdielectric.cpp eval (value x
+ * |cos_theta_o|); delta BSDFs give 0 */
+static V3 pt_bsdf_eval(const sms_bsdf &b, V3 wi, V3 wo) {
+    if (b.type == SMS_BSDF_DIFFUSE) {
+        if (!(wi.z > 0.f && wo.z > 0.f)) return V3(0.f);
+        return V3(b.albedo[0], b.albedo[1], b.albedo[2]) * (kInvPi * wo.z);
+    }
+    if (!(b.alpha > 0.f)) return V3(0.f);
+    return V3(b.type == SMS_BSDF_CONDUCTOR ? roughconductor_eval(b.alpha, b.eta, b.k, wi, wo)
+                                           : roughdielectric_eval(b.alpha, b.eta, wi, wo));
+}
+
+static float pt_bsdf_pdf(const sms_bsdf &b, V3 wi, V3 wo) {
+    if (b.type == SMS_BSDF_DIFFUSE) return (wi.z > 0.f && wo.z > 0.f) ? kInvPi * wo.z : 0.f;
+    return b.alpha > 0.f ? pt_rough_pdf(b, wi, wo) : 0.f;
+}
+
+/* rough sampling: m ~ D cos (microfacet.h, sample_visible = false), then
+ * reflection, or for a dielectric reflection / refraction by the Fresnel
+ * reflectance at m (roughdielectric.cpp sample); weight = value / density */
+static bool pt_rough_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u3, PtBsdf &bs) {
+    const float ci = wi.z;
+    float pm;
+    const V3 m = beckmann_sample(b.alpha, u2, u3, pm);
+    bs.delta = false;
+    bs.eta = 1.f;
+    if (b.type == SMS_BSDF_CONDUCTOR) {
+        if (!(ci > 0.f)) return false;
+        bs.wo = m * (2.f * dot(wi, m)) - wi;
+        if (!(bs.wo.z > 0.f)) return false;
+    } else {
+        float cos_t;
+        const float F = fresnel(dot(wi, m), b.eta, &cos_t);
+        const bool outside = dot(wi, m) >= 0.f;
+        const float eta_it = outside ? b.eta : 1.f / b.eta, eta_ti = outside ? 1.f / b.eta : b.eta;
+        if (u1 <= F) {
+            bs.wo = m * (2.f * dot(wi, m)) - wi;
+            if (!(bs.wo.z * ci > 0.f)) return false;
+        } else {
+            bs.wo = m * (dot(wi, m) * eta_ti + cos_t) - wi * eta_ti;
+            if (!(bs.wo.z * ci < 0.f)) return false;
+            bs.eta = eta_it;
+        }
+    }
+    bs.pdf = pt_rough_pdf(b, wi, bs.wo);
+    if (!(bs.pdf > 0.f)) return false;
+    bs.weight = pt_bsdf_eval(b, wi, bs.wo) * (1.f / bs.pdf);
+    return true;
+}
+
 /* diffuse.cpp / dielectric.cpp / conductor.cpp sample() (smooth, radiance) */
 static bool pt_bsdf_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u3, PtBsdf &bs) {
     const float ci = wi.z;
+    if (b.type != SMS_BSDF_DIFFUSE && b.alpha > 0.f) return pt_rough_sample(b, wi, u1, u2, u3, bs);
     if (b.type == SMS_BSDF_DIFFUSE) {
         if (!(ci > 0.f)) return false;
         bs.wo = pt_cosine_hemisphere(u2, u3);
@@ -2150,10 +2316,11 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         if (integ == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) != 0;
         else if (integ == SMS_INTEGRATOR_PATH_SMS_MS)
             on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
-        const bool smooth = s.bsdf.type == SMS_BSDF_DIFFUSE;
+        const bool diffuse = s.bsdf.type == SMS_BSDF_DIFFUSE;
+        const bool smooth = diffuse || is_rough(s.bsdf);   /* BSDFFlags::Smooth: diffuse or glossy */
         V3 albedo(s.bsdf.albedo[0], s.bsdf.albedo[1], s.bsdf.albedo[2]);
         /* SMS at a receiver (path_sms_ss.cpp:115-121, path_sms_ms.cpp:226-232) */
-        if (integ != SMS_INTEGRATOR_PATH && receiver && !on_caster && smooth &&
+        if (integ != SMS_INTEGRATOR_PATH && receiver && !on_caster && diffuse &&
             (opt.max_depth < 0 || depth + bounces < opt.max_depth)) {
             Query q;
             q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
@@ -2174,10 +2341,10 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 Ray sr; sr.o = si.p; sr.d = ds.d;
                 sr.mint = kRayEps * (1.f + hmax_abs(si.p)); sr.maxt = ds.dist * (1.f - kShadowEps);
                 if (!ray_test(sc, sr) && smooth) {
-                    float co = dot(ds.d, n_sh);
-                    if (wi.z > 0.f && co > 0.f) {
-                        V3 bv = albedo * (kInvPi * co);
-                        float w = ds.delta ? 1.f : mis_weight(ds.pdf, kInvPi * co);
+                    V3 wo(dot(ds.d, fs), dot(ds.d, ft), dot(ds.d, n_sh));
+                    V3 bv = pt_bsdf_eval(s.bsdf, wi, wo);
+                    if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
+                        float w = ds.delta ? 1.f : mis_weight(ds.pdf, pt_bsdf_pdf(s.bsdf, wi, wo));
                         L += thr * bv * ds.spec * w;
                     }
                 }

@@ -179,6 +179,7 @@ struct DevShape {
     float bcx, bcy, bcz;   // bounding-box centre
     int reflective;        // complex ior: MNEE initialisation aims at the box centre
     float albedo[3];       // diffuse reflectance (path tracer)
+    float alpha;           // Beckmann roughness of a rough dielectric / conductor (0: smooth)
 };
 
 // Target of the MNEE initialisation (manifold_ss.cpp:229-241,
@@ -570,8 +571,14 @@ SMS_HD void d_sphcoords(f3 w, f3 du, f3 dv, float &dtu, float &dpu, float &dtv,
 
 // Angle-difference constraint and Newton step (manifold_ss.cpp:494-636) with
 // n_offset = (0, 0, 1).  Returns false when the step is invalid.
+SMS_HD void frame_and_derivative(const Vtx &v, f3 &s, f3 &t, f3 &dsdu, f3 &dsdv, f3 &dtdu, f3 &dtdv);
+
+// Angle-difference constraint and Newton step (manifold_ss.cpp:494-636).  `no`
+// is the offset normal in the shading frame (manifold_ss.cpp:560-569): the
+// specular transform uses m = s no.x + t no.y + n no.z and its derivatives;
+// (0, 0, 1) leaves n untouched.
 SMS_HD bool step_anglediff(f3 x, const Vtx &v, f3 lp, float &c0, float &c1,
-                                               float &dx0, float &dx1) {
+                                               float &dx0, float &dx1, f3 no = f3{0.f, 0.f, 1.f}) {
     f3 wi = x - v.p;
     float ili = length(wi);
     if (ili < 1e-3f) return false;
@@ -585,6 +592,14 @@ SMS_HD bool step_anglediff(f3 x, const Vtx &v, f3 lp, float &c0, float &c1,
     f3 dwo_du = (v.dp_du - wo * dot(wo, v.dp_du)) * -ilo;
     f3 dwo_dv = (v.dp_dv - wo * dot(wo, v.dp_dv)) * -ilo;
     const bool refl = v.eta == 1.f;
+    f3 nn = v.n, nn_du = v.dn_du, nn_dv = v.dn_dv;
+    if (no.x != 0.f || no.y != 0.f) {
+        f3 fs, ft, fsdu, fsdv, ftdu, ftdv;
+        frame_and_derivative(v, fs, ft, fsdu, fsdv, ftdu, ftdv);
+        nn = fs * no.x + ft * no.y + v.n * no.z;
+        nn_du = fsdu * no.x + ftdu * no.y + v.dn_du * no.z;
+        nn_dv = fsdv * no.x + ftdv * no.y + v.dn_dv * no.z;
+    }
     // Try the transform of wi first, then of wo (manifold_ss.cpp:573-624).
     f3 a = wi, a_du = dwi_du, a_dv = dwi_dv;   // transformed
     f3 b = wo, b_du = dwo_du, b_dv = dwo_dv;   // compared against
@@ -597,16 +612,16 @@ SMS_HD bool step_anglediff(f3 x, const Vtx &v, f3 lp, float &c0, float &c1,
             b = wi; b_du = dwi_du; b_dv = dwi_dv;
         }
         if (refl) {
-            t = v.n * (2.f * dot(a, v.n)) - a;
+            t = nn * (2.f * dot(a, nn)) - a;
             ok = true;
         } else {
-            ok = refract(a, v.n, v.eta, t);
+            ok = refract(a, nn, v.eta, t);
         }
     }
     if (!ok) return false;
     f3 t_du, t_dv;
-    if (refl) d_reflect(a, a_du, a_dv, v.n, v.dn_du, v.dn_dv, t_du, t_dv);
-    else d_refract(a, a_du, a_dv, v.n, v.dn_du, v.dn_dv, v.eta, t_du, t_dv);
+    if (refl) d_reflect(a, a_du, a_dv, nn, nn_du, nn_dv, t_du, t_dv);
+    else d_refract(a, a_du, a_dv, nn, nn_du, nn_dv, v.eta, t_du, t_dv);
     float tb, pb, tt, pt;
     sphcoords(b, tb, pb);
     sphcoords(t, tt, pt);
@@ -645,8 +660,9 @@ SMS_HD void frame_and_derivative(const Vtx &v, f3 &s, f3 &t, f3 &dsdu, f3 &dsdv,
 }
 
 // Half-vector constraint and Newton step (manifold_ss.cpp:407-492).
+// `no`: offset normal; the constraint is H_st - no_xy (manifold_ss.cpp:485-488).
 SMS_HD bool step_halfvector(f3 x, const Vtx &v, f3 lp, float &c0, float &c1,
-                                                float &dx0, float &dx1) {
+                                                float &dx0, float &dx1, f3 no = f3{0.f, 0.f, 1.f}) {
     f3 wo = lp - v.p;
     float ilo = length(wo);
     if (ilo < 1e-3f) return false;
@@ -674,7 +690,7 @@ SMS_HD bool step_halfvector(f3 x, const Vtx &v, f3 lp, float &c0, float &c1,
          dot(dtdu, h) + dot(t, dh_du), dot(dtdv, h) + dot(t, dh_dv)};
     float dj = det2(J);
     if (fabsf(dj) < 1e-6f) return false;
-    c0 = dot(s, h); c1 = dot(t, h);
+    c0 = dot(s, h) - no.x; c1 = dot(t, h) - no.y;
     float id = 1.f / dj;
     dx0 = (J.d * id) * c0 + (-J.b * id) * c1;
     dx1 = (-J.c * id) * c0 + (J.a * id) * c1;
@@ -708,6 +724,71 @@ SMS_HD float fresnel_conductor(float cos_i, float er, float ek) {
     return 0.5f * (rs + rp);
 }
 
+// ------------------------------------------------- Beckmann microfacets
+// Isotropic Beckmann distribution (include/mitsuba/render/microfacet.h): D(m)
+// with the same underflow cut-off, Smith's G1 through Walter et al. 2007's
+// rational approximation (eq. 27 of "Microfacet Models for Refraction through
+// Rough Surfaces"), and sampling of m with density D(m) cos(theta_m).
+SMS_HD float beckmann_D(f3 m, float alpha) {
+    float c2 = m.z * m.z;
+    float r = expf(-((m.x * m.x + m.y * m.y) / (alpha * alpha)) / c2) / (kPi * alpha * alpha * c2 * c2);
+    return r * m.z > 1e-20f ? r : 0.f;
+}
+
+SMS_HD float beckmann_G1(f3 v, f3 m, float alpha) {
+    float xy = alpha * alpha * (v.x * v.x + v.y * v.y);
+    float r;
+    if (xy == 0.f) {
+        r = 1.f;
+    } else {
+        float a = 1.f / sqrtf(xy / (v.z * v.z)), a2 = a * a;
+        r = a >= 1.6f ? 1.f : (3.535f * a + 2.181f * a2) / (1.f + 2.276f * a + 2.577f * a2);
+    }
+    return dot(v, m) * v.z <= 0.f ? 0.f : r;
+}
+
+SMS_HD f3 beckmann_sample(float alpha, float u0, float u1, float &pdf) {
+    float sp, cp;
+#ifdef __CUDA_ARCH__
+    sincosf(2.f * kPi * u1, &sp, &cp);
+#else
+    sp = std::sin(2.f * kPi * u1); cp = std::cos(2.f * kPi * u1);
+#endif
+    float ct = 1.f / sqrtf(1.f - alpha * alpha * logf(1.f - u0));
+    float c2 = ct * ct;
+    pdf = (1.f - u0) / (kPi * alpha * alpha * fmaxf(c2 * ct, 1e-20f));
+    float st = sqrtf(1.f - c2);
+    return mk(cp * st, sp * st, ct);
+}
+
+// Rough conductor BSDF value times cos(theta_o) (roughconductor.cpp eval), local frame.
+SMS_HD float roughconductor_eval(float alpha, float er, float ek, f3 wi, f3 wo) {
+    if (!(wi.z > 0.f && wo.z > 0.f)) return 0.f;
+    f3 h = normalize(wo + wi);
+    float D = beckmann_D(h, alpha);
+    if (D == 0.f) return 0.f;
+    float G = beckmann_G1(wi, h, alpha) * beckmann_G1(wo, h, alpha);
+    return D * G / (4.f * wi.z) * fresnel_conductor(dot(wi, h), er, ek);
+}
+
+// Rough dielectric BSDF value times |cos(theta_o)| (roughdielectric.cpp eval,
+// radiance transport), local frame.
+SMS_HD float roughdielectric_eval(float alpha, float eta_, f3 wi, f3 wo) {
+    const float ci = wi.z, co = wo.z;
+    if (ci == 0.f) return 0.f;
+    const bool reflect = ci * co > 0.f;
+    const float eta = ci > 0.f ? eta_ : 1.f / eta_, inv_eta = ci > 0.f ? 1.f / eta_ : eta_;
+    f3 m = normalize(wi + wo * (reflect ? 1.f : eta));
+    if (m.z < 0.f) m = -m;
+    float D = beckmann_D(m, alpha);
+    float F = fresnel_dielectric(dot(wi, m), eta_);
+    float G = beckmann_G1(wi, m, alpha) * beckmann_G1(wo, m, alpha);
+    if (reflect) return F * D * G / (4.f * fabsf(ci));
+    float den = dot(wi, m) + eta * dot(wo, m);
+    return fabsf((inv_eta * inv_eta) * (1.f - F) * D * G * eta * eta * dot(wi, m) * dot(wo, m) /
+                 (ci * den * den));
+}
+
 // specular_reflectance for smooth BSDFs (manifold_ss.cpp:638-693).
 SMS_HD float specular_reflectance(const DevShape &s, f3 shn, f3 wo) {
     float cos_t = dot(shn, wo);
@@ -718,6 +799,30 @@ SMS_HD float specular_reflectance(const DevShape &s, f3 shn, f3 wo) {
         return (1.f - fresnel_dielectric(cos_t, eta)) * eta * eta;
     }
     return fresnel_conductor(fabsf(cos_t), 0.f, 1.f);
+}
+
+// specular_reflectance of a rough BSDF (manifold_ss.cpp:648-669): the BSDF
+// value for wi (toward the shading point) and wo (toward the light) in the
+// shading frame (n, tangent from dp_du), turned into the half-vector domain.
+SMS_HD float specular_reflectance_rough(const DevShape &s, f3 n, f3 dp_du, f3 wi_w, f3 wo_w) {
+    f3 fs = dp_du - n * dot(n, dp_du);
+    fs = normalize(fs);
+    f3 ft = cross(n, fs);
+    f3 wi = mk(dot(wi_w, fs), dot(wi_w, ft), dot(wi_w, n));
+    f3 wo = mk(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
+    const bool complex_ior = s.bsdf_type == kBsdfConductor && s.k != 0.f;
+    if (complex_ior) {
+        float f = roughconductor_eval(s.alpha, s.eta, s.k, wi, wo);
+        f3 h = normalize(wi + wo);
+        return f * 4.f * fabsf(dot(wo, h));
+    }
+    float f = s.bsdf_type == kBsdfConductor ? roughconductor_eval(s.alpha, s.eta, s.k, wi, wo)
+                                            : roughdielectric_eval(s.alpha, s.eta, wi, wo);
+    float eta = s.eta;
+    if (wi.z < 0.f) eta = 1.f / eta;
+    f3 h = -normalize(wi + wo * eta);
+    float a = dot(wi, h) + eta * dot(wo, h);
+    return f * a * a / (eta * eta * fabsf(dot(wo, h)));
 }
 
 // Generalized geometric term for a positional endpoint (manifold_ss.cpp:695-857,

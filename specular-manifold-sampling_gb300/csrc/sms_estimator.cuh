@@ -108,6 +108,20 @@ SMS_D uint64_t query_stream(const SolverCfg &cfg, uint64_t stream_off, uint32_t 
                        : stream_off + (uint64_t)qi;
 }
 
+// Offset normal of a rough caster (manifold_ss.cpp:60-70): an isotropic
+// Beckmann microfacet normal drawn from the next 2 numbers of rng (the
+// caster's first draws), with density p_off = D(m) cos(theta_m); (0, 0, 1)
+// and 1 for a smooth caster, which draws nothing.
+SMS_D f3 caster_offset(const DevShape &s, Pcg32 &rng, float &p_off) {
+    p_off = 1.f;
+    if (!(s.alpha > 0.f)) return mk(0.f, 0.f, 1.f);
+    const float u0 = rng.next_f32(), u1 = rng.next_f32();
+    return beckmann_sample(s.alpha, u0, u1, p_off);
+}
+
+// Random numbers a caster takes before its walks (the offset normal).
+SMS_D uint32_t caster_draws(const DevShape &s) { return s.alpha > 0.f ? 2u : 0u; }
+
 SMS_D Pcg32 query_rng(uint64_t seed, uint64_t stream, uint64_t position) {
     Pcg32 r;
     r.seed(seed, stream);
@@ -173,7 +187,7 @@ SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
 // sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
 // explicit seed point.  Returns ok; v holds the solution vertex.
 SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
-                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr) {
+                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr, f3 no = f3{0.f, 0.f, 1.f}) {
     f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
     Hit h;
     trace(sc, x, d, kRayEps, INFINITY, false, h, err);
@@ -187,8 +201,8 @@ SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f
     bool accepted = false, conv = false;
     while (it < cfg.max_iterations) {
         float c0, c1, dx0, dx1;
-        bool sok = cfg.halfvector ? step_halfvector(x, v, lp, c0, c1, dx0, dx1)
-                                  : step_anglediff(x, v, lp, c0, c1, dx0, dx1);
+        bool sok = cfg.halfvector ? step_halfvector(x, v, lp, c0, c1, dx0, dx1, no)
+                                  : step_anglediff(x, v, lp, c0, c1, dx0, dx1, no);
         if (!sok) break;
         if (sqrtf(c0 * c0 + c1 * c1) < cfg.solver_threshold) { conv = true; break; }
         f3 pp = v.p - (v.dp_du * dx0 + v.dp_dv * dx1) * (cfg.step_scale * beta);
@@ -218,7 +232,9 @@ SMS_D f3 contribution(const DevScene &sc, f3 x, const Light &L, const Vtx &sol, 
     make_orthonormal(vt.dp_du, vt.dp_dv, vt.dn_du, vt.dn_dv);
     f3 yp, ydu, ydv, lw, lp;
     if (!emitter_endpoint(sc, L, vt.p, yp, ydu, ydv, lw, lp, err, st)) return splat(0.f);
-    float F = specular_reflectance(sc.shapes[vt.shape], vt.n, normalize(lp - vt.p));
+    const DevShape &sh = sc.shapes[vt.shape];
+    float F = sh.alpha > 0.f ? specular_reflectance_rough(sh, vt.n, vt.dp_du, normalize(x - vt.p), normalize(lp - vt.p))
+                             : specular_reflectance(sh, vt.n, normalize(lp - vt.p));
     F *= geometric_term(x, vt, yp, ydu, ydv);
     return lw * F;
 }

@@ -193,8 +193,11 @@ static sms_status check_bsdf(const sms_bsdf *b) {
         return fail(SMS_ERR_INVALID_ARG, "unknown bsdf type");
     if (b->type == SMS_BSDF_DIELECTRIC && !(b->eta > 0.f))
         return fail(SMS_ERR_INVALID_ARG, "dielectric eta must be positive");
+    if (!(b->alpha >= 0.f) || !std::isfinite(b->alpha))
+        return fail(SMS_ERR_INVALID_ARG, "bsdf roughness alpha must be finite and >= 0");
     return SMS_OK;
 }
+
 
 extern "C" sms_status sms_scene_add_sphere(sms_scene *s, const float center[3], float radius, int32_t flip,
                                            const sms_bsdf *bsdf, uint32_t flags, int32_t *id) {
@@ -362,6 +365,9 @@ struct sms_ctx {
     float defensive = 0.1f;
     float *gmm = nullptr;
     uint32_t gmm_n = 0;
+    // offset normals of rough shapes are built for the single-scatter
+    // estimator only: rough multi-scatter chain shapes / glinty shapes
+    bool ms_rough = false, glint_rough = false;
 };
 
 template <typename T>
@@ -459,6 +465,10 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         ds.eta = h.bsdf.eta;
         ds.k = h.bsdf.k;
         ds.albedo[0] = h.bsdf.albedo[0]; ds.albedo[1] = h.bsdf.albedo[1]; ds.albedo[2] = h.bsdf.albedo[2];
+        ds.alpha = h.bsdf.type == SMS_BSDF_DIFFUSE ? 0.f : h.bsdf.alpha;
+        if (ds.alpha > 0.f && (h.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)))
+            c->ms_rough = true;
+        if (ds.alpha > 0.f && (h.flags & SMS_SHAPE_GLINTY)) c->glint_rough = true;
         // manifold.h:94-96: real ior -> eta, complex or non-specular -> 1
         bool real_ior = h.bsdf.type == SMS_BSDF_DIELECTRIC ||
                         (h.bsdf.type == SMS_BSDF_CONDUCTOR && h.bsdf.k == 0.f);
@@ -918,6 +928,8 @@ int set_last_error_impl(int st, const char *msg) {
 static sms_status check_ms_cfg(sms_ctx *c) {
     if (c->cfg.bounces < 1 || c->cfg.bounces > kMaxBounces)
         return fail(SMS_ERR_UNSUPPORTED, "bounces must be between 1 and 4");
+    if (c->ms_rough)
+        return fail(SMS_ERR_UNSUPPORTED, "rough (alpha > 0) multi-scatter chain shapes are not supported");
     return SMS_OK;
 }
 
@@ -1021,6 +1033,7 @@ extern "C" sms_status sms_ms_walk_batch(sms_ctx *c, int32_t caster, const float 
 static sms_status check_glint_scene(sms_ctx *c) {
     if (c->dsc.glinty_shape < 0 || c->dsc.nmap_res == 0)
         return fail(SMS_ERR_INVALID_ARG, "the scene has no normal map (sms_scene_set_normalmap)");
+    if (c->glint_rough) return fail(SMS_ERR_UNSUPPORTED, "rough (alpha > 0) glinty shapes are not supported");
     return SMS_OK;
 }
 

@@ -286,10 +286,86 @@ struct BsdfSample {
     bool delta;
 };
 
-// BSDF::sample of diffuse.cpp, dielectric.cpp, conductor.cpp (smooth),
-// radiance transport, local frame.  Returns false for a zero weight.
+// Density of rough_sample below for the pair (wi, wo): microfacet normal m of
+// the pair, D(m) cos(theta_m) times the Jacobian of the reflection or
+// refraction (the densities of roughconductor.cpp / roughdielectric.cpp pdf
+// with normals drawn from D cos instead of the visible normals).
+SMS_D float rough_pdf(const DevShape &s, f3 wi, f3 wo) {
+    const float ci = wi.z, co = wo.z;
+    if (s.bsdf_type == kBsdfConductor) {
+        if (!(ci > 0.f && co > 0.f)) return 0.f;
+        f3 h = normalize(wo + wi);
+        return beckmann_D(h, s.alpha) * h.z / (4.f * dot(wo, h));
+    }
+    if (ci == 0.f) return 0.f;
+    const bool reflect = ci * co > 0.f;
+    const float eta = ci > 0.f ? s.eta : 1.f / s.eta;
+    f3 m = normalize(wi + wo * (reflect ? 1.f : eta));
+    if (m.z < 0.f) m = -m;
+    if (dot(wi, m) * ci <= 0.f || dot(wo, m) * co <= 0.f) return 0.f;
+    const float F = fresnel_dielectric(dot(wi, m), s.eta);
+    const float pm = beckmann_D(m, s.alpha) * m.z;
+    if (reflect) return F * pm / (4.f * fabsf(dot(wo, m)));
+    const float den = dot(wi, m) + eta * dot(wo, m);
+    return (1.f - F) * pm * eta * eta * fabsf(dot(wo, m)) / (den * den);
+}
+
+// BSDF value x |cos(theta_o)| of the BSDFs emitter sampling evaluates:
+// diffuse (diffuse.cpp eval) and rough (roughconductor.cpp,
+// roughdielectric.cpp eval); delta BSDFs give 0.
+SMS_D f3 bsdf_eval(const DevShape &s, f3 wi, f3 wo) {
+    if (s.bsdf_type == kBsdfDiffuse) {
+        if (!(wi.z > 0.f && wo.z > 0.f)) return splat(0.f);
+        return mk(s.albedo[0], s.albedo[1], s.albedo[2]) * (kInvPi * wo.z);
+    }
+    if (!(s.alpha > 0.f)) return splat(0.f);
+    return splat(s.bsdf_type == kBsdfConductor ? roughconductor_eval(s.alpha, s.eta, s.k, wi, wo)
+                                               : roughdielectric_eval(s.alpha, s.eta, wi, wo));
+}
+
+SMS_D float bsdf_pdf(const DevShape &s, f3 wi, f3 wo) {
+    if (s.bsdf_type == kBsdfDiffuse) return (wi.z > 0.f && wo.z > 0.f) ? kInvPi * wo.z : 0.f;
+    return s.alpha > 0.f ? rough_pdf(s, wi, wo) : 0.f;
+}
+
+// Rough conductor / dielectric sampling: microfacet normal m with density
+// D(m) cos(theta_m) (microfacet.h, sample_visible = false), then reflection
+// about m, or for a dielectric reflection / refraction chosen by the Fresnel
+// reflectance at m (roughdielectric.cpp sample); weight = value / density.
+SMS_D bool rough_sample(const DevShape &s, f3 wi, float u1, float u2, float u3, BsdfSample &bs) {
+    const float ci = wi.z;
+    float pm;
+    const f3 m = beckmann_sample(s.alpha, u2, u3, pm);
+    bs.delta = false;
+    bs.eta = 1.f;
+    if (s.bsdf_type == kBsdfConductor) {
+        if (!(ci > 0.f)) return false;
+        bs.wo = m * (2.f * dot(wi, m)) - wi;
+        if (!(bs.wo.z > 0.f)) return false;
+    } else {
+        float cos_t, eta_it, eta_ti;
+        const float F = fresnel_full(dot(wi, m), s.eta, cos_t, eta_it, eta_ti);
+        if (u1 <= F) {
+            bs.wo = m * (2.f * dot(wi, m)) - wi;
+            if (!(bs.wo.z * ci > 0.f)) return false;
+        } else {
+            bs.wo = m * (dot(wi, m) * eta_ti + cos_t) - wi * eta_ti;
+            if (!(bs.wo.z * ci < 0.f)) return false;
+            bs.eta = eta_it;
+        }
+    }
+    bs.pdf = rough_pdf(s, wi, bs.wo);
+    if (!(bs.pdf > 0.f)) return false;
+    bs.weight = bsdf_eval(s, wi, bs.wo) * (1.f / bs.pdf);
+    return true;
+}
+
+// BSDF::sample of diffuse.cpp, dielectric.cpp, conductor.cpp (smooth) and the
+// rough variants above, radiance transport, local frame.  Returns false for a
+// zero weight.
 SMS_D bool bsdf_sample(const DevShape &s, f3 wi, float u1, float u2, float u3, BsdfSample &bs) {
     const float ci = wi.z;
+    if (s.bsdf_type != kBsdfDiffuse && s.alpha > 0.f) return rough_sample(s, wi, u1, u2, u3, bs);
     if (s.bsdf_type == kBsdfDiffuse) {
         if (!(ci > 0.f)) return false;
         bs.wo = cosine_hemisphere(u2, u3);
@@ -422,10 +498,11 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & kShapeFlagCasterSingle) != 0;
             else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS)
                 on_caster = (s.flags & (kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
-            const bool smooth = s.bsdf_type == kBsdfDiffuse;
+            const bool diffuse = s.bsdf_type == kBsdfDiffuse;
+            const bool smooth = diffuse || s.alpha > 0.f;   // BSDFFlags::Smooth: diffuse or glossy
             const f3 albedo = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
             // ---- SMS query of a receiver vertex (solved after this launch)
-            if (P.integrator != SMS_INTEGRATOR_PATH && receiver && !on_caster && smooth &&
+            if (P.integrator != SMS_INTEGRATOR_PATH && receiver && !on_caster && diffuse &&
                 (P.max_depth < 0 || depth + P.bounces < P.max_depth)) {
                 const float row[kStageRows] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
                                                si.dp_du.x, si.dp_du.y, si.dp_du.z, si.dp_dv.x, si.dp_dv.y, si.dp_dv.z,
@@ -446,11 +523,10 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                     float mint = kRayEps * (1.f + max_abs(si.p));
                     bool occ = trace(sc, si.p, ds.d, mint, ds.dist * (1.f - kShadowEps), true, hs, err);
                     if (!occ && smooth) {
-                        float co = dot(ds.d, n_sh);
-                        if (wi.z > 0.f && co > 0.f) {
-                            f3 bv = albedo * (kInvPi * co);
-                            float bpdf = kInvPi * co;
-                            float w = ds.delta ? 1.f : mis_weight(ds.pdf, bpdf);
+                        const f3 wo = mk(dot(ds.d, fs), dot(ds.d, ft), dot(ds.d, n_sh));
+                        const f3 bv = bsdf_eval(s, wi, wo);
+                        if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
+                            float w = ds.delta ? 1.f : mis_weight(ds.pdf, bsdf_pdf(s, wi, wo));
                             L = L + thr * bv * ds.spec * w;
                         }
                     }

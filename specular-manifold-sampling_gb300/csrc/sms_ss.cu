@@ -103,8 +103,17 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
         if (work && gl == 0) st.conns++;
         f3 acc = splat(0.f);
         int n_unique = 0;
+        uint64_t cpos = 3u;   // stream position of the caster's first draw
         for (int c = 0; c < sc.n_casters_ss; ++c) {
             int caster = sc.casters_ss[c];
+            const DevShape &cs = sc.shapes[caster];
+            float p_off = 1.f;
+            f3 no = mk(0.f, 0.f, 1.f);
+            if (work && cs.alpha > 0.f) {
+                Pcg32 r0 = query_rng(seed, query_stream(cfg, stream_off, qi), cpos);
+                no = caster_offset(cs, r0, p_off);
+            }
+            const uint64_t wpos = cpos + caster_draws(cs);
             int nrec = 0;
             f3 cur = splat(0.f);
             for (int m0 = 0; m0 < M; m0 += G) {
@@ -112,12 +121,12 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
                 bool cand = false;
                 f3 dir = splat(0.f), contrib = splat(0.f);
                 if (work && m < M) {
-                    Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + 2u * ((uint64_t)c * M + m));
+                    Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), wpos + 2u * (uint64_t)m);
                     float sx = rng.next_f32(), sy = rng.next_f32();
-                    f3 sp = sample_position(sc, sc.shapes[caster], sx, sy);
+                    f3 sp = sample_position(sc, cs, sx, sy);
                     Vtx v;
                     int it;
-                    bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
+                    bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no);
                     st.walks++;
                     st.newton += (unsigned)it;
                     if (ok) {
@@ -159,8 +168,9 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
                     __syncwarp();
                 }
             }
-            acc = acc + cur;
+            acc = acc + cur * (1.f / p_off);
             n_unique += nrec;
+            cpos = wpos + 2u * (uint64_t)M;
         }
         if (live && gl == 0) {
             value[qi] = acc.x;
@@ -273,6 +283,9 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
         if (have_light) {
             const int caster = sc.casters_ss[c];
             rng.advance(pos - 3u);
+            float p_off;
+            const f3 no = caster_offset(sc.shapes[caster], rng, p_off);
+            pos += caster_draws(sc.shapes[caster]);
             f3 sp;
             if constexpr (kLearned) {
                 const float us = rng.next_f32(), sx = rng.next_f32(), sy = rng.next_f32();
@@ -285,7 +298,7 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
             }
             Vtx v;
             int it;
-            bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st);
+            bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no);
             st.walks++;
             st.newton += (unsigned)it;
             nw++;
@@ -294,7 +307,8 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
                 if (visible(sc, L.p, v.p, err, st)) {
                     f3 dir = normalize(v.p - Q.x);
                     f3 spec = contribution(sc, Q.x, L, v, err, st);
-                    f3 val = diffuse_eval(Q, dir) * spec;
+                    // the caster's estimate is divided by the offset density (manifold_ss.cpp:199)
+                    f3 val = diffuse_eval(Q, dir) * spec * (1.f / p_off);
                     scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;
                     scr.val[qi] = val.x; scr.val[(size_t)n + qi] = val.y; scr.val[2 * (size_t)n + qi] = val.z;
                     enqueue = true;
@@ -362,6 +376,8 @@ __global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCf
     Light L;
     Pcg32 base;
     f3 dir0 = splat(0.f);
+    f3 no = mk(0.f, 0.f, 1.f);
+    const DevShape &cshape = sc.shapes[caster];
     while (true) {
         // groups without a query take the next one
         const bool need = !have && !drained;
@@ -378,6 +394,13 @@ __global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCf
                 pos = scr.pos[qi];
                 dir0 = mk(scr.dir0[qi], scr.dir0[(size_t)n + qi], scr.dir0[2 * (size_t)n + qi]);
                 t0 = 1;
+                if (cshape.alpha > 0.f) {
+                    // the offset normal drawn before the first walk
+                    Pcg32 r0 = base;
+                    r0.advance((uint64_t)(pos - 3u - kStride - 2u));
+                    float p_off;
+                    no = caster_offset(cshape, r0, p_off);
+                }
             } else {
                 drained = true;
             }
@@ -398,7 +421,7 @@ __global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCf
                 sp = sample_position(sc, sc.shapes[caster], sx, sy);
             }
             Vtx v;
-            succ = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st) &&
+            succ = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no) &&
                    fabsf(dot(dir0, normalize(v.p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
         }
         const unsigned b = (__ballot_sync(full, succ) & gmask) >> gbase;

@@ -14,7 +14,8 @@ silently half-loaded):
       <transform name="to_world"> with translate / scale / matrix children
       (spheres: translate and uniform scale only);
       nested <bsdf>: dielectric (int_ior / ext_ior, names from
-      include/mitsuba/render/ior.h), conductor (eta, k), diffuse (reflectance);
+      include/mitsuba/render/ior.h), conductor (eta, k), diffuse (reflectance),
+      roughdielectric / roughconductor (isotropic Beckmann alpha);
       no bsdf -> diffuse (shape.cpp:73-74);
       nested <emitter type="area"> with radiance (spheres only)
   <emitter type="point">  position (point), intensity (spectrum / rgb / float)
@@ -167,6 +168,19 @@ def _bsdf(sms, el):
     if t == "conductor":
         eta, k = _spectrum(p, "eta", (0.0,) * 3), _spectrum(p, "k", (1.0,) * 3)
         return sms.Bsdf(sms.BSDF_CONDUCTOR, float(np.mean(eta)), float(np.mean(k)))
+    if t in ("roughdielectric", "roughconductor"):
+        # roughdielectric.cpp / roughconductor.cpp: isotropic Beckmann only
+        dist = p["distribution"][1].get("value").lower() if "distribution" in p else "beckmann"
+        if dist != "beckmann":
+            raise ValueError(f"microfacet distribution '{dist}' is not supported (beckmann only)")
+        if "alpha_u" in p or "alpha_v" in p:
+            raise ValueError("anisotropic roughness (alpha_u / alpha_v) is not supported")
+        alpha = _float(p, "alpha", 0.1)
+        if t == "roughdielectric":
+            return sms.Bsdf(sms.BSDF_DIELECTRIC, _float(p, "int_ior", 1.5046) / _float(p, "ext_ior", 1.000277),
+                            alpha=alpha)
+        eta, k = _spectrum(p, "eta", (0.0,) * 3), _spectrum(p, "k", (1.0,) * 3)
+        return sms.Bsdf(sms.BSDF_CONDUCTOR, float(np.mean(eta)), float(np.mean(k)), alpha=alpha)
     if t == "diffuse":
         return sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, _spectrum(p, "reflectance", (0.5,) * 3))
     raise ValueError(f"unsupported bsdf type '{t}'")

@@ -182,3 +182,23 @@ def test_render_argument_errors(sms, workloads, gpu_lib):
     with pytest.raises(sms.SMSError):
         ctx.render(cam, sms.RenderOptions())
     ctx.close()
+
+
+@pytest.mark.parametrize("alpha", [0.2, 0.5])
+def test_rough_caustic_is_unbiased_against_path(sms, workloads, gpu_lib, alpha):
+    """Glossy caustic through a rough dielectric sheet from a point light:
+    path_sms_ss (offset normals, half-vector constraints) against plain path
+    tracing, which reaches the light by emitter sampling at the rough vertex.
+    Camera under the sheet: every light path crosses it."""
+    W = workloads
+    d = sms.SceneDesc()
+    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
+    d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3),
+               sms.SHAPE_CAUSTIC_RECEIVER, UV=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
+    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.3, [])
+    d.add_mesh(P, F, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5, alpha=alpha), sms.SHAPE_CAUSTIC_CASTER_SINGLE, N=N, UV=UV)
+    d.add_point_emitter((0.3, 0.2, 4.0), (40.0,) * 3, sms.EMITTER_CAUSTIC_SINGLE)
+    ctx = sms.Context(sms.Scene(d), sms.SMSConfig(biased=False, max_trials=-1, halfvector_constraints=True))
+    cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 32, 32)
+    _compare_integrators(sms, ctx, cam, "path_sms_ss", 8192, 256, 4)
+    ctx.close()

@@ -252,3 +252,60 @@ def test_mnee_init_walks_and_connect(sms, workloads, oracle, gpu_lib, conductor)
     vo, co, wo, _ = oracle.OracleScene(desc).connect_batch(bcfg, q, seed=2)
     assert np.all(cg <= 1) and np.mean(cg == co) > 1 - STRICT_MISMATCH
     ctx.close()
+
+
+def _rough_scene(sms, W, conductor, alpha):
+    """A rough caster over a point light's receiver plane: a flat Beckmann
+    dielectric sheet (refraction) or a rough conductor sphere (reflection)."""
+    d = sms.SceneDesc()
+    if conductor:
+        d.add_sphere((0.0, 0.0, 1.5), 1.0, sms.Bsdf(sms.BSDF_CONDUCTOR, 0.2, 3.0, alpha=alpha),
+                     sms.SHAPE_CAUSTIC_CASTER_SINGLE)
+        d.add_point_emitter((0.0, 0.0, 5.0), (100.0,) * 3, sms.EMITTER_CAUSTIC_SINGLE)
+    else:
+        P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.3, [])
+        d.add_mesh(P, F, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5, alpha=alpha), sms.SHAPE_CAUSTIC_CASTER_SINGLE,
+                   N=N, UV=UV)
+        d.add_point_emitter((0.3, 0.2, 4.0), (40.0,) * 3, sms.EMITTER_CAUSTIC_SINGLE)
+    return d
+
+
+@pytest.mark.parametrize("biased", [True, False])
+@pytest.mark.parametrize("conductor", [False, True])
+def test_rough_caster_connect(sms, workloads, oracle, gpu_lib, biased, conductor):
+    """Rough casters: each query draws a Beckmann offset normal after its
+    emitter sample (manifold_ss.cpp:60-70), walks to the offset-normal
+    constraint and divides by the offset density; the glossy reflectance is
+    the BSDF value in the half-vector domain (:648-669).  GPU vs oracle on the
+    same random streams, against the oracle-vs-FMA floor."""
+    W = workloads
+    desc = _rough_scene(sms, W, conductor, 0.2)
+    cfg = sms.SMSConfig(biased=True, max_trials=16) if biased else sms.SMSConfig(biased=False, max_trials=256)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    q = W.sphere_queries(48) if conductor else W.plane_queries(
+        (W.pcg32_streams_f32(9, np.arange(4096, dtype=np.uint64), 2).T * 1.6 - 0.8).astype(np.float32))
+    vg, cg, wg = sms.SpecularManifoldSingleScatter(ctx).specular_manifold_sampling(q, seed=3)
+    vo, co, wo, _ = oracle.OracleScene(desc).connect_batch(cfg, q, seed=3)
+    vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=3)
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    print(f"rough conductor={conductor} biased={biased}: count mismatch {g_cm:.4f} differs {g_diff:.4f} "
+          f"(floor {f_cm:.4f}/{f_diff:.4f}) median rel {g_med:.1e} nonzero {np.mean(vo[0] > 0):.3f}")
+    assert np.mean(vo[0] > 0) > 0.05                 # the glossy caustic is there
+    assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+    assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+    assert g_med < 1e-3
+    ctx.close()
+
+
+def test_rough_multi_scatter_and_glints_are_refused(sms, workloads, gpu_lib):
+    W = workloads
+    d = sms.SceneDesc()
+    P, N, UV, F = W.heightfield_mesh(8, 1.0, 1.3, [])
+    d.add_mesh(P, F, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5, alpha=0.1), sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    d.add_point_emitter((0.0, 0.0, 4.0), (40.0,) * 3, sms.EMITTER_CAUSTIC_MULTI)
+    ctx = sms.Context(sms.Scene(d), sms.SMSConfig(bounces=1, biased=True, max_trials=4))
+    with pytest.raises(sms.SMSError) as e:
+        sms.SpecularManifoldMultiScatter(ctx).specular_manifold_sampling(W.sphere_queries(4))
+    assert e.value.status == 4
+    ctx.close()

@@ -98,7 +98,9 @@ def test_obj_shape_and_area_emitter(sms, tmp_path):
 
 @pytest.mark.parametrize("body,what", [
     ('<shape type="cylinder"/>', "cylinder"),
-    ('<shape type="sphere"><bsdf type="roughconductor"/></shape>', "roughconductor"),
+    ('<shape type="sphere"><bsdf type="roughconductor"><string name="distribution" value="ggx"/></bsdf></shape>',
+     "ggx"),
+    ('<shape type="sphere"><bsdf type="plastic"/></shape>', "plastic"),
     ('<emitter type="envmap"/>', "envmap"),
     ('<shape type="sphere"><transform name="to_world"><rotate x="1" angle="3"/></transform></shape>',
      "translation and a uniform scale"),
@@ -153,3 +155,18 @@ def test_render_setup_from_xml(sms, workloads, tmp_path):
     path.write_text(RENDER_XML.replace('type="path_sms_ss"', 'type="bdpt"'))
     with pytest.raises(ValueError):
         sms.load_render_setup(path)
+
+
+def test_rough_bsdfs_from_xml(sms, tmp_path):
+    body = """<scene version="2.0.0">
+      <shape type="sphere"><float name="radius" value="1"/>
+        <bsdf type="roughdielectric"><float name="alpha" value="0.3"/><float name="int_ior" value="1.5"/>
+          <float name="ext_ior" value="1.0"/></bsdf></shape>
+      <shape type="sphere"><float name="radius" value="1"/>
+        <bsdf type="roughconductor"><float name="alpha" value="0.05"/></bsdf></shape>
+    </scene>"""
+    (tmp_path / "rough.xml").write_text(body)
+    desc, _, _ = sms.load_scene(tmp_path / "rough.xml")
+    b0, b1 = desc.spheres[0][3], desc.spheres[1][3]
+    assert b0.type == sms.BSDF_DIELECTRIC and b0.alpha == pytest.approx(0.3) and b0.eta == pytest.approx(1.5)
+    assert b1.type == sms.BSDF_CONDUCTOR and b1.alpha == pytest.approx(0.05)

@@ -497,9 +497,10 @@ typedef struct sms_camera {
 #define SMS_FOV_SMALLER  3
 #define SMS_FOV_LARGER   4
 
-#define SMS_INTEGRATOR_PATH        0
-#define SMS_INTEGRATOR_PATH_SMS_SS 1
-#define SMS_INTEGRATOR_PATH_SMS_MS 2
+#define SMS_INTEGRATOR_PATH            0
+#define SMS_INTEGRATOR_PATH_SMS_SS     1
+#define SMS_INTEGRATOR_PATH_SMS_MS     2
+#define SMS_INTEGRATOR_PATH_SMS_GLINTS 3   /* src/integrators/path_sms_glints.cpp:62-194 */
 typedef struct sms_render_options {
     int32_t  integrator;                 /* SMS_INTEGRATOR_*                        */
     int32_t  max_depth;                  /* -1 = unbounded                          */
@@ -509,6 +510,9 @@ typedef struct sms_render_options {
     int32_t  biased_mnee;                /* path_sms_ss (false)                     */
     uint64_t seed;                       /* 0                                       */
     uint32_t max_paths;                  /* paths per wavefront, 0 = 1,048,576      */
+    float    glint_diff_scale_factor_clamp; /* 0: ray differentials of the camera are
+                                           scaled by max(1/sqrt(spp), this)
+                                           (src/librender/integrator.cpp:41,164-165) */
 } sms_render_options;
 void sms_render_options_default(sms_render_options *opt);
 
@@ -521,7 +525,17 @@ uint64_t sms_render_sms_seed(uint64_t seed);
  * and is asynchronous on the context stream apart from one small
  * device-to-host read per bounce (the number of SMS queries).
  * path_sms_ms with mnee_init and without biased_mnee returns
- * SMS_ERR_UNSUPPORTED (its MNEE bookkeeping is not implemented). */
+ * SMS_ERR_UNSUPPORTED (its MNEE bookkeeping is not implemented).
+ *
+ * path_sms_glints: camera rays carry ray differentials; at the first hit of
+ * the glinty shape the glint estimator (the context's config) runs over the
+ * pixel footprint, weighted by the sensor importance and MIS against a BSDF
+ * sample inside the footprint, both with the LEAN-mapping density of the
+ * footprint (manifold_glints.cpp:28-223, the LEAN mip pyramid of
+ * src/librender/normalmap.cpp, include/mitsuba/render/lean.h); the
+ * normal-mapped conductor reflects about the bilinear slope normal elsewhere.
+ * The LEAN pyramid (5 floats per texel over all levels, 4/3 x 20 bytes per
+ * texel of the slope map) is built on the device at the first glint render. */
 sms_status sms_render(sms_ctx *ctx, const sms_camera *cam, const sms_render_options *opt, float *image);
 sms_status sms_render_device(sms_ctx *ctx, const sms_camera *cam, const sms_render_options *opt,
                              float *image_dev);

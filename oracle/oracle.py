@@ -44,10 +44,11 @@ class _Camera(C.Structure):
 class _RenderOptions(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
                 ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
-                ("seed", C.c_uint64), ("max_paths", C.c_uint32)]
+                ("seed", C.c_uint64), ("max_paths", C.c_uint32),
+                ("glint_diff_scale_factor_clamp", C.c_float)]
 
 
-_INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2}
+_INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3}
 _FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 
@@ -93,6 +94,7 @@ def load(fma: bool = False):
         "oracle_ss_connect_learned_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, i32, f32, vp, vp,
                                                   vp, vp, vp, C.c_int, vp]),
         "oracle_fresnel": (f32, [f32, f32, C.POINTER(f32)]),
+        "oracle_glint_lean_pdf": (f32, [vp, f32, f32, vp, vp, vp]),
         "oracle_render": (i32, [vp, C.POINTER(_Config), C.POINTER(_Camera), C.POINTER(_RenderOptions), vp, C.c_int]),
         "oracle_fresnel_conductor": (f32, [f32, f32, f32]),
         "oracle_uniform_sphere": (None, [f32, f32, C.POINTER(f32)]),
@@ -252,6 +254,13 @@ class OracleScene:
                  "bernoulli_trial_iterations_max", "walks", "newton_iterations", "connections"]
         return value, count, walks, dict(zip(names, stats.tolist()))
 
+    def glint_lean_pdf(self, u: float, v: float, duv, wi, wo) -> float:
+        """LEAN-mapping density of the glints integrator's MIS (local frame)."""
+        a = np.ascontiguousarray(duv, np.float32)
+        b = np.ascontiguousarray(wi, np.float32)
+        c = np.ascontiguousarray(wo, np.float32)
+        return float(self._lib.oracle_glint_lean_pdf(self._h, u, v, a.ctypes.data, b.ctypes.data, c.ctypes.data))
+
     def render(self, config, camera, options, nthreads: int | None = None) -> np.ndarray:
         """The library's sms_render restated path by path: camera / options
         are objects with the fields of the library's Camera / RenderOptions."""
@@ -267,6 +276,7 @@ class OracleScene:
         o.max_depth, o.rr_depth, o.spp = options.max_depth, options.rr_depth, options.spp
         o.disable_reflected_emitters = int(options.disable_reflected_emitters)
         o.biased_mnee, o.seed, o.max_paths = int(options.biased_mnee), options.seed, options.max_paths
+        o.glint_diff_scale_factor_clamp = float(getattr(options, "glint_diff_scale_factor_clamp", 0.0))
         img = np.zeros((camera.height, camera.width, 3), np.float32)
         nt = nthreads or os.cpu_count() or 1
         self._lib.oracle_render(self._h, C.byref(_cfg(config)), C.byref(cam), C.byref(o), img.ctypes.data, nt)

@@ -164,6 +164,9 @@ struct NormalMap {
     uint32_t res = 0;
     float tiles = 1.f;
     std::vector<float> sx, sy;
+    /* LEAN mip pyramid (src/librender/normalmap.cpp:36-89): per level, 5
+     * floats per texel (sx, sy, sx^2 + s0, sy^2 + s0, sx sy); built on first use */
+    std::vector<std::vector<float>> lean;
 };
 
 struct Scene {
@@ -2268,6 +2271,170 @@ static bool pt_bsdf_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u
     return true;
 }
 
+/* ---- LEAN mapping for the glints integrator ---------------------------
+ * Level 0 from the slope map with the base variance 0.5 * 1e-4^2 of
+ * normalmap.cpp:36-40; each coarser level the 2x2 box average of the finer one
+ * (Bitmap::resample with a box filter at exactly half the size). */
+static void build_lean(NormalMap &m) {
+    if (!m.lean.empty() || m.res == 0) return;
+    const float base_sigma_2 = 0.5f * 0.0001f * 0.0001f;
+    std::vector<float> l0(5 * (size_t)m.res * m.res);
+    for (size_t i = 0; i < (size_t)m.res * m.res; ++i) {
+        float x = m.sx[i], y = m.sy[i];
+        l0[5 * i] = x; l0[5 * i + 1] = y;
+        l0[5 * i + 2] = x * x + base_sigma_2; l0[5 * i + 3] = y * y + base_sigma_2; l0[5 * i + 4] = x * y;
+    }
+    m.lean.push_back(std::move(l0));
+    uint32_t res = m.res;
+    while (res > 1) {
+        uint32_t r2 = res / 2;
+        const std::vector<float> &src = m.lean.back();
+        std::vector<float> dst(5 * (size_t)r2 * r2);
+        for (uint32_t y = 0; y < r2; ++y)
+            for (uint32_t x = 0; x < r2; ++x)
+                for (int c = 0; c < 5; ++c) {
+                    float a = src[5 * ((size_t)(2 * y) * res + 2 * x) + c] + src[5 * ((size_t)(2 * y) * res + 2 * x + 1) + c];
+                    float b = src[5 * ((size_t)(2 * y + 1) * res + 2 * x) + c] +
+                              src[5 * ((size_t)(2 * y + 1) * res + 2 * x + 1) + c];
+                    dst[5 * ((size_t)y * r2 + x) + c] = 0.25f * (a + b);
+                }
+        m.lean.push_back(std::move(dst));
+        res = r2;
+    }
+}
+
+/* NormalmapBSDF::mipmap_level (normalmap.cpp:374-388); a footprint finer than
+ * a texel (negative level) takes level 0 */
+static int lean_level(const NormalMap &m, V2 duv_dx, V2 duv_dy) {
+    const int L = (int)m.lean.size();
+    float w = 2.f * std::max(std::max(std::fabs(m.tiles * duv_dx.x), std::fabs(m.tiles * duv_dx.y)),
+                             std::max(std::fabs(m.tiles * duv_dy.x), std::fabs(m.tiles * duv_dy.y)));
+    float lv = std::ceil((float)(L - 1) + std::log2(std::max(w, 1e-8f)));
+    if (!(lv > 0.f)) return 0;
+    return (int)std::min(lv, (float)(L - 1));
+}
+
+/* Bilinear LEAN lookup (normalmap.h:62-104, 199-233): mean slope mu and
+ * covariance (a, c; c, b) at the tiled uv on level l */
+static void lean_lookup(const NormalMap &m, V2 uv_in, int l, V2 &mu, float &sa, float &sb, float &sc) {
+    uint32_t res = m.res >> l;
+    float u = uv_in.x * m.tiles, v = uv_in.y * m.tiles;
+    u -= std::floor(u); v -= std::floor(v);
+    float fr = (float)res, duv = 1.f / fr;
+    float px = std::min(std::max((u - 0.5f * duv) * fr, 0.f), fr - 1.f);
+    float py = std::min(std::max((v - 0.5f * duv) * fr, 0.f), fr - 1.f);
+    uint32_t x0 = (uint32_t)std::floor(px), y0 = (uint32_t)std::floor(py);
+    uint32_t x1 = std::min(x0 + 1, res - 1), y1 = std::min(y0 + 1, res - 1);
+    x0 = std::min(x0, res - 1); y0 = std::min(y0, res - 1);
+    float wx = px - (float)x0, wy = py - (float)y0;
+    const std::vector<float> &d = m.lean[l];
+    float vv[5];
+    for (int c = 0; c < 5; ++c) {
+        float v00 = d[5 * ((size_t)y0 * res + x0) + c], v10 = d[5 * ((size_t)y0 * res + x1) + c];
+        float v01 = d[5 * ((size_t)y1 * res + x0) + c], v11 = d[5 * ((size_t)y1 * res + x1) + c];
+        float a = (1.f - wx) * v00 + wx * v10, b = (1.f - wx) * v01 + wx * v11;
+        vv[c] = (1.f - wy) * a + wy * b;
+    }
+    mu.x = vv[0]; mu.y = vv[1];
+    sa = std::max(0.f, vv[2] - vv[0] * vv[0]);
+    sb = std::max(0.f, vv[3] - vv[1] * vv[1]);
+    sc = std::max(0.f, vv[4] - vv[0] * vv[1]);
+}
+
+/* LEAN/LEADR distribution (include/mitsuba/render/lean.h, after Dupuy's
+ * reference implementation): parameters from the LEAN moments plus a base
+ * Beckmann roughness, visible-normal density, shadowing. */
+struct LeanP { V3 n; float ax, ay, rho, srho, tx, ty; };
+static LeanP lean_params(V2 mu, float sa, float sb, float sc, float alpha) {
+    float e1 = mu.x, e2 = mu.y;
+    float lax = std::sqrt(2.f * sa), lay = std::sqrt(2.f * sb);
+    float rho = 2.f * sc / (lax * lay);
+    float e3 = 0.5f * lax * lax + e1 * e1 + 0.5f * alpha * alpha;
+    float e4 = 0.5f * lay * lay + e2 * e2 + 0.5f * alpha * alpha;
+    float e5 = 0.5f * rho * lax * lay + e1 * e2;
+    LeanP p;
+    p.tx = e1; p.ty = e2;
+    p.ax = std::sqrt(2.f * std::max(0.f, e3 - e1 * e1));
+    p.ay = std::sqrt(2.f * std::max(0.f, e4 - e2 * e2));
+    p.rho = 2.f * (e5 - e1 * e2) / (p.ax * p.ay);
+    p.srho = std::sqrt(1.f - p.rho * p.rho);
+    p.n = normalize(V3(-p.tx, -p.ty, 1.f));
+    return p;
+}
+static float lean_sigma_std(float ct) {
+    if (ct == 1.f) return 1.f;
+    float st = std::sqrt(1.f - ct * ct), nu = ct / st;
+    float tmp = std::exp(-nu * nu) * 0.56418958354775628695f;   /* 1 / sqrt(pi) */
+    return 0.5f * (ct * (1.f + std::erf(nu)) + st * tmp);
+}
+static float lean_sigma(V3 k, const LeanP &p) {
+    float a = k.x * p.ax + k.y * p.ay * p.rho, b = k.y * p.ay * p.srho, c = k.z - k.x * p.tx - k.y * p.ty;
+    float nrm = std::sqrt(a * a + b * b + c * c);
+    return nrm * lean_sigma_std(c / nrm);
+}
+static float lean_g1(V3 k, const LeanP &p) { return dot(k, p.n) > 0.f ? k.z / lean_sigma(k, p) : 0.f; }
+static float lean_ndf(V3 h, const LeanP &p) {
+    if (!(h.z > 5.9604644775390625e-08f)) return 0.f;
+    float t1 = h.z * h.z, t2 = t1 * t1;
+    float sx = -h.x / h.z - p.tx, sy = -h.y / h.z - p.ty;
+    float nrm = p.ax * p.ay * p.srho;
+    float x = sx / p.ax, y = (p.ax * sy - p.rho * p.ay * sx) / (p.ax * p.ay * p.srho);
+    return kInvPi * std::exp(-(x * x + y * y)) / nrm / t2;
+}
+/* SpecularManifoldGlints::lean_pdf (manifold_glints.cpp:557-579), local frame */
+static float glint_lean_pdf(const NormalMap &m, V2 uv, V2 duv_dx, V2 duv_dy, V3 wi, V3 wo) {
+    if (wi.z < 0.f || wo.z < 0.f) return 0.f;
+    V2 mu; float sa, sb, sc;
+    lean_lookup(m, uv, lean_level(m, duv_dx, duv_dy), mu, sa, sb, sc);
+    LeanP p = lean_params(mu, sa, sb, sc, 0.f);
+    V3 h = normalize(wo + wi);
+    float G = lean_g1(wo, p) * lean_g1(wi, p);   /* LEAN::gaf: G1 ignores h */
+    if (!(G > 0.f)) return 0.f;
+    float dp = dot(wi, h);
+    float vndf = dp > 0.f ? dp * lean_ndf(h, p) / lean_sigma(wi, p) : 0.f;
+    return vndf / (4.f * dot(wi, h));
+}
+
+/* NormalmapBSDF::frame (normalmap.cpp:236-257) at level 0: the base shading
+ * frame (n, tangent from dp_du) tilted to the bilinear slope normal */
+static void nm_frame(const NormalMap &m, V3 n, V3 dp_du, V2 uv, V3 &pn, V3 &ps, V3 &pt) {
+    V3 bs = normalize(dp_du - n * dot(n, dp_du)), bt = cross(n, bs);
+    V2 sl = nm_slope(m, uv);
+    pn = normalize(bs * -sl.x + bt * -sl.y + n);
+    ps = normalize(dp_du - pn * dot(pn, dp_du));
+    pt = cross(pn, ps);
+}
+
+/* NormalmapBSDF::sample with a smooth conductor inside (normalmap.cpp:
+ * 116-139, conductor.cpp sample): reflection about the perturbed normal,
+ * world-space directions; weight = Fresnel. */
+static bool nm_conductor_sample(const NormalMap &m, const sms_bsdf &b, V3 n, V3 dp_du, V2 uv, V3 wi_w,
+                                V3 &wo_w, float &weight) {
+    V3 pn, ps, pt;
+    nm_frame(m, n, dp_du, uv, pn, ps, pt);
+    float ci = dot(wi_w, pn);
+    if (!(ci > 0.f)) return false;
+    wo_w = pn * (2.f * ci) - wi_w;
+    if (!(dot(wo_w, n) * dot(wo_w, pn) > 0.f)) return false;
+    weight = fresnel_conductor(ci, b.eta, b.k);
+    return true;
+}
+
+/* PerspectiveCamera::importance (perspective.cpp:224-276) x film size for the
+ * world-space direction d from the camera */
+static float pt_importance(const sms_camera &cam, const double tm[2], V3 d) {
+    const float *M = cam.to_world;
+    V3 dl(M[0] * d.x + M[4] * d.y + M[8] * d.z, M[1] * d.x + M[5] * d.y + M[9] * d.z,
+          M[2] * d.x + M[6] * d.y + M[10] * d.z);
+    if (!(dl.z > 0.f)) return 0.f;
+    float ic = 1.f / dl.z;
+    float px = dl.x * ic, py = dl.y * ic;
+    float tx = (float)tm[0], ty = (float)tm[1];
+    if (!(px >= -tx && px <= tx && py >= -ty && py <= ty)) return 0.f;
+    float norm_ = 1.f / (4.f * tx * ty);
+    return norm_ * ic * ic * ic * (float)cam.width * (float)cam.height;
+}
+
 /* One camera sample (path id g) of the integrator; returns its radiance. */
 static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &cam, const sms_render_options &opt,
                     const double tm[2], uint64_t g, Stats &st) {
@@ -2289,6 +2456,19 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
     float near_clip = cam.near_clip > 0.f ? cam.near_clip : 1e-2f;
     float far_clip = cam.far_clip > near_clip ? cam.far_clip : 1e4f;
     ray.mint = near_clip * inv_z; ray.maxt = far_clip * inv_z;
+    /* ray differentials (perspective.cpp:198-220), scaled by
+       max(1/sqrt(spp), glint_diff_scale_factor_clamp) (integrator.cpp:164-165) */
+    V3 rdx, rdy;
+    {
+        auto cam_dir = [&](float ax, float ay) {
+            V3 c = normalize(V3((float)tm[0] * (1.f - 2.f * ax), (float)tm[1] * (1.f - 2.f * ay), 1.f));
+            return normalize(V3(M[0] * c.x + M[1] * c.y + M[2] * c.z, M[4] * c.x + M[5] * c.y + M[6] * c.z,
+                                M[8] * c.x + M[9] * c.y + M[10] * c.z));
+        };
+        float scale = std::max(1.f / std::sqrt((float)opt.spp), opt.glint_diff_scale_factor_clamp);
+        rdx = ray.d + (cam_dir(sx + 1.f / (float)cam.width, sy) - ray.d) * scale;
+        rdy = ray.d + (cam_dir(sx, sy + 1.f / (float)cam.height) - ray.d) * scale;
+    }
     SI si = ray_intersect(sc, ray);
     V3 L(0.f), thr(1.f);
     float eta = 1.f;
@@ -2317,7 +2497,70 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         else if (integ == SMS_INTEGRATOR_PATH_SMS_MS)
             on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
         const bool diffuse = s.bsdf.type == SMS_BSDF_DIFFUSE;
-        const bool smooth = diffuse || is_rough(s.bsdf);   /* BSDFFlags::Smooth: diffuse or glossy */
+        /* the glinty shape carries a normal-mapped conductor (delta reflection) */
+        const bool nmapped = si.shape == sc.glinty_shape && sc.nmap.res > 0;
+        const bool smooth = !nmapped && (diffuse || is_rough(s.bsdf));   /* BSDFFlags::Smooth */
+        const bool on_glinty = integ == SMS_INTEGRATOR_PATH_SMS_GLINTS && depth == 1 && nmapped &&
+                               (s.flags & SMS_SHAPE_GLINTY);
+        if (on_glinty) {
+            /* SurfaceInteraction::compute_partials (interaction.h:216-248) */
+            float dn = dot(si.n, si.p);
+            V3 dp_dx = ray.o + rdx * ((dn - dot(si.n, ray.o)) / dot(si.n, rdx)) - si.p;
+            V3 dp_dy = ray.o + rdy * ((dn - dot(si.n, ray.o)) / dot(si.n, rdy)) - si.p;
+            float a00 = dot(si.dp_du, si.dp_du), a01 = dot(si.dp_du, si.dp_dv), a11 = dot(si.dp_dv, si.dp_dv);
+            float inv_det = 1.f / (a00 * a11 - a01 * a01);
+            if (!std::isfinite(inv_det)) inv_det = 0.f;
+            float b0x = dot(si.dp_du, dp_dx), b1x = dot(si.dp_dv, dp_dx);
+            float b0y = dot(si.dp_du, dp_dy), b1y = dot(si.dp_dv, dp_dy);
+            GQuery gq;
+            gq.p = si.p; gq.n = si.shn; gq.dp_du = si.dp_du; gq.dp_dv = si.dp_dv; gq.sensor = ray.o; gq.uv = si.uv;
+            gq.duv_dx.x = (a11 * b0x - a01 * b1x) * inv_det; gq.duv_dx.y = (a00 * b1x - a01 * b0x) * inv_det;
+            gq.duv_dy.x = (a11 * b0y - a01 * b1y) * inv_det; gq.duv_dy.y = (a00 * b1y - a01 * b0y) * inv_det;
+            V3 fs0 = normalize(si.dp_du - si.shn * dot(si.shn, si.dp_du)), ft0 = cross(si.shn, fs0);
+            auto local = [&](V3 w) { return V3(dot(w, fs0), dot(w, ft0), dot(w, si.shn)); };
+            const V3 wi_l = local(-ray.d);
+            /* SMS strategy (manifold_glints.cpp:40-176) */
+            PCG32 grng;
+            grng.seed(sms_seed(opt.seed), g + (1ull << 48));
+            int gc = 0, gw = 0;
+            V3 gv = glint_connect(sc, cfg, gq, grng, gc, gw, st);
+            if (gv.x != 0.f || gv.y != 0.f || gv.z != 0.f) {
+                PCG32 r2;
+                r2.seed(sms_seed(opt.seed), g + (1ull << 48));
+                Query qq; qq.p = si.p;
+                EI ei = sample_emitter_interaction(sc, sc.emitters_all, qq, r2);
+                V3 ed = ei.p - si.p;
+                float edist = norm(ed);
+                ed *= 1.f / edist;
+                float p_sms = 1.f;
+                if (!ei.is_point) p_sms = pt_emitter_pdf(sc, sc.shapes[sc.emitters[ei.emitter].shape], si.p, ei.p, ed, edist);
+                float p_bsdf = glint_lean_pdf(sc.nmap, gq.uv, gq.duv_dx, gq.duv_dy, local(normalize(gq.sensor - si.p)),
+                                              local(ed)) + 1.f;
+                float mis = cfg.bsdf_strategy_only ? 0.f : mis_weight(p_sms, p_bsdf);
+                float We = pt_importance(cam, tm, normalize(si.p - ray.o));
+                L += thr * gv * (mis * We);
+            }
+            /* BSDF strategy inside the footprint (manifold_glints.cpp:178-220) */
+            V2 fp = rng.next_2d();
+            (void)rng.next_f32(); (void)rng.next_2d();
+            V2 uvo;
+            uvo.x = si.uv.x + (fp.x - 0.5f) * gq.duv_dx.x + (fp.y - 0.5f) * gq.duv_dy.x;
+            uvo.y = si.uv.y + (fp.x - 0.5f) * gq.duv_dx.y + (fp.y - 0.5f) * gq.duv_dy.y;
+            V3 bwo; float bw;
+            if (nm_conductor_sample(sc.nmap, s.bsdf, si.shn, si.dp_du, uvo, -ray.d, bwo, bw)) {
+                Ray br; br.o = si.p; br.d = bwo; br.mint = kRayEps * (1.f + hmax_abs(si.p)); br.maxt = kInf;
+                SI sb = ray_intersect(sc, br);
+                if (sb.valid() && sc.shapes[sb.shape].emitter >= 0) {
+                    const Shape &es = sc.shapes[sb.shape];
+                    V3 ep = br.o + br.d * sb.t;
+                    V3 Le = pt_emitted(sc, es, ep, br.d);
+                    float p_bsdf = glint_lean_pdf(sc.nmap, uvo, gq.duv_dx, gq.duv_dy, wi_l, local(bwo)) + 1.f;
+                    float p_sms = pt_emitter_pdf(sc, es, si.p, ep, bwo, sb.t);
+                    float mis = cfg.sms_strategy_only ? 0.f : mis_weight(p_bsdf, p_sms);
+                    L += thr * Le * (mis * bw);
+                }
+            }
+        }
         V3 albedo(s.bsdf.albedo[0], s.bsdf.albedo[1], s.bsdf.albedo[2]);
         /* SMS at a receiver (path_sms_ss.cpp:115-121, path_sms_ms.cpp:226-232) */
         if (integ != SMS_INTEGRATOR_PATH && receiver && !on_caster && diffuse &&
@@ -2332,7 +2575,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             L += thr * v;
         }
         /* emitter sampling */
-        bool nee = smooth && !on_caster;
+        bool nee = smooth && !on_caster && !on_glinty;
         if (integ == SMS_INTEGRATOR_PATH_SMS_SS) nee = nee || (depth == 1 && !opt.disable_reflected_emitters);
         if (nee) {
             float ex = rng.next_f32(), ey = rng.next_f32();
@@ -2353,7 +2596,13 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         /* BSDF sampling */
         float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
         PtBsdf bs;
-        if (!pt_bsdf_sample(s.bsdf, wi, u1, u2, u3, bs)) break;
+        if (nmapped) {
+            /* normal-mapped conductor at the hit's own uv */
+            V3 wo_w; float w;
+            if (!nm_conductor_sample(sc.nmap, s.bsdf, si.shn, si.dp_du, si.uv, wiw, wo_w, w)) break;
+            bs.wo = V3(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n_sh));
+            bs.weight = V3(w); bs.pdf = 1.f; bs.eta = 1.f; bs.delta = true;
+        } else if (!pt_bsdf_sample(s.bsdf, wi, u1, u2, u3, bs)) break;
         thr = thr * bs.weight;
         eta *= bs.eta;
         if (!bs.delta) spec_cam = false;
@@ -2369,6 +2618,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             bool allow = true;
             if (integ == SMS_INTEGRATOR_PATH_SMS_SS) allow = !on_caster || (depth == 1 && !opt.disable_reflected_emitters);
             else if (integ == SMS_INTEGRATOR_PATH_SMS_MS) allow = !on_caster || spec_cam;
+            else if (integ == SMS_INTEGRATOR_PATH_SMS_GLINTS) allow = !on_glinty;
             if (allow) {
                 float epdf = bs.delta ? 0.f : pt_emitter_pdf(sc, es, si.p, ep, nr.d, si2.t);
                 L += thr * Le * mis_weight(bs.pdf, epdf);
@@ -2860,6 +3110,7 @@ int oracle_render(void *s, const sms_config *cfg, const sms_camera *cam, const s
                   float *image, int nthreads) {
     Scene *sc = as_scene(s);
     if (!sc->finalized) oracle_scene_finalize(s);
+    if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS) build_lean(sc->nmap);
     const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
     const double aspect = (double)cam->width / (double)cam->height;
     const double t = std::tan(0.5 * (double)cam->fov * 3.14159265358979323846 / 180.0);
@@ -2895,6 +3146,18 @@ int oracle_render(void *s, const sms_config *cfg, const sms_camera *cam, const s
         for (int c = 0; c < 3; ++c) image[3 * p + c] = acc[c] * (1.f / (float)opt->spp);
     }
     return 0;
+}
+
+/* LEAN density of the glints integrator's MIS (glint_lean_pdf) for tests:
+ * duv = (duv_dx, duv_dy), wi / wo in the local frame of the glinty shape. */
+float oracle_glint_lean_pdf(void *s, float u, float v, const float *duv, const float *wi, const float *wo) {
+    Scene *sc = as_scene(s);
+    if (!sc->finalized) oracle_scene_finalize(s);
+    build_lean(sc->nmap);
+    V2 uv; uv.x = u; uv.y = v;
+    V2 dx; dx.x = duv[0]; dx.y = duv[1];
+    V2 dy; dy.x = duv[2]; dy.y = duv[3];
+    return glint_lean_pdf(sc->nmap, uv, dx, dy, V3(wi[0], wi[1], wi[2]), V3(wo[0], wo[1], wo[2]));
 }
 
 void oracle_uniform_sphere(float u, float v, float *out) {

@@ -49,7 +49,7 @@ PROPOSAL_FEATURES = 9
 PROPOSAL_OUTPUTS = 40
 PROPOSAL_PARAMS = 21808
 
-INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2}
+INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3}
 FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device limit",
@@ -106,7 +106,8 @@ class _Camera(C.Structure):
 class _RenderOptions(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
                 ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
-                ("seed", C.c_uint64), ("max_paths", C.c_uint32)]
+                ("seed", C.c_uint64), ("max_paths", C.c_uint32),
+                ("glint_diff_scale_factor_clamp", C.c_float)]
 
 
 class _Profile(C.Structure):
@@ -621,6 +622,7 @@ class RenderOptions:
     biased_mnee: bool = False
     seed: int = 0
     max_paths: int = 0
+    glint_diff_scale_factor_clamp: float = 0.0
 
     def to_c(self) -> _RenderOptions:
         o = _RenderOptions()
@@ -629,6 +631,7 @@ class RenderOptions:
         o.disable_reflected_emitters = int(self.disable_reflected_emitters)
         o.biased_mnee = int(self.biased_mnee)
         o.seed, o.max_paths = self.seed, self.max_paths
+        o.glint_diff_scale_factor_clamp = self.glint_diff_scale_factor_clamp
         return o
 
 

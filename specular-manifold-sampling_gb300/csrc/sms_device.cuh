@@ -70,6 +70,7 @@ constexpr int kStackDepth = 32;
 constexpr int kMaxCasters = 8;
 constexpr int kMaxEmitters = 16;
 constexpr int kMaxSpheres = 16;
+constexpr int kMaxLeanLevels = 20;
 
 // Device error flags (bitwise or-ed into DevCounters::error).
 constexpr uint32_t kErrStackOverflow = 1u;
@@ -227,6 +228,11 @@ struct DevScene {
     uint32_t nmap_res;
     float nmap_tiles;
     int glinty_shape;
+    // LEAN mip pyramid of the slope map (glints integrator): level l starts at
+    // lean + lean_off[l] (floats), 5 floats per texel, (nmap_res >> l)^2 texels
+    const float *lean;
+    uint32_t lean_off[kMaxLeanLevels];
+    int lean_levels;
     const DevEmitter *emitters;
 };
 

@@ -483,6 +483,55 @@ __global__ void __launch_bounds__(128) glint_trials_kernel(DevScene sc, SolverCf
 }
 
 // ---------------------------------------------------------------- launchers
+// --------------------------------------------------------- LEAN pyramid
+// Level 0 from the FP16 slope map (sx, sy, sx^2 + s0, sy^2 + s0, sx sy; s0 the
+// base variance of normalmap.cpp:36-40), each coarser level the 2x2 average
+// of the finer one (the box-filtered halving of normalmap.cpp:73-89).  Plain
+// rounded multiplies and adds, so the pyramid matches a scalar build bit for
+// bit.
+__global__ void lean_level0_kernel(DevScene sc, float *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = sc.nmap_res * sc.nmap_res;
+    if (i >= n) return;
+    uint32_t bits = __ldg(sc.nmap + i);
+    float2 t = __half22float2(*reinterpret_cast<__half2 *>(&bits));
+    float *o = out + 5 * (size_t)i;
+    const float s0 = 0.5f * 0.0001f * 0.0001f;
+    o[0] = t.x;
+    o[1] = t.y;
+    o[2] = __fadd_rn(__fmul_rn(t.x, t.x), s0);
+    o[3] = __fadd_rn(__fmul_rn(t.y, t.y), s0);
+    o[4] = __fmul_rn(t.x, t.y);
+}
+
+__global__ void lean_downsample_kernel(const float *src, uint32_t res, float *dst) {
+    const uint32_t r2 = res / 2;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= r2 * r2) return;
+    const uint32_t x = i % r2, y = i / r2;
+    const size_t a0 = 5 * ((size_t)(2 * y) * res + 2 * x), a1 = a0 + 5;
+    const size_t b0 = 5 * ((size_t)(2 * y + 1) * res + 2 * x), b1 = b0 + 5;
+    #pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        float a = __fadd_rn(src[a0 + c], src[a1 + c]), b = __fadd_rn(src[b0 + c], src[b1 + c]);
+        dst[5 * (size_t)i + c] = __fmul_rn(0.25f, __fadd_rn(a, b));
+    }
+}
+
+cudaError_t launch_lean_build(const DevScene &sc, float *out, const uint32_t *offsets, int levels, cudaStream_t s) {
+    const uint32_t n0 = sc.nmap_res * sc.nmap_res;
+    lean_level0_kernel<<<(n0 + 255) / 256, 256, 0, s>>>(sc, out + offsets[0]);
+    cudaError_t e = cudaGetLastError();
+    uint32_t res = sc.nmap_res;
+    for (int l = 1; l < levels && e == cudaSuccess; ++l) {
+        const uint32_t r2 = res / 2;
+        lean_downsample_kernel<<<(r2 * r2 + 255) / 256, 256, 0, s>>>(out + offsets[l - 1], res, out + offsets[l]);
+        e = cudaGetLastError();
+        res = r2;
+    }
+    return e;
+}
+
 cudaError_t launch_glint_walk(const DevScene &sc, const SolverCfg &cfg, const float *q, const float *w, uint32_t n,
                               float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s) {
     if (n == 0) return cudaSuccess;

@@ -368,6 +368,7 @@ struct sms_ctx {
     // offset normals of rough shapes are built for the single-scatter
     // estimator only: rough multi-scatter chain shapes / glinty shapes
     bool ms_rough = false, glint_rough = false;
+    float *lean = nullptr;   // LEAN pyramid of the slope map (glints integrator), built on first use
 };
 
 template <typename T>
@@ -411,6 +412,7 @@ extern "C" void sms_ctx_destroy(sms_ctx *c) {
     for (void *p : c->allocs) cudaFree(p);
     if (c->io) cudaFree(c->io);
     if (c->scratch) cudaFree(c->scratch);
+    if (c->lean) cudaFree(c->lean);
     if (c->ms_tmpl) cudaFree(c->ms_tmpl);
     if (c->gmm) cudaFree(c->gmm);
     for (sms_proposal *p : c->proposals) proposal_detach(p);
@@ -916,6 +918,8 @@ bool ctx_view(sms_ctx *c, CtxView &out) {
     out.proposal_bound = c->prop != nullptr;
     out.trial_group = c->trial_group;
     out.bounces = c->cfg.bounces;
+    out.bsdf_strategy_only = c->cfg.bsdf_strategy_only;
+    out.sms_strategy_only = c->cfg.sms_strategy_only;
     return true;
 }
 
@@ -1037,8 +1041,8 @@ static sms_status check_glint_scene(sms_ctx *c) {
     return SMS_OK;
 }
 
-extern "C" sms_status sms_glint_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
-                                                     uint64_t stream_off, sms_result *out) {
+sms_status ctx_glint_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
+                             const uint64_t *streams, sms_result *out) {
     if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
         return fail(SMS_ERR_INVALID_ARG, "sms_glint_connect_batch_device: null argument");
     if (sms_status st = check_glint_scene(c)) return st;
@@ -1049,8 +1053,40 @@ extern "C" sms_status sms_glint_connect_batch_device(sms_ctx *c, const float *q,
     SsScratch scr{};
     if (!c->cfg.biased)
         if (sms_status st = ensure_scratch(c, n, scr)) return st;
-    CUDA_TRY(launch_glint_connect(c->dsc, solver_cfg(c->cfg), q, n, seed, stream_off, out->value, out->count,
-                                  out->walks, c->ctr, scr, c->num_sms, c->blocks_per_sm, &c->timer, c->stream));
+    SolverCfg sc = solver_cfg(c->cfg);
+    sc.streams = streams;
+    CUDA_TRY(launch_glint_connect(c->dsc, sc, q, n, seed, stream_off, out->value, out->count, out->walks, c->ctr,
+                                  scr, c->num_sms, c->blocks_per_sm, &c->timer, c->stream));
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_glint_connect_batch_device(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
+                                                     uint64_t stream_off, sms_result *out) {
+    return ctx_glint_connect(c, q, n, seed, stream_off, nullptr, out);
+}
+
+sms_status ctx_ensure_lean(sms_ctx *c) {
+    if (sms_status st = check_glint_scene(c)) return st;
+    if (c->lean) return SMS_OK;
+    const uint32_t res = c->dsc.nmap_res;
+    if (res & (res - 1)) return fail(SMS_ERR_UNSUPPORTED, "the LEAN pyramid needs a power-of-two slope map");
+    int levels = 0;
+    size_t total = 0;
+    uint32_t offs[kMaxLeanLevels];
+    for (uint32_t r = res; r >= 1 && levels < kMaxLeanLevels; r /= 2) {
+        offs[levels++] = (uint32_t)total;
+        total += 5 * (size_t)r * r;
+        if (r == 1) break;
+    }
+    if (total > 0xffffffffull) return fail(SMS_ERR_UNSUPPORTED, "slope map too large for the LEAN pyramid");
+    CUDA_TRY(cudaSetDevice(c->device));
+    void *p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, total * sizeof(float)));
+    c->lean = reinterpret_cast<float *>(p);
+    CUDA_TRY(launch_lean_build(c->dsc, c->lean, offs, levels, c->stream));
+    c->dsc.lean = c->lean;
+    for (int l = 0; l < levels; ++l) c->dsc.lean_off[l] = offs[l];
+    c->dsc.lean_levels = levels;
     return SMS_OK;
 }
 

@@ -89,6 +89,9 @@ cudaError_t launch_glint_connect(const DevScene &sc, const SolverCfg &cfg, const
                                  uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                                  const SsScratch &scr, int num_sms, int blocks_per_sm, PhaseTimer *tm, cudaStream_t s);
 
+// LEAN mip pyramid of the slope map: `levels` levels, level l at out + offsets[l].
+cudaError_t launch_lean_build(const DevScene &sc, float *out, const uint32_t *offsets, int levels, cudaStream_t s);
+
 // Read-only view of a context for entry points defined outside sms_host.cu.
 struct CtxView {
     int device;
@@ -104,6 +107,7 @@ struct CtxView {
     bool proposal_bound;            // a learned proposal seeds the SS estimator
     int trial_group;                // lanes per query of the trial kernel (0: auto)
     int bounces;                    // multi-scatter chain length (sms_config::bounces)
+    int bsdf_strategy_only, sms_strategy_only;   // glints MIS switches (sms_config)
 };
 
 }  // namespace sms
@@ -118,6 +122,11 @@ sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
                           const uint64_t *streams, sms_result *out);
 sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
                           const uint64_t *streams, sms_result *out);
+sms_status ctx_glint_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
+                             const uint64_t *streams, sms_result *out);
+// Builds the LEAN pyramid of the context's slope map on first use (the
+// context's scene view then carries it).
+sms_status ctx_ensure_lean(sms_ctx *c);
 // Reads and clears the device error flags of a context (synchronizes its
 // stream); SMS_ERR_DEVICE_LIMIT with the reasons when any was set.
 sms_status ctx_check_device_error(sms_ctx *c);

@@ -1,0 +1,170 @@
+// sms_lean.cuh -- LEAN mapping and the normal-mapped conductor for the glints
+// integrator (device side).
+//
+// References: the LEAN mip pyramid of src/librender/normalmap.cpp:36-89 and
+// its lookups (include/mitsuba/render/normalmap.h:62-104, 199-233), the
+// footprint level of NormalmapBSDF::mipmap_level (src/bsdfs/normalmap.cpp:
+// 374-388), the LEAN/LEADR distribution of include/mitsuba/render/lean.h
+// (after Dupuy's reference implementation), SpecularManifoldGlints::lean_pdf
+// (src/librender/manifold_glints.cpp:557-579), NormalmapBSDF::frame / sample
+// with a smooth conductor inside (normalmap.cpp:116-139, 236-257).
+#pragma once
+#include <cuda_fp16.h>
+
+#include "sms_device.cuh"
+
+namespace sms {
+
+// Base variance of the slopes at level 0: 0.5 * alpha^2, alpha = 1e-4
+// (normalmap.cpp:36-40).
+constexpr float kLeanBaseSigma2 = 0.5f * 0.0001f * 0.0001f;
+
+SMS_HD float2 nm_texel(const DevScene &sc, uint32_t idx) {
+#ifdef __CUDA_ARCH__
+    uint32_t bits = __ldg(sc.nmap + idx);
+    __half2 h = *reinterpret_cast<__half2 *>(&bits);
+    return __half22float2(h);
+#else
+    (void)sc; (void)idx;
+    return make_float2(0.f, 0.f);
+#endif
+}
+
+// Bilinear slope at level 0 after the tiling wrap (normalmap.cpp:305-316).
+SMS_D float2 nm_slope0(const DevScene &sc, float u_in, float v_in) {
+    float u = u_in * sc.nmap_tiles, v = v_in * sc.nmap_tiles;
+    u -= floorf(u);
+    v -= floorf(v);
+    const uint32_t R = sc.nmap_res;
+    float res = (float)R, duv = 1.f / res;
+    float px = fminf(fmaxf((u - 0.5f * duv) * res, 0.f), res - 1.f);
+    float py = fminf(fmaxf((v - 0.5f * duv) * res, 0.f), res - 1.f);
+    uint32_t x0 = (uint32_t)floorf(px), y0 = (uint32_t)floorf(py);
+    uint32_t x1 = min(x0 + 1, R - 1), y1 = min(y0 + 1, R - 1);
+    x0 = min(x0, R - 1);
+    y0 = min(y0, R - 1);
+    float wx = px - (float)x0, wy = py - (float)y0;
+    float2 t00 = nm_texel(sc, y0 * R + x0), t10 = nm_texel(sc, y0 * R + x1), t01 = nm_texel(sc, y1 * R + x0),
+           t11 = nm_texel(sc, y1 * R + x1);
+    float w0x = 1.f - wx, w0y = 1.f - wy;
+    return make_float2(w0y * (w0x * t00.x + wx * t10.x) + wy * (w0x * t01.x + wx * t11.x),
+                       w0y * (w0x * t00.y + wx * t10.y) + wy * (w0x * t01.y + wx * t11.y));
+}
+
+// Footprint level (a footprint finer than one texel takes level 0).
+SMS_D int lean_level(const DevScene &sc, float dxu, float dxv, float dyu, float dyv) {
+    const float t = sc.nmap_tiles;
+    float w = 2.f * fmaxf(fmaxf(fabsf(t * dxu), fabsf(t * dxv)), fmaxf(fabsf(t * dyu), fabsf(t * dyv)));
+    float lv = ceilf((float)(sc.lean_levels - 1) + log2f(fmaxf(w, 1e-8f)));
+    if (!(lv > 0.f)) return 0;
+    return (int)fminf(lv, (float)(sc.lean_levels - 1));
+}
+
+// Bilinear LEAN lookup: mean slope and covariance (a, c; c, b) on level l.
+SMS_D void lean_lookup(const DevScene &sc, float u_in, float v_in, int l, float &mx, float &my, float &sa,
+                       float &sb, float &scv) {
+    const uint32_t res = sc.nmap_res >> l;
+    float u = u_in * sc.nmap_tiles, v = v_in * sc.nmap_tiles;
+    u -= floorf(u);
+    v -= floorf(v);
+    float fr = (float)res, duv = 1.f / fr;
+    float px = fminf(fmaxf((u - 0.5f * duv) * fr, 0.f), fr - 1.f);
+    float py = fminf(fmaxf((v - 0.5f * duv) * fr, 0.f), fr - 1.f);
+    uint32_t x0 = (uint32_t)floorf(px), y0 = (uint32_t)floorf(py);
+    uint32_t x1 = min(x0 + 1, res - 1), y1 = min(y0 + 1, res - 1);
+    x0 = min(x0, res - 1);
+    y0 = min(y0, res - 1);
+    float wx = px - (float)x0, wy = py - (float)y0;
+    const float *d = sc.lean + sc.lean_off[l];
+    float vv[5];
+    #pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        float v00 = __ldg(d + 5 * ((size_t)y0 * res + x0) + c), v10 = __ldg(d + 5 * ((size_t)y0 * res + x1) + c);
+        float v01 = __ldg(d + 5 * ((size_t)y1 * res + x0) + c), v11 = __ldg(d + 5 * ((size_t)y1 * res + x1) + c);
+        float a = (1.f - wx) * v00 + wx * v10, b = (1.f - wx) * v01 + wx * v11;
+        vv[c] = (1.f - wy) * a + wy * b;
+    }
+    mx = vv[0];
+    my = vv[1];
+    sa = fmaxf(0.f, vv[2] - vv[0] * vv[0]);
+    sb = fmaxf(0.f, vv[3] - vv[1] * vv[1]);
+    scv = fmaxf(0.f, vv[4] - vv[0] * vv[1]);
+}
+
+struct LeanP {
+    f3 n;
+    float ax, ay, rho, srho, tx, ty;
+};
+
+SMS_D LeanP lean_params(float mx, float my, float sa, float sb, float scv, float alpha) {
+    float lax = sqrtf(2.f * sa), lay = sqrtf(2.f * sb);
+    float rho = 2.f * scv / (lax * lay);
+    float e3 = 0.5f * lax * lax + mx * mx + 0.5f * alpha * alpha;
+    float e4 = 0.5f * lay * lay + my * my + 0.5f * alpha * alpha;
+    float e5 = 0.5f * rho * lax * lay + mx * my;
+    LeanP p;
+    p.tx = mx;
+    p.ty = my;
+    p.ax = sqrtf(2.f * fmaxf(0.f, e3 - mx * mx));
+    p.ay = sqrtf(2.f * fmaxf(0.f, e4 - my * my));
+    p.rho = 2.f * (e5 - mx * my) / (p.ax * p.ay);
+    p.srho = sqrtf(1.f - p.rho * p.rho);
+    p.n = normalize(mk(-p.tx, -p.ty, 1.f));
+    return p;
+}
+
+SMS_D float lean_sigma_std(float ct) {
+    if (ct == 1.f) return 1.f;
+    float st = sqrtf(1.f - ct * ct), nu = ct / st;
+    float tmp = expf(-nu * nu) * 0.56418958354775628695f;   // 1 / sqrt(pi)
+    return 0.5f * (ct * (1.f + erff(nu)) + st * tmp);
+}
+
+SMS_D float lean_sigma(f3 k, const LeanP &p) {
+    float a = k.x * p.ax + k.y * p.ay * p.rho, b = k.y * p.ay * p.srho, c = k.z - k.x * p.tx - k.y * p.ty;
+    float nrm = sqrtf(a * a + b * b + c * c);
+    return nrm * lean_sigma_std(c / nrm);
+}
+
+SMS_D float lean_g1(f3 k, const LeanP &p) { return dot(k, p.n) > 0.f ? k.z / lean_sigma(k, p) : 0.f; }
+
+SMS_D float lean_ndf(f3 h, const LeanP &p) {
+    if (!(h.z > 5.9604644775390625e-08f)) return 0.f;
+    float t1 = h.z * h.z, t2 = t1 * t1;
+    float sx = -h.x / h.z - p.tx, sy = -h.y / h.z - p.ty;
+    float nrm = p.ax * p.ay * p.srho;
+    float x = sx / p.ax, y = (p.ax * sy - p.rho * p.ay * sx) / (p.ax * p.ay * p.srho);
+    return kInvPi * expf(-(x * x + y * y)) / nrm / t2;
+}
+
+// LEAN density of reflecting wi into wo over the footprint at uv.
+SMS_D float glint_lean_pdf(const DevScene &sc, float u, float v, float dxu, float dxv, float dyu, float dyv, f3 wi,
+                           f3 wo) {
+    if (wi.z < 0.f || wo.z < 0.f) return 0.f;
+    float mx, my, sa, sb, scv;
+    lean_lookup(sc, u, v, lean_level(sc, dxu, dxv, dyu, dyv), mx, my, sa, sb, scv);
+    LeanP p = lean_params(mx, my, sa, sb, scv, 0.f);
+    f3 h = normalize(wo + wi);
+    float G = lean_g1(wo, p) * lean_g1(wi, p);
+    if (!(G > 0.f)) return 0.f;
+    float dp = dot(wi, h);
+    float vndf = dp > 0.f ? dp * lean_ndf(h, p) / lean_sigma(wi, p) : 0.f;
+    return vndf / (4.f * dot(wi, h));
+}
+
+// Normal-mapped smooth conductor: reflection about the bilinear slope normal
+// of level 0 at uv; world-space directions; weight = Fresnel.
+SMS_D bool nm_conductor_sample(const DevScene &sc, const DevShape &s, f3 n, f3 dp_du, float u, float v, f3 wi_w,
+                               f3 &wo_w, float &weight) {
+    f3 bs = normalize(dp_du - n * dot(n, dp_du)), bt = cross(n, bs);
+    float2 sl = nm_slope0(sc, u, v);
+    f3 pn = normalize(bs * -sl.x + bt * -sl.y + n);
+    float ci = dot(wi_w, pn);
+    if (!(ci > 0.f)) return false;
+    wo_w = pn * (2.f * ci) - wi_w;
+    if (!(dot(wo_w, n) * dot(wo_w, pn) > 0.f)) return false;
+    weight = fresnel_conductor(ci, s.eta, s.k);
+    return true;
+}
+
+}  // namespace sms

@@ -475,7 +475,10 @@ __global__ void __launch_bounds__(128) ms_walk_kernel(DevScene sc, SolverCfg cfg
 // deduplicated before the contribution, which itself tests visibility
 // (:147-195).
 template <int K, int G>
-__global__ void __launch_bounds__(128, 4) ms_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
+#ifndef SMS_MS_BIASED_MIN_BLOCKS
+#define SMS_MS_BIASED_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
                                                         int *__restrict__ walks, DevCounters *ctr) {

@@ -40,6 +40,7 @@
 #include "sms_device.cuh"
 #include "sms_estimator.cuh"
 #include "sms_kernels.h"
+#include "sms_lean.cuh"
 
 namespace sms {
 namespace {
@@ -47,7 +48,8 @@ namespace {
 constexpr int kPtBlock = 256;
 constexpr uint32_t kPtDefaultPaths = 1u << 20;
 constexpr int kPtHardDepth = 4096;        // bounce limit of an unbounded path
-constexpr int kStageRows = 19;            // 16 query rows + 3 throughput rows
+constexpr int kQueryRowsMax = 21;        // glint queries; single / multi scatter use 16
+constexpr int kStageRows = 24;            // query rows, then 3 throughput rows at 21..23
 
 // path flags
 constexpr int kAlive = 1, kPrevReceiver = 2, kSpecularCamera = 4;
@@ -67,12 +69,15 @@ struct PtParams {
     int mnee_check;       // path_sms_ss with mnee_init and !biased_mnee
     uint64_t seed;
     SolverCfg solver;     // for the MNEE check walk
+    float diff_scale;     // ray-differential scale (glints)
+    int bsdf_strategy_only, sms_strategy_only;
 };
 
 struct PtState {
     uint64_t *rng_state, *rng_inc;
     float *o, *d, *thr, *L, *prev_p;      // 3 x cap
     float *eta, *hit_t, *hit_u, *hit_v;   // cap
+    float *cam_s;                         // 2 x cap: the camera sample position
     int *hit_shape, *flags;               // cap
     uint32_t *hit_prim;                   // cap
     float *stage;                         // kStageRows x cap
@@ -80,11 +85,12 @@ struct PtState {
     uint32_t *block_q, *block_a;          // per block
     uint32_t *totals;                     // [0] queries, [1] live paths
     // pending SMS batch (qcap entries, appended bounce by bounce)
-    float *qraw;                          // 16 x qcap, stride qcap
+    int qrows;                            // query rows: 16, or 21 for glints
+    float *qraw;                          // qrows x qcap, stride qcap
     float *qw;                            // 3 x qcap: path throughput
     uint32_t *qmap;                       // qcap: query -> path
     uint64_t *qstream;                    // qcap: random-number stream
-    float *q;                             // 16 x nq packed (stride nq)
+    float *q;                             // qrows x nq packed (stride nq)
     float *value;                         // 3 x nq
     int *count, *walks;                   // nq
     uint32_t cap, qcap;
@@ -458,13 +464,35 @@ __global__ void __launch_bounds__(kPtBlock) pt_camera_kernel(DevScene sc, PtCam 
     S.hit_t[i] = h.t; S.hit_u[i] = h.u; S.hit_v[i] = h.v;
     S.hit_shape[i] = h.shape; S.hit_prim[i] = h.prim;
     S.flags[i] = (h.shape >= 0 ? kAlive : 0) | kSpecularCamera;
+    S.cam_s[i] = sx;
+    S.cam_s[(size_t)S.cap + i] = sy;
     store_rng(S, i, rng);
+}
+
+// World-space direction through the image-plane sample (sx, sy).
+SMS_D f3 cam_dir(const PtCam &cam, float sx, float sy) {
+    f3 dc = normalize(mk(cam.tx * (1.f - 2.f * sx), cam.ty * (1.f - 2.f * sy), 1.f));
+    return normalize(mk(cam.m[0] * dc.x + cam.m[1] * dc.y + cam.m[2] * dc.z,
+                        cam.m[4] * dc.x + cam.m[5] * dc.y + cam.m[6] * dc.z,
+                        cam.m[8] * dc.x + cam.m[9] * dc.y + cam.m[10] * dc.z));
+}
+
+// PerspectiveCamera::importance (perspective.cpp:224-276) x film size for the
+// world-space direction d from the camera (camera-to-world taken as rigid).
+SMS_D float cam_importance(const PtCam &cam, f3 d) {
+    f3 dl = mk(cam.m[0] * d.x + cam.m[4] * d.y + cam.m[8] * d.z, cam.m[1] * d.x + cam.m[5] * d.y + cam.m[9] * d.z,
+               cam.m[2] * d.x + cam.m[6] * d.y + cam.m[10] * d.z);
+    if (!(dl.z > 0.f)) return 0.f;
+    float ic = 1.f / dl.z;
+    float px = dl.x * ic, py = dl.y * ic;
+    if (!(px >= -cam.tx && px <= cam.tx && py >= -cam.ty && py <= cam.ty)) return 0.f;
+    return (1.f / (4.f * cam.tx * cam.ty)) * ic * ic * ic * (float)cam.width * (float)cam.height;
 }
 
 // ------------------------------------------------------------------ bounce
 template <bool kMneeCheck>
 __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtParams P, PtState S, int depth,
-                                                             uint32_t n, DevCounters *ctr) {
+                                                             uint32_t n, DevCounters *ctr, PtCam cam) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     int want = 0, alive_out = 0;
     uint32_t err = 0;
@@ -499,20 +527,75 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS)
                 on_caster = (s.flags & (kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
             const bool diffuse = s.bsdf_type == kBsdfDiffuse;
-            const bool smooth = diffuse || s.alpha > 0.f;   // BSDFFlags::Smooth: diffuse or glossy
+            // the glinty shape carries a normal-mapped conductor (delta reflection)
+            const bool nmapped = shape == sc.glinty_shape && sc.nmap_res > 0;
+            const bool smooth = !nmapped && (diffuse || s.alpha > 0.f);   // BSDFFlags::Smooth
+            const bool on_glinty = P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS && depth == 1 && nmapped &&
+                                   (s.flags & kShapeFlagGlinty);
             const f3 albedo = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
-            // ---- SMS query of a receiver vertex (solved after this launch)
-            if (P.integrator != SMS_INTEGRATOR_PATH && receiver && !on_caster && diffuse &&
-                (P.max_depth < 0 || depth + P.bounces < P.max_depth)) {
+            if (on_glinty) {
+                // ray differentials of the camera ray (perspective.cpp:198-220),
+                // scaled (integrator.cpp:164-165), then compute_partials
+                // (interaction.h:216-248)
+                const float sx = S.cam_s[i], sy = S.cam_s[(size_t)S.cap + i];
+                const f3 rdx = d + (cam_dir(cam, sx + 1.f / (float)cam.width, sy) - d) * P.diff_scale;
+                const f3 rdy = d + (cam_dir(cam, sx, sy + 1.f / (float)cam.height) - d) * P.diff_scale;
+                const float dn = dot(si.n, si.p);
+                const f3 dp_dx = o + rdx * ((dn - dot(si.n, o)) / dot(si.n, rdx)) - si.p;
+                const f3 dp_dy = o + rdy * ((dn - dot(si.n, o)) / dot(si.n, rdy)) - si.p;
+                const float a00 = dot(si.dp_du, si.dp_du), a01 = dot(si.dp_du, si.dp_dv);
+                const float a11 = dot(si.dp_dv, si.dp_dv);
+                float inv_det = 1.f / (a00 * a11 - a01 * a01);
+                if (!isfinite(inv_det)) inv_det = 0.f;
+                const float b0x = dot(si.dp_du, dp_dx), b1x = dot(si.dp_dv, dp_dx);
+                const float b0y = dot(si.dp_du, dp_dy), b1y = dot(si.dp_dv, dp_dy);
+                const float dxu = (a11 * b0x - a01 * b1x) * inv_det, dxv = (a00 * b1x - a01 * b0x) * inv_det;
+                const float dyu = (a11 * b0y - a01 * b1y) * inv_det, dyv = (a00 * b1y - a01 * b0y) * inv_det;
+                // SMS strategy: stage the glint query (solved after this launch)
                 const float row[kStageRows] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
                                                si.dp_du.x, si.dp_du.y, si.dp_du.z, si.dp_dv.x, si.dp_dv.y, si.dp_dv.z,
-                                               albedo.x, albedo.y, albedo.z, wi.z, thr.x, thr.y, thr.z};
+                                               si.u, si.v, dxu, dxv, dyu, dyv, o.x, o.y, o.z, thr.x, thr.y, thr.z};
                 #pragma unroll
                 for (int k = 0; k < kStageRows; ++k) S.stage[(size_t)k * S.cap + i] = row[k];
                 want = 1;
+                // BSDF strategy inside the footprint (manifold_glints.cpp:178-220)
+                const float fpx = rng.next_f32(), fpy = rng.next_f32();
+                (void)rng.next_f32(); (void)rng.next_f32(); (void)rng.next_f32();
+                const float uo = si.u + (fpx - 0.5f) * dxu + (fpy - 0.5f) * dyu;
+                const float vo = si.v + (fpx - 0.5f) * dxv + (fpy - 0.5f) * dyv;
+                f3 bwo;
+                float bw;
+                if (nm_conductor_sample(sc, s, n_sh, si.dp_du, uo, vo, wiw, bwo, bw)) {
+                    Hit hb;
+                    trace(sc, si.p, bwo, kRayEps * (1.f + max_abs(si.p)), INFINITY, false, hb, err);
+                    if (hb.shape >= 0 && sc.shapes[hb.shape].emitter >= 0) {
+                        const DevShape &es = sc.shapes[hb.shape];
+                        const f3 ep = si.p + bwo * hb.t;
+                        const f3 Le = emitted(sc, es, ep, bwo);
+                        const f3 bwo_l = mk(dot(bwo, fs), dot(bwo, ft), dot(bwo, n_sh));
+                        const float p_bsdf = glint_lean_pdf(sc, uo, vo, dxu, dxv, dyu, dyv, wi, bwo_l) + 1.f;
+                        const float p_sms = emitter_pdf(sc, es, si.p, ep, bwo, hb.t);
+                        const float mis = P.sms_strategy_only ? 0.f : mis_weight(p_bsdf, p_sms);
+                        L = L + thr * Le * (mis * bw);
+                    }
+                }
+            }
+            // ---- SMS query of a receiver vertex (solved after this launch)
+            if (P.integrator != SMS_INTEGRATOR_PATH && receiver && !on_caster && diffuse &&
+                (P.max_depth < 0 || depth + P.bounces < P.max_depth)) {
+                const float row[SMS_QUERY_FIELDS] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
+                                                     si.dp_du.x, si.dp_du.y, si.dp_du.z,
+                                                     si.dp_dv.x, si.dp_dv.y, si.dp_dv.z,
+                                                     albedo.x, albedo.y, albedo.z, wi.z};
+                #pragma unroll
+                for (int k = 0; k < SMS_QUERY_FIELDS; ++k) S.stage[(size_t)k * S.cap + i] = row[k];
+                S.stage[(size_t)21 * S.cap + i] = thr.x;
+                S.stage[(size_t)22 * S.cap + i] = thr.y;
+                S.stage[(size_t)23 * S.cap + i] = thr.z;
+                want = 1;
             }
             // ---- emitter sampling
-            bool nee = smooth && !on_caster;
+            bool nee = smooth && !on_caster && !on_glinty;
             if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS)
                 nee = nee || (depth == 1 && !P.disable_reflected_emitters);
             if (nee) {
@@ -535,7 +618,20 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             // ---- BSDF sampling
             float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
             BsdfSample bs;
-            bool ok = bsdf_sample(s, wi, u1, u2, u3, bs);
+            bool ok;
+            if (nmapped) {
+                // normal-mapped conductor at the hit's own uv
+                f3 wo_w;
+                float w;
+                ok = nm_conductor_sample(sc, s, n_sh, si.dp_du, si.u, si.v, wiw, wo_w, w);
+                bs.wo = mk(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n_sh));
+                bs.weight = splat(w);
+                bs.pdf = 1.f;
+                bs.eta = 1.f;
+                bs.delta = true;
+            } else {
+                ok = bsdf_sample(s, wi, u1, u2, u3, bs);
+            }
             if (ok) {
                 thr = thr * bs.weight;
                 eta *= bs.eta;
@@ -556,6 +652,8 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                         allow = !on_caster || (depth == 1 && !P.disable_reflected_emitters);
                     else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS)
                         allow = !on_caster || (flags & kSpecularCamera);
+                    else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS)
+                        allow = !on_glinty;
                     if (allow) {
                         float epdf = bs.delta ? 0.f : emitter_pdf(sc, es, si.p, ep, d2, h2.t);
                         L = L + thr * Le * mis_weight(bs.pdf, epdf);
@@ -663,10 +761,9 @@ __global__ void __launch_bounds__(kPtBlock) pt_gather_kernel(PtState S, uint32_t
     uint32_t r = S.block_q[blockIdx.x] + __popc(m & ((1u << lane) - 1u));
     for (unsigned k = 0; k < wid; ++k) r += warp_cnt[k];
     const uint32_t e = base + r;
+    for (int k = 0; k < S.qrows; ++k) S.qraw[(size_t)k * S.qcap + e] = S.stage[(size_t)k * S.cap + i];
     #pragma unroll
-    for (int k = 0; k < 16; ++k) S.qraw[(size_t)k * S.qcap + e] = S.stage[(size_t)k * S.cap + i];
-    #pragma unroll
-    for (int k = 0; k < 3; ++k) S.qw[(size_t)k * S.qcap + e] = S.stage[(size_t)(16 + k) * S.cap + i];
+    for (int k = 0; k < 3; ++k) S.qw[(size_t)k * S.qcap + e] = S.stage[(size_t)(21 + k) * S.cap + i];
     S.qmap[e] = i;
     S.qstream[e] = g0 + i + ((uint64_t)depth << 48);
 }
@@ -675,8 +772,43 @@ __global__ void __launch_bounds__(kPtBlock) pt_gather_kernel(PtState S, uint32_t
 __global__ void __launch_bounds__(kPtBlock) pt_pack_kernel(PtState S, uint32_t nq) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nq) return;
-    #pragma unroll
-    for (int f = 0; f < 16; ++f) S.q[(size_t)f * nq + k] = S.qraw[(size_t)f * S.qcap + k];
+    for (int f = 0; f < S.qrows; ++f) S.q[(size_t)f * nq + k] = S.qraw[(size_t)f * S.qcap + k];
+}
+
+// Glint estimates of entries [b, b + cnt) -> path radiance: the SMS strategy
+// of manifold_glints.cpp:150-176 with its MIS weight against the BSDF
+// strategy (emitter-sampling density vs LEAN density + 1) and the sensor
+// importance.  The emitter sample is redrawn from the query's stream (its
+// first 3 numbers, as the estimator drew it).
+__global__ void __launch_bounds__(kPtBlock) pt_glint_add_kernel(DevScene sc, PtCam cam, PtState S, uint32_t nq,
+                                                                uint32_t b, uint32_t cnt, uint64_t sseed,
+                                                                int bsdf_strategy_only) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= cnt) return;
+    const uint32_t k = b + r;
+    const f3 v = mk(S.value[k], S.value[(size_t)nq + k], S.value[2 * (size_t)nq + k]);
+    if (v.x == 0.f && v.y == 0.f && v.z == 0.f) return;
+    auto Q = [&](int f) { return S.q[(size_t)f * nq + k]; };
+    const f3 p = mk(Q(0), Q(1), Q(2)), n = mk(Q(3), Q(4), Q(5)), dpdu = mk(Q(6), Q(7), Q(8));
+    const float u = Q(12), vv = Q(13), dxu = Q(14), dxv = Q(15), dyu = Q(16), dyv = Q(17);
+    const f3 sensor = mk(Q(18), Q(19), Q(20));
+    Pcg32 rng = query_rng(sseed, S.qstream[k], 0);
+    Light Lt;
+    if (!sample_emitter(sc, sc.emitters_all, sc.n_emitters_all, rng, p, Lt)) return;
+    f3 ed = Lt.p - p;
+    const float edist = length(ed);
+    ed = ed * (1.f / edist);
+    float p_sms = 1.f;
+    if (Lt.kind == 1) p_sms = emitter_pdf(sc, sc.shapes[sc.emitters[Lt.eidx].shape], p, Lt.p, ed, edist);
+    const f3 fs = normalize(dpdu - n * dot(n, dpdu)), ft = cross(n, fs);
+    const f3 wiw = normalize(sensor - p);
+    const f3 wi = mk(dot(wiw, fs), dot(wiw, ft), dot(wiw, n)), wo = mk(dot(ed, fs), dot(ed, ft), dot(ed, n));
+    const float p_bsdf = glint_lean_pdf(sc, u, vv, dxu, dxv, dyu, dyv, wi, wo) + 1.f;
+    const float mis = bsdf_strategy_only ? 0.f : mis_weight(p_sms, p_bsdf);
+    const float We = cam_importance(cam, normalize(p - sensor));
+    const uint32_t i = S.qmap[k];
+    const f3 w = mk(S.qw[k], S.qw[(size_t)S.qcap + k], S.qw[2 * (size_t)S.qcap + k]);
+    st3s(S.L, S.cap, i, ld3s(S.L, S.cap, i) + w * v * (mis * We));
 }
 
 // Entries [b, b + cnt) of the solved batch (one bounce: each path at most
@@ -777,8 +909,13 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     std::string why;
     if (!camera_params(cam, pc, why)) return rfail(SMS_ERR_INVALID_ARG, "sms_render: " + why);
     if (opt->spp <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: spp must be positive");
-    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_SMS_MS)
+    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_SMS_GLINTS)
         return rfail(SMS_ERR_INVALID_ARG, "sms_render: unknown integrator");
+    const bool glints = opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS;
+    if (glints) {
+        // the footprint MIS needs the LEAN pyramid of the slope map
+        if (sms_status est = ctx_ensure_lean(c)) return est;
+    }
     if (opt->rr_depth <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: rr_depth must be positive");
     if (opt->max_depth < -1) return rfail(SMS_ERR_INVALID_ARG, "sms_render: max_depth must be -1 or >= 0");
     if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee)
@@ -794,6 +931,9 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     P.mnee_check = opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee;
     P.seed = opt->seed;
     P.solver = v.solver;
+    P.diff_scale = std::max(1.f / std::sqrt((float)opt->spp), opt->glint_diff_scale_factor_clamp);
+    P.bsdf_strategy_only = v.bsdf_strategy_only;
+    P.sms_strategy_only = v.sms_strategy_only;
 
     const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
     const uint64_t total = wh * (uint64_t)opt->spp;
@@ -811,12 +951,12 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
                  o_d = take(12 * (size_t)cap), o_thr = take(12 * (size_t)cap), o_L = take(12 * (size_t)cap),
                  o_pp = take(12 * (size_t)cap), o_eta = take(4 * (size_t)cap), o_ht = take(4 * (size_t)cap),
                  o_hu = take(4 * (size_t)cap), o_hv = take(4 * (size_t)cap), o_hs = take(4 * (size_t)cap),
-                 o_fl = take(4 * (size_t)cap), o_hp = take(4 * (size_t)cap),
+                 o_fl = take(4 * (size_t)cap), o_hp = take(4 * (size_t)cap), o_cs = take(8 * (size_t)cap),
                  o_st = take(4 * (size_t)kStageRows * cap), o_w = take(4 * (size_t)cap),
                  o_bq = take(4 * (size_t)n_blocks_cap), o_ba = take(4 * (size_t)n_blocks_cap), o_tot = take(16),
-                 o_qr = take(4 * (size_t)SMS_QUERY_FIELDS * qcap), o_qw = take(12 * (size_t)qcap),
+                 o_qr = take(4 * (size_t)kQueryRowsMax * qcap), o_qw = take(12 * (size_t)qcap),
                  o_qm = take(4 * (size_t)qcap), o_qs = take(8 * (size_t)qcap),
-                 o_q = take(4 * (size_t)SMS_QUERY_FIELDS * qcap), o_val = take(12 * (size_t)qcap),
+                 o_q = take(4 * (size_t)kQueryRowsMax * qcap), o_val = take(12 * (size_t)qcap),
                  o_cnt = take(4 * (size_t)qcap), o_wk = take(4 * (size_t)qcap);
     char *blk = nullptr;
     uint32_t *host_tot = nullptr;
@@ -835,13 +975,18 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return rfail(SMS_ERR_CUDA, std::string("pt_pack_kernel: ") + cudaGetErrorString(e));
         sms_result r{S.value, S.count, S.walks};
-        sms_status fs = P.integrator == SMS_INTEGRATOR_PATH_SMS_MS
+        sms_status fs = glints ? ctx_glint_connect(c, S.q, pending, sseed, 0, S.qstream, &r)
+                        : P.integrator == SMS_INTEGRATOR_PATH_SMS_MS
                             ? ctx_ms_connect(c, S.q, pending, sseed, 0, S.qstream, &r)
                             : ctx_ss_connect(c, S.q, pending, sseed, 0, S.qstream, &r);
         if (fs) return fs;
         for (size_t k = 0; k < seg_base.size(); ++k) {
-            pt_sms_add_kernel<<<(seg_cnt[k] + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, pending, seg_base[k],
-                                                                                         seg_cnt[k]);
+            const uint32_t g = (seg_cnt[k] + kPtBlock - 1) / kPtBlock;
+            if (glints)
+                pt_glint_add_kernel<<<g, kPtBlock, 0, s>>>(*v.scene, pc, S, pending, seg_base[k], seg_cnt[k], sseed,
+                                                            P.bsdf_strategy_only);
+            else
+                pt_sms_add_kernel<<<g, kPtBlock, 0, s>>>(S, pending, seg_base[k], seg_cnt[k]);
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) return rfail(SMS_ERR_CUDA, std::string("pt_sms_add_kernel: ") + cudaGetErrorString(e));
@@ -867,6 +1012,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     S.hit_shape = reinterpret_cast<int *>(blk + o_hs);
     S.flags = reinterpret_cast<int *>(blk + o_fl);
     S.hit_prim = reinterpret_cast<uint32_t *>(blk + o_hp);
+    S.cam_s = reinterpret_cast<float *>(blk + o_cs);
     S.stage = reinterpret_cast<float *>(blk + o_st);
     S.want = reinterpret_cast<int *>(blk + o_w);
     S.block_q = reinterpret_cast<uint32_t *>(blk + o_bq);
@@ -882,6 +1028,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     S.walks = reinterpret_cast<int *>(blk + o_wk);
     S.cap = cap;
     S.qcap = qcap;
+    S.qrows = glints ? kQueryRowsMax : SMS_QUERY_FIELDS;
     PT_TRY(cudaMemsetAsync(image, 0, img_n * sizeof(float), s));
     while (g0 < total) {
         uint32_t n;
@@ -901,8 +1048,10 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
                 st = flush();
                 if (st) goto done;
             }
-            if (P.mnee_check) pt_bounce_kernel<true><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters);
-            else pt_bounce_kernel<false><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters);
+            if (P.mnee_check)
+                pt_bounce_kernel<true><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters, pc);
+            else
+                pt_bounce_kernel<false><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters, pc);
             PT_TRY(cudaGetLastError());
             pt_scan_kernel<<<1, 1024, 0, s>>>(S, nb);
             PT_TRY(cudaGetLastError());

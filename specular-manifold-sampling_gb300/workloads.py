@@ -346,5 +346,13 @@ def glint_queries(width: int = 1024, fov_deg: float = 30.0, diff_scale: float = 
     return q
 
 
+def glint_render_camera(width: int = 64, height: int = 64, fov: float = 30.0):
+    """The glint benchmark's camera (60 degrees from the normal, looking at the
+    plane's centre) as a Camera for the path tracer."""
+    from . import Camera
+    cam, _ = glint_camera()
+    return Camera.look_at(tuple(cam), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), fov, width, height)
+
+
 def glint_config() -> SMSConfig:
     return SMSConfig(biased=True, max_trials=64, max_iterations=10, glints_vectorized=True)

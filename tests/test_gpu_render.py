@@ -202,3 +202,20 @@ def test_rough_caustic_is_unbiased_against_path(sms, workloads, gpu_lib, alpha):
     cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 32, 32)
     _compare_integrators(sms, ctx, cam, "path_sms_ss", 8192, 256, 4)
     ctx.close()
+
+
+@pytest.mark.parametrize("biased", [True, False])
+def test_glints_integrator_matches_oracle(sms, workloads, oracle, gpu_lib, biased):
+    """path_sms_glints (manifold_glints.cpp:28-223 inside path_sms_glints.cpp):
+    glint SMS over each camera footprint with sensor importance and LEAN-MIS,
+    on the GPU against the oracle (LEAN pyramid built on the device), against
+    the oracle-vs-FMA floor."""
+    W = workloads
+    desc = W.glint_scene(map_res=512)
+    cfg = W.glint_config()
+    if not biased:
+        cfg = sms.SMSConfig(biased=False, max_trials=64, max_iterations=10)
+    g, o, f = _check_against_oracle(sms, oracle, desc, cfg, W.glint_render_camera(32, 32),
+                                    sms.RenderOptions(integrator="path_sms_glints", spp=4, seed=7))
+    assert (o[..., 0] > 0).mean() > 0.005
+    assert abs(g.mean() - o.mean()) <= 3.0 * abs(f.mean() - o.mean()) + 0.02 * o.mean()

@@ -265,6 +265,37 @@ def render_study(torch, sms, W, dev, width=512, height=512, spp=16):
                          "sample": f"64x64 pixels x 4 spp path_sms_ss, {dt:.2f} s"}
     out["speedup_vs_cpu_oracle"] = out["path_sms_ss"]["samples_per_s"] / out["cpu_oracle"]["samples_per_s"]
     ctx.close()
+    # glints: the 8192^2 slope-map plane of the glint configuration, path_sms_glints
+    gdesc = W.glint_scene()
+    gcfg = W.glint_config()
+    gctx = sms.Context(sms.Scene(gdesc), gcfg, device=dev)
+    gstream = torch.cuda.ExternalStream(gctx.stream, device=dev)
+    gcam = W.glint_render_camera(width, height)
+    gopt = sms.RenderOptions(integrator="path_sms_glints", spp=spp, seed=1)
+    with DeviceTimer(torch, gstream) as t_first:   # includes the LEAN pyramid build
+        gctx.render_device(gcam, gopt, img.data_ptr())
+    gctx.reset_stats()
+    times = []
+    for k in range(3):
+        gopt.seed = 2 + k
+        with DeviceTimer(torch, gstream) as t:
+            gctx.render_device(gcam, gopt, img.data_ptr())
+        times.append(t.ms)
+    st = gctx.stats()
+    ms = float(np.mean(times))
+    out["path_sms_glints"] = {"scene": "glint plane, 8192^2 FP16 slope map, point light; biased vectorized M=64",
+                              "ms_per_image": ms, "samples_per_s": width * height * spp / (ms / 1e3),
+                              "glint_connections_per_s": st["connections"] / (3 * ms / 1e3),
+                              "first_image_ms_with_lean_build": t_first.ms, "mean": float(img.mean().item())}
+    gosc = O.OracleScene(gdesc)
+    gosc.glint_lean_pdf(0.5, 0.5, [1e-3, 0.0, 0.0, 1e-3], [0.0, 0.0, 1.0], [0.0, 0.0, 1.0])   # builds its LEAN pyramid
+    t0 = time.perf_counter()
+    gosc.render(gcfg, W.glint_render_camera(64, 64), sms.RenderOptions(integrator="path_sms_glints", spp=1, seed=1),
+                nthreads=cores)
+    dt = time.perf_counter() - t0
+    out["path_sms_glints"]["cpu_oracle"] = {"samples_per_s": 64 * 64 / dt, "cores": cores, "kind": "port",
+                                            "sample": f"64x64 pixels x 1 spp path_sms_glints, {dt:.2f} s"}
+    gctx.close()
     return out
 
 

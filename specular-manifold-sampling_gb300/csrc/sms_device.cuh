@@ -219,6 +219,7 @@ struct DevScene {
     float4 sphere[kMaxSpheres];  // center xyz, radius
     // caustic lists (scene.cpp:95-112)
     int n_casters_ss, casters_ss[kMaxCasters];
+    uint32_t casters_ss_rough;   // bit c: single-scatter caster c is rough (alpha > 0)
     int n_emitters_ss, emitters_ss[kMaxEmitters];
     int n_casters_ms, casters_ms[kMaxCasters];
     int n_emitters_ms, emitters_ms[kMaxEmitters];

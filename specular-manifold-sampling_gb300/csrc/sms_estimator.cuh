@@ -186,8 +186,12 @@ SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
 // ------------------------------------------------------------------- walk
 // sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
 // explicit seed point.  Returns ok; v holds the solution vertex.
+// kOffset: the caster is rough and `no` is its offset normal; without it the
+// constraint uses the vertex normal and `no` is ignored (compiled away).
+template <bool kOffset = false>
 SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
-                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr, f3 no = f3{0.f, 0.f, 1.f}) {
+                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr, f3 no_in = f3{0.f, 0.f, 1.f}) {
+    const f3 no = kOffset ? no_in : f3{0.f, 0.f, 1.f};
     f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
     Hit h;
     trace(sc, x, d, kRayEps, INFINITY, false, h, err);

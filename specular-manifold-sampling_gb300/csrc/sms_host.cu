@@ -537,6 +537,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         }
         if (h.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) {
             if (d.n_casters_ss >= kMaxCasters) return fail(SMS_ERR_UNSUPPORTED, "too many casters");
+            if (ds.alpha > 0.f) d.casters_ss_rough |= 1u << d.n_casters_ss;
             d.casters_ss[d.n_casters_ss++] = (int)i;
         }
         if (h.flags & SMS_SHAPE_CAUSTIC_CASTER_MULTI) {

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(128) ss_walk_kernel(DevScene sc, SolverCfg cfg
 // Group of G lanes per query; walk m of caster c sits at stream position
 // 3 + 2 (c M + m).  Contributions are summed in walk order over the first
 // occurrences of each solution direction, exactly as manifold_ss.cpp:146-196.
-template <int G>
+template <int G, bool kRough>
 __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
             const DevShape &cs = sc.shapes[caster];
             float p_off = 1.f;
             f3 no = mk(0.f, 0.f, 1.f);
-            if (work && cs.alpha > 0.f) {
+            if (kRough && work && cs.alpha > 0.f) {
                 Pcg32 r0 = query_rng(seed, query_stream(cfg, stream_off, qi), cpos);
                 no = caster_offset(cs, r0, p_off);
             }
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
                     f3 sp = sample_position(sc, cs, sx, sy);
                     Vtx v;
                     int it;
-                    bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no);
+                    bool ok = ss_walk<kRough>(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no);
                     st.walks++;
                     st.newton += (unsigned)it;
                     if (ok) {
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
                     __syncwarp();
                 }
             }
-            acc = acc + cur * (1.f / p_off);
+            acc = kRough ? acc + cur * (1.f / p_off) : acc + cur;
             n_unique += nrec;
             cpos = wpos + 2u * (uint64_t)M;
         }
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(128, 3) ss_proposal_kernel(DevScene sc, Solver
 // kLearned: seeds come from the query's learned mixture (three draws per walk,
 // mlp::proposal_seed, mixture from ss_proposal_kernel) instead of two-draw
 // uniform seeding.
-template <bool kLearned>
+template <bool kLearned, bool kRough>
 __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
                                                        float *__restrict__ value, int *__restrict__ count,
@@ -283,9 +283,12 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
         if (have_light) {
             const int caster = sc.casters_ss[c];
             rng.advance(pos - 3u);
-            float p_off;
-            const f3 no = caster_offset(sc.shapes[caster], rng, p_off);
-            pos += caster_draws(sc.shapes[caster]);
+            float p_off = 1.f;
+            f3 no = mk(0.f, 0.f, 1.f);
+            if (kRough) {
+                no = caster_offset(sc.shapes[caster], rng, p_off);
+                pos += caster_draws(sc.shapes[caster]);
+            }
             f3 sp;
             if constexpr (kLearned) {
                 const float us = rng.next_f32(), sx = rng.next_f32(), sy = rng.next_f32();
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
             }
             Vtx v;
             int it;
-            bool ok = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no);
+            bool ok = ss_walk<kRough>(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no);
             st.walks++;
             st.newton += (unsigned)it;
             nw++;
@@ -308,7 +311,7 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
                     f3 dir = normalize(v.p - Q.x);
                     f3 spec = contribution(sc, Q.x, L, v, err, st);
                     // the caster's estimate is divided by the offset density (manifold_ss.cpp:199)
-                    f3 val = diffuse_eval(Q, dir) * spec * (1.f / p_off);
+                    f3 val = kRough ? diffuse_eval(Q, dir) * spec * (1.f / p_off) : diffuse_eval(Q, dir) * spec;
                     scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;
                     scr.val[qi] = val.x; scr.val[(size_t)n + qi] = val.y; scr.val[2 * (size_t)n + qi] = val.z;
                     enqueue = true;
@@ -351,7 +354,7 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
 //
 // All lanes run one warp-uniform loop: groups whose query finished fetch the
 // next one at the top, so every ballot and shuffle has the whole warp.
-template <bool kLearned, int G>
+template <bool kLearned, int G, bool kRough>
 __global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
@@ -394,7 +397,7 @@ __global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCf
                 pos = scr.pos[qi];
                 dir0 = mk(scr.dir0[qi], scr.dir0[(size_t)n + qi], scr.dir0[2 * (size_t)n + qi]);
                 t0 = 1;
-                if (cshape.alpha > 0.f) {
+                if (kRough) {
                     // the offset normal drawn before the first walk
                     Pcg32 r0 = base;
                     r0.advance((uint64_t)(pos - 3u - kStride - 2u));
@@ -421,7 +424,7 @@ __global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCf
                 sp = sample_position(sc, sc.shapes[caster], sx, sy);
             }
             Vtx v;
-            succ = ss_walk(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no) &&
+            succ = ss_walk<kRough>(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no) &&
                    fabsf(dot(dir0, normalize(v.p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
         }
         const unsigned b = (__ballot_sync(full, succ) & gmask) >> gbase;
@@ -570,8 +573,9 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
         uint32_t blocks_needed = (n + groups_per_block - 1) / groups_per_block;
         uint32_t blocks = std::min<uint32_t>(blocks_needed, (uint32_t)(num_sms * bps));
         phase_begin(tm, kPhaseSsBiased, s);
-        if (G == 16) ss_biased_kernel<16><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
-        else ss_biased_kernel<32><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
+        auto biased = sc.casters_ss_rough ? (G == 16 ? ss_biased_kernel<16, true> : ss_biased_kernel<32, true>)
+                                          : (G == 16 ? ss_biased_kernel<16, false> : ss_biased_kernel<32, false>);
+        biased<<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
         phase_end(tm, s);
         return cudaGetLastError();
     }
@@ -586,6 +590,7 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
         cudaError_t e = cudaMemsetAsync(&ctr->trial_count, 0, 2 * sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
         const bool learned = prop && prop->shape == sc.casters_ss[c];
+        const bool rough = (sc.casters_ss_rough >> c) & 1u;
         const mlp::SeedProposal pr = learned ? *prop : mlp::SeedProposal{};
         phase_begin(tm, kPhaseSsFirst, s);
         if (learned) {
@@ -594,21 +599,32 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
             if (e != cudaSuccess) return e;
             const uint32_t pblocks = std::min<uint32_t>((n + 127) / 128, (uint32_t)num_sms * 3);
             ss_proposal_kernel<<<pblocks, 128, smem, s>>>(sc, cfg, q, n, seed, stream_off, pr);
-            ss_first_kernel<true><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value,
-                                                                  count, walks, scr, ctr, pr);
+            auto first = rough ? ss_first_kernel<true, true> : ss_first_kernel<true, false>;
+            first<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr,
+                                                  pr);
         } else {
-            ss_first_kernel<false><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count,
-                                                                   walks, scr, ctr, pr);
+            auto first = rough ? ss_first_kernel<false, true> : ss_first_kernel<false, false>;
+            first<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr,
+                                                  pr);
         }
         phase_end(tm, s);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         phase_begin(tm, kPhaseSsTrials, s);
         const int group = trial_group > 0 ? trial_group : (learned ? 8 : 32);
-        auto trials = learned ? (group == 8 ? ss_trials_kernel<true, 8>
-                                            : group == 16 ? ss_trials_kernel<true, 16> : ss_trials_kernel<true, 32>)
-                              : (group == 8 ? ss_trials_kernel<false, 8>
-                                            : group == 16 ? ss_trials_kernel<false, 16> : ss_trials_kernel<false, 32>);
+        auto trials =
+            rough ? (learned ? (group == 8    ? ss_trials_kernel<true, 8, true>
+                                : group == 16 ? ss_trials_kernel<true, 16, true>
+                                              : ss_trials_kernel<true, 32, true>)
+                             : (group == 8    ? ss_trials_kernel<false, 8, true>
+                                : group == 16 ? ss_trials_kernel<false, 16, true>
+                                              : ss_trials_kernel<false, 32, true>))
+                  : (learned ? (group == 8    ? ss_trials_kernel<true, 8, false>
+                                : group == 16 ? ss_trials_kernel<true, 16, false>
+                                              : ss_trials_kernel<true, 32, false>)
+                             : (group == 8    ? ss_trials_kernel<false, 8, false>
+                                : group == 16 ? ss_trials_kernel<false, 16, false>
+                                              : ss_trials_kernel<false, 32, false>));
         trials<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr, pr);
         phase_end(tm, s);
         e = cudaGetLastError();

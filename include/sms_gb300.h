@@ -60,7 +60,11 @@ const char *sms_last_error(void);
  * the SMS integrators read (path_sms_glints.cpp:42-54). */
 typedef struct sms_config {
     int32_t biased;                 /* false */
-    int32_t twostage;               /* false */
+    int32_t twostage;               /* false; two-stage solver on normal-mapped
+                                       single-scatter casters (every caster must
+                                       carry the map, else SMS_ERR_UNSUPPORTED;
+                                       multi-scatter and glints ignore it, as
+                                       the reference does) */
     int32_t halfvector_constraints; /* false */
     int32_t mnee_init;              /* false; straight-line seeds (manifold_ss.cpp:229-241) */
     float   step_scale;             /* 1     */
@@ -166,7 +170,16 @@ sms_status sms_scene_add_area_emitter(sms_scene *scene, int32_t shape_id,
  * the reference's LEAN data, src/librender/normalmap.cpp:7-36, as used by
  * NormalmapBSDF::slope, src/bsdfs/normalmap.cpp:305-336).  slopes: res*res
  * interleaved FP16 pairs (IEEE binary16 bit patterns), row-major with v as the
- * row; tiles as the BSDF's "tiles" parameter.  Marks the shape glinty. */
+ * row; tiles as the BSDF's "tiles" parameter.  A shape without caster or
+ * bouncer flags becomes glinty.  On a caster / bouncer the map is the
+ * reference's normalmap BSDF around the shape's dielectric / conductor: its
+ * manifold vertices take the normal-mapped frame and its derivative
+ * (src/bsdfs/normalmap.cpp:236-290), and cfg.twostage enables the two-stage
+ * solver on it (manifold_ss.cpp:253-270): each walk first solves on the
+ * smoothed surface (the top level of the map's LEAN pyramid) toward a slope
+ * drawn from that level's Gaussian, then on the full map.  Walks on a
+ * normal-mapped caster take a learned proposal's seeds: SMS_ERR_UNSUPPORTED.
+ * One normal map per scene. */
 sms_status sms_scene_set_normalmap(sms_scene *scene, int32_t shape_id,
                                    const uint16_t *slopes, uint32_t res, float tiles);
 
@@ -305,11 +318,15 @@ sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *queries_dev,
  * the reference's figure scripts use.
  *   queries   SoA as above (n columns)
  *   walk_in   SoA, SMS_WALK_IN_FIELDS rows: ei.p (3), p_start (3),
- *             sample (2; used by sample_position when p_start == 0)
+ *             sample (2; used by sample_position when p_start == 0); with
+ *             cfg.twostage SMS_SS_WALK_IN_FIELDS_TWOSTAGE rows, the last two
+ *             the sample of the smoothed solve's slope (manifold_ss.cpp:258)
  *   caster    shape id of the specular shape to walk on
  *   walk_out  SoA, SMS_WALK_OUT_FIELDS rows: ok, iterations, p_final (3),
- *             p_init (3), n_final (3)   (ok/iterations stored as floats)       */
+ *             p_init (3), n_final (3)   (ok/iterations stored as floats;
+ *             n_final is the vertex normal, the map's on a normal-mapped caster) */
 #define SMS_WALK_IN_FIELDS 8
+#define SMS_SS_WALK_IN_FIELDS_TWOSTAGE 10
 #define SMS_WALK_OUT_FIELDS 11
 sms_status sms_ss_walk_batch(sms_ctx *ctx, int32_t caster, const float *queries,
                              const float *walk_in, uint32_t n, float *walk_out);

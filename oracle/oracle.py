@@ -98,6 +98,7 @@ def load(fma: bool = False):
         "oracle_render": (i32, [vp, C.POINTER(_Config), C.POINTER(_Camera), C.POINTER(_RenderOptions), vp, C.c_int]),
         "oracle_fresnel_conductor": (f32, [f32, f32, f32]),
         "oracle_uniform_sphere": (None, [f32, f32, C.POINTER(f32)]),
+        "oracle_sample_slope_gaussian": (None, [vp, f32, f32, f32, vp, vp]),
         "oracle_pcg32": (None, [u64, u64, u32, vp]),
         "oracle_pcg32_f32": (None, [u64, u64, u32, vp]),
     }
@@ -163,6 +164,8 @@ class OracleScene:
         n = queries.shape[1]
         q = np.ascontiguousarray(queries, np.float32)
         w = np.ascontiguousarray(walk_in, np.float32)
+        if w.shape != (10 if config.twostage else 8, n):
+            raise ValueError(f"walk_in shape {w.shape} does not fit the config")
         out = np.zeros((11, n), np.float32)
         self._lib.oracle_ss_walk_batch(self._h, C.byref(_cfg(config)), caster, q.ctypes.data, w.ctypes.data, n,
                                   out.ctypes.data)
@@ -286,3 +289,13 @@ class OracleScene:
         if getattr(self, "_h", None) and getattr(self, "_lib", None) is not None:
             self._lib.oracle_scene_destroy(self._h)
             self._h = None
+
+
+def sample_slope_gaussian(mu, a: float, b: float, c: float, u) -> np.ndarray:
+    """The two-stage solver's slope draw from N(mu, (a, c; c, b)) for the
+    uniform pair u (manifold.h:326-345)."""
+    m = np.ascontiguousarray(mu, np.float32)
+    uu = np.ascontiguousarray(u, np.float32)
+    out = np.zeros(2, np.float32)
+    load().oracle_sample_slope_gaussian(m.ctypes.data, a, b, c, uu.ctypes.data, out.ctypes.data)
+    return out

@@ -544,15 +544,62 @@ static V3 mnee_target(const Shape &s, V3 lp) {
     return real_ior ? lp : s.bbox_center;
 }
 
-/* frame.h:197-240 (compute_shading_frame{,_derivative}); bsdf.cpp:17-31 */
-static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v) {
+static V2 nm_slope(const NormalMap &m, V2 uv);
+static void nm_slope_derivative(const NormalMap &m, V2 uv, V2 &du, V2 &dv);
+
+/* A caster / bouncer carrying the scene's normal map (the reference's
+ * normalmap BSDF around its dielectric / conductor). */
+static bool nm_frames(const Scene &sc, int shape) {
+    const uint32_t chain = SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER;
+    return shape == sc.glinty_shape && sc.nmap.res > 0 && (sc.shapes[shape].flags & chain) != 0;
+}
+
+/* NormalmapBSDF::frame / frame_derivative (normalmap.cpp:236-290): the base
+ * frame (n0, tangent from dp_du) and its derivative applied to the slope
+ * normal (-s_x, -s_y, 1) at level 0 and its derivative; coarse = the
+ * two-stage solver's smoothing 1: the top LEAN level (mean slope, no
+ * derivative). */
+static void nm_vertex_frame(const Scene &sc, const SI &si, V3 n0, V3 dn0_du, V3 dn0_dv, bool coarse, V3 &n,
+                            V3 &dn_du, V3 &dn_dv) {
+    V3 s0 = si.dp_du - n0 * dot(n0, si.dp_du);
+    const float inv_len = 1.f / norm(s0);
+    s0 *= inv_len;
+    const V3 t0 = cross(n0, s0);
+    V3 ds_du = (-dn0_du * dot(n0, si.dp_du) - n0 * dot(dn0_du, si.dp_du)) * inv_len;
+    V3 ds_dv = (-dn0_dv * dot(n0, si.dp_du) - n0 * dot(dn0_dv, si.dp_du)) * inv_len;
+    ds_du -= s0 * dot(ds_du, s0);
+    ds_dv -= s0 * dot(ds_dv, s0);
+    const V3 dt_du = cross(dn0_du, s0) + cross(n0, ds_du), dt_dv = cross(dn0_dv, s0) + cross(n0, ds_dv);
+    V3 nl, dl_du, dl_dv;
+    if (coarse) {
+        const std::vector<float> &t = sc.nmap.lean.back();
+        nl = V3(-t[0], -t[1], 1.f);
+        dl_du = V3(0.f); dl_dv = V3(0.f);
+    } else {
+        V2 sl = nm_slope(sc.nmap, si.uv), du, dv;
+        nm_slope_derivative(sc.nmap, si.uv, du, dv);
+        nl = V3(-sl.x, -sl.y, 1.f);
+        dl_du = V3(-du.x, -du.y, 0.f);
+        dl_dv = V3(-dv.x, -dv.y, 0.f);
+    }
+    V3 wn = s0 * nl.x + t0 * nl.y + n0 * nl.z;
+    const float il = 1.f / norm(wn);
+    wn *= il;
+    V3 a = (s0 * dl_du.x + t0 * dl_du.y + n0 * dl_du.z + ds_du * nl.x + dt_du * nl.y + dn0_du * nl.z) * il;
+    V3 b = (s0 * dl_dv.x + t0 * dl_dv.y + n0 * dl_dv.z + ds_dv * nl.x + dt_dv * nl.y + dn0_dv * nl.z) * il;
+    n = wn;
+    dn_du = a - wn * dot(a, wn);
+    dn_dv = b - wn * dot(b, wn);
+}
+
+/* frame.h:197-240 (compute_shading_frame{,_derivative}); bsdf.cpp:17-31;
+ * nm_coarse: the two-stage solver's smoothed frame on a normal-mapped shape */
+static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v, bool nm_coarse = false) {
     const Shape &sh = sc.shapes[si.shape];
     v.p = si.p; v.dp_du = si.dp_du; v.dp_dv = si.dp_dv; v.gn = si.n; v.uv = si.uv;
     v.shape = si.shape; v.fixed_direction = false;
     v.eta = bsdf_eta(sh.bsdf);
     V3 n = si.shn;
-    V3 s = normalize(si.dp_du - n * dot(n, si.dp_du));
-    v.n = n; v.s = s; v.t = cross(n, s);
     V3 dndu, dndv;
     if (sh.kind == 0) {
         float inv_r = (sh.flip ? -1.f : 1.f) / sh.radius;   /* sphere.cpp:376-382 */
@@ -560,6 +607,9 @@ static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v) {
     } else {
         mesh_normal_derivative(sh, si, dndu, dndv);
     }
+    if (nm_frames(sc, si.shape)) nm_vertex_frame(sc, si, si.shn, dndu, dndv, nm_coarse, n, dndu, dndv);
+    V3 s = normalize(si.dp_du - n * dot(n, si.dp_du));
+    v.n = n; v.s = s; v.t = cross(n, s);
     V3 s0 = si.dp_du - n * dot(n, si.dp_du);
     float inv_len_s = 1.f / norm(s0);
     s0 *= inv_len_s;
@@ -753,9 +803,11 @@ struct Cfg {
     sms_config c;
 };
 
-/* manifold_ss.cpp:329-405.  Returns (ok, si_current, iterations). */
+/* manifold_ss.cpp:329-405.  Returns (ok, si_current, iterations); coarse:
+ * smoothing = 1 (the two-stage solver's first solve, manifold_ss.cpp:262). */
 static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MVertex &init,
-                          const EI &ei, SI &si_out, int &iters_out, V3 no = V3(0.f, 0.f, 1.f)) {
+                          const EI &ei, SI &si_out, int &iters_out, V3 no = V3(0.f, 0.f, 1.f),
+                          bool coarse = false) {
     MVertex vtx = init;
     bool success = false;
     int it = 0;
@@ -776,7 +828,7 @@ static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MV
             continue;
         }
         beta = std::min(1.f, 2.f * beta);
-        vertex_from_si(sc, si_current, vtx);
+        vertex_from_si(sc, si_current, vtx, coarse);
         it++;
     }
     iters_out = it;
@@ -806,10 +858,28 @@ static Query load_query(const float *q, uint32_t n, uint32_t i) {
     return r;
 }
 
-/* manifold_ss.cpp:203-279 (twostage: unsupported); no = offset normal */
+/* sample_gaussian (manifold.h:326-345) through square_to_std_normal
+ * (warp.h:184-190): a slope from N(mu, sigma), sigma = (a, c; c, b). */
+static V2 sample_slope_gaussian(V2 mu, float a, float b, float c, V2 u) {
+    const float r = std::sqrt(-2.f * std::log(1.f - u.x)), ph = 2.f * kPi * u.y;
+    const float px = std::cos(ph) * r, py = std::sin(ph) * r;
+    const float sx = std::sqrt(a), sy = std::sqrt(b);
+    const float rho = c / (sx * sy);
+    const float ka = std::sqrt(1.f + rho), kb = std::sqrt(1.f - rho);
+    const float d0 = 0.5f * ka + 0.5f * kb, d1 = 0.5f * ka - 0.5f * kb;
+    return V2{(d0 * px + d1 * py) * sx + mu.x, (d1 * px + d0 * py) * sy + mu.y};
+}
+
+/* manifold_ss.cpp:203-279; no = offset normal.  cfg.twostage (:253-270, a
+ * normal-mapped caster): a first solve on the smoothed surface (the top LEAN
+ * level's frame) toward a slope drawn from that level's Gaussian around the
+ * mean of its mean slope and the offset slope (the two numbers g), then the
+ * solve on the full map from its solution.  g is drawn for every walk (the
+ * reference draws it after the first ray hit the caster), so that every walk
+ * owns a fixed run of random numbers. */
 static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, const Query &q,
                         const EI &ei, V2 sample, V3 p_start, SI &si_final, SI &si_init,
-                        int &iters, V3 no = V3(0.f, 0.f, 1.f)) {
+                        int &iters, V3 no = V3(0.f, 0.f, 1.f), V2 g = V2{0.f, 0.f}) {
     const Shape &shape = sc.shapes[caster];
     V3 p = sample_position(shape, sample);
     if (p_start.x != 0.f || p_start.y != 0.f || p_start.z != 0.f) p = p_start;
@@ -820,8 +890,22 @@ static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, cons
     iters = 0;
     if (!si_init.valid() || caster != si_init.shape) return false;
     MVertex v0;
-    vertex_from_si(sc, si_init, v0);
+    vertex_from_si(sc, si_init, v0, cfg.twostage != 0);
+    int it1 = 0;
+    if (cfg.twostage) {
+        const std::vector<float> &t = sc.nmap.lean.back();
+        const float a = std::max(0.f, t[2] - t[0] * t[0]), b = std::max(0.f, t[3] - t[1] * t[1]),
+                    c = std::max(0.f, t[4] - t[0] * t[1]);
+        const V2 mu{0.5f * (t[0] - no.x / no.z), 0.5f * (t[1] - no.y / no.z)};
+        const V2 sl = sample_slope_gaussian(mu, a, b, c, g);
+        const V3 ln = normalize(V3(-sl.x, -sl.y, 1.f));
+        SI si_smooth;
+        const bool ok1 = newton_solver(sc, cfg, q.p, v0, ei, si_smooth, it1, ln, true);
+        if (!ok1 || !si_smooth.valid()) { iters = it1; return false; }
+        vertex_from_si(sc, si_smooth, v0, false);
+    }
     bool ok = newton_solver(sc, cfg, q.p, v0, ei, si_final, iters, no);
+    iters += it1;
     return ok && si_final.valid();
 }
 
@@ -1187,9 +1271,11 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
                 smp = rng.next_2d();
                 return V3(0.f);
             };
+            auto stage_of = [&]() { return cfg.twostage ? rng.next_2d() : V2{0.f, 0.f}; };
             V2 smp;
             V3 ps = seed_of(smp);
-            bool ok = sample_path(sc, cfg, caster, q, ei, smp, ps, si_final, si_init, it, no);
+            V2 g = stage_of();
+            bool ok = sample_path(sc, cfg, caster, q, ei, smp, ps, si_final, si_init, it, no, g);
             walks_out++; st.walks++; st.newton += it;
             if (!ok) { st.failed++; continue; }
             st.succeeded++;
@@ -1205,7 +1291,8 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
                 int it2 = 0;
                 V2 smp2;
                 V3 ps2 = seed_of(smp2);
-                bool ok2 = sample_path(sc, cfg, caster, q, ei, smp2, ps2, sf, si0, it2, no);
+                V2 g2 = stage_of();
+                bool ok2 = sample_path(sc, cfg, caster, q, ei, smp2, ps2, sf, si0, it2, no, g2);
                 walks_out++; st.walks++; st.newton += it2;
                 if (ok2) {
                     V3 dt = normalize(sf.p - q.p);
@@ -1222,7 +1309,9 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
         } else {
             std::vector<V3> solutions;
             for (int m = 0; m < cfg.max_trials; ++m) {
-                bool ok = sample_path(sc, cfg, caster, q, ei, rng.next_2d(), V3(0.f), si_final, si_init, it, no);
+                const V2 smp = rng.next_2d();
+                const V2 g = cfg.twostage ? rng.next_2d() : V2{0.f, 0.f};
+                bool ok = sample_path(sc, cfg, caster, q, ei, smp, V3(0.f), si_final, si_init, it, no, g);
                 walks_out++; st.walks++; st.newton += it;
                 if (!ok) { st.failed++; continue; }
                 st.succeeded++;
@@ -2420,6 +2509,23 @@ static bool nm_conductor_sample(const NormalMap &m, const sms_bsdf &b, V3 n, V3 
     return true;
 }
 
+/* NormalmapBSDF::sample (normalmap.cpp:118-135) around any smooth nested BSDF:
+ * sampled in the perturbed frame at uv, the direction taken back to the
+ * shading frame (fs, ft, n) and kept when it lies on the same side of both
+ * frames' normals. */
+static bool nm_bsdf_sample(const NormalMap &m, const sms_bsdf &b, V3 fs, V3 ft, V3 n, V3 dp_du, V2 uv, V3 wi_w,
+                           float u1, float u2, float u3, PtBsdf &bs) {
+    V3 pn, ps, pt;
+    nm_frame(m, n, dp_du, uv, pn, ps, pt);
+    const V3 wi(dot(wi_w, ps), dot(wi_w, pt), dot(wi_w, pn));
+    if (!pt_bsdf_sample(b, wi, u1, u2, u3, bs)) return false;
+    const V3 wo_w = ps * bs.wo.x + pt * bs.wo.y + pn * bs.wo.z;
+    const V3 wo(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
+    if (!(bs.wo.z * wo.z > 0.f)) return false;
+    bs.wo = wo;
+    return true;
+}
+
 /* PerspectiveCamera::importance (perspective.cpp:224-276) x film size for the
  * world-space direction d from the camera */
 static float pt_importance(const sms_camera &cam, const double tm[2], V3 d) {
@@ -2597,11 +2703,8 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
         PtBsdf bs;
         if (nmapped) {
-            /* normal-mapped conductor at the hit's own uv */
-            V3 wo_w; float w;
-            if (!nm_conductor_sample(sc.nmap, s.bsdf, si.shn, si.dp_du, si.uv, wiw, wo_w, w)) break;
-            bs.wo = V3(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n_sh));
-            bs.weight = V3(w); bs.pdf = 1.f; bs.eta = 1.f; bs.delta = true;
+            /* the normal-mapped BSDF at the hit's own uv */
+            if (!nm_bsdf_sample(sc.nmap, s.bsdf, fs, ft, n_sh, si.dp_du, si.uv, wiw, u1, u2, u3, bs)) break;
         } else if (!pt_bsdf_sample(s.bsdf, wi, u1, u2, u3, bs)) break;
         thr = thr * bs.weight;
         eta *= bs.eta;
@@ -2631,7 +2734,9 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 ei.p = ep;
                 SI sf, s0;
                 int it = 0;
-                bool found = sample_path(sc, cfg, si.shape, q, ei, V2{0.5f, 0.5f}, V3(0.f), sf, s0, it);
+                sms_config c1 = cfg;
+                c1.twostage = 0;   /* the library refuses twostage with this check */
+                bool found = sample_path(sc, c1, si.shape, q, ei, V2{0.5f, 0.5f}, V3(0.f), sf, s0, it);
                 if (found) {
                     V3 dpt = normalize(si.p - prev_p), dmn = normalize(sf.p - prev_p);
                     found = std::fabs(dot(dpt, dmn) - 1.f) < cfg.uniqueness_threshold;
@@ -2766,7 +2871,10 @@ void oracle_scene_finalize(void *s) {
 }
 
 /* Per-walk sample_path with explicit ei.p and start point (SoA in/out as in
- * include/sms_gb300.h sms_ss_walk_batch). */
+ * include/sms_gb300.h sms_ss_walk_batch; with cfg.twostage walk_in carries
+ * SMS_SS_WALK_IN_FIELDS_TWOSTAGE rows, the last two the slope sample).
+ * n_final is the solution vertex's normal (the normal map's, on a
+ * normal-mapped caster). */
 int oracle_ss_walk_batch(void *s, const sms_config *cfg, int caster, const float *queries,
                          const float *walk_in, uint32_t n, float *out) {
     Scene *sc = as_scene(s);
@@ -2777,11 +2885,15 @@ int oracle_ss_walk_batch(void *s, const sms_config *cfg, int caster, const float
         EI ei; ei.p = V3(w(0), w(1), w(2)); ei.is_point = true;
         V3 ps(w(3), w(4), w(5));
         V2 smp; smp.x = w(6); smp.y = w(7);
+        V2 g;
+        if (cfg->twostage) { g.x = w(8); g.y = w(9); }
         SI sf, s0;
         int it = 0;
-        bool ok = sample_path(*sc, *cfg, caster, q, ei, smp, ps, sf, s0, it);
+        bool ok = sample_path(*sc, *cfg, caster, q, ei, smp, ps, sf, s0, it, V3(0.f, 0.f, 1.f), g);
+        MVertex vf;
+        if (ok) vertex_from_si(*sc, sf, vf);
         float vals[SMS_WALK_OUT_FIELDS] = {ok ? 1.f : 0.f, (float)it, sf.p.x, sf.p.y, sf.p.z,
-                                           s0.p.x, s0.p.y, s0.p.z, sf.shn.x, sf.shn.y, sf.shn.z};
+                                           s0.p.x, s0.p.y, s0.p.z, vf.n.x, vf.n.y, vf.n.z};
         if (!ok) { for (int k = 2; k < 5; ++k) vals[k] = 0.f; for (int k = 8; k < 11; ++k) vals[k] = 0.f; }
         if (!s0.valid()) for (int k = 5; k < 8; ++k) vals[k] = 0.f;
         for (int k = 0; k < SMS_WALK_OUT_FIELDS; ++k) out[(size_t)k * n + i] = vals[k];
@@ -3042,7 +3154,11 @@ int oracle_scene_set_normalmap(void *s, int shape, const uint16_t *slopes_half, 
     sc->nmap.sx.resize(n);
     sc->nmap.sy.resize(n);
     for (size_t i = 0; i < n; ++i) { sc->nmap.sx[i] = h2f(slopes_half[2 * i]); sc->nmap.sy[i] = h2f(slopes_half[2 * i + 1]); }
+    sc->nmap.lean.clear();
     sc->glinty_shape = shape;
+    const uint32_t chain = SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER;
+    if (!(sc->shapes[shape].flags & chain)) sc->shapes[shape].flags |= SMS_SHAPE_GLINTY;
+    else build_lean(sc->nmap);   /* the two-stage solver's smoothed frames read its top level */
     return 0;
 }
 
@@ -3158,6 +3274,15 @@ float oracle_glint_lean_pdf(void *s, float u, float v, const float *duv, const f
     V2 dx; dx.x = duv[0]; dx.y = duv[1];
     V2 dy; dy.x = duv[2]; dy.y = duv[3];
     return glint_lean_pdf(sc->nmap, uv, dx, dy, V3(wi[0], wi[1], wi[2]), V3(wo[0], wo[1], wo[2]));
+}
+
+/* The two-stage solver's slope sample (sample_gaussian) for tests: mu (2),
+ * sigma = (a, c; c, b), u (2); out = the slope. */
+void oracle_sample_slope_gaussian(const float *mu, float a, float b, float c, const float *u, float *out) {
+    V2 m; m.x = mu[0]; m.y = mu[1];
+    V2 uu; uu.x = u[0]; uu.y = u[1];
+    V2 r = sample_slope_gaussian(m, a, b, c, uu);
+    out[0] = r.x; out[1] = r.y;
 }
 
 void oracle_uniform_sphere(float u, float v, float *out) {

@@ -29,6 +29,7 @@ LIB_PATH = PKG_DIR / "libsms_gb300.so"
 QUERY_FIELDS = 16
 NOALLOC_MAX_QUERIES = 1 << 18
 WALK_IN_FIELDS = 8
+SS_WALK_IN_FIELDS_TWOSTAGE = 10
 WALK_OUT_FIELDS = 11
 MS_WALK_OUT_FIELDS = 9
 GLINT_QUERY_FIELDS = 21
@@ -681,10 +682,11 @@ class SpecularManifoldSingleScatter:
 
     def sample_path(self, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
         """Per-walk sample_path with explicit emitter point and start point.
-        walk_in: (8, n) rows ei.p(3), p_start(3), sample(2).  Returns (11, n)."""
+        walk_in: (8, n) rows ei.p(3), p_start(3), sample(2); with the twostage
+        solver (10, n), rows 8-9 the smoothed solve's slope sample.  Returns (11, n)."""
         n = queries.shape[1]
         q = _soa(queries, QUERY_FIELDS, n)
-        w = _soa(walk_in, WALK_IN_FIELDS, n)
+        w = _soa(walk_in, SS_WALK_IN_FIELDS_TWOSTAGE if self.ctx.config.twostage else WALK_IN_FIELDS, n)
         out = np.zeros((WALK_OUT_FIELDS, n), np.float32)
         _check(_LIB.sms_ss_walk_batch(self.ctx.handle, caster, _ptr(q), _ptr(w), n, _ptr(out)))
         return out

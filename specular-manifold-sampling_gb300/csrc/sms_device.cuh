@@ -19,6 +19,7 @@
 #include <cstdint>
 #include <cstring>
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 
 // Every helper here is host+device so that the host-side tests can run the
 // exact traversal and vertex code the kernels run.
@@ -181,6 +182,7 @@ struct DevShape {
     int reflective;        // complex ior: MNEE initialisation aims at the box centre
     float albedo[3];       // diffuse reflectance (path tracer)
     float alpha;           // Beckmann roughness of a rough dielectric / conductor (0: smooth)
+    int nmap_frames;       // manifold vertices on this shape use its normal map (a caster / bouncer)
 };
 
 // Target of the MNEE initialisation (manifold_ss.cpp:229-241,
@@ -220,6 +222,7 @@ struct DevScene {
     // caustic lists (scene.cpp:95-112)
     int n_casters_ss, casters_ss[kMaxCasters];
     uint32_t casters_ss_rough;   // bit c: single-scatter caster c is rough (alpha > 0)
+    uint32_t casters_ss_nm;      // bit c: single-scatter caster c carries the normal map
     int n_emitters_ss, emitters_ss[kMaxEmitters];
     int n_casters_ms, casters_ms[kMaxCasters];
     int n_emitters_ms, emitters_ms[kMaxEmitters];
@@ -228,7 +231,8 @@ struct DevScene {
     const uint32_t *nmap;      // one __half2 per texel
     uint32_t nmap_res;
     float nmap_tiles;
-    int glinty_shape;
+    int glinty_shape;           // the shape carrying the slope map
+    int nmap_shape;             // same id: normal-mapped manifold-vertex frames
     // LEAN mip pyramid of the slope map (glints integrator): level l starts at
     // lean + lean_off[l] (floats), 5 floats per texel, (nmap_res >> l)^2 texels
     const float *lean;
@@ -490,8 +494,124 @@ struct Vtx {
 };
 
 // ManifoldVertex(si) (manifold.h:89-113) from a closest hit.
+SMS_HD float2 nm_texel(const DevScene &sc, uint32_t idx) {
+#ifdef __CUDA_ARCH__
+    uint32_t bits = __ldg(sc.nmap + idx);
+    __half2 h = *reinterpret_cast<__half2 *>(&bits);
+    return __half22float2(h);
+#else
+    (void)sc; (void)idx;
+    return make_float2(0.f, 0.f);
+#endif
+}
+
+// Bilinear slope at level 0 after the tiling wrap (normalmap.cpp:305-316).
+SMS_HD float2 nm_slope0(const DevScene &sc, float u_in, float v_in) {
+    float u = u_in * sc.nmap_tiles, v = v_in * sc.nmap_tiles;
+    u -= floorf(u);
+    v -= floorf(v);
+    const uint32_t R = sc.nmap_res;
+    float res = (float)R, duv = 1.f / res;
+    float px = fminf(fmaxf((u - 0.5f * duv) * res, 0.f), res - 1.f);
+    float py = fminf(fmaxf((v - 0.5f * duv) * res, 0.f), res - 1.f);
+    uint32_t x0 = (uint32_t)floorf(px), y0 = (uint32_t)floorf(py);
+    uint32_t x1 = min(x0 + 1, R - 1), y1 = min(y0 + 1, R - 1);
+    x0 = min(x0, R - 1);
+    y0 = min(y0, R - 1);
+    float wx = px - (float)x0, wy = py - (float)y0;
+    float2 t00 = nm_texel(sc, y0 * R + x0), t10 = nm_texel(sc, y0 * R + x1), t01 = nm_texel(sc, y1 * R + x0),
+           t11 = nm_texel(sc, y1 * R + x1);
+    float w0x = 1.f - wx, w0y = 1.f - wy;
+    return make_float2(w0y * (w0x * t00.x + wx * t10.x) + wy * (w0x * t01.x + wx * t11.x),
+                       w0y * (w0x * t00.y + wx * t10.y) + wy * (w0x * t01.y + wx * t11.y));
+}
+
+// Bilinear slope at level 0 and its uv derivative x res x tiles
+// (normalmap.h:125-193 with the tiling scale of normalmap.cpp:270-273).
+SMS_HD float2 nm_slope0_d(const DevScene &sc, float u_in, float v_in, float2 &du, float2 &dv) {
+    float u = u_in * sc.nmap_tiles, v = v_in * sc.nmap_tiles;
+    u -= floorf(u);
+    v -= floorf(v);
+    const uint32_t R = sc.nmap_res;
+    float res = (float)R, duv = 1.f / res;
+    float px = fminf(fmaxf((u - 0.5f * duv) * res, 0.f), res - 1.f);
+    float py = fminf(fmaxf((v - 0.5f * duv) * res, 0.f), res - 1.f);
+    uint32_t x0 = (uint32_t)floorf(px), y0 = (uint32_t)floorf(py);
+    uint32_t x1 = min(x0 + 1, R - 1), y1 = min(y0 + 1, R - 1);
+    x0 = min(x0, R - 1);
+    y0 = min(y0, R - 1);
+    float wx = px - (float)x0, wy = py - (float)y0;
+    float2 t00 = nm_texel(sc, y0 * R + x0), t10 = nm_texel(sc, y0 * R + x1), t01 = nm_texel(sc, y1 * R + x0),
+           t11 = nm_texel(sc, y1 * R + x1);
+    float w0x = 1.f - wx, w0y = 1.f - wy;
+    float tmpx = t01.x + t10.x - t11.x, tmpy = t01.y + t10.y - t11.y;
+    du = make_float2((t10.x + t00.x * (wy - 1.f) - tmpx * wy) * res * sc.nmap_tiles,
+                     (t10.y + t00.y * (wy - 1.f) - tmpy * wy) * res * sc.nmap_tiles);
+    dv = make_float2((t01.x + t00.x * (wx - 1.f) - tmpx * wx) * res * sc.nmap_tiles,
+                     (t01.y + t00.y * (wx - 1.f) - tmpy * wx) * res * sc.nmap_tiles);
+    return make_float2(w0y * (w0x * t00.x + wx * t10.x) + wy * (w0x * t01.x + wx * t11.x),
+                       w0y * (w0x * t00.y + wx * t10.y) + wy * (w0x * t01.y + wx * t11.y));
+}
+
+// Mean slope and covariance of the whole map: the top level of the LEAN
+// pyramid (the lookup of a surface point without uv partials,
+// normalmap.cpp:374-377, as the two-stage solver's lean() call makes it).
+SMS_HD void nm_top_lean(const DevScene &sc, float &mx, float &my, float &sa, float &sb, float &scv) {
+    const float *t = sc.lean + sc.lean_off[sc.lean_levels - 1];
+    mx = t[0];
+    my = t[1];
+    sa = fmaxf(0.f, t[2] - t[0] * t[0]);
+    sb = fmaxf(0.f, t[3] - t[1] * t[1]);
+    scv = fmaxf(0.f, t[4] - t[0] * t[1]);
+}
+
+// ManifoldVertex frame of a normal-mapped shape (NormalmapBSDF::frame /
+// frame_derivative, normalmap.cpp:236-290): the base shading frame (n0,
+// tangent from dp_du) and its derivative (frame.h:197-240) applied to the
+// slope normal (-s_x, -s_y, 1) and its uv derivative.  coarse: the two-stage
+// solver's smoothing = 1, i.e. the top LEAN level (mean slope, no derivative).
+SMS_HD void nm_vertex_frame(const DevScene &sc, f3 p, f3 dp_du, f3 n0, f3 dn0_du, f3 dn0_dv, float u, float v,
+                            bool coarse, f3 &n, f3 &dn_du, f3 &dn_dv) {
+    (void)p;
+    f3 s0 = dp_du - n0 * dot(n0, dp_du);
+    const float inv_len = 1.f / length(s0);
+    s0 = s0 * inv_len;
+    const f3 t0 = cross(n0, s0);
+    f3 ds_du = (-dn0_du * dot(n0, dp_du) - n0 * dot(dn0_du, dp_du)) * inv_len;
+    f3 ds_dv = (-dn0_dv * dot(n0, dp_du) - n0 * dot(dn0_dv, dp_du)) * inv_len;
+    ds_du = ds_du - s0 * dot(ds_du, s0);
+    ds_dv = ds_dv - s0 * dot(ds_dv, s0);
+    const f3 dt_du = cross(dn0_du, s0) + cross(n0, ds_du), dt_dv = cross(dn0_dv, s0) + cross(n0, ds_dv);
+    f3 nl, dl_du, dl_dv;
+    if (coarse) {
+        float mx, my, sa, sb, scv;
+        nm_top_lean(sc, mx, my, sa, sb, scv);
+        nl = mk(-mx, -my, 1.f);
+        dl_du = splat(0.f);
+        dl_dv = splat(0.f);
+    } else {
+        float2 du, dv;
+        const float2 sl = nm_slope0_d(sc, u, v, du, dv);
+        nl = mk(-sl.x, -sl.y, 1.f);
+        dl_du = mk(-du.x, -du.y, 0.f);
+        dl_dv = mk(-dv.x, -dv.y, 0.f);
+    }
+    f3 wn = s0 * nl.x + t0 * nl.y + n0 * nl.z;
+    const float il = 1.f / length(wn);
+    wn = wn * il;
+    f3 a = (s0 * dl_du.x + t0 * dl_du.y + n0 * dl_du.z + ds_du * nl.x + dt_du * nl.y + dn0_du * nl.z) * il;
+    f3 b = (s0 * dl_dv.x + t0 * dl_dv.y + n0 * dl_dv.z + ds_dv * nl.x + dt_dv * nl.y + dn0_dv * nl.z) * il;
+    n = wn;
+    dn_du = a - wn * dot(a, wn);
+    dn_dv = b - wn * dot(b, wn);
+}
+
+// kNM: apply the scene's normal map where the shape carries it (false: the
+// caller knows no normal-mapped shape is involved, and the check is compiled
+// away); nm_coarse: the two-stage solver's smoothed frame.
+template <bool kNM = true>
 SMS_HD void vertex_from_hit(const DevScene &sc, f3 o, f3 d, const Hit &h, Vtx &v,
-                                                SurfPt *si_out = nullptr) {
+                                                SurfPt *si_out = nullptr, bool nm_coarse = false) {
     const DevShape &s = sc.shapes[h.shape];
     SurfPt si;
     f3 dndu, dndv;
@@ -508,6 +628,8 @@ SMS_HD void vertex_from_hit(const DevScene &sc, f3 o, f3 d, const Hit &h, Vtx &v
     }
     v.p = si.p; v.dp_du = si.dp_du; v.dp_dv = si.dp_dv;
     v.n = si.shn; v.gn = si.n; v.dn_du = dndu; v.dn_dv = dndv;
+    if (kNM && h.shape == sc.nmap_shape && sc.nmap_res > 0 && s.nmap_frames)
+        nm_vertex_frame(sc, si.p, si.dp_du, si.shn, dndu, dndv, si.u, si.v, nm_coarse, v.n, v.dn_du, v.dn_dv);
     v.eta = s.spec_eta;
     v.shape = h.shape;
     if (dot(v.n, v.gn) < 0.f) v.gn = -v.gn;

@@ -157,7 +157,7 @@ SMS_D bool emitter_endpoint(const DevScene &sc, const Light &L, f3 p, f3 &yp, f3
         st.ray(h);
         if (h.shape < 0) return false;
         Vtx vy;
-        vertex_from_hit(sc, o, d, h, vy);
+        vertex_from_hit<false>(sc, o, d, h, vy);
         make_orthonormal(vy.dp_du, vy.dp_dv, vy.dn_du, vy.dn_dv);
         yp = vy.p; ydu = vy.dp_du; ydv = vy.dp_dv;
         return true;
@@ -188,21 +188,18 @@ SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
 // explicit seed point.  Returns ok; v holds the solution vertex.
 // kOffset: the caster is rough and `no` is its offset normal; without it the
 // constraint uses the vertex normal and `no` is ignored (compiled away).
-template <bool kOffset = false>
-SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
-                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr, f3 no_in = f3{0.f, 0.f, 1.f}) {
-    const f3 no = kOffset ? no_in : f3{0.f, 0.f, 1.f};
-    f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
-    Hit h;
-    trace(sc, x, d, kRayEps, INFINITY, false, h, err);
-    st.ray(h);
-    it = 0;
-    if (h.shape < 0) return false;
-    vertex_from_hit(sc, x, d, h, v);
-    if (p_init) *p_init = v.p;
-    if (h.shape != caster) return false;
+// newton_solver (manifold_ss.cpp:331-405) from the vertex v with offset normal
+// no; coarse: the two-stage solver's smoothed frames (smoothing = 1).  it
+// counts this solve's iterations; h is its ray-cast scratch.  On success v is
+// the accepted solution and, with kTrack, (h_acc, d_acc) the hit that
+// produced it; true = converged there and admissible
+// (reflection vs refraction, :391-402).
+template <bool kTrack, bool kNM>
+SMS_D bool ss_newton(const DevScene &sc, const SolverCfg &cfg, f3 x, f3 lp, Vtx &v, Hit &h, Hit &h_acc, f3 &d_acc,
+                     int &it, uint32_t &err, LaneStats &st, f3 no, bool coarse) {
     float beta = 1.f;
     bool accepted = false, conv = false;
+    it = 0;
     while (it < cfg.max_iterations) {
         float c0, c1, dx0, dx1;
         bool sok = cfg.halfvector ? step_halfvector(x, v, lp, c0, c1, dx0, dx1, no)
@@ -220,7 +217,11 @@ SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f
             continue;
         }
         beta = fminf(1.f, 2.f * beta);
-        vertex_from_hit(sc, x, dd, h, v);
+        vertex_from_hit<kNM>(sc, x, dd, h, v, nullptr, coarse);
+        if constexpr (kTrack) {
+            h_acc = h;
+            d_acc = dd;
+        }
         accepted = true;
     }
     // newton_solver returns si_current: valid only after an accepted step.
@@ -228,6 +229,62 @@ SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f
     f3 wx = normalize(x - v.p), wy = normalize(lp - v.p);
     bool refraction = dot(v.gn, wx) * dot(v.gn, wy) < 0.f;
     return (v.eta == 1.f) ? !refraction : refraction;
+}
+
+// sample_gaussian (manifold.h:326-345): a slope from N(mu, sigma) with sigma =
+// (a, c; c, b), through the standard normal of warp.h:184-190.
+SMS_D float2 sample_slope_gaussian(float mx, float my, float sa, float sb, float scv, float u0, float u1) {
+    const float r = sqrtf(-2.f * logf(1.f - u0));
+    float sp, cp;
+    sincosf(2.f * kPi * u1, &sp, &cp);
+    const float px = cp * r, py = sp * r;
+    const float sx = sqrtf(sa), sy = sqrtf(sb);
+    const float rho = scv / (sx * sy);
+    const float a = sqrtf(1.f + rho), b = sqrtf(1.f - rho);
+    const float d0 = 0.5f * a + 0.5f * b, d1 = 0.5f * a - 0.5f * b;
+    return make_float2((d0 * px + d1 * py) * sx + mx, (d1 * px + d0 * py) * sy + my);
+}
+
+// sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
+// explicit seed point.  kOffset: the caster is rough and `no` is its offset
+// normal (otherwise ignored and compiled away).  kTwoStage: the two-stage
+// solver on a normal-mapped caster (:253-270): first a solve on the smoothed
+// surface toward a slope drawn from the map's LEAN distribution (g0, g1 the
+// two numbers), then the solve on the full normal map from its solution.
+// Returns ok; v holds the solution vertex; it counts all iterations.
+// kNM: the caster may be normal-mapped (its manifold vertices read the map).
+template <bool kOffset = false, bool kTwoStage = false, bool kNM = false>
+SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
+                   uint32_t &err, LaneStats &st, f3 *p_init = nullptr, f3 no_in = f3{0.f, 0.f, 1.f}, float g0 = 0.f,
+                   float g1 = 0.f) {
+    const f3 no = kOffset ? no_in : f3{0.f, 0.f, 1.f};
+    f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
+    Hit h;
+    trace(sc, x, d, kRayEps, INFINITY, false, h, err);
+    st.ray(h);
+    it = 0;
+    if (h.shape < 0) return false;
+    vertex_from_hit<kNM>(sc, x, d, h, v, nullptr, kTwoStage);
+    if (p_init) *p_init = v.p;
+    if (h.shape != caster) return false;
+    if constexpr (kTwoStage) {
+        Hit h_acc = h;
+        f3 d_acc = d;
+        float mx, my, sa, sb, scv;
+        nm_top_lean(sc, mx, my, sa, sb, scv);
+        const float2 sl = sample_slope_gaussian(0.5f * (mx - no.x / no.z), 0.5f * (my - no.y / no.z), sa, sb, scv,
+                                                g0, g1);
+        const f3 ln = normalize(mk(-sl.x, -sl.y, 1.f));
+        int it1;
+        const bool ok1 = ss_newton<true, kNM>(sc, cfg, x, lp, v, h, h_acc, d_acc, it1, err, st, ln, true);
+        it = it1;
+        if (!ok1) return false;
+        vertex_from_hit<kNM>(sc, x, d_acc, h_acc, v, nullptr, false);   // ManifoldVertex(si_smooth, 0)
+    }
+    int it2;
+    const bool ok = ss_newton<false, kNM>(sc, cfg, x, lp, v, h, h, d, it2, err, st, no, false);
+    it += it2;
+    return ok;
 }
 
 // evaluate_path_contribution (manifold_ss.cpp:281-327) for a flat receiver.

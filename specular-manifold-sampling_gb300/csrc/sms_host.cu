@@ -280,7 +280,10 @@ extern "C" sms_status sms_scene_set_normalmap(sms_scene *s, int32_t shape, const
     s->nmap_res = res;
     s->nmap_tiles = tiles;
     s->nmap.assign(slopes, slopes + 2 * (size_t)res * res);
-    s->shapes[shape].flags |= SMS_SHAPE_GLINTY;
+    // a shape that is no caster / bouncer becomes glinty; a caster or bouncer
+    // keeps its role and its manifold vertices take the normal-mapped frame
+    const uint32_t chain = SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER;
+    if (!(s->shapes[shape].flags & chain)) s->shapes[shape].flags |= SMS_SHAPE_GLINTY;
     return SMS_OK;
 }
 
@@ -368,6 +371,8 @@ struct sms_ctx {
     // offset normals of rough shapes are built for the single-scatter
     // estimator only: rough multi-scatter chain shapes / glinty shapes
     bool ms_rough = false, glint_rough = false;
+    bool ms_nm = false;   // a multi-scatter chain shape carries the normal map
+    bool nm_rough = false;   // the normal-mapped shape is rough
     float *lean = nullptr;   // LEAN pyramid of the slope map (glints integrator), built on first use
 };
 
@@ -393,13 +398,13 @@ static SolverCfg solver_cfg(const sms_config &c) {
     s.uniqueness_threshold = c.uniqueness_threshold;
     s.step_scale = c.step_scale;
     s.mnee_init = c.mnee_init;
+    s.twostage = c.twostage;
     s.streams = nullptr;
     return s;
 }
 
 static sms_status validate_cfg(const sms_config *c) {
     if (!c) return fail(SMS_ERR_INVALID_ARG, "null config");
-    if (c->twostage) return fail(SMS_ERR_UNSUPPORTED, "twostage solver is not implemented");
     if (c->max_iterations < 0) return fail(SMS_ERR_INVALID_ARG, "max_iterations must be >= 0");
     return SMS_OK;
 }
@@ -468,9 +473,15 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         ds.k = h.bsdf.k;
         ds.albedo[0] = h.bsdf.albedo[0]; ds.albedo[1] = h.bsdf.albedo[1]; ds.albedo[2] = h.bsdf.albedo[2];
         ds.alpha = h.bsdf.type == SMS_BSDF_DIFFUSE ? 0.f : h.bsdf.alpha;
+        ds.nmap_frames = ((int)i == s->nmap_shape && s->nmap_res > 0 &&
+                          (h.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI |
+                                      SMS_SHAPE_CAUSTIC_BOUNCER))) ? 1 : 0;
         if (ds.alpha > 0.f && (h.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)))
             c->ms_rough = true;
         if (ds.alpha > 0.f && (h.flags & SMS_SHAPE_GLINTY)) c->glint_rough = true;
+        if (ds.nmap_frames && (h.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)))
+            c->ms_nm = true;
+        if ((int)i == s->nmap_shape && s->nmap_res > 0 && ds.alpha > 0.f) c->nm_rough = true;
         // manifold.h:94-96: real ior -> eta, complex or non-specular -> 1
         bool real_ior = h.bsdf.type == SMS_BSDF_DIELECTRIC ||
                         (h.bsdf.type == SMS_BSDF_CONDUCTOR && h.bsdf.k == 0.f);
@@ -538,6 +549,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         if (h.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) {
             if (d.n_casters_ss >= kMaxCasters) return fail(SMS_ERR_UNSUPPORTED, "too many casters");
             if (ds.alpha > 0.f) d.casters_ss_rough |= 1u << d.n_casters_ss;
+            if (ds.nmap_frames) d.casters_ss_nm |= 1u << d.n_casters_ss;
             d.casters_ss[d.n_casters_ss++] = (int)i;
         }
         if (h.flags & SMS_SHAPE_CAUSTIC_CASTER_MULTI) {
@@ -548,6 +560,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
     }
     std::vector<DevEmitter> em;
     d.glinty_shape = s->nmap_shape;
+    d.nmap_shape = s->nmap_res > 0 ? s->nmap_shape : -1;
     d.nmap_res = s->nmap_res;
     d.nmap_tiles = s->nmap_tiles;
     for (size_t i = 0; i < s->emitters.size(); ++i) {
@@ -760,6 +773,27 @@ static sms_status ensure_scratch(sms_ctx *c, uint32_t n, SsScratch &scr) {
     return SMS_OK;
 }
 
+// Normal-mapped single-scatter casters: the two-stage solver
+// (manifold_ss.cpp:253-270) draws its first slope from the map's LEAN
+// distribution, so it needs the pyramid, and every caster must carry the map
+// (on a caster without one the reference's lean() is zero and the sampled
+// slope is NaN: no walk converges).  A learned proposal seeds plain casters only.
+static sms_status check_ss_normalmap(sms_ctx *c) {
+    const uint32_t all = c->dsc.n_casters_ss >= 32 ? ~0u : ((1u << c->dsc.n_casters_ss) - 1u);
+    if (c->cfg.twostage) {
+        if (c->dsc.n_casters_ss > 0 && (c->dsc.casters_ss_nm & all) != all)
+            return fail(SMS_ERR_UNSUPPORTED, "the twostage solver needs every single-scatter caster normal-mapped");
+        if (c->dsc.n_casters_ss > 0)
+            if (sms_status st = ctx_build_lean(c)) return st;
+    }
+    mlp::SeedProposal pr{};
+    if (c->prop && proposal_seed_desc(c->prop, pr))
+        for (int k = 0; k < c->dsc.n_casters_ss; ++k)
+            if (c->dsc.casters_ss[k] == pr.shape && ((c->dsc.casters_ss_nm >> k) & 1u))
+                return fail(SMS_ERR_UNSUPPORTED, "a learned proposal cannot seed a normal-mapped caster");
+    return SMS_OK;
+}
+
 // Single-scatter connection of n device-resident queries; streams (may be
 // null) as SolverCfg::streams.
 sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
@@ -771,6 +805,7 @@ sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
         return fail(SMS_ERR_INVALID_ARG, "max_trials too large for the biased estimator");
     if (c->prop && c->cfg.biased)
         return fail(SMS_ERR_UNSUPPORTED, "a learned proposal seeds the unbiased estimator only");
+    if (sms_status st = check_ss_normalmap(c)) return st;
     CUDA_TRY(cudaSetDevice(c->device));
     SsScratch scr{};
     if (!c->cfg.biased)
@@ -880,8 +915,16 @@ extern "C" sms_status sms_ss_walk_batch(sms_ctx *c, int32_t caster, const float 
     if (!c || (n && (!q || !w || !out))) return fail(SMS_ERR_INVALID_ARG, "sms_ss_walk_batch: null argument");
     if (caster < 0 || caster >= c->dsc.n_shapes) return fail(SMS_ERR_INVALID_ARG, "unknown caster shape id");
     if (n == 0) return SMS_OK;
+    if (c->cfg.twostage) {
+        bool nm = false;
+        for (int k = 0; k < c->dsc.n_casters_ss; ++k)
+            nm |= c->dsc.casters_ss[k] == caster && ((c->dsc.casters_ss_nm >> k) & 1u);
+        if (!nm) return fail(SMS_ERR_UNSUPPORTED, "the twostage solver needs a normal-mapped single-scatter caster");
+        if (sms_status st = ctx_build_lean(c)) return st;
+    }
     CUDA_TRY(cudaSetDevice(c->device));
-    size_t qb = (size_t)SMS_QUERY_FIELDS * n * sizeof(float), wb = (size_t)SMS_WALK_IN_FIELDS * n * sizeof(float),
+    const int wrows = c->cfg.twostage ? SMS_SS_WALK_IN_FIELDS_TWOSTAGE : SMS_WALK_IN_FIELDS;
+    size_t qb = (size_t)SMS_QUERY_FIELDS * n * sizeof(float), wb = (size_t)wrows * n * sizeof(float),
            ob = (size_t)SMS_WALK_OUT_FIELDS * n * sizeof(float);
     if (sms_status st = ensure_io(c, qb + wb + ob)) return st;
     char *dbuf = reinterpret_cast<char *>(c->io);
@@ -920,6 +963,7 @@ bool ctx_view(sms_ctx *c, CtxView &out) {
     out.trial_group = c->trial_group;
     out.bounces = c->cfg.bounces;
     out.bsdf_strategy_only = c->cfg.bsdf_strategy_only;
+    out.nm_rough = c->nm_rough;
     out.sms_strategy_only = c->cfg.sms_strategy_only;
     return true;
 }
@@ -935,6 +979,7 @@ static sms_status check_ms_cfg(sms_ctx *c) {
         return fail(SMS_ERR_UNSUPPORTED, "bounces must be between 1 and 4");
     if (c->ms_rough)
         return fail(SMS_ERR_UNSUPPORTED, "rough (alpha > 0) multi-scatter chain shapes are not supported");
+    if (c->ms_nm) return fail(SMS_ERR_UNSUPPORTED, "normal-mapped multi-scatter chain shapes are not supported");
     return SMS_OK;
 }
 
@@ -1068,7 +1113,12 @@ extern "C" sms_status sms_glint_connect_batch_device(sms_ctx *c, const float *q,
 
 sms_status ctx_ensure_lean(sms_ctx *c) {
     if (sms_status st = check_glint_scene(c)) return st;
+    return ctx_build_lean(c);
+}
+
+sms_status ctx_build_lean(sms_ctx *c) {
     if (c->lean) return SMS_OK;
+    if (c->dsc.nmap_res == 0) return fail(SMS_ERR_INVALID_ARG, "the scene has no normal map (sms_scene_set_normalmap)");
     const uint32_t res = c->dsc.nmap_res;
     if (res & (res - 1)) return fail(SMS_ERR_UNSUPPORTED, "the LEAN pyramid needs a power-of-two slope map");
     int levels = 0;

@@ -28,6 +28,7 @@ struct SolverCfg {
     float uniqueness_threshold;
     float step_scale;
     int mnee_init;      // seed along the straight path (manifold_ss.cpp:229-241)
+    int twostage;       // two-stage solver on normal-mapped casters (manifold_ss.cpp:253-270)
     // Optional per-query random-number stream table: query i draws from stream
     // streams[i] instead of stream_off + i (the path tracer keys each query by
     // its path and bounce, so that results do not depend on which paths of a
@@ -70,6 +71,17 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
                               DevCounters *ctr, const SsScratch &scr, int num_sms, int blocks_per_sm,
                               PhaseTimer *tm, cudaStream_t s, const mlp::SeedProposal *prop = nullptr,
                               int trial_group = 0);
+// The proposal network for every query of a batch (ss_proposal_kernel).
+cudaError_t launch_ss_proposal(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
+                               uint64_t stream_off, const mlp::SeedProposal &pr, int num_sms, cudaStream_t s);
+// Normal-mapped caster variants (sms_ss_nm.cu), var = the caster variant bits.
+cudaError_t launch_ss_biased_nm(int var, const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n,
+                                uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
+                                DevCounters *ctr, int num_sms, int bps, PhaseTimer *tm, cudaStream_t s);
+cudaError_t launch_ss_caster_nm(int var, const DevScene &sc, const SolverCfg &cfg, int c, const float *q, uint32_t n,
+                                uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
+                                DevCounters *ctr, const SsScratch &scr, int num_sms, int bps, PhaseTimer *tm,
+                                cudaStream_t s, int trial_group);
 // Training pairs for a learned proposal (see ss_collect_kernel).
 cudaError_t launch_ss_collect(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q, uint32_t n,
                               uint64_t seed, uint64_t stream_off, int per_query, const mlp::SeedFrame &fr,
@@ -108,6 +120,7 @@ struct CtxView {
     int trial_group;                // lanes per query of the trial kernel (0: auto)
     int bounces;                    // multi-scatter chain length (sms_config::bounces)
     int bsdf_strategy_only, sms_strategy_only;   // glints MIS switches (sms_config)
+    bool nm_rough;                  // the normal-mapped shape is rough (alpha > 0)
 };
 
 }  // namespace sms
@@ -124,9 +137,11 @@ sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
                           const uint64_t *streams, sms_result *out);
 sms_status ctx_glint_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
                              const uint64_t *streams, sms_result *out);
-// Builds the LEAN pyramid of the context's slope map on first use (the
-// context's scene view then carries it).
+// Checks the glints scene, then builds the LEAN pyramid (ctx_build_lean).
 sms_status ctx_ensure_lean(sms_ctx *c);
+// Builds the LEAN pyramid of the scene's normal map on first use (the
+// context's scene view then carries it).
+sms_status ctx_build_lean(sms_ctx *c);
 // Reads and clears the device error flags of a context (synchronizes its
 // stream); SMS_ERR_DEVICE_LIMIT with the reasons when any was set.
 sms_status ctx_check_device_error(sms_ctx *c);

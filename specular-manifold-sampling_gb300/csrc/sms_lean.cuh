@@ -19,38 +19,6 @@ namespace sms {
 // (normalmap.cpp:36-40).
 constexpr float kLeanBaseSigma2 = 0.5f * 0.0001f * 0.0001f;
 
-SMS_HD float2 nm_texel(const DevScene &sc, uint32_t idx) {
-#ifdef __CUDA_ARCH__
-    uint32_t bits = __ldg(sc.nmap + idx);
-    __half2 h = *reinterpret_cast<__half2 *>(&bits);
-    return __half22float2(h);
-#else
-    (void)sc; (void)idx;
-    return make_float2(0.f, 0.f);
-#endif
-}
-
-// Bilinear slope at level 0 after the tiling wrap (normalmap.cpp:305-316).
-SMS_D float2 nm_slope0(const DevScene &sc, float u_in, float v_in) {
-    float u = u_in * sc.nmap_tiles, v = v_in * sc.nmap_tiles;
-    u -= floorf(u);
-    v -= floorf(v);
-    const uint32_t R = sc.nmap_res;
-    float res = (float)R, duv = 1.f / res;
-    float px = fminf(fmaxf((u - 0.5f * duv) * res, 0.f), res - 1.f);
-    float py = fminf(fmaxf((v - 0.5f * duv) * res, 0.f), res - 1.f);
-    uint32_t x0 = (uint32_t)floorf(px), y0 = (uint32_t)floorf(py);
-    uint32_t x1 = min(x0 + 1, R - 1), y1 = min(y0 + 1, R - 1);
-    x0 = min(x0, R - 1);
-    y0 = min(y0, R - 1);
-    float wx = px - (float)x0, wy = py - (float)y0;
-    float2 t00 = nm_texel(sc, y0 * R + x0), t10 = nm_texel(sc, y0 * R + x1), t01 = nm_texel(sc, y1 * R + x0),
-           t11 = nm_texel(sc, y1 * R + x1);
-    float w0x = 1.f - wx, w0y = 1.f - wy;
-    return make_float2(w0y * (w0x * t00.x + wx * t10.x) + wy * (w0x * t01.x + wx * t11.x),
-                       w0y * (w0x * t00.y + wx * t10.y) + wy * (w0x * t01.y + wx * t11.y));
-}
-
 // Footprint level (a footprint finer than one texel takes level 0).
 SMS_D int lean_level(const DevScene &sc, float dxu, float dxv, float dyu, float dyv) {
     const float t = sc.nmap_tiles;

@@ -71,7 +71,7 @@ SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool c
         if (h.shape < 0) return false;
         if (check_flags && !chain_shape(sc, h.shape)) return false;
         if (tmpl && h.shape != tmpl[b]) return false;
-        vertex_from_hit(sc, o, wo, h, c.v[b]);
+        vertex_from_hit<false>(sc, o, wo, h, c.v[b]);
         if (shapes) shapes[b] = h.shape;
         f3 wi = -wo;
         if (straight) {
@@ -337,7 +337,7 @@ SMS_D float chain_reflectance(const DevScene &sc, f3 x0, f3 lp, const Chain<K> &
         st.ray(h);
         if (h.shape < 0) return 0.f;
         Vtx hv;
-        vertex_from_hit(sc, o, d, h, hv);
+        vertex_from_hit<false>(sc, o, d, h, hv);
         f3 wo = k + 1 < K ? normalize(c.v[k + 1].p - hv.p) : normalize(lp - hv.p);
         val *= specular_reflectance(sc.shapes[h.shape], hv.n, wo);
         o = hv.p;

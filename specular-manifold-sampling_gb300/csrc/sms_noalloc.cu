@@ -67,6 +67,16 @@ extern "C" sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *qu
         return set_last_error(SMS_ERR_UNSUPPORTED,
                               "sms_ss_connect_batch_noalloc: a bound learned proposal needs per-query mixture "
                               "scratch; use sms_ss_connect_batch_device");
+    if (v.solver.twostage && v.scene->n_casters_ss > 0) {
+        const uint32_t all = v.scene->n_casters_ss >= 32 ? ~0u : ((1u << v.scene->n_casters_ss) - 1u);
+        if ((v.scene->casters_ss_nm & all) != all)
+            return set_last_error(SMS_ERR_UNSUPPORTED, "sms_ss_connect_batch_noalloc: the twostage solver needs "
+                                                       "every single-scatter caster normal-mapped");
+        if (!v.scene->lean)
+            return set_last_error(SMS_ERR_UNSUPPORTED, "sms_ss_connect_batch_noalloc: the twostage solver needs the "
+                                                       "LEAN pyramid, which the first sms_ss_connect_batch_device "
+                                                       "call builds");
+    }
     cudaError_t e = cudaSetDevice(v.device);
     if (e != cudaSuccess) return set_last_error(SMS_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     void *base = nullptr;

@@ -408,6 +408,25 @@ SMS_D bool bsdf_sample(const DevShape &s, f3 wi, float u1, float u2, float u3, B
     return true;
 }
 
+// NormalmapBSDF::sample (normalmap.cpp:118-135) around any smooth nested BSDF:
+// sampled in the frame of the level-0 slope normal at uv, the direction taken
+// back to the shading frame (fs, ft, n) and kept when it lies on the same side
+// of both frames' normals.
+SMS_D bool nm_bsdf_sample(const DevScene &sc, const DevShape &s, f3 fs, f3 ft, f3 n, f3 dp_du, float u, float v,
+                          f3 wi_w, float u1, float u2, float u3, BsdfSample &bs) {
+    const f3 bs0 = normalize(dp_du - n * dot(n, dp_du)), bt0 = cross(n, bs0);
+    const float2 sl = nm_slope0(sc, u, v);
+    const f3 pn = normalize(bs0 * -sl.x + bt0 * -sl.y + n);
+    const f3 ps = normalize(dp_du - pn * dot(pn, dp_du)), pt = cross(pn, ps);
+    const f3 wi = mk(dot(wi_w, ps), dot(wi_w, pt), dot(wi_w, pn));
+    if (!bsdf_sample(s, wi, u1, u2, u3, bs)) return false;
+    const f3 wo_w = ps * bs.wo.x + pt * bs.wo.y + pn * bs.wo.z;
+    const f3 wo = mk(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
+    if (!(bs.wo.z * wo.z > 0.f)) return false;
+    bs.wo = wo;
+    return true;
+}
+
 // Caustic single-scatter flag of emitter e (used by the MNEE check).
 SMS_D bool emitter_is_caustic_ss(const DevScene &sc, int e) {
     for (int k = 0; k < sc.n_emitters_ss; ++k)
@@ -620,15 +639,8 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             BsdfSample bs;
             bool ok;
             if (nmapped) {
-                // normal-mapped conductor at the hit's own uv
-                f3 wo_w;
-                float w;
-                ok = nm_conductor_sample(sc, s, n_sh, si.dp_du, si.u, si.v, wiw, wo_w, w);
-                bs.wo = mk(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n_sh));
-                bs.weight = splat(w);
-                bs.pdf = 1.f;
-                bs.eta = 1.f;
-                bs.delta = true;
+                // the normal-mapped BSDF at the hit's own uv
+                ok = nm_bsdf_sample(sc, s, fs, ft, n_sh, si.dp_du, si.u, si.v, wiw, u1, u2, u3, bs);
             } else {
                 ok = bsdf_sample(s, wi, u1, u2, u3, bs);
             }
@@ -665,7 +677,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                         Vtx v;
                         int it;
                         LaneStats st;
-                        bool found = ss_walk(sc, P.solver, shape, xp, ep, si.p, v, it, err, st);
+                        bool found = ss_walk<false, false, true>(sc, P.solver, shape, xp, ep, si.p, v, it, err, st);
                         if (found) {
                             f3 dpt = normalize(si.p - xp), dmn = normalize(v.p - xp);
                             found = fabsf(dot(dpt, dmn) - 1.f) < P.solver.uniqueness_threshold;
@@ -916,6 +928,11 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         // the footprint MIS needs the LEAN pyramid of the slope map
         if (sms_status est = ctx_ensure_lean(c)) return est;
     }
+    if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee &&
+        v.solver.twostage)
+        return rfail(SMS_ERR_UNSUPPORTED, "path_sms_ss: unbiased MNEE with the twostage solver is not supported");
+    if (v.nm_rough)
+        return rfail(SMS_ERR_UNSUPPORTED, "sms_render: a rough (alpha > 0) normal-mapped shape is not supported");
     if (opt->rr_depth <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: rr_depth must be positive");
     if (opt->max_depth < -1) return rfail(SMS_ERR_INVALID_ARG, "sms_render: max_depth must be -1 or >= 0");
     if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee)

@@ -257,6 +257,41 @@ def slab_config() -> SMSConfig:
     return SMSConfig(biased=True, max_trials=32, max_iterations=30, bounces=2)
 
 
+# -------------------------------------------------- normal-mapped caster
+def nm_plane_slopes(res: int = 256, amp: float = 0.15, freq: int = 1) -> np.ndarray:
+    """(res, res, 2) float16 slopes of a smooth periodic bump pattern (freq
+    periods of the base pattern across the map)."""
+    t = (np.arange(res) + 0.5) / res
+    vv, uu = np.meshgrid(t, t, indexing="ij")
+    sx = amp * np.sin(2 * np.pi * freq * (2 * uu + vv))
+    sy = (amp / 1.5) * np.cos(2 * np.pi * freq * (uu - 2 * vv))
+    return np.stack([sx, sy], axis=-1).astype(np.float16)
+
+
+def nm_plane_scene(conductor: bool = False, res: int = 256, alpha: float = 0.0, amp: float = 0.15,
+                   freq: int = 1) -> SceneDesc:
+    """The quad z = 1 over [-1, 1]^2 carrying a slope map (the normalmap BSDF
+    around a dielectric or conductor), flagged as a single-scatter caster.  The
+    point light sits above it (refraction down to the receiver z = 0) or, for
+    the conductor, below the receiver (reflection down to it)."""
+    d = SceneDesc()
+    P = np.array([[-1, -1, 1.0], [1, -1, 1.0], [1, 1, 1.0], [-1, 1, 1.0]], np.float32)
+    UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    F = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    b = Bsdf(BSDF_CONDUCTOR, 0.2, 3.0, alpha=alpha) if conductor else Bsdf(BSDF_DIELECTRIC, 1.5, alpha=alpha)
+    sid = d.add_mesh(P, F, b, SHAPE_CAUSTIC_CASTER_SINGLE, UV=UV)
+    d.normalmap = (sid, nm_plane_slopes(res, amp, freq), 1.0)
+    d.add_point_emitter((0.3, -0.2, -3.0) if conductor else (0.3, -0.2, 4.0), (100.0,) * 3,
+                        EMITTER_CAUSTIC_SINGLE)
+    return d
+
+
+def nm_plane_queries(n: int, seed: int = 9, extent: float = 0.8) -> np.ndarray:
+    """Receiver points (x, y, 0) uniform in [-extent, extent]^2."""
+    u = pcg32_streams_f32(seed, np.arange(n, dtype=np.uint64), 2)
+    return plane_queries(((u.T * 2.0 - 1.0) * extent).astype(np.float32))
+
+
 # ----------------------------------------------------------------- glints
 GLINT_QUERY_FIELDS = 21
 

@@ -221,8 +221,9 @@ def test_bad_arguments(sms, workloads, gpu_lib):
     q = W.sphere_queries(2)
     with pytest.raises(sms.SMSError):
         ss.sample_path(7, q, np.zeros((8, q.shape[1]), np.float32))
+    ctx.set_config(sms.SMSConfig(twostage=True))
     with pytest.raises(sms.SMSError):
-        ctx.set_config(sms.SMSConfig(twostage=True))
+        ss.specular_manifold_sampling(q)   # twostage on a caster without a normal map
     with pytest.raises(ValueError):
         ss.specular_manifold_sampling(np.zeros((15, 4), np.float32))
 

@@ -392,3 +392,127 @@ def test_mnee_init_ignores_the_random_seed(sms, workloads, oracle, conductor):
     if not conductor:
         # refraction: the straight line toward the light starts next to the solution
         assert outs[0][0].sum() > 10
+
+
+def _nm_plane(sms, conductor, res=256):
+    """Flat quad z = 1 with a smooth slope map (the reference's normalmap BSDF
+    around a dielectric / conductor) flagged as a single-scatter caster."""
+    d = sms.SceneDesc()
+    P = np.array([[-1, -1, 1.0], [1, -1, 1.0], [1, 1, 1.0], [-1, 1, 1.0]], np.float32)
+    UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    F = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    b = sms.Bsdf(sms.BSDF_CONDUCTOR, 0.2, 3.0) if conductor else sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)
+    sid = d.add_mesh(P, F, b, sms.SHAPE_CAUSTIC_CASTER_SINGLE, UV=UV)
+    t = (np.arange(res) + 0.5) / res
+    vv, uu = np.meshgrid(t, t, indexing="ij")
+    sl = np.stack([0.15 * np.sin(2 * np.pi * (2 * uu + vv)), 0.1 * np.cos(2 * np.pi * (uu - 2 * vv))], axis=-1)
+    d.normalmap = (sid, sl.astype(np.float16), 1.0)
+    d.add_point_emitter((0.3, -0.2, 4.0), (100.0, 100.0, 100.0))
+    return d
+
+
+@pytest.mark.parametrize("halfvector", [False, True])
+@pytest.mark.parametrize("conductor", [False, True])
+def test_newton_jacobian_on_a_normal_mapped_caster(sms, oracle, halfvector, conductor):
+    """Normal-mapped caster: the manifold vertex takes the normal-mapped frame
+    and its derivative (normalmap.cpp:236-290, the bilinear slope derivative
+    of normalmap.h:125-193).  Central differences of the constraint inside one
+    bilinear cell of the slope map match the Newton Jacobian."""
+    res = 256
+    desc = _nm_plane(sms, conductor, res)
+    osc = oracle.OracleScene(desc)
+    rng = np.random.default_rng(41 + 2 * halfvector + conductor)
+    lp = np.array([0.3, -0.2, 4.0], np.float32)
+    # the map is in effect: the constraint differs from the bare plane's
+    desc.normalmap = None
+    bare = oracle.OracleScene(desc)
+    x0 = np.array([0.2, 0.1, 0.0], np.float32)
+    assert not np.allclose(osc.step_at(0, halfvector, 0.37, 0.61, x0, lp)[1:3],
+                           bare.step_at(0, halfvector, 0.37, 0.61, x0, lp)[1:3], atol=1e-4)
+    h = 2e-4
+    checked = 0
+    for _ in range(100):
+        # cell centres of the bilinear interpolant sit at integer multiples of 1/res
+        i, j = rng.integers(4, res - 4, size=2)
+        u = (i + rng.uniform(-0.3, 0.3)) / res
+        v = (j + rng.uniform(-0.3, 0.3)) / res
+        if abs(u - v) < 0.01:
+            continue   # keep the differences inside one triangle
+        x = np.array([rng.uniform(-1, 1), rng.uniform(-1, 1), 0.0], np.float32)
+        c0 = osc.step_at(0, halfvector, u, v, x, lp)
+        if not c0[0]:
+            continue
+        J = c0[3:7].reshape(2, 2).astype(np.float64)
+        scale = max(1.0, np.abs(J).max())
+        cols = []
+        for du, dv in ((h, 0.0), (0.0, h)):
+            a = osc.step_at(0, halfvector, u + du, v + dv, x, lp)
+            bb = osc.step_at(0, halfvector, u - du, v - dv, x, lp)
+            cols.append((a[1:3].astype(np.float64) - bb[1:3]) / (2 * h) if a[0] and bb[0] else None)
+        if any(c is None for c in cols) or max(np.abs(c).max() for c in cols) > 1e3:
+            continue
+        fd = np.stack(cols, axis=1)
+        assert np.abs(J - fd).max() < 2e-2 * scale, (u, v, x.tolist(), J, fd)
+        checked += 1
+    assert checked >= 20
+
+
+def test_two_stage_slope_gaussian_moments(oracle):
+    """sample_gaussian (manifold.h:326-345): mean mu and covariance sigma for a
+    correlated sigma, through square_to_std_normal (warp.h:184-190)."""
+    from oracle import oracle as O
+    mu, a, b, c = np.array([0.1, -0.2], np.float32), 0.04, 0.01, 0.012
+    u = np.random.default_rng(5).random((20000, 2)).astype(np.float32)
+    s = np.array([O.sample_slope_gaussian(mu, a, b, c, x) for x in u])
+    assert np.allclose(s.mean(0), mu, atol=0.006)
+    cov = np.cov(s.T)
+    assert np.allclose(cov, [[a, c], [c, b]], rtol=0.06, atol=5e-4)
+
+
+@pytest.mark.parametrize("conductor,freq", [(False, 4), (True, 1)])
+def test_two_stage_solver_is_unbiased(sms, workloads, oracle, conductor, freq):
+    """The two-stage solver (manifold_ss.cpp:253-270) only changes where walks
+    start: the unbiased estimator gives the same expectation with and without
+    it on a normal-mapped caster, and it converges more often on the bumpier
+    map (its purpose)."""
+    W = workloads
+    osc = oracle.OracleScene(W.nm_plane_scene(conductor=conductor, freq=freq))
+    q = W.nm_plane_queries(4096)
+    res = {}
+    for two in (False, True):
+        cfg = sms.SMSConfig(biased=False, max_trials=-1, twostage=two)
+        m, succ = [], 0.0
+        for r in range(8):
+            v, c, w, st = osc.connect_batch(cfg, q, seed=200 + r)
+            m.append(float(v[0].mean()))
+            succ += st["solver_succeeded"] / st["walks"]
+        res[two] = (np.mean(m), np.std(m, ddof=1) / np.sqrt(len(m)), succ / 8)
+    (a, sa, pa), (b, sb, pb) = res[False], res[True]
+    assert a > 0.05
+    assert abs(a - b) < 4.0 * np.hypot(sa, sb) + 0.02 * a, res
+    assert pb > pa, res
+
+
+def test_two_stage_walk_inputs(sms, workloads, oracle):
+    """With twostage the per-walk harness takes two more rows (the smoothed
+    solve's slope sample); the same walk with different slope samples can end
+    on different solutions, and more walks converge than without it."""
+    W = workloads
+    osc = oracle.OracleScene(W.nm_plane_scene(freq=4))
+    cfg = sms.SMSConfig(twostage=True)
+    q = W.nm_plane_queries(256)
+    w = np.zeros((10, 256), np.float32)
+    w[0:3] = np.array([0.3, -0.2, 4.0], np.float32)[:, None]
+    u = W.pcg32_streams_f32(3, np.arange(256, dtype=np.uint64), 4)
+    w[6:10] = u
+    with pytest.raises(ValueError):
+        osc.walk_batch(cfg, 0, q, w[:8])
+    a = osc.walk_batch(cfg, 0, q, w)
+    w2 = w.copy()
+    w2[8:10] = 1.0 - w[8:10]
+    b = osc.walk_batch(cfg, 0, q, w2)
+    assert a[0].mean() > 0.05
+    both = (a[0] > 0.5) & (b[0] > 0.5)
+    assert np.any(np.linalg.norm(a[2:5, both] - b[2:5, both], axis=0) > 1e-3)
+    plain = osc.walk_batch(sms.SMSConfig(), 0, q, w[:8])
+    assert a[0].mean() > plain[0].mean()

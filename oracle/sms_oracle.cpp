@@ -1047,13 +1047,24 @@ static float roughdielectric_eval(float alpha, float eta_, V3 wi, V3 wo) {
 }
 /* manifold_ss.cpp:648-669: a rough BSDF's value in the half-vector domain;
  * wi toward the shading point, wo toward the light (world space). */
+/* On a normal-mapped shape, NormalmapBSDF::eval (normalmap.cpp:172-181)
+ * evaluates the nested BSDF in the perturbed frame and keeps wo only on the
+ * same side of the perturbed and the unperturbed normal; the half-vector
+ * factor flips eta by the side of wi in the unperturbed frame (si.wi). */
 static float specular_reflectance_rough(const Scene &sc, const SI &si, V3 wi_w, V3 wo_w) {
     const sms_bsdf &b = sc.shapes[si.shape].bsdf;
+    const bool nm = nm_frames(sc, si.shape);
     V3 n = si.shn;
+    if (nm) {
+        MVertex v;
+        vertex_from_si(sc, si, v);
+        n = v.n;
+    }
     V3 fs = normalize(si.dp_du - n * dot(n, si.dp_du));
     V3 ft = cross(n, fs);
     V3 wi(dot(wi_w, fs), dot(wi_w, ft), dot(wi_w, n));
     V3 wo(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
+    if (nm && !(dot(wo_w, si.shn) * wo.z > 0.f)) return 0.f;
     if (b.type == SMS_BSDF_CONDUCTOR && b.k != 0.f) {
         float f = roughconductor_eval(b.alpha, b.eta, b.k, wi, wo);
         V3 h = normalize(wi + wo);
@@ -1062,7 +1073,7 @@ static float specular_reflectance_rough(const Scene &sc, const SI &si, V3 wi_w, 
     float f = b.type == SMS_BSDF_CONDUCTOR ? roughconductor_eval(b.alpha, b.eta, b.k, wi, wo)
                                            : roughdielectric_eval(b.alpha, b.eta, wi, wo);
     float eta = b.eta;
-    if (wi.z < 0.f) eta = 1.f / eta;
+    if ((nm ? dot(wi_w, si.shn) : wi.z) < 0.f) eta = 1.f / eta;
     V3 h = -normalize(wi + wo * eta);
     float a = dot(wi, h) + eta * dot(wo, h);
     return f * a * a / (eta * eta * std::fabs(dot(wo, h)));

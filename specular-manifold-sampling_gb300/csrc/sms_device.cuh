@@ -489,6 +489,7 @@ SMS_HD void mesh_dn(const MeshTri &m, int has_normals, f3 p, f3 &dndu, f3 &dndv)
 // dp_du and dn_du/dn_dv only where the half-vector constraint needs it.
 struct Vtx {
     f3 p, dp_du, dp_dv, n, dn_du, dn_dv, gn;
+    f3 n0;   // shading normal before the normal map (n where there is none)
     float eta;
     int shape;
 };
@@ -628,6 +629,7 @@ SMS_HD void vertex_from_hit(const DevScene &sc, f3 o, f3 d, const Hit &h, Vtx &v
     }
     v.p = si.p; v.dp_du = si.dp_du; v.dp_dv = si.dp_dv;
     v.n = si.shn; v.gn = si.n; v.dn_du = dndu; v.dn_dv = dndv;
+    v.n0 = si.shn;
     if (kNM && h.shape == sc.nmap_shape && sc.nmap_res > 0 && s.nmap_frames)
         nm_vertex_frame(sc, si.p, si.dp_du, si.shn, dndu, dndv, si.u, si.v, nm_coarse, v.n, v.dn_du, v.dn_dv);
     v.eta = s.spec_eta;
@@ -933,12 +935,19 @@ SMS_HD float specular_reflectance(const DevShape &s, f3 shn, f3 wo) {
 // specular_reflectance of a rough BSDF (manifold_ss.cpp:648-669): the BSDF
 // value for wi (toward the shading point) and wo (toward the light) in the
 // shading frame (n, tangent from dp_du), turned into the half-vector domain.
-SMS_HD float specular_reflectance_rough(const DevShape &s, f3 n, f3 dp_du, f3 wi_w, f3 wo_w) {
+// nm: the shape carries the normal map, n is its perturbed normal and n0 the
+// shading normal under it -- NormalmapBSDF::eval (normalmap.cpp:172-181)
+// evaluates the nested BSDF in the perturbed frame and keeps wo only on the
+// same side of both normals, while the half-vector factor flips eta by the
+// side of wi in the unperturbed frame.
+SMS_HD float specular_reflectance_rough(const DevShape &s, f3 n, f3 dp_du, f3 wi_w, f3 wo_w, f3 n0 = f3{0.f, 0.f, 0.f},
+                                        bool nm = false) {
     f3 fs = dp_du - n * dot(n, dp_du);
     fs = normalize(fs);
     f3 ft = cross(n, fs);
     f3 wi = mk(dot(wi_w, fs), dot(wi_w, ft), dot(wi_w, n));
     f3 wo = mk(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
+    if (nm && !(dot(wo_w, n0) * wo.z > 0.f)) return 0.f;
     const bool complex_ior = s.bsdf_type == kBsdfConductor && s.k != 0.f;
     if (complex_ior) {
         float f = roughconductor_eval(s.alpha, s.eta, s.k, wi, wo);
@@ -948,7 +957,7 @@ SMS_HD float specular_reflectance_rough(const DevShape &s, f3 n, f3 dp_du, f3 wi
     float f = s.bsdf_type == kBsdfConductor ? roughconductor_eval(s.alpha, s.eta, s.k, wi, wo)
                                             : roughdielectric_eval(s.alpha, s.eta, wi, wo);
     float eta = s.eta;
-    if (wi.z < 0.f) eta = 1.f / eta;
+    if ((nm ? dot(wi_w, n0) : wi.z) < 0.f) eta = 1.f / eta;
     f3 h = -normalize(wi + wo * eta);
     float a = dot(wi, h) + eta * dot(wo, h);
     return f * a * a / (eta * eta * fabsf(dot(wo, h)));

@@ -287,14 +287,18 @@ SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f
     return ok;
 }
 
-// evaluate_path_contribution (manifold_ss.cpp:281-327) for a flat receiver.
+// evaluate_path_contribution (manifold_ss.cpp:281-327) for a flat receiver;
+// kNM: the caster may carry the normal map.
+template <bool kNM = false>
 SMS_D f3 contribution(const DevScene &sc, f3 x, const Light &L, const Vtx &sol, uint32_t &err, LaneStats &st) {
     Vtx vt = sol;
     make_orthonormal(vt.dp_du, vt.dp_dv, vt.dn_du, vt.dn_dv);
     f3 yp, ydu, ydv, lw, lp;
     if (!emitter_endpoint(sc, L, vt.p, yp, ydu, ydv, lw, lp, err, st)) return splat(0.f);
     const DevShape &sh = sc.shapes[vt.shape];
-    float F = sh.alpha > 0.f ? specular_reflectance_rough(sh, vt.n, vt.dp_du, normalize(x - vt.p), normalize(lp - vt.p))
+    const bool nm = kNM && vt.shape == sc.nmap_shape && sh.nmap_frames;
+    float F = sh.alpha > 0.f ? specular_reflectance_rough(sh, vt.n, vt.dp_du, normalize(x - vt.p), normalize(lp - vt.p),
+                                                          vt.n0, nm)
                              : specular_reflectance(sh, vt.n, normalize(lp - vt.p));
     F *= geometric_term(x, vt, yp, ydu, ydv);
     return lw * F;

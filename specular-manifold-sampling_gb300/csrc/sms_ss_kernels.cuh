@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
                             dir = normalize(v.p - Q.x);
                             // evaluated for every visible solution; only first
                             // occurrences are kept below
-                            contrib = diffuse_eval(Q, dir) * contribution(sc, Q.x, L, v, err, st);
+                            contrib = diffuse_eval(Q, dir) * contribution<kNM>(sc, Q.x, L, v, err, st);
                         }
                     } else {
                         st.fail++;
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
                 st.succ++;
                 if (visible(sc, L.p, v.p, err, st)) {
                     f3 dir = normalize(v.p - Q.x);
-                    f3 spec = contribution(sc, Q.x, L, v, err, st);
+                    f3 spec = contribution<kNM>(sc, Q.x, L, v, err, st);
                     // the caster's estimate is divided by the offset density (manifold_ss.cpp:199)
                     f3 val = kRough ? diffuse_eval(Q, dir) * spec * (1.f / p_off) : diffuse_eval(Q, dir) * spec;
                     scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;

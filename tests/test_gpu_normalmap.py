@@ -95,7 +95,7 @@ def test_normal_mapped_connect(sms, workloads, oracle, gpu_lib, biased, twostage
     q = W.nm_plane_queries(4096)
     vg, cg, wg = sms.SpecularManifoldSingleScatter(ctx).specular_manifold_sampling(q, seed=3)
     vo, co, wo, st_o = oracle.OracleScene(desc).connect_batch(cfg, q, seed=3)
-    vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=3)
+    vf, cf, wf, st_f = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=3)
     g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
     f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
     print(f"nm connect biased={biased} twostage={twostage} alpha={alpha}: count mismatch {g_cm:.4f} differs "
@@ -105,7 +105,9 @@ def test_normal_mapped_connect(sms, workloads, oracle, gpu_lib, biased, twostage
     assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
     assert g_med < 1e-3
     st = ctx.stats()
-    assert abs(st["walks"] - st_o["walks"]) <= 0.02 * st_o["walks"] + 16
+    # total walks: the queries whose outcome flips under rounding carry their
+    # own trial counts, so the yardstick is again the oracle builds' difference
+    assert abs(st["walks"] - st_o["walks"]) <= 3 * abs(st_f["walks"] - st_o["walks"]) + 0.02 * st_o["walks"] + 16
     ctx.close()
 
 

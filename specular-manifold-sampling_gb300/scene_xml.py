@@ -15,7 +15,10 @@ silently half-loaded):
       (spheres: translate and uniform scale only);
       nested <bsdf>: dielectric (int_ior / ext_ior, names from
       include/mitsuba/render/ior.h), conductor (eta, k), diffuse (reflectance),
-      roughdielectric / roughconductor (isotropic Beckmann alpha);
+      roughdielectric / roughconductor (isotropic Beckmann alpha),
+      normalmap around any of these (filename of an OpenEXR or PNG RGB normal
+      map, tiles; src/bsdfs/normalmap.cpp:24-58; one normal-mapped shape per
+      scene); a top-level <bsdf id="..."> referenced by <ref id="..."/>;
       no bsdf -> diffuse (shape.cpp:73-74);
       nested <emitter type="area"> with radiance (spheres only)
   <emitter type="point">  position (point), intensity (spectrum / rgb / float)
@@ -154,17 +157,54 @@ def _transform(el):
     return M
 
 
-def _bsdf(sms, el):
+def _bsdf_nm(sms, el, refs, base):
+    """(Bsdf, normal map or None) of a <bsdf> element; the normal map is
+    (float16 slopes (res, res, 2), tiles) of a normalmap BSDF."""
+    if el is not None and el.get("type") == "normalmap":
+        p = _props(el)
+        if not _bool(p, "use_slopes", True):
+            raise ValueError("normalmap with use_slopes = false is not supported")
+        if _bool(p, "lean_fallback"):
+            raise ValueError("normalmap lean_fallback is not supported")
+        if "filename" not in p:
+            raise ValueError("normalmap without a filename")
+        from .image_io import normalmap_slopes
+        inner = [c for c in el if c.tag in ("bsdf", "ref")]
+        if len(inner) != 1:
+            raise ValueError("normalmap needs exactly one nested bsdf")
+        b, nm = _bsdf_nm(sms, _deref(inner[0], refs), refs, base)
+        if nm is not None:
+            raise ValueError("nested normal maps are not supported")
+        return b, (normalmap_slopes(base / p["filename"][1].get("value")), _float(p, "tiles", 1.0))
+    return _bsdf(sms, el, refs), None
+
+
+def _deref(el, refs):
+    if el is not None and el.tag == "ref":
+        rid = el.get("id")
+        if rid not in refs:
+            raise ValueError(f"unknown bsdf reference '{rid}'")
+        return refs[rid]
+    return el
+
+
+def _bsdf(sms, el, refs=None):
+    el = _deref(el, refs or {})
     if el is None:
         return sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5, 0.5, 0.5))
     t = el.get("type")
     p = _props(el)
+    if t == "normalmap":
+        raise ValueError("a normalmap bsdf is only supported directly on a shape")
     if t == "twosided":
-        inner = [c for c in el if c.tag == "bsdf"]
-        return _bsdf(sms, inner[0] if inner else None)
+        inner = [c for c in el if c.tag in ("bsdf", "ref")]
+        return _bsdf(sms, inner[0] if inner else None, refs)
     if t == "dielectric":
         # dielectric.cpp:177-186: eta = int_ior / ext_ior, defaults bk7 / air
         return sms.Bsdf(sms.BSDF_DIELECTRIC, _float(p, "int_ior", 1.5046) / _float(p, "ext_ior", 1.000277))
+    if t in ("conductor", "roughconductor") and p.get("material", (None, None))[1] is not None:
+        if p["material"][1].get("value", "none").lower() != "none":
+            raise ValueError("named conductor materials are not supported; give eta and k")
     if t == "conductor":
         eta, k = _spectrum(p, "eta", (0.0,) * 3), _spectrum(p, "k", (1.0,) * 3)
         return sms.Bsdf(sms.BSDF_CONDUCTOR, float(np.mean(eta)), float(np.mean(k)))
@@ -213,6 +253,7 @@ def load_scene_xml(sms, path):
         raise ValueError("not a <scene> document")
     desc = sms.SceneDesc()
     config, itype = None, None
+    refs = {c.get("id"): c for c in root if c.tag == "bsdf" and c.get("id") is not None}
     for el in root:
         if el.tag in _IGNORED:
             continue
@@ -220,7 +261,9 @@ def load_scene_xml(sms, path):
             config, itype = sms.SMSConfig.from_xml(ET.tostring(el, encoding="unicode"))
             continue
         if el.tag == "bsdf":
-            raise ValueError("top-level <bsdf> references are not supported; nest the bsdf in its shape")
+            if el.get("id") is None:
+                raise ValueError("a top-level <bsdf> needs an id")
+            continue
         p = _props(el)
         if el.tag == "emitter":
             if el.get("type") != "point":
@@ -231,11 +274,11 @@ def load_scene_xml(sms, path):
         if el.tag != "shape":
             raise ValueError(f"unsupported element <{el.tag}>")
         t = el.get("type")
-        bsdf_el = next((c for c in el if c.tag == "bsdf"), None)
+        bsdf_el = next((c for c in el if c.tag in ("bsdf", "ref")), None)
         tr_el = next((c for c in el if c.tag == "transform" and c.get("name") == "to_world"), None)
         M = _transform(tr_el) if tr_el is not None else np.eye(4)
         flags = _flags(sms, p)
-        b = _bsdf(sms, bsdf_el)
+        b, nm = _bsdf_nm(sms, _deref(bsdf_el, refs), refs, path.parent)
         if t == "sphere":
             c = np.array(_point(p, "center", (0.0, 0.0, 0.0)), np.float64)
             r = _float(p, "radius", 1.0)
@@ -264,6 +307,10 @@ def load_scene_xml(sms, path):
             sid = desc.add_mesh(P, F, b, flags, N=N, UV=UV)
         else:
             raise ValueError(f"unsupported shape type '{t}'")
+        if nm is not None:
+            if desc.normalmap is not None:
+                raise ValueError("more than one normal-mapped shape (one normal map per scene)")
+            desc.normalmap = (sid, nm[0], nm[1])
         for em in (c for c in el if c.tag == "emitter"):
             if em.get("type") != "area":
                 raise ValueError("only area emitters may be nested in a shape")

@@ -518,6 +518,12 @@ typedef struct sms_camera {
 #define SMS_INTEGRATOR_PATH_SMS_SS     1
 #define SMS_INTEGRATOR_PATH_SMS_MS     2
 #define SMS_INTEGRATOR_PATH_SMS_GLINTS 3   /* src/integrators/path_sms_glints.cpp:62-194 */
+/* Plain path tracing restricted to the light paths path_sms_ss / path_sms_ms
+ * account for (the paper's equal-time comparisons): src/integrators/
+ * path_filtered_ss.cpp:36-181 and path_filtered_ms.cpp:36-206 (chain length
+ * = the context's cfg.bounces). */
+#define SMS_INTEGRATOR_PATH_FILTERED_SS 4
+#define SMS_INTEGRATOR_PATH_FILTERED_MS 5
 typedef struct sms_render_options {
     int32_t  integrator;                 /* SMS_INTEGRATOR_*                        */
     int32_t  max_depth;                  /* -1 = unbounded                          */

@@ -48,7 +48,8 @@ class _RenderOptions(C.Structure):
                 ("glint_diff_scale_factor_clamp", C.c_float)]
 
 
-_INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3}
+_INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
+                "path_filtered_ms": 5}
 _FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 

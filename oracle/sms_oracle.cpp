@@ -2264,7 +2264,12 @@ static V3 pt_cosine_hemisphere(float u1, float u2) {
     return V3(px, py, safe_sqrt(1.f - px * px - py * py));
 }
 
-struct PtBsdf { V3 wo, weight; float pdf = 0.f, eta = 1.f; bool delta = false; };
+struct PtBsdf {
+    V3 wo, weight;
+    float pdf = 0.f, eta = 1.f;
+    bool delta = false;
+    bool transmit = false;   /* BSDFFlags::Transmission of the sampled lobe */
+};
 
 /* density of pt_rough_sample for (wi, wo): D(m) cos(theta_m) x the Jacobian
  * of reflection / refraction (roughconductor.cpp / roughdielectric.cpp pdf
@@ -2530,6 +2535,7 @@ static bool nm_bsdf_sample(const NormalMap &m, const sms_bsdf &b, V3 fs, V3 ft, 
     nm_frame(m, n, dp_du, uv, pn, ps, pt);
     const V3 wi(dot(wi_w, ps), dot(wi_w, pt), dot(wi_w, pn));
     if (!pt_bsdf_sample(b, wi, u1, u2, u3, bs)) return false;
+    bs.transmit = bs.wo.z * wi.z < 0.f;
     const V3 wo_w = ps * bs.wo.x + pt * bs.wo.y + pn * bs.wo.z;
     const V3 wo(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
     if (!(bs.wo.z * wo.z > 0.f)) return false;
@@ -2593,7 +2599,11 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
     bool spec_cam = true, prev_receiver = false;
     V3 prev_p;
     const int integ = opt.integrator;
-    const int bounces = integ == SMS_INTEGRATOR_PATH_SMS_MS ? cfg.bounces : 1;
+    const bool filtered_ss = integ == SMS_INTEGRATOR_PATH_FILTERED_SS, filtered_ms = integ == SMS_INTEGRATOR_PATH_FILTERED_MS;
+    const int bounces = (integ == SMS_INTEGRATOR_PATH_SMS_MS || filtered_ms) ? cfg.bounces : 1;
+    /* PathRecord of path_filtered_ms.cpp:219-301 (state 0 default, 1 receiver,
+       2 caster, 3 emitter; chain bounce count), after the camera ray */
+    int rec = (si.valid() && (sc.shapes[si.shape].flags & SMS_SHAPE_CAUSTIC_RECEIVER)) ? 1 : 0, rec_b = 0;
     for (int depth = 1;; ++depth) {
         if (!si.valid()) break;
         if (depth > opt.rr_depth) {
@@ -2611,8 +2621,15 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         const bool receiver = (s.flags & SMS_SHAPE_CAUSTIC_RECEIVER) != 0;
         bool on_caster = false;
         if (integ == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) != 0;
-        else if (integ == SMS_INTEGRATOR_PATH_SMS_MS)
+        else if (integ == SMS_INTEGRATOR_PATH_SMS_MS || filtered_ms)
             on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
+        else if (filtered_ss)
+            on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI)) != 0;
+        const bool glint_case = depth == 1 && !opt.disable_reflected_emitters;
+        /* path_filtered_ss.cpp:109-110; light_connection_valid (path_filtered_ms.cpp:240-242) */
+        const bool valid_conn = filtered_ss ? on_caster && (prev_receiver || glint_case)
+                                            : filtered_ms && rec == 2 && rec_b == bounces;
+        const float caustic_eta = bsdf_eta(s.bsdf);
         const bool diffuse = s.bsdf.type == SMS_BSDF_DIFFUSE;
         /* the glinty shape carries a normal-mapped conductor (delta reflection) */
         const bool nmapped = si.shape == sc.glinty_shape && sc.nmap.res > 0;
@@ -2680,7 +2697,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         }
         V3 albedo(s.bsdf.albedo[0], s.bsdf.albedo[1], s.bsdf.albedo[2]);
         /* SMS at a receiver (path_sms_ss.cpp:115-121, path_sms_ms.cpp:226-232) */
-        if (integ != SMS_INTEGRATOR_PATH && receiver && !on_caster && diffuse &&
+        if (integ != SMS_INTEGRATOR_PATH && !filtered_ss && !filtered_ms && receiver && !on_caster && diffuse &&
             (opt.max_depth < 0 || depth + bounces < opt.max_depth)) {
             Query q;
             q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
@@ -2694,6 +2711,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         /* emitter sampling */
         bool nee = smooth && !on_caster && !on_glinty;
         if (integ == SMS_INTEGRATOR_PATH_SMS_SS) nee = nee || (depth == 1 && !opt.disable_reflected_emitters);
+        if (filtered_ss || filtered_ms) nee = smooth && (!on_caster || valid_conn);
         if (nee) {
             float ex = rng.next_f32(), ey = rng.next_f32();
             PtDir ds;
@@ -2705,6 +2723,11 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                     V3 bv = pt_bsdf_eval(s.bsdf, wi, wo);
                     if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
                         float w = ds.delta ? 1.f : mis_weight(ds.pdf, pt_bsdf_pdf(s.bsdf, wi, wo));
+                        /* path_filtered_ss.cpp:127-142 / path_filtered_ms.cpp:137-150 */
+                        if (valid_conn && (filtered_ms || depth > 1)) {
+                            const bool refraction = wo.z * wi.z < 0.f;
+                            if (caustic_eta == 1.f ? refraction : !refraction) w = 0.f;
+                        }
                         L += thr * bv * ds.spec * w;
                     }
                 }
@@ -2716,7 +2739,10 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         if (nmapped) {
             /* the normal-mapped BSDF at the hit's own uv */
             if (!nm_bsdf_sample(sc.nmap, s.bsdf, fs, ft, n_sh, si.dp_du, si.uv, wiw, u1, u2, u3, bs)) break;
-        } else if (!pt_bsdf_sample(s.bsdf, wi, u1, u2, u3, bs)) break;
+        } else {
+            if (!pt_bsdf_sample(s.bsdf, wi, u1, u2, u3, bs)) break;
+            bs.transmit = bs.wo.z * wi.z < 0.f;
+        }
         thr = thr * bs.weight;
         eta *= bs.eta;
         if (!bs.delta) spec_cam = false;
@@ -2725,6 +2751,25 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         nr.o = si.p; nr.d = fs * bs.wo.x + ft * bs.wo.y + n_sh * bs.wo.z;
         nr.mint = kRayEps * (1.f + hmax_abs(si.p)); nr.maxt = kInf;
         SI si2 = ray_intersect(sc, nr);
+        if (filtered_ms) {
+            /* PathRecord::state_transition (path_filtered_ms.cpp:244-300) */
+            const bool nv = si2.valid();
+            const uint32_t nf = nv ? sc.shapes[si2.shape].flags : 0u;
+            if (nv && (nf & SMS_SHAPE_CAUSTIC_RECEIVER)) { rec = 1; rec_b = 0; }
+            else if (rec == 1) {
+                if (nv && (nf & SMS_SHAPE_CAUSTIC_CASTER_MULTI)) { rec = 2; rec_b = 1; }
+                else { rec = 0; rec_b = 0; }
+            } else if (rec == 2) {
+                if (rec_b < bounces && nv && (nf & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER))) {
+                    if (caustic_eta == 1.f ? bs.transmit : !bs.transmit) { rec = 0; rec_b = 0; }
+                    else rec_b++;
+                } else if (rec_b == bounces && nv && sc.shapes[si2.shape].emitter >= 0 &&
+                           std::find(sc.emitters_ms.begin(), sc.emitters_ms.end(), sc.shapes[si2.shape].emitter) !=
+                               sc.emitters_ms.end()) {
+                    rec = 3;
+                } else { rec = 0; rec_b = 0; }
+            } else { rec = 0; rec_b = 0; }
+        }
         if (si2.valid() && sc.shapes[si2.shape].emitter >= 0) {
             const Shape &es = sc.shapes[si2.shape];
             V3 ep = nr.o + nr.d * si2.t;
@@ -2733,6 +2778,10 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             if (integ == SMS_INTEGRATOR_PATH_SMS_SS) allow = !on_caster || (depth == 1 && !opt.disable_reflected_emitters);
             else if (integ == SMS_INTEGRATOR_PATH_SMS_MS) allow = !on_caster || spec_cam;
             else if (integ == SMS_INTEGRATOR_PATH_SMS_GLINTS) allow = !on_glinty;
+            else if (filtered_ss)   /* path_filtered_ss.cpp:166-172 */
+                allow = !on_caster || (prev_receiver && (caustic_eta == 1.f ? !bs.transmit : bs.transmit)) || glint_case;
+            else if (filtered_ms)   /* light_hit_valid (path_filtered_ms.cpp:191) */
+                allow = !on_caster || (rec == 3 && rec_b == bounces) || spec_cam;
             if (allow) {
                 float epdf = bs.delta ? 0.f : pt_emitter_pdf(sc, es, si.p, ep, nr.d, si2.t);
                 L += thr * Le * mis_weight(bs.pdf, epdf);

@@ -50,7 +50,8 @@ PROPOSAL_FEATURES = 9
 PROPOSAL_OUTPUTS = 40
 PROPOSAL_PARAMS = 21808
 
-INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3}
+INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
+               "path_filtered_ms": 5}
 FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device limit",

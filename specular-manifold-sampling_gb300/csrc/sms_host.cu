@@ -95,7 +95,7 @@ extern "C" sms_status sms_config_parse_xml(const char *xml, sms_config *cfg, cha
     if (!attr(itag, "type", type)) return fail(SMS_ERR_PARSE, "<integrator> without type");
     sms_config c;
     sms_config_default(&c);
-    if (type == "path_sms_ms") c.bounces = 2;
+    if (type == "path_sms_ms" || type == "path_filtered_ms") c.bounces = 2;   // path_sms_ms.cpp:152, path_filtered_ms.cpp:58
     size_t end = s.find("</integrator>", ie);
     if (end == std::string::npos) end = s.size();
     size_t pos = ie + 1;

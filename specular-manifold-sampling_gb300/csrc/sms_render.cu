@@ -51,8 +51,11 @@ constexpr int kPtHardDepth = 4096;        // bounce limit of an unbounded path
 constexpr int kQueryRowsMax = 21;        // glint queries; single / multi scatter use 16
 constexpr int kStageRows = 24;            // query rows, then 3 throughput rows at 21..23
 
-// path flags
+// path flags; bits 3-4 and 5-7 hold the multi-bounce filter's path record
+// (path_filtered_ms.cpp:219-301): its state and chain bounce count
 constexpr int kAlive = 1, kPrevReceiver = 2, kSpecularCamera = 4;
+constexpr int kRecShift = 3, kRecBounceShift = 5;
+constexpr int kRecDefault = 0, kRecReceiver = 1, kRecCaster = 2, kRecEmitter = 3;
 
 struct PtCam {
     float m[12];          // rows 0..2 of camera-to-world
@@ -290,6 +293,7 @@ struct BsdfSample {
     f3 wo, weight;
     float pdf, eta;
     bool delta;
+    bool transmit;   // BSDFFlags::Transmission of the sampled lobe
 };
 
 // Density of rough_sample below for the pair (wi, wo): microfacet normal m of
@@ -420,6 +424,7 @@ SMS_D bool nm_bsdf_sample(const DevScene &sc, const DevShape &s, f3 fs, f3 ft, f
     const f3 ps = normalize(dp_du - pn * dot(pn, dp_du)), pt = cross(pn, ps);
     const f3 wi = mk(dot(wi_w, ps), dot(wi_w, pt), dot(wi_w, pn));
     if (!bsdf_sample(s, wi, u1, u2, u3, bs)) return false;
+    bs.transmit = bs.wo.z * wi.z < 0.f;
     const f3 wo_w = ps * bs.wo.x + pt * bs.wo.y + pn * bs.wo.z;
     const f3 wo = mk(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
     if (!(bs.wo.z * wo.z > 0.f)) return false;
@@ -431,6 +436,12 @@ SMS_D bool nm_bsdf_sample(const DevScene &sc, const DevShape &s, f3 fs, f3 ft, f
 SMS_D bool emitter_is_caustic_ss(const DevScene &sc, int e) {
     for (int k = 0; k < sc.n_emitters_ss; ++k)
         if (sc.emitters_ss[k] == e) return true;
+    return false;
+}
+
+SMS_D bool emitter_is_caustic_ms(const DevScene &sc, int e) {
+    for (int k = 0; k < sc.n_emitters_ms; ++k)
+        if (sc.emitters_ms[k] == e) return true;
     return false;
 }
 
@@ -482,7 +493,10 @@ __global__ void __launch_bounds__(kPtBlock) pt_camera_kernel(DevScene sc, PtCam 
     S.eta[i] = 1.f;
     S.hit_t[i] = h.t; S.hit_u[i] = h.u; S.hit_v[i] = h.v;
     S.hit_shape[i] = h.shape; S.hit_prim[i] = h.prim;
-    S.flags[i] = (h.shape >= 0 ? kAlive : 0) | kSpecularCamera;
+    // path record of the multi-bounce filter after the camera ray
+    // (state_transition(si, si, ...) of path_filtered_ms.cpp:79)
+    const int rec = (h.shape >= 0 && (sc.shapes[h.shape].flags & kShapeFlagReceiver)) ? kRecReceiver : kRecDefault;
+    S.flags[i] = (h.shape >= 0 ? kAlive : 0) | kSpecularCamera | (rec << kRecShift);
     S.cam_s[i] = sx;
     S.cam_s[(size_t)S.cap + i] = sy;
     store_rng(S, i, rng);
@@ -543,8 +557,20 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             const bool receiver = (s.flags & kShapeFlagReceiver) != 0;
             bool on_caster = false;
             if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & kShapeFlagCasterSingle) != 0;
-            else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS)
+            else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS || P.integrator == SMS_INTEGRATOR_PATH_FILTERED_MS)
                 on_caster = (s.flags & (kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
+            else if (P.integrator == SMS_INTEGRATOR_PATH_FILTERED_SS)
+                on_caster = (s.flags & (kShapeFlagCasterSingle | kShapeFlagCasterMulti)) != 0;
+            const bool filtered_ss = P.integrator == SMS_INTEGRATOR_PATH_FILTERED_SS;
+            const bool filtered_ms = P.integrator == SMS_INTEGRATOR_PATH_FILTERED_MS;
+            const bool filtered = filtered_ss || filtered_ms;
+            const bool glint_case = depth == 1 && !P.disable_reflected_emitters;
+            int rec = (flags >> kRecShift) & 3, rec_b = (flags >> kRecBounceShift) & 7;
+            // the connection the SMS estimators would have made from here
+            // (path_filtered_ss.cpp:109-110; light_connection_valid,
+            // path_filtered_ms.cpp:240-242)
+            const bool valid_conn = filtered_ss ? on_caster && ((flags & kPrevReceiver) || glint_case)
+                                                : filtered_ms && rec == kRecCaster && rec_b == P.bounces;
             const bool diffuse = s.bsdf_type == kBsdfDiffuse;
             // the glinty shape carries a normal-mapped conductor (delta reflection)
             const bool nmapped = shape == sc.glinty_shape && sc.nmap_res > 0;
@@ -600,7 +626,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                 }
             }
             // ---- SMS query of a receiver vertex (solved after this launch)
-            if (P.integrator != SMS_INTEGRATOR_PATH && receiver && !on_caster && diffuse &&
+            if (P.integrator != SMS_INTEGRATOR_PATH && !filtered && receiver && !on_caster && diffuse &&
                 (P.max_depth < 0 || depth + P.bounces < P.max_depth)) {
                 const float row[SMS_QUERY_FIELDS] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
                                                      si.dp_du.x, si.dp_du.y, si.dp_du.z,
@@ -617,6 +643,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             bool nee = smooth && !on_caster && !on_glinty;
             if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS)
                 nee = nee || (depth == 1 && !P.disable_reflected_emitters);
+            if (filtered) nee = smooth && (!on_caster || valid_conn);
             if (nee) {
                 float ux = rng.next_f32(), uy = rng.next_f32();
                 DirSample ds;
@@ -629,6 +656,13 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                         const f3 bv = bsdf_eval(s, wi, wo);
                         if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
                             float w = ds.delta ? 1.f : mis_weight(ds.pdf, bsdf_pdf(s, wi, wo));
+                            // a filtered caustic connection must scatter the way
+                            // SMS solves it: reflection on conductors, refraction
+                            // on dielectrics (path_filtered_ss.cpp:127-142)
+                            if (valid_conn && (filtered_ms || depth > 1)) {
+                                const bool refraction = wo.z * wi.z < 0.f;
+                                if (s.spec_eta == 1.f ? refraction : !refraction) w = 0.f;
+                            }
                             L = L + thr * bv * ds.spec * w;
                         }
                     }
@@ -643,6 +677,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                 ok = nm_bsdf_sample(sc, s, fs, ft, n_sh, si.dp_du, si.u, si.v, wiw, u1, u2, u3, bs);
             } else {
                 ok = bsdf_sample(s, wi, u1, u2, u3, bs);
+                bs.transmit = bs.wo.z * wi.z < 0.f;
             }
             if (ok) {
                 thr = thr * bs.weight;
@@ -655,6 +690,31 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                 f3 d2 = fs * bs.wo.x + ft * bs.wo.y + n_sh * bs.wo.z;
                 Hit h2;
                 trace(sc, si.p, d2, kRayEps * (1.f + max_abs(si.p)), INFINITY, false, h2, err);
+                if (filtered_ms) {
+                    // PathRecord::state_transition (path_filtered_ms.cpp:244-300)
+                    const bool nv = h2.shape >= 0;
+                    const uint32_t nf = nv ? sc.shapes[h2.shape].flags : 0u;
+                    if (nv && (nf & kShapeFlagReceiver)) {
+                        rec = kRecReceiver; rec_b = 0;
+                    } else if (rec == kRecReceiver) {
+                        if (nv && (nf & kShapeFlagCasterMulti)) { rec = kRecCaster; rec_b = 1; }
+                        else { rec = kRecDefault; rec_b = 0; }
+                    } else if (rec == kRecCaster) {
+                        if (rec_b < P.bounces && nv && (nf & (kShapeFlagCasterMulti | kShapeFlagBouncer))) {
+                            // the chain continues only with the scattering SMS solves
+                            if (s.spec_eta == 1.f ? bs.transmit : !bs.transmit) { rec = kRecDefault; rec_b = 0; }
+                            else rec_b++;
+                        } else if (rec_b == P.bounces && nv && sc.shapes[h2.shape].emitter >= 0 &&
+                                   emitter_is_caustic_ms(sc, sc.shapes[h2.shape].emitter)) {
+                            rec = kRecEmitter;
+                        } else {
+                            rec = kRecDefault; rec_b = 0;
+                        }
+                    } else {
+                        rec = kRecDefault; rec_b = 0;
+                    }
+                    flags = (flags & ~(0x1F << kRecShift)) | (rec << kRecShift) | (rec_b << kRecBounceShift);
+                }
                 if (h2.shape >= 0 && sc.shapes[h2.shape].emitter >= 0) {
                     const DevShape &es = sc.shapes[h2.shape];
                     const f3 ep = si.p + d2 * h2.t;
@@ -666,6 +726,11 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                         allow = !on_caster || (flags & kSpecularCamera);
                     else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS)
                         allow = !on_glinty;
+                    else if (filtered_ss)   // path_filtered_ss.cpp:166-172
+                        allow = !on_caster || ((flags & kPrevReceiver) && (s.spec_eta == 1.f ? !bs.transmit : bs.transmit)) ||
+                                glint_case;
+                    else if (filtered_ms)   // light_hit_valid, path_filtered_ms.cpp:191
+                        allow = !on_caster || (rec == kRecEmitter && rec_b == P.bounces) || (flags & kSpecularCamera);
                     if (allow) {
                         float epdf = bs.delta ? 0.f : emitter_pdf(sc, es, si.p, ep, d2, h2.t);
                         L = L + thr * Le * mis_weight(bs.pdf, epdf);
@@ -921,7 +986,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     std::string why;
     if (!camera_params(cam, pc, why)) return rfail(SMS_ERR_INVALID_ARG, "sms_render: " + why);
     if (opt->spp <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: spp must be positive");
-    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_SMS_GLINTS)
+    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_FILTERED_MS)
         return rfail(SMS_ERR_INVALID_ARG, "sms_render: unknown integrator");
     const bool glints = opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS;
     if (glints) {
@@ -935,6 +1000,8 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         return rfail(SMS_ERR_UNSUPPORTED, "sms_render: a rough (alpha > 0) normal-mapped shape is not supported");
     if (opt->rr_depth <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: rr_depth must be positive");
     if (opt->max_depth < -1) return rfail(SMS_ERR_INVALID_ARG, "sms_render: max_depth must be -1 or >= 0");
+    if (opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS && (v.bounces < 1 || v.bounces > kMaxBounces))
+        return rfail(SMS_ERR_UNSUPPORTED, "path_filtered_ms: bounces must be between 1 and 4");
     if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee)
         return rfail(SMS_ERR_UNSUPPORTED, "path_sms_ms: unbiased MNEE (mnee_init without biased_mnee) is not "
                                           "implemented");
@@ -944,7 +1011,8 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     P.rr_depth = opt->rr_depth;
     P.disable_reflected_emitters = opt->disable_reflected_emitters;
     P.biased_mnee = opt->biased_mnee;
-    P.bounces = opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS ? v.bounces : 1;
+    P.bounces = (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS || opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS)
+                    ? v.bounces : 1;
     P.mnee_check = opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee;
     P.seed = opt->seed;
     P.solver = v.solver;

@@ -34,7 +34,7 @@ load_render_setup reads the rendering side of the same file:
       <transform name="to_world"> (lookat / translate / scale / rotate / matrix),
       <film> width, height (hdrfilm defaults 768 x 576), <sampler> sample_count
       (independent sampler default 4)   (src/sensors/perspective.cpp)
-  <integrator type="path|path_sms_ss|path_sms_ms">  max_depth, rr_depth
+  <integrator type="path|path_sms_ss|path_sms_ms|path_filtered_ss|path_filtered_ms">  max_depth, rr_depth
       (src/librender/integrator.cpp:300-320), disable_reflected_emitters,
       biased_mnee (path_sms_ss.cpp:59-60)
 and returns (Camera, RenderOptions).
@@ -55,7 +55,7 @@ IOR = {"vacuum": 1.0, "helium": 1.000036, "hydrogen": 1.000132, "air": 1.000277,
        "amber": 1.55, "pet": 1.5750, "diamond": 2.419}
 
 _IGNORED = {"sensor", "film", "sampler", "default"}
-_INTEGRATOR_TYPES = {"path", "path_sms_ss", "path_sms_ms"}
+_INTEGRATOR_TYPES = {"path", "path_sms_ss", "path_sms_ms", "path_filtered_ss", "path_filtered_ms"}
 
 
 def _props(el):

@@ -81,15 +81,16 @@ def test_render_is_deterministic_and_wavefront_invariant(sms, workloads, gpu_lib
     ctx.close()
 
 
-def _compare_integrators(sms, ctx, cam, integ, spp_path, spp_sms, reps, block=4, rel=0.02):
-    """Plain path tracing vs integrator `integ` on 4x4-pixel blocks: the
-    difference of the means must lie within 5 standard errors (from the
-    spread of `reps` independent runs) plus `rel` of the value."""
+def _compare_integrators(sms, ctx, cam, integ, spp_path, spp_sms, reps, block=4, rel=0.02, base="path"):
+    """Integrator `base` (plain path tracing by default) vs integrator `integ`
+    on 4x4-pixel blocks: the difference of the means must lie within 5
+    standard errors (from the spread of `reps` independent runs) plus `rel` of
+    the value."""
     runs = {}
-    for name, spp in (("path", spp_path), (integ, spp_sms)):
+    for name, spp in ((base, spp_path), (integ, spp_sms)):
         runs[name] = np.stack([_blocks(ctx.render(cam, sms.RenderOptions(integrator=name, spp=spp, seed=900 + r)),
                                        block) for r in range(reps)])
-    a, b = runs["path"], runs[integ]
+    a, b = runs[base], runs[integ]
     se = np.sqrt(a.var(0, ddof=1) / reps + b.var(0, ddof=1) / reps)
     diff = np.abs(a.mean(0) - b.mean(0))
     assert np.all(diff < 5.0 * se + rel * a.mean(0) + 1e-3), (a.mean(0), b.mean(0), se)
@@ -118,6 +119,23 @@ def test_unbiased_mnee_is_unbiased_against_path(sms, workloads, gpu_lib):
     ctx.close()
 
 
+def _slab_desc(sms, W):
+    """Flat glass slab (caster_multi top sheet z = 1.3, bouncer bottom sheet
+    z = 1) over the diffuse floor, sphere light above (caustic_emitter_multi)."""
+    d = sms.SceneDesc()
+    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
+    d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3),
+               sms.SHAPE_CAUSTIC_RECEIVER, UV=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
+    glass = sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)
+    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.3, [])
+    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.0, [], flip_normals=True)
+    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_BOUNCER, N=N, UV=UV)
+    light = d.add_sphere((0.0, 0.0, 4.0), 0.5, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+    d.add_area_emitter(light, (40.0,) * 3, sms.EMITTER_CAUSTIC_MULTI)
+    return d
+
+
 def test_path_sms_ms_matches_path_on_flat_slab(sms, workloads, gpu_lib):
     """Two-bounce chains through a flat glass slab over the floor: path_sms_ms
     (bounces = 2, unbiased, half-vector constraints) against plain path
@@ -130,18 +148,8 @@ def test_path_sms_ms_matches_path_on_flat_slab(sms, workloads, gpu_lib):
     tolerance.  With the light straight above, the angle-difference
     constraints sit at their pole: walks rarely converge and the unbiased
     estimate, while still unbiased, is too heavy-tailed for a 4-run test."""
-    d = sms.SceneDesc()
-    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
-    d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3),
-               sms.SHAPE_CAUSTIC_RECEIVER, UV=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
     W = workloads
-    glass = sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)
-    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.3, [])
-    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
-    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.0, [], flip_normals=True)
-    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_BOUNCER, N=N, UV=UV)
-    light = d.add_sphere((0.0, 0.0, 4.0), 0.5, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
-    d.add_area_emitter(light, (40.0,) * 3, sms.EMITTER_CAUSTIC_MULTI)
+    d = _slab_desc(sms, W)
     cfg = sms.SMSConfig(biased=False, max_trials=-1, bounces=2, halfvector_constraints=True)
     ctx = sms.Context(sms.Scene(d), cfg)
     cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 32, 32)
@@ -219,3 +227,44 @@ def test_glints_integrator_matches_oracle(sms, workloads, oracle, gpu_lib, biase
                                     sms.RenderOptions(integrator="path_sms_glints", spp=4, seed=7))
     assert (o[..., 0] > 0).mean() > 0.005
     assert abs(g.mean() - o.mean()) <= 3.0 * abs(f.mean() - o.mean()) + 0.02 * o.mean()
+
+
+@pytest.mark.parametrize("integrator", ["path_filtered_ss", "path_filtered_ms"])
+def test_filtered_integrators_match_oracle(sms, workloads, oracle, gpu_lib, integrator):
+    """path_filtered_ss / path_filtered_ms (plain path tracing restricted to
+    the paths the SMS integrators account for) on the GPU against the oracle,
+    against the oracle-vs-FMA floor."""
+    W = workloads
+    if integrator == "path_filtered_ss":
+        desc, cfg, cam = W.pool_scene(res=32), W.water_config(), W.pool_camera(16, 16)
+    else:
+        desc = _slab_desc(sms, W)
+        cfg = sms.SMSConfig(bounces=2)
+        cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 16, 16)
+    g, o, f = _check_against_oracle(sms, oracle, desc, cfg, cam, sms.RenderOptions(integrator=integrator, spp=8,
+                                                                                   seed=21))
+    assert o.mean() > 0.0
+
+
+def test_path_filtered_ss_matches_path_sms_ss(sms, workloads, gpu_lib):
+    """Flat water: path_filtered_ss finds by BSDF and emitter sampling exactly
+    the light paths unbiased path_sms_ss accounts for (path_filtered_ss.cpp:
+    27-35), so the two estimate the same image."""
+    W = workloads
+    cfg = W.water_config()
+    cfg.max_trials = -1
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=32, wave_scale=0.0)), cfg)
+    _compare_integrators(sms, ctx, W.pool_camera(32, 32), "path_sms_ss", 4096, 512, 4, base="path_filtered_ss")
+    ctx.close()
+
+
+def test_path_filtered_ms_matches_path_sms_ms(sms, workloads, gpu_lib):
+    """The flat slab seen from under it: path_filtered_ms (its path record
+    keeps exactly the receiver -> caster -> bouncer -> light chains of
+    path_filtered_ms.cpp:219-301) against unbiased path_sms_ms."""
+    W = workloads
+    cfg = sms.SMSConfig(biased=False, max_trials=-1, bounces=2, halfvector_constraints=True)
+    ctx = sms.Context(sms.Scene(_slab_desc(sms, W)), cfg)
+    cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 32, 32)
+    _compare_integrators(sms, ctx, cam, "path_sms_ms", 4096, 512, 4, base="path_filtered_ms")
+    ctx.close()

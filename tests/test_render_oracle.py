@@ -151,3 +151,43 @@ def test_glints_integrator_oracle(sms, workloads, O):
     cfg.bsdf_strategy_only = True
     c = osc.render(cfg, cam, opt)
     assert c.max() == 0.0
+
+
+def test_filtered_integrators_without_flags_equal_path(sms, workloads, O):
+    """Without caustic flags the filtered path tracers filter nothing and draw
+    the same random numbers as path: the same image."""
+    W = workloads
+    d = sms.SceneDesc()
+    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
+    d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3))
+    P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.0, W.water_params())
+    d.add_mesh(P, F, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.33), 0, N=N, UV=UV)
+    light = d.add_sphere((0.0, 0.0, 4.0), 0.5, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+    d.add_area_emitter(light, (40.0,) * 3, 0)
+    osc = O.OracleScene(d)
+    cam = W.pool_camera(8, 8)
+    a = osc.render(W.water_config(), cam, sms.RenderOptions(integrator="path", spp=4, seed=3, rr_depth=100))
+    for integ in ("path_filtered_ss", "path_filtered_ms"):
+        b = osc.render(sms.SMSConfig(bounces=2), cam, sms.RenderOptions(integrator=integ, spp=4, seed=3, rr_depth=100))
+        assert np.array_equal(a, b), integ
+    assert a.mean() > 0.0
+
+
+def test_path_filtered_ss_matches_path_sms_ss_on_flat_water(sms, workloads, O):
+    """The oracle's path_filtered_ss and unbiased path_sms_ss estimate the
+    same image (path_filtered_ss.cpp:27-35) on flat water; plain path tracing
+    also carries the caustics reflected off the water, which both filter."""
+    W = workloads
+    osc = O.OracleScene(W.pool_scene(res=16, wave_scale=0.0))
+    cam = W.pool_camera(12, 12)
+    cfg = W.water_config()
+    cfg.max_trials = -1
+    runs = {}
+    for integ, spp in (("path_filtered_ss", 2048), ("path_sms_ss", 256)):
+        runs[integ] = np.stack([_blocks(osc.render(cfg, cam, sms.RenderOptions(integrator=integ, spp=spp,
+                                                                                seed=70 + r)), 3)
+                                for r in range(4)])
+    a, b = runs["path_filtered_ss"], runs["path_sms_ss"]
+    se = np.sqrt(a.var(0, ddof=1) / 4 + b.var(0, ddof=1) / 4)
+    assert np.all(np.abs(a.mean(0) - b.mean(0)) < 5.0 * se + 0.01 * a.mean(0) + 1e-3), (a.mean(0), b.mean(0), se)
+    assert abs(a.mean() - b.mean()) < 0.03 * a.mean()

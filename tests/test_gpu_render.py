@@ -119,18 +119,22 @@ def test_unbiased_mnee_is_unbiased_against_path(sms, workloads, gpu_lib):
     ctx.close()
 
 
-def _slab_desc(sms, W):
+def _slab_desc(sms, W, caster_below=False):
     """Flat glass slab (caster_multi top sheet z = 1.3, bouncer bottom sheet
-    z = 1) over the diffuse floor, sphere light above (caustic_emitter_multi)."""
+    z = 1, or the other way round) over the diffuse floor, sphere light above
+    (caustic_emitter_multi)."""
     d = sms.SceneDesc()
     fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
     d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3),
                sms.SHAPE_CAUSTIC_RECEIVER, UV=np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
     glass = sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)
+    top, bottom = sms.SHAPE_CAUSTIC_CASTER_MULTI, sms.SHAPE_CAUSTIC_BOUNCER
+    if caster_below:
+        top, bottom = bottom, top
     P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.3, [])
-    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    d.add_mesh(P, F, glass, top, N=N, UV=UV)
     P, N, UV, F = W.heightfield_mesh(16, 1.0, 1.0, [], flip_normals=True)
-    d.add_mesh(P, F, glass, sms.SHAPE_CAUSTIC_BOUNCER, N=N, UV=UV)
+    d.add_mesh(P, F, glass, bottom, N=N, UV=UV)
     light = d.add_sphere((0.0, 0.0, 4.0), 0.5, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
     d.add_area_emitter(light, (40.0,) * 3, sms.EMITTER_CAUSTIC_MULTI)
     return d
@@ -238,7 +242,7 @@ def test_filtered_integrators_match_oracle(sms, workloads, oracle, gpu_lib, inte
     if integrator == "path_filtered_ss":
         desc, cfg, cam = W.pool_scene(res=32), W.water_config(), W.pool_camera(16, 16)
     else:
-        desc = _slab_desc(sms, W)
+        desc = _slab_desc(sms, W, caster_below=True)
         cfg = sms.SMSConfig(bounces=2)
         cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 16, 16)
     g, o, f = _check_against_oracle(sms, oracle, desc, cfg, cam, sms.RenderOptions(integrator=integrator, spp=8,
@@ -261,10 +265,13 @@ def test_path_filtered_ss_matches_path_sms_ss(sms, workloads, gpu_lib):
 def test_path_filtered_ms_matches_path_sms_ms(sms, workloads, gpu_lib):
     """The flat slab seen from under it: path_filtered_ms (its path record
     keeps exactly the receiver -> caster -> bouncer -> light chains of
-    path_filtered_ms.cpp:219-301) against unbiased path_sms_ms."""
+    path_filtered_ms.cpp:219-301) against unbiased path_sms_ms.  The record
+    wants the first specular vertex after the receiver to be a
+    caustic_caster_multi shape, so the caster is the slab's lower sheet here
+    (path_sms_ms's seed paths may start on either, manifold_ms.cpp:351)."""
     W = workloads
     cfg = sms.SMSConfig(biased=False, max_trials=-1, bounces=2, halfvector_constraints=True)
-    ctx = sms.Context(sms.Scene(_slab_desc(sms, W)), cfg)
+    ctx = sms.Context(sms.Scene(_slab_desc(sms, W, caster_below=True)), cfg)
     cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 32, 32)
     _compare_integrators(sms, ctx, cam, "path_sms_ms", 4096, 512, 4, base="path_filtered_ms")
     ctx.close()

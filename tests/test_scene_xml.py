@@ -155,6 +155,12 @@ def test_render_setup_from_xml(sms, workloads, tmp_path):
     path.write_text(RENDER_XML.replace('type="path_sms_ss"', 'type="bdpt"'))
     with pytest.raises(ValueError):
         sms.load_render_setup(path)
+    # the filtered comparison integrators; path_filtered_ms defaults to 2 bounces
+    path.write_text(RENDER_XML.replace('type="path_sms_ss"', 'type="path_filtered_ms"'))
+    cam, opt = sms.load_render_setup(path)
+    assert opt.integrator == "path_filtered_ms"
+    _, cfg, kind = sms.load_scene(path)
+    assert kind == "path_filtered_ms" and cfg.bounces == 2
 
 
 def test_rough_bsdfs_from_xml(sms, tmp_path):

@@ -536,8 +536,20 @@ typedef struct sms_render_options {
     float    glint_diff_scale_factor_clamp; /* 0: ray differentials of the camera are
                                            scaled by max(1/sqrt(spp), this)
                                            (src/librender/integrator.cpp:41,164-165) */
+    uint32_t samples_per_pass;           /* 0 = spp; spp must be a multiple of it
+                                            (integrator.cpp:35,61-68)              */
+    float    timeout;                    /* seconds, <= 0: none.  Passes of
+                                            samples_per_pass spp are rendered until
+                                            the time is up; the image is the mean
+                                            of the passes done (integrator.cpp:36,
+                                            143-146: the reference stops at the
+                                            block, here at the pass) */
 } sms_render_options;
 void sms_render_options_default(sms_render_options *opt);
+
+/* Samples per pixel of the context's last render (spp, or fewer after a
+ * timeout). */
+uint32_t sms_render_spp_done(const sms_ctx *ctx);
 
 /* State seed of the SMS streams (SplitMix64 of the seed). */
 uint64_t sms_render_sms_seed(uint64_t seed);

@@ -45,7 +45,8 @@ class _RenderOptions(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
                 ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
                 ("seed", C.c_uint64), ("max_paths", C.c_uint32),
-                ("glint_diff_scale_factor_clamp", C.c_float)]
+                ("glint_diff_scale_factor_clamp", C.c_float), ("samples_per_pass", C.c_uint32),
+                ("timeout", C.c_float)]
 
 
 _INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,

@@ -109,7 +109,8 @@ class _RenderOptions(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
                 ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
                 ("seed", C.c_uint64), ("max_paths", C.c_uint32),
-                ("glint_diff_scale_factor_clamp", C.c_float)]
+                ("glint_diff_scale_factor_clamp", C.c_float), ("samples_per_pass", C.c_uint32),
+                ("timeout", C.c_float)]
 
 
 class _Profile(C.Structure):
@@ -180,6 +181,7 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_render_options_default": (None, [C.POINTER(_RenderOptions)]),
         "sms_render_sms_seed": (u64, [u64]),
         "sms_render": (i32, [vp, C.POINTER(_Camera), C.POINTER(_RenderOptions), vp]),
+        "sms_render_spp_done": (u32, [vp]),
         "sms_render_device": (i32, [vp, C.POINTER(_Camera), C.POINTER(_RenderOptions), vp]),
     }
     for name, (res, args) in sig.items():
@@ -440,6 +442,10 @@ class Context:
         _check(_LIB.sms_render(self._h, C.byref(camera.to_c()), C.byref(options.to_c()), _ptr(img)))
         return img
 
+    def render_spp_done(self) -> int:
+        """Samples per pixel of the last render (fewer than spp after a timeout)."""
+        return int(_LIB.sms_render_spp_done(self._h))
+
     def render_device(self, camera: "Camera", options: "RenderOptions", image_ptr: int):
         """Render into a device buffer of height * width * 3 floats."""
         _check(_LIB.sms_render_device(self._h, C.byref(camera.to_c()), C.byref(options.to_c()), image_ptr))
@@ -625,6 +631,8 @@ class RenderOptions:
     seed: int = 0
     max_paths: int = 0
     glint_diff_scale_factor_clamp: float = 0.0
+    samples_per_pass: int = 0         # 0 = spp (integrator.cpp:35)
+    timeout: float = -1.0             # seconds, <= 0: none (integrator.cpp:36)
 
     def to_c(self) -> _RenderOptions:
         o = _RenderOptions()
@@ -634,6 +642,7 @@ class RenderOptions:
         o.biased_mnee = int(self.biased_mnee)
         o.seed, o.max_paths = self.seed, self.max_paths
         o.glint_diff_scale_factor_clamp = self.glint_diff_scale_factor_clamp
+        o.samples_per_pass, o.timeout = self.samples_per_pass, self.timeout
         return o
 
 

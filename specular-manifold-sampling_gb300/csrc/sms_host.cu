@@ -372,6 +372,7 @@ struct sms_ctx {
     // estimator only: rough multi-scatter chain shapes / glinty shapes
     bool ms_rough = false, glint_rough = false;
     bool ms_nm = false;   // a multi-scatter chain shape carries the normal map
+    uint32_t render_spp = 0;   // samples per pixel of the last render
     bool nm_rough = false;   // the normal-mapped shape is rough
     float *lean = nullptr;   // LEAN pyramid of the slope map (glints integrator), built on first use
 };
@@ -1110,6 +1111,12 @@ extern "C" sms_status sms_glint_connect_batch_device(sms_ctx *c, const float *q,
                                                      uint64_t stream_off, sms_result *out) {
     return ctx_glint_connect(c, q, n, seed, stream_off, nullptr, out);
 }
+
+void ctx_set_render_spp(sms_ctx *c, uint32_t spp) {
+    if (c) c->render_spp = spp;
+}
+
+extern "C" uint32_t sms_render_spp_done(const sms_ctx *c) { return c ? c->render_spp : 0u; }
 
 sms_status ctx_ensure_lean(sms_ctx *c) {
     if (sms_status st = check_glint_scene(c)) return st;

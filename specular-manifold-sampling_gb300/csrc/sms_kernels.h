@@ -139,6 +139,8 @@ sms_status ctx_glint_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t se
                              const uint64_t *streams, sms_result *out);
 // Checks the glints scene, then builds the LEAN pyramid (ctx_build_lean).
 sms_status ctx_ensure_lean(sms_ctx *c);
+// Samples per pixel of the context's last render (sms_render_spp_done).
+void ctx_set_render_spp(sms_ctx *c, uint32_t spp);
 // Builds the LEAN pyramid of the scene's normal map on first use (the
 // context's scene view then carries it).
 sms_status ctx_build_lean(sms_ctx *c);

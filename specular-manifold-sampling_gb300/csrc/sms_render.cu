@@ -29,6 +29,7 @@
 // all random numbers are keyed by path and bounce they do not depend on the
 // wavefront size.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -986,6 +987,10 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     std::string why;
     if (!camera_params(cam, pc, why)) return rfail(SMS_ERR_INVALID_ARG, "sms_render: " + why);
     if (opt->spp <= 0) return rfail(SMS_ERR_INVALID_ARG, "sms_render: spp must be positive");
+    const uint32_t spp_pass = opt->samples_per_pass == 0 ? (uint32_t)opt->spp
+                                                         : std::min<uint32_t>(opt->samples_per_pass, (uint32_t)opt->spp);
+    if ((uint32_t)opt->spp % spp_pass != 0)
+        return rfail(SMS_ERR_INVALID_ARG, "sms_render: spp must be a multiple of samples_per_pass");
     if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_FILTERED_MS)
         return rfail(SMS_ERR_INVALID_ARG, "sms_render: unknown integrator");
     const bool glints = opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS;
@@ -1022,6 +1027,8 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
 
     const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
     const uint64_t total = wh * (uint64_t)opt->spp;
+    const uint64_t pass = wh * (uint64_t)spp_pass;   // paths per pass
+    std::chrono::steady_clock::time_point t_start;
     if (total >= (1ull << 48)) return rfail(SMS_ERR_INVALID_ARG, "sms_render: more than 2^48 samples");
     uint32_t cap = opt->max_paths ? opt->max_paths : kPtDefaultPaths;
     if (wh <= cap) cap = (uint32_t)(std::min<uint64_t>(cap / wh, (uint64_t)opt->spp) * wh);
@@ -1115,10 +1122,17 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     S.qcap = qcap;
     S.qrows = glints ? kQueryRowsMax : SMS_QUERY_FIELDS;
     PT_TRY(cudaMemsetAsync(image, 0, img_n * sizeof(float), s));
+    ctx_set_render_spp(c, 0);
+    t_start = std::chrono::steady_clock::now();
     while (g0 < total) {
+        // timeout: stop at a pass boundary once the time is up
+        if (opt->timeout > 0.f && g0 > 0 && g0 % pass == 0 &&
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() > opt->timeout)
+            break;
         uint32_t n;
         if (wh <= cap) n = (uint32_t)std::min<uint64_t>(cap, total - g0);
         else n = (uint32_t)std::min<uint64_t>(cap, wh - g0 % wh);
+        n = (uint32_t)std::min<uint64_t>(n, pass - g0 % pass);
         const uint32_t nb = (n + kPtBlock - 1) / kPtBlock;
         pt_camera_kernel<<<nb, kPtBlock, 0, s>>>(*v.scene, pc, S, g0, n, P.seed);
         PT_TRY(cudaGetLastError());
@@ -1164,8 +1178,12 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         }
         g0 += n;
     }
-    pt_scale_kernel<<<(unsigned)((img_n + 255) / 256), 256, 0, s>>>(image, img_n, 1.f / (float)opt->spp);
-    PT_TRY(cudaGetLastError());
+    {
+        const uint32_t spp_done = (uint32_t)(g0 / wh);
+        pt_scale_kernel<<<(unsigned)((img_n + 255) / 256), 256, 0, s>>>(image, img_n, 1.f / (float)spp_done);
+        PT_TRY(cudaGetLastError());
+        ctx_set_render_spp(c, spp_done);
+    }
     st = ctx_check_device_error(c);
 done:
     if (blk) {

@@ -35,7 +35,8 @@ load_render_setup reads the rendering side of the same file:
       <film> width, height (hdrfilm defaults 768 x 576), <sampler> sample_count
       (independent sampler default 4)   (src/sensors/perspective.cpp)
   <integrator type="path|path_sms_ss|path_sms_ms|path_filtered_ss|path_filtered_ms">  max_depth, rr_depth
-      (src/librender/integrator.cpp:300-320), disable_reflected_emitters,
+      (src/librender/integrator.cpp:300-320), samples_per_pass, timeout,
+      glint_diff_scale_factor_clamp (:35-41), disable_reflected_emitters,
       biased_mnee (path_sms_ss.cpp:59-60)
 and returns (Camera, RenderOptions).
 """
@@ -361,4 +362,7 @@ def load_render_setup(sms, path):
         opt.rr_depth = _int(ip, "rr_depth", 5)
         opt.disable_reflected_emitters = _bool(ip, "disable_reflected_emitters")
         opt.biased_mnee = _bool(ip, "biased_mnee")
+        opt.samples_per_pass = _int(ip, "samples_per_pass", 0)
+        opt.timeout = _float(ip, "timeout", -1.0)
+        opt.glint_diff_scale_factor_clamp = _float(ip, "glint_diff_scale_factor_clamp", 0.0)
     return cam, opt

@@ -275,3 +275,24 @@ def test_path_filtered_ms_matches_path_sms_ms(sms, workloads, gpu_lib):
     cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 32, 32)
     _compare_integrators(sms, ctx, cam, "path_sms_ms", 4096, 512, 4, base="path_filtered_ms")
     ctx.close()
+
+
+def test_render_passes_and_timeout(sms, workloads, gpu_lib):
+    """samples_per_pass / timeout (integrator.cpp:35-36, 61-68, 143-146):
+    passes change nothing but the summation order; a timeout that has run
+    out after the first pass leaves its mean (spp_done = samples_per_pass,
+    the same paths as a 1-pass render); spp must be a multiple of the pass."""
+    W = workloads
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=32)), W.water_config())
+    cam = W.pool_camera(24, 16)
+    a = ctx.render(cam, sms.RenderOptions(spp=8, seed=4))
+    assert ctx.render_spp_done() == 8
+    b = ctx.render(cam, sms.RenderOptions(spp=8, seed=4, samples_per_pass=2))
+    assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
+    c = ctx.render(cam, sms.RenderOptions(spp=64, seed=4, samples_per_pass=1, timeout=1e-6))
+    assert ctx.render_spp_done() == 1
+    d = ctx.render(cam, sms.RenderOptions(spp=1, seed=4))
+    assert np.array_equal(c, d)
+    with pytest.raises(sms.SMSError):
+        ctx.render(cam, sms.RenderOptions(spp=8, samples_per_pass=3))
+    ctx.close()

@@ -161,6 +161,12 @@ def test_render_setup_from_xml(sms, workloads, tmp_path):
     assert opt.integrator == "path_filtered_ms"
     _, cfg, kind = sms.load_scene(path)
     assert kind == "path_filtered_ms" and cfg.bounces == 2
+    # equal-time rendering parameters of the integrator (integrator.cpp:35-41)
+    path.write_text(RENDER_XML.replace('<integer name="rr_depth" value="3"/>',
+                                       '<integer name="rr_depth" value="3"/><float name="timeout" value="2.5"/>'
+                                       '<integer name="samples_per_pass" value="4"/>'))
+    cam, opt = sms.load_render_setup(path)
+    assert (opt.timeout, opt.samples_per_pass) == (2.5, 4)
 
 
 def test_rough_bsdfs_from_xml(sms, tmp_path):

@@ -226,9 +226,11 @@ def secondary_configs(torch, sms, W, dev):
 def render_study(torch, sms, W, dev, width=512, height=512, spp=16):
     """Whole images through the path tracer around the SMS solver (sms_render):
     the pool scene (512^2 water heightfield over a diffuse floor, sphere area
-    light), path_sms_ss with the unbiased estimator (cap 256) and plain path
-    tracing, width x height x spp samples; the oracle's restatement of the
-    same integrator on the host cores for a bounded 64 x 64 x 4 sample."""
+    light), path_sms_ss with the unbiased estimator (cap 256), plain path
+    tracing and the paper's comparison integrator path_filtered_ss (the same
+    light paths as path_sms_ss, found by BSDF and emitter sampling),
+    width x height x spp samples; the oracle's restatement of path_sms_ss on
+    the host cores for a bounded 64 x 64 x 4 sample."""
     from oracle import oracle as O
     desc = W.pool_scene(res=512)
     cfg = W.water_config()
@@ -239,7 +241,7 @@ def render_study(torch, sms, W, dev, width=512, height=512, spp=16):
     cam = W.pool_camera(width, height)
     out = {"scene": "pool: 512^2 water heightfield (IOR 1.33) over a diffuse floor, sphere area light r=0.5",
            "image": [width, height], "spp": spp}
-    for integ in ("path_sms_ss", "path"):
+    for integ in ("path_sms_ss", "path", "path_filtered_ss"):
         opt = sms.RenderOptions(integrator=integ, spp=spp, seed=1)
         ctx.render_device(cam, opt, img.data_ptr())
         ctx.reset_stats()

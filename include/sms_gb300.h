@@ -559,8 +559,10 @@ uint64_t sms_render_sms_seed(uint64_t seed);
  * returns when the image is there; sms_render_device takes a device pointer
  * and is asynchronous on the context stream apart from one small
  * device-to-host read per bounce (the number of SMS queries).
- * path_sms_ms with mnee_init and without biased_mnee returns
- * SMS_ERR_UNSUPPORTED (its MNEE bookkeeping is not implemented).
+ * Unbiased MNEE (mnee_init without biased_mnee): path_sms_ss and path_sms_ms
+ * add a BSDF-sampled caustic path when the deterministic MNEE walk from its
+ * receiver does not find the same chain (path_sms_ss.cpp:207-241,
+ * path_sms_ms.cpp:54-142, 323-360).
  *
  * path_sms_glints: camera rays carry ray differentials; at the first hit of
  * the glinty shape the glint estimator (the context's config) runs over the

@@ -2604,6 +2604,12 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
     /* PathRecord of path_filtered_ms.cpp:219-301 (state 0 default, 1 receiver,
        2 caster, 3 emitter; chain bounce count), after the camera ray */
     int rec = (si.valid() && (sc.shapes[si.shape].flags & SMS_SHAPE_CAUSTIC_RECEIVER)) ? 1 : 0, rec_b = 0;
+    /* MNEEHelper of path_sms_ms.cpp:54-142 for unbiased MNEE: the same states
+       in rec / rec_b, plus the receiver point and the specular vertices */
+    const bool mnee_ms = integ == SMS_INTEGRATOR_PATH_SMS_MS && cfg.mnee_init && !opt.biased_mnee;
+    V3 mnee_end = rec == 1 ? si.p : V3(0.f);
+    int mnee_shape = -1;
+    std::vector<V3> mnee_pos;
     for (int depth = 1;; ++depth) {
         if (!si.valid()) break;
         if (depth > opt.rr_depth) {
@@ -2770,6 +2776,27 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 } else { rec = 0; rec_b = 0; }
             } else { rec = 0; rec_b = 0; }
         }
+        if (mnee_ms) {
+            /* MNEEHelper::state_transition (path_sms_ms.cpp:84-140) */
+            const bool nv = si2.valid();
+            const uint32_t nf = nv ? sc.shapes[si2.shape].flags : 0u;
+            if (nv && (nf & SMS_SHAPE_CAUSTIC_RECEIVER)) {
+                rec = 1; rec_b = 0; mnee_end = si2.p; mnee_pos.clear();
+            } else if (rec == 1) {
+                if (nv && (nf & SMS_SHAPE_CAUSTIC_CASTER_MULTI)) {
+                    rec = 2; rec_b = 1; mnee_shape = si2.shape; mnee_pos.assign(1, si2.p);
+                } else { rec = 0; rec_b = 0; }
+            } else if (rec == 2) {
+                if (rec_b < bounces && nv && (nf & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER))) {
+                    mnee_pos.push_back(si2.p);
+                    rec_b++;
+                } else if (rec_b == bounces && nv && sc.shapes[si2.shape].emitter >= 0 &&
+                           std::find(sc.emitters_ms.begin(), sc.emitters_ms.end(), sc.shapes[si2.shape].emitter) !=
+                               sc.emitters_ms.end()) {
+                    rec = 3;
+                } else { rec = 0; rec_b = 0; }
+            } else { rec = 0; rec_b = 0; }
+        }
         if (si2.valid() && sc.shapes[si2.shape].emitter >= 0) {
             const Shape &es = sc.shapes[si2.shape];
             V3 ep = nr.o + nr.d * si2.t;
@@ -2785,6 +2812,19 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             if (allow) {
                 float epdf = bs.delta ? 0.f : pt_emitter_pdf(sc, es, si.p, ep, nr.d, si2.t);
                 L += thr * Le * mis_weight(bs.pdf, epdf);
+            } else if (mnee_ms && rec == 3 && rec_b == bounces) {
+                /* path_sms_ms.cpp:323-360: the MNEE walk from the receiver point */
+                Query q;
+                q.p = mnee_end;
+                std::vector<int> tmpl;
+                std::vector<MVertex> path;
+                int it = 0;
+                bool seed_ok = false;
+                bool found = ms_sample_path(sc, cfg, mnee_shape, q, ep, V2{0.5f, 0.5f}, V3(0.f), tmpl, true, path, it,
+                                            seed_ok);
+                for (size_t k = 0; found && k < path.size(); ++k)
+                    if (!(norm(path[k].p - mnee_pos[k]) < 1e-5f)) found = false;
+                if (!found) L += thr * Le;
             } else if (integ == SMS_INTEGRATOR_PATH_SMS_SS && cfg.mnee_init && !opt.biased_mnee && prev_receiver &&
                        std::find(sc.emitters_ss.begin(), sc.emitters_ss.end(), es.emitter) != sc.emitters_ss.end()) {
                 /* path_sms_ss.cpp:207-241: the MNEE walk from the previous vertex */

@@ -74,6 +74,10 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
 // The proposal network for every query of a batch (ss_proposal_kernel).
 cudaError_t launch_ss_proposal(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                                uint64_t stream_off, const mlp::SeedProposal &pr, int num_sms, cudaStream_t s);
+// The unbiased-MNEE test of path_sms_ms for a wavefront (ms_mnee_check_kernel).
+cudaError_t launch_ms_mnee_check(const DevScene &sc, const SolverCfg &cfg, int bounces, const float *rec,
+                                 const float *stage, const int *want, float *L, uint32_t n, uint32_t stride,
+                                 DevCounters *ctr, cudaStream_t s);
 // Normal-mapped caster variants (sms_ss_nm.cu), var = the caster variant bits.
 cudaError_t launch_ss_biased_nm(int var, const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n,
                                 uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,

@@ -13,6 +13,23 @@ template <int K>
 cudaError_t ms_connect_k(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                          uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                          const SsScratch &scr, int *tmpl, int num_sms, int bps, PhaseTimer *tm, cudaStream_t s);
+template <int K>
+cudaError_t ms_mnee_check_k(const DevScene &sc, const SolverCfg &cfg, const float *rec, const float *stage,
+                            const int *want, float *L, uint32_t n, uint32_t stride, DevCounters *ctr,
+                            cudaStream_t s);
+
+cudaError_t launch_ms_mnee_check(const DevScene &sc, const SolverCfg &cfg, int bounces, const float *rec,
+                                 const float *stage, const int *want, float *L, uint32_t n, uint32_t stride,
+                                 DevCounters *ctr, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    switch (bounces) {
+    case 1: return ms_mnee_check_k<1>(sc, cfg, rec, stage, want, L, n, stride, ctr, s);
+    case 2: return ms_mnee_check_k<2>(sc, cfg, rec, stage, want, L, n, stride, ctr, s);
+    case 3: return ms_mnee_check_k<3>(sc, cfg, rec, stage, want, L, n, stride, ctr, s);
+    case 4: return ms_mnee_check_k<4>(sc, cfg, rec, stage, want, L, n, stride, ctr, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
 
 cudaError_t launch_ms_walk(const DevScene &sc, const SolverCfg &cfg, int bounces, int caster, const float *q,
                            const float *w, uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s) {

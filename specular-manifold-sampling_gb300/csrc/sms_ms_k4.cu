@@ -9,4 +9,8 @@ template cudaError_t ms_connect_k<4>(const DevScene &sc, const SolverCfg &cfg, c
                                      uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                                      const SsScratch &scr, int *tmpl, int num_sms, int bps, PhaseTimer *tm, cudaStream_t s);
 
+template cudaError_t ms_mnee_check_k<4>(const DevScene &sc, const SolverCfg &cfg, const float *rec,
+                                        const float *stage, const int *want, float *L, uint32_t n,
+                                        uint32_t stride, DevCounters *ctr, cudaStream_t s);
+
 }  // namespace sms

@@ -473,6 +473,45 @@ __global__ void __launch_bounds__(128) ms_walk_kernel(DevScene sc, SolverCfg cfg
     flush_stats(st, ctr, err, kPhaseMsWalk);
 }
 
+// ------------------------------------------------ unbiased-MNEE test
+// The test of path_sms_ms.cpp:323-360 for the wavefront paths with want[i]
+// (their BSDF-sampled ray reached a caustic emitter through a complete
+// specular chain): the MNEE walk from the receiver point -- the straight seed
+// chain toward the light point (or the first specular shape's box centre),
+// its own shapes as the template, then Newton -- and, where it does not end on
+// the chain the path recorded (every vertex within 1e-5), the path's emitter
+// contribution is added to its radiance.  rec (16 rows of `stride`): receiver
+// point (3), first specular shape (int bits), recorded vertices (3 K);
+// stage rows 0-2 the light point, 3-5 the contribution; L: 3 rows.
+template <int K>
+__global__ void __launch_bounds__(128) ms_mnee_check_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ rec,
+                                                            const float *__restrict__ stage,
+                                                            const int *__restrict__ want, float *__restrict__ L,
+                                                            uint32_t n, uint32_t stride, DevCounters *ctr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    LaneStats st;
+    uint32_t err = 0;
+    if (i < n && want[i]) {
+        auto R = [&](int k) { return rec[(size_t)k * stride + i]; };
+        auto S = [&](int k) { return stage[(size_t)k * stride + i]; };
+        const f3 x0 = mk(R(0), R(1), R(2)), lp = mk(S(0), S(1), S(2));
+        const int caster = __float_as_int(R(3));
+        Chain<K> c;
+        int shapes[K];
+        int it = 0;
+        bool ok = seed_chain<K>(sc, cfg, caster, x0, lp, lp, nullptr, c, shapes, err, st) &&
+                  chain_newton<K>(sc, cfg, x0, lp, shapes, c, it, err, st);
+        #pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (ok && !(length(c.v[k].p - mk(R(4 + 3 * k), R(5 + 3 * k), R(6 + 3 * k))) < 1e-5f)) ok = false;
+        if (!ok) {
+            #pragma unroll
+            for (int k = 0; k < 3; ++k) L[(size_t)k * stride + i] += S(3 + k);
+        }
+    }
+    flush_stats(st, ctr, err, kPhaseMs);
+}
+
 // -------------------------------------------------------- biased estimator
 // G lanes per query, one walk per lane; walk m of caster c at stream position
 // 3 + 2 (c M + m).  Unlike the single-scatter estimator, solutions are
@@ -763,6 +802,14 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
 }
 
 // ---------------------------------------------------------------- launchers
+template <int K>
+cudaError_t ms_mnee_check_k(const DevScene &sc, const SolverCfg &cfg, const float *rec, const float *stage,
+                            const int *want, float *L, uint32_t n, uint32_t stride, DevCounters *ctr,
+                            cudaStream_t s) {
+    ms_mnee_check_kernel<K><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, rec, stage, want, L, n, stride, ctr);
+    return cudaGetLastError();
+}
+
 template <int K>
 cudaError_t ms_walk_k(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q, const float *w,
                       uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s) {

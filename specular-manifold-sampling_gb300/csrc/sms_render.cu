@@ -57,6 +57,9 @@ constexpr int kStageRows = 24;            // query rows, then 3 throughput rows 
 constexpr int kAlive = 1, kPrevReceiver = 2, kSpecularCamera = 4;
 constexpr int kRecShift = 3, kRecBounceShift = 5;
 constexpr int kRecDefault = 0, kRecReceiver = 1, kRecCaster = 2, kRecEmitter = 3;
+// rows of the MNEE record: receiver point (3), first specular shape (int
+// bits), specular vertices (3 per bounce)
+constexpr int kMneeRows = 4 + 3 * kMaxBounces;
 
 struct PtCam {
     float m[12];          // rows 0..2 of camera-to-world
@@ -71,6 +74,7 @@ struct PtParams {
     int disable_reflected_emitters, biased_mnee;
     int bounces;          // SMS chain length (path_sms_ms)
     int mnee_check;       // path_sms_ss with mnee_init and !biased_mnee
+    int mnee_ms;          // path_sms_ms with mnee_init and !biased_mnee
     uint64_t seed;
     SolverCfg solver;     // for the MNEE check walk
     float diff_scale;     // ray-differential scale (glints)
@@ -86,6 +90,12 @@ struct PtState {
     uint32_t *hit_prim;                   // cap
     float *stage;                         // kStageRows x cap
     int *want;                            // cap
+    // path_sms_ms unbiased MNEE (MNEEHelper, path_sms_ms.cpp:54-142): per
+    // path the receiver point, the first specular shape and the specular
+    // vertices since (kMneeRows x cap; null when off), and the paths whose
+    // emitter hit awaits the MNEE test of this bounce
+    float *mnee;
+    int *mnee_want;
     uint32_t *block_q, *block_a;          // per block
     uint32_t *totals;                     // [0] queries, [1] live paths
     // pending SMS batch (qcap entries, appended bounce by bounce)
@@ -497,6 +507,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_camera_kernel(DevScene sc, PtCam 
     // path record of the multi-bounce filter after the camera ray
     // (state_transition(si, si, ...) of path_filtered_ms.cpp:79)
     const int rec = (h.shape >= 0 && (sc.shapes[h.shape].flags & kShapeFlagReceiver)) ? kRecReceiver : kRecDefault;
+    if (S.mnee && rec == kRecReceiver) st3s(S.mnee, S.cap, i, o + d * h.t);
     S.flags[i] = (h.shape >= 0 ? kAlive : 0) | kSpecularCamera | (rec << kRecShift);
     S.cam_s[i] = sx;
     S.cam_s[(size_t)S.cap + i] = sy;
@@ -530,6 +541,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     int want = 0, alive_out = 0;
     uint32_t err = 0;
+    if (i < n && S.mnee_want) S.mnee_want[i] = 0;
     if (i < n && (S.flags[i] & kAlive)) {
         int flags = S.flags[i];
         Pcg32 rng = load_rng(S, i);
@@ -716,6 +728,39 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                     }
                     flags = (flags & ~(0x1F << kRecShift)) | (rec << kRecShift) | (rec_b << kRecBounceShift);
                 }
+                if (P.mnee_ms) {
+                    // MNEEHelper::state_transition (path_sms_ms.cpp:84-140): like
+                    // the filter's record, without its scattering-type test, and
+                    // keeping the receiver point and the specular vertices
+                    const bool nv = h2.shape >= 0;
+                    const uint32_t nf = nv ? sc.shapes[h2.shape].flags : 0u;
+                    const f3 p2 = si.p + d2 * h2.t;
+                    if (nv && (nf & kShapeFlagReceiver)) {
+                        rec = kRecReceiver; rec_b = 0;
+                        st3s(S.mnee, S.cap, i, p2);
+                    } else if (rec == kRecReceiver) {
+                        if (nv && (nf & kShapeFlagCasterMulti)) {
+                            rec = kRecCaster; rec_b = 1;
+                            S.mnee[(size_t)3 * S.cap + i] = __int_as_float(h2.shape);
+                            st3s(S.mnee + (size_t)4 * S.cap, S.cap, i, p2);
+                        } else {
+                            rec = kRecDefault; rec_b = 0;
+                        }
+                    } else if (rec == kRecCaster) {
+                        if (rec_b < P.bounces && nv && (nf & (kShapeFlagCasterMulti | kShapeFlagBouncer))) {
+                            st3s(S.mnee + (size_t)(4 + 3 * rec_b) * S.cap, S.cap, i, p2);
+                            rec_b++;
+                        } else if (rec_b == P.bounces && nv && sc.shapes[h2.shape].emitter >= 0 &&
+                                   emitter_is_caustic_ms(sc, sc.shapes[h2.shape].emitter)) {
+                            rec = kRecEmitter;
+                        } else {
+                            rec = kRecDefault; rec_b = 0;
+                        }
+                    } else {
+                        rec = kRecDefault; rec_b = 0;
+                    }
+                    flags = (flags & ~(0x1F << kRecShift)) | (rec << kRecShift) | (rec_b << kRecBounceShift);
+                }
                 if (h2.shape >= 0 && sc.shapes[h2.shape].emitter >= 0) {
                     const DevShape &es = sc.shapes[h2.shape];
                     const f3 ep = si.p + d2 * h2.t;
@@ -735,6 +780,15 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                     if (allow) {
                         float epdf = bs.delta ? 0.f : emitter_pdf(sc, es, si.p, ep, d2, h2.t);
                         L = L + thr * Le * mis_weight(bs.pdf, epdf);
+                    } else if (P.mnee_ms && rec == kRecEmitter && rec_b == P.bounces) {
+                        // path_sms_ms.cpp:323-360: the MNEE test runs after this
+                        // launch (ms_mnee_check_kernel); stage the light point and
+                        // the contribution it adds when MNEE misses this chain
+                        const f3 c = thr * Le;
+                        const float row[6] = {ep.x, ep.y, ep.z, c.x, c.y, c.z};
+                        #pragma unroll
+                        for (int k = 0; k < 6; ++k) S.stage[(size_t)k * S.cap + i] = row[k];
+                        S.mnee_want[i] = 1;
                     } else if (kMneeCheck && (flags & kPrevReceiver) &&
                                (sc.emitters[es.emitter].kind == 1) && emitter_is_caustic_ss(sc, es.emitter)) {
                         // path_sms_ss.cpp:207-241: add the path unless the MNEE
@@ -1007,9 +1061,6 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     if (opt->max_depth < -1) return rfail(SMS_ERR_INVALID_ARG, "sms_render: max_depth must be -1 or >= 0");
     if (opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS && (v.bounces < 1 || v.bounces > kMaxBounces))
         return rfail(SMS_ERR_UNSUPPORTED, "path_filtered_ms: bounces must be between 1 and 4");
-    if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee)
-        return rfail(SMS_ERR_UNSUPPORTED, "path_sms_ms: unbiased MNEE (mnee_init without biased_mnee) is not "
-                                          "implemented");
     PtParams P{};
     P.integrator = opt->integrator;
     P.max_depth = opt->max_depth;
@@ -1019,6 +1070,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     P.bounces = (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS || opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS)
                     ? v.bounces : 1;
     P.mnee_check = opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee;
+    P.mnee_ms = opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee;
     P.seed = opt->seed;
     P.solver = v.solver;
     P.diff_scale = std::max(1.f / std::sqrt((float)opt->spp), opt->glint_diff_scale_factor_clamp);
@@ -1049,7 +1101,9 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
                  o_qr = take(4 * (size_t)kQueryRowsMax * qcap), o_qw = take(12 * (size_t)qcap),
                  o_qm = take(4 * (size_t)qcap), o_qs = take(8 * (size_t)qcap),
                  o_q = take(4 * (size_t)kQueryRowsMax * qcap), o_val = take(12 * (size_t)qcap),
-                 o_cnt = take(4 * (size_t)qcap), o_wk = take(4 * (size_t)qcap);
+                 o_cnt = take(4 * (size_t)qcap), o_wk = take(4 * (size_t)qcap),
+                 o_mn = take(P.mnee_ms ? 4 * (size_t)kMneeRows * cap : 0),
+                 o_mw = take(P.mnee_ms ? 4 * (size_t)cap : 0);
     char *blk = nullptr;
     uint32_t *host_tot = nullptr;
     sms_status st = SMS_OK;
@@ -1118,6 +1172,8 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     S.value = reinterpret_cast<float *>(blk + o_val);
     S.count = reinterpret_cast<int *>(blk + o_cnt);
     S.walks = reinterpret_cast<int *>(blk + o_wk);
+    S.mnee = P.mnee_ms ? reinterpret_cast<float *>(blk + o_mn) : nullptr;
+    S.mnee_want = P.mnee_ms ? reinterpret_cast<int *>(blk + o_mw) : nullptr;
     S.cap = cap;
     S.qcap = qcap;
     S.qrows = glints ? kQueryRowsMax : SMS_QUERY_FIELDS;
@@ -1152,6 +1208,10 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
             else
                 pt_bounce_kernel<false><<<nb, kPtBlock, 0, s>>>(*v.scene, P, S, depth, n, v.counters, pc);
             PT_TRY(cudaGetLastError());
+            if (P.mnee_ms) {
+                PT_TRY(launch_ms_mnee_check(*v.scene, P.solver, P.bounces, S.mnee, S.stage, S.mnee_want, S.L, n,
+                                            S.cap, v.counters, s));
+            }
             pt_scan_kernel<<<1, 1024, 0, s>>>(S, nb);
             PT_TRY(cudaGetLastError());
             pt_gather_kernel<<<nb, kPtBlock, 0, s>>>(S, n, pending, g0, depth);

@@ -182,9 +182,9 @@ def test_render_with_learned_proposal(sms, workloads, gpu_lib):
 
 def test_render_argument_errors(sms, workloads, gpu_lib):
     W = workloads
-    ctx = sms.Context(sms.Scene(W.pool_scene(res=16)), sms.SMSConfig(mnee_init=True, bounces=2))
-    with pytest.raises(sms.SMSError) as e:
-        ctx.render(W.pool_camera(8, 8), sms.RenderOptions(integrator="path_sms_ms"))
+    ctx = sms.Context(sms.Scene(W.pool_scene(res=16)), sms.SMSConfig(mnee_init=True, bounces=5))
+    with pytest.raises(sms.SMSError) as e:   # chains of 1..4 vertices
+        ctx.render(W.pool_camera(8, 8), sms.RenderOptions(integrator="path_filtered_ms"))
     assert e.value.status == 4
     with pytest.raises(sms.SMSError) as e:
         ctx.render(W.pool_camera(8, 8), sms.RenderOptions(spp=0))
@@ -295,4 +295,22 @@ def test_render_passes_and_timeout(sms, workloads, gpu_lib):
     assert np.array_equal(c, d)
     with pytest.raises(sms.SMSError):
         ctx.render(cam, sms.RenderOptions(spp=8, samples_per_pass=3))
+    ctx.close()
+
+
+def test_unbiased_mnee_multi_scatter(sms, workloads, oracle, gpu_lib):
+    """path_sms_ms with mnee_init and without biased_mnee (MNEEHelper,
+    path_sms_ms.cpp:54-142, 323-360): the deterministic MNEE chain plus the
+    BSDF-sampled chains MNEE does not reproduce.  GPU vs oracle within the
+    FMA floor, and unbiased against plain path tracing under the slab."""
+    W = workloads
+    desc = _slab_desc(sms, W, caster_below=True)
+    cfg = sms.SMSConfig(biased=True, max_trials=1, mnee_init=True, bounces=2, halfvector_constraints=True)
+    cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 16, 16)
+    g, o, f = _check_against_oracle(sms, oracle, desc, cfg, cam,
+                                    sms.RenderOptions(integrator="path_sms_ms", spp=8, seed=17))
+    assert o.mean() > 0.0
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    cam = sms.Camera.look_at((0.0, 0.0, 0.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, 32, 32)
+    _compare_integrators(sms, ctx, cam, "path_sms_ms", 4096, 512, 4)
     ctx.close()

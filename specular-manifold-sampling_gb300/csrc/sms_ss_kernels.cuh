@@ -20,6 +20,14 @@
 
 namespace sms {
 
+// Resident blocks per SM the first-walk and trial kernels are compiled for
+// (128 threads each): 8 gives 64 registers per thread, the measured optimum of
+// the latency-bound walks (the headline step at 4 / 6 / 7 / 8 / 10 blocks:
+// 62.4 / 53.3 / 50.6 / 49.7 / 57.8 ms).
+#ifndef SMS_SS_WALK_MIN_BLOCKS
+#define SMS_SS_WALK_MIN_BLOCKS 8
+#endif
+
 // ------------------------------------------------------ biased estimator
 // Group of G lanes per query; walk m of caster c sits at stream position
 // 3 + 2 (c M + m).  Contributions are summed in walk order over the first
@@ -148,7 +156,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
 // mlp::proposal_seed, mixture from ss_proposal_kernel) instead of two-draw
 // uniform seeding.
 template <bool kLearned, int kVar>
-__global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+__global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_first_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
                                                        float *__restrict__ value, int *__restrict__ count,
                                                        int *__restrict__ walks, SsScratch scr, DevCounters *ctr,
@@ -261,7 +269,7 @@ __global__ void __launch_bounds__(128, 8) ss_first_kernel(DevScene sc, SolverCfg
 // All lanes run one warp-uniform loop: groups whose query finished fetch the
 // next one at the top, so every ballot and shuffle has the whole warp.
 template <bool kLearned, int G, int kVar>
-__global__ void __launch_bounds__(128, 8) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
+__global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
                                                         int *__restrict__ walks, SsScratch scr, DevCounters *ctr,

@@ -562,6 +562,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
     std::vector<DevEmitter> em;
     d.glinty_shape = s->nmap_shape;
     d.nmap_shape = s->nmap_res > 0 ? s->nmap_shape : -1;
+    d.ms_nm = c->ms_nm ? 1 : 0;
     d.nmap_res = s->nmap_res;
     d.nmap_tiles = s->nmap_tiles;
     for (size_t i = 0; i < s->emitters.size(); ++i) {
@@ -980,7 +981,6 @@ static sms_status check_ms_cfg(sms_ctx *c) {
         return fail(SMS_ERR_UNSUPPORTED, "bounces must be between 1 and 4");
     if (c->ms_rough)
         return fail(SMS_ERR_UNSUPPORTED, "rough (alpha > 0) multi-scatter chain shapes are not supported");
-    if (c->ms_nm) return fail(SMS_ERR_UNSUPPORTED, "normal-mapped multi-scatter chain shapes are not supported");
     return SMS_OK;
 }
 

@@ -1,7 +1,9 @@
 // sms_ms_kernels.cuh -- multi-scatter SMS kernels (k-bounce specular chains) for
-// sm_103a and their per-chain-length launchers.  Each chain length K is
-// instantiated in its own translation unit (sms_ms_k1.cu .. sms_ms_k4.cu) so
-// the four compile in parallel; sms_ms.cu dispatches on K.
+// sm_103a and their per-chain-length launchers, templated on the chain length
+// K and on kNM (chain shapes may carry the normal map).  Each (K, kNM) pair is
+// instantiated in its own translation unit (sms_ms_k1.cu .. sms_ms_k4.cu,
+// sms_ms_nm_k1.cu .. sms_ms_nm_k4.cu) so they compile in parallel; sms_ms.cu
+// dispatches.
 //
 // Reference: SpecularManifoldMultiScatter (src/librender/manifold_ms.cpp):
 //   specular_manifold_sampling :27-201, sample_path :203-227,
@@ -61,7 +63,7 @@ SMS_D bool chain_shape(const DevScene &sc, int s) {
 // hit (sample_seed_path :327-397, reproject :865-917).  tmpl (K shape ids) or
 // null; check_flags restricts hits to caster_multi / bouncer shapes; straight
 // keeps the direction at every hit (the MNEE seed path, :378-397).
-template <int K>
+template <int K, bool kNM = false>
 SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool check_flags, Chain<K> &c,
                        int *shapes, uint32_t &err, LaneStats &st, bool straight = false) {
     f3 wo = normalize(x1 - x0);
@@ -75,7 +77,7 @@ SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool c
         if (h.shape < 0) return false;
         if (check_flags && !chain_shape(sc, h.shape)) return false;
         if (tmpl && h.shape != tmpl[b]) return false;
-        vertex_from_hit<false>(sc, o, wo, h, c.v[b]);
+        vertex_from_hit<kNM>(sc, o, wo, h, c.v[b]);
         if (shapes) shapes[b] = h.shape;
         f3 wi = -wo;
         if (straight) {
@@ -94,12 +96,12 @@ SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool c
 // The seed path of a walk (sample_seed_path :280-408): toward the sampled
 // point x1, or with cfg.mnee_init along the straight line toward the MNEE
 // target without scattering.
-template <int K>
+template <int K, bool kNM = false>
 SMS_D bool seed_chain(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x0, f3 x1, f3 lp, const int *tmpl,
                       Chain<K> &c, int *shapes, uint32_t &err, LaneStats &st) {
     if (cfg.mnee_init)
-        return trace_chain<K>(sc, x0, mnee_target(sc.shapes[caster], lp), tmpl, true, c, shapes, err, st, true);
-    return trace_chain<K>(sc, x0, x1, tmpl, true, c, shapes, err, st);
+        return trace_chain<K, kNM>(sc, x0, mnee_target(sc.shapes[caster], lp), tmpl, true, c, shapes, err, st, true);
+    return trace_chain<K, kNM>(sc, x0, x1, tmpl, true, c, shapes, err, st);
 }
 
 // Angle-difference constraint of vertex i and its blocks w.r.t. the previous,
@@ -293,7 +295,7 @@ SMS_D bool chain_step(const SolverCfg &cfg, f3 x0, f3 lp, const Chain<K> &c, boo
 
 // newton_solver (:410-498).  c holds the seed path on entry and the solution
 // on success; tmpl = the estimate's template shapes.
-template <int K>
+template <int K, bool kNM = false>
 SMS_D bool chain_newton(const DevScene &sc, const SolverCfg &cfg, f3 x0, f3 lp, const int *tmpl, Chain<K> &c,
                         int &it, uint32_t &err, LaneStats &st) {
     it = 0;
@@ -306,7 +308,7 @@ SMS_D bool chain_newton(const DevScene &sc, const SolverCfg &cfg, f3 x0, f3 lp, 
         if (conv) break;
         f3 p0 = c.v[0].p - (c.v[0].dp_du * du + c.v[0].dp_dv * dv) * (cfg.step_scale * beta);
         Chain<K> prop;
-        if (trace_chain<K>(sc, x0, p0, tmpl, false, prop, nullptr, err, st)) {
+        if (trace_chain<K, kNM>(sc, x0, p0, tmpl, false, prop, nullptr, err, st)) {
             beta = fminf(1.f, 2.f * beta);
             c = prop;
             need = true;
@@ -329,7 +331,7 @@ SMS_D bool chain_newton(const DevScene &sc, const SolverCfg &cfg, f3 x0, f3 lp, 
 
 // specular_reflectance (:920-1023): Fresnel along the re-traced chain, then
 // the light visibility test.
-template <int K>
+template <int K, bool kNM = false>
 SMS_D float chain_reflectance(const DevScene &sc, f3 x0, f3 lp, const Chain<K> &c, uint32_t &err, LaneStats &st) {
     f3 o = x0, d = normalize(c.v[0].p - x0);
     float val = 1.f;
@@ -341,7 +343,7 @@ SMS_D float chain_reflectance(const DevScene &sc, f3 x0, f3 lp, const Chain<K> &
         st.ray(h);
         if (h.shape < 0) return 0.f;
         Vtx hv;
-        vertex_from_hit<false>(sc, o, d, h, hv);
+        vertex_from_hit<kNM>(sc, o, d, h, hv);
         f3 wo = k + 1 < K ? normalize(c.v[k + 1].p - hv.p) : normalize(lp - hv.p);
         val *= specular_reflectance(sc.shapes[h.shape], hv.n, wo);
         o = hv.p;
@@ -428,7 +430,7 @@ SMS_D float chain_geometric(f3 x, const Chain<K> &c, f3 yp, f3 ydu, f3 ydv) {
 }
 
 // evaluate_path_contribution (:229-278).
-template <int K>
+template <int K, bool kNM = false>
 SMS_D f3 chain_contribution(const DevScene &sc, f3 x, const Light &L, const Chain<K> &sol, uint32_t &err,
                             LaneStats &st) {
     f3 yp, ydu, ydv, lw, lp;
@@ -436,13 +438,13 @@ SMS_D f3 chain_contribution(const DevScene &sc, f3 x, const Light &L, const Chai
     Chain<K> c = sol;
     #pragma unroll
     for (int i = 0; i < K; ++i) make_orthonormal(c.v[i].dp_du, c.v[i].dp_dv, c.v[i].dn_du, c.v[i].dn_dv);
-    float F = chain_reflectance<K>(sc, x, lp, c, err, st);
+    float F = chain_reflectance<K, kNM>(sc, x, lp, c, err, st);
     F *= chain_geometric<K>(x, c, yp, ydu, ydv);
     return lw * F;
 }
 
 // -------------------------------------------------------------- walk kernel
-template <int K>
+template <int K, bool kNM>
 __global__ void __launch_bounds__(128) ms_walk_kernel(DevScene sc, SolverCfg cfg, int caster, const float *__restrict__ q,
                                                       const float *__restrict__ w, uint32_t n, float *__restrict__ out,
                                                       DevCounters *ctr) {
@@ -460,8 +462,8 @@ __global__ void __launch_bounds__(128) ms_walk_kernel(DevScene sc, SolverCfg cfg
         Chain<K> c;
         int shapes[K];
         int it = 0;
-        bool seed_ok = seed_chain<K>(sc, cfg, caster, x, x1, lp, nullptr, c, shapes, err, st);
-        bool ok = seed_ok && chain_newton<K>(sc, cfg, x, lp, shapes, c, it, err, st);
+        bool seed_ok = seed_chain<K, kNM>(sc, cfg, caster, x, x1, lp, nullptr, c, shapes, err, st);
+        bool ok = seed_ok && chain_newton<K, kNM>(sc, cfg, x, lp, shapes, c, it, err, st);
         float res[kMsWalkOutFields] = {ok ? 1.f : 0.f, (float)it, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, seed_ok ? 1.f : 0.f};
         if (ok) {
             res[2] = c.v[0].p.x; res[3] = c.v[0].p.y; res[4] = c.v[0].p.z;
@@ -483,7 +485,7 @@ __global__ void __launch_bounds__(128) ms_walk_kernel(DevScene sc, SolverCfg cfg
 // contribution is added to its radiance.  rec (16 rows of `stride`): receiver
 // point (3), first specular shape (int bits), recorded vertices (3 K);
 // stage rows 0-2 the light point, 3-5 the contribution; L: 3 rows.
-template <int K>
+template <int K, bool kNM>
 __global__ void __launch_bounds__(128) ms_mnee_check_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ rec,
                                                             const float *__restrict__ stage,
                                                             const int *__restrict__ want, float *__restrict__ L,
@@ -499,8 +501,8 @@ __global__ void __launch_bounds__(128) ms_mnee_check_kernel(DevScene sc, SolverC
         Chain<K> c;
         int shapes[K];
         int it = 0;
-        bool ok = seed_chain<K>(sc, cfg, caster, x0, lp, lp, nullptr, c, shapes, err, st) &&
-                  chain_newton<K>(sc, cfg, x0, lp, shapes, c, it, err, st);
+        bool ok = seed_chain<K, kNM>(sc, cfg, caster, x0, lp, lp, nullptr, c, shapes, err, st) &&
+                  chain_newton<K, kNM>(sc, cfg, x0, lp, shapes, c, it, err, st);
         #pragma unroll
         for (int k = 0; k < K; ++k)
             if (ok && !(length(c.v[k].p - mk(R(4 + 3 * k), R(5 + 3 * k), R(6 + 3 * k))) < 1e-5f)) ok = false;
@@ -517,7 +519,7 @@ __global__ void __launch_bounds__(128) ms_mnee_check_kernel(DevScene sc, SolverC
 // 3 + 2 (c M + m).  Unlike the single-scatter estimator, solutions are
 // deduplicated before the contribution, which itself tests visibility
 // (:147-195).
-template <int K, int G>
+template <int K, int G, bool kNM>
 #ifndef SMS_MS_BIASED_MIN_BLOCKS
 #define SMS_MS_BIASED_MIN_BLOCKS 4
 #endif
@@ -572,7 +574,7 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                     Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + 2u * ((uint64_t)ci * M + m));
                     float sx = rng.next_f32(), sy = rng.next_f32();
                     f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
-                    seed_ok = seed_chain<K>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st);
+                    seed_ok = seed_chain<K, kNM>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st);
                 }
                 // the first completed seed path of the estimate is the template
                 unsigned sb = __ballot_sync(kFull, seed_ok) & gmask;
@@ -596,7 +598,7 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                         #pragma unroll
                         for (int b = 0; b < K; ++b) match = match && shapes[b] == tmpl[b];
                     }
-                    ok = match && chain_newton<K>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st);
+                    ok = match && chain_newton<K, kNM>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st);
                 }
                 if (act) {
                     st.walks++;
@@ -629,7 +631,7 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                     __syncwarp();
                 }
                 f3 contrib = splat(0.f);
-                if (keep) contrib = diffuse_eval(Q, dir) * chain_contribution<K>(sc, Q.x, L, c, err, st);
+                if (keep) contrib = diffuse_eval(Q, dir) * chain_contribution<K, kNM>(sc, Q.x, L, c, err, st);
                 // sum in walk order
                 for (int k = 0; k < G; ++k) {
                     const int src = gbase + k;
@@ -657,7 +659,7 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
 // Part 1: one lane per query runs the first walk (its seed path is the
 // template) and the contribution; every success is queued for trials
 // (:95-110; the contribution tests visibility itself).
-template <int K>
+template <int K, bool kNM>
 __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cfg, int ci, const float *__restrict__ qs,
                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
                                                        float *__restrict__ value, int *__restrict__ count,
@@ -691,15 +693,15 @@ __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cf
             Chain<K> c;
             int shapes[K];
             int it = 0;
-            bool ok = seed_chain<K>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st) &&
-                      chain_newton<K>(sc, cfg, Q.x, L.p, shapes, c, it, err, st);
+            bool ok = seed_chain<K, kNM>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st) &&
+                      chain_newton<K, kNM>(sc, cfg, Q.x, L.p, shapes, c, it, err, st);
             st.walks++;
             st.newton += (unsigned)it;
             nw++;
             if (ok) {
                 st.succ++;
                 f3 dir = normalize(c.v[0].p - Q.x);
-                f3 spec = chain_contribution<K>(sc, Q.x, L, c, err, st);
+                f3 spec = chain_contribution<K, kNM>(sc, Q.x, L, c, err, st);
                 f3 val = diffuse_eval(Q, dir) * spec;
                 scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;
                 scr.val[qi] = val.x; scr.val[(size_t)n + qi] = val.y; scr.val[2 * (size_t)n + qi] = val.z;
@@ -730,7 +732,7 @@ __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cf
 
 // Part 2: Bernoulli trials, 32 per warp step (:111-135); trial walks must
 // reproduce the template's shapes.
-template <int K>
+template <int K, bool kNM>
 __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg cfg, int ci, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
@@ -768,8 +770,8 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
                 float sx = rng.next_f32(), sy = rng.next_f32();
                 f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
                 Chain<K> c;
-                bool ok = seed_chain<K>(sc, cfg, caster, Q.x, x1, L.p, tmpl, c, nullptr, err, st) &&
-                          chain_newton<K>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st);
+                bool ok = seed_chain<K, kNM>(sc, cfg, caster, Q.x, x1, L.p, tmpl, c, nullptr, err, st) &&
+                          chain_newton<K, kNM>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st);
                 succ = ok && fabsf(dot(dir0, normalize(c.v[0].p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
             }
             unsigned b = __ballot_sync(kFull, succ);
@@ -802,24 +804,24 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
 }
 
 // ---------------------------------------------------------------- launchers
-template <int K>
+template <int K, bool kNM>
 cudaError_t ms_mnee_check_k(const DevScene &sc, const SolverCfg &cfg, const float *rec, const float *stage,
                             const int *want, float *L, uint32_t n, uint32_t stride, DevCounters *ctr,
                             cudaStream_t s) {
-    ms_mnee_check_kernel<K><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, rec, stage, want, L, n, stride, ctr);
+    ms_mnee_check_kernel<K, kNM><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, rec, stage, want, L, n, stride, ctr);
     return cudaGetLastError();
 }
 
-template <int K>
+template <int K, bool kNM>
 cudaError_t ms_walk_k(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q, const float *w,
                       uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm, cudaStream_t s) {
     phase_begin(tm, kPhaseMsWalk, s);
-    ms_walk_kernel<K><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, caster, q, w, n, out, ctr);
+    ms_walk_kernel<K, kNM><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, caster, q, w, n, out, ctr);
     phase_end(tm, s);
     return cudaGetLastError();
 }
 
-template <int K>
+template <int K, bool kNM>
 cudaError_t ms_connect_k(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                          uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                          const SsScratch &scr, int *tmpl, int num_sms, int bps, PhaseTimer *tm, cudaStream_t s) {
@@ -828,8 +830,8 @@ cudaError_t ms_connect_k(const DevScene &sc, const SolverCfg &cfg, const float *
         const uint32_t gpb = 128 / G;
         uint32_t blocks = std::min<uint32_t>((n + gpb - 1) / gpb, (uint32_t)(num_sms * bps));
         phase_begin(tm, kPhaseMs, s);
-        if (G == 16) ms_biased_kernel<K, 16><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
-        else ms_biased_kernel<K, 32><<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
+        auto kernel = G == 16 ? ms_biased_kernel<K, 16, kNM> : ms_biased_kernel<K, 32, kNM>;
+        kernel<<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
         phase_end(tm, s);
         return cudaGetLastError();
     }
@@ -837,10 +839,11 @@ cudaError_t ms_connect_k(const DevScene &sc, const SolverCfg &cfg, const float *
         cudaError_t e = cudaMemsetAsync(&ctr->trial_count, 0, 2 * sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
         phase_begin(tm, kPhaseMs, s);
-        ms_first_kernel<K><<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr,
-                                                           tmpl, ctr);
-        ms_trials_kernel<K><<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr,
-                                                          tmpl, ctr);
+        auto first = ms_first_kernel<K, kNM>;
+        auto trials = ms_trials_kernel<K, kNM>;
+        first<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, tmpl, ctr);
+        trials<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, tmpl,
+                                              ctr);
         phase_end(tm, s);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;

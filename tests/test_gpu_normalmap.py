@@ -142,8 +142,7 @@ def test_normal_mapped_noalloc_matches_device_path(sms, workloads, gpu_lib):
 def test_normal_map_refusals(sms, workloads, gpu_lib):
     """twostage needs every single-scatter caster normal-mapped (the
     reference's lean() of a plain BSDF is zero: its slope draw is NaN and no
-    walk converges); normal-mapped multi-scatter chains, learned seeds on a
-    normal-mapped caster and rough normal-mapped shapes in a render are not
+    walk converges); rough normal-mapped shapes in a render are not
     supported."""
     W = workloads
     ctx = sms.Context(sms.Scene(W.sphere_scene()), sms.SMSConfig(twostage=True))
@@ -154,18 +153,6 @@ def test_normal_map_refusals(sms, workloads, gpu_lib):
         with pytest.raises(sms.SMSError) as e:
             call()
         assert e.value.status == UNSUPPORTED
-    ctx.close()
-    ms = sms.SceneDesc()
-    P = np.array([[-1, -1, 1.0], [1, -1, 1.0], [1, 1, 1.0], [-1, 1, 1.0]], np.float32)
-    UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
-    sid = ms.add_mesh(P, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5),
-                      sms.SHAPE_CAUSTIC_CASTER_MULTI, UV=UV)
-    ms.normalmap = (sid, W.nm_plane_slopes(64), 1.0)
-    ms.add_point_emitter((0.0, 0.0, 4.0), (40.0,) * 3, sms.EMITTER_CAUSTIC_MULTI)
-    ctx = sms.Context(sms.Scene(ms), sms.SMSConfig(bounces=1, biased=True, max_trials=4))
-    with pytest.raises(sms.SMSError) as e:
-        sms.SpecularManifoldMultiScatter(ctx).specular_manifold_sampling(W.nm_plane_queries(4))
-    assert e.value.status == UNSUPPORTED
     ctx.close()
     ctx = sms.Context(sms.Scene(W.nm_plane_scene(alpha=0.2)), sms.SMSConfig())
     with pytest.raises(sms.SMSError) as e:
@@ -203,3 +190,54 @@ def test_normal_mapped_caustic_is_unbiased_against_path(sms, workloads, gpu_lib,
     ctx = sms.Context(sms.Scene(_nm_pool(W, 1)), sms.SMSConfig(biased=False, max_trials=-1, twostage=twostage))
     _compare_integrators(sms, ctx, W.pool_camera(32, 32), "path_sms_ss", 4096, 512, 4)
     ctx.close()
+
+
+def _nm_ms_scene(sms, W, conductor):
+    """The normal-mapped plane as a one-vertex multi-scatter chain."""
+    d = W.nm_plane_scene(conductor=conductor, freq=4)
+    P, N, UV, F, b, _ = d.meshes[0]
+    d.meshes[0] = (P, N, UV, F, b, sms.SHAPE_CAUSTIC_CASTER_MULTI)
+    pos, inten, _ = d.point_emitters[0]
+    d.point_emitters[0] = (pos, inten, sms.EMITTER_CAUSTIC_MULTI)
+    return d
+
+
+@pytest.mark.parametrize("conductor", [False, True])
+def test_normal_mapped_multi_scatter(sms, workloads, oracle, gpu_lib, conductor):
+    """Multi-scatter chains on a normal-mapped shape (the chain kernels built
+    with the normal-mapped frames): per-walk and biased / unbiased estimates,
+    GPU vs oracle against the FMA floor."""
+    W = workloads
+    desc = _nm_ms_scene(sms, W, conductor)
+    light = (0.3, -0.2, -3.0) if conductor else (0.3, -0.2, 4.0)
+    n = 4096
+    q = W.nm_plane_queries(n)
+    cfg = sms.SMSConfig(bounces=1)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    w = _walk_inputs(W, n, light, False)
+    out_g = sms.SpecularManifoldMultiScatter(ctx).sample_path(0, q, w)
+    out_o = oracle.OracleScene(desc).ms_walk_batch(cfg, 0, q, w)
+    out_f = oracle.OracleScene(desc, fma=True).ms_walk_batch(cfg, 0, q, w)
+    g = np.mean((out_g[0] > 0.5) != (out_o[0] > 0.5))
+    f = np.mean((out_f[0] > 0.5) != (out_o[0] > 0.5))
+    both = (out_g[0] > 0.5) & (out_o[0] > 0.5)
+    print(f"nm ms walks conductor={conductor}: mismatch {g:.4f} floor {f:.4f} both {both.sum()}")
+    assert both.sum() > 50
+    assert g <= FLOOR_FACTOR * f + FLOOR_SLACK
+    assert np.median(np.linalg.norm(out_g[2:5, both] - out_o[2:5, both], axis=0)) < 1e-5
+    ctx.close()
+    for biased in (True, False):
+        cfg = sms.SMSConfig(bounces=1, biased=biased, max_trials=16 if biased else 256)
+        ctx = sms.Context(sms.Scene(desc), cfg)
+        vg, cg, wg = sms.SpecularManifoldMultiScatter(ctx).specular_manifold_sampling(q, seed=5)
+        vo, co, wo, _ = oracle.OracleScene(desc).connect_batch(cfg, q, seed=5, multi=True)
+        vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=5, multi=True)
+        g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+        f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+        print(f"nm ms connect conductor={conductor} biased={biased}: count mismatch {g_cm:.4f} differs {g_diff:.4f} "
+              f"(floor {f_cm:.4f}/{f_diff:.4f}) median rel {g_med:.1e} nonzero {np.mean(vo[0] > 0):.3f}")
+        assert np.mean(vo[0] > 0) > 0.02
+        assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+        assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+        assert g_med < 1e-3
+        ctx.close()

@@ -570,7 +570,8 @@ uint64_t sms_render_sms_seed(uint64_t seed);
  * sample inside the footprint, both with the LEAN-mapping density of the
  * footprint (manifold_glints.cpp:28-223, the LEAN mip pyramid of
  * src/librender/normalmap.cpp, include/mitsuba/render/lean.h); the
- * normal-mapped conductor reflects about the bilinear slope normal elsewhere.
+ * normal-mapped BSDF samples its nested BSDF in the frame of the bilinear
+ * slope normal elsewhere (normalmap.cpp:118-135).
  * The LEAN pyramid (5 floats per texel over all levels, 4/3 x 20 bytes per
  * texel of the slope map) is built on the device at the first glint render. */
 sms_status sms_render(sms_ctx *ctx, const sms_camera *cam, const sms_render_options *opt, float *image);

@@ -2637,7 +2637,8 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                                             : filtered_ms && rec == 2 && rec_b == bounces;
         const float caustic_eta = bsdf_eta(s.bsdf);
         const bool diffuse = s.bsdf.type == SMS_BSDF_DIFFUSE;
-        /* the glinty shape carries a normal-mapped conductor (delta reflection) */
+        /* the normal-mapped shape (glinty, or a caster / bouncer) carries the
+           normalmap BSDF around its smooth conductor or dielectric */
         const bool nmapped = si.shape == sc.glinty_shape && sc.nmap.res > 0;
         const bool smooth = !nmapped && (diffuse || is_rough(s.bsdf));   /* BSDFFlags::Smooth */
         const bool on_glinty = integ == SMS_INTEGRATOR_PATH_SMS_GLINTS && depth == 1 && nmapped &&

@@ -585,7 +585,8 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             const bool valid_conn = filtered_ss ? on_caster && ((flags & kPrevReceiver) || glint_case)
                                                 : filtered_ms && rec == kRecCaster && rec_b == P.bounces;
             const bool diffuse = s.bsdf_type == kBsdfDiffuse;
-            // the glinty shape carries a normal-mapped conductor (delta reflection)
+            // the normal-mapped shape (glinty, or a caster / bouncer) carries the
+            // normalmap BSDF around its smooth conductor or dielectric
             const bool nmapped = shape == sc.glinty_shape && sc.nmap_res > 0;
             const bool smooth = !nmapped && (diffuse || s.alpha > 0.f);   // BSDFFlags::Smooth
             const bool on_glinty = P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS && depth == 1 && nmapped &&

@@ -290,11 +290,13 @@ SMS_HD bool tri_hit(float4 a, float4 b, float4 c, f3 o, f3 d, float mint,
     return u >= 0.f && u <= 1.f && v >= 0.f && u + v <= 1.f && t >= mint && t <= maxt;
 }
 
+// Slab test of one box; inv the reciprocal direction, oi = o * inv, so that
+// each slab distance (lo - o) / d is one FMA.
 SMS_HD bool box2(float lox, float loy, float loz, float hix, float hiy, float hiz,
-                                     f3 o, f3 inv, float tmin, float tmax, float &tn) {
-    float tx0 = (lox - o.x) * inv.x, tx1 = (hix - o.x) * inv.x;
-    float ty0 = (loy - o.y) * inv.y, ty1 = (hiy - o.y) * inv.y;
-    float tz0 = (loz - o.z) * inv.z, tz1 = (hiz - o.z) * inv.z;
+                                     f3 inv, f3 oi, float tmin, float tmax, float &tn) {
+    float tx0 = fmaf(lox, inv.x, -oi.x), tx1 = fmaf(hix, inv.x, -oi.x);
+    float ty0 = fmaf(loy, inv.y, -oi.y), ty1 = fmaf(hiy, inv.y, -oi.y);
+    float tz0 = fmaf(loz, inv.z, -oi.z), tz1 = fmaf(hiz, inv.z, -oi.z);
     float t0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
     float t1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
     tn = t0;
@@ -323,10 +325,12 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
         }
     }
     if (sc.n_tris == 0) return found;
-    // Reciprocal direction; a zero component gives +-inf, which the slab test
-    // handles (0 * inf = NaN comparisons leave the interval unchanged through
-    // fminf/fmaxf, which return the non-NaN operand).
-    f3 inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    // Reciprocal direction, a zero component replaced by 1e-20 of its sign so
+    // that every slab distance is finite (a slab the ray runs inside then
+    // spans about +-1e20 and constrains nothing).
+    auto rcp_dir = [](float x) { return 1.f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
+    const f3 inv = mk(rcp_dir(d.x), rcp_dir(d.y), rcp_dir(d.z));
+    const f3 oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
     int stack[kStackDepth];
     int sp = 0;
     int node = 0;
@@ -339,8 +343,8 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
         float4 n0 = sms_ldg(np), n1 = sms_ldg(np + 1), n2 = sms_ldg(np + 2);
         int4 n3 = sms_ldg(reinterpret_cast<const int4 *>(np + 3));
         float tl, tr;
-        bool hl = box2(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, o, inv, mint, hit.t, tl);
-        bool hr = box2(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, o, inv, mint, hit.t, tr);
+        bool hl = box2(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oi, mint, hit.t, tl);
+        bool hr = box2(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oi, mint, hit.t, tr);
         // Leaves are processed right away; inner children are pushed.
         int next = -1;
         #pragma unroll

@@ -281,12 +281,24 @@ SMS_HD bool tri_hit(float4 a, float4 b, float4 c, f3 o, f3 d, float mint,
                                         float maxt, float &t, float &u, float &v) {
     f3 p0 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
     f3 pvec = cross(d, e2);
-    float inv_det = 1.f / dot(e1, pvec);
+    const float det = dot(e1, pvec);
     f3 tvec = o - p0;
-    u = dot(tvec, pvec) * inv_det;
+    const float un = dot(tvec, pvec);
     f3 qvec = cross(tvec, e1);
-    v = dot(d, qvec) * inv_det;
-    t = dot(e2, qvec) * inv_det;
+    const float vn = dot(d, qvec), tn = dot(e2, qvec);
+    // The same bounds on the numerators, scaled by |det| and widened by a
+    // relative 1e-6 (more than the rounding of the quotients), reject most
+    // triangles before the reciprocal; the test on the quotients decides.
+    const float sg = det < 0.f ? -1.f : 1.f, ad = fabsf(det);
+    const float us = un * sg, vs = vn * sg, ts = tn * sg;
+    const float hi = ad * (1.f + 1e-6f);
+    if (!(us >= 0.f && vs >= 0.f && us <= hi && us + vs <= hi && ts >= mint * ad * (1.f - 1e-6f) &&
+          ts <= maxt * hi))
+        return false;
+    const float inv_det = 1.f / det;
+    u = un * inv_det;
+    v = vn * inv_det;
+    t = tn * inv_det;
     return u >= 0.f && u <= 1.f && v >= 0.f && u + v <= 1.f && t >= mint && t <= maxt;
 }
 

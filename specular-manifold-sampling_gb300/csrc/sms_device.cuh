@@ -284,17 +284,18 @@ SMS_HD bool tri_hit(float4 a, float4 b, float4 c, f3 o, f3 d, float mint,
     const float det = dot(e1, pvec);
     f3 tvec = o - p0;
     const float un = dot(tvec, pvec);
-    f3 qvec = cross(tvec, e1);
-    const float vn = dot(d, qvec), tn = dot(e2, qvec);
     // The same bounds on the numerators, scaled by |det| and widened by a
     // relative 1e-6 (more than the rounding of the quotients), reject most
-    // triangles before the reciprocal; the test on the quotients decides.
+    // triangles before the reciprocal (the first barycentric before the
+    // second cross product); the test on the quotients decides.
     const float sg = det < 0.f ? -1.f : 1.f, ad = fabsf(det);
-    const float us = un * sg, vs = vn * sg, ts = tn * sg;
+    const float us = un * sg;
     const float hi = ad * (1.f + 1e-6f);
-    if (!(us >= 0.f && vs >= 0.f && us <= hi && us + vs <= hi && ts >= mint * ad * (1.f - 1e-6f) &&
-          ts <= maxt * hi))
-        return false;
+    if (!(us >= 0.f && us <= hi)) return false;
+    f3 qvec = cross(tvec, e1);
+    const float vn = dot(d, qvec), tn = dot(e2, qvec);
+    const float vs = vn * sg, ts = tn * sg;
+    if (!(vs >= 0.f && us + vs <= hi && ts >= mint * ad * (1.f - 1e-6f) && ts <= maxt * hi)) return false;
     const float inv_det = 1.f / det;
     u = un * inv_det;
     v = vn * inv_det;

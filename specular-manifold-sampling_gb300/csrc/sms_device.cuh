@@ -358,26 +358,24 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
         float tl, tr;
         bool hl = box2(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oi, mint, hit.t, tl);
         bool hr = box2(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oi, mint, hit.t, tr);
-        // Leaves are processed right away; inner children are pushed.
+        // Leaves are processed right away, the triangles of both hit leaf
+        // children in one loop (left first), so that lanes whose leaves sit on
+        // different sides test their triangles together; inner children are
+        // pushed.
         int next = -1;
-        #pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            bool h = side == 0 ? hl : hr;
-            int child = side == 0 ? n3.x : n3.y;
-            int cnt = side == 0 ? n3.z : n3.w;
-            if (!h || cnt == 0) continue;
-            hit.tests += (uint32_t)cnt;
-            for (int k = 0; k < cnt; ++k) {
-                const float4 *tp = sc.tris + 3 * (size_t)(child + k);
-                float4 a = sms_ldg(tp), b = sms_ldg(tp + 1), c = sms_ldg(tp + 2);
-                float t, u, v;
-                if (tri_hit(a, b, c, o, d, mint, hit.t, t, u, v) && (!found || t < hit.t)) {
-                    hit.t = t; hit.u = u; hit.v = v;
-                    hit.shape = sms_as_int(a.w);
-                    hit.prim = (uint32_t)sms_as_int(b.w);
-                    found = true;
-                    if (any_hit) return true;
-                }
+        const int c0 = hl ? n3.z : 0, nt = c0 + (hr ? n3.w : 0);
+        hit.tests += (uint32_t)nt;
+        for (int k = 0; k < nt; ++k) {
+            const int ti = k < c0 ? n3.x + k : n3.y + (k - c0);
+            const float4 *tp = sc.tris + 3 * (size_t)ti;
+            float4 a = sms_ldg(tp), b = sms_ldg(tp + 1), c = sms_ldg(tp + 2);
+            float t, u, v;
+            if (tri_hit(a, b, c, o, d, mint, hit.t, t, u, v) && (!found || t < hit.t)) {
+                hit.t = t; hit.u = u; hit.v = v;
+                hit.shape = sms_as_int(a.w);
+                hit.prim = (uint32_t)sms_as_int(b.w);
+                found = true;
+                if (any_hit) return true;
             }
         }
         bool il = hl && n3.z == 0, ir = hr && n3.w == 0;

@@ -464,7 +464,6 @@ SMS_HD void mesh_surface(const MeshTri &m, int has_normals, float b1, float b2,
     f3 n = normalize(cross(dp0, dp1));
     si.n = n;
     f3 dpdu, dpdv;
-    onb(n, dpdu, dpdv);
     si.u = m.u0 * b0 + m.u1 * b1 + m.u2 * b2;
     si.v = m.v0 * b0 + m.v1 * b1 + m.v2 * b2;
     float du0 = m.u1 - m.u0, dv0 = m.v1 - m.v0, du1 = m.u2 - m.u0, dv1 = m.v2 - m.v0;
@@ -473,6 +472,8 @@ SMS_HD void mesh_surface(const MeshTri &m, int has_normals, float b1, float b2,
         float inv = 1.f / dt;
         dpdu = (dp0 * dv1 - dp1 * dv0) * inv;
         dpdv = (dp1 * du0 - dp0 * du1) * inv;
+    } else {
+        onb(n, dpdu, dpdv);   // degenerate uv parameterization
     }
     if (has_normals) n = normalize(m.n0 * b0 + m.n1 * b1 + m.n2 * b2);
     si.shn = n;

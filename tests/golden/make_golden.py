@@ -18,6 +18,10 @@
   oracle_small.npz     oracle outputs on small cases (regression pin of the
                        restatement; the GPU tests compare the library to the
                        oracle run live on the same host).
+  oracle_nm.npz        the same for normal-mapped casters: per-walk outputs
+                       with the two-stage solver and unbiased estimates with
+                       and without it on the 4-period normal-mapped plane
+                       (``--only nm`` regenerates this file alone).
 """
 from __future__ import annotations
 
@@ -129,11 +133,33 @@ def analytic_cases():
     return cases
 
 
+def nm_cases(sms, W, O):
+    desc = W.nm_plane_scene(freq=4)
+    osc = O.OracleScene(desc)
+    n = 128
+    q = W.nm_plane_queries(n)
+    w = np.zeros((10, n), np.float32)
+    w[0:3] = np.array([0.3, -0.2, 4.0], np.float32)[:, None]
+    w[6:10] = W.pcg32_streams_f32(13, np.arange(n, dtype=np.uint64), 4)
+    res = {"nm_walk_twostage": osc.walk_batch(sms.SMSConfig(twostage=True), 0, q, w)}
+    for two in (False, True):
+        cfg = sms.SMSConfig(biased=False, max_trials=64, twostage=two)
+        v, c, wk, st = osc.connect_batch(cfg, W.nm_plane_queries(256), seed=9, nthreads=1)
+        tag = "twostage" if two else "plain"
+        res[f"nm_{tag}_value"], res[f"nm_{tag}_count"], res[f"nm_{tag}_walks"] = v, c, wk
+    return res
+
+
 def main():
     sms = load_package()
     from sms_gb300 import workloads as W
     sys.path.insert(0, str(ROOT))
     from oracle import oracle as O
+
+    np.savez_compressed(OUT / "oracle_nm.npz", **nm_cases(sms, W, O))
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "nm":
+        print("wrote oracle_nm.npz")
+        return
 
     r = W.Pcg32(42, 54)
     kat = {

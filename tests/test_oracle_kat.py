@@ -516,3 +516,24 @@ def test_two_stage_walk_inputs(sms, workloads, oracle):
     assert np.any(np.linalg.norm(a[2:5, both] - b[2:5, both], axis=0) > 1e-3)
     plain = osc.walk_batch(sms.SMSConfig(), 0, q, w[:8])
     assert a[0].mean() > plain[0].mean()
+
+
+def test_normal_mapped_oracle_regression(sms, workloads, oracle):
+    """Bit-exact regression of the oracle's normal-mapped caster restatement
+    (two-stage walks, unbiased estimates with and without the two-stage
+    solver) against tests/golden/oracle_nm.npz."""
+    W = workloads
+    ref = np.load(GOLDEN / "oracle_nm.npz")
+    osc = oracle.OracleScene(W.nm_plane_scene(freq=4))
+    n = 128
+    q = W.nm_plane_queries(n)
+    w = np.zeros((10, n), np.float32)
+    w[0:3] = np.array([0.3, -0.2, 4.0], np.float32)[:, None]
+    w[6:10] = W.pcg32_streams_f32(13, np.arange(n, dtype=np.uint64), 4)
+    np.testing.assert_array_equal(osc.walk_batch(sms.SMSConfig(twostage=True), 0, q, w), ref["nm_walk_twostage"])
+    for two in (False, True):
+        cfg = sms.SMSConfig(biased=False, max_trials=64, twostage=two)
+        v, c, wk, st = osc.connect_batch(cfg, W.nm_plane_queries(256), seed=9, nthreads=2)
+        tag = "twostage" if two else "plain"
+        assert np.array_equal(c, ref[f"nm_{tag}_count"]) and np.array_equal(wk, ref[f"nm_{tag}_walks"])
+        np.testing.assert_allclose(v, ref[f"nm_{tag}_value"], rtol=1e-6, atol=1e-9)

@@ -619,9 +619,11 @@ class Camera:
 
 @dataclass
 class RenderOptions:
-    """Integrator parameters: path / path_sms_ss / path_sms_ms with the
-    MonteCarloIntegrator fields (src/librender/integrator.cpp:300-320) and the
-    SMS integrators' switches (path_sms_ss.cpp:59-60)."""
+    """Integrator parameters: path, path_sms_ss, path_sms_ms, path_sms_glints,
+    path_filtered_ss or path_filtered_ms with the MonteCarloIntegrator fields
+    (src/librender/integrator.cpp:300-320), the sampling integrator's passes,
+    timeout and glint ray-differential clamp (:35-41) and the SMS integrators'
+    switches (path_sms_ss.cpp:59-60)."""
     integrator: str = "path_sms_ss"
     max_depth: int = -1
     rr_depth: int = 5

@@ -42,10 +42,12 @@ def _rle(b: bytes) -> bytes:
     return bytes(out)
 
 
-def _write_exr(path, chans, comp):
-    """chans: name -> (float32 array (h, w), pixel type 0 uint / 1 half / 2 float)."""
+def _write_exr(path, chans, comp, origin=(0, 0)):
+    """chans: name -> (float32 array (h, w), pixel type 0 uint / 1 half / 2 float);
+    origin: the data window's first pixel (x, y)."""
     names = sorted(chans)
     h, w = chans[names[0]][0].shape
+    x0, y0 = origin
     hdr = bytearray(struct.pack("<ii", 20000630, 2))
 
     def attr(name, typ, data):
@@ -54,7 +56,7 @@ def _write_exr(path, chans, comp):
     attr("channels", "chlist",
          b"".join(n.encode() + b"\0" + struct.pack("<iB3xii", chans[n][1], 0, 1, 1) for n in names) + b"\0")
     attr("compression", "compression", bytes([comp]))
-    attr("dataWindow", "box2i", struct.pack("<iiii", 0, 0, w - 1, h - 1))
+    attr("dataWindow", "box2i", struct.pack("<iiii", x0, y0, x0 + w - 1, y0 + h - 1))
     attr("displayWindow", "box2i", struct.pack("<iiii", 0, 0, w - 1, h - 1))
     attr("lineOrder", "lineOrder", b"\0")
     attr("pixelAspectRatio", "float", struct.pack("<f", 1.0))
@@ -73,7 +75,7 @@ def _write_exr(path, chans, comp):
             enc = _rle(pre) if comp == 1 else zlib.compress(pre)
             if len(enc) < len(raw):
                 data = enc
-        chunks.append(struct.pack("<ii", y, len(data)) + data)
+        chunks.append(struct.pack("<ii", y0 + y, len(data)) + data)
     pos = len(hdr) + 8 * len(chunks)
     offs = []
     for c in chunks:
@@ -218,3 +220,15 @@ def test_scene_xml_normalmap_bsdf(sms, io, oracle, tmp_path):
       </shape></scene>"""))
     with pytest.raises(ValueError, match="one normal map"):
         sms.load_scene(tmp_path / "two.xml")
+
+
+def test_exr_data_window_and_uint(io, tmp_path):
+    """A data window that does not start at the origin (chunks addressed by
+    their absolute first scanline) and UINT channels."""
+    rng = np.random.default_rng(3)
+    A = rng.random((21, 7)).astype(np.float32)
+    U = rng.integers(0, 1 << 20, size=(21, 7)).astype(np.float32)
+    f = tmp_path / "w.exr"
+    _write_exr(f, {"A": (A, 2), "U": (U, 0)}, 3, origin=(5, -4))
+    ch = io.read_exr(f)
+    assert np.array_equal(ch["A"], A) and np.array_equal(ch["U"], U)

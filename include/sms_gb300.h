@@ -302,9 +302,14 @@ sms_status sms_ss_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
  *     8 MiB on every GPU that loads the library, kept until process exit);
  *     larger batches are rejected with SMS_ERR_INVALID_ARG -- split them and
  *     use stream_offset, which keeps results identical.
- *   - The first call on a device looks up the array's device address (and lets
- *     the CUDA runtime load the module that holds it); make that first call
- *     before any stream capture.
+ *   - It accepts and refuses the same configurations as the device entry
+ *     point (same checks), except that it never builds the two-stage solver's
+ *     LEAN pyramid: with twostage, call sms_ss_connect_batch_device once first.
+ *     A bound learned proposal is refused (its mixtures need more scratch).
+ *   - The first call on a device (and the first after cudaDeviceReset) looks
+ *     up the array's device address and lets the CUDA runtime load the module
+ *     that holds it; make that first call before any stream capture.
+ *   - Its kernels are not included in sms_profile_read's phase times.
  *   - All calls, from every context on a device, share the one array: calls
  *     whose kernels overlap on the GPU (different streams, or different
  *     contexts) race on it.  Calls issued on one stream are safe.

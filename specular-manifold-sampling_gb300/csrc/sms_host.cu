@@ -796,6 +796,25 @@ static sms_status check_ss_normalmap(sms_ctx *c) {
     return SMS_OK;
 }
 
+// Configuration checks of a single-scatter connection call, shared by the
+// device entry point and the allocation-free one so both accept and refuse the
+// same configurations.  With may_allocate false a missing LEAN pyramid is
+// reported instead of built (building it allocates).
+sms_status ctx_ss_check(sms_ctx *c, bool may_allocate) {
+    if (c->cfg.biased && c->cfg.max_trials > (1 << 24))
+        return fail(SMS_ERR_INVALID_ARG, "max_trials too large for the biased estimator");
+    if (c->prop && c->cfg.biased)
+        return fail(SMS_ERR_UNSUPPORTED, "a learned proposal seeds the unbiased estimator only");
+    if (!may_allocate && c->cfg.twostage && c->dsc.n_casters_ss > 0 && !c->lean) {
+        const uint32_t all = c->dsc.n_casters_ss >= 32 ? ~0u : ((1u << c->dsc.n_casters_ss) - 1u);
+        if ((c->dsc.casters_ss_nm & all) != all)
+            return fail(SMS_ERR_UNSUPPORTED, "the twostage solver needs every single-scatter caster normal-mapped");
+        return fail(SMS_ERR_UNSUPPORTED, "the twostage solver needs the LEAN pyramid, which the first "
+                                         "sms_ss_connect_batch_device call builds");
+    }
+    return check_ss_normalmap(c);
+}
+
 // Single-scatter connection of n device-resident queries; streams (may be
 // null) as SolverCfg::streams.
 sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
@@ -803,11 +822,7 @@ sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
     if (!c || !out || (n && (!q || !out->value || !out->count || !out->walks)))
         return fail(SMS_ERR_INVALID_ARG, "sms_ss_connect_batch_device: null argument");
     if (n == 0) return SMS_OK;
-    if (c->cfg.biased && c->cfg.max_trials > (1 << 24))
-        return fail(SMS_ERR_INVALID_ARG, "max_trials too large for the biased estimator");
-    if (c->prop && c->cfg.biased)
-        return fail(SMS_ERR_UNSUPPORTED, "a learned proposal seeds the unbiased estimator only");
-    if (sms_status st = check_ss_normalmap(c)) return st;
+    if (sms_status st = ctx_ss_check(c, true)) return st;
     CUDA_TRY(cudaSetDevice(c->device));
     SsScratch scr{};
     if (!c->cfg.biased)

@@ -137,6 +137,11 @@ bool ctx_view(sms_ctx *c, sms::CtxView &out);
 // per-query stream table (SolverCfg::streams).
 sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
                           const uint64_t *streams, sms_result *out);
+// Configuration checks of a single-scatter connection (max_trials bound, learned
+// proposal, two-stage solver and normal maps), shared by every single-scatter
+// connection entry point.  may_allocate false: report a missing LEAN pyramid
+// instead of building it.
+sms_status ctx_ss_check(sms_ctx *c, bool may_allocate);
 sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,
                           const uint64_t *streams, sms_result *out);
 sms_status ctx_glint_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed, uint64_t stream_off,

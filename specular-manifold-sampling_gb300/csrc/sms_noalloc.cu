@@ -7,6 +7,8 @@
 // it grows the context's per-query scratch of the unbiased estimator on demand.
 // sms_ss_connect_batch_noalloc runs the same kernels, but takes that scratch
 // from the fixed device array below and makes no allocating call at all.
+#include <cuda.h>
+
 #include <mutex>
 #include <string>
 
@@ -29,21 +31,72 @@ constexpr uint32_t kNoAllocMaxQueries = 1u << 18;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[(size_t)kNoAllocMaxQueries * 32];
 
 constexpr int kNoAllocMaxDevices = 64;
-static void *g_scratch_ptr[kNoAllocMaxDevices];
+
+// Cached device address of g_noalloc_scratch, per device, with the id of the
+// CUDA context it was looked up in.  cudaDeviceReset destroys the primary
+// context; the runtime then reloads this library's module in a new context,
+// where the array may sit elsewhere, so an address is reused only while the
+// device's current context is the one it came from.
+struct ScratchAddr {
+    unsigned long long ctx_id;
+    void *ptr;
+};
+static ScratchAddr g_scratch_addr[kNoAllocMaxDevices];
 static std::mutex g_scratch_mu;
 
-// Device address of g_noalloc_scratch on the current device (looked up once per
-// device; in host code the symbol name is only a host-side stand-in).
+using CuCtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CuCtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+// Id of the calling thread's current CUDA context (unique for the life of
+// the process); false when the driver cannot tell.
+static bool current_ctx_id(unsigned long long *id) {
+    static CuCtxGetCurrentFn get_current = nullptr;
+    static CuCtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CuCtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CuCtxGetIdFn>(p);
+    });
+    CUcontext cx = nullptr;
+    if (!get_current || !get_id || get_current(&cx) != CUDA_SUCCESS || !cx) return false;
+    return get_id(cx, id) == CUDA_SUCCESS;
+}
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the symbol name is only a host-side stand-in; cudaGetSymbolAddress gives
+// the address kernels can use.  The lookup runs once per device and context
+// (the first one also lets the runtime load the module that holds the array).
 static cudaError_t noalloc_scratch(int device, void **out) {
     if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[device]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[device] = p;
+    unsigned long long id = 0;
+    const bool have_id = current_ctx_id(&id);
+    ScratchAddr &a = g_scratch_addr[device];
+    if (have_id && a.ptr && a.ctx_id == id) {
+        *out = a.ptr;
+        return cudaSuccess;
     }
-    *out = g_scratch_ptr[device];
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        a.ptr = nullptr;
+        return e;
+    }
+    // The lookup may have created the context: take its id now.
+    if (have_id || current_ctx_id(&id)) {
+        a.ctx_id = id;
+        a.ptr = p;
+    } else {
+        a.ptr = nullptr;   // no context id: look the address up on every call
+    }
+    *out = p;
     return cudaSuccess;
 }
 
@@ -67,16 +120,9 @@ extern "C" sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *qu
         return set_last_error(SMS_ERR_UNSUPPORTED,
                               "sms_ss_connect_batch_noalloc: a bound learned proposal needs per-query mixture "
                               "scratch; use sms_ss_connect_batch_device");
-    if (v.solver.twostage && v.scene->n_casters_ss > 0) {
-        const uint32_t all = v.scene->n_casters_ss >= 32 ? ~0u : ((1u << v.scene->n_casters_ss) - 1u);
-        if ((v.scene->casters_ss_nm & all) != all)
-            return set_last_error(SMS_ERR_UNSUPPORTED, "sms_ss_connect_batch_noalloc: the twostage solver needs "
-                                                       "every single-scatter caster normal-mapped");
-        if (!v.scene->lean)
-            return set_last_error(SMS_ERR_UNSUPPORTED, "sms_ss_connect_batch_noalloc: the twostage solver needs the "
-                                                       "LEAN pyramid, which the first sms_ss_connect_batch_device "
-                                                       "call builds");
-    }
+    // Same configuration checks as sms_ss_connect_batch_device, except that a
+    // missing LEAN pyramid is reported rather than built.
+    if (sms_status st = ctx_ss_check(ctx, false)) return st;
     cudaError_t e = cudaSetDevice(v.device);
     if (e != cudaSuccess) return set_last_error(SMS_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     void *base = nullptr;
@@ -94,8 +140,10 @@ extern "C" sms_status sms_ss_connect_batch_noalloc(sms_ctx *ctx, const float *qu
     // Nothing in the scratch has to start at zero: every query's entries are
     // written before they are read within the call, and the trial-queue
     // counters live in the context and are cleared by the launch itself.
+    // No phase timer: recording it may create CUDA events (an allocation), so
+    // these calls do not appear in sms_profile_read.
     e = launch_ss_connect(*v.scene, v.solver, queries_dev, n, seed, stream_offset, out_dev->value, out_dev->count,
-                          out_dev->walks, v.counters, scr, v.num_sms, v.blocks_per_sm, v.timer, v.stream, nullptr,
+                          out_dev->walks, v.counters, scr, v.num_sms, v.blocks_per_sm, nullptr, v.stream, nullptr,
                           v.trial_group);
     if (e != cudaSuccess) return set_last_error(SMS_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     return SMS_OK;

@@ -90,3 +90,34 @@ def test_noalloc_call_replays_from_a_cuda_graph(sms, workloads, gpu_lib):
         np.testing.assert_array_equal(val.cpu().numpy(), v_ref)
     del g
     ctx.close()
+
+
+def test_noalloc_biased_matches_device_and_shares_its_checks(sms, workloads, gpu_lib):
+    """The biased estimator through the allocation-free call gives the device
+    entry point's results, and a configuration the device entry point refuses
+    (a biased max_trials above 2^24) is refused here too."""
+    import dataclasses
+
+    import torch
+    W = workloads
+    scene = sms.Scene(W.sphere_scene(conductor=True))
+    ctx = sms.Context(scene, W.sphere_config())
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    n = 4096
+    q_dev = torch.from_numpy(W.sphere_queries(64)).cuda()
+    for seed in (1, 2):
+        v_ref, c_ref, w_ref = _run(ss.specular_manifold_sampling_device, ctx, q_dev, n, seed)
+        v, c, w = _run(ss.specular_manifold_sampling_noalloc, ctx, q_dev, n, seed)
+        assert np.array_equal(c, c_ref) and np.array_equal(w, w_ref)
+        np.testing.assert_allclose(v, v_ref, rtol=1e-6, atol=0)
+        assert (c > 0).sum() > 0
+    ctx.close()
+    bad = dataclasses.replace(W.sphere_config(), max_trials=(1 << 24) + 1)
+    ctx = sms.Context(scene, bad)
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    out = torch.zeros((5, n), dtype=torch.float32, device="cuda")
+    for fn in (ss.specular_manifold_sampling_device, ss.specular_manifold_sampling_noalloc):
+        with pytest.raises(sms.SMSError) as e:
+            fn(q_dev.data_ptr(), n, out[0].data_ptr(), out[3].data_ptr(), out[4].data_ptr(), seed=1)
+        assert e.value.status == 1 and "max_trials" in str(e.value)
+    ctx.close()

@@ -16,6 +16,12 @@ import numpy as np
 ORACLE_DIR = Path(__file__).resolve().parent
 LIB_PATH = ORACLE_DIR / "liboracle.so"
 FMA_LIB_PATH = ORACLE_DIR / "liboracle_fma.so"
+# The four builds of sms_oracle.cpp (oracle/Makefile): FP32 (the oracle proper),
+# FP32 with FMA contraction (chaos floor), FP64 (basin classifier) and FP32 on
+# the counting scalar of op_count.h (operation counts, results identical to f32).
+VARIANT_PATHS = {"f32": LIB_PATH, "fma": FMA_LIB_PATH, "f64": ORACLE_DIR / "liboracle_f64.so",
+                 "ops": ORACLE_DIR / "liboracle_ops.so"}
+OP_COUNT_NAMES = ("add", "mul", "div", "sqrt", "transcendental", "box_tests", "triangle_tests", "traversal_flops")
 
 _LIB = None
 _LIBS = {}
@@ -62,14 +68,15 @@ def build() -> Path:
     return LIB_PATH
 
 
-def load(fma: bool = False):
+def load(fma: bool = False, variant: str | None = None):
     """The oracle library; fma=True gives the FMA-contracted build used to
-    measure the floating-point chaos floor."""
+    measure the floating-point chaos floor; variant picks any of the builds
+    of VARIANT_PATHS by name."""
     global _LIB
-    key = bool(fma)
+    key = variant or ("fma" if fma else "f32")
     if key in _LIBS:
         return _LIBS[key]
-    path = FMA_LIB_PATH if fma else LIB_PATH
+    path = VARIANT_PATHS[key]
     if not path.exists():
         build()
     lib = C.CDLL(str(path))
@@ -103,15 +110,31 @@ def load(fma: bool = False):
         "oracle_sample_slope_gaussian": (None, [vp, f32, f32, f32, vp, vp]),
         "oracle_pcg32": (None, [u64, u64, u32, vp]),
         "oracle_pcg32_f32": (None, [u64, u64, u32, vp]),
+        "oracle_build_kind": (i32, []),
+        "oracle_opcount_read": (None, [vp]),
+        "oracle_opcount_reset": (None, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
     _LIBS[key] = lib
-    if not fma:
+    if key == "f32":
         _LIB = lib
     return lib
+
+
+def op_counts(lib) -> dict:
+    """Operation counts of the counting build since the last reset_op_counts."""
+    out = np.zeros(len(OP_COUNT_NAMES), np.uint64)
+    lib.oracle_opcount_read(out.ctypes.data)
+    d = dict(zip(OP_COUNT_NAMES, (int(x) for x in out)))
+    d["flops"] = sum(d[k] for k in OP_COUNT_NAMES[:5])
+    return d
+
+
+def reset_op_counts(lib) -> None:
+    lib.oracle_opcount_reset()
 
 
 def _f3(v):
@@ -136,8 +159,8 @@ def _bsdf(b) -> _Bsdf:
 class OracleScene:
     """The oracle's copy of a SceneDesc (same shape ids, same emitter order)."""
 
-    def __init__(self, desc, fma: bool = False):
-        lib = load(fma)
+    def __init__(self, desc, fma: bool = False, variant: str | None = None):
+        lib = load(fma, variant)
         self._lib = lib
         self._h = lib.oracle_scene_create()
         self._keep = []

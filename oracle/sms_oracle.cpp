@@ -27,58 +27,95 @@
 #include <cstring>
 #include <limits>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "../include/sms_gb300.h"
 
+#if defined(ORC_OPCOUNT)
+#include "op_count.h"
+#endif
+
 namespace orc {
 
-static const float kInf = std::numeric_limits<float>::infinity();
-static const float kPi = 3.14159265358979323846f;
-static const float kInvPi = 0.31830988618379067154f;
+/* The scalar type of every walk computation.  float is the oracle proper;
+ * liboracle_f64.so builds the same source with double (the basin classifier:
+ * a walk whose outcome is the same in FP32, FP32 with FMA contraction and FP64
+ * is well conditioned), and liboracle_ops.so with the counting float of
+ * op_count.h (algorithmic FLOPs; results identical to the float build). */
+#if defined(ORC_OPCOUNT)
+typedef orc_opcount::CFloat Float;
+#define ORC_COUNT_FP64_OPS(n) (orc_opcount::counters().add += (n))
+#define ORC_TRAVERSAL_SCOPE(is_tri) orc_opcount::TraversalScope orc_scope_(is_tri)
+#elif defined(ORC_DOUBLE)
+typedef double Float;
+#define ORC_COUNT_FP64_OPS(n) ((void)0)
+#define ORC_TRAVERSAL_SCOPE(is_tri) ((void)0)
+#else
+typedef float Float;
+#define ORC_COUNT_FP64_OPS(n) ((void)0)
+#define ORC_TRAVERSAL_SCOPE(is_tri) ((void)0)
+#endif
+
+/* std::max / std::min for operands that may differ in type (a Float and a
+ * float literal when Float is double); same selection rule as std::max/min. */
+template <class A, class B>
+static inline typename std::common_type<A, B>::type omax(A a, B b) {
+    typedef typename std::common_type<A, B>::type T;
+    return ((T)a < (T)b) ? (T)b : (T)a;
+}
+template <class A, class B>
+static inline typename std::common_type<A, B>::type omin(A a, B b) {
+    typedef typename std::common_type<A, B>::type T;
+    return ((T)b < (T)a) ? (T)b : (T)a;
+}
+
+static const Float kInf = std::numeric_limits<float>::infinity();
+static const Float kPi = 3.14159265358979323846f;
+static const Float kInvPi = 0.31830988618379067154f;
 /* include/mitsuba/core/math.h:37-38 */
-static const float kRayEps = (std::numeric_limits<float>::epsilon() / 2.f) * 1500.f;
-static const float kShadowEps = kRayEps * 10.f;
+static const Float kRayEps = (std::numeric_limits<float>::epsilon() / 2.f) * 1500.f;
+static const Float kShadowEps = kRayEps * 10.f;
 
 /* ------------------------------------------------------------ vector math */
 struct V3 {
-    float x = 0.f, y = 0.f, z = 0.f;
+    Float x = 0.f, y = 0.f, z = 0.f;
     V3() {}
-    V3(float a) : x(a), y(a), z(a) {}
-    V3(float a, float b, float c) : x(a), y(b), z(c) {}
-    float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+    V3(Float a) : x(a), y(a), z(a) {}
+    V3(Float a, Float b, Float c) : x(a), y(b), z(c) {}
+    Float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
 };
 static inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 static inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 static inline V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }
-static inline V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-static inline V3 operator*(float s, V3 a) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3 operator*(V3 a, Float s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3 operator*(Float s, V3 a) { return {a.x * s, a.y * s, a.z * s}; }
 static inline V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
 static inline V3 &operator+=(V3 &a, V3 b) { a = a + b; return a; }
 static inline V3 &operator-=(V3 &a, V3 b) { a = a - b; return a; }
-static inline V3 &operator*=(V3 &a, float s) { a = a * s; return a; }
-static inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline V3 &operator*=(V3 &a, Float s) { a = a * s; return a; }
+static inline Float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 static inline V3 cross(V3 a, V3 b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
-static inline float norm(V3 a) { return std::sqrt(dot(a, a)); }
+static inline Float norm(V3 a) { return std::sqrt(dot(a, a)); }
 static inline V3 normalize(V3 a) { return a * (1.f / norm(a)); }
-static inline float hmax_abs(V3 a) {
-    return std::max(std::fabs(a.x), std::max(std::fabs(a.y), std::fabs(a.z)));
+static inline Float hmax_abs(V3 a) {
+    return omax(std::fabs(a.x), omax(std::fabs(a.y), std::fabs(a.z)));
 }
-static inline float safe_sqrt(float v) { return std::sqrt(std::max(v, 0.f)); }
-static inline float safe_acos(float v) { return std::acos(std::min(1.f, std::max(-1.f, v))); }
-static inline float safe_asin(float v) { return std::asin(std::min(1.f, std::max(-1.f, v))); }
+static inline Float safe_sqrt(Float v) { return std::sqrt(omax(v, 0.f)); }
+static inline Float safe_acos(Float v) { return std::acos(omin(1.f, omax(-1.f, v))); }
+static inline Float safe_asin(Float v) { return std::asin(omin(1.f, omax(-1.f, v))); }
 
-struct V2 { float x = 0.f, y = 0.f; };
+struct V2 { Float x = 0.f, y = 0.f; };
 
 /* 2x2 matrix, row-major m[r][c] */
 struct M2 {
-    float m[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    Float m[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
 };
-static inline float det(const M2 &a) { return a.m[0][0] * a.m[1][1] - a.m[0][1] * a.m[1][0]; }
+static inline Float det(const M2 &a) { return a.m[0][0] * a.m[1][1] - a.m[0][1] * a.m[1][0]; }
 static inline M2 inverse(const M2 &a) {
-    float id = 1.f / det(a);
+    Float id = 1.f / det(a);
     M2 r;
     r.m[0][0] = a.m[1][1] * id;  r.m[0][1] = -a.m[0][1] * id;
     r.m[1][0] = -a.m[1][0] * id; r.m[1][1] = a.m[0][0] * id;
@@ -98,9 +135,9 @@ static inline V2 mul(const M2 &a, V2 v) {
 /* Orthonormal basis of Duff et al. 2017, as used by the reference's
  * coordinate_system (include/mitsuba/core/vector.h:116-135). */
 static void coordinate_system(V3 n, V3 &s, V3 &t) {
-    float sign = std::copysign(1.f, n.z);
-    float a = -1.f / (sign + n.z);
-    float b = n.x * n.y * a;
+    Float sign = std::copysign(1.f, n.z);
+    Float a = -1.f / (sign + n.z);
+    Float b = n.x * n.y * a;
     s = V3(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
     t = V3(b, sign + n.y * n.y * a, -n.y);
 }
@@ -125,11 +162,11 @@ struct PCG32 {
         uint32_t rot = (uint32_t)(old >> 59u);
         return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
     }
-    float next_f32() {
+    Float next_f32() {
         uint32_t bits = (next_u32() >> 9) | 0x3f800000u;
         float f;
         std::memcpy(&f, &bits, 4);
-        return f - 1.f;
+        return Float(f - 1.f);
     }
     V2 next_2d() { V2 r; r.x = next_f32(); r.y = next_f32(); return r; }
 };
@@ -137,12 +174,12 @@ struct PCG32 {
 /* ------------------------------------------------------------------ scene */
 struct Shape {
     int kind = 0; /* 0 sphere, 1 mesh */
-    V3 center; float radius = 1.f; bool flip = false;
+    V3 center; Float radius = 1.f; bool flip = false;
     std::vector<V3> P, N;
     std::vector<V2> UV;
     std::vector<uint32_t> F;
-    std::vector<float> pmf, cdf; /* area distribution over faces */
-    float area_sum = 0.f, area_norm = 0.f;
+    std::vector<Float> pmf, cdf; /* area distribution over faces */
+    Float area_sum = 0.f, area_norm = 0.f;
     uint32_t valid_lo = 0, valid_hi = 0;
     sms_bsdf bsdf{};
     uint32_t flags = 0;
@@ -155,18 +192,18 @@ struct Emitter {
     V3 p; V3 radiance; int shape = -1; uint32_t flags = 0;
 };
 
-struct BNode { float lo[3], hi[3]; int left = -1, right = -1; uint32_t first = 0, count = 0; };
+struct BNode { Float lo[3], hi[3]; int left = -1, right = -1; uint32_t first = 0, count = 0; int axis = 0; };
 
 /* Slope-based normal map, level 0 (channels sx, sy of the reference's LEAN
  * data, src/librender/normalmap.cpp:7-36), stored as FP16 by the library and
  * widened to FP32 here. */
 struct NormalMap {
     uint32_t res = 0;
-    float tiles = 1.f;
-    std::vector<float> sx, sy;
+    Float tiles = 1.f;
+    std::vector<Float> sx, sy;
     /* LEAN mip pyramid (src/librender/normalmap.cpp:36-89): per level, 5
      * floats per texel (sx, sy, sx^2 + s0, sy^2 + s0, sx sy); built on first use */
-    std::vector<std::vector<float>> lean;
+    std::vector<std::vector<Float>> lean;
 };
 
 struct Scene {
@@ -185,7 +222,7 @@ struct Scene {
 /* Surface interaction: the subset of the reference's SurfaceInteraction3f the
  * SMS path reads (include/mitsuba/render/interaction.h). */
 struct SI {
-    float t = kInf;
+    Float t = kInf;
     V3 p, n, shn, dp_du, dp_dv;
     V2 uv;
     int shape = -1;
@@ -195,7 +232,7 @@ struct SI {
 
 struct Ray {
     V3 o, d;
-    float mint = kRayEps, maxt = kInf;
+    Float mint = kRayEps, maxt = kInf;
 };
 
 /* ---- sphere: src/shapes/sphere.cpp:275-297 (FP64 quadratic), math.h:371 */
@@ -209,17 +246,18 @@ static bool solve_quadratic(double a, double b, double c, double &x0, double &x1
         double sq = std::sqrt(discrim);
         double temp = -0.5 * (b + std::copysign(sq, b));
         double x0p = temp / a, x1p = c / temp;
-        x0 = std::min(x0p, x1p);
-        x1 = std::max(x0p, x1p);
+        x0 = omin(x0p, x1p);
+        x1 = omax(x0p, x1p);
     }
     return active;
 }
 
-static bool sphere_intersect(const Shape &s, const Ray &r, float &t_out) {
-    double mint = r.mint, maxt = r.maxt;
-    double ox = (double)r.o.x - s.center.x, oy = (double)r.o.y - s.center.y,
-           oz = (double)r.o.z - s.center.z;
-    double dx = r.d.x, dy = r.d.y, dz = r.d.z;
+static bool sphere_intersect(const Shape &s, const Ray &r, Float &t_out) {
+    ORC_COUNT_FP64_OPS(31);   /* the FP64 arithmetic below: 30 add/mul/div + 1 sqrt */
+    double mint = (double)r.mint, maxt = (double)r.maxt;
+    double ox = (double)r.o.x - (double)s.center.x, oy = (double)r.o.y - (double)s.center.y,
+           oz = (double)r.o.z - (double)s.center.z;
+    double dx = (double)r.d.x, dy = (double)r.d.y, dz = (double)r.d.z;
     double A = dx * dx + dy * dy + dz * dz;
     double B = 2.0 * (ox * dx + oy * dy + oz * dz);
     double C = ox * ox + oy * oy + oz * oz - (double)s.radius * (double)s.radius;
@@ -228,7 +266,7 @@ static bool sphere_intersect(const Shape &s, const Ray &r, float &t_out) {
     bool out_bounds = !(n0 <= maxt && f0 >= mint);
     bool in_bounds = n0 < mint && f0 > maxt;
     if (!(found && !out_bounds && !in_bounds)) return false;
-    t_out = (float)(n0 < mint ? f0 : n0);
+    t_out = (Float)(n0 < mint ? f0 : n0);
     return true;
 }
 
@@ -238,18 +276,18 @@ static void sphere_fill(const Shape &s, const Ray &r, SI &si) {
     V3 n = normalize(hit - s.center);
     si.p = n * s.radius + s.center;
     V3 local = (si.p - s.center) * (1.f / s.radius);
-    float rd2 = local.x * local.x + local.y * local.y;
+    Float rd2 = local.x * local.x + local.y * local.y;
     /* angle to +z, robust form: 2 asin(|v - (0,0,+-1)| / 2) */
-    float sz = std::copysign(1.f, local.z);
-    float tmp = 2.f * safe_asin(0.5f * norm(V3(local.x, local.y, local.z - sz)));
-    float theta = local.z >= 0.f ? tmp : kPi - tmp;
-    float phi = std::atan2(local.y, local.x);
+    Float sz = std::copysign(1.f, local.z);
+    Float tmp = 2.f * safe_asin(0.5f * norm(V3(local.x, local.y, local.z - sz)));
+    Float theta = local.z >= 0.f ? tmp : kPi - tmp;
+    Float phi = std::atan2(local.y, local.x);
     if (phi < 0.f) phi += 2.f * kPi;
     si.uv.x = phi * (0.5f / kPi);
     si.uv.y = theta * (1.f / kPi);
     V3 dpdu(-local.y, local.x, 0.f);
-    float rd = std::sqrt(rd2), inv_rd = 1.f / rd;
-    float cphi = local.x * inv_rd, sphi = local.y * inv_rd;
+    Float rd = std::sqrt(rd2), inv_rd = 1.f / rd;
+    Float cphi = local.x * inv_rd, sphi = local.y * inv_rd;
     V3 dpdv(local.z * cphi, local.z * sphi, -rd);
     if (rd == 0.f) dpdv = V3(1.f, 0.f, 0.f);
     si.dp_du = dpdu * (s.radius * 2.f * kPi);
@@ -260,11 +298,12 @@ static void sphere_fill(const Shape &s, const Ray &r, SI &si) {
 }
 
 /* ---- triangles: include/mitsuba/render/mesh.h:203-228 (Moller-Trumbore) */
-static bool tri_intersect(const Shape &m, uint32_t f, const Ray &r, float &u, float &v, float &t) {
+static bool tri_intersect(const Shape &m, uint32_t f, const Ray &r, Float &u, Float &v, Float &t) {
+    ORC_TRAVERSAL_SCOPE(true);
     V3 p0 = m.P[m.F[3 * f]], p1 = m.P[m.F[3 * f + 1]], p2 = m.P[m.F[3 * f + 2]];
     V3 e1 = p1 - p0, e2 = p2 - p0;
     V3 pvec = cross(r.d, e2);
-    float inv_det = 1.f / dot(e1, pvec);
+    Float inv_det = 1.f / dot(e1, pvec);
     V3 tvec = r.o - p0;
     u = dot(tvec, pvec) * inv_det;
     bool active = u >= 0.f && u <= 1.f;
@@ -277,10 +316,10 @@ static bool tri_intersect(const Shape &m, uint32_t f, const Ray &r, float &u, fl
 }
 
 /* src/librender/mesh.cpp:618-687 */
-static void mesh_fill(const Shape &m, float b1, float b2, SI &si) {
+static void mesh_fill(const Shape &m, Float b1, Float b2, SI &si) {
     uint32_t f = si.prim;
     uint32_t i0 = m.F[3 * f], i1 = m.F[3 * f + 1], i2 = m.F[3 * f + 2];
-    float b0 = 1.f - b1 - b2;
+    Float b0 = 1.f - b1 - b2;
     V3 p0 = m.P[i0], p1 = m.P[i1], p2 = m.P[i2];
     V3 dp0 = p1 - p0, dp1 = p2 - p0;
     si.p = p0 * b0 + p1 * b1 + p2 * b2;
@@ -296,9 +335,9 @@ static void mesh_fill(const Shape &m, float b1, float b2, SI &si) {
     uv.x = uv0.x * b0 + uv1.x * b1 + uv2.x * b2;
     uv.y = uv0.y * b0 + uv1.y * b1 + uv2.y * b2;
     V2 duv0{uv1.x - uv0.x, uv1.y - uv0.y}, duv1{uv2.x - uv0.x, uv2.y - uv0.y};
-    float dt = duv0.x * duv1.y - duv0.y * duv1.x;
+    Float dt = duv0.x * duv1.y - duv0.y * duv1.x;
     if (dt != 0.f) {
-        float inv = 1.f / dt;
+        Float inv = 1.f / dt;
         dpdu = (dp0 * duv1.y - dp1 * duv0.y) * inv;
         dpdv = (dp1 * duv0.x - dp0 * duv1.x) * inv;
     }
@@ -318,13 +357,13 @@ static void mesh_normal_derivative(const Shape &m, const SI &si, V3 &dndu, V3 &d
     V3 p0 = m.P[i0], p1 = m.P[i1], p2 = m.P[i2];
     V3 n0 = m.N[i0], n1 = m.N[i1], n2 = m.N[i2];
     V3 rel = si.p - p0, du = p1 - p0, dv = p2 - p0;
-    float b1 = dot(du, rel), b2 = dot(dv, rel), a11 = dot(du, du), a12 = dot(du, dv),
+    Float b1 = dot(du, rel), b2 = dot(dv, rel), a11 = dot(du, du), a12 = dot(du, dv),
           a22 = dot(dv, dv);
-    float inv_det = 1.f / (a11 * a22 - a12 * a12);
-    float u = (a22 * b1 - a12 * b2) * inv_det, v = (a11 * b2 - a12 * b1) * inv_det,
+    Float inv_det = 1.f / (a11 * a22 - a12 * a12);
+    Float u = (a22 * b1 - a12 * b2) * inv_det, v = (a11 * b2 - a12 * b1) * inv_det,
           w = 1.f - u - v;
     V3 N = n1 * u + n2 * v + n0 * w;
-    float il = 1.f / std::sqrt(dot(N, N));
+    Float il = 1.f / std::sqrt(dot(N, N));
     N *= il;
     dndu = (n1 - n0) * il;
     dndv = (n2 - n0) * il;
@@ -334,68 +373,125 @@ static void mesh_normal_derivative(const Shape &m, const SI &si, V3 &dndu, V3 &d
     if (!m.UV.empty()) { uv0 = m.UV[i0]; uv1 = m.UV[i1]; uv2 = m.UV[i2]; }
     else { uv0 = {0.f, 0.f}; uv1 = {1.f, 0.f}; uv2 = {0.f, 1.f}; }
     V2 duv1{uv1.x - uv0.x, uv1.y - uv0.y}, duv2{uv2.x - uv0.x, uv2.y - uv0.y};
-    float id = 1.f / (duv1.x * duv2.y - duv1.y * duv2.x);
+    Float id = 1.f / (duv1.x * duv2.y - duv1.y * duv2.x);
     V3 a = (dndu * duv2.y - dndv * duv1.y) * id;
     V3 b = (dndv * duv1.x - dndu * duv2.x) * id;
     dndu = a;
     dndv = b;
 }
 
-/* ---- oracle BVH: median split, exact closest hit.  Any exact structure
- * gives the reference kd-tree's closest-hit result. */
-static void bvh_bounds(const Scene &sc, uint32_t prim, float lo[3], float hi[3], float c[3]) {
+/* ---- oracle BVH: binned SAH (16 bins per axis, leaves of at most 4
+ * triangles), exact closest hit.  Any exact structure gives the reference
+ * kd-tree's closest-hit result; the SAH split only makes the CPU baseline
+ * traverse fewer nodes. */
+static void bvh_bounds(const Scene &sc, uint32_t prim, Float lo[3], Float hi[3], Float c[3]) {
     const Shape &m = sc.shapes[sc.tri_shape[prim]];
     uint32_t f = sc.tri_face[prim];
     for (int k = 0; k < 3; ++k) { lo[k] = kInf; hi[k] = -kInf; }
     for (int j = 0; j < 3; ++j) {
         V3 p = m.P[m.F[3 * f + j]];
-        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); }
+        for (int k = 0; k < 3; ++k) { lo[k] = omin(lo[k], p[k]); hi[k] = omax(hi[k], p[k]); }
     }
     for (int k = 0; k < 3; ++k) c[k] = 0.5f * (lo[k] + hi[k]);
 }
 
-static int bvh_build_rec(Scene &sc, std::vector<uint32_t> &idx, std::vector<float> &cen,
+/* Half surface area of a box given as lo/hi arrays (doubles: build only). */
+static double bvh_half_area(const double lo[3], const double hi[3]) {
+    double d0 = hi[0] - lo[0], d1 = hi[1] - lo[1], d2 = hi[2] - lo[2];
+    if (d0 < 0 || d1 < 0 || d2 < 0) return 0.0;
+    return d0 * d1 + d1 * d2 + d2 * d0;
+}
+
+static int bvh_build_rec(Scene &sc, std::vector<uint32_t> &idx, std::vector<Float> &cen,
                          uint32_t first, uint32_t count, std::vector<BNode> &out) {
+    const int kBins = 16;
     BNode node;
     for (int k = 0; k < 3; ++k) { node.lo[k] = kInf; node.hi[k] = -kInf; }
-    float clo[3] = {kInf, kInf, kInf}, chi[3] = {-kInf, -kInf, -kInf};
+    Float clo[3] = {kInf, kInf, kInf}, chi[3] = {-kInf, -kInf, -kInf};
     for (uint32_t i = first; i < first + count; ++i) {
-        float lo[3], hi[3], c[3];
+        Float lo[3], hi[3], c[3];
         bvh_bounds(sc, idx[i], lo, hi, c);
         for (int k = 0; k < 3; ++k) {
-            node.lo[k] = std::min(node.lo[k], lo[k]); node.hi[k] = std::max(node.hi[k], hi[k]);
-            clo[k] = std::min(clo[k], c[k]); chi[k] = std::max(chi[k], c[k]);
+            node.lo[k] = omin(node.lo[k], lo[k]); node.hi[k] = omax(node.hi[k], hi[k]);
+            clo[k] = omin(clo[k], c[k]); chi[k] = omax(chi[k], c[k]);
         }
     }
-    /* pad so that float rounding in the slab test never drops a triangle that
+    /* pad so that Float rounding in the slab test never drops a triangle that
        the exact triangle test would accept */
     for (int k = 0; k < 3; ++k) {
-        float pad = 1e-6f * std::max(1.f, std::max(std::fabs(node.lo[k]), std::fabs(node.hi[k])));
+        Float pad = 1e-6f * omax(1.f, omax(std::fabs(node.lo[k]), std::fabs(node.hi[k])));
         node.lo[k] -= pad; node.hi[k] += pad;
     }
     int id = (int)out.size();
     out.push_back(node);
     if (count <= 4) { out[id].first = first; out[id].count = count; return id; }
-    int axis = 0;
-    for (int k = 1; k < 3; ++k) if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
-    uint32_t mid = first + count / 2;
-    std::nth_element(idx.begin() + first, idx.begin() + mid, idx.begin() + first + count,
-                     [&](uint32_t a, uint32_t b) {
-                         if (cen[3 * a + axis] != cen[3 * b + axis])
-                             return cen[3 * a + axis] < cen[3 * b + axis];
-                         return a < b;
-                     });
+    /* binned SAH over the centroid bounds */
+    int best_axis = -1, best_split = 0;
+    double best_cost = std::numeric_limits<double>::infinity();
+    for (int axis = 0; axis < 3; ++axis) {
+        double ext = (double)chi[axis] - (double)clo[axis];
+        if (!(ext > 0.0)) continue;
+        uint32_t cnt[kBins] = {};
+        double blo[kBins][3], bhi[kBins][3];
+        for (int b = 0; b < kBins; ++b)
+            for (int k = 0; k < 3; ++k) { blo[b][k] = 1e30; bhi[b][k] = -1e30; }
+        for (uint32_t i = first; i < first + count; ++i) {
+            int b = (int)(kBins * (((double)cen[3 * idx[i] + axis] - (double)clo[axis]) / ext));
+            b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+            Float lo[3], hi[3], c[3];
+            bvh_bounds(sc, idx[i], lo, hi, c);
+            ++cnt[b];
+            for (int k = 0; k < 3; ++k) {
+                blo[b][k] = std::min(blo[b][k], (double)lo[k]);
+                bhi[b][k] = std::max(bhi[b][k], (double)hi[k]);
+            }
+        }
+        double rarea[kBins]; uint32_t rcnt[kBins];
+        double acc_lo[3] = {1e30, 1e30, 1e30}, acc_hi[3] = {-1e30, -1e30, -1e30};
+        uint32_t acc = 0;
+        for (int b = kBins - 1; b > 0; --b) {
+            for (int k = 0; k < 3; ++k) { acc_lo[k] = std::min(acc_lo[k], blo[b][k]); acc_hi[k] = std::max(acc_hi[k], bhi[b][k]); }
+            acc += cnt[b];
+            rarea[b] = bvh_half_area(acc_lo, acc_hi); rcnt[b] = acc;
+        }
+        double l_lo[3] = {1e30, 1e30, 1e30}, l_hi[3] = {-1e30, -1e30, -1e30};
+        uint32_t lc = 0;
+        for (int b = 0; b < kBins - 1; ++b) {
+            for (int k = 0; k < 3; ++k) { l_lo[k] = std::min(l_lo[k], blo[b][k]); l_hi[k] = std::max(l_hi[k], bhi[b][k]); }
+            lc += cnt[b];
+            if (lc == 0 || rcnt[b + 1] == 0) continue;
+            double cost = bvh_half_area(l_lo, l_hi) * lc + rarea[b + 1] * rcnt[b + 1];
+            if (cost < best_cost) { best_cost = cost; best_axis = axis; best_split = b; }
+        }
+    }
+    uint32_t mid;
+    int axis = best_axis;
+    if (axis >= 0) {
+        double ext = (double)chi[axis] - (double)clo[axis];
+        auto it = std::partition(idx.begin() + first, idx.begin() + first + count, [&](uint32_t a) {
+            int b = (int)(kBins * (((double)cen[3 * a + axis] - (double)clo[axis]) / ext));
+            b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+            return b <= best_split;
+        });
+        mid = (uint32_t)(it - idx.begin());
+    } else {
+        /* every centroid coincides: split the range in half */
+        axis = 0;
+        mid = first + count / 2;
+    }
+    if (mid == first || mid == first + count) mid = first + count / 2;
     int l = bvh_build_rec(sc, idx, cen, first, mid - first, out);
     int r = bvh_build_rec(sc, idx, cen, mid, first + count - mid, out);
-    out[id].left = l; out[id].right = r; out[id].count = 0;
+    out[id].left = l; out[id].right = r; out[id].count = 0; out[id].axis = axis;
     return id;
 }
 
-static bool box_hit(const BNode &n, const Ray &r, float tmax) {
-    float t0 = r.mint, t1 = tmax;
+static bool box_hit(const BNode &n, const Ray &r, Float tmax) {
+    ORC_TRAVERSAL_SCOPE(false);
+    Float t0 = r.mint, t1 = tmax;
     for (int k = 0; k < 3; ++k) {
-        float inv = 1.f / r.d[k];
-        float a = (n.lo[k] - r.o[k]) * inv, b = (n.hi[k] - r.o[k]) * inv;
+        Float inv = 1.f / r.d[k];
+        Float a = (n.lo[k] - r.o[k]) * inv, b = (n.hi[k] - r.o[k]) * inv;
         if (a > b) std::swap(a, b);
         /* NaN (0 * inf) leaves the interval unchanged */
         if (a > t0) t0 = a;
@@ -415,12 +511,12 @@ static SI ray_intersect(const Scene &sc, const Ray &ray) {
     SI si;
     /* a NaN ray hits nothing (all intersection comparisons are false) */
     if (ray_is_nan(ray)) return si;
-    float best = ray.maxt;
-    int best_shape = -1; uint32_t best_prim = 0; float bu = 0.f, bv = 0.f;
+    Float best = ray.maxt;
+    int best_shape = -1; uint32_t best_prim = 0; Float bu = 0.f, bv = 0.f;
     bool hit = false;
     for (size_t s = 0; s < sc.shapes.size(); ++s) {
         if (sc.shapes[s].kind != 0) continue;
-        float t;
+        Float t;
         Ray r = ray; r.maxt = best;
         if (sphere_intersect(sc.shapes[s], r, t) && (!hit || t < best)) {
             best = t; best_shape = (int)s; hit = true;
@@ -434,15 +530,23 @@ static SI ray_intersect(const Scene &sc, const Ray &ray) {
             if (n.count) {
                 for (uint32_t i = n.first; i < n.first + n.count; ++i) {
                     const Shape &m = sc.shapes[sc.tri_shape[i]];
-                    float u, v, t;
+                    Float u, v, t;
                     Ray r = ray; r.maxt = best;
-                    if (tri_intersect(m, sc.tri_face[i], r, u, v, t) && (!hit || t < best)) {
+                    /* equal distances (a ray through a shared edge) go to the lower
+                       (shape, face) index, so the hit does not depend on the tree */
+                    if (tri_intersect(m, sc.tri_face[i], r, u, v, t) &&
+                        (!hit || t < best ||
+                         (t == best && best_shape >= 0 && sc.shapes[best_shape].kind != 0 &&
+                          ((int)sc.tri_shape[i] < best_shape ||
+                           ((int)sc.tri_shape[i] == best_shape && sc.tri_face[i] < best_prim))))) {
                         best = t; best_shape = (int)sc.tri_shape[i]; best_prim = sc.tri_face[i];
                         bu = u; bv = v; hit = true;
                     }
                 }
-            } else {
+            } else if (ray.d[n.axis] < 0.f) {   /* near child last, so it pops first */
                 stack[sp++] = n.left; stack[sp++] = n.right;
+            } else {
+                stack[sp++] = n.right; stack[sp++] = n.left;
             }
         }
     }
@@ -458,7 +562,7 @@ static SI ray_intersect(const Scene &sc, const Ray &ray) {
 static bool ray_test(const Scene &sc, const Ray &ray) {
     if (ray_is_nan(ray)) return false;
     for (const Shape &s : sc.shapes) {
-        float t;
+        Float t;
         if (s.kind == 0 && sphere_intersect(s, ray, t)) return true;
     }
     if (sc.nodes.empty()) return false;
@@ -468,7 +572,7 @@ static bool ray_test(const Scene &sc, const Ray &ray) {
         if (!box_hit(n, ray, ray.maxt)) continue;
         if (n.count) {
             for (uint32_t i = n.first; i < n.first + n.count; ++i) {
-                float u, v, t;
+                Float u, v, t;
                 if (tri_intersect(sc.shapes[sc.tri_shape[i]], sc.tri_face[i], ray, u, v, t)) return true;
             }
         } else { stack[sp++] = n.left; stack[sp++] = n.right; }
@@ -478,9 +582,9 @@ static bool ray_test(const Scene &sc, const Ray &ray) {
 
 /* ---- sampling: warp.h:153-156,262-267; mesh.cpp:541-586; distr_1d.h:144-201 */
 static V3 square_to_uniform_sphere(V2 s) {
-    float z = 1.f - 2.f * s.y;
-    float r = safe_sqrt(1.f - z * z);
-    float ang = 2.f * kPi * s.x;
+    Float z = 1.f - 2.f * s.y;
+    Float r = safe_sqrt(1.f - z * z);
+    Float ang = 2.f * kPi * s.x;
     return V3(r * std::cos(ang), r * std::sin(ang), z);
 }
 
@@ -491,7 +595,7 @@ static V3 sample_position(const Shape &s, V2 sample, V3 *n_out = nullptr) {
         return local * s.radius + s.center;
     }
     /* DiscreteDistribution::sample_reuse on sample.y */
-    float value = sample.y * s.area_sum;
+    Float value = sample.y * s.area_sum;
     uint32_t lo = s.valid_lo, hi = s.valid_hi;
     /* first index in [lo, hi] whose cdf >= value (hi if none) */
     while (lo < hi) {
@@ -499,11 +603,11 @@ static V3 sample_position(const Shape &s, V2 sample, V3 *n_out = nullptr) {
         if (s.cdf[mid] < value) lo = mid + 1; else hi = mid;
     }
     uint32_t f = lo;
-    float pmf = s.pmf[f] * s.area_norm;
-    float cdf_prev = f > 0 ? s.cdf[f - 1] * s.area_norm : 0.f;
-    float y = (sample.y - cdf_prev) / pmf;
-    float tq = safe_sqrt(1.f - sample.x);
-    float bx = 1.f - tq, by = tq * y;
+    Float pmf = s.pmf[f] * s.area_norm;
+    Float cdf_prev = f > 0 ? s.cdf[f - 1] * s.area_norm : Float(0.f);
+    Float y = (sample.y - cdf_prev) / pmf;
+    Float tq = safe_sqrt(1.f - sample.x);
+    Float bx = 1.f - tq, by = tq * y;
     V3 p0 = s.P[s.F[3 * f]], p1 = s.P[s.F[3 * f + 1]], p2 = s.P[s.F[3 * f + 2]];
     V3 e0 = p1 - p0, e1 = p2 - p0;
     if (n_out) {
@@ -520,7 +624,7 @@ static V3 sample_position(const Shape &s, V2 sample, V3 *n_out = nullptr) {
 /* include/mitsuba/render/manifold.h:50-141 */
 struct MVertex {
     V3 p, dp_du, dp_dv, n, gn, dn_du, dn_dv, s, t, ds_du, ds_dv, dt_du, dt_dv;
-    float eta = 1.f;
+    Float eta = 1.f;
     V2 uv;
     int shape = -1;
     bool fixed_direction = false;
@@ -529,7 +633,7 @@ struct MVertex {
 /* manifold.h:94-96: eta = real(ior) when imag(ior) == 0, else 1.  Conductors
  * with k = 0 therefore behave like dielectrics; non-specular BSDFs have
  * ior = (0, 1) (bsdf.cpp:58-60) -> 1. */
-static float bsdf_eta(const sms_bsdf &b) {
+static Float bsdf_eta(const sms_bsdf &b) {
     if (b.type == SMS_BSDF_DIELECTRIC) return b.eta;
     if (b.type == SMS_BSDF_CONDUCTOR && b.k == 0.f) return b.eta;
     return 1.f;
@@ -562,7 +666,7 @@ static bool nm_frames(const Scene &sc, int shape) {
 static void nm_vertex_frame(const Scene &sc, const SI &si, V3 n0, V3 dn0_du, V3 dn0_dv, bool coarse, V3 &n,
                             V3 &dn_du, V3 &dn_dv) {
     V3 s0 = si.dp_du - n0 * dot(n0, si.dp_du);
-    const float inv_len = 1.f / norm(s0);
+    const Float inv_len = 1.f / norm(s0);
     s0 *= inv_len;
     const V3 t0 = cross(n0, s0);
     V3 ds_du = (-dn0_du * dot(n0, si.dp_du) - n0 * dot(dn0_du, si.dp_du)) * inv_len;
@@ -572,7 +676,7 @@ static void nm_vertex_frame(const Scene &sc, const SI &si, V3 n0, V3 dn0_du, V3 
     const V3 dt_du = cross(dn0_du, s0) + cross(n0, ds_du), dt_dv = cross(dn0_dv, s0) + cross(n0, ds_dv);
     V3 nl, dl_du, dl_dv;
     if (coarse) {
-        const std::vector<float> &t = sc.nmap.lean.back();
+        const std::vector<Float> &t = sc.nmap.lean.back();
         nl = V3(-t[0], -t[1], 1.f);
         dl_du = V3(0.f); dl_dv = V3(0.f);
     } else {
@@ -583,7 +687,7 @@ static void nm_vertex_frame(const Scene &sc, const SI &si, V3 n0, V3 dn0_du, V3 
         dl_dv = V3(-dv.x, -dv.y, 0.f);
     }
     V3 wn = s0 * nl.x + t0 * nl.y + n0 * nl.z;
-    const float il = 1.f / norm(wn);
+    const Float il = 1.f / norm(wn);
     wn *= il;
     V3 a = (s0 * dl_du.x + t0 * dl_du.y + n0 * dl_du.z + ds_du * nl.x + dt_du * nl.y + dn0_du * nl.z) * il;
     V3 b = (s0 * dl_dv.x + t0 * dl_dv.y + n0 * dl_dv.z + ds_dv * nl.x + dt_dv * nl.y + dn0_dv * nl.z) * il;
@@ -602,7 +706,7 @@ static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v, bool nm_co
     V3 n = si.shn;
     V3 dndu, dndv;
     if (sh.kind == 0) {
-        float inv_r = (sh.flip ? -1.f : 1.f) / sh.radius;   /* sphere.cpp:376-382 */
+        Float inv_r = (sh.flip ? -1.f : 1.f) / sh.radius;   /* sphere.cpp:376-382 */
         dndu = si.dp_du * inv_r; dndv = si.dp_dv * inv_r;
     } else {
         mesh_normal_derivative(sh, si, dndu, dndv);
@@ -611,7 +715,7 @@ static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v, bool nm_co
     V3 s = normalize(si.dp_du - n * dot(n, si.dp_du));
     v.n = n; v.s = s; v.t = cross(n, s);
     V3 s0 = si.dp_du - n * dot(n, si.dp_du);
-    float inv_len_s = 1.f / norm(s0);
+    Float inv_len_s = 1.f / norm(s0);
     s0 *= inv_len_s;
     V3 dsdu = (-dndu * dot(n, si.dp_du) - n * dot(dndu, si.dp_du)) * inv_len_s;
     V3 dsdv = (-dndv * dot(n, si.dp_du) - n * dot(dndv, si.dp_du)) * inv_len_s;
@@ -626,9 +730,9 @@ static void vertex_from_si(const Scene &sc, const SI &si, MVertex &v, bool nm_co
 
 /* manifold.h:115-126 */
 static void make_orthonormal(MVertex &v) {
-    float inv = 1.f / norm(v.dp_du);
+    Float inv = 1.f / norm(v.dp_du);
     v.dp_du *= inv; v.dn_du *= inv;
-    float dp = dot(v.dp_du, v.dp_dv);
+    Float dp = dot(v.dp_du, v.dp_dv);
     V3 a = v.dp_dv - v.dp_du * dp, b = v.dn_dv - v.dn_du * dp;
     inv = 1.f / norm(a);
     v.dp_dv = a * inv; v.dn_dv = b * inv;
@@ -637,7 +741,7 @@ static void make_orthonormal(MVertex &v) {
 /* ------------------------------------------------ emitter interaction */
 struct EI {
     V3 p, n, d, weight;
-    float pdf = 0.f;
+    Float pdf = 0.f;
     int emitter = -1;
     bool is_point = false, is_area = false;
 };
@@ -646,26 +750,26 @@ struct EI {
 /* manifold.h:348-418 */
 static bool reflect(V3 w, V3 n, V3 &out) { out = n * (2.f * dot(w, n)) - w; return true; }
 static void d_reflect(V3 w, V3 dwdu, V3 dwdv, V3 n, V3 dndu, V3 dndv, V3 &ou, V3 &ov) {
-    float dwn = dot(w, n), dun = dot(dwdu, n), dvn = dot(dwdv, n), wdu = dot(w, dndu),
+    Float dwn = dot(w, n), dun = dot(dwdu, n), dvn = dot(dwdv, n), wdu = dot(w, dndu),
           wdv = dot(w, dndv);
     ou = ((n * (dun + wdu)) + dndu * dwn) * 2.f - dwdu;
     ov = ((n * (dvn + wdv)) + dndv * dwn) * 2.f - dwdv;
 }
-static bool refract(V3 w, V3 n, float eta_, V3 &out) {
-    float eta = 1.f / eta_;
+static bool refract(V3 w, V3 n, Float eta_, V3 &out) {
+    Float eta = 1.f / eta_;
     if (dot(w, n) < 0.f) { eta = 1.f / eta; n = -n; }
-    float dwn = dot(w, n);
-    float root = 1.f - eta * eta * (1.f - dwn * dwn);
+    Float dwn = dot(w, n);
+    Float root = 1.f - eta * eta * (1.f - dwn * dwn);
     if (root < 0.f) { out = V3(0.f); return false; }
     out = -(w - n * dwn) * eta - n * std::sqrt(root);
     return true;
 }
-static void d_refract(V3 w, V3 dwdu, V3 dwdv, V3 n, V3 dndu, V3 dndv, float eta_, V3 &ou, V3 &ov) {
-    float eta = 1.f / eta_;
+static void d_refract(V3 w, V3 dwdu, V3 dwdv, V3 n, V3 dndu, V3 dndv, Float eta_, V3 &ou, V3 &ov) {
+    Float eta = 1.f / eta_;
     if (dot(w, n) < 0.f) { eta = 1.f / eta; n = -n; dndu = -dndu; dndv = -dndv; }
-    float dwn = dot(w, n), dun = dot(dwdu, n), dvn = dot(dwdv, n), wdu = dot(w, dndu),
+    Float dwn = dot(w, n), dun = dot(dwdu, n), dvn = dot(dwdv, n), wdu = dot(w, dndu),
           wdv = dot(w, dndv);
-    float root = std::sqrt(1.f - eta * eta * (1.f - dwn * dwn));
+    Float root = std::sqrt(1.f - eta * eta * (1.f - dwn * dwn));
     V3 a_u = -(dwdu - (n * (dun + wdu) + dndu * dwn)) * eta;
     V3 b_u = -(dndu * root + n * (1.f / (2.f * root)) * (-eta * eta * (-2.f * dwn * (dun + wdu))));
     V3 a_v = -(dwdv - (n * (dvn + wdv) + dndv * dwn)) * eta;
@@ -674,18 +778,18 @@ static void d_refract(V3 w, V3 dwdu, V3 dwdv, V3 n, V3 dndu, V3 dndv, float eta_
     ov = a_v + b_v;
 }
 /* manifold.h:420-443 */
-static void sphcoords(V3 w, float &theta, float &phi) {
+static void sphcoords(V3 w, Float &theta, Float &phi) {
     theta = safe_acos(w.z);
     phi = std::atan2(w.y, w.x);
     if (phi < 0.f) phi += 2.f * kPi;
 }
-static void d_sphcoords(V3 w, V3 dwdu, V3 dwdv, float &dtu, float &dpu, float &dtv, float &dpv) {
-    float d_acos = -1.f / safe_sqrt(1.f - w.z * w.z);
+static void d_sphcoords(V3 w, V3 dwdu, V3 dwdv, Float &dtu, Float &dpu, Float &dtv, Float &dpv) {
+    Float d_acos = -1.f / safe_sqrt(1.f - w.z * w.z);
     dtu = d_acos * dwdu.z;
     dtv = d_acos * dwdv.z;
-    float yx = w.y / w.x;
-    float d_atan = 1.f / (1.f + yx * yx);
-    float inv = 1.f / (w.x * w.x);
+    Float yx = w.y / w.x;
+    Float d_atan = 1.f / (1.f + yx * yx);
+    Float inv = 1.f / (w.x * w.x);
     dpu = d_atan * (w.x * dwdu.y - w.y * dwdu.x) * inv;
     dpv = d_atan * (w.x * dwdv.y - w.y * dwdv.x) * inv;
     if (w.x == 0.f) { dpu = 0.f; dpv = 0.f; }
@@ -696,13 +800,13 @@ static void d_sphcoords(V3 w, V3 dwdu, V3 dwdv, float &dtu, float &dpu, float &d
 static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr,
                            V3 no = V3(0.f, 0.f, 1.f)) {
     V3 wi = x - v1.p;
-    float ili = norm(wi);
+    Float ili = norm(wi);
     if (ili < 1e-3f) return false;
     ili = 1.f / ili; wi *= ili;
     V3 dwi_du = (v1.dp_du - wi * dot(wi, v1.dp_du)) * -ili;
     V3 dwi_dv = (v1.dp_dv - wi * dot(wi, v1.dp_dv)) * -ili;
     V3 wo = ei.p - v1.p;
-    float ilo = norm(wo);
+    Float ilo = norm(wo);
     if (ilo < 1e-3f) return false;
     ilo = 1.f / ilo; wo *= ilo;
     V3 dwo_du = (v1.dp_du - wo * dot(wo, v1.dp_du)) * -ilo;
@@ -728,12 +832,12 @@ static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX,
     if (transform(wi, wio)) {
         V3 dwio_du, dwio_dv;
         d_transform(wi, dwi_du, dwi_dv, dwio_du, dwio_dv);
-        float to, po, tio, pio;
+        Float to, po, tio, pio;
         sphcoords(wo, to, po); sphcoords(wio, tio, pio);
-        float dt = to - tio, dp = po - pio;
+        Float dt = to - tio, dp = po - pio;
         if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
         C = V2{dt, dp};
-        float a0, a1, a2, a3, b0, b1, b2, b3;
+        Float a0, a1, a2, a3, b0, b1, b2, b3;
         d_sphcoords(wo, dwo_du, dwo_dv, a0, a1, a2, a3);
         d_sphcoords(wio, dwio_du, dwio_dv, b0, b1, b2, b3);
         J.m[0][0] = a0 - b0; J.m[1][0] = a1 - b1; J.m[0][1] = a2 - b2; J.m[1][1] = a3 - b3;
@@ -743,19 +847,19 @@ static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX,
     if (transform(wo, woi) && !success) {
         V3 dwoi_du, dwoi_dv;
         d_transform(wo, dwo_du, dwo_dv, dwoi_du, dwoi_dv);
-        float ti, pi, toi, poi;
+        Float ti, pi, toi, poi;
         sphcoords(wi, ti, pi); sphcoords(woi, toi, poi);
-        float dt = ti - toi, dp = pi - poi;
+        Float dt = ti - toi, dp = pi - poi;
         if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
         C = V2{dt, dp};
-        float a0, a1, a2, a3, b0, b1, b2, b3;
+        Float a0, a1, a2, a3, b0, b1, b2, b3;
         d_sphcoords(wi, dwi_du, dwi_dv, a0, a1, a2, a3);
         d_sphcoords(woi, dwoi_du, dwoi_dv, b0, b1, b2, b3);
         J.m[0][0] = a0 - b0; J.m[1][0] = a1 - b1; J.m[0][1] = a2 - b2; J.m[1][1] = a3 - b3;
         success = true;
     }
     if (J_out) *J_out = J;
-    float d = det(J);
+    Float d = det(J);
     if (std::fabs(d) < 1e-6f) return false;
     dX = mul(inverse(J), C);
     return success;
@@ -765,18 +869,18 @@ static bool step_anglediff(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX,
 static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX, M2 *J_out = nullptr,
                             V3 no = V3(0.f, 0.f, 1.f)) {
     V3 wo = ei.p - v1.p;
-    float ilo = norm(wo);
+    Float ilo = norm(wo);
     if (ilo < 1e-3f) return false;
     ilo = 1.f / ilo; wo *= ilo;
     V3 wi = x - v1.p;
-    float ili = norm(wi);
+    Float ili = norm(wi);
     if (ili < 1e-3f) return false;
     ili = 1.f / ili; wi *= ili;
-    float eta = v1.eta;
+    Float eta = v1.eta;
     if (dot(wi, v1.gn) < 0.f) eta = 1.f / eta;
     V3 h = wi + wo * eta;
     if (eta != 1.f) h *= -1.f;
-    float ilh = 1.f / norm(h);
+    Float ilh = 1.f / norm(h);
     h *= ilh;
     ilo *= eta * ilh;
     ili *= ilh;
@@ -791,7 +895,7 @@ static bool step_halfvector(V3 x, const MVertex &v1, const EI &ei, V2 &C, V2 &dX
     J.m[0][1] = dot(v1.ds_dv, h) + dot(v1.s, dh_dv);
     J.m[1][1] = dot(v1.dt_dv, h) + dot(v1.t, dh_dv);
     if (J_out) { *J_out = J; C = V2{dot(v1.s, h) - no.x, dot(v1.t, h) - no.y}; }
-    float d = det(J);
+    Float d = det(J);
     if (std::fabs(d) < 1e-6f) return false;
     C = V2{dot(v1.s, h) - no.x, dot(v1.t, h) - no.y};   /* H - N (manifold_ss.cpp:485-488) */
     dX = mul(inverse(J), C);
@@ -811,7 +915,7 @@ static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MV
     MVertex vtx = init;
     bool success = false;
     int it = 0;
-    float beta = 1.f;
+    Float beta = 1.f;
     SI si_current;
     while (it < cfg.max_iterations) {
         V2 C, dX;
@@ -827,7 +931,7 @@ static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MV
             it += 1;
             continue;
         }
-        beta = std::min(1.f, 2.f * beta);
+        beta = omin(1.f, 2.f * beta);
         vertex_from_si(sc, si_current, vtx, coarse);
         it++;
     }
@@ -836,7 +940,7 @@ static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MV
     if (!success) return false;
     V3 wx = normalize(x - vtx.p);
     V3 wy = normalize(ei.p - vtx.p);
-    float cx = dot(vtx.gn, wx), cy = dot(vtx.gn, wy);
+    Float cx = dot(vtx.gn, wx), cy = dot(vtx.gn, wy);
     bool refraction = cx * cy < 0.f;
     bool reflection = !refraction;
     if ((vtx.eta == 1.f && !reflection) || (vtx.eta != 1.f && !refraction)) return false;
@@ -846,7 +950,7 @@ static bool newton_solver(const Scene &sc, const sms_config &cfg, V3 x, const MV
 /* ----------------------------------------------------------- query */
 struct Query {
     V3 p, n, dp_du, dp_dv, albedo;
-    float cos_i = 1.f;
+    Float cos_i = 1.f;
 };
 
 static Query load_query(const float *q, uint32_t n, uint32_t i) {
@@ -860,13 +964,13 @@ static Query load_query(const float *q, uint32_t n, uint32_t i) {
 
 /* sample_gaussian (manifold.h:326-345) through square_to_std_normal
  * (warp.h:184-190): a slope from N(mu, sigma), sigma = (a, c; c, b). */
-static V2 sample_slope_gaussian(V2 mu, float a, float b, float c, V2 u) {
-    const float r = std::sqrt(-2.f * std::log(1.f - u.x)), ph = 2.f * kPi * u.y;
-    const float px = std::cos(ph) * r, py = std::sin(ph) * r;
-    const float sx = std::sqrt(a), sy = std::sqrt(b);
-    const float rho = c / (sx * sy);
-    const float ka = std::sqrt(1.f + rho), kb = std::sqrt(1.f - rho);
-    const float d0 = 0.5f * ka + 0.5f * kb, d1 = 0.5f * ka - 0.5f * kb;
+static V2 sample_slope_gaussian(V2 mu, Float a, Float b, Float c, V2 u) {
+    const Float r = std::sqrt(-2.f * std::log(1.f - u.x)), ph = 2.f * kPi * u.y;
+    const Float px = std::cos(ph) * r, py = std::sin(ph) * r;
+    const Float sx = std::sqrt(a), sy = std::sqrt(b);
+    const Float rho = c / (sx * sy);
+    const Float ka = std::sqrt(1.f + rho), kb = std::sqrt(1.f - rho);
+    const Float d0 = 0.5f * ka + 0.5f * kb, d1 = 0.5f * ka - 0.5f * kb;
     return V2{(d0 * px + d1 * py) * sx + mu.x, (d1 * px + d0 * py) * sy + mu.y};
 }
 
@@ -893,9 +997,9 @@ static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, cons
     vertex_from_si(sc, si_init, v0, cfg.twostage != 0);
     int it1 = 0;
     if (cfg.twostage) {
-        const std::vector<float> &t = sc.nmap.lean.back();
-        const float a = std::max(0.f, t[2] - t[0] * t[0]), b = std::max(0.f, t[3] - t[1] * t[1]),
-                    c = std::max(0.f, t[4] - t[0] * t[1]);
+        const std::vector<Float> &t = sc.nmap.lean.back();
+        const Float a = omax(0.f, t[2] - t[0] * t[0]), b = omax(0.f, t[3] - t[1] * t[1]),
+                    c = omax(0.f, t[4] - t[0] * t[1]);
         const V2 mu{0.5f * (t[0] - no.x / no.z), 0.5f * (t[1] - no.y / no.z)};
         const V2 sl = sample_slope_gaussian(mu, a, b, c, g);
         const V3 ln = normalize(V3(-sl.x, -sl.y, 1.f));
@@ -913,9 +1017,9 @@ static bool sample_path(const Scene &sc, const sms_config &cfg, int caster, cons
 static EI sample_emitter_interaction(const Scene &sc, const std::vector<int> &em, const Query &q, PCG32 &rng) {
     EI ei;
     if (em.empty()) return ei;
-    float es = rng.next_f32();
-    float emitter_pdf = 1.f / (float)em.size();
-    uint32_t idx = std::min((uint32_t)(es * (float)em.size()), (uint32_t)em.size() - 1);
+    Float es = rng.next_f32();
+    Float emitter_pdf = 1.f / (Float)em.size();
+    uint32_t idx = omin((uint32_t)(es * (Float)em.size()), (uint32_t)em.size() - 1);
     const Emitter &e = sc.emitters[em[idx]];
     ei.emitter = em[idx];
     V3 spec(0.f);
@@ -924,8 +1028,8 @@ static EI sample_emitter_interaction(const Scene &sc, const std::vector<int> &em
         const Shape &s = sc.shapes[e.shape];
         V3 n;
         V3 p = sample_position(s, rng.next_2d(), &n);
-        float area = 4.f * kPi * s.radius * s.radius;
-        float pdf = 1.f / area;
+        Float area = 4.f * kPi * s.radius * s.radius;
+        Float pdf = 1.f / area;
         /* area.cpp:71-79 with wi = (0,0,1): cos_theta > 0 -> radiance */
         spec = V3(e.radiance.x / pdf, e.radiance.y / pdf, e.radiance.z / pdf);
         ei.p = p; ei.n = n; ei.d = normalize(p - q.p); ei.pdf = pdf;
@@ -933,8 +1037,8 @@ static EI sample_emitter_interaction(const Scene &sc, const std::vector<int> &em
         ei.is_point = true;
         (void)rng.next_2d(); /* point.cpp:74-100 consumes a 2D sample */
         V3 d = e.p - q.p;
-        float dist = norm(d);
-        float inv = 1.f / dist;
+        Float dist = norm(d);
+        Float inv = 1.f / dist;
         d *= inv;
         V3 s = e.radiance * (inv * inv);
         ei.p = e.p; ei.d = d; ei.n = d; ei.pdf = 1.f;
@@ -946,48 +1050,48 @@ static EI sample_emitter_interaction(const Scene &sc, const std::vector<int> &em
 }
 
 /* fresnel.h:34-80 */
-static float fresnel(float cos_i, float eta, float *cos_t_out = nullptr) {
+static Float fresnel(Float cos_i, Float eta, Float *cos_t_out = nullptr) {
     bool outside = cos_i >= 0.f;
-    float rcp_eta = 1.f / eta;
-    float eta_it = outside ? eta : rcp_eta, eta_ti = outside ? rcp_eta : eta;
-    float ct2 = 1.f - (1.f - cos_i * cos_i) * (eta_ti * eta_ti);
-    float ci = std::fabs(cos_i), ct = safe_sqrt(ct2);
+    Float rcp_eta = 1.f / eta;
+    Float eta_it = outside ? eta : rcp_eta, eta_ti = outside ? rcp_eta : eta;
+    Float ct2 = 1.f - (1.f - cos_i * cos_i) * (eta_ti * eta_ti);
+    Float ci = std::fabs(cos_i), ct = safe_sqrt(ct2);
     bool index_matched = eta == 1.f;
     bool special = index_matched || ci == 0.f;
-    float r_sc = index_matched ? 0.f : 1.f;
-    float a_s = (ci - eta_it * ct) / (ci + eta_it * ct);
-    float a_p = (ct - eta_it * ci) / (ct + eta_it * ci);
-    float r = 0.5f * (a_s * a_s + a_p * a_p);
+    Float r_sc = index_matched ? 0.f : 1.f;
+    Float a_s = (ci - eta_it * ct) / (ci + eta_it * ct);
+    Float a_p = (ct - eta_it * ci) / (ct + eta_it * ci);
+    Float r = 0.5f * (a_s * a_s + a_p * a_p);
     if (special) r = r_sc;
     if (cos_t_out) *cos_t_out = cos_i >= 0.f ? -ct : ct;
     return r;
 }
 /* fresnel.h:92-120 */
-static float fresnel_conductor(float cos_i, float er, float ei_) {
-    float c2 = cos_i * cos_i, s2 = 1.f - c2, s4 = s2 * s2;
-    float t1 = er * er - ei_ * ei_ - s2;
-    float a2pb2 = safe_sqrt(t1 * t1 + 4.f * ei_ * ei_ * er * er);
-    float a = safe_sqrt(0.5f * (a2pb2 + t1));
-    float term1 = a2pb2 + c2, term2 = 2.f * cos_i * a;
-    float rs = (term1 - term2) / (term1 + term2);
-    float term3 = a2pb2 * c2 + s4, term4 = term2 * s2;
-    float rp = rs * (term3 - term4) / (term3 + term4);
+static Float fresnel_conductor(Float cos_i, Float er, Float ei_) {
+    Float c2 = cos_i * cos_i, s2 = 1.f - c2, s4 = s2 * s2;
+    Float t1 = er * er - ei_ * ei_ - s2;
+    Float a2pb2 = safe_sqrt(t1 * t1 + 4.f * ei_ * ei_ * er * er);
+    Float a = safe_sqrt(0.5f * (a2pb2 + t1));
+    Float term1 = a2pb2 + c2, term2 = 2.f * cos_i * a;
+    Float rs = (term1 - term2) / (term1 + term2);
+    Float term3 = a2pb2 * c2 + s4, term4 = term2 * s2;
+    Float rp = rs * (term3 - term4) / (term3 + term4);
     return 0.5f * (rs + rp);
 }
 
 /* manifold_ss.cpp:638-693 (smooth BSDFs) */
-static float specular_reflectance(const Scene &sc, const SI &si, V3 wo) {
+static Float specular_reflectance(const Scene &sc, const SI &si, V3 wo) {
     if (!si.valid()) return 0.f;
     const sms_bsdf &b = sc.shapes[si.shape].bsdf;
     V3 n = si.shn;
-    float cos_theta = dot(n, wo);
+    Float cos_theta = dot(n, wo);
     if (b.type == SMS_BSDF_CONDUCTOR && b.k != 0.f)
         return fresnel_conductor(std::fabs(cos_theta), b.eta, b.k);
     if (b.type == SMS_BSDF_DIELECTRIC || b.type == SMS_BSDF_CONDUCTOR) {
         /* real ior: the "reflection" mask is false -> transmission branch */
-        float eta = b.eta;
+        Float eta = b.eta;
         if (cos_theta < 0.f) eta = 1.f / eta;
-        float F = fresnel(cos_theta, eta);
+        Float F = fresnel(cos_theta, eta);
         return (1.f - F) * eta * eta;
     }
     /* diffuse: ior (0,1) has a nonzero imaginary part -> conductor formula */
@@ -997,51 +1101,51 @@ static float specular_reflectance(const Scene &sc, const SI &si, V3 wo) {
 /* ---- isotropic Beckmann microfacets (include/mitsuba/render/microfacet.h):
  * D(m) with its underflow cut-off; Smith G1 by the rational approximation of
  * Walter et al. 2007 (eq. 27); sampling of m with density D(m) cos(theta_m). */
-static float beckmann_D(V3 m, float alpha) {
-    float c2 = m.z * m.z;
-    float r = std::exp(-((m.x * m.x + m.y * m.y) / (alpha * alpha)) / c2) / (kPi * alpha * alpha * c2 * c2);
-    return r * m.z > 1e-20f ? r : 0.f;
+static Float beckmann_D(V3 m, Float alpha) {
+    Float c2 = m.z * m.z;
+    Float r = std::exp(-((m.x * m.x + m.y * m.y) / (alpha * alpha)) / c2) / (kPi * alpha * alpha * c2 * c2);
+    return r * m.z > 1e-20f ? r : Float(0.f);
 }
-static float beckmann_G1(V3 v, V3 m, float alpha) {
-    float xy = alpha * alpha * (v.x * v.x + v.y * v.y);
-    float r = 1.f;
+static Float beckmann_G1(V3 v, V3 m, Float alpha) {
+    Float xy = alpha * alpha * (v.x * v.x + v.y * v.y);
+    Float r = 1.f;
     if (xy != 0.f) {
-        float a = 1.f / std::sqrt(xy / (v.z * v.z)), a2 = a * a;
-        r = a >= 1.6f ? 1.f : (3.535f * a + 2.181f * a2) / (1.f + 2.276f * a + 2.577f * a2);
+        Float a = 1.f / std::sqrt(xy / (v.z * v.z)), a2 = a * a;
+        r = a >= 1.6f ? Float(1.f) : (3.535f * a + 2.181f * a2) / (1.f + 2.276f * a + 2.577f * a2);
     }
-    return dot(v, m) * v.z <= 0.f ? 0.f : r;
+    return dot(v, m) * v.z <= 0.f ? Float(0.f) : r;
 }
-static V3 beckmann_sample(float alpha, float u0, float u1, float &pdf) {
-    float ang = 2.f * kPi * u1;
-    float sp = std::sin(ang), cp = std::cos(ang);
-    float ct = 1.f / std::sqrt(1.f - alpha * alpha * std::log(1.f - u0));
-    float c2 = ct * ct;
-    pdf = (1.f - u0) / (kPi * alpha * alpha * std::max(c2 * ct, 1e-20f));
-    float st = std::sqrt(1.f - c2);
+static V3 beckmann_sample(Float alpha, Float u0, Float u1, Float &pdf) {
+    Float ang = 2.f * kPi * u1;
+    Float sp = std::sin(ang), cp = std::cos(ang);
+    Float ct = 1.f / std::sqrt(1.f - alpha * alpha * std::log(1.f - u0));
+    Float c2 = ct * ct;
+    pdf = (1.f - u0) / (kPi * alpha * alpha * omax(c2 * ct, 1e-20f));
+    Float st = std::sqrt(1.f - c2);
     return V3(cp * st, sp * st, ct);
 }
 /* roughconductor.cpp eval (value x cos_theta_o), local frame */
-static float roughconductor_eval(float alpha, float er, float ek, V3 wi, V3 wo) {
+static Float roughconductor_eval(Float alpha, Float er, Float ek, V3 wi, V3 wo) {
     if (!(wi.z > 0.f && wo.z > 0.f)) return 0.f;
     V3 h = normalize(wo + wi);
-    float D = beckmann_D(h, alpha);
+    Float D = beckmann_D(h, alpha);
     if (D == 0.f) return 0.f;
-    float G = beckmann_G1(wi, h, alpha) * beckmann_G1(wo, h, alpha);
+    Float G = beckmann_G1(wi, h, alpha) * beckmann_G1(wo, h, alpha);
     return D * G / (4.f * wi.z) * fresnel_conductor(dot(wi, h), er, ek);
 }
 /* roughdielectric.cpp eval (value x |cos_theta_o|, radiance transport), local frame */
-static float roughdielectric_eval(float alpha, float eta_, V3 wi, V3 wo) {
-    const float ci = wi.z, co = wo.z;
+static Float roughdielectric_eval(Float alpha, Float eta_, V3 wi, V3 wo) {
+    const Float ci = wi.z, co = wo.z;
     if (ci == 0.f) return 0.f;
     const bool reflect = ci * co > 0.f;
-    const float eta = ci > 0.f ? eta_ : 1.f / eta_, inv_eta = ci > 0.f ? 1.f / eta_ : eta_;
-    V3 m = normalize(wi + wo * (reflect ? 1.f : eta));
+    const Float eta = ci > 0.f ? eta_ : 1.f / eta_, inv_eta = ci > 0.f ? 1.f / eta_ : eta_;
+    V3 m = normalize(wi + wo * (reflect ? Float(1.f) : eta));
     if (m.z < 0.f) m = -m;
-    float D = beckmann_D(m, alpha);
-    float F = fresnel(dot(wi, m), eta_);
-    float G = beckmann_G1(wi, m, alpha) * beckmann_G1(wo, m, alpha);
+    Float D = beckmann_D(m, alpha);
+    Float F = fresnel(dot(wi, m), eta_);
+    Float G = beckmann_G1(wi, m, alpha) * beckmann_G1(wo, m, alpha);
     if (reflect) return F * D * G / (4.f * std::fabs(ci));
-    float den = dot(wi, m) + eta * dot(wo, m);
+    Float den = dot(wi, m) + eta * dot(wo, m);
     return std::fabs((inv_eta * inv_eta) * (1.f - F) * D * G * eta * eta * dot(wi, m) * dot(wo, m) /
                      (ci * den * den));
 }
@@ -1051,7 +1155,7 @@ static float roughdielectric_eval(float alpha, float eta_, V3 wi, V3 wo) {
  * evaluates the nested BSDF in the perturbed frame and keeps wo only on the
  * same side of the perturbed and the unperturbed normal; the half-vector
  * factor flips eta by the side of wi in the unperturbed frame (si.wi). */
-static float specular_reflectance_rough(const Scene &sc, const SI &si, V3 wi_w, V3 wo_w) {
+static Float specular_reflectance_rough(const Scene &sc, const SI &si, V3 wi_w, V3 wo_w) {
     const sms_bsdf &b = sc.shapes[si.shape].bsdf;
     const bool nm = nm_frames(sc, si.shape);
     V3 n = si.shn;
@@ -1066,47 +1170,47 @@ static float specular_reflectance_rough(const Scene &sc, const SI &si, V3 wi_w, 
     V3 wo(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
     if (nm && !(dot(wo_w, si.shn) * wo.z > 0.f)) return 0.f;
     if (b.type == SMS_BSDF_CONDUCTOR && b.k != 0.f) {
-        float f = roughconductor_eval(b.alpha, b.eta, b.k, wi, wo);
+        Float f = roughconductor_eval(b.alpha, b.eta, b.k, wi, wo);
         V3 h = normalize(wi + wo);
         return f * 4.f * std::fabs(dot(wo, h));
     }
-    float f = b.type == SMS_BSDF_CONDUCTOR ? roughconductor_eval(b.alpha, b.eta, b.k, wi, wo)
+    Float f = b.type == SMS_BSDF_CONDUCTOR ? roughconductor_eval(b.alpha, b.eta, b.k, wi, wo)
                                            : roughdielectric_eval(b.alpha, b.eta, wi, wo);
-    float eta = b.eta;
+    Float eta = b.eta;
     if ((nm ? dot(wi_w, si.shn) : wi.z) < 0.f) eta = 1.f / eta;
     V3 h = -normalize(wi + wo * eta);
-    float a = dot(wi, h) + eta * dot(wo, h);
+    Float a = dot(wi, h) + eta * dot(wo, h);
     return f * a * a / (eta * eta * std::fabs(dot(wo, h)));
 }
 
 static bool is_rough(const sms_bsdf &b) { return b.type != SMS_BSDF_DIFFUSE && b.alpha > 0.f; }
 
 /* manifold_ss.cpp:695-857 */
-static float geometric_term(const MVertex &v0, const MVertex &v1, const MVertex &v2) {
+static Float geometric_term(const MVertex &v0, const MVertex &v1, const MVertex &v2) {
     V3 wi = v0.p - v1.p;
-    float ili = norm(wi);
+    Float ili = norm(wi);
     if (ili < 1e-3f) return 0.f;
     ili = 1.f / ili; wi *= ili;
     V3 wo = v2.p - v1.p;
-    float ilo = norm(wo);
+    Float ilo = norm(wo);
     if (ilo < 1e-3f) return 0.f;
     ilo = 1.f / ilo; wo *= ilo;
-    float eta = v1.eta;
+    Float eta = v1.eta;
     if (dot(wi, v1.gn) < 0.f) eta = 1.f / eta;
     V3 h = wi + wo * eta;
     if (eta != 1.f) h *= -1.f;
-    float ilh = 1.f / norm(h);
+    Float ilh = 1.f / norm(h);
     h *= ilh;
     ilo *= eta * ilh;
     ili *= ilh;
-    float dpdu_n = dot(v1.dp_du, v1.n), dpdv_n = dot(v1.dp_dv, v1.n);
+    Float dpdu_n = dot(v1.dp_du, v1.n), dpdv_n = dot(v1.dp_dv, v1.n);
     V3 s = v1.dp_du - v1.n * dpdu_n, t = v1.dp_dv - v1.n * dpdv_n;
     V3 dh_du = -v1.dp_du * (ili + ilo) + wi * (dot(wi, v1.dp_du) * ili) + wo * (dot(wo, v1.dp_du) * ilo);
     V3 dh_dv = -v1.dp_dv * (ili + ilo) + wi * (dot(wi, v1.dp_dv) * ili) + wo * (dot(wo, v1.dp_dv) * ilo);
     dh_du -= h * dot(dh_du, h);
     dh_dv -= h * dot(dh_dv, h);
     if (eta != 1.f) { dh_du *= -1.f; dh_dv *= -1.f; }
-    float hn = dot(h, v1.n), hdu = dot(h, v1.dn_du), hdv = dot(h, v1.dn_dv);
+    Float hn = dot(h, v1.n), hdu = dot(h, v1.dn_du), hdv = dot(h, v1.dn_dv);
     M2 d11;
     d11.m[0][0] = dot(dh_du, s) - dot(v1.dp_du, v1.dn_du) * hn - dpdu_n * hdu;
     d11.m[0][1] = dot(dh_dv, s) - dot(v1.dp_du, v1.dn_dv) * hn - dpdu_n * hdv;
@@ -1120,14 +1224,14 @@ static float geometric_term(const MVertex &v0, const MVertex &v1, const MVertex 
     M2 d12;
     d12.m[0][0] = dot(dh_du, s); d12.m[0][1] = dot(dh_dv, s);
     d12.m[1][0] = dot(dh_du, t); d12.m[1][1] = dot(dh_dv, t);
-    float d = det(d11);
+    Float d = det(d11);
     if (std::fabs(d) < 1e-6f) return 0.f;
-    float dx1_dx2 = std::fabs(det(mul(inverse(d11), d12)));
-    dx1_dx2 = std::min(dx1_dx2, 1.f);
+    Float dx1_dx2 = std::fabs(det(mul(inverse(d11), d12)));
+    dx1_dx2 = omin(dx1_dx2, 1.f);
     V3 dd = v0.p - v1.p;
-    float inv_r2 = 1.f / dot(dd, dd);
+    Float inv_r2 = 1.f / dot(dd, dd);
     dd *= std::sqrt(inv_r2);
-    float dw0_dx1 = std::fabs(dot(dd, v1.gn)) * inv_r2;
+    Float dw0_dx1 = std::fabs(dot(dd, v1.gn)) * inv_r2;
     return dw0_dx1 * dx1_dx2;
 }
 
@@ -1160,12 +1264,12 @@ static V3 evaluate_path_contribution(const Scene &sc, const Query &q, const EI &
     if (ei.is_point) {
         const Emitter &e = sc.emitters[ei.emitter];
         V3 d = e.p - si_final.p;
-        float dist = norm(d);
-        float inv = 1.f / dist;
+        Float dist = norm(d);
+        Float inv = 1.f / dist;
         d *= inv;
         V3 spec = e.radiance * (inv * inv);
         ei.p = e.p; ei.d = d; ei.n = d;
-        float emitter_pdf = ei.pdf;
+        Float emitter_pdf = ei.pdf;
         ei.pdf = 1.f;
         ei.weight = (spec * dist) * dist;
         ei.pdf *= emitter_pdf;
@@ -1179,7 +1283,7 @@ static V3 evaluate_path_contribution(const Scene &sc, const Query &q, const EI &
     vx.dn_du = V3(0.f); vx.dn_dv = V3(0.f);
     make_orthonormal(vx);
     /* path_throughput = 1 * F * G * weight (manifold_ss.cpp:322-326) */
-    float f = is_rough(sc.shapes[si_final.shape].bsdf)
+    Float f = is_rough(sc.shapes[si_final.shape].bsdf)
                   ? specular_reflectance_rough(sc, si_final, normalize(q.p - si_final.p), normalize(ei.p - si_final.p))
                   : specular_reflectance(sc, si_final, normalize(ei.p - si_final.p));
     f *= geometric_term(vx, vtx, vy);
@@ -1188,14 +1292,14 @@ static V3 evaluate_path_contribution(const Scene &sc, const Query &q, const EI &
 
 /* src/bsdfs/diffuse.cpp eval: albedo / pi * cos_theta_o (both cosines > 0) */
 static V3 diffuse_eval(const Query &q, V3 dir) {
-    float co = dot(dir, q.n);
+    Float co = dot(dir, q.n);
     if (q.cos_i <= 0.f || co <= 0.f) return V3(0.f);
     return (q.albedo * kInvPi) * co;
 }
 
 static bool visible(const Scene &sc, const EI &ei, V3 p) {
     V3 d = p - ei.p;
-    float dist = norm(d);
+    Float dist = norm(d);
     d *= 1.f / dist;
     Ray r; r.o = ei.p; r.d = d;
     r.mint = kRayEps * (1.f + hmax_abs(ei.p));
@@ -1225,16 +1329,16 @@ static void update_max(std::atomic<uint64_t> &a, uint64_t v) {
  * 16) with stride `stride`. */
 struct Learned {
     int shape = -1;
-    float defensive = 1.f;
+    Float defensive = 1.f;
     int kind = 0;               /* 0 box frame, 1 sphere */
     V3 org, ax_u, ax_v;
     const float *mix = nullptr;
     size_t stride = 0;
 };
 
-static V3 learned_seed_point(const Learned &L, float u, float v) {
+static V3 learned_seed_point(const Learned &L, Float u, Float v) {
     if (L.kind == 1) {
-        float th = kPi * u, ph = 2.f * kPi * v;
+        Float th = kPi * u, ph = 2.f * kPi * v;
         return L.org + V3(std::sin(th) * std::cos(ph), std::sin(th) * std::sin(ph), std::cos(th)) * L.ax_u.x;
     }
     return L.org + L.ax_u * u + L.ax_v * v;
@@ -1243,16 +1347,16 @@ static V3 learned_seed_point(const Learned &L, float u, float v) {
 /* one walk's seed: returns p_start for sample_path (zero = uniform seeding
  * with `sample`) */
 static V3 learned_seed(const Learned &L, PCG32 &rng, V2 &sample) {
-    float us = rng.next_f32();
+    Float us = rng.next_f32();
     sample = rng.next_2d();
     if (us < L.defensive) return V3(0.f);
-    float u2 = (us - L.defensive) / (1.f - L.defensive);
+    Float u2 = (us - L.defensive) / (1.f - L.defensive);
     int k = 0;
     while (k < 7 && u2 >= L.mix[(size_t)k * L.stride]) ++k;
-    float r = std::sqrt(-2.f * std::log(1.f - sample.x));
-    float ang = 2.f * kPi * sample.y;
-    float u = L.mix[(size_t)(8 + 2 * k) * L.stride] + L.mix[(size_t)(24 + 2 * k) * L.stride] * (r * std::cos(ang));
-    float v = L.mix[(size_t)(9 + 2 * k) * L.stride] + L.mix[(size_t)(25 + 2 * k) * L.stride] * (r * std::sin(ang));
+    Float r = std::sqrt(-2.f * std::log(1.f - sample.x));
+    Float ang = 2.f * kPi * sample.y;
+    Float u = L.mix[(size_t)(8 + 2 * k) * L.stride] + L.mix[(size_t)(24 + 2 * k) * L.stride] * (r * std::cos(ang));
+    Float v = L.mix[(size_t)(9 + 2 * k) * L.stride] + L.mix[(size_t)(25 + 2 * k) * L.stride] * (r * std::sin(ang));
     return learned_seed_point(L, u, v);
 }
 
@@ -1269,7 +1373,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
         int it = 0;
         /* offset normal of a rough caster (manifold_ss.cpp:60-70) */
         V3 no(0.f, 0.f, 1.f);
-        float p_offset = 1.f;
+        Float p_offset = 1.f;
         if (is_rough(sc.shapes[caster].bsdf)) {
             V2 u = rng.next_2d();
             no = beckmann_sample(sc.shapes[caster].bsdf.alpha, u.x, u.y, p_offset);
@@ -1294,7 +1398,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             if (!visible(sc, ei, si_final.p)) continue;
             V3 spec = evaluate_path_contribution(sc, q, ei, si_final);
             V3 bsdf = diffuse_eval(q, direction);
-            float inv_prob = 1.f;
+            Float inv_prob = 1.f;
             int iterations = 1;
             st.calls++;
             while (true) {
@@ -1389,7 +1493,7 @@ static bool invert_tridiagonal_step(std::vector<MSBlock> &b) {
 }
 
 /* manifold_ms.cpp:1234-1268 (Jakob & Marschner 2012) */
-static float invert_tridiagonal_geo(std::vector<MSBlock> &b) {
+static Float invert_tridiagonal_geo(std::vector<MSBlock> &b) {
     auto inv = [](const M2 &A, M2 &Ai) {
         if (std::fabs(det(A)) == 0.f) return false;
         Ai = inverse(A);
@@ -1409,7 +1513,7 @@ static float invert_tridiagonal_geo(std::vector<MSBlock> &b) {
     return std::fabs(det(mneg(b[0].inv_lambda)));
 }
 
-static void d_sph_pair(V3 w, V3 du, V3 dv, float &a, float &b, float &c, float &d) { d_sphcoords(w, du, dv, a, b, c, d); }
+static void d_sph_pair(V3 w, V3 du, V3 dv, Float &a, Float &b, Float &c, Float &d) { d_sphcoords(w, du, dv, a, b, c, d); }
 
 /* manifold_ms.cpp:631-857 (n_offset = (0,0,1), positional light) */
 static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::vector<MSBlock> &b) {
@@ -1419,13 +1523,13 @@ static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::
     for (size_t i = 0; i < k; ++i) {
         V3 xp = i == 0 ? x0 : v[i - 1].p, xn = i == k - 1 ? lp : v[i + 1].p, xc = v[i].p;
         V3 wo = xn - xc;
-        float ilo = norm(wo);
+        Float ilo = norm(wo);
         if (ilo < 1e-3f) return false;
         ilo = 1.f / ilo; wo *= ilo;
         V3 dwo_du = (v[i].dp_du - wo * dot(wo, v[i].dp_du)) * -ilo;
         V3 dwo_dv = (v[i].dp_dv - wo * dot(wo, v[i].dp_dv)) * -ilo;
         V3 wi = xp - xc;
-        float ili = norm(wi);
+        Float ili = norm(wi);
         if (ili < 1e-3f) return false;
         ili = 1.f / ili; wi *= ili;
         V3 dwi_du = (v[i].dp_du - wi * dot(wi, v[i].dp_du)) * -ili;
@@ -1440,12 +1544,12 @@ static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::
         bool ok_i = false;
         V3 wio;
         if (transform(wi, wio)) {
-            float to, po, tio, pio;
+            Float to, po, tio, pio;
             sphcoords(wo, to, po); sphcoords(wio, tio, pio);
-            float dt = to - tio, dp = po - pio;
+            Float dt = to - tio, dp = po - pio;
             if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
             b[i].C.x = dt; b[i].C.y = dp;
-            float a0, a1, a2, a3, c0, c1, c2, c3;
+            Float a0, a1, a2, a3, c0, c1, c2, c3;
             if (i > 0) {
                 V3 du = (v[i - 1].dp_du - wi * dot(wi, v[i - 1].dp_du)) * ili;
                 V3 dv = (v[i - 1].dp_dv - wi * dot(wi, v[i - 1].dp_dv)) * ili;
@@ -1469,12 +1573,12 @@ static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::
         }
         V3 woi;
         if (transform(wo, woi) && !ok_i) {
-            float ti, pi, toi, poi;
+            Float ti, pi, toi, poi;
             sphcoords(wi, ti, pi); sphcoords(woi, toi, poi);
-            float dt = ti - toi, dp = pi - poi;
+            Float dt = ti - toi, dp = pi - poi;
             if (dp < -kPi) dp += 2.f * kPi; else if (dp > kPi) dp -= 2.f * kPi;
             b[i].C.x = dt; b[i].C.y = dp;
-            float a0, a1, a2, a3, c0, c1, c2, c3;
+            Float a0, a1, a2, a3, c0, c1, c2, c3;
             if (i > 0) {
                 V3 du = (v[i - 1].dp_du - wi * dot(wi, v[i - 1].dp_du)) * ili;
                 V3 dv = (v[i - 1].dp_dv - wi * dot(wi, v[i - 1].dp_dv)) * ili;
@@ -1508,18 +1612,18 @@ static bool ms_step_halfvector(V3 x0, V3 lp, const std::vector<MVertex> &v, std:
     for (size_t i = 0; i < k; ++i) {
         V3 xp = i == 0 ? x0 : v[i - 1].p, xn = i == k - 1 ? lp : v[i + 1].p, xc = v[i].p;
         V3 wo = xn - xc;
-        float ilo = norm(wo);
+        Float ilo = norm(wo);
         if (ilo < 1e-3f) return false;
         ilo = 1.f / ilo; wo *= ilo;
         V3 wi = xp - xc;
-        float ili = norm(wi);
+        Float ili = norm(wi);
         if (ili < 1e-3f) return false;
         ili = 1.f / ili; wi *= ili;
-        float eta = v[i].eta;
+        Float eta = v[i].eta;
         if (dot(wi, v[i].gn) < 0.f) eta = 1.f / eta;
         V3 h = wi + wo * eta;
         if (eta != 1.f) h *= -1.f;
-        float ilh = 1.f / norm(h);
+        Float ilh = 1.f / norm(h);
         h *= ilh;
         ilo *= eta * ilh;
         ili *= ilh;
@@ -1598,7 +1702,7 @@ static bool ms_newton(const Scene &sc, const sms_config &cfg, V3 x0, V3 lp, cons
                       std::vector<MVertex> &path, int &iters) {
     bool success = false;
     int it = 0;
-    float beta = 1.f;
+    Float beta = 1.f;
     bool needs_update = true;
     std::vector<MSBlock> b;
     while (it < cfg.max_iterations) {
@@ -1616,7 +1720,7 @@ static bool ms_newton(const Scene &sc, const sms_config &cfg, V3 x0, V3 lp, cons
         std::vector<MVertex> prop;
         bool proj = ms_trace_chain(sc, (int)path.size(), x0, p0, tmpl, false, prop) && prop.size() == tmpl.size();
         if (!proj) { beta = 0.5f * beta; needs_update = false; }
-        else { beta = std::min(1.f, 2.f * beta); path = prop; needs_update = true; }
+        else { beta = omin(1.f, 2.f * beta); path = prop; needs_update = true; }
         it++;
     }
     iters = it;
@@ -1654,10 +1758,10 @@ static bool ms_sample_path(const Scene &sc, const sms_config &cfg, int caster, c
 }
 
 /* manifold_ms.cpp:920-1023 (smooth BSDFs) */
-static float ms_specular_reflectance(const Scene &sc, V3 x0, V3 lp, const std::vector<MVertex> &path) {
+static Float ms_specular_reflectance(const Scene &sc, V3 x0, V3 lp, const std::vector<MVertex> &path) {
     if (path.empty()) return 0.f;
     Ray ray; ray.o = x0; ray.d = normalize(path[0].p - x0);
-    float val = 1.f;
+    Float val = 1.f;
     SI si;
     for (size_t k = 0; k < path.size(); ++k) {
         si = ray_intersect(sc, ray);
@@ -1674,7 +1778,7 @@ static float ms_specular_reflectance(const Scene &sc, V3 x0, V3 lp, const std::v
 }
 
 /* manifold_ms.cpp:1025-1190 (positional endpoint) */
-static float ms_geometric_term(const MVertex &vx, const std::vector<MVertex> &path, const MVertex &vy) {
+static Float ms_geometric_term(const MVertex &vx, const std::vector<MVertex> &path, const MVertex &vy) {
     std::vector<MVertex> v = path;
     v.push_back(vy);
     size_t k = v.size();
@@ -1682,23 +1786,23 @@ static float ms_geometric_term(const MVertex &vx, const std::vector<MVertex> &pa
     for (size_t i = 0; i + 1 < k; ++i) {
         V3 xc = v[i].p, xn = v[i + 1].p;
         V3 wo = xn - xc;
-        float ilo = norm(wo);
+        Float ilo = norm(wo);
         if (ilo < 1e-3f) return 0.f;
         ilo = 1.f / ilo; wo *= ilo;
         V3 xp = i == 0 ? vx.p : v[i - 1].p;
         V3 wi = xp - xc;
-        float ili = norm(wi);
+        Float ili = norm(wi);
         if (ili < 1e-3f) return 0.f;
         ili = 1.f / ili; wi *= ili;
-        float eta = v[i].eta;
+        Float eta = v[i].eta;
         if (dot(wi, v[i].gn) < 0.f) eta = 1.f / eta;
         V3 h = wi + wo * eta;
         if (eta != 1.f) h *= -1.f;
-        float ilh = 1.f / norm(h);
+        Float ilh = 1.f / norm(h);
         h *= ilh;
         ilo *= eta * ilh;
         ili *= ilh;
-        float dpdu_n = dot(v[i].dp_du, v[i].n), dpdv_n = dot(v[i].dp_dv, v[i].n);
+        Float dpdu_n = dot(v[i].dp_du, v[i].n), dpdv_n = dot(v[i].dp_dv, v[i].n);
         V3 s = v[i].dp_du - v[i].n * dpdu_n, t = v[i].dp_dv - v[i].n * dpdv_n;
         V3 du, dv;
         if (i > 0) {
@@ -1713,7 +1817,7 @@ static float ms_geometric_term(const MVertex &vx, const std::vector<MVertex> &pa
         dv = -v[i].dp_dv * (ili + ilo) + wi * (dot(wi, v[i].dp_dv) * ili) + wo * (dot(wo, v[i].dp_dv) * ilo);
         du -= h * dot(du, h); dv -= h * dot(dv, h);
         if (eta != 1.f) { du *= -1.f; dv *= -1.f; }
-        float hn = dot(h, v[i].n), hdu = dot(h, v[i].dn_du), hdv = dot(h, v[i].dn_dv);
+        Float hn = dot(h, v[i].n), hdu = dot(h, v[i].dn_du), hdv = dot(h, v[i].dn_dv);
         b[i].cur.m[0][0] = dot(du, s) - dot(v[i].dp_du, v[i].dn_du) * hn - dpdu_n * hdu;
         b[i].cur.m[0][1] = dot(dv, s) - dot(v[i].dp_du, v[i].dn_dv) * hn - dpdu_n * hdv;
         b[i].cur.m[1][0] = dot(du, t) - dot(v[i].dp_dv, v[i].dn_du) * hn - dpdv_n * hdu;
@@ -1725,9 +1829,9 @@ static float ms_geometric_term(const MVertex &vx, const std::vector<MVertex> &pa
         b[i].next.m[0][0] = dot(s, du); b[i].next.m[0][1] = dot(s, dv);
         b[i].next.m[1][0] = dot(t, du); b[i].next.m[1][1] = dot(t, dv);
     }
-    float dx1_dxend = invert_tridiagonal_geo(b);
+    Float dx1_dxend = invert_tridiagonal_geo(b);
     V3 d = vx.p - v[0].p;
-    float inv_r2 = 1.f / dot(d, d);
+    Float inv_r2 = 1.f / dot(d, d);
     d *= std::sqrt(inv_r2);
     return std::fabs(dot(d, v[0].gn)) * inv_r2 * dx1_dxend;
 }
@@ -1739,10 +1843,10 @@ static V3 ms_contribution(const Scene &sc, const Query &q, const EI &ei_in, cons
     if (ei.is_point) {
         const Emitter &e = sc.emitters[ei.emitter];
         V3 d = e.p - last.p;
-        float dist = norm(d);
-        float inv = 1.f / dist;
+        Float dist = norm(d);
+        Float inv = 1.f / dist;
         V3 spec = e.radiance * (inv * inv);
-        float emitter_pdf = ei.pdf;
+        Float emitter_pdf = ei.pdf;
         ei.p = e.p;
         ei.pdf = 1.f;
         ei.weight = (spec * dist) * dist;
@@ -1757,7 +1861,7 @@ static V3 ms_contribution(const Scene &sc, const Query &q, const EI &ei_in, cons
     vx.p = q.p; vx.dp_du = q.dp_du; vx.dp_dv = q.dp_dv; vx.gn = q.n; vx.n = q.n;
     vx.dn_du = V3(0.f); vx.dn_dv = V3(0.f);
     make_orthonormal(vx);
-    float f = ms_specular_reflectance(sc, q.p, ei.p, path);
+    Float f = ms_specular_reflectance(sc, q.p, ei.p, path);
     f *= ms_geometric_term(vx, path, vy);
     return V3(f * ei.weight.x, f * ei.weight.y, f * ei.weight.z);
 }
@@ -1785,7 +1889,7 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             V3 direction = normalize(path[0].p - q.p);
             V3 spec = ms_contribution(sc, q, ei, path);
             V3 bsdf = diffuse_eval(q, direction);
-            float inv_prob = 1.f;
+            Float inv_prob = 1.f;
             int iterations = 1;
             st.calls++;
             while (true) {
@@ -1850,31 +1954,31 @@ static GQuery load_gquery(const float *q, uint32_t n, uint32_t i) {
 
 /* bilinear setup of Normalmap::eval_normal (normalmap.h:62-104) at level 0
  * after the tiling wrap of NormalmapBSDF::slope (src/bsdfs/normalmap.cpp:305-316) */
-static void nm_texels(const NormalMap &m, V2 uv_in, uint32_t idx[4], float &wx, float &wy) {
-    float u = uv_in.x * m.tiles, v = uv_in.y * m.tiles;
+static void nm_texels(const NormalMap &m, V2 uv_in, uint32_t idx[4], Float &wx, Float &wy) {
+    Float u = uv_in.x * m.tiles, v = uv_in.y * m.tiles;
     u -= std::floor(u);
     v -= std::floor(v);
-    float res = (float)m.res;
-    float duv = 1.f / res;
-    float px = (u - 0.5f * duv) * res, py = (v - 0.5f * duv) * res;
-    px = std::min(std::max(px, 0.f), res - 1.f);
-    py = std::min(std::max(py, 0.f), res - 1.f);
+    Float res = (Float)m.res;
+    Float duv = 1.f / res;
+    Float px = (u - 0.5f * duv) * res, py = (v - 0.5f * duv) * res;
+    px = omin(omax(px, 0.f), res - 1.f);
+    py = omin(omax(py, 0.f), res - 1.f);
     uint32_t x0 = (uint32_t)std::floor(px), y0 = (uint32_t)std::floor(py);
-    uint32_t x1 = std::min(x0 + 1, m.res - 1), y1 = std::min(y0 + 1, m.res - 1);
-    x0 = std::min(x0, m.res - 1); y0 = std::min(y0, m.res - 1);
+    uint32_t x1 = omin(x0 + 1, m.res - 1), y1 = omin(y0 + 1, m.res - 1);
+    x0 = omin(x0, m.res - 1); y0 = omin(y0, m.res - 1);
     idx[0] = y0 * m.res + x0; idx[1] = y0 * m.res + x1; idx[2] = y1 * m.res + x0; idx[3] = y1 * m.res + x1;
-    wx = px - (float)x0;
-    wy = py - (float)y0;
+    wx = px - (Float)x0;
+    wy = py - (Float)y0;
 }
 
 /* NormalmapBSDF::slope: (-n[0], -n[1]) of the bilinear slope normal */
 static V2 nm_slope(const NormalMap &m, V2 uv) {
-    uint32_t id[4]; float wx, wy;
+    uint32_t id[4]; Float wx, wy;
     nm_texels(m, uv, id, wx, wy);
-    float w0x = 1.f - wx, w0y = 1.f - wy;
+    Float w0x = 1.f - wx, w0y = 1.f - wy;
     V2 r;
-    float a0 = w0x * m.sx[id[0]] + wx * m.sx[id[1]], a1 = w0x * m.sx[id[2]] + wx * m.sx[id[3]];
-    float b0 = w0x * m.sy[id[0]] + wx * m.sy[id[1]], b1 = w0x * m.sy[id[2]] + wx * m.sy[id[3]];
+    Float a0 = w0x * m.sx[id[0]] + wx * m.sx[id[1]], a1 = w0x * m.sx[id[2]] + wx * m.sx[id[3]];
+    Float b0 = w0x * m.sy[id[0]] + wx * m.sy[id[1]], b1 = w0x * m.sy[id[2]] + wx * m.sy[id[3]];
     r.x = w0y * a0 + wy * a1;
     r.y = w0y * b0 + wy * b1;
     return r;
@@ -1883,16 +1987,16 @@ static V2 nm_slope(const NormalMap &m, V2 uv) {
 /* NormalmapBSDF::slope_derivative (normalmap.cpp:318-336 with
  * normalmap.h:125-193): analytic bilinear derivative x res x tiles */
 static void nm_slope_derivative(const NormalMap &m, V2 uv, V2 &du, V2 &dv) {
-    uint32_t id[4]; float wx, wy;
+    uint32_t id[4]; Float wx, wy;
     nm_texels(m, uv, id, wx, wy);
-    float res = (float)m.res;
-    auto d = [&](const std::vector<float> &c, float &ou, float &ov) {
-        float v00 = c[id[0]], v10 = c[id[1]], v01 = c[id[2]], v11 = c[id[3]];
-        float tmp = v01 + v10 - v11;
+    Float res = (Float)m.res;
+    auto d = [&](const std::vector<Float> &c, Float &ou, Float &ov) {
+        Float v00 = c[id[0]], v10 = c[id[1]], v01 = c[id[2]], v11 = c[id[3]];
+        Float tmp = v01 + v10 - v11;
         ou = (v10 + v00 * (wy - 1.f) - tmp * wy) * res;
         ov = (v01 + v00 * (wx - 1.f) - tmp * wx) * res;
     };
-    float ux, vx_, uy, vy_;
+    Float ux, vx_, uy, vy_;
     d(m.sx, ux, vx_);
     d(m.sy, uy, vy_);
     du.x = ux * m.tiles; du.y = uy * m.tiles;
@@ -1915,10 +2019,10 @@ static bool glint_step(const NormalMap &m, V2 target, V2 uv, V2 &C, V2 &dX) {
 /* manifold_glints.h:162-194 */
 static bool inside_triangle(V2 p, V2 a, V2 b, V2 c) {
     V2 v0{c.x - a.x, c.y - a.y}, v1{b.x - a.x, b.y - a.y}, v2{p.x - a.x, p.y - a.y};
-    float d00 = v0.x * v0.x + v0.y * v0.y, d01 = v0.x * v1.x + v0.y * v1.y, d02 = v0.x * v2.x + v0.y * v2.y,
+    Float d00 = v0.x * v0.x + v0.y * v0.y, d01 = v0.x * v1.x + v0.y * v1.y, d02 = v0.x * v2.x + v0.y * v2.y,
           d11 = v1.x * v1.x + v1.y * v1.y, d12 = v1.x * v2.x + v1.y * v2.y;
-    float inv = 1.f / (d00 * d11 - d01 * d01);
-    float u = (d11 * d02 - d01 * d12) * inv, v = (d00 * d12 - d01 * d02) * inv;
+    Float inv = 1.f / (d00 * d11 - d01 * d01);
+    Float u = (d11 * d02 - d01 * d12) * inv, v = (d00 * d12 - d01 * d02) * inv;
     return u >= 0.f && v >= 0.f && u + v < 1.f;
 }
 
@@ -1926,14 +2030,14 @@ static bool inside_triangle(V2 p, V2 a, V2 b, V2 c) {
 static bool glint_newton(const sms_config &cfg, const NormalMap &m, V2 target, V2 uv_init, const GQuery &q, V2 &uv_out,
                          int &iters) {
     V2 uv = uv_init;
-    auto corner = [&](float a, float b) {
+    auto corner = [&](Float a, Float b) {
         V2 r; r.x = q.uv.x + a * q.duv_dx.x + b * q.duv_dy.x; r.y = q.uv.y + a * q.duv_dx.y + b * q.duv_dy.y;
         return r;
     };
     V2 fa = corner(0.5f, 0.5f), fb = corner(0.5f, -0.5f), fc = corner(-0.5f, -0.5f), fd = corner(-0.5f, 0.5f);
     bool success = false;
     int it = 0;
-    float beta = 1.f;
+    Float beta = 1.f;
     while (it < cfg.max_iterations) {
         V2 C, step;
         if (!glint_step(m, target, uv, C, step)) break;
@@ -1946,7 +2050,7 @@ static bool glint_newton(const sms_config &cfg, const NormalMap &m, V2 target, V
             it++;
             continue;
         }
-        beta = std::min(1.f, 2.f * beta);
+        beta = omin(1.f, 2.f * beta);
         uv = prop;
         it++;
     }
@@ -1991,7 +2095,7 @@ static void glint_vertex(const NormalMap &m, const GQuery &q, V2 uv, MVertex &v)
     nm_slope_derivative(m, uv, du, dv);
     V3 nl(-sl.x, -sl.y, 1.f);
     V3 wn = s * nl.x + t * nl.y + q.n * nl.z;
-    float inv_len = 1.f / norm(wn);
+    Float inv_len = 1.f / norm(wn);
     wn *= inv_len;
     /* eval_normal_derivatives returns (-d sx, -d sy, 0); the frame maps it to world */
     V3 dnu = (s * -du.x + t * -du.y) * inv_len;
@@ -2005,27 +2109,27 @@ static void glint_vertex(const NormalMap &m, const GQuery &q, V2 uv, MVertex &v)
 }
 
 /* manifold_glints.cpp:411-554 (positional light) */
-static float glint_geometric_term(const MVertex &v0, const MVertex &v1, const MVertex &v2) {
+static Float glint_geometric_term(const MVertex &v0, const MVertex &v1, const MVertex &v2) {
     V3 wi = v0.p - v1.p;
-    float ili = norm(wi);
+    Float ili = norm(wi);
     if (ili < 1e-3f) return 0.f;
     ili = 1.f / ili; wi *= ili;
     V3 wo = v2.p - v1.p;
-    float ilo = norm(wo);
+    Float ilo = norm(wo);
     if (ilo < 1e-3f) return 0.f;
     ilo = 1.f / ilo; wo *= ilo;
     V3 h = wi + wo;
-    float ilh = 1.f / norm(h);
+    Float ilh = 1.f / norm(h);
     h *= ilh;
     ilo *= ilh;
     ili *= ilh;
-    float dpdu_n = dot(v1.dp_du, v1.n), dpdv_n = dot(v1.dp_dv, v1.n);
+    Float dpdu_n = dot(v1.dp_du, v1.n), dpdv_n = dot(v1.dp_dv, v1.n);
     V3 s = v1.dp_du - v1.n * dpdu_n, t = v1.dp_dv - v1.n * dpdv_n;
     V3 dh_du = -v1.dp_du * (ili + ilo) + wi * (dot(wi, v1.dp_du) * ili) + wo * (dot(wo, v1.dp_du) * ilo);
     V3 dh_dv = -v1.dp_dv * (ili + ilo) + wi * (dot(wi, v1.dp_dv) * ili) + wo * (dot(wo, v1.dp_dv) * ilo);
     dh_du -= h * dot(dh_du, h);
     dh_dv -= h * dot(dh_dv, h);
-    float hn = dot(h, v1.n), hdu = dot(h, v1.dn_du), hdv = dot(h, v1.dn_dv);
+    Float hn = dot(h, v1.n), hdu = dot(h, v1.dn_du), hdv = dot(h, v1.dn_dv);
     M2 d11;
     d11.m[0][0] = dot(dh_du, s) - dot(v1.dp_du, v1.dn_du) * hn - dpdu_n * hdu;
     d11.m[0][1] = dot(dh_dv, s) - dot(v1.dp_du, v1.dn_dv) * hn - dpdu_n * hdv;
@@ -2039,24 +2143,24 @@ static float glint_geometric_term(const MVertex &v0, const MVertex &v1, const MV
     d12.m[0][0] = dot(dh_du, s); d12.m[0][1] = dot(dh_dv, s);
     d12.m[1][0] = dot(dh_du, t); d12.m[1][1] = dot(dh_dv, t);
     if (std::fabs(det(d11)) < 1e-6f) return 0.f;
-    float dx1_dx2 = std::fabs(det(mul(inverse(d11), d12)));
+    Float dx1_dx2 = std::fabs(det(mul(inverse(d11), d12)));
     V3 d = v0.p - v1.p;
-    float inv_r2 = 1.f / dot(d, d);
+    Float inv_r2 = 1.f / dot(d, d);
     d *= std::sqrt(inv_r2);
-    float G = std::fabs(dot(d, v1.gn)) * inv_r2 * dx1_dx2;
-    return std::min(1e-5f, G);
+    Float G = std::fabs(dot(d, v1.gn)) * inv_r2 * dx1_dx2;
+    return omin(1e-5f, G);
 }
 
 /* manifold_glints.cpp:375-409 (delta BSDF): Fresnel at the normal-mapped normal */
-static float glint_reflectance(const sms_bsdf &b, V3 n, V3 wo) {
-    float cos_theta = dot(n, wo);
+static Float glint_reflectance(const sms_bsdf &b, V3 n, V3 wo) {
+    Float cos_theta = dot(n, wo);
     if (b.type == SMS_BSDF_CONDUCTOR && b.k != 0.f) return fresnel_conductor(std::fabs(cos_theta), b.eta, b.k);
     if (b.type == SMS_BSDF_DIELECTRIC || b.type == SMS_BSDF_CONDUCTOR) return fresnel(std::fabs(cos_theta), b.eta);
     return fresnel_conductor(std::fabs(cos_theta), 0.f, 1.f);
 }
 
 /* manifold_glints.cpp:267-294 */
-static float glint_contribution(const Scene &sc, const GQuery &q, const EI &ei, V2 uv) {
+static Float glint_contribution(const Scene &sc, const GQuery &q, const EI &ei, V2 uv) {
     MVertex vy;
     if (!emitter_vertex(sc, ei, q.p, vy)) return 0.f;
     MVertex vx;
@@ -2068,7 +2172,7 @@ static float glint_contribution(const Scene &sc, const GQuery &q, const EI &ei, 
     glint_vertex(sc.nmap, q, uv, vt);
     MVertex vt_o = vt;
     make_orthonormal(vt_o);
-    float f = glint_reflectance(sc.shapes[sc.glinty_shape].bsdf, vt.n, normalize(ei.p - q.p));
+    Float f = glint_reflectance(sc.shapes[sc.glinty_shape].bsdf, vt.n, normalize(ei.p - q.p));
     f *= glint_geometric_term(vx, vt_o, vy);
     return f;
 }
@@ -2083,13 +2187,13 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
     if (ei.emitter < 0 || sc.glinty_shape < 0 || sc.nmap.res == 0) return V3(0.f);
     st.connections++;
     V3 d = ei.p - q.p;
-    float dist = norm(d);
+    Float dist = norm(d);
     d *= 1.f / dist;
     Ray r; r.o = q.p; r.d = d;
     r.mint = kRayEps * (1.f + hmax_abs(q.p));
     r.maxt = dist * (1.f - kRayEps);
     if (ray_test(sc, r)) return V3(0.f);
-    float w = 0.f;
+    Float w = 0.f;
     V2 uvf, uvi;
     int it;
     if (!cfg.biased) {
@@ -2097,8 +2201,8 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
         walks_out++; st.walks++; st.newton += it;
         if (!ok) { st.failed++; return V3(0.f); }
         st.succeeded++;
-        float spec = glint_contribution(sc, q, ei, uvf);
-        float inv_prob = 1.f;
+        Float spec = glint_contribution(sc, q, ei, uvf);
+        Float inv_prob = 1.f;
         int iterations = 1;
         st.calls++;
         while (true) {
@@ -2106,7 +2210,7 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
             int it2;
             bool ok2 = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvt, uvi2, it2);
             walks_out++; st.walks++; st.newton += it2;
-            float dx = uvt.x - uvf.x, dy = uvt.y - uvf.y;
+            Float dx = uvt.x - uvf.x, dy = uvt.y - uvf.y;
             if (ok2 && std::sqrt(dx * dx + dy * dy) < cfg.uniqueness_threshold) break;
             inv_prob += 1.f;
             iterations++;
@@ -2125,7 +2229,7 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
             st.succeeded++;
             bool dup = false;
             for (const V2 &u : sols) {
-                float dx = uvf.x - u.x, dy = uvf.y - u.y;
+                Float dx = uvf.x - u.x, dy = uvf.y - u.y;
                 if (std::sqrt(dx * dx + dy * dy) < cfg.uniqueness_threshold) { dup = true; break; }
             }
             if (dup) continue;
@@ -2153,18 +2257,18 @@ static uint64_t sms_seed(uint64_t seed) {
     return z ^ (z >> 31);
 }
 
-static float mis_weight(float a, float b) {   /* path.cpp:227-231 */
+static Float mis_weight(Float a, Float b) {   /* path.cpp:227-231 */
     a *= a; b *= b;
-    return a > 0.f ? a / (a + b) : 0.f;
+    return a > 0.f ? a / (a + b) : Float(0.f);
 }
 
-static float hmax_v(V3 v) { return std::max(v.x, std::max(v.y, v.z)); }
+static Float hmax_v(V3 v) { return omax(v.x, omax(v.y, v.z)); }
 
 /* sh_frame of the surface interaction: tangent from dp_du (kdtree.h:2334-2366) */
 static void pt_frame(const SI &si, V3 &s, V3 &t) {
     V3 n = si.shn;
     V3 a = si.dp_du - n * dot(n, si.dp_du);
-    float l2 = dot(a, a);
+    Float l2 = dot(a, a);
     if (l2 > 1e-20f) { s = a * (1.f / std::sqrt(l2)); t = cross(n, s); }
     else coordinate_system(n, s, t);
 }
@@ -2179,55 +2283,55 @@ static V3 pt_emitted(const Scene &sc, const Shape &s, V3 p, V3 d) {
 }
 
 /* Sphere::pdf_direction x emitter pick (scene.cpp:206-220) */
-static float pt_emitter_pdf(const Scene &sc, const Shape &s, V3 x, V3 p, V3 d, float dist) {
+static Float pt_emitter_pdf(const Scene &sc, const Shape &s, V3 x, V3 p, V3 d, Float dist) {
     V3 n = normalize(p - s.center);
     if (s.flip) n = -n;
     if (!(dot(d, n) < 0.f)) return 0.f;
-    float sin_a = s.radius / norm(s.center - x);
-    float cos_a = safe_sqrt(1.f - sin_a * sin_a);
-    float pdf;
+    Float sin_a = s.radius / norm(s.center - x);
+    Float cos_a = safe_sqrt(1.f - sin_a * sin_a);
+    Float pdf;
     if (sin_a < 1.f - 5.9604644775390625e-08f) pdf = (0.5f * kInvPi) / (1.f - cos_a);
     else pdf = (1.f / (4.f * kPi * s.radius * s.radius)) * dist * dist / std::fabs(dot(d, n));
-    return sc.emitters_all.size() > 1 ? pdf * (1.f / (float)sc.emitters_all.size()) : pdf;
+    return sc.emitters_all.size() > 1 ? pdf * (1.f / (Float)sc.emitters_all.size()) : pdf;
 }
 
-struct PtDir { V3 d, spec; float dist = 0.f, pdf = 0.f; bool delta = false; };
+struct PtDir { V3 d, spec; Float dist = 0.f, pdf = 0.f; bool delta = false; };
 
 /* Scene::sample_emitter_direction (scene.cpp:156-196), point.cpp and
  * area.cpp + Sphere::sample_direction (sphere.cpp) */
-static bool pt_sample_emitter(const Scene &sc, V3 x, float ux, float uy, PtDir &ds) {
+static bool pt_sample_emitter(const Scene &sc, V3 x, Float ux, Float uy, PtDir &ds) {
     const int ne = (int)sc.emitters_all.size();
     if (ne == 0) return false;
     int idx = 0;
     if (ne > 1) {
-        float epdf = 1.f / (float)ne;
-        idx = (int)std::min((uint32_t)(ux * (float)ne), (uint32_t)ne - 1);
-        ux = (ux - (float)idx * epdf) * (float)ne;
+        Float epdf = 1.f / (Float)ne;
+        idx = (int)omin((uint32_t)(ux * (Float)ne), (uint32_t)ne - 1);
+        ux = (ux - (Float)idx * epdf) * (Float)ne;
     }
     const Emitter &e = sc.emitters[sc.emitters_all[idx]];
     if (e.kind == 0) {
         V3 d = e.p - x;
         ds.dist = norm(d);
-        float inv = 1.f / ds.dist;
+        Float inv = 1.f / ds.dist;
         ds.d = d * inv; ds.pdf = 1.f; ds.delta = true;
         ds.spec = e.radiance * (inv * inv);
     } else {
         const Shape &s = sc.shapes[e.shape];
         V3 dc = s.center - x;
-        float dc2 = dot(dc, dc);
-        float r_adj = s.radius * (s.flip ? (1.f + kRayEps) : (1.f - kRayEps));
+        Float dc2 = dot(dc, dc);
+        Float r_adj = s.radius * (s.flip ? (1.f + kRayEps) : (1.f - kRayEps));
         V3 p, n;
         if (dc2 > r_adj * r_adj) {
-            float inv_dc = 1.f / std::sqrt(dc2);
-            float sin_max = s.radius * inv_dc, sin2_max = sin_max * sin_max, inv_sin_max = 1.f / sin_max;
-            float cos_max = safe_sqrt(1.f - sin2_max);
-            float a = (cos_max - 1.f) * ux + 1.f;
-            float sin2 = sin2_max > 0.00068523f ? 1.f - a * a : sin2_max * ux;
-            float cos_t = safe_sqrt(1.f - sin2);
-            float cos_al = sin2 * inv_sin_max + cos_t * safe_sqrt(1.f - sin2 * inv_sin_max * inv_sin_max);
-            float sin_al = safe_sqrt(1.f - cos_al * cos_al);
-            float ang = uy * (2.f * kPi);
-            float sp = std::sin(ang), cp = std::cos(ang);
+            Float inv_dc = 1.f / std::sqrt(dc2);
+            Float sin_max = s.radius * inv_dc, sin2_max = sin_max * sin_max, inv_sin_max = 1.f / sin_max;
+            Float cos_max = safe_sqrt(1.f - sin2_max);
+            Float a = (cos_max - 1.f) * ux + 1.f;
+            Float sin2 = sin2_max > 0.00068523f ? 1.f - a * a : sin2_max * ux;
+            Float cos_t = safe_sqrt(1.f - sin2);
+            Float cos_al = sin2 * inv_sin_max + cos_t * safe_sqrt(1.f - sin2 * inv_sin_max * inv_sin_max);
+            Float sin_al = safe_sqrt(1.f - cos_al * cos_al);
+            Float ang = uy * (2.f * kPi);
+            Float sp = std::sin(ang), cp = std::cos(ang);
             V3 fz = dc * -inv_dc, fs, ft;
             coordinate_system(fz, fs, ft);
             V3 dl = fs * (cp * sin_al) + ft * (sp * sin_al) + fz * cos_al;
@@ -2235,12 +2339,12 @@ static bool pt_sample_emitter(const Scene &sc, V3 x, float ux, float uy, PtDir &
             V3 dv = p - x;
             ds.dist = norm(dv);
             ds.d = dv * (1.f / ds.dist);
-            ds.pdf = ds.dist == 0.f ? 0.f : (0.5f * kInvPi) / (1.f - cos_max);
+            ds.pdf = ds.dist == 0.f ? Float(0.f) : (0.5f * kInvPi) / (1.f - cos_max);
         } else {
             V3 dl = square_to_uniform_sphere(V2{ux, uy});
             p = dl * s.radius + s.center; n = dl;
             V3 dv = p - x;
-            float dist2 = dot(dv, dv);
+            Float dist2 = dot(dv, dv);
             ds.dist = std::sqrt(dist2);
             ds.d = dv * (1.f / ds.dist);
             ds.pdf = (1.f / (4.f * kPi * s.radius * s.radius)) * dist2 / std::fabs(dot(ds.d, n));
@@ -2250,23 +2354,23 @@ static bool pt_sample_emitter(const Scene &sc, V3 x, float ux, float uy, PtDir &
         if (!(dot(ds.d, n) < 0.f && ds.pdf != 0.f)) return false;
         ds.spec = e.radiance * (1.f / ds.pdf);
     }
-    if (ne > 1) { ds.pdf *= 1.f / (float)ne; ds.spec = ds.spec * (float)ne; }
+    if (ne > 1) { ds.pdf *= 1.f / (Float)ne; ds.spec = ds.spec * (Float)ne; }
     return ds.pdf != 0.f;
 }
 
 /* warp.h:54-90 concentric disk, lifted to the cosine hemisphere (warp.h:332-340) */
-static V3 pt_cosine_hemisphere(float u1, float u2) {
-    float x = 2.f * u1 - 1.f, y = 2.f * u2 - 1.f, r, phi;
+static V3 pt_cosine_hemisphere(Float u1, Float u2) {
+    Float x = 2.f * u1 - 1.f, y = 2.f * u2 - 1.f, r, phi;
     if (x == 0.f && y == 0.f) { r = 0.f; phi = 0.f; }
     else if (std::fabs(x) < std::fabs(y)) { r = y; phi = 0.5f * kPi - (x / y) * (0.25f * kPi); }
     else { r = x; phi = (y / x) * (0.25f * kPi); }
-    float px = r * std::cos(phi), py = r * std::sin(phi);
+    Float px = r * std::cos(phi), py = r * std::sin(phi);
     return V3(px, py, safe_sqrt(1.f - px * px - py * py));
 }
 
 struct PtBsdf {
     V3 wo, weight;
-    float pdf = 0.f, eta = 1.f;
+    Float pdf = 0.f, eta = 1.f;
     bool delta = false;
     bool transmit = false;   /* BSDFFlags::Transmission of the sampled lobe */
 };
@@ -2274,8 +2378,8 @@ struct PtBsdf {
 /* density of pt_rough_sample for (wi, wo): D(m) cos(theta_m) x the Jacobian
  * of reflection / refraction (roughconductor.cpp / roughdielectric.cpp pdf
  * with normals drawn from D cos instead of the visible normals) */
-static float pt_rough_pdf(const sms_bsdf &b, V3 wi, V3 wo) {
-    const float ci = wi.z, co = wo.z;
+static Float pt_rough_pdf(const sms_bsdf &b, V3 wi, V3 wo) {
+    const Float ci = wi.z, co = wo.z;
     if (b.type == SMS_BSDF_CONDUCTOR) {
         if (!(ci > 0.f && co > 0.f)) return 0.f;
         V3 h = normalize(wo + wi);
@@ -2283,14 +2387,14 @@ static float pt_rough_pdf(const sms_bsdf &b, V3 wi, V3 wo) {
     }
     if (ci == 0.f) return 0.f;
     const bool reflect = ci * co > 0.f;
-    const float eta = ci > 0.f ? b.eta : 1.f / b.eta;
-    V3 m = normalize(wi + wo * (reflect ? 1.f : eta));
+    const Float eta = ci > 0.f ? b.eta : 1.f / b.eta;
+    V3 m = normalize(wi + wo * (reflect ? Float(1.f) : eta));
     if (m.z < 0.f) m = -m;
     if (dot(wi, m) * ci <= 0.f || dot(wo, m) * co <= 0.f) return 0.f;
-    const float F = fresnel(dot(wi, m), b.eta);
-    const float pm = beckmann_D(m, b.alpha) * m.z;
+    const Float F = fresnel(dot(wi, m), b.eta);
+    const Float pm = beckmann_D(m, b.alpha) * m.z;
     if (reflect) return F * pm / (4.f * std::fabs(dot(wo, m)));
-    const float den = dot(wi, m) + eta * dot(wo, m);
+    const Float den = dot(wi, m) + eta * dot(wo, m);
     return (1.f - F) * pm * eta * eta * std::fabs(dot(wo, m)) / (den * den);
 }
 
@@ -2306,17 +2410,17 @@ static V3 pt_bsdf_eval(const sms_bsdf &b, V3 wi, V3 wo) {
                                            : roughdielectric_eval(b.alpha, b.eta, wi, wo));
 }
 
-static float pt_bsdf_pdf(const sms_bsdf &b, V3 wi, V3 wo) {
-    if (b.type == SMS_BSDF_DIFFUSE) return (wi.z > 0.f && wo.z > 0.f) ? kInvPi * wo.z : 0.f;
-    return b.alpha > 0.f ? pt_rough_pdf(b, wi, wo) : 0.f;
+static Float pt_bsdf_pdf(const sms_bsdf &b, V3 wi, V3 wo) {
+    if (b.type == SMS_BSDF_DIFFUSE) return (wi.z > 0.f && wo.z > 0.f) ? kInvPi * wo.z : Float(0.f);
+    return b.alpha > 0.f ? pt_rough_pdf(b, wi, wo) : Float(0.f);
 }
 
 /* rough sampling: m ~ D cos (microfacet.h, sample_visible = false), then
  * reflection, or for a dielectric reflection / refraction by the Fresnel
  * reflectance at m (roughdielectric.cpp sample); weight = value / density */
-static bool pt_rough_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u3, PtBsdf &bs) {
-    const float ci = wi.z;
-    float pm;
+static bool pt_rough_sample(const sms_bsdf &b, V3 wi, Float u1, Float u2, Float u3, PtBsdf &bs) {
+    const Float ci = wi.z;
+    Float pm;
     const V3 m = beckmann_sample(b.alpha, u2, u3, pm);
     bs.delta = false;
     bs.eta = 1.f;
@@ -2325,10 +2429,10 @@ static bool pt_rough_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float 
         bs.wo = m * (2.f * dot(wi, m)) - wi;
         if (!(bs.wo.z > 0.f)) return false;
     } else {
-        float cos_t;
-        const float F = fresnel(dot(wi, m), b.eta, &cos_t);
+        Float cos_t;
+        const Float F = fresnel(dot(wi, m), b.eta, &cos_t);
         const bool outside = dot(wi, m) >= 0.f;
-        const float eta_it = outside ? b.eta : 1.f / b.eta, eta_ti = outside ? 1.f / b.eta : b.eta;
+        const Float eta_it = outside ? b.eta : 1.f / b.eta, eta_ti = outside ? 1.f / b.eta : b.eta;
         if (u1 <= F) {
             bs.wo = m * (2.f * dot(wi, m)) - wi;
             if (!(bs.wo.z * ci > 0.f)) return false;
@@ -2345,8 +2449,8 @@ static bool pt_rough_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float 
 }
 
 /* diffuse.cpp / dielectric.cpp / conductor.cpp sample() (smooth, radiance) */
-static bool pt_bsdf_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u3, PtBsdf &bs) {
-    const float ci = wi.z;
+static bool pt_bsdf_sample(const sms_bsdf &b, V3 wi, Float u1, Float u2, Float u3, PtBsdf &bs) {
+    const Float ci = wi.z;
     if (b.type != SMS_BSDF_DIFFUSE && b.alpha > 0.f) return pt_rough_sample(b, wi, u1, u2, u3, bs);
     if (b.type == SMS_BSDF_DIFFUSE) {
         if (!(ci > 0.f)) return false;
@@ -2356,11 +2460,11 @@ static bool pt_bsdf_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u
         return bs.pdf > 0.f;
     }
     if (b.type == SMS_BSDF_DIELECTRIC) {
-        float cos_t_abs;
-        float r = fresnel(ci, b.eta, &cos_t_abs);
+        Float cos_t_abs;
+        Float r = fresnel(ci, b.eta, &cos_t_abs);
         bool outside = ci >= 0.f;
-        float eta_it = outside ? b.eta : 1.f / b.eta, eta_ti = outside ? 1.f / b.eta : b.eta;
-        float cos_t = outside ? -std::fabs(cos_t_abs) : std::fabs(cos_t_abs);
+        Float eta_it = outside ? b.eta : 1.f / b.eta, eta_ti = outside ? 1.f / b.eta : b.eta;
+        Float cos_t = outside ? -std::fabs(cos_t_abs) : std::fabs(cos_t_abs);
         bs.delta = true;
         if (u1 <= r) {
             bs.wo = V3(-wi.x, -wi.y, wi.z); bs.pdf = r; bs.eta = 1.f; bs.weight = V3(1.f);
@@ -2382,10 +2486,10 @@ static bool pt_bsdf_sample(const sms_bsdf &b, V3 wi, float u1, float u2, float u
  * (Bitmap::resample with a box filter at exactly half the size). */
 static void build_lean(NormalMap &m) {
     if (!m.lean.empty() || m.res == 0) return;
-    const float base_sigma_2 = 0.5f * 0.0001f * 0.0001f;
-    std::vector<float> l0(5 * (size_t)m.res * m.res);
+    const Float base_sigma_2 = 0.5f * 0.0001f * 0.0001f;
+    std::vector<Float> l0(5 * (size_t)m.res * m.res);
     for (size_t i = 0; i < (size_t)m.res * m.res; ++i) {
-        float x = m.sx[i], y = m.sy[i];
+        Float x = m.sx[i], y = m.sy[i];
         l0[5 * i] = x; l0[5 * i + 1] = y;
         l0[5 * i + 2] = x * x + base_sigma_2; l0[5 * i + 3] = y * y + base_sigma_2; l0[5 * i + 4] = x * y;
     }
@@ -2393,13 +2497,13 @@ static void build_lean(NormalMap &m) {
     uint32_t res = m.res;
     while (res > 1) {
         uint32_t r2 = res / 2;
-        const std::vector<float> &src = m.lean.back();
-        std::vector<float> dst(5 * (size_t)r2 * r2);
+        const std::vector<Float> &src = m.lean.back();
+        std::vector<Float> dst(5 * (size_t)r2 * r2);
         for (uint32_t y = 0; y < r2; ++y)
             for (uint32_t x = 0; x < r2; ++x)
                 for (int c = 0; c < 5; ++c) {
-                    float a = src[5 * ((size_t)(2 * y) * res + 2 * x) + c] + src[5 * ((size_t)(2 * y) * res + 2 * x + 1) + c];
-                    float b = src[5 * ((size_t)(2 * y + 1) * res + 2 * x) + c] +
+                    Float a = src[5 * ((size_t)(2 * y) * res + 2 * x) + c] + src[5 * ((size_t)(2 * y) * res + 2 * x + 1) + c];
+                    Float b = src[5 * ((size_t)(2 * y + 1) * res + 2 * x) + c] +
                               src[5 * ((size_t)(2 * y + 1) * res + 2 * x + 1) + c];
                     dst[5 * ((size_t)y * r2 + x) + c] = 0.25f * (a + b);
                 }
@@ -2412,91 +2516,91 @@ static void build_lean(NormalMap &m) {
  * a texel (negative level) takes level 0 */
 static int lean_level(const NormalMap &m, V2 duv_dx, V2 duv_dy) {
     const int L = (int)m.lean.size();
-    float w = 2.f * std::max(std::max(std::fabs(m.tiles * duv_dx.x), std::fabs(m.tiles * duv_dx.y)),
-                             std::max(std::fabs(m.tiles * duv_dy.x), std::fabs(m.tiles * duv_dy.y)));
-    float lv = std::ceil((float)(L - 1) + std::log2(std::max(w, 1e-8f)));
+    Float w = 2.f * omax(omax(std::fabs(m.tiles * duv_dx.x), std::fabs(m.tiles * duv_dx.y)),
+                             omax(std::fabs(m.tiles * duv_dy.x), std::fabs(m.tiles * duv_dy.y)));
+    Float lv = std::ceil((Float)(L - 1) + std::log2(omax(w, 1e-8f)));
     if (!(lv > 0.f)) return 0;
-    return (int)std::min(lv, (float)(L - 1));
+    return (int)omin(lv, (Float)(L - 1));
 }
 
 /* Bilinear LEAN lookup (normalmap.h:62-104, 199-233): mean slope mu and
  * covariance (a, c; c, b) at the tiled uv on level l */
-static void lean_lookup(const NormalMap &m, V2 uv_in, int l, V2 &mu, float &sa, float &sb, float &sc) {
+static void lean_lookup(const NormalMap &m, V2 uv_in, int l, V2 &mu, Float &sa, Float &sb, Float &sc) {
     uint32_t res = m.res >> l;
-    float u = uv_in.x * m.tiles, v = uv_in.y * m.tiles;
+    Float u = uv_in.x * m.tiles, v = uv_in.y * m.tiles;
     u -= std::floor(u); v -= std::floor(v);
-    float fr = (float)res, duv = 1.f / fr;
-    float px = std::min(std::max((u - 0.5f * duv) * fr, 0.f), fr - 1.f);
-    float py = std::min(std::max((v - 0.5f * duv) * fr, 0.f), fr - 1.f);
+    Float fr = (Float)res, duv = 1.f / fr;
+    Float px = omin(omax((u - 0.5f * duv) * fr, 0.f), fr - 1.f);
+    Float py = omin(omax((v - 0.5f * duv) * fr, 0.f), fr - 1.f);
     uint32_t x0 = (uint32_t)std::floor(px), y0 = (uint32_t)std::floor(py);
-    uint32_t x1 = std::min(x0 + 1, res - 1), y1 = std::min(y0 + 1, res - 1);
-    x0 = std::min(x0, res - 1); y0 = std::min(y0, res - 1);
-    float wx = px - (float)x0, wy = py - (float)y0;
-    const std::vector<float> &d = m.lean[l];
-    float vv[5];
+    uint32_t x1 = omin(x0 + 1, res - 1), y1 = omin(y0 + 1, res - 1);
+    x0 = omin(x0, res - 1); y0 = omin(y0, res - 1);
+    Float wx = px - (Float)x0, wy = py - (Float)y0;
+    const std::vector<Float> &d = m.lean[l];
+    Float vv[5];
     for (int c = 0; c < 5; ++c) {
-        float v00 = d[5 * ((size_t)y0 * res + x0) + c], v10 = d[5 * ((size_t)y0 * res + x1) + c];
-        float v01 = d[5 * ((size_t)y1 * res + x0) + c], v11 = d[5 * ((size_t)y1 * res + x1) + c];
-        float a = (1.f - wx) * v00 + wx * v10, b = (1.f - wx) * v01 + wx * v11;
+        Float v00 = d[5 * ((size_t)y0 * res + x0) + c], v10 = d[5 * ((size_t)y0 * res + x1) + c];
+        Float v01 = d[5 * ((size_t)y1 * res + x0) + c], v11 = d[5 * ((size_t)y1 * res + x1) + c];
+        Float a = (1.f - wx) * v00 + wx * v10, b = (1.f - wx) * v01 + wx * v11;
         vv[c] = (1.f - wy) * a + wy * b;
     }
     mu.x = vv[0]; mu.y = vv[1];
-    sa = std::max(0.f, vv[2] - vv[0] * vv[0]);
-    sb = std::max(0.f, vv[3] - vv[1] * vv[1]);
-    sc = std::max(0.f, vv[4] - vv[0] * vv[1]);
+    sa = omax(0.f, vv[2] - vv[0] * vv[0]);
+    sb = omax(0.f, vv[3] - vv[1] * vv[1]);
+    sc = omax(0.f, vv[4] - vv[0] * vv[1]);
 }
 
 /* LEAN/LEADR distribution (include/mitsuba/render/lean.h, after Dupuy's
  * reference implementation): parameters from the LEAN moments plus a base
  * Beckmann roughness, visible-normal density, shadowing. */
-struct LeanP { V3 n; float ax, ay, rho, srho, tx, ty; };
-static LeanP lean_params(V2 mu, float sa, float sb, float sc, float alpha) {
-    float e1 = mu.x, e2 = mu.y;
-    float lax = std::sqrt(2.f * sa), lay = std::sqrt(2.f * sb);
-    float rho = 2.f * sc / (lax * lay);
-    float e3 = 0.5f * lax * lax + e1 * e1 + 0.5f * alpha * alpha;
-    float e4 = 0.5f * lay * lay + e2 * e2 + 0.5f * alpha * alpha;
-    float e5 = 0.5f * rho * lax * lay + e1 * e2;
+struct LeanP { V3 n; Float ax, ay, rho, srho, tx, ty; };
+static LeanP lean_params(V2 mu, Float sa, Float sb, Float sc, Float alpha) {
+    Float e1 = mu.x, e2 = mu.y;
+    Float lax = std::sqrt(2.f * sa), lay = std::sqrt(2.f * sb);
+    Float rho = 2.f * sc / (lax * lay);
+    Float e3 = 0.5f * lax * lax + e1 * e1 + 0.5f * alpha * alpha;
+    Float e4 = 0.5f * lay * lay + e2 * e2 + 0.5f * alpha * alpha;
+    Float e5 = 0.5f * rho * lax * lay + e1 * e2;
     LeanP p;
     p.tx = e1; p.ty = e2;
-    p.ax = std::sqrt(2.f * std::max(0.f, e3 - e1 * e1));
-    p.ay = std::sqrt(2.f * std::max(0.f, e4 - e2 * e2));
+    p.ax = std::sqrt(2.f * omax(0.f, e3 - e1 * e1));
+    p.ay = std::sqrt(2.f * omax(0.f, e4 - e2 * e2));
     p.rho = 2.f * (e5 - e1 * e2) / (p.ax * p.ay);
     p.srho = std::sqrt(1.f - p.rho * p.rho);
     p.n = normalize(V3(-p.tx, -p.ty, 1.f));
     return p;
 }
-static float lean_sigma_std(float ct) {
+static Float lean_sigma_std(Float ct) {
     if (ct == 1.f) return 1.f;
-    float st = std::sqrt(1.f - ct * ct), nu = ct / st;
-    float tmp = std::exp(-nu * nu) * 0.56418958354775628695f;   /* 1 / sqrt(pi) */
+    Float st = std::sqrt(1.f - ct * ct), nu = ct / st;
+    Float tmp = std::exp(-nu * nu) * 0.56418958354775628695f;   /* 1 / sqrt(pi) */
     return 0.5f * (ct * (1.f + std::erf(nu)) + st * tmp);
 }
-static float lean_sigma(V3 k, const LeanP &p) {
-    float a = k.x * p.ax + k.y * p.ay * p.rho, b = k.y * p.ay * p.srho, c = k.z - k.x * p.tx - k.y * p.ty;
-    float nrm = std::sqrt(a * a + b * b + c * c);
+static Float lean_sigma(V3 k, const LeanP &p) {
+    Float a = k.x * p.ax + k.y * p.ay * p.rho, b = k.y * p.ay * p.srho, c = k.z - k.x * p.tx - k.y * p.ty;
+    Float nrm = std::sqrt(a * a + b * b + c * c);
     return nrm * lean_sigma_std(c / nrm);
 }
-static float lean_g1(V3 k, const LeanP &p) { return dot(k, p.n) > 0.f ? k.z / lean_sigma(k, p) : 0.f; }
-static float lean_ndf(V3 h, const LeanP &p) {
+static Float lean_g1(V3 k, const LeanP &p) { return dot(k, p.n) > 0.f ? k.z / lean_sigma(k, p) : Float(0.f); }
+static Float lean_ndf(V3 h, const LeanP &p) {
     if (!(h.z > 5.9604644775390625e-08f)) return 0.f;
-    float t1 = h.z * h.z, t2 = t1 * t1;
-    float sx = -h.x / h.z - p.tx, sy = -h.y / h.z - p.ty;
-    float nrm = p.ax * p.ay * p.srho;
-    float x = sx / p.ax, y = (p.ax * sy - p.rho * p.ay * sx) / (p.ax * p.ay * p.srho);
+    Float t1 = h.z * h.z, t2 = t1 * t1;
+    Float sx = -h.x / h.z - p.tx, sy = -h.y / h.z - p.ty;
+    Float nrm = p.ax * p.ay * p.srho;
+    Float x = sx / p.ax, y = (p.ax * sy - p.rho * p.ay * sx) / (p.ax * p.ay * p.srho);
     return kInvPi * std::exp(-(x * x + y * y)) / nrm / t2;
 }
 /* SpecularManifoldGlints::lean_pdf (manifold_glints.cpp:557-579), local frame */
-static float glint_lean_pdf(const NormalMap &m, V2 uv, V2 duv_dx, V2 duv_dy, V3 wi, V3 wo) {
+static Float glint_lean_pdf(const NormalMap &m, V2 uv, V2 duv_dx, V2 duv_dy, V3 wi, V3 wo) {
     if (wi.z < 0.f || wo.z < 0.f) return 0.f;
-    V2 mu; float sa, sb, sc;
+    V2 mu; Float sa, sb, sc;
     lean_lookup(m, uv, lean_level(m, duv_dx, duv_dy), mu, sa, sb, sc);
     LeanP p = lean_params(mu, sa, sb, sc, 0.f);
     V3 h = normalize(wo + wi);
-    float G = lean_g1(wo, p) * lean_g1(wi, p);   /* LEAN::gaf: G1 ignores h */
+    Float G = lean_g1(wo, p) * lean_g1(wi, p);   /* LEAN::gaf: G1 ignores h */
     if (!(G > 0.f)) return 0.f;
-    float dp = dot(wi, h);
-    float vndf = dp > 0.f ? dp * lean_ndf(h, p) / lean_sigma(wi, p) : 0.f;
+    Float dp = dot(wi, h);
+    Float vndf = dp > 0.f ? dp * lean_ndf(h, p) / lean_sigma(wi, p) : Float(0.f);
     return vndf / (4.f * dot(wi, h));
 }
 
@@ -2514,10 +2618,10 @@ static void nm_frame(const NormalMap &m, V3 n, V3 dp_du, V2 uv, V3 &pn, V3 &ps, 
  * 116-139, conductor.cpp sample): reflection about the perturbed normal,
  * world-space directions; weight = Fresnel. */
 static bool nm_conductor_sample(const NormalMap &m, const sms_bsdf &b, V3 n, V3 dp_du, V2 uv, V3 wi_w,
-                                V3 &wo_w, float &weight) {
+                                V3 &wo_w, Float &weight) {
     V3 pn, ps, pt;
     nm_frame(m, n, dp_du, uv, pn, ps, pt);
-    float ci = dot(wi_w, pn);
+    Float ci = dot(wi_w, pn);
     if (!(ci > 0.f)) return false;
     wo_w = pn * (2.f * ci) - wi_w;
     if (!(dot(wo_w, n) * dot(wo_w, pn) > 0.f)) return false;
@@ -2530,7 +2634,7 @@ static bool nm_conductor_sample(const NormalMap &m, const sms_bsdf &b, V3 n, V3 
  * shading frame (fs, ft, n) and kept when it lies on the same side of both
  * frames' normals. */
 static bool nm_bsdf_sample(const NormalMap &m, const sms_bsdf &b, V3 fs, V3 ft, V3 n, V3 dp_du, V2 uv, V3 wi_w,
-                           float u1, float u2, float u3, PtBsdf &bs) {
+                           Float u1, Float u2, Float u3, PtBsdf &bs) {
     V3 pn, ps, pt;
     nm_frame(m, n, dp_du, uv, pn, ps, pt);
     const V3 wi(dot(wi_w, ps), dot(wi_w, pt), dot(wi_w, pn));
@@ -2545,17 +2649,17 @@ static bool nm_bsdf_sample(const NormalMap &m, const sms_bsdf &b, V3 fs, V3 ft, 
 
 /* PerspectiveCamera::importance (perspective.cpp:224-276) x film size for the
  * world-space direction d from the camera */
-static float pt_importance(const sms_camera &cam, const double tm[2], V3 d) {
+static Float pt_importance(const sms_camera &cam, const double tm[2], V3 d) {
     const float *M = cam.to_world;
     V3 dl(M[0] * d.x + M[4] * d.y + M[8] * d.z, M[1] * d.x + M[5] * d.y + M[9] * d.z,
           M[2] * d.x + M[6] * d.y + M[10] * d.z);
     if (!(dl.z > 0.f)) return 0.f;
-    float ic = 1.f / dl.z;
-    float px = dl.x * ic, py = dl.y * ic;
-    float tx = (float)tm[0], ty = (float)tm[1];
+    Float ic = 1.f / dl.z;
+    Float px = dl.x * ic, py = dl.y * ic;
+    Float tx = (Float)tm[0], ty = (Float)tm[1];
     if (!(px >= -tx && px <= tx && py >= -ty && py <= ty)) return 0.f;
-    float norm_ = 1.f / (4.f * tx * ty);
-    return norm_ * ic * ic * ic * (float)cam.width * (float)cam.height;
+    Float norm_ = 1.f / (4.f * tx * ty);
+    return norm_ * ic * ic * ic * (Float)cam.width * (Float)cam.height;
 }
 
 /* One camera sample (path id g) of the integrator; returns its radiance. */
@@ -2566,35 +2670,35 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
     const uint32_t px = pix % (uint32_t)cam.width, py = pix / (uint32_t)cam.width;
     PCG32 rng;
     rng.seed(opt.seed, g);
-    float ux = rng.next_f32(), uy = rng.next_f32();
+    Float ux = rng.next_f32(), uy = rng.next_f32();
     (void)rng.next_f32();
-    float sx = ((float)px + ux) / (float)cam.width, sy = ((float)py + uy) / (float)cam.height;
-    V3 dc = normalize(V3((float)tm[0] * (1.f - 2.f * sx), (float)tm[1] * (1.f - 2.f * sy), 1.f));
-    float inv_z = 1.f / dc.z;
+    Float sx = ((Float)px + ux) / (Float)cam.width, sy = ((Float)py + uy) / (Float)cam.height;
+    V3 dc = normalize(V3((Float)tm[0] * (1.f - 2.f * sx), (Float)tm[1] * (1.f - 2.f * sy), 1.f));
+    Float inv_z = 1.f / dc.z;
     const float *M = cam.to_world;
     Ray ray;
     ray.o = V3(M[3], M[7], M[11]);
     ray.d = normalize(V3(M[0] * dc.x + M[1] * dc.y + M[2] * dc.z, M[4] * dc.x + M[5] * dc.y + M[6] * dc.z,
                          M[8] * dc.x + M[9] * dc.y + M[10] * dc.z));
-    float near_clip = cam.near_clip > 0.f ? cam.near_clip : 1e-2f;
-    float far_clip = cam.far_clip > near_clip ? cam.far_clip : 1e4f;
+    Float near_clip = cam.near_clip > 0.f ? cam.near_clip : 1e-2f;
+    Float far_clip = cam.far_clip > near_clip ? cam.far_clip : 1e4f;
     ray.mint = near_clip * inv_z; ray.maxt = far_clip * inv_z;
     /* ray differentials (perspective.cpp:198-220), scaled by
        max(1/sqrt(spp), glint_diff_scale_factor_clamp) (integrator.cpp:164-165) */
     V3 rdx, rdy;
     {
-        auto cam_dir = [&](float ax, float ay) {
-            V3 c = normalize(V3((float)tm[0] * (1.f - 2.f * ax), (float)tm[1] * (1.f - 2.f * ay), 1.f));
+        auto cam_dir = [&](Float ax, Float ay) {
+            V3 c = normalize(V3((Float)tm[0] * (1.f - 2.f * ax), (Float)tm[1] * (1.f - 2.f * ay), 1.f));
             return normalize(V3(M[0] * c.x + M[1] * c.y + M[2] * c.z, M[4] * c.x + M[5] * c.y + M[6] * c.z,
                                 M[8] * c.x + M[9] * c.y + M[10] * c.z));
         };
-        float scale = std::max(1.f / std::sqrt((float)opt.spp), opt.glint_diff_scale_factor_clamp);
-        rdx = ray.d + (cam_dir(sx + 1.f / (float)cam.width, sy) - ray.d) * scale;
-        rdy = ray.d + (cam_dir(sx, sy + 1.f / (float)cam.height) - ray.d) * scale;
+        Float scale = omax(1.f / std::sqrt((Float)opt.spp), opt.glint_diff_scale_factor_clamp);
+        rdx = ray.d + (cam_dir(sx + 1.f / (Float)cam.width, sy) - ray.d) * scale;
+        rdy = ray.d + (cam_dir(sx, sy + 1.f / (Float)cam.height) - ray.d) * scale;
     }
     SI si = ray_intersect(sc, ray);
     V3 L(0.f), thr(1.f);
-    float eta = 1.f;
+    Float eta = 1.f;
     if (si.valid()) L += pt_emitted(sc, sc.shapes[si.shape], si.p, ray.d);
     bool spec_cam = true, prev_receiver = false;
     V3 prev_p;
@@ -2613,8 +2717,8 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
     for (int depth = 1;; ++depth) {
         if (!si.valid()) break;
         if (depth > opt.rr_depth) {
-            float q = std::min(hmax_v(thr) * eta * eta, 0.95f);
-            float u = rng.next_f32();
+            Float q = omin(hmax_v(thr) * eta * eta, 0.95f);
+            Float u = rng.next_f32();
             if (integ == SMS_INTEGRATOR_PATH ? !(u < q) : (u > q)) break;
             thr = thr * (1.f / q);
         }
@@ -2635,7 +2739,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         /* path_filtered_ss.cpp:109-110; light_connection_valid (path_filtered_ms.cpp:240-242) */
         const bool valid_conn = filtered_ss ? on_caster && (prev_receiver || glint_case)
                                             : filtered_ms && rec == 2 && rec_b == bounces;
-        const float caustic_eta = bsdf_eta(s.bsdf);
+        const Float caustic_eta = bsdf_eta(s.bsdf);
         const bool diffuse = s.bsdf.type == SMS_BSDF_DIFFUSE;
         /* the normal-mapped shape (glinty, or a caster / bouncer) carries the
            normalmap BSDF around its smooth conductor or dielectric */
@@ -2645,14 +2749,14 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                                (s.flags & SMS_SHAPE_GLINTY);
         if (on_glinty) {
             /* SurfaceInteraction::compute_partials (interaction.h:216-248) */
-            float dn = dot(si.n, si.p);
+            Float dn = dot(si.n, si.p);
             V3 dp_dx = ray.o + rdx * ((dn - dot(si.n, ray.o)) / dot(si.n, rdx)) - si.p;
             V3 dp_dy = ray.o + rdy * ((dn - dot(si.n, ray.o)) / dot(si.n, rdy)) - si.p;
-            float a00 = dot(si.dp_du, si.dp_du), a01 = dot(si.dp_du, si.dp_dv), a11 = dot(si.dp_dv, si.dp_dv);
-            float inv_det = 1.f / (a00 * a11 - a01 * a01);
+            Float a00 = dot(si.dp_du, si.dp_du), a01 = dot(si.dp_du, si.dp_dv), a11 = dot(si.dp_dv, si.dp_dv);
+            Float inv_det = 1.f / (a00 * a11 - a01 * a01);
             if (!std::isfinite(inv_det)) inv_det = 0.f;
-            float b0x = dot(si.dp_du, dp_dx), b1x = dot(si.dp_dv, dp_dx);
-            float b0y = dot(si.dp_du, dp_dy), b1y = dot(si.dp_dv, dp_dy);
+            Float b0x = dot(si.dp_du, dp_dx), b1x = dot(si.dp_dv, dp_dx);
+            Float b0y = dot(si.dp_du, dp_dy), b1y = dot(si.dp_dv, dp_dy);
             GQuery gq;
             gq.p = si.p; gq.n = si.shn; gq.dp_du = si.dp_du; gq.dp_dv = si.dp_dv; gq.sensor = ray.o; gq.uv = si.uv;
             gq.duv_dx.x = (a11 * b0x - a01 * b1x) * inv_det; gq.duv_dx.y = (a00 * b1x - a01 * b0x) * inv_det;
@@ -2671,14 +2775,14 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 Query qq; qq.p = si.p;
                 EI ei = sample_emitter_interaction(sc, sc.emitters_all, qq, r2);
                 V3 ed = ei.p - si.p;
-                float edist = norm(ed);
+                Float edist = norm(ed);
                 ed *= 1.f / edist;
-                float p_sms = 1.f;
+                Float p_sms = 1.f;
                 if (!ei.is_point) p_sms = pt_emitter_pdf(sc, sc.shapes[sc.emitters[ei.emitter].shape], si.p, ei.p, ed, edist);
-                float p_bsdf = glint_lean_pdf(sc.nmap, gq.uv, gq.duv_dx, gq.duv_dy, local(normalize(gq.sensor - si.p)),
+                Float p_bsdf = glint_lean_pdf(sc.nmap, gq.uv, gq.duv_dx, gq.duv_dy, local(normalize(gq.sensor - si.p)),
                                               local(ed)) + 1.f;
-                float mis = cfg.bsdf_strategy_only ? 0.f : mis_weight(p_sms, p_bsdf);
-                float We = pt_importance(cam, tm, normalize(si.p - ray.o));
+                Float mis = cfg.bsdf_strategy_only ? Float(0.f) : mis_weight(p_sms, p_bsdf);
+                Float We = pt_importance(cam, tm, normalize(si.p - ray.o));
                 L += thr * gv * (mis * We);
             }
             /* BSDF strategy inside the footprint (manifold_glints.cpp:178-220) */
@@ -2687,7 +2791,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             V2 uvo;
             uvo.x = si.uv.x + (fp.x - 0.5f) * gq.duv_dx.x + (fp.y - 0.5f) * gq.duv_dy.x;
             uvo.y = si.uv.y + (fp.x - 0.5f) * gq.duv_dx.y + (fp.y - 0.5f) * gq.duv_dy.y;
-            V3 bwo; float bw;
+            V3 bwo; Float bw;
             if (nm_conductor_sample(sc.nmap, s.bsdf, si.shn, si.dp_du, uvo, -ray.d, bwo, bw)) {
                 Ray br; br.o = si.p; br.d = bwo; br.mint = kRayEps * (1.f + hmax_abs(si.p)); br.maxt = kInf;
                 SI sb = ray_intersect(sc, br);
@@ -2695,9 +2799,9 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                     const Shape &es = sc.shapes[sb.shape];
                     V3 ep = br.o + br.d * sb.t;
                     V3 Le = pt_emitted(sc, es, ep, br.d);
-                    float p_bsdf = glint_lean_pdf(sc.nmap, uvo, gq.duv_dx, gq.duv_dy, wi_l, local(bwo)) + 1.f;
-                    float p_sms = pt_emitter_pdf(sc, es, si.p, ep, bwo, sb.t);
-                    float mis = cfg.sms_strategy_only ? 0.f : mis_weight(p_bsdf, p_sms);
+                    Float p_bsdf = glint_lean_pdf(sc.nmap, uvo, gq.duv_dx, gq.duv_dy, wi_l, local(bwo)) + 1.f;
+                    Float p_sms = pt_emitter_pdf(sc, es, si.p, ep, bwo, sb.t);
+                    Float mis = cfg.sms_strategy_only ? Float(0.f) : mis_weight(p_bsdf, p_sms);
                     L += thr * Le * (mis * bw);
                 }
             }
@@ -2720,7 +2824,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         if (integ == SMS_INTEGRATOR_PATH_SMS_SS) nee = nee || (depth == 1 && !opt.disable_reflected_emitters);
         if (filtered_ss || filtered_ms) nee = smooth && (!on_caster || valid_conn);
         if (nee) {
-            float ex = rng.next_f32(), ey = rng.next_f32();
+            Float ex = rng.next_f32(), ey = rng.next_f32();
             PtDir ds;
             if (pt_sample_emitter(sc, si.p, ex, ey, ds)) {
                 Ray sr; sr.o = si.p; sr.d = ds.d;
@@ -2729,7 +2833,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                     V3 wo(dot(ds.d, fs), dot(ds.d, ft), dot(ds.d, n_sh));
                     V3 bv = pt_bsdf_eval(s.bsdf, wi, wo);
                     if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
-                        float w = ds.delta ? 1.f : mis_weight(ds.pdf, pt_bsdf_pdf(s.bsdf, wi, wo));
+                        Float w = ds.delta ? Float(1.f) : mis_weight(ds.pdf, pt_bsdf_pdf(s.bsdf, wi, wo));
                         /* path_filtered_ss.cpp:127-142 / path_filtered_ms.cpp:137-150 */
                         if (valid_conn && (filtered_ms || depth > 1)) {
                             const bool refraction = wo.z * wi.z < 0.f;
@@ -2741,7 +2845,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             }
         }
         /* BSDF sampling */
-        float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
+        Float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
         PtBsdf bs;
         if (nmapped) {
             /* the normal-mapped BSDF at the hit's own uv */
@@ -2811,7 +2915,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             else if (filtered_ms)   /* light_hit_valid (path_filtered_ms.cpp:191) */
                 allow = !on_caster || (rec == 3 && rec_b == bounces) || spec_cam;
             if (allow) {
-                float epdf = bs.delta ? 0.f : pt_emitter_pdf(sc, es, si.p, ep, nr.d, si2.t);
+                Float epdf = bs.delta ? Float(0.f) : pt_emitter_pdf(sc, es, si.p, ep, nr.d, si2.t);
                 L += thr * Le * mis_weight(bs.pdf, epdf);
             } else if (mnee_ms && rec == 3 && rec_b == bounces) {
                 /* path_sms_ms.cpp:323-360: the MNEE walk from the receiver point */
@@ -2860,6 +2964,33 @@ static Scene *as_scene(void *p) { return reinterpret_cast<Scene *>(p); }
 using namespace orc;
 
 extern "C" {
+
+/* Which scalar type this build computes with: 0 float, 1 double, 2 counting float. */
+int oracle_build_kind() {
+#if defined(ORC_OPCOUNT)
+    return 2;
+#elif defined(ORC_DOUBLE)
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+/* Operation counts since the last reset, summed over every thread: add/sub,
+ * mul, div, sqrt, transcendental, BVH box tests, triangle tests, FLOPs inside
+ * those tests; zeros unless ORC_OPCOUNT. */
+void oracle_opcount_read(uint64_t *out) {
+#if defined(ORC_OPCOUNT)
+    orc_opcount::read_counters(out);
+#else
+    for (int i = 0; i < 8; ++i) out[i] = 0;
+#endif
+}
+void oracle_opcount_reset() {
+#if defined(ORC_OPCOUNT)
+    orc_opcount::reset_counters();
+#endif
+}
 
 void *oracle_scene_create() { return new Scene(); }
 void oracle_scene_destroy(void *s) { delete as_scene(s); }
@@ -2956,10 +3087,10 @@ void oracle_scene_finalize(void *s) {
     size_t np = sc->tri_shape.size();
     if (np) {
         std::vector<uint32_t> order(np);
-        std::vector<float> cen(3 * np);
+        std::vector<Float> cen(3 * np);
         for (uint32_t i = 0; i < np; ++i) {
             order[i] = i;
-            float lo[3], hi[3], c[3];
+            Float lo[3], hi[3], c[3];
             bvh_bounds(*sc, i, lo, hi, c);
             for (int k = 0; k < 3; ++k) cen[3 * i + k] = c[k];
         }
@@ -2993,8 +3124,9 @@ int oracle_ss_walk_batch(void *s, const sms_config *cfg, int caster, const float
         bool ok = sample_path(*sc, *cfg, caster, q, ei, smp, ps, sf, s0, it, V3(0.f, 0.f, 1.f), g);
         MVertex vf;
         if (ok) vertex_from_si(*sc, sf, vf);
-        float vals[SMS_WALK_OUT_FIELDS] = {ok ? 1.f : 0.f, (float)it, sf.p.x, sf.p.y, sf.p.z,
-                                           s0.p.x, s0.p.y, s0.p.z, vf.n.x, vf.n.y, vf.n.z};
+        float vals[SMS_WALK_OUT_FIELDS] = {ok ? 1.f : 0.f, (float)it, (float)sf.p.x, (float)sf.p.y,
+                                           (float)sf.p.z, (float)s0.p.x, (float)s0.p.y, (float)s0.p.z,
+                                           (float)vf.n.x, (float)vf.n.y, (float)vf.n.z};
         if (!ok) { for (int k = 2; k < 5; ++k) vals[k] = 0.f; for (int k = 8; k < 11; ++k) vals[k] = 0.f; }
         if (!s0.valid()) for (int k = 5; k < 8; ++k) vals[k] = 0.f;
         for (int k = 0; k < SMS_WALK_OUT_FIELDS; ++k) out[(size_t)k * n + i] = vals[k];
@@ -3277,7 +3409,7 @@ int oracle_glint_walk_batch(void *s, const sms_config *cfg, const float *queries
         V2 uvf, uvi;
         int it = 0;
         bool ok = sample_glint(*cfg, sc->nmap, q, lp, fp, uvf, uvi, it);
-        float vals[6] = {ok ? 1.f : 0.f, (float)it, uvf.x, uvf.y, uvi.x, uvi.y};
+        float vals[6] = {ok ? 1.f : 0.f, (float)it, (float)uvf.x, (float)uvf.y, (float)uvi.x, (float)uvi.y};
         for (int k = 0; k < 6; ++k) out[(size_t)k * n + i] = vals[k];
     }
     return 0;
@@ -3319,8 +3451,13 @@ int oracle_glint_connect_batch(void *s, const sms_config *cfg, const float *quer
 }
 
 /* Known-answer hooks for the dependency pins (fresnel.h:34-120, warp.h). */
-float oracle_fresnel(float cos_i, float eta, float *cos_t) { return fresnel(cos_i, eta, cos_t); }
-float oracle_fresnel_conductor(float cos_i, float eta, float k) { return fresnel_conductor(cos_i, eta, k); }
+float oracle_fresnel(float cos_i, float eta, float *cos_t) {
+    Float ct = 0.f;
+    const Float r = fresnel(cos_i, eta, cos_t ? &ct : nullptr);
+    if (cos_t) *cos_t = (float)ct;
+    return (float)r;
+}
+float oracle_fresnel_conductor(float cos_i, float eta, float k) { return (float)fresnel_conductor(cos_i, eta, k); }
 /* Image of spp samples per pixel (height x width x 3, row-major), the
  * library's sms_render restated path by path; nthreads host threads. */
 int oracle_render(void *s, const sms_config *cfg, const sms_camera *cam, const sms_render_options *opt,

@@ -58,6 +58,36 @@ def peaks():
     return 6800.0, "fallback"
 
 
+# Nominal FP32 SIMT peak of one GB300: 152 SMs x 128 FP32 lanes x 2 FLOP (FMA)
+# x the SM clock (no measured figure exists for it; the clock is the one sampled
+# during the timed region, else the 2070 MHz maximum).
+def fp32_peak_tflops(sm_mhz=None):
+    return 152 * 128 * 2 * (sm_mhz or 2070.0) * 1e6 / 1e12
+
+
+# Algorithmic bytes of the traversal, per the oracle's tree (a node: box 24 B +
+# child / leaf word 8 B = 32 B; a triangle: 3 vertices = 36 B).  One device node
+# record holds the boxes of both children, which the traversal tests together:
+# two oracle nodes, 64 B.
+NODE_RECORD_BYTES = 2 * 32
+TRIANGLE_BYTES = 36
+
+
+def flops_per_unit():
+    """FP32 work per ray / box test / triangle test / Newton iteration of each
+    benchmark configuration, counted by the oracle's op-counting build
+    (profiles/flops_per_unit.json, written by oracle/count_flops.py)."""
+    p = ROOT / "profiles" / "flops_per_unit.json"
+    return json.loads(p.read_text())["configs"] if p.exists() else {}
+
+
+def fp32_work(units, rays, box_tests, tri_tests):
+    """FLOPs of a kernel from its own ray, box-test and triangle-test counts."""
+    if not units:
+        return None
+    return rays * units["flops_per_ray"] + box_tests * units["flops_per_box"] + tri_tests * units["flops_per_triangle"]
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -138,17 +168,80 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline_sample(sms, W, n_sample: int, nthreads: int, seed: int = 1):
+def cpu_baseline_sample(sms, W, n_sample: int, nthreads: int, seed: int = 1, osc=None):
     """Time the oracle on a bounded sample of the workload (first n_sample
     queries of the 1M set).  Returns (connections/s, seconds, n_sample)."""
     from oracle import oracle as O
-    desc = W.water_scene()
-    osc = O.OracleScene(desc)
+    osc = osc or O.OracleScene(W.water_scene())
     q = W.water_queries(n_sample)
     t0 = time.perf_counter()
     osc.connect_batch(W.water_config(), q, seed=seed, nthreads=nthreads)
     dt = time.perf_counter() - t0
     return n_sample / dt, dt, n_sample
+
+
+def cpu_baseline_configs(sms, W, cores: int):
+    """The oracle's connections/s on bounded samples of the other benchmark
+    configurations, all cores and one thread."""
+    from oracle import oracle as O
+    cases = [
+        ("sphere_biased_m16", W.sphere_scene, W.sphere_config, lambda: W.sphere_queries(64), {}, 1024),
+        ("slab_two_bounce_biased_m32", W.slab_scene, W.slab_config, lambda: W.slab_queries(8192), {"multi": True},
+         512),
+        ("glints_8192_vectorized_m64", W.glint_scene, W.glint_config,
+         lambda: np.ascontiguousarray(W.glint_queries(1024)[:, ::16]), {"glints": True}, 4096),
+    ]
+    out = {}
+    for name, scene, config, queries, kw, n1 in cases:
+        osc = O.OracleScene(scene())
+        q = queries()
+        cfg = config()
+        osc.connect_batch(cfg, q[:, :64], seed=1, nthreads=cores, **kw)   # first touch (LEAN, caches)
+        t0 = time.perf_counter()
+        osc.connect_batch(cfg, q, seed=2, nthreads=cores, **kw)
+        dt = time.perf_counter() - t0
+        q1 = np.ascontiguousarray(q[:, :n1])
+        t1 = time.perf_counter()
+        osc.connect_batch(cfg, q1, seed=2, nthreads=1, **kw)
+        dt1 = time.perf_counter() - t1
+        out[name] = {"value": q.shape[1] / dt, "unit": UNIT, "cores": cores, "kind": "port",
+                     "single_thread": n1 / dt1,
+                     "sample": f"{q.shape[1]} queries ({dt:.2f} s); single thread {n1} queries ({dt1:.2f} s)"}
+    return out
+
+
+def basin_sample(sms, W, ctx, n: int = 16384):
+    """Per-walk parity on a sample of the headline workload's walks (explicit
+    seeds, light centre): the fraction of walks whose outcome differs between
+    the oracle's FP32, FP32-FMA and FP64 builds and one-ulp input nudges (basin
+    crossings), and the GPU's mismatch against the oracle on the rest."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import basin as B
+    from oracle import oracle as O
+    desc = W.water_scene()
+    cfg = sms.SMSConfig()
+    q = W.water_queries(n)
+    u = W.pcg32_streams_f32(11, np.arange(n, dtype=np.uint64), 2)
+    w = np.zeros((8, n), np.float32)
+    w[0], w[1], w[2] = 0.0, 0.05, 10.0
+    w[6], w[7] = u[0], u[1]
+    ens = B.oracle_walks(O, desc, "walk_batch", cfg, 0, q, w)
+    base = O.OracleScene(desc)
+    for up in (True, False):
+        ens["nudge_up" if up else "nudge_down"] = base.walk_batch(cfg, 0, q, B.nudge(w, slice(6, 8), up))
+    mask = B.well_conditioned_walks(ens)
+    saved = ctx.config
+    ctx.set_config(cfg)
+    out_g = sms.SpecularManifoldSingleScatter(ctx).sample_path(0, q, w)
+    ctx.set_config(saved)
+    agree = B.walk_outcome_equal(out_g, ens["f32"])
+    loo = B.leave_one_out_rates(ens)
+    return {"walks": n, "basin_crossing_fraction": 1.0 - float(mask.mean()),
+            "gpu_mismatch_well_conditioned": float(np.mean(~agree[mask])),
+            "gpu_mismatch_all": float(np.mean(~agree)),
+            "oracle_leave_one_out_max": max(loo.values()),
+            "note": "first walks of the headline scene from explicit seeds (light centre); well conditioned = "
+                    "same outcome in the oracle's FP32, FP32-FMA and FP64 builds and with the seeds nudged one ulp"}
 
 
 class DeviceTimer:
@@ -210,6 +303,16 @@ def secondary_configs(torch, sms, W, dev):
                      "walks_per_s": st["walks"] / (5 * t / 1e3), "walks_per_connection": walks,
                      "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),
                      "newton_iterations_per_s": its_per_s}
+        units = flops_per_unit().get(name)
+        if units:
+            if kind == "glints":
+                flops = st["newton_iterations"] * units["flops_per_newton_iteration"]
+            else:
+                flops = fp32_work(units, st["rays"], 2 * st["bvh_nodes"], st["tri_tests"])
+            tf = flops / (5 * t / 1e3) / 1e12
+            out[name]["fp32"] = {"achieved_tflops": tf, "peak_tflops": fp32_peak_tflops(),
+                                 "frac": tf / fp32_peak_tflops(), "peak_kind": "nominal",
+                                 "flops_per_newton_iteration": units["flops_per_newton_iteration"]}
         if kind == "glints":
             # one iteration gathers a 2x2 FP16 (sx, sy) texel block: 16 B of the
             # 256 MiB slope map (larger than L2)
@@ -562,15 +665,29 @@ def run_ours(args):
     e2e_value = world * n * args.steps / e2e_s
 
     # Roofline of the dominant kernel.  Algorithmic bytes per launch = the BVH
-    # node records (64 B) and triangle records (48 B) its traversals fetch, as
-    # counted by the kernel, plus its share of query/result I/O.
+    # nodes (32 B each; a device node record holds two) and triangles (36 B)
+    # its traversals fetch, as counted by the kernel.  Its FP32 work = rays x
+    # FLOPs per ray + box tests x FLOPs per box + triangle tests x FLOPs per
+    # triangle, the per-unit figures counted by the oracle on this workload.
     phases = {k: v for k, v in prof.items() if v["launches"]}
     dom = max(phases, key=lambda k: phases[k]["ms"])
     dp = phases[dom]
     per_launch_ms = dp["ms"] / dp["launches"]
-    alg_bytes = (dp["bvh_nodes"] * 64 + dp["tri_tests"] * 48) / dp["launches"]
+    alg_bytes = (dp["bvh_nodes"] * NODE_RECORD_BYTES + dp["tri_tests"] * TRIANGLE_BYTES) / dp["launches"]
     peak, peak_kind = peaks()
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    units = flops_per_unit().get("water_512_unbiased")
+    fp32 = None
+    if units:
+        flops = fp32_work(units, dp["rays"], 2 * dp["bvh_nodes"], dp["tri_tests"]) / dp["launches"]
+        tf = flops / (per_launch_ms / 1e3) / 1e12
+        fp32 = {"achieved_tflops": tf, "peak_tflops": fp32_peak_tflops(), "frac": tf / fp32_peak_tflops(),
+                "peak_kind": "nominal: 152 SMs x 128 lanes x FMA x 2070 MHz", "flops_per_launch": flops,
+                "flops_per_ray": units["flops_per_ray"], "flops_per_box": units["flops_per_box"],
+                "flops_per_triangle": units["flops_per_triangle"],
+                "note": "FLOPs counted by the oracle's op-counting build on this workload "
+                        "(profiles/flops_per_unit.json) x the kernel's own ray / box / triangle counts "
+                        "(speculative trial walks included)"}
     traffic = None
     tpath = ROOT / "profiles" / "traffic.json"
     if tpath.exists():
@@ -593,9 +710,10 @@ def run_ours(args):
         "phases_ms_per_step": {k: v["ms"] / args.steps for k, v in phases.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "bytes_per_launch": alg_bytes, "launch_ms": per_launch_ms,
-                     "note": "algorithmic bytes = BVH node (64 B) + triangle (48 B) records fetched by the "
-                             "kernel's traversals; the scene is L2-resident, so DRAM traffic stays far below"},
+                     "bytes_per_launch": alg_bytes, "launch_ms": per_launch_ms, "fp32": fp32,
+                     "note": "algorithmic bytes = BVH nodes (32 B; two per device node record) + triangles "
+                             "(36 B) fetched by the kernel's traversals; the scene is L2-resident, so DRAM "
+                             "traffic stays far below; the kernel is latency- and issue-bound (fp32)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16 * 4,
                 "d2h_bytes_per_step": n * 5 * 4},
         "gpu_launches": gpu_launches,
@@ -619,11 +737,18 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_render:
         line["render"] = render_study(torch, sms, W, dev, args.render_size, args.render_size, args.render_spp)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
         cores = os.cpu_count() or 1
         sample = int(os.environ.get("SMS_CPU_SAMPLE", str(N_QUERIES)))
-        v, dt, ns = cpu_baseline_sample(sms, W, sample, cores)
+        osc = O.OracleScene(W.water_scene())
+        v, dt, ns = cpu_baseline_sample(sms, W, sample, cores, osc=osc)
+        v1, dt1, ns1 = cpu_baseline_sample(sms, W, 8192, 1, osc=osc)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"first {ns} of the 1M queries, {dt:.1f} s"}
+                                "sample": f"first {ns} of the 1M queries, {dt:.1f} s; single thread: first "
+                                          f"{ns1} queries, {dt1:.1f} s",
+                                "single_thread": v1, "build": "g++ -O3, binned-SAH tree, std::thread per core",
+                                "configs": cpu_baseline_configs(sms, W, cores),
+                                "parity_sample": basin_sample(sms, W, ctx)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -24,15 +24,16 @@
 namespace orc_opcount {
 
 /* add .. transc: every counted operation.  box, tri: BVH box tests and
- * ray-triangle tests; trav: the FLOPs inside those tests (a subset of the
- * first five), so that traversal work can be scaled by the GPU's own node
- * and triangle counts, which depend on its tree. */
+ * ray-triangle tests; box_flops, tri_flops: the FLOPs inside those tests (a
+ * subset of the first five), so that traversal work can be scaled by the GPU's
+ * own node and triangle counts, which depend on its tree; rays: scene ray
+ * casts (closest hit and occlusion). */
 struct Counters {
     uint64_t add = 0, mul = 0, div = 0, sqrt = 0, transc = 0;
-    uint64_t box = 0, tri = 0, trav = 0;
+    uint64_t box = 0, tri = 0, box_flops = 0, tri_flops = 0, rays = 0;
     uint64_t flops() const { return add + mul + div + sqrt + transc; }
 };
-const int kNumCounters = 8;
+const int kNumCounters = 10;
 
 /* Totals of the threads that have exited (worker threads of a batch call). */
 inline std::atomic<uint64_t> *totals() {
@@ -48,7 +49,7 @@ struct ThreadCounters {
     ~ThreadCounters() {
         std::atomic<uint64_t> *t = totals();
         t[0] += c.add; t[1] += c.mul; t[2] += c.div; t[3] += c.sqrt; t[4] += c.transc;
-        t[5] += c.box; t[6] += c.tri; t[7] += c.trav;
+        t[5] += c.box; t[6] += c.tri; t[7] += c.box_flops; t[8] += c.tri_flops; t[9] += c.rays;
     }
 };
 
@@ -62,7 +63,8 @@ inline void read_counters(uint64_t out[kNumCounters]) {
     std::atomic<uint64_t> *t = totals();
     out[0] = t[0] + c.add; out[1] = t[1] + c.mul; out[2] = t[2] + c.div;
     out[3] = t[3] + c.sqrt; out[4] = t[4] + c.transc;
-    out[5] = t[5] + c.box; out[6] = t[6] + c.tri; out[7] = t[7] + c.trav;
+    out[5] = t[5] + c.box; out[6] = t[6] + c.tri; out[7] = t[7] + c.box_flops; out[8] = t[8] + c.tri_flops;
+    out[9] = t[9] + c.rays;
 }
 
 inline void reset_counters() {
@@ -77,8 +79,8 @@ struct TraversalScope {
     explicit TraversalScope(bool is_tri) : tri(is_tri), start(counters().flops()) {}
     ~TraversalScope() {
         Counters &c = counters();
-        if (tri) ++c.tri; else ++c.box;
-        c.trav += c.flops() - start;
+        if (tri) { ++c.tri; c.tri_flops += c.flops() - start; }
+        else { ++c.box; c.box_flops += c.flops() - start; }
     }
 };
 

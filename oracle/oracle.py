@@ -21,7 +21,8 @@ FMA_LIB_PATH = ORACLE_DIR / "liboracle_fma.so"
 # the counting scalar of op_count.h (operation counts, results identical to f32).
 VARIANT_PATHS = {"f32": LIB_PATH, "fma": FMA_LIB_PATH, "f64": ORACLE_DIR / "liboracle_f64.so",
                  "ops": ORACLE_DIR / "liboracle_ops.so"}
-OP_COUNT_NAMES = ("add", "mul", "div", "sqrt", "transcendental", "box_tests", "triangle_tests", "traversal_flops")
+OP_COUNT_NAMES = ("add", "mul", "div", "sqrt", "transcendental", "box_tests", "triangle_tests", "box_flops",
+                  "triangle_flops", "rays")
 
 _LIB = None
 _LIBS = {}
@@ -135,6 +136,27 @@ def op_counts(lib) -> dict:
 
 def reset_op_counts(lib) -> None:
     lib.oracle_opcount_reset()
+
+
+def flops_per_unit(desc, config, queries, seed: int = 1, nthreads: int | None = None, **kw) -> dict:
+    """Algorithmic FP32 work of one connection batch, from the counting build:
+    FLOPs per ray cast outside the traversal (Newton steps, vertex builds,
+    sampling, contributions: all non-traversal work divided by the rays cast),
+    per BVH box test and per ray-triangle test.  A kernel's FLOPs are then
+    rays x per_ray + box tests x per_box + triangle tests x per_triangle with
+    its own counts (its tree differs from the oracle's)."""
+    lib = load(variant="ops")
+    sc = OracleScene(desc, variant="ops")
+    reset_op_counts(lib)
+    _, _, _, st = sc.connect_batch(config, queries, seed=seed, nthreads=nthreads, **kw)
+    c = op_counts(lib)
+    trav = c["box_flops"] + c["triangle_flops"]
+    return {"flops_per_ray": (c["flops"] - trav) / max(1, c["rays"]),
+            "flops_per_box": c["box_flops"] / max(1, c["box_tests"]),
+            "flops_per_triangle": c["triangle_flops"] / max(1, c["triangle_tests"]),
+            "flops_per_newton_iteration": c["flops"] / max(1, st["newton_iterations"]),
+            "transcendentals_per_newton_iteration": c["transcendental"] / max(1, st["newton_iterations"]),
+            "counts": c, "stats": st, "queries": int(queries.shape[1])}
 
 
 def _f3(v):

@@ -47,14 +47,17 @@ namespace orc {
 typedef orc_opcount::CFloat Float;
 #define ORC_COUNT_FP64_OPS(n) (orc_opcount::counters().add += (n))
 #define ORC_TRAVERSAL_SCOPE(is_tri) orc_opcount::TraversalScope orc_scope_(is_tri)
+#define ORC_COUNT_RAY() (++orc_opcount::counters().rays)
 #elif defined(ORC_DOUBLE)
 typedef double Float;
 #define ORC_COUNT_FP64_OPS(n) ((void)0)
 #define ORC_TRAVERSAL_SCOPE(is_tri) ((void)0)
+#define ORC_COUNT_RAY() ((void)0)
 #else
 typedef float Float;
 #define ORC_COUNT_FP64_OPS(n) ((void)0)
 #define ORC_TRAVERSAL_SCOPE(is_tri) ((void)0)
+#define ORC_COUNT_RAY() ((void)0)
 #endif
 
 /* std::max / std::min for operands that may differ in type (a Float and a
@@ -508,6 +511,7 @@ static bool ray_is_nan(const Ray &r) {
 }
 
 static SI ray_intersect(const Scene &sc, const Ray &ray) {
+    ORC_COUNT_RAY();
     SI si;
     /* a NaN ray hits nothing (all intersection comparisons are false) */
     if (ray_is_nan(ray)) return si;
@@ -560,6 +564,7 @@ static SI ray_intersect(const Scene &sc, const Ray &ray) {
 
 /* Scene::ray_test (src/librender/scene.cpp:144-152) */
 static bool ray_test(const Scene &sc, const Ray &ray) {
+    ORC_COUNT_RAY();
     if (ray_is_nan(ray)) return false;
     for (const Shape &s : sc.shapes) {
         Float t;
@@ -2978,12 +2983,13 @@ int oracle_build_kind() {
 
 /* Operation counts since the last reset, summed over every thread: add/sub,
  * mul, div, sqrt, transcendental, BVH box tests, triangle tests, FLOPs inside
- * those tests; zeros unless ORC_OPCOUNT. */
+ * the box tests, FLOPs inside the triangle tests, ray casts; zeros unless
+ * ORC_OPCOUNT. */
 void oracle_opcount_read(uint64_t *out) {
 #if defined(ORC_OPCOUNT)
     orc_opcount::read_counters(out);
 #else
-    for (int i = 0; i < 8; ++i) out[i] = 0;
+    for (int i = 0; i < 10; ++i) out[i] = 0;
 #endif
 }
 void oracle_opcount_reset() {

@@ -338,6 +338,7 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
         }
     }
     if (sc.n_tris == 0) return found;
+    bool tri_best = false;
     // Reciprocal direction, a zero component replaced by 1e-20 of its sign so
     // that every slab distance is finite (a slab the ray runs inside then
     // spans about +-1e20 and constrains nothing).
@@ -370,12 +371,20 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
             const float4 *tp = sc.tris + 3 * (size_t)ti;
             float4 a = sms_ldg(tp), b = sms_ldg(tp + 1), c = sms_ldg(tp + 2);
             float t, u, v;
-            if (tri_hit(a, b, c, o, d, mint, hit.t, t, u, v) && (!found || t < hit.t)) {
-                hit.t = t; hit.u = u; hit.v = v;
-                hit.shape = sms_as_int(a.w);
-                hit.prim = (uint32_t)sms_as_int(b.w);
-                found = true;
-                if (any_hit) return true;
+            if (tri_hit(a, b, c, o, d, mint, hit.t, t, u, v)) {
+                const int shape = sms_as_int(a.w);
+                const uint32_t prim = (uint32_t)sms_as_int(b.w);
+                // Equal distances (a ray through a shared edge) go to the lower
+                // (shape, face) index, so the hit does not depend on the tree.
+                if (!found || t < hit.t ||
+                    (t == hit.t && tri_best && (shape < hit.shape || (shape == hit.shape && prim < hit.prim)))) {
+                    hit.t = t; hit.u = u; hit.v = v;
+                    hit.shape = shape;
+                    hit.prim = prim;
+                    found = true;
+                    tri_best = true;
+                    if (any_hit) return true;
+                }
             }
         }
         bool il = hl && n3.z == 0, ir = hr && n3.w == 0;

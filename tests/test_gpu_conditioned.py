@@ -1,0 +1,203 @@
+"""GPU parity on well-conditioned walks and connections, and parity at the
+benchmark's own sizes, through the C ABI.
+
+A walk is well conditioned when the oracle gives the same outcome (converged
+flag and solution) in FP32, FP32 with FMA contraction, FP64, and FP32 with its
+inputs moved by one ulp either way (tests/basin.py); the rest is the
+basin-crossing fraction, which is printed.  On well-conditioned walks the GPU
+must agree with the oracle on all but WELL_CONDITIONED_MISMATCH = 0.1 % of the
+walks -- or, on a chaotic scene, on all but the fraction that one more
+perturbation of the oracle itself flips: the largest leave-one-out rate of the
+ensemble (a member's mismatch on the walks the other members agree on).  On the
+spheres and glints that rate is zero; on the water heightfield, whose walks
+change basin under a one-ulp seed nudge several percent of the time, it is
+not.  Biased
+unique-solution counts on the conductor sphere must be bit-exact on every
+well-conditioned query of the full 64 x 64 grid (the glass sphere of the same
+scene has no single-refraction solution below it: zero counts on both sides).
+The headline scene (512 x 512 water, 65,536 of the benchmark's own queries)
+and the 8192^2 glint map (65,536 camera footprints) are also held to the
+oracle-vs-FMA floor rule of the other parity tests.
+"""
+import numpy as np
+import pytest
+
+import basin as B
+from test_gpu_ss_parity import FLOOR_FACTOR, FLOOR_SLACK, _connect_diff
+
+pytestmark = pytest.mark.gpu
+
+WELL_CONDITIONED_MISMATCH = 0.001
+
+
+def _walk_ensemble(oracle, desc, fn, args, walk_in_index, nudge_rows):
+    """Oracle outputs of the same walks in three builds and with the walk
+    inputs (argument walk_in_index) moved by one ulp up and down."""
+    ens = B.oracle_walks(oracle, desc, fn, *args)
+    base = oracle.OracleScene(desc)
+    for up in (True, False):
+        a = list(args)
+        a[walk_in_index] = B.nudge(args[walk_in_index], nudge_rows, up)
+        ens["nudge_up" if up else "nudge_down"] = getattr(base, fn)(*a)
+    return ens
+
+
+def _check_walks(label, out_g, ens, rows=slice(2, 5)):
+    mask = B.well_conditioned_walks(ens, rows)
+    agree = B.walk_outcome_equal(out_g, ens["f32"], rows)
+    mism = float(np.mean(~agree[mask]))
+    basin = 1.0 - float(mask.mean())
+    loo = B.leave_one_out_rates(ens, rows)
+    print(f"{label}: basin-crossing {basin:.4f} | gpu mismatch on well-conditioned {mism:.5f} "
+          f"({int((~agree[mask]).sum())} of {int(mask.sum())}) | all walks {float(np.mean(~agree)):.4f} | "
+          f"oracle leave-one-out " + " ".join(f"{k} {v:.4f}" for k, v in loo.items()))
+    assert mask.sum() > 0.5 * len(mask)
+    assert mism < max(WELL_CONDITIONED_MISMATCH, max(loo.values()))
+    return basin, mism
+
+
+def _ss_walk_in(W, n, light, seed=11):
+    u = W.pcg32_streams_f32(seed, np.arange(n, dtype=np.uint64), 2)
+    w = np.zeros((8, n), np.float32)
+    w[0], w[1], w[2] = light
+    w[6], w[7] = u[0], u[1]
+    return w
+
+
+@pytest.mark.parametrize("halfvector", [False, True])
+@pytest.mark.parametrize("conductor", [False, True])
+def test_sphere_walks_well_conditioned(sms, workloads, oracle, gpu_lib, conductor, halfvector):
+    W = workloads
+    desc = W.sphere_scene(conductor=conductor)
+    cfg = sms.SMSConfig(halfvector_constraints=halfvector)
+    ss = sms.SpecularManifoldSingleScatter(sms.Context(sms.Scene(desc), cfg))
+    q = W.sphere_queries(64)
+    w = _ss_walk_in(W, q.shape[1], (0.0, 0.0, 5.0))
+    ens = _walk_ensemble(oracle, desc, "walk_batch", (cfg, 0, q, w), 3, slice(6, 8))
+    _check_walks(f"sphere conductor={conductor} halfvector={halfvector}", ss.sample_path(0, q, w), ens)
+
+
+@pytest.mark.parametrize("res", [128, 512])
+def test_water_walks_well_conditioned(sms, workloads, oracle, gpu_lib, res):
+    W = workloads
+    desc = W.water_scene(res=res)
+    cfg = sms.SMSConfig()
+    ss = sms.SpecularManifoldSingleScatter(sms.Context(sms.Scene(desc), cfg))
+    n = 16384
+    q = W.water_queries(n)
+    w = _ss_walk_in(W, n, (0.0, 0.05, 10.0))
+    ens = _walk_ensemble(oracle, desc, "walk_batch", (cfg, 0, q, w), 3, slice(6, 8))
+    _check_walks(f"water{res}", ss.sample_path(0, q, w), ens)
+
+
+def test_slab_walks_well_conditioned(sms, workloads, oracle, gpu_lib):
+    W = workloads
+    desc = W.slab_scene()
+    cfg = sms.SMSConfig(bounces=2, max_iterations=30)
+    ms = sms.SpecularManifoldMultiScatter(sms.Context(sms.Scene(desc), cfg))
+    n = 8192
+    q = W.slab_queries(n)
+    w = _ss_walk_in(W, n, (0.0, 0.0, 5.0))
+    ens = _walk_ensemble(oracle, desc, "ms_walk_batch", (cfg, 0, q, w), 3, slice(6, 8))
+    _check_walks("slab", ms.sample_path(0, q, w), ens, rows=slice(2, 8))
+
+
+def test_glint_walks_well_conditioned(sms, workloads, oracle, gpu_lib):
+    W = workloads
+    desc = W.glint_scene(map_res=1024)
+    cfg = W.glint_config()
+    gl = sms.SpecularManifoldGlints(sms.Context(sms.Scene(desc), cfg))
+    q = W.glint_queries(128)
+    n = q.shape[1]
+    _, light = W.glint_camera()
+    u = W.pcg32_streams_f32(5, np.arange(n, dtype=np.uint64), 2)
+    w = np.zeros((5, n), np.float32)
+    w[0:3] = np.asarray(light, np.float32)[:, None]
+    w[3], w[4] = u[0], u[1]
+    ens = _walk_ensemble(oracle, desc, "glint_walk_batch", (cfg, q, w), 2, slice(3, 5))
+    _check_walks("glints 1024^2", gl.sample_glint(q, w), ens, rows=slice(2, 4))
+
+
+def test_sphere_counts_bit_exact(sms, workloads, oracle, gpu_lib):
+    """Biased unique-solution counts (manifold_ss.cpp:142-197) on the full
+    64 x 64 grid of the conductor sphere: equal on every well-conditioned
+    query."""
+    W = workloads
+    desc = W.sphere_scene(conductor=True)
+    cfg = W.sphere_config()
+    ss = sms.SpecularManifoldSingleScatter(sms.Context(sms.Scene(desc), cfg))
+    q = W.sphere_queries(64)
+    vg, cg, wg = ss.specular_manifold_sampling(q, seed=1)
+    ens = B.oracle_connections(oracle, desc, cfg, q, seed=1)
+    base = oracle.OracleScene(desc)
+    for up in (True, False):
+        ens["nudge_up" if up else "nudge_down"] = base.connect_batch(cfg, B.nudge(q, slice(0, 3), up), seed=1)
+    mask = B.well_conditioned_connections(ens)
+    co = ens["f32"][1]
+    print(f"sphere counts: unique {int(co.sum())} (oracle) vs {int(cg.sum())} (gpu); well-conditioned "
+          f"{int(mask.sum())}/{len(mask)}; mismatches there {int((cg != co)[mask].sum())}, elsewhere "
+          f"{int((cg != co)[~mask].sum())}")
+    assert co.sum() > 100
+    assert np.array_equal(cg[mask], co[mask])
+    assert np.array_equal(wg, ens["f32"][2])
+    # the glass sphere of the same scene: no solution on either side
+    desc_g = W.sphere_scene(conductor=False)
+    ss_g = sms.SpecularManifoldSingleScatter(sms.Context(sms.Scene(desc_g), cfg))
+    _, cgg, _ = ss_g.specular_manifold_sampling(q, seed=1)
+    _, cog, _, _ = oracle.OracleScene(desc_g).connect_batch(cfg, q, seed=1)
+    assert cgg.sum() == 0 and cog.sum() == 0
+
+
+def test_water512_connect_benchmark_queries(sms, workloads, oracle, gpu_lib):
+    """The headline configuration itself: 512 x 512 water (522,242 triangles),
+    unbiased, trials <= 256, on the first 65,536 of the benchmark's 1M
+    queries (seed 3)."""
+    W = workloads
+    desc = W.water_scene(res=512)
+    cfg = W.water_config()
+    ss = sms.SpecularManifoldSingleScatter(sms.Context(sms.Scene(desc), cfg))
+    n = 65536
+    q = W.water_queries(n)
+    vg, cg, wg = ss.specular_manifold_sampling(q, seed=3)
+    ens = B.oracle_connections(oracle, desc, cfg, q, seed=3)
+    base = oracle.OracleScene(desc)
+    for up in (True, False):
+        ens["nudge_up" if up else "nudge_down"] = base.connect_batch(cfg, B.nudge(q, slice(0, 3), up), seed=3)
+    vo, co, wo, _ = ens["f32"]
+    vf, cf, wf, _ = ens["fma"]
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    mask = B.well_conditioned_connections(ens)
+    agree = B.connection_equal((vg, cg, wg), ens["f32"])
+    mism = float(np.mean(~agree[mask]))
+    loo = B.leave_one_out_connection_rates(ens)
+    print(f"water512 connect 65536: count mismatch {g_cm:.4f} differs {g_diff:.4f} (floor {f_cm:.4f}/{f_diff:.4f}) "
+          f"median rel {g_med:.1e}; ill-conditioned {1 - mask.mean():.4f}; gpu differs on well-conditioned "
+          f"{mism:.5f}; oracle leave-one-out " + " ".join(f"{k} {v:.4f}" for k, v in loo.items()))
+    assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+    assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+    assert g_med < 1e-4
+    assert mism < max(WELL_CONDITIONED_MISMATCH, max(loo.values()))
+
+
+def test_glint8192_connect_benchmark_footprints(sms, workloads, oracle, gpu_lib):
+    """The glint benchmark's 8192^2 FP16 map, on 65,536 of its 1024^2 camera
+    footprints (every k-th query), biased vectorized estimator."""
+    W = workloads
+    desc = W.glint_scene(map_res=8192)
+    cfg = W.glint_config()
+    gl = sms.SpecularManifoldGlints(sms.Context(sms.Scene(desc), cfg))
+    qa = W.glint_queries(1024)
+    step = qa.shape[1] // 65536
+    q = np.ascontiguousarray(qa[:, ::step][:, :65536])
+    vg, cg, wg = gl.specular_manifold_sampling(q, seed=3)
+    vo, co, wo, _ = oracle.OracleScene(desc).connect_batch(cfg, q, seed=3, glints=True)
+    vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=3, glints=True)
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    print(f"glint8192 connect 65536: count mismatch {g_cm:.5f} differs {g_diff:.5f} (floor {f_cm:.5f}/{f_diff:.5f}) "
+          f"median rel {g_med:.1e} nonzero {(co > 0).mean():.3f}")
+    assert (co > 0).sum() > 500
+    assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+    assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+    assert g_med < 1e-4

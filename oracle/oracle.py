@@ -62,8 +62,8 @@ _FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 
 def build() -> Path:
-    """Compile liboracle.so with the committed Makefile."""
-    r = subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], capture_output=True, text=True)
+    """Compile the oracle's four builds with the committed Makefile."""
+    r = subprocess.run(["make", "-s", "-j4", "-C", str(ORACLE_DIR)], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
     return LIB_PATH

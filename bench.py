@@ -227,8 +227,9 @@ def basin_sample(sms, W, ctx, n: int = 16384):
     w[6], w[7] = u[0], u[1]
     ens = B.oracle_walks(O, desc, "walk_batch", cfg, 0, q, w)
     base = O.OracleScene(desc)
-    for up in (True, False):
-        ens["nudge_up" if up else "nudge_down"] = base.walk_batch(cfg, 0, q, B.nudge(w, slice(6, 8), up))
+    for name, rows in (("seed", slice(6, 8)), ("light", slice(0, 3))):
+        for up in (True, False):
+            ens[f"{name}_{'up' if up else 'down'}"] = base.walk_batch(cfg, 0, q, B.nudge(w, rows, up))
     mask = B.well_conditioned_walks(ens)
     saved = ctx.config
     ctx.set_config(cfg)
@@ -241,7 +242,8 @@ def basin_sample(sms, W, ctx, n: int = 16384):
             "gpu_mismatch_all": float(np.mean(~agree)),
             "oracle_leave_one_out_max": max(loo.values()),
             "note": "first walks of the headline scene from explicit seeds (light centre); well conditioned = "
-                    "same outcome in the oracle's FP32, FP32-FMA and FP64 builds and with the seeds nudged one ulp"}
+                    "same outcome in the oracle's FP32, FP32-FMA and FP64 builds and with the seed sample or the light point "
+                    "nudged one ulp"}
 
 
 class DeviceTimer:
@@ -451,11 +453,12 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     ws = torch.empty(ns, dtype=torch.int32, device=f"cuda:{dev}")
     torch.cuda.synchronize()
     tune = autotune_ss(sms, ctx, qs.data_ptr(), ns, vs.data_ptr(), cs.data_ptr(), ws.data_ptr(),
-                       blocks_per_sm=(16,), trial_groups=(8, 16, 32), seed=99)
+                       blocks_per_sm=(16,), trial_groups=(8, 16, 32), treelets=(0,), seed=99)
     learned_group = tune["best"][1]
     ctx.set_proposal(None)
     ctx.set_launch(0, 0)
     ctx.set_trial_group(0)
+    ctx.set_treelet(0)
 
     def render(spp, seed, offset, learned, stats=None):
         ctx.set_proposal(prop if learned else None, 0.1)
@@ -700,6 +703,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "queries_per_step": n, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}",
                    "launch": ({"blocks_per_sm": tuned["best"][0], "trial_group": tuned["best"][1],
+                               "treelet_nodes": tuned["best"][2],
                                "autotune_ms": tuned["ms"]} if tuned else "library default")},
         "walks_per_s": world * st["walks"] / total_s,
         "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),

@@ -202,6 +202,12 @@ sms_status sms_ctx_set_launch(sms_ctx *ctx, int32_t blocks_per_sm, int32_t threa
  * 8 with a learned proposal.  No counterpart in the reference (a tuning knob
  * of the batched solver). */
 sms_status sms_ctx_set_trial_group(sms_ctx *ctx, int32_t group);
+/* Top node records of the scene's tree (stored breadth first) that the
+ * Bernoulli-trial kernel copies into each block's shared memory before it
+ * traverses, 0..384 (0 = none, the default).  Replaces node fetches through
+ * L1 for the top levels; results do not depend on it.  No counterpart in the
+ * reference (a staging knob of the batched solver, set by the autotuner). */
+sms_status sms_ctx_set_treelet(sms_ctx *ctx, int32_t nodes);
 
 /* ---------------------------------------------------------------- queries */
 /* Shading-point query, SoA with SMS_QUERY_FIELDS rows of n floats each:

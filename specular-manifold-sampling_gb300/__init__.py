@@ -147,6 +147,7 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ctx_stream": (vp, [vp]),
         "sms_ctx_set_launch": (i32, [vp, i32, i32]),
         "sms_ctx_set_trial_group": (i32, [vp, i32]),
+        "sms_ctx_set_treelet": (i32, [vp, i32]),
         "sms_stats_read": (i32, [vp, C.POINTER(_Stats)]),
         "sms_stats_reset": (i32, [vp]),
         "sms_ctx_set_profiling": (i32, [vp, i32]),
@@ -416,6 +417,11 @@ class Context:
     def set_trial_group(self, group: int = 0):
         """Lanes per query of the Bernoulli-trial kernel (0 auto, 8, 16, 32)."""
         _check(_LIB.sms_ctx_set_trial_group(self._h, group))
+
+    def set_treelet(self, nodes: int = 0):
+        """Top node records of the tree the Bernoulli-trial kernel stages in
+        shared memory (0..384, 0 = none)."""
+        _check(_LIB.sms_ctx_set_treelet(self._h, nodes))
 
     def stats(self) -> dict:
         s = _Stats()

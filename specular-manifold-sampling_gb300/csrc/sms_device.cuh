@@ -240,7 +240,24 @@ struct DevScene {
     uint32_t lean_off[kMaxLeanLevels];
     int lean_levels;
     const DevEmitter *emitters;
+    // The first n_tnodes node records (the top levels of the tree: records are
+    // stored breadth first) are also held in the launching kernel's dynamic
+    // shared memory (sms_tree_smem), filled by tree_smem_fill; 0 = none.
+    uint32_t n_tnodes;
 };
+
+#ifdef __CUDACC__
+// Dynamic shared memory of a kernel that stages the top of the tree.
+extern __shared__ __align__(16) float4 sms_tree_smem[];
+
+// Copy the first sc.n_tnodes node records into sms_tree_smem (all threads of
+// the block call it before any traversal).
+__device__ __forceinline__ void tree_smem_fill(const DevScene &sc) {
+    if (sc.n_tnodes == 0) return;
+    for (uint32_t i = threadIdx.x; i < 4 * sc.n_tnodes; i += blockDim.x) sms_tree_smem[i] = __ldg(sc.nodes + i);
+    __syncthreads();
+}
+#endif
 
 // ------------------------------------------------------------------ hits
 struct Hit {
@@ -353,9 +370,20 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
     while (true) {
         if (budget-- == 0) { err |= kErrTraversalLimit; return false; }
         hit.nodes++;
-        const float4 *np = sc.nodes + 4 * (size_t)node;
-        float4 n0 = sms_ldg(np), n1 = sms_ldg(np + 1), n2 = sms_ldg(np + 2);
-        int4 n3 = sms_ldg(reinterpret_cast<const int4 *>(np + 3));
+        float4 n0, n1, n2;
+        int4 n3;
+#ifdef __CUDA_ARCH__
+        if ((uint32_t)node < sc.n_tnodes) {
+            const float4 *sp = sms_tree_smem + 4 * node;
+            n0 = sp[0]; n1 = sp[1]; n2 = sp[2];
+            n3 = *reinterpret_cast<const int4 *>(sp + 3);
+        } else
+#endif
+        {
+            const float4 *np = sc.nodes + 4 * (size_t)node;
+            n0 = sms_ldg(np); n1 = sms_ldg(np + 1); n2 = sms_ldg(np + 2);
+            n3 = sms_ldg(reinterpret_cast<const int4 *>(np + 3));
+        }
         float tl, tr;
         bool hl = box2(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, inv, oi, mint, hit.t, tl);
         bool hr = box2(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, inv, oi, mint, hit.t, tr);

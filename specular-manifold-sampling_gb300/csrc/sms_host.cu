@@ -350,6 +350,7 @@ struct sms_ctx {
     int blocks_per_sm = 0;
     int threads = 128;
     int trial_group = 0;          // lanes per query of the Bernoulli-trial kernel (0: auto)
+    uint32_t treelet = 0;         // node records the trial kernel stages in shared memory
     // device staging for the host-pointer entry points
     void *io = nullptr;
     size_t io_bytes = 0;
@@ -673,6 +674,14 @@ extern "C" sms_status sms_ctx_set_trial_group(sms_ctx *c, int32_t group) {
     return SMS_OK;
 }
 
+extern "C" sms_status sms_ctx_set_treelet(sms_ctx *c, int32_t nodes) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    if (nodes < 0 || nodes > kMaxTreeletNodes)
+        return fail(SMS_ERR_INVALID_ARG, "treelet size must be in [0, 384] node records");
+    c->treelet = (uint32_t)nodes;
+    return SMS_OK;
+}
+
 extern "C" sms_status sms_ctx_set_launch(sms_ctx *c, int32_t bps, int32_t tpb) {
     if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
     if (bps < 0 || tpb < 0) return fail(SMS_ERR_INVALID_ARG, "negative launch parameter");
@@ -847,7 +856,7 @@ sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
     sc.streams = streams;
     CUDA_TRY(launch_ss_connect(c->dsc, sc, q, n, seed, stream_off, out->value, out->count, out->walks, c->ctr, scr,
                                c->num_sms, c->blocks_per_sm, &c->timer, c->stream, c->prop ? &pr : nullptr,
-                               c->trial_group));
+                               c->trial_group, c->treelet));
     return SMS_OK;
 }
 

@@ -63,6 +63,10 @@ struct SsScratch {
 // Bytes of SsScratch for n queries.
 inline size_t ss_scratch_bytes(uint32_t n) { return (size_t)n * (4 + 12 + 12 + 4); }
 
+// Largest shared-memory treelet of the trial kernel: 384 node records (24 KB
+// per block; 8 resident blocks of 128 threads stay within 227 KB per SM).
+constexpr int kMaxTreeletNodes = 384;
+
 cudaError_t launch_ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, const float *q,
                            const float *w, uint32_t n, float *out, DevCounters *ctr, PhaseTimer *tm,
                            cudaStream_t s);
@@ -70,7 +74,7 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
                               uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
                               DevCounters *ctr, const SsScratch &scr, int num_sms, int blocks_per_sm,
                               PhaseTimer *tm, cudaStream_t s, const mlp::SeedProposal *prop = nullptr,
-                              int trial_group = 0);
+                              int trial_group = 0, uint32_t treelet = 0);
 // The proposal network for every query of a batch (ss_proposal_kernel).
 cudaError_t launch_ss_proposal(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                                uint64_t stream_off, const mlp::SeedProposal &pr, int num_sms, cudaStream_t s);

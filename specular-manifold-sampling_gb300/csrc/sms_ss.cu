@@ -245,7 +245,7 @@ static int ss_variant(const DevScene &sc, const SolverCfg &cfg, int c) {
 cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                               uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                               const SsScratch &scr, int num_sms, int blocks_per_sm, PhaseTimer *tm,
-                              cudaStream_t s, const mlp::SeedProposal *prop, int trial_group) {
+                              cudaStream_t s, const mlp::SeedProposal *prop, int trial_group, uint32_t treelet) {
     if (n == 0) return cudaSuccess;
     const int bps = blocks_per_sm > 0 ? blocks_per_sm : 16;
     if (cfg.biased) {
@@ -273,10 +273,10 @@ cudaError_t launch_ss_connect(const DevScene &sc, const SolverCfg &cfg, const fl
                                     bps, tm, s, trial_group);
         else if (var)
             e = ss_caster_launch<1, true>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, ctr, scr, num_sms,
-                                          bps, tm, s, prop, trial_group);
+                                          bps, tm, s, prop, trial_group, treelet);
         else
             e = ss_caster_launch<0, true>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, ctr, scr, num_sms,
-                                          bps, tm, s, prop, trial_group);
+                                          bps, tm, s, prop, trial_group, treelet);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_trials_kernel(
                                                         mlp::SeedProposal pr) {
     static_assert(G == 8 || G == 16 || G == 32, "group size");
     constexpr bool kRough = (kVar & 1) != 0, kTwo = (kVar & 2) != 0, kNM = (kVar & 4) != 0;
+    tree_smem_fill(sc);
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31;
     const unsigned gbase = lane & ~(unsigned)(G - 1), gl = lane - gbase;
@@ -408,8 +409,12 @@ template <int kVar, bool kLearnedOk>
 cudaError_t ss_caster_launch(const DevScene &sc, const SolverCfg &cfg, int c, const float *q, uint32_t n,
                              uint64_t seed, uint64_t stream_off, float *value, int *count, int *walks,
                              DevCounters *ctr, const SsScratch &scr, int num_sms, int bps, PhaseTimer *tm,
-                             cudaStream_t s, const mlp::SeedProposal *prop, int trial_group) {
+                             cudaStream_t s, const mlp::SeedProposal *prop, int trial_group, uint32_t treelet = 0) {
     const bool learned = kLearnedOk && prop && prop->shape == sc.casters_ss[c];
+    // the trial kernel holds the top `treelet` node records in shared memory
+    DevScene st = sc;
+    st.n_tnodes = std::min<uint32_t>(treelet, sc.n_nodes);
+    const size_t tsmem = (size_t)st.n_tnodes * 4 * sizeof(float4);
     const mlp::SeedProposal pr = learned ? *prop : mlp::SeedProposal{};
     phase_begin(tm, kPhaseSsFirst, s);
     cudaError_t e = cudaSuccess;
@@ -433,14 +438,15 @@ cudaError_t ss_caster_launch(const DevScene &sc, const SolverCfg &cfg, int c, co
         if (learned) {
             auto trials = group == 8 ? ss_trials_kernel<true, 8, kVar>
                           : group == 16 ? ss_trials_kernel<true, 16, kVar> : ss_trials_kernel<true, 32, kVar>;
-            trials<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr,
-                                                 pr);
+            trials<<<num_sms * bps, 128, tsmem, s>>>(st, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr,
+                                                     pr);
         }
     }
     if (!learned) {
         auto trials = group == 8 ? ss_trials_kernel<false, 8, kVar>
                       : group == 16 ? ss_trials_kernel<false, 16, kVar> : ss_trials_kernel<false, 32, kVar>;
-        trials<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr, pr);
+        trials<<<num_sms * bps, 128, tsmem, s>>>(st, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr,
+                                                 pr);
     }
     phase_end(tm, s);
     return cudaGetLastError();

@@ -3,7 +3,8 @@ benchmark's own sizes, through the C ABI.
 
 A walk is well conditioned when the oracle gives the same outcome (converged
 flag and solution) in FP32, FP32 with FMA contraction, FP64, and FP32 with its
-inputs moved by one ulp either way (tests/basin.py); the rest is the
+seed sample or its light point moved by one ulp either way (tests/basin.py);
+the rest is the
 basin-crossing fraction, which is printed.  On well-conditioned walks the GPU
 must agree with the oracle on all but WELL_CONDITIONED_MISMATCH = 0.1 % of the
 walks -- or, on a chaotic scene, on all but the fraction that one more
@@ -32,13 +33,15 @@ WELL_CONDITIONED_MISMATCH = 0.001
 
 def _walk_ensemble(oracle, desc, fn, args, walk_in_index, nudge_rows):
     """Oracle outputs of the same walks in three builds and with the walk
-    inputs (argument walk_in_index) moved by one ulp up and down."""
+    inputs (argument walk_in_index) moved by one ulp up and down: the seed
+    sample (nudge_rows) and the light point (rows 0-2)."""
     ens = B.oracle_walks(oracle, desc, fn, *args)
     base = oracle.OracleScene(desc)
-    for up in (True, False):
-        a = list(args)
-        a[walk_in_index] = B.nudge(args[walk_in_index], nudge_rows, up)
-        ens["nudge_up" if up else "nudge_down"] = getattr(base, fn)(*a)
+    for name, rows in (("seed", nudge_rows), ("light", slice(0, 3))):
+        for up in (True, False):
+            a = list(args)
+            a[walk_in_index] = B.nudge(args[walk_in_index], rows, up)
+            ens[f"{name}_{'up' if up else 'down'}"] = getattr(base, fn)(*a)
     return ens
 
 

@@ -280,10 +280,11 @@ def connect_timed(torch, sms, ctx, kind, q_dev, n, seed, stream_offset=0):
     return val, t.ms
 
 
-def secondary_configs(torch, sms, W, dev):
+def secondary_configs(torch, sms, W, dev, only=None, calls=5):
     """Throughput of the other solver configurations (one GPU): sphere
     (biased, 16 walks), two-bounce slab (biased, 32 walks, 512k queries) and
-    glints (8192^2 FP16 slope map, 1024^2 pixels, 64 seeds, vectorized)."""
+    glints (8192^2 FP16 slope map, 1024^2 pixels, 64 seeds, vectorized).
+    only: run just that configuration (for profiling one kernel)."""
     out = {}
     cases = [
         ("sphere_biased_m16", "ss", W.sphere_scene, W.sphere_config, lambda: W.sphere_queries(64), 16),
@@ -291,18 +292,20 @@ def secondary_configs(torch, sms, W, dev):
         ("glints_8192_vectorized_m64", "glints", W.glint_scene, W.glint_config, lambda: W.glint_queries(1024), 64),
     ]
     for name, kind, scene, config, queries, walks in cases:
+        if only and name != only:
+            continue
         ctx = sms.Context(sms.Scene(scene()), config(), device=dev)
         q = torch.from_numpy(np.ascontiguousarray(queries(), np.float32)).to(f"cuda:{dev}")
         n = q.shape[1]
         for i in range(3):
             connect_timed(torch, sms, ctx, kind, q, n, seed=50 + i)
         ctx.reset_stats()
-        ms = [connect_timed(torch, sms, ctx, kind, q, n, seed=60 + i)[1] for i in range(5)]
+        ms = [connect_timed(torch, sms, ctx, kind, q, n, seed=60 + i)[1] for i in range(calls)]
         st = ctx.stats()
         t = float(np.mean(ms))
-        its_per_s = st["newton_iterations"] / (5 * t / 1e3)
+        its_per_s = st["newton_iterations"] / (calls * t / 1e3)
         out[name] = {"queries": n, "ms_per_call": t, "connections_per_s": n / (t / 1e3),
-                     "walks_per_s": st["walks"] / (5 * t / 1e3), "walks_per_connection": walks,
+                     "walks_per_s": st["walks"] / (calls * t / 1e3), "walks_per_connection": walks,
                      "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),
                      "newton_iterations_per_s": its_per_s}
         units = flops_per_unit().get(name)
@@ -311,7 +314,7 @@ def secondary_configs(torch, sms, W, dev):
                 flops = st["newton_iterations"] * units["flops_per_newton_iteration"]
             else:
                 flops = fp32_work(units, st["rays"], 2 * st["bvh_nodes"], st["tri_tests"])
-            tf = flops / (5 * t / 1e3) / 1e12
+            tf = flops / (calls * t / 1e3) / 1e12
             out[name]["fp32"] = {"achieved_tflops": tf, "peak_tflops": fp32_peak_tflops(),
                                  "frac": tf / fp32_peak_tflops(), "peak_kind": "nominal",
                                  "flops_per_newton_iteration": units["flops_per_newton_iteration"]}
@@ -323,7 +326,7 @@ def secondary_configs(torch, sms, W, dev):
             out[name]["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                                      "frac": gbs / peak, "bytes_per_iteration": 16}
         else:
-            out[name]["rays_per_s"] = st["rays"] / (5 * t / 1e3)
+            out[name]["rays_per_s"] = st["rays"] / (calls * t / 1e3)
         ctx.close()
     return out
 
@@ -777,6 +780,9 @@ def main():
     ap.add_argument("--no-render", action="store_true", help="skip the path-tracer images")
     ap.add_argument("--render-only", action="store_true",
                     help="only the path-tracer images (one JSON object; for profiling the renderer)")
+    ap.add_argument("--secondary-only", default=None,
+                    help="only this secondary configuration, 3 warm-up and `--steps` timed calls (one JSON "
+                         "object; for profiling its kernel)")
     ap.add_argument("--render-size", type=int, default=512)
     ap.add_argument("--render-spp", type=int, default=16)
     args = ap.parse_args()
@@ -786,6 +792,13 @@ def main():
         from sms_gb300 import workloads as W
         print(json.dumps({"render": render_study(torch, sms, W, 0, args.render_size, args.render_size,
                                                  args.render_spp)}), flush=True)
+        return
+    if args.secondary_only:
+        import torch
+        sms = load_package()
+        from sms_gb300 import workloads as W
+        print(json.dumps({"configs": secondary_configs(torch, sms, W, 0, only=args.secondary_only,
+                                                       calls=args.steps)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

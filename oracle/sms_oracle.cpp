@@ -1521,7 +1521,8 @@ static Float invert_tridiagonal_geo(std::vector<MSBlock> &b) {
 static void d_sph_pair(V3 w, V3 du, V3 dv, Float &a, Float &b, Float &c, Float &d) { d_sphcoords(w, du, dv, a, b, c, d); }
 
 /* manifold_ms.cpp:631-857 (n_offset = (0,0,1), positional light) */
-static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::vector<MSBlock> &b) {
+static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::vector<MSBlock> &b,
+                              const std::vector<V3> *offs = nullptr) {
     size_t k = v.size();
     b.assign(k, MSBlock());
     bool success = true;
@@ -1541,6 +1542,13 @@ static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::
         V3 dwi_dv = (v[i].dp_dv - wi * dot(wi, v[i].dp_dv)) * -ili;
         const MVertex &vi = v[i];
         V3 n = vi.n, dndu = vi.dn_du, dndv = vi.dn_dv;
+        if (offs) {
+            /* offset normal of vertex i (:707-717); no-ops for (0, 0, 1) */
+            const V3 o = (*offs)[i];
+            n = vi.s * o.x + vi.t * o.y + vi.n * o.z;
+            dndu = vi.ds_du * o.x + vi.dt_du * o.y + vi.dn_du * o.z;
+            dndv = vi.ds_dv * o.x + vi.dt_dv * o.y + vi.dn_dv * o.z;
+        }
         auto transform = [&](V3 w, V3 &out) { return vi.eta == 1.f ? reflect(w, n, out) : refract(w, n, vi.eta, out); };
         auto d_transform = [&](V3 w, V3 du, V3 dv, V3 nd_u, V3 nd_v, V3 &ou, V3 &ov) {
             if (vi.eta == 1.f) d_reflect(w, du, dv, n, nd_u, nd_v, ou, ov);
@@ -1611,7 +1619,8 @@ static bool ms_step_anglediff(V3 x0, V3 lp, const std::vector<MVertex> &v, std::
 }
 
 /* manifold_ms.cpp:500-629 */
-static bool ms_step_halfvector(V3 x0, V3 lp, const std::vector<MVertex> &v, std::vector<MSBlock> &b) {
+static bool ms_step_halfvector(V3 x0, V3 lp, const std::vector<MVertex> &v, std::vector<MSBlock> &b,
+                               const std::vector<V3> *offs = nullptr) {
     size_t k = v.size();
     b.assign(k, MSBlock());
     for (size_t i = 0; i < k; ++i) {
@@ -1659,6 +1668,10 @@ static bool ms_step_halfvector(V3 x0, V3 lp, const std::vector<MVertex> &v, std:
         }
         b[i].C.x = dot(v[i].s, h);
         b[i].C.y = dot(v[i].t, h);
+        if (offs) {   /* C = H - N (:618-621) */
+            b[i].C.x = b[i].C.x - (*offs)[i].x;
+            b[i].C.y = b[i].C.y - (*offs)[i].y;
+        }
     }
     return invert_tridiagonal_step(b);
 }
@@ -1677,9 +1690,21 @@ static Ray spawn_ray(V3 p, V3 d) {
 /* Trace the specular chain from x0 toward x1 (sample_seed_path :280-408 with
  * first_path/template shapes, reproject :859-918).  template_shapes empty ->
  * any caster_multi/bouncer shape is allowed (first path). */
+/* Offset normals of a rough chain (manifold_ms.cpp:356-375): draw (non-null)
+ * holds the walk's 2 numbers per vertex; a rough vertex of a first path draws
+ * a Beckmann offset from them (its density multiplies *pdf), a smooth one keeps
+ * (0, 0, 1).  Otherwise offs holds the template's offsets (null: all smooth). */
+struct ChainOffsets {
+    std::vector<V3> *offs = nullptr;
+    const V2 *draw = nullptr;
+    Float *pdf = nullptr;
+};
+
 static bool ms_trace_chain(const Scene &sc, int bounces, V3 x0, V3 x1, const std::vector<int> &tmpl,
-                           bool require_chain_flags, std::vector<MVertex> &path, bool straight = false) {
+                           bool require_chain_flags, std::vector<MVertex> &path, bool straight = false,
+                           ChainOffsets co = ChainOffsets()) {
     path.clear();
+    if (co.draw) { co.offs->clear(); *co.pdf = 1.f; }
     V3 wo = normalize(x1 - x0);
     Ray ray; ray.o = x0; ray.d = wo;
     while ((int)path.size() < bounces) {
@@ -1691,11 +1716,26 @@ static bool ms_trace_chain(const Scene &sc, int bounces, V3 x0, V3 x1, const std
         MVertex v;
         vertex_from_si(sc, si, v);
         path.push_back(v);
+        V3 m = v.n;
+        if (co.draw) {
+            V3 o(0.f, 0.f, 1.f);
+            const sms_bsdf &bs = sc.shapes[si.shape].bsdf;
+            if (is_rough(bs)) {
+                Float p_o;
+                o = beckmann_sample(bs.alpha, co.draw[bounce].x, co.draw[bounce].y, p_o);
+                *co.pdf *= p_o;
+            }
+            co.offs->push_back(o);
+        }
+        if (co.offs && (int)co.offs->size() > bounce) {
+            const V3 o = (*co.offs)[bounce];
+            m = v.s * o.x + v.t * o.y + v.n * o.z;   /* :380-382, :894-897 */
+        }
         V3 wi = -wo;
         bool ok = true;
         if (straight) { /* MNEE seed path: no scattering (manifold_ms.cpp:377-397) */ }
-        else if (v.eta == 1.f) ok = reflect(wi, v.n, wo);
-        else ok = refract(wi, v.n, v.eta, wo);
+        else if (v.eta == 1.f) ok = reflect(wi, m, wo);
+        else ok = refract(wi, m, v.eta, wo);
         if (!ok) return false;
         ray = spawn_ray(si.p, wo);
     }
@@ -1704,7 +1744,7 @@ static bool ms_trace_chain(const Scene &sc, int bounces, V3 x0, V3 x1, const std
 
 /* manifold_ms.cpp:410-498 */
 static bool ms_newton(const Scene &sc, const sms_config &cfg, V3 x0, V3 lp, const std::vector<int> &tmpl,
-                      std::vector<MVertex> &path, int &iters) {
+                      std::vector<MVertex> &path, int &iters, std::vector<V3> *offs = nullptr) {
     bool success = false;
     int it = 0;
     Float beta = 1.f;
@@ -1713,7 +1753,8 @@ static bool ms_newton(const Scene &sc, const sms_config &cfg, V3 x0, V3 lp, cons
     while (it < cfg.max_iterations) {
         bool ok = true;
         if (needs_update)
-            ok = cfg.halfvector_constraints ? ms_step_halfvector(x0, lp, path, b) : ms_step_anglediff(x0, lp, path, b);
+            ok = cfg.halfvector_constraints ? ms_step_halfvector(x0, lp, path, b, offs)
+                                            : ms_step_anglediff(x0, lp, path, b, offs);
         if (!ok) break;
         bool conv = true;
         for (const MSBlock &bl : b)
@@ -1723,7 +1764,10 @@ static bool ms_newton(const Scene &sc, const sms_config &cfg, V3 x0, V3 lp, cons
         const MVertex &v0 = path[0];
         V3 p0 = v0.p - (v0.dp_du * b[0].dx.x + v0.dp_dv * b[0].dx.y) * (cfg.step_scale * beta);
         std::vector<MVertex> prop;
-        bool proj = ms_trace_chain(sc, (int)path.size(), x0, p0, tmpl, false, prop) && prop.size() == tmpl.size();
+        ChainOffsets co;
+        co.offs = offs;
+        bool proj = ms_trace_chain(sc, (int)path.size(), x0, p0, tmpl, false, prop, false, co) &&
+                    prop.size() == tmpl.size();
         if (!proj) { beta = 0.5f * beta; needs_update = false; }
         else { beta = omin(1.f, 2.f * beta); path = prop; needs_update = true; }
         it++;
@@ -1743,26 +1787,44 @@ static bool ms_newton(const Scene &sc, const sms_config &cfg, V3 x0, V3 lp, cons
 
 /* sample_path (:203-227): seed path + Newton.  seed_shapes: in = template
  * (empty for a first path), out = this walk's seed shapes. */
+/* The offsets of an estimate's template (rough chains). */
+struct MsOffsets {
+    std::vector<V3> offs;   /* one per chain vertex */
+    Float pdf = 1.f;
+};
+
 static bool ms_sample_path(const Scene &sc, const sms_config &cfg, int caster, const Query &q, V3 lp, V2 sample,
                            V3 p_start, std::vector<int> &tmpl, bool first_path, std::vector<MVertex> &path,
-                           int &iters, bool &seed_ok) {
+                           int &iters, bool &seed_ok, MsOffsets *mo = nullptr, const V2 *draw = nullptr) {
     iters = 0;
     seed_ok = false;
     V3 x1 = sample_position(sc.shapes[caster], sample);
     if (p_start.x != 0.f || p_start.y != 0.f || p_start.z != 0.f) x1 = p_start;
     static const std::vector<int> none;
     if (cfg.mnee_init) x1 = mnee_target(sc.shapes[caster], lp);
-    if (!ms_trace_chain(sc, cfg.bounces, q.p, x1, first_path ? none : tmpl, true, path, cfg.mnee_init != 0))
+    /* a first path draws its own offsets; later walks follow the template's */
+    std::vector<V3> own;
+    Float own_pdf = 1.f;
+    ChainOffsets co;
+    if (mo) {
+        if (first_path) { co.offs = &own; co.draw = draw; co.pdf = &own_pdf; }
+        else co.offs = &mo->offs;
+    }
+    if (!ms_trace_chain(sc, cfg.bounces, q.p, x1, first_path ? none : tmpl, true, path, cfg.mnee_init != 0, co))
         return false;
     seed_ok = true;
     if (first_path) {
         tmpl.clear();
         for (const MVertex &v : path) tmpl.push_back(v.shape);
+        if (mo) { mo->offs = own; mo->pdf = own_pdf; }
     }
-    return ms_newton(sc, cfg, q.p, lp, tmpl, path, iters);
+    return ms_newton(sc, cfg, q.p, lp, tmpl, path, iters, mo ? &mo->offs : nullptr);
 }
 
-/* manifold_ms.cpp:920-1023 (smooth BSDFs) */
+/* manifold_ms.cpp:920-1023.  At a rough vertex the reference computes the
+ * glossy BSDF value in the half-vector domain (:963-985) but multiplies only
+ * the delta branch's factor into the throughput (:1007), so a rough vertex
+ * contributes 1; restated as is. */
 static Float ms_specular_reflectance(const Scene &sc, V3 x0, V3 lp, const std::vector<MVertex> &path) {
     if (path.empty()) return 0.f;
     Ray ray; ray.o = x0; ray.d = normalize(path[0].p - x0);
@@ -1772,7 +1834,7 @@ static Float ms_specular_reflectance(const Scene &sc, V3 x0, V3 lp, const std::v
         si = ray_intersect(sc, ray);
         if (!si.valid()) return 0.f;
         V3 wo = k + 1 < path.size() ? normalize(path[k + 1].p - si.p) : normalize(lp - si.p);
-        val *= specular_reflectance(sc, si, wo);
+        if (!is_rough(sc.shapes[si.shape].bsdf)) val *= specular_reflectance(sc, si, wo);
         ray = Ray(); ray.o = si.p; ray.d = wo;
     }
     Ray vis; vis.o = si.p; vis.d = normalize(lp - si.p);
@@ -1871,6 +1933,34 @@ static V3 ms_contribution(const Scene &sc, const Query &q, const EI &ei_in, cons
     return V3(f * ei.weight.x, f * ei.weight.y, f * ei.weight.z);
 }
 
+/* A chain shape (caster_multi or bouncer) with a rough BSDF: the estimate
+ * samples offset normals (manifold_ms.cpp:356-375). */
+static bool ms_rough_chain(const Scene &sc) {
+    for (size_t s = 0; s < sc.shapes.size(); ++s)
+        if (is_chain_shape(sc, (int)s) && is_rough(sc.shapes[s].bsdf)) return true;
+    return false;
+}
+
+/* The random numbers of one walk.  Smooth chains: the seed position's 2 (the
+ * reference's draw order).  Rough chains: every walk owns a fixed run of
+ * 2 + 2 bounces numbers -- the seed position, then 2 per chain vertex for an
+ * offset normal, used only by a first path at a rough vertex.  (The reference
+ * draws those only when they are used, so later walks' positions in its
+ * sampler depend on earlier walks' outcomes; the fixed run keeps walks
+ * independent, as the batched device estimators need, with the same
+ * expectation.) */
+struct MsWalkDraws {
+    V2 seed;
+    V2 offs[8];
+};
+static MsWalkDraws ms_walk_draws(PCG32 &rng, bool rough, int bounces) {
+    MsWalkDraws d;
+    d.seed = rng.next_2d();
+    if (rough)
+        for (int b = 0; b < bounces; ++b) d.offs[b] = rng.next_2d();
+    return d;
+}
+
 /* manifold_ms.cpp:27-201 */
 static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG32 &rng, int &count_out,
                      int &walks_out, Stats &st) {
@@ -1879,15 +1969,20 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
     V3 result(0.f);
     if (sc.casters_ms.empty() || ei.emitter < 0) return result;
     st.connections++;
+    const bool rough = ms_rough_chain(sc);
     for (int caster : sc.casters_ms) {
         V3 value(0.f);
         std::vector<int> tmpl;
         std::vector<MVertex> path;
         int it = 0;
         bool seed_ok;
+        MsOffsets mo;
+        MsOffsets *mop = rough ? &mo : nullptr;
         if (!cfg.biased) {
             count_out = 0;
-            bool ok = ms_sample_path(sc, cfg, caster, q, ei.p, rng.next_2d(), V3(0.f), tmpl, true, path, it, seed_ok);
+            MsWalkDraws wd = ms_walk_draws(rng, rough, cfg.bounces);
+            bool ok = ms_sample_path(sc, cfg, caster, q, ei.p, wd.seed, V3(0.f), tmpl, true, path, it, seed_ok, mop,
+                                     wd.offs);
             walks_out++; st.walks++; st.newton += it;
             if (!ok) { st.failed++; continue; }
             st.succeeded++;
@@ -1900,7 +1995,9 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             while (true) {
                 std::vector<MVertex> tp;
                 int it2 = 0;
-                bool ok2 = ms_sample_path(sc, cfg, caster, q, ei.p, rng.next_2d(), V3(0.f), tmpl, false, tp, it2, seed_ok);
+                MsWalkDraws td = ms_walk_draws(rng, rough, cfg.bounces);
+                bool ok2 = ms_sample_path(sc, cfg, caster, q, ei.p, td.seed, V3(0.f), tmpl, false, tp, it2, seed_ok,
+                                          mop, td.offs);
                 walks_out++; st.walks++; st.newton += it2;
                 if (ok2 && std::fabs(dot(direction, normalize(tp[0].p - q.p)) - 1.f) < cfg.uniqueness_threshold) break;
                 inv_prob += 1.f;
@@ -1915,7 +2012,9 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             std::vector<V3> solutions;
             for (int m = 0; m < cfg.max_trials; ++m) {
                 bool first = tmpl.empty();
-                bool ok = ms_sample_path(sc, cfg, caster, q, ei.p, rng.next_2d(), V3(0.f), tmpl, first, path, it, seed_ok);
+                MsWalkDraws wd = ms_walk_draws(rng, rough, cfg.bounces);
+                bool ok = ms_sample_path(sc, cfg, caster, q, ei.p, wd.seed, V3(0.f), tmpl, first, path, it, seed_ok,
+                                         mop, wd.offs);
                 if (!seed_ok && first) tmpl.clear();
                 walks_out++; st.walks++; st.newton += it;
                 if (!ok) { st.failed++; continue; }
@@ -1932,7 +2031,8 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             }
             count_out += (int)solutions.size();
         }
-        result += value;
+        /* result += value / m_offset_normals_pdf (:198) */
+        result += rough ? V3(value.x / mo.pdf, value.y / mo.pdf, value.z / mo.pdf) : value;
     }
     return result;
 }
@@ -2069,9 +2169,74 @@ static void base_frame(const GQuery &q, V3 &s, V3 &t) {
     t = cross(q.n, s);
 }
 
-/* manifold_glints.cpp:225-265 */
+/* Inverse error function.  enoki's erfinv (the reference's) is not in the
+ * checkout; this one starts from Winitzki's closed-form approximation (S.
+ * Winitzki, "A handy approximation for the error function and its inverse",
+ * 2008) and refines it with Newton steps on std::erf in double, so it is
+ * accurate to double rounding before the final conversion. */
+static double erfinv_double(double y) {
+    if (!(y > -1.0)) return -std::numeric_limits<double>::infinity();
+    if (!(y < 1.0)) return std::numeric_limits<double>::infinity();
+    const double a = 0.147, pi = 3.14159265358979323846;
+    const double l = std::log((1.0 - y) * (1.0 + y));
+    const double b = 2.0 / (pi * a) + 0.5 * l;
+    double x = std::copysign(std::sqrt(std::sqrt(b * b - l / a) - b), y);
+    for (int i = 0; i < 4; ++i) {
+        const double e = std::erf(x) - y;
+        x -= e / (2.0 / std::sqrt(pi) * std::exp(-x * x));
+    }
+    return x;
+}
+static Float erfinv_f(Float y) {
+    ORC_COUNT_FP64_OPS(1);
+    return Float((float)erfinv_double((double)y));
+}
+
+/* Visible-normal sampling of an isotropic Beckmann distribution
+ * (include/mitsuba/render/microfacet.h:287-314 with sample_visible_11,
+ * :357-394, smith_g1 :331-355, Frame3f::sincos_phi frame.h:107-118): the
+ * offset normal of a rough glinty surface (manifold_glints.cpp:56-64). */
+static V3 beckmann_sample_visible(Float alpha, V3 wi, V2 u, Float &pdf) {
+    V3 wp = normalize(V3(alpha * wi.x, alpha * wi.y, wi.z));
+    Float st2 = wp.x * wp.x + wp.y * wp.y;
+    Float sin_phi = 0.f, cos_phi = 1.f;
+    if (!(std::fabs(st2) <= 4.f * std::numeric_limits<float>::epsilon())) {
+        Float inv = 1.f / std::sqrt(st2);
+        cos_phi = omin(1.f, omax(-1.f, wp.x * inv));
+        sin_phi = omin(1.f, omax(-1.f, wp.y * inv));
+    }
+    const Float cos_i = wp.z;
+    /* sample_visible_11, Beckmann */
+    const Float tan_i = safe_sqrt(1.f - cos_i * cos_i) / cos_i;
+    const Float cot_i = 1.f / tan_i;
+    const Float maxval = std::erf(cot_i);
+    V2 sm;
+    sm.x = omax(omin(u.x, 1.f - 1e-6f), 1e-6f);
+    sm.y = omax(omin(u.y, 1.f - 1e-6f), 1e-6f);
+    const Float kInvSqrtPi = 0.56418958354775628695f;
+    Float x = maxval - (maxval + 1.f) * std::erf(std::sqrt(-std::log(sm.x)));
+    sm.x = sm.x * (1.f + maxval + kInvSqrtPi * tan_i * std::exp(-(cot_i * cot_i)));
+    for (int i = 0; i < 3; ++i) {
+        Float slope = erfinv_f(x);
+        Float value = 1.f + x + kInvSqrtPi * tan_i * std::exp(-(slope * slope)) - sm.x;
+        Float deriv = 1.f - slope * tan_i;
+        x = x - value / deriv;
+    }
+    V2 sl;
+    sl.x = erfinv_f(x);
+    sl.y = erfinv_f(2.f * sm.y - 1.f);
+    /* rotate and unstretch */
+    V2 r;
+    r.x = (cos_phi * sl.x - sin_phi * sl.y) * alpha;
+    r.y = (sin_phi * sl.x + cos_phi * sl.y) * alpha;
+    V3 m = normalize(V3(-r.x, -r.y, 1.f));
+    pdf = beckmann_D(m, alpha) * beckmann_G1(wi, m, alpha) * std::fabs(dot(wi, m)) / wi.z;
+    return m;
+}
+
+/* manifold_glints.cpp:225-265; no = the offset normal (local frame) */
 static bool sample_glint(const sms_config &cfg, const NormalMap &m, const GQuery &q, V3 lp, V2 fp, V2 &uv_final,
-                         V2 &uv_init, int &iters) {
+                         V2 &uv_init, int &iters, V3 no = V3(0.f, 0.f, 1.f)) {
     iters = 0;
     V3 s, t;
     base_frame(q, s, t);
@@ -2080,8 +2245,8 @@ static bool sample_glint(const sms_config &cfg, const NormalMap &m, const GQuery
     if (wi.z <= 0.f || wo.z <= 0.f) return false;
     V3 h = normalize(wi + wo);
     V2 target;
-    target.x = -h.x / h.z + (-0.f / 1.f);
-    target.y = -h.y / h.z + (-0.f / 1.f);
+    target.x = -h.x / h.z + (-no.x / no.z);
+    target.y = -h.y / h.z + (-no.y / no.z);
     V2 duv;
     duv.x = (fp.x - 0.5f) * q.duv_dx.x + (fp.y - 0.5f) * q.duv_dy.x;
     duv.y = (fp.x - 0.5f) * q.duv_dx.y + (fp.y - 0.5f) * q.duv_dy.y;
@@ -2164,6 +2329,29 @@ static Float glint_reflectance(const sms_bsdf &b, V3 n, V3 wo) {
     return fresnel_conductor(std::fabs(cos_theta), 0.f, 1.f);
 }
 
+/* specular_reflectance (manifold_glints.cpp:375-409) of a rough glinty
+ * surface: the BSDF value (NormalmapBSDF::eval, normalmap.cpp:172-181: the
+ * nested rough BSDF in the normal-mapped frame at uv, wo kept only on the same
+ * side of both frames) moved to the half-vector domain, x 4 |wo . h| in the
+ * base frame. */
+static Float glint_rough_reflectance(const Scene &sc, const GQuery &q, V2 uv, V3 wi_w, V3 wo_w) {
+    const sms_bsdf &b = sc.shapes[sc.glinty_shape].bsdf;
+    MVertex vt;
+    glint_vertex(sc.nmap, q, uv, vt);
+    V3 n = vt.n;
+    V3 fs = normalize(q.dp_du - n * dot(n, q.dp_du));
+    V3 ft = cross(n, fs);
+    V3 wi(dot(wi_w, fs), dot(wi_w, ft), dot(wi_w, n)), wo(dot(wo_w, fs), dot(wo_w, ft), dot(wo_w, n));
+    if (!(dot(wo_w, q.n) * wo.z > 0.f)) return 0.f;
+    Float f = b.type == SMS_BSDF_CONDUCTOR ? roughconductor_eval(b.alpha, b.eta, b.k, wi, wo)
+                                           : roughdielectric_eval(b.alpha, b.eta, wi, wo);
+    V3 bs, bt;
+    base_frame(q, bs, bt);
+    V3 wil(dot(wi_w, bs), dot(wi_w, bt), dot(wi_w, q.n)), wol(dot(wo_w, bs), dot(wo_w, bt), dot(wo_w, q.n));
+    V3 h = normalize(wil + wol);
+    return f * 4.f * std::fabs(dot(wol, h));
+}
+
 /* manifold_glints.cpp:267-294 */
 static Float glint_contribution(const Scene &sc, const GQuery &q, const EI &ei, V2 uv) {
     MVertex vy;
@@ -2177,7 +2365,9 @@ static Float glint_contribution(const Scene &sc, const GQuery &q, const EI &ei, 
     glint_vertex(sc.nmap, q, uv, vt);
     MVertex vt_o = vt;
     make_orthonormal(vt_o);
-    Float f = glint_reflectance(sc.shapes[sc.glinty_shape].bsdf, vt.n, normalize(ei.p - q.p));
+    const sms_bsdf &gb = sc.shapes[sc.glinty_shape].bsdf;
+    Float f = is_rough(gb) ? glint_rough_reflectance(sc, q, uv, normalize(q.sensor - q.p), normalize(ei.p - q.p))
+                           : glint_reflectance(gb, vt.n, normalize(ei.p - q.p));
     f *= glint_geometric_term(vx, vt_o, vy);
     return f;
 }
@@ -2198,11 +2388,22 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
     r.mint = kRayEps * (1.f + hmax_abs(q.p));
     r.maxt = dist * (1.f - kRayEps);
     if (ray_test(sc, r)) return V3(0.f);
+    /* offset normal of a rough glinty surface (:56-64): visible normals of the
+       Beckmann distribution seen from the sensor direction */
+    V3 no(0.f, 0.f, 1.f);
+    Float p_off = 1.f;
+    const sms_bsdf &gb = sc.shapes[sc.glinty_shape].bsdf;
+    if (is_rough(gb)) {
+        V3 bs, bt;
+        base_frame(q, bs, bt);
+        V3 wiw = normalize(q.sensor - q.p);
+        no = beckmann_sample_visible(gb.alpha, V3(dot(wiw, bs), dot(wiw, bt), dot(wiw, q.n)), rng.next_2d(), p_off);
+    }
     Float w = 0.f;
     V2 uvf, uvi;
     int it;
     if (!cfg.biased) {
-        bool ok = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvf, uvi, it);
+        bool ok = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvf, uvi, it, no);
         walks_out++; st.walks++; st.newton += it;
         if (!ok) { st.failed++; return V3(0.f); }
         st.succeeded++;
@@ -2213,7 +2414,7 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
         while (true) {
             V2 uvt, uvi2;
             int it2;
-            bool ok2 = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvt, uvi2, it2);
+            bool ok2 = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvt, uvi2, it2, no);
             walks_out++; st.walks++; st.newton += it2;
             Float dx = uvt.x - uvf.x, dy = uvt.y - uvf.y;
             if (ok2 && std::sqrt(dx * dx + dy * dy) < cfg.uniqueness_threshold) break;
@@ -2228,7 +2429,7 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
     } else {
         std::vector<V2> sols;
         for (int m = 0; m < cfg.max_trials; ++m) {
-            bool ok = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvf, uvi, it);
+            bool ok = sample_glint(cfg, sc.nmap, q, ei.p, rng.next_2d(), uvf, uvi, it, no);
             walks_out++; st.walks++; st.newton += it;
             if (!ok) { st.failed++; continue; }
             st.succeeded++;
@@ -2243,6 +2444,7 @@ static V3 glint_connect(const Scene &sc, const sms_config &cfg, const GQuery &q,
         }
         count_out = (int)sols.size();
     }
+    w = w / p_off;   /* sms_weight /= p_offset (:141) */
     return V3(w * ei.weight.x, w * ei.weight.y, w * ei.weight.z);
 }
 

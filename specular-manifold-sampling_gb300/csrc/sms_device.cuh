@@ -224,6 +224,7 @@ struct DevScene {
     uint32_t casters_ss_rough;   // bit c: single-scatter caster c is rough (alpha > 0)
     uint32_t casters_ss_nm;      // bit c: single-scatter caster c carries the normal map
     int ms_nm;                   // a multi-scatter chain shape carries the normal map
+    int ms_rough;                // a multi-scatter chain shape is rough (alpha > 0)
     int n_emitters_ss, emitters_ss[kMaxEmitters];
     int n_casters_ms, casters_ms[kMaxCasters];
     int n_emitters_ms, emitters_ms[kMaxEmitters];

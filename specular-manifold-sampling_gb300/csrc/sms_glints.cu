@@ -100,10 +100,63 @@ SMS_D void base_frame(const GQuery &q, f3 &s, f3 &t) {
     t = cross(q.n, s);
 }
 
+// Visible-normal sampling of an isotropic Beckmann distribution seen from wi
+// (include/mitsuba/render/microfacet.h:287-314, sample_visible_11 :357-394,
+// smith_g1 :331-355, Frame3f::sincos_phi frame.h:107-118): the offset normal
+// of a rough glinty surface (manifold_glints.cpp:56-64); pdf = D G1 |wi.m| /
+// cos_theta(wi).
+SMS_D f3 beckmann_sample_visible(float alpha, f3 wi, float u0, float u1, float &pdf) {
+    const f3 wp = normalize(mk(alpha * wi.x, alpha * wi.y, wi.z));
+    const float st2 = wp.x * wp.x + wp.y * wp.y;
+    float sin_phi = 0.f, cos_phi = 1.f;
+    if (!(fabsf(st2) <= 4.f * 1.1920929e-7f)) {
+        const float inv = 1.f / sqrtf(st2);
+        cos_phi = fminf(1.f, fmaxf(-1.f, wp.x * inv));
+        sin_phi = fminf(1.f, fmaxf(-1.f, wp.y * inv));
+    }
+    const float cos_i = wp.z;
+    const float tan_i = sqrtf(fmaxf(1.f - cos_i * cos_i, 0.f)) / cos_i;
+    const float cot_i = 1.f / tan_i;
+    const float maxval = erff(cot_i);
+    const float sx = fmaxf(fminf(u0, 1.f - 1e-6f), 1e-6f), sy = fmaxf(fminf(u1, 1.f - 1e-6f), 1e-6f);
+    const float kInvSqrtPi = 0.56418958354775628695f;
+    float x = maxval - (maxval + 1.f) * erff(sqrtf(-logf(sx)));
+    const float target = sx * (1.f + maxval + kInvSqrtPi * tan_i * expf(-(cot_i * cot_i)));
+    #pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+        const float slope = erfinvf(x);
+        const float value = 1.f + x + kInvSqrtPi * tan_i * expf(-(slope * slope)) - target;
+        const float deriv = 1.f - slope * tan_i;
+        x = x - value / deriv;
+    }
+    const float slx = erfinvf(x), sly = erfinvf(2.f * sy - 1.f);
+    const float rx = (cos_phi * slx - sin_phi * sly) * alpha, ry = (sin_phi * slx + cos_phi * sly) * alpha;
+    const f3 m = normalize(mk(-rx, -ry, 1.f));
+    pdf = beckmann_D(m, alpha) * beckmann_G1(wi, m, alpha) * fabsf(dot(wi, m)) / wi.z;
+    return m;
+}
+
+// Offset normal of the query's glinty surface, from the 2 numbers after the
+// emitter sample: (0, 0, 1) and density 1 when the surface is smooth.
+SMS_D f3 glint_offset(const DevScene &sc, const GQuery &q, Pcg32 rng_at_3, float &p_off) {
+    p_off = 1.f;
+    const DevShape &gs = sc.shapes[sc.glinty_shape];
+    if (!(gs.alpha > 0.f)) return mk(0.f, 0.f, 1.f);
+    const float u0 = rng_at_3.next_f32(), u1 = rng_at_3.next_f32();
+    const f3 bs = normalize(q.dp_du - q.n * dot(q.n, q.dp_du)), bt = cross(q.n, bs);
+    const f3 wiw = normalize(q.sensor - q.p);
+    return beckmann_sample_visible(gs.alpha, mk(dot(wiw, bs), dot(wiw, bt), dot(wiw, q.n)), u0, u1, p_off);
+}
+
+// Random numbers the glint estimator takes after the emitter sample before its
+// walks: the offset normal's 2 on a rough glinty surface.
+SMS_D uint32_t glint_offset_numbers(const DevScene &sc) { return sc.shapes[sc.glinty_shape].alpha > 0.f ? 2u : 0u; }
+
 // sample_glint (:225-265) from an explicit footprint sample fp; Newton in uv
 // with footprint containment (:296-343).  Returns ok; uv = final position.
+// no: the offset normal (local frame), added to the target slope (:243-246).
 SMS_D bool glint_walk(const DevScene &sc, const SolverCfg &cfg, const GQuery &q, f3 lp, f2 fp, f2 &uv, f2 &uv_init,
-                      int &it) {
+                      int &it, f3 no = f3{0.f, 0.f, 1.f}) {
     it = 0;
     f3 s, t;
     base_frame(q, s, t);
@@ -113,7 +166,7 @@ SMS_D bool glint_walk(const DevScene &sc, const SolverCfg &cfg, const GQuery &q,
     uv_init = uv;
     if (wi.z <= 0.f || wo.z <= 0.f) return false;
     f3 h = normalize(wi + wo);
-    f2 target = {-h.x / h.z + (-0.f), -h.y / h.z + (-0.f)};
+    f2 target = {-h.x / h.z + (-no.x / no.z), -h.y / h.z + (-no.y / no.z)};
     f2 duv = {(fp.x - 0.5f) * q.duv_dx.x + (fp.y - 0.5f) * q.duv_dy.x,
               (fp.x - 0.5f) * q.duv_dx.y + (fp.y - 0.5f) * q.duv_dy.y};
     uv_init = {q.uv.x + duv.x, q.uv.y + duv.y};
@@ -177,7 +230,23 @@ SMS_D float glint_contribution(const DevScene &sc, const GQuery &q, const Light 
     float cos_theta = dot(wn, normalize(lp - q.p));
     const DevShape &shp = sc.shapes[sc.glinty_shape];
     float F;
-    if (shp.bsdf_type == kBsdfConductor && shp.k != 0.f) F = fresnel_conductor(fabsf(cos_theta), shp.eta, shp.k);
+    if (shp.alpha > 0.f) {
+        // glossy (:383-393): NormalmapBSDF::eval, the nested rough BSDF in the
+        // normal-mapped frame at uv (normalmap.cpp:172-181), x 4 |wo . h| in
+        // the base frame
+        const f3 wiw = normalize(q.sensor - q.p), wow = normalize(lp - q.p);
+        const f3 fs = normalize(q.dp_du - wn * dot(wn, q.dp_du)), ft = cross(wn, fs);
+        const f3 wip = mk(dot(wiw, fs), dot(wiw, ft), dot(wiw, wn)), wop = mk(dot(wow, fs), dot(wow, ft), dot(wow, wn));
+        if (!(dot(wow, q.n) * wop.z > 0.f)) {
+            F = 0.f;
+        } else {
+            const float f = shp.bsdf_type == kBsdfConductor ? roughconductor_eval(shp.alpha, shp.eta, shp.k, wip, wop)
+                                                            : roughdielectric_eval(shp.alpha, shp.eta, wip, wop);
+            const f3 wil = mk(dot(wiw, s), dot(wiw, t), dot(wiw, q.n)), wol = mk(dot(wow, s), dot(wow, t), dot(wow, q.n));
+            const f3 hl = normalize(wil + wol);
+            F = f * 4.f * fabsf(dot(wol, hl));
+        }
+    } else if (shp.bsdf_type == kBsdfConductor && shp.k != 0.f) F = fresnel_conductor(fabsf(cos_theta), shp.eta, shp.k);
     else if (shp.bsdf_type == kBsdfDielectric || shp.bsdf_type == kBsdfConductor)
         F = fresnel_dielectric(fabsf(cos_theta), shp.eta);
     else F = fresnel_conductor(fabsf(cos_theta), 0.f, 1.f);
@@ -307,16 +376,21 @@ __global__ void __launch_bounds__(128, 8) glint_biased_kernel(DevScene sc, Solve
         if (counted && gl == 0) st.conns++;
         int nrec = 0;
         float acc = 0.f;
+        // offset normal of a rough glinty surface (:56-64), the same on every lane
+        float p_off = 1.f;
+        f3 no = mk(0.f, 0.f, 1.f);
+        const uint32_t n_off = glint_offset_numbers(sc);
+        if (work && n_off) no = glint_offset(sc, Q, query_rng(seed, query_stream(cfg, stream_off, qi), 3u), p_off);
         for (int m0 = 0; m0 < M; m0 += G) {
             int m = m0 + gl;
             bool ok = false;
             f2 uv = {0.f, 0.f};
             if (work && m < M) {
-                Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + 2u * (uint64_t)m);
+                Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + n_off + 2u * (uint64_t)m);
                 float fx = rng.next_f32(), fy = rng.next_f32();
                 f2 uv0;
                 int it;
-                ok = glint_walk(sc, cfg, Q, L.p, f2{fx, fy}, uv, uv0, it);
+                ok = glint_walk(sc, cfg, Q, L.p, f2{fx, fy}, uv, uv0, it, no);
                 st.walks++;
                 st.newton += (unsigned)it;
                 if (ok) st.succ++; else st.fail++;
@@ -354,7 +428,7 @@ __global__ void __launch_bounds__(128, 8) glint_biased_kernel(DevScene sc, Solve
             }
         }
         if (live && gl == 0) {
-            f3 v = L.w * acc;
+            f3 v = L.w * (acc / p_off);   // sms_weight /= p_offset (:141)
             if (!work) v = splat(0.f);
             value[qi] = v.x;
             value[(size_t)n + qi] = v.y;
@@ -383,11 +457,15 @@ __global__ void __launch_bounds__(128) glint_first_kernel(DevScene sc, SolverCfg
         bool have = glint_light(sc, rng, Q, L, vis, err, st) && sc.glinty_shape >= 0 && sc.nmap_res > 0;
         int nw = 0;
         if (have) st.conns++;
+        const uint32_t n_off = have ? glint_offset_numbers(sc) : 0u;
         if (have && vis) {
+            float p_off;
+            const f3 no = glint_offset(sc, Q, rng, p_off);
+            rng.advance(n_off);
             float fx = rng.next_f32(), fy = rng.next_f32();
             f2 uv, uv0;
             int it;
-            bool ok = glint_walk(sc, cfg, Q, L.p, f2{fx, fy}, uv, uv0, it);
+            bool ok = glint_walk(sc, cfg, Q, L.p, f2{fx, fy}, uv, uv0, it, no);
             st.walks++;
             st.newton += (unsigned)it;
             nw = 1;
@@ -401,7 +479,7 @@ __global__ void __launch_bounds__(128) glint_first_kernel(DevScene sc, SolverCfg
                 st.fail++;
             }
         }
-        scr.pos[qi] = 5u;
+        scr.pos[qi] = 5u + n_off;
         value[qi] = 0.f;
         value[(size_t)n + qi] = 0.f;
         value[2 * (size_t)n + qi] = 0.f;
@@ -441,6 +519,9 @@ __global__ void __launch_bounds__(128) glint_trials_kernel(DevScene sc, SolverCf
         Light L;
         sample_emitter(sc, sc.emitters_all, sc.n_emitters_all, base, Q.p, L);   // at position 3
         f2 uv0 = {scr.dir0[qi], scr.dir0[(size_t)n + qi]};
+        float p_off;
+        const f3 no = glint_offset(sc, Q, base, p_off);
+        const uint32_t n_off = glint_offset_numbers(sc);
         int first = 0;
         for (int t0 = 1; t0 <= cap; t0 += 32) {
             int t = t0 + (int)lane;
@@ -448,10 +529,10 @@ __global__ void __launch_bounds__(128) glint_trials_kernel(DevScene sc, SolverCf
             int it = 0;
             if (t <= cap) {
                 Pcg32 rng = base;
-                rng.advance(2u + 2u * (uint64_t)(t - 1));
+                rng.advance(2u + n_off + 2u * (uint64_t)(t - 1));
                 float fx = rng.next_f32(), fy = rng.next_f32();
                 f2 uv, uvi;
-                bool ok = glint_walk(sc, cfg, Q, L.p, f2{fx, fy}, uv, uvi, it);
+                bool ok = glint_walk(sc, cfg, Q, L.p, f2{fx, fy}, uv, uvi, it, no);
                 float dx = uv.x - uv0.x, dy = uv.y - uv0.y;
                 succ = ok && sqrtf(dx * dx + dy * dy) < cfg.uniqueness_threshold;
             }
@@ -468,7 +549,7 @@ __global__ void __launch_bounds__(128) glint_trials_kernel(DevScene sc, SolverCf
             float inv_prob = first ? (float)first : 0.f;
             int trial_walks = first ? first : cap;
             if (!first && cfg.max_trials <= 0) err |= kErrTrialLimit;
-            f3 v = L.w * (scr.val[qi] * inv_prob);
+            f3 v = L.w * ((scr.val[qi] * inv_prob) / p_off);   // sms_weight /= p_offset (:141)
             value[qi] = v.x;
             value[(size_t)n + qi] = v.y;
             value[2 * (size_t)n + qi] = v.z;

@@ -357,7 +357,7 @@ struct sms_ctx {
     // per-query scratch of the unbiased estimators
     void *scratch = nullptr;
     uint32_t scratch_n = 0;
-    int *ms_tmpl = nullptr;       // multi-scatter template shapes, kMaxBounces x n
+    int *ms_tmpl = nullptr;       // multi-scatter templates, (4 kMaxBounces + 1) x n words
     uint32_t ms_tmpl_n = 0;
     PhaseTimer timer;
     std::vector<int> casters_ss;
@@ -564,6 +564,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
     d.glinty_shape = s->nmap_shape;
     d.nmap_shape = s->nmap_res > 0 ? s->nmap_shape : -1;
     d.ms_nm = c->ms_nm ? 1 : 0;
+    d.ms_rough = c->ms_rough ? 1 : 0;
     d.nmap_res = s->nmap_res;
     d.nmap_tiles = s->nmap_tiles;
     for (size_t i = 0; i < s->emitters.size(); ++i) {
@@ -1003,8 +1004,8 @@ int set_last_error_impl(int st, const char *msg) {
 static sms_status check_ms_cfg(sms_ctx *c) {
     if (c->cfg.bounces < 1 || c->cfg.bounces > kMaxBounces)
         return fail(SMS_ERR_UNSUPPORTED, "bounces must be between 1 and 4");
-    if (c->ms_rough)
-        return fail(SMS_ERR_UNSUPPORTED, "rough (alpha > 0) multi-scatter chain shapes are not supported");
+    if (c->ms_rough && c->ms_nm)
+        return fail(SMS_ERR_UNSUPPORTED, "rough (alpha > 0) normal-mapped multi-scatter chain shapes are not supported");
     return SMS_OK;
 }
 
@@ -1027,7 +1028,9 @@ sms_status ctx_ms_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
                 c->ms_tmpl = nullptr;
                 c->ms_tmpl_n = 0;
             }
-            CUDA_TRY(cudaMalloc(&c->ms_tmpl, (size_t)kMaxBounces * n * sizeof(int)));
+            // template shapes (kMaxBounces rows), then the template's offset
+            // normals (3 kMaxBounces rows) and their density (1 row)
+            CUDA_TRY(cudaMalloc(&c->ms_tmpl, (size_t)(4 * kMaxBounces + 1) * n * sizeof(int)));
             c->ms_tmpl_n = n;
         }
     }
@@ -1108,7 +1111,6 @@ extern "C" sms_status sms_ms_walk_batch(sms_ctx *c, int32_t caster, const float 
 static sms_status check_glint_scene(sms_ctx *c) {
     if (c->dsc.glinty_shape < 0 || c->dsc.nmap_res == 0)
         return fail(SMS_ERR_INVALID_ARG, "the scene has no normal map (sms_scene_set_normalmap)");
-    if (c->glint_rough) return fail(SMS_ERR_UNSUPPORTED, "rough (alpha > 0) glinty shapes are not supported");
     return SMS_OK;
 }
 

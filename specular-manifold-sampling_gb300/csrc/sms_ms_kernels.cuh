@@ -59,16 +59,32 @@ SMS_D bool chain_shape(const DevScene &sc, int s) {
     return (f & (kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
 }
 
+// Offset normals of a rough chain (sample_seed_path :356-375): the walk of a
+// first path draws them (draw: 2 numbers per vertex; a rough vertex samples a
+// Beckmann offset from its pair, a smooth one keeps (0, 0, 1); out: the
+// offsets and the product of their densities); later walks scatter about the
+// template's offsets (offs).
+template <int K>
+struct ChainOffsets {
+    const f3 *offs = nullptr;     // template offsets (K) or null
+    const float *draw = nullptr;  // first path: 2 K numbers
+    f3 *out = nullptr;            // first path: its offsets (K)
+    float *pdf = nullptr;         // first path: product of the offset densities
+};
+
 // Trace a specular chain from x0 toward x1, reflecting or refracting at each
 // hit (sample_seed_path :327-397, reproject :865-917).  tmpl (K shape ids) or
 // null; check_flags restricts hits to caster_multi / bouncer shapes; straight
-// keeps the direction at every hit (the MNEE seed path, :378-397).
-template <int K, bool kNM = false>
+// keeps the direction at every hit (the MNEE seed path, :378-397).  kRough:
+// scattering about the offset normals of co (:380-382, :894-897).
+template <int K, bool kNM = false, bool kRough = false>
 SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool check_flags, Chain<K> &c,
-                       int *shapes, uint32_t &err, LaneStats &st, bool straight = false) {
+                       int *shapes, uint32_t &err, LaneStats &st, bool straight = false,
+                       ChainOffsets<K> co = ChainOffsets<K>()) {
     f3 wo = normalize(x1 - x0);
     f3 o = x0;
     float mint = kRayEps;
+    if (kRough && co.draw) *co.pdf = 1.f;
     #pragma unroll
     for (int b = 0; b < K; ++b) {
         Hit h;
@@ -79,12 +95,32 @@ SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool c
         if (tmpl && h.shape != tmpl[b]) return false;
         vertex_from_hit<kNM>(sc, o, wo, h, c.v[b]);
         if (shapes) shapes[b] = h.shape;
+        f3 m = c.v[b].n;
+        if constexpr (kRough) {
+            if (co.draw || co.offs) {
+                f3 on = mk(0.f, 0.f, 1.f);
+                if (co.draw) {
+                    const DevShape &hs = sc.shapes[h.shape];
+                    if (hs.alpha > 0.f) {
+                        float p;
+                        on = beckmann_sample(hs.alpha, co.draw[2 * b], co.draw[2 * b + 1], p);
+                        *co.pdf *= p;
+                    }
+                    co.out[b] = on;
+                } else {
+                    on = co.offs[b];
+                }
+                f3 fs, ft, fsdu, fsdv, ftdu, ftdv;
+                frame_and_derivative(c.v[b], fs, ft, fsdu, fsdv, ftdu, ftdv);
+                m = fs * on.x + ft * on.y + c.v[b].n * on.z;
+            }
+        }
         f3 wi = -wo;
         if (straight) {
             // no scattering: the chain continues along the straight line
         } else if (c.v[b].eta == 1.f) {
-            wo = c.v[b].n * (2.f * dot(wi, c.v[b].n)) - wi;
-        } else if (!refract(wi, c.v[b].n, c.v[b].eta, wo)) {
+            wo = m * (2.f * dot(wi, m)) - wi;
+        } else if (!refract(wi, m, c.v[b].eta, wo)) {
             return false;
         }
         o = c.v[b].p;
@@ -96,18 +132,21 @@ SMS_D bool trace_chain(const DevScene &sc, f3 x0, f3 x1, const int *tmpl, bool c
 // The seed path of a walk (sample_seed_path :280-408): toward the sampled
 // point x1, or with cfg.mnee_init along the straight line toward the MNEE
 // target without scattering.
-template <int K, bool kNM = false>
+template <int K, bool kNM = false, bool kRough = false>
 SMS_D bool seed_chain(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x0, f3 x1, f3 lp, const int *tmpl,
-                      Chain<K> &c, int *shapes, uint32_t &err, LaneStats &st) {
+                      Chain<K> &c, int *shapes, uint32_t &err, LaneStats &st,
+                      ChainOffsets<K> co = ChainOffsets<K>()) {
     if (cfg.mnee_init)
-        return trace_chain<K, kNM>(sc, x0, mnee_target(sc.shapes[caster], lp), tmpl, true, c, shapes, err, st, true);
-    return trace_chain<K, kNM>(sc, x0, x1, tmpl, true, c, shapes, err, st);
+        return trace_chain<K, kNM, kRough>(sc, x0, mnee_target(sc.shapes[caster], lp), tmpl, true, c, shapes, err,
+                                           st, true, co);
+    return trace_chain<K, kNM, kRough>(sc, x0, x1, tmpl, true, c, shapes, err, st, false, co);
 }
 
 // Angle-difference constraint of vertex i and its blocks w.r.t. the previous,
-// current and next vertex (:631-857), n_offset = (0,0,1).
+// current and next vertex (:631-857); `no` is the vertex's offset normal in
+// its shading frame (:707-717; (0, 0, 1) keeps the vertex normal).
 SMS_D bool vertex_anglediff(f3 xp, const Vtx &vc, f3 xn, const Vtx *vp, const Vtx *vn, float &c0, float &c1,
-                            M2 &prev, M2 &cur, M2 &next) {
+                            M2 &prev, M2 &cur, M2 &next, f3 no = f3{0.f, 0.f, 1.f}) {
     prev = {0.f, 0.f, 0.f, 0.f};
     cur = prev;
     next = prev;
@@ -126,13 +165,21 @@ SMS_D bool vertex_anglediff(f3 xp, const Vtx &vc, f3 xn, const Vtx *vp, const Vt
     f3 dwi_dv = (vc.dp_dv - wi * dot(wi, vc.dp_dv)) * -ili;
     const bool refl = vc.eta == 1.f;
     const f3 z = splat(0.f);
+    f3 nn = vc.n, nn_du = vc.dn_du, nn_dv = vc.dn_dv;
+    if (no.x != 0.f || no.y != 0.f) {
+        f3 fs, ft, fsdu, fsdv, ftdu, ftdv;
+        frame_and_derivative(vc, fs, ft, fsdu, fsdv, ftdu, ftdv);
+        nn = fs * no.x + ft * no.y + vc.n * no.z;
+        nn_du = fsdu * no.x + ftdu * no.y + vc.dn_du * no.z;
+        nn_dv = fsdv * no.x + ftdv * no.y + vc.dn_dv * no.z;
+    }
     auto xform = [&](f3 w, f3 &out) {
-        if (refl) { out = vc.n * (2.f * dot(w, vc.n)) - w; return true; }
-        return refract(w, vc.n, vc.eta, out);
+        if (refl) { out = nn * (2.f * dot(w, nn)) - w; return true; }
+        return refract(w, nn, vc.eta, out);
     };
     auto dxform = [&](f3 w, f3 du, f3 dv, f3 ndu, f3 ndv, f3 &ou, f3 &ov) {
-        if (refl) d_reflect(w, du, dv, vc.n, ndu, ndv, ou, ov);
-        else d_refract(w, du, dv, vc.n, ndu, ndv, vc.eta, ou, ov);
+        if (refl) d_reflect(w, du, dv, nn, ndu, ndv, ou, ov);
+        else d_refract(w, du, dv, nn, ndu, ndv, vc.eta, ou, ov);
     };
     float a0, a1, a2, a3, b0, b1, b2, b3;
     f3 t;
@@ -151,7 +198,7 @@ SMS_D bool vertex_anglediff(f3 xp, const Vtx &vc, f3 xn, const Vtx *vp, const Vt
             prev = sph_block(-b0, -b1, -b2, -b3);
         }
         f3 ou, ov;
-        dxform(wi, dwi_du, dwi_dv, vc.dn_du, vc.dn_dv, ou, ov);
+        dxform(wi, dwi_du, dwi_dv, nn_du, nn_dv, ou, ov);
         d_sphcoords(wo, dwo_du, dwo_dv, a0, a1, a2, a3);
         d_sphcoords(t, ou, ov, b0, b1, b2, b3);
         cur = sph_block(a0 - b0, a1 - b1, a2 - b2, a3 - b3);
@@ -175,7 +222,7 @@ SMS_D bool vertex_anglediff(f3 xp, const Vtx &vc, f3 xn, const Vtx *vp, const Vt
             prev = sph_block(a0, a1, a2, a3);
         }
         f3 ou, ov;
-        dxform(wo, dwo_du, dwo_dv, vc.dn_du, vc.dn_dv, ou, ov);
+        dxform(wo, dwo_du, dwo_dv, nn_du, nn_dv, ou, ov);
         d_sphcoords(wi, dwi_du, dwi_dv, a0, a1, a2, a3);
         d_sphcoords(t, ou, ov, b0, b1, b2, b3);
         cur = sph_block(a0 - b0, a1 - b1, a2 - b2, a3 - b3);
@@ -190,9 +237,10 @@ SMS_D bool vertex_anglediff(f3 xp, const Vtx &vc, f3 xn, const Vtx *vp, const Vt
     return false;
 }
 
-// Half-vector constraint of vertex i and its blocks (:500-629).
+// Half-vector constraint of vertex i and its blocks (:500-629); C = H - N with
+// N the offset normal's (x, y) (:618-621).
 SMS_D bool vertex_halfvector(f3 xp, const Vtx &vc, f3 xn, const Vtx *vp, const Vtx *vn, float &c0, float &c1,
-                             M2 &prev, M2 &cur, M2 &next) {
+                             M2 &prev, M2 &cur, M2 &next, f3 no = f3{0.f, 0.f, 1.f}) {
     prev = {0.f, 0.f, 0.f, 0.f};
     cur = prev;
     next = prev;
@@ -234,16 +282,17 @@ SMS_D bool vertex_halfvector(f3 xp, const Vtx &vc, f3 xn, const Vtx *vp, const V
         if (eta != 1.f) { du = du * -1.f; dv = dv * -1.f; }
         next = {dot(s, du), dot(s, dv), dot(t, du), dot(t, dv)};
     }
-    c0 = dot(s, h);
-    c1 = dot(t, h);
+    c0 = dot(s, h) - no.x;
+    c1 = dot(t, h) - no.y;
     return true;
 }
 
 // Constraints, blocks and the block-Thomas Newton step (:1192-1232).  Returns
 // false when a constraint or the solve fails; conv = all |C_i| <= threshold;
 // dx0 = step of the first vertex (the only one reprojection uses).
-template <int K>
-SMS_D bool chain_step(const SolverCfg &cfg, f3 x0, f3 lp, const Chain<K> &c, bool &conv, float &dx0u, float &dx0v) {
+template <int K, bool kRough = false>
+SMS_D bool chain_step(const SolverCfg &cfg, f3 x0, f3 lp, const Chain<K> &c, bool &conv, float &dx0u, float &dx0v,
+                      const f3 *offs = nullptr) {
     float C0[K], C1[K];
     M2 P[K], Cu[K], N[K];
     #pragma unroll
@@ -252,8 +301,9 @@ SMS_D bool chain_step(const SolverCfg &cfg, f3 x0, f3 lp, const Chain<K> &c, boo
         f3 xn = i == K - 1 ? lp : c.v[i + 1].p;
         const Vtx *vp = i > 0 ? &c.v[i - 1] : nullptr;
         const Vtx *vn = i < K - 1 ? &c.v[i + 1] : nullptr;
-        bool ok = cfg.halfvector ? vertex_halfvector(xp, c.v[i], xn, vp, vn, C0[i], C1[i], P[i], Cu[i], N[i])
-                                 : vertex_anglediff(xp, c.v[i], xn, vp, vn, C0[i], C1[i], P[i], Cu[i], N[i]);
+        const f3 no = kRough && offs ? offs[i] : f3{0.f, 0.f, 1.f};
+        bool ok = cfg.halfvector ? vertex_halfvector(xp, c.v[i], xn, vp, vn, C0[i], C1[i], P[i], Cu[i], N[i], no)
+                                 : vertex_anglediff(xp, c.v[i], xn, vp, vn, C0[i], C1[i], P[i], Cu[i], N[i], no);
         if (!ok) return false;
     }
     M2 tmp[K], il[K];
@@ -295,20 +345,22 @@ SMS_D bool chain_step(const SolverCfg &cfg, f3 x0, f3 lp, const Chain<K> &c, boo
 
 // newton_solver (:410-498).  c holds the seed path on entry and the solution
 // on success; tmpl = the estimate's template shapes.
-template <int K, bool kNM = false>
+template <int K, bool kNM = false, bool kRough = false>
 SMS_D bool chain_newton(const DevScene &sc, const SolverCfg &cfg, f3 x0, f3 lp, const int *tmpl, Chain<K> &c,
-                        int &it, uint32_t &err, LaneStats &st) {
+                        int &it, uint32_t &err, LaneStats &st, const f3 *offs = nullptr) {
+    ChainOffsets<K> co;
+    co.offs = offs;
     it = 0;
     float beta = 1.f;
     bool need = true, conv = false, ok = true;
     float du = 0.f, dv = 0.f;
     while (it < cfg.max_iterations) {
-        if (need) ok = chain_step<K>(cfg, x0, lp, c, conv, du, dv);
+        if (need) ok = chain_step<K, kRough>(cfg, x0, lp, c, conv, du, dv, offs);
         if (!ok) break;
         if (conv) break;
         f3 p0 = c.v[0].p - (c.v[0].dp_du * du + c.v[0].dp_dv * dv) * (cfg.step_scale * beta);
         Chain<K> prop;
-        if (trace_chain<K, kNM>(sc, x0, p0, tmpl, false, prop, nullptr, err, st)) {
+        if (trace_chain<K, kNM, kRough>(sc, x0, p0, tmpl, false, prop, nullptr, err, st, false, co)) {
             beta = fminf(1.f, 2.f * beta);
             c = prop;
             need = true;
@@ -330,8 +382,11 @@ SMS_D bool chain_newton(const DevScene &sc, const SolverCfg &cfg, f3 x0, f3 lp, 
 }
 
 // specular_reflectance (:920-1023): Fresnel along the re-traced chain, then
-// the light visibility test.
-template <int K, bool kNM = false>
+// the light visibility test.  At a rough vertex the reference computes the
+// glossy BSDF value in the half-vector domain (:963-985) but multiplies only
+// the delta branch's factor into the throughput (:1007): a rough vertex
+// contributes 1, restated as is.
+template <int K, bool kNM = false, bool kRough = false>
 SMS_D float chain_reflectance(const DevScene &sc, f3 x0, f3 lp, const Chain<K> &c, uint32_t &err, LaneStats &st) {
     f3 o = x0, d = normalize(c.v[0].p - x0);
     float val = 1.f;
@@ -345,7 +400,7 @@ SMS_D float chain_reflectance(const DevScene &sc, f3 x0, f3 lp, const Chain<K> &
         Vtx hv;
         vertex_from_hit<kNM>(sc, o, d, h, hv);
         f3 wo = k + 1 < K ? normalize(c.v[k + 1].p - hv.p) : normalize(lp - hv.p);
-        val *= specular_reflectance(sc.shapes[h.shape], hv.n, wo);
+        if (!kRough || !(sc.shapes[h.shape].alpha > 0.f)) val *= specular_reflectance(sc.shapes[h.shape], hv.n, wo);
         o = hv.p;
         d = wo;
         last = hv.p;
@@ -430,7 +485,7 @@ SMS_D float chain_geometric(f3 x, const Chain<K> &c, f3 yp, f3 ydu, f3 ydv) {
 }
 
 // evaluate_path_contribution (:229-278).
-template <int K, bool kNM = false>
+template <int K, bool kNM = false, bool kRough = false>
 SMS_D f3 chain_contribution(const DevScene &sc, f3 x, const Light &L, const Chain<K> &sol, uint32_t &err,
                             LaneStats &st) {
     f3 yp, ydu, ydv, lw, lp;
@@ -438,7 +493,7 @@ SMS_D f3 chain_contribution(const DevScene &sc, f3 x, const Light &L, const Chai
     Chain<K> c = sol;
     #pragma unroll
     for (int i = 0; i < K; ++i) make_orthonormal(c.v[i].dp_du, c.v[i].dp_dv, c.v[i].dn_du, c.v[i].dn_dv);
-    float F = chain_reflectance<K, kNM>(sc, x, lp, c, err, st);
+    float F = chain_reflectance<K, kNM, kRough>(sc, x, lp, c, err, st);
     F *= chain_geometric<K>(x, c, yp, ydu, ydv);
     return lw * F;
 }
@@ -514,12 +569,27 @@ __global__ void __launch_bounds__(128) ms_mnee_check_kernel(DevScene sc, SolverC
     flush_stats(st, ctr, err, kPhaseMs);
 }
 
+// Random numbers per walk: the seed position's 2; with rough chain shapes
+// (kRough) a fixed run of 2 + 2 K: the seed position, then 2 per chain vertex
+// for its offset normal, used only by a first path at a rough vertex (the
+// reference draws those only when it uses them; the fixed run keeps walks
+// independent, as lanes running side by side need, with the same expectation).
+template <int K, bool kRough>
+constexpr uint32_t ms_walk_numbers() { return kRough ? 2u + 2u * (uint32_t)K : 2u; }
+
+// Offset normals of an estimate's template in the unbiased estimator's scratch:
+// rows 3 b + j (vertex b, component j) and row 3 kMaxBounces (the product of
+// their densities) of the float block after the kMaxBounces template-shape rows.
+SMS_D float *ms_offset_rows(int *tmpl, uint32_t n) { return reinterpret_cast<float *>(tmpl + (size_t)kMaxBounces * n); }
+
 // -------------------------------------------------------- biased estimator
 // G lanes per query, one walk per lane; walk m of caster c at stream position
-// 3 + 2 (c M + m).  Unlike the single-scatter estimator, solutions are
-// deduplicated before the contribution, which itself tests visibility
-// (:147-195).
-template <int K, int G, bool kNM>
+// 3 + r (c M + m), r the walk's numbers.  Unlike the single-scatter estimator,
+// solutions are deduplicated before the contribution, which itself tests
+// visibility (:147-195).  kRough: the first complete seed path (the template)
+// also fixes the offset normals; walks after it in its chunk retrace their
+// seed paths about them (:160, :372-375).
+template <int K, int G, bool kNM, bool kRough = false>
 #ifndef SMS_MS_BIASED_MIN_BLOCKS
 #define SMS_MS_BIASED_MIN_BLOCKS 4
 #endif
@@ -537,6 +607,7 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
     LaneStats st;
     uint32_t err = 0;
     const int M = cfg.max_trials > 0 ? cfg.max_trials : 0;
+    constexpr uint32_t kRun = ms_walk_numbers<K, kRough>();
     const uint32_t groups_total = gridDim.x * kGroupsPerBlock;
     const uint32_t rounds = (n + groups_total - 1) / groups_total;
     for (uint32_t r = 0; r < rounds; ++r) {
@@ -562,6 +633,10 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
             for (int b = 0; b < K; ++b) tmpl[b] = -1;
             int nrec = 0;
             f3 cur = splat(0.f);
+            f3 toff[K];           // the template's offset normals (kRough)
+            float tpdf = 1.f;
+            #pragma unroll
+            for (int b = 0; b < K; ++b) toff[b] = mk(0.f, 0.f, 1.f);
             for (int m0 = 0; m0 < M; m0 += G) {
                 int m = m0 + gl;
                 bool act = work && m < M;
@@ -570,11 +645,30 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                 #pragma unroll
                 for (int b = 0; b < K; ++b) shapes[b] = -1;
                 bool seed_ok = false;
+                f3 x1 = splat(0.f);
+                f3 own[K];
+                float own_pdf = 1.f;
+                #pragma unroll
+                for (int b = 0; b < K; ++b) own[b] = mk(0.f, 0.f, 1.f);
                 if (act) {
-                    Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + 2u * ((uint64_t)ci * M + m));
+                    Pcg32 rng = query_rng(seed, query_stream(cfg, stream_off, qi), 3u + kRun * ((uint64_t)ci * M + m));
                     float sx = rng.next_f32(), sy = rng.next_f32();
-                    f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
-                    seed_ok = seed_chain<K, kNM>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st);
+                    x1 = sample_position(sc, sc.shapes[caster], sx, sy);
+                    if constexpr (kRough) {
+                        float dr[2 * K];
+                        #pragma unroll
+                        for (int j = 0; j < 2 * K; ++j) dr[j] = rng.next_f32();
+                        ChainOffsets<K> co;
+                        if (have_tmpl) {
+                            co.offs = toff;
+                        } else {
+                            co.draw = dr; co.out = own; co.pdf = &own_pdf;
+                        }
+                        seed_ok = seed_chain<K, kNM, true>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st,
+                                                           co);
+                    } else {
+                        seed_ok = seed_chain<K, kNM>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st);
+                    }
                 }
                 // the first completed seed path of the estimate is the template
                 unsigned sb = __ballot_sync(kFull, seed_ok) & gmask;
@@ -583,12 +677,37 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                 #pragma unroll
                 for (int b = 0; b < K; ++b)
                     tshape[b] = __shfl_sync(kFull, shapes[b], first_lane >= 0 ? first_lane : (int)lane);
+                // the first completed lane's offsets, broadcast by the whole warp
+                // (the two groups of a 16-lane split may differ in what follows)
+                f3 foff[K];
+                float fpdf = 1.f;
+                if constexpr (kRough) {
+                    const int src = first_lane >= 0 ? first_lane : (int)lane;
+                    #pragma unroll
+                    for (int b = 0; b < K; ++b)
+                        foff[b] = mk(__shfl_sync(kFull, own[b].x, src), __shfl_sync(kFull, own[b].y, src),
+                                     __shfl_sync(kFull, own[b].z, src));
+                    fpdf = __shfl_sync(kFull, own_pdf, src);
+                }
                 bool is_template_walk = false;
                 if (!have_tmpl && first_lane >= 0) {
                     #pragma unroll
                     for (int b = 0; b < K; ++b) tmpl[b] = tshape[b];
                     have_tmpl = true;
                     is_template_walk = (int)lane == first_lane;
+                    if constexpr (kRough) {
+                        #pragma unroll
+                        for (int b = 0; b < K; ++b) toff[b] = foff[b];
+                        tpdf = fpdf;
+                        // walks after the template walk are not first paths:
+                        // their seed paths scatter about the template's offsets
+                        if (act && (int)lane > first_lane) {
+                            ChainOffsets<K> co;
+                            co.offs = toff;
+                            seed_ok = seed_chain<K, kNM, true>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err,
+                                                               st, co);
+                        }
+                    }
                 }
                 bool ok = false;
                 int it = 0;
@@ -598,7 +717,8 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                         #pragma unroll
                         for (int b = 0; b < K; ++b) match = match && shapes[b] == tmpl[b];
                     }
-                    ok = match && chain_newton<K, kNM>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st);
+                    ok = match && chain_newton<K, kNM, kRough>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st,
+                                                               kRough ? toff : nullptr);
                 }
                 if (act) {
                     st.walks++;
@@ -631,7 +751,8 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                     __syncwarp();
                 }
                 f3 contrib = splat(0.f);
-                if (keep) contrib = diffuse_eval(Q, dir) * chain_contribution<K, kNM>(sc, Q.x, L, c, err, st);
+                if (keep)
+                    contrib = diffuse_eval(Q, dir) * chain_contribution<K, kNM, kRough>(sc, Q.x, L, c, err, st);
                 // sum in walk order
                 for (int k = 0; k < G; ++k) {
                     const int src = gbase + k;
@@ -641,6 +762,8 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                     if (kk) cur = cur + vk;
                 }
             }
+            // result += value / m_offset_normals_pdf (:198)
+            if (kRough) cur = mk(cur.x / tpdf, cur.y / tpdf, cur.z / tpdf);
             acc = acc + cur;
             n_unique += nrec;
         }
@@ -658,8 +781,9 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
 // ------------------------------------------------------ unbiased estimator
 // Part 1: one lane per query runs the first walk (its seed path is the
 // template) and the contribution; every success is queued for trials
-// (:95-110; the contribution tests visibility itself).
-template <int K, bool kNM>
+// (:95-110; the contribution tests visibility itself).  kRough: the first walk
+// draws the offset normals the trials keep.
+template <int K, bool kNM, bool kRough = false>
 __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cfg, int ci, const float *__restrict__ qs,
                                                        uint32_t n, uint64_t seed, uint64_t stream_off,
                                                        float *__restrict__ value, int *__restrict__ count,
@@ -688,25 +812,44 @@ __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cf
             int caster = sc.casters_ms[ci];
             rng.advance(pos - 3u);
             float sx = rng.next_f32(), sy = rng.next_f32();
-            pos += 2u;
+            pos += ms_walk_numbers<K, kRough>();
             f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
             Chain<K> c;
             int shapes[K];
             int it = 0;
-            bool ok = seed_chain<K, kNM>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st) &&
-                      chain_newton<K, kNM>(sc, cfg, Q.x, L.p, shapes, c, it, err, st);
+            f3 own[K];
+            float own_pdf = 1.f;
+            ChainOffsets<K> co;
+            float dr[2 * K];
+            if constexpr (kRough) {
+                #pragma unroll
+                for (int j = 0; j < 2 * K; ++j) dr[j] = rng.next_f32();
+                co.draw = dr; co.out = own; co.pdf = &own_pdf;
+            }
+            bool ok = seed_chain<K, kNM, kRough>(sc, cfg, caster, Q.x, x1, L.p, nullptr, c, shapes, err, st, co) &&
+                      chain_newton<K, kNM, kRough>(sc, cfg, Q.x, L.p, shapes, c, it, err, st, kRough ? own : nullptr);
             st.walks++;
             st.newton += (unsigned)it;
             nw++;
             if (ok) {
                 st.succ++;
                 f3 dir = normalize(c.v[0].p - Q.x);
-                f3 spec = chain_contribution<K, kNM>(sc, Q.x, L, c, err, st);
+                f3 spec = chain_contribution<K, kNM, kRough>(sc, Q.x, L, c, err, st);
                 f3 val = diffuse_eval(Q, dir) * spec;
                 scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;
                 scr.val[qi] = val.x; scr.val[(size_t)n + qi] = val.y; scr.val[2 * (size_t)n + qi] = val.z;
                 #pragma unroll
                 for (int b = 0; b < K; ++b) tmpl_out[(size_t)b * n + qi] = shapes[b];
+                if constexpr (kRough) {
+                    float *orow = ms_offset_rows(tmpl_out, n);
+                    #pragma unroll
+                    for (int b = 0; b < K; ++b) {
+                        orow[(size_t)(3 * b) * n + qi] = own[b].x;
+                        orow[(size_t)(3 * b + 1) * n + qi] = own[b].y;
+                        orow[(size_t)(3 * b + 2) * n + qi] = own[b].z;
+                    }
+                    orow[(size_t)(3 * kMaxBounces) * n + qi] = own_pdf;
+                }
                 enqueue = true;
             } else {
                 st.fail++;
@@ -731,8 +874,8 @@ __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cf
 }
 
 // Part 2: Bernoulli trials, 32 per warp step (:111-135); trial walks must
-// reproduce the template's shapes.
-template <int K, bool kNM>
+// reproduce the template's shapes (and, kRough, scatter about its offsets).
+template <int K, bool kNM, bool kRough = false>
 __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg cfg, int ci, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
@@ -759,6 +902,19 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
         int tmpl[K];
         #pragma unroll
         for (int b = 0; b < K; ++b) tmpl[b] = tmpl_in[(size_t)b * n + qi];
+        f3 toff[K];
+        float tpdf = 1.f;
+        #pragma unroll
+        for (int b = 0; b < K; ++b) toff[b] = mk(0.f, 0.f, 1.f);
+        if constexpr (kRough) {
+            const float *orow = ms_offset_rows(const_cast<int *>(tmpl_in), n);
+            #pragma unroll
+            for (int b = 0; b < K; ++b)
+                toff[b] = mk(orow[(size_t)(3 * b) * n + qi], orow[(size_t)(3 * b + 1) * n + qi],
+                             orow[(size_t)(3 * b + 2) * n + qi]);
+            tpdf = orow[(size_t)(3 * kMaxBounces) * n + qi];
+        }
+        constexpr uint32_t kRun = ms_walk_numbers<K, kRough>();
         int first = 0;
         for (int t0 = 1; t0 <= cap; t0 += 32) {
             int t = t0 + (int)lane;
@@ -766,12 +922,15 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
             int it = 0;
             if (t <= cap) {
                 Pcg32 rng = base;
-                rng.advance((uint64_t)(pos - 3u) + 2u * (uint64_t)(t - 1));
+                rng.advance((uint64_t)(pos - 3u) + kRun * (uint64_t)(t - 1));
                 float sx = rng.next_f32(), sy = rng.next_f32();
                 f3 x1 = sample_position(sc, sc.shapes[caster], sx, sy);
                 Chain<K> c;
-                bool ok = seed_chain<K, kNM>(sc, cfg, caster, Q.x, x1, L.p, tmpl, c, nullptr, err, st) &&
-                          chain_newton<K, kNM>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st);
+                ChainOffsets<K> co;
+                co.offs = toff;
+                bool ok = seed_chain<K, kNM, kRough>(sc, cfg, caster, Q.x, x1, L.p, tmpl, c, nullptr, err, st, co) &&
+                          chain_newton<K, kNM, kRough>(sc, cfg, Q.x, L.p, tmpl, c, it, err, st,
+                                                       kRough ? toff : nullptr);
                 succ = ok && fabsf(dot(dir0, normalize(c.v[0].p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
             }
             unsigned b = __ballot_sync(kFull, succ);
@@ -789,12 +948,14 @@ __global__ void __launch_bounds__(128) ms_trials_kernel(DevScene sc, SolverCfg c
             if (!first && cfg.max_trials <= 0) err |= kErrTrialLimit;
             f3 val = mk(scr.val[qi], scr.val[(size_t)n + qi], scr.val[2 * (size_t)n + qi]);
             f3 cur = val * inv_prob;
+            // result += value / m_offset_normals_pdf (:198)
+            if (kRough) cur = mk(cur.x / tpdf, cur.y / tpdf, cur.z / tpdf);
             value[qi] += cur.x;
             value[(size_t)n + qi] += cur.y;
             value[2 * (size_t)n + qi] += cur.z;
             count[qi] = first ? iterations : -1;
             walks[qi] += trial_walks;
-            scr.pos[qi] = pos + 2u * (uint32_t)trial_walks;
+            scr.pos[qi] = pos + kRun * (uint32_t)trial_walks;
             st.calls++;
             st.iters += (unsigned long long)iterations;
             st.imax = max(st.imax, (unsigned long long)iterations);
@@ -821,7 +982,7 @@ cudaError_t ms_walk_k(const DevScene &sc, const SolverCfg &cfg, int caster, cons
     return cudaGetLastError();
 }
 
-template <int K, bool kNM>
+template <int K, bool kNM, bool kRough = false>
 cudaError_t ms_connect_k(const DevScene &sc, const SolverCfg &cfg, const float *q, uint32_t n, uint64_t seed,
                          uint64_t stream_off, float *value, int *count, int *walks, DevCounters *ctr,
                          const SsScratch &scr, int *tmpl, int num_sms, int bps, PhaseTimer *tm, cudaStream_t s) {
@@ -830,7 +991,7 @@ cudaError_t ms_connect_k(const DevScene &sc, const SolverCfg &cfg, const float *
         const uint32_t gpb = 128 / G;
         uint32_t blocks = std::min<uint32_t>((n + gpb - 1) / gpb, (uint32_t)(num_sms * bps));
         phase_begin(tm, kPhaseMs, s);
-        auto kernel = G == 16 ? ms_biased_kernel<K, 16, kNM> : ms_biased_kernel<K, 32, kNM>;
+        auto kernel = G == 16 ? ms_biased_kernel<K, 16, kNM, kRough> : ms_biased_kernel<K, 32, kNM, kRough>;
         kernel<<<blocks, 128, 0, s>>>(sc, cfg, q, n, seed, stream_off, value, count, walks, ctr);
         phase_end(tm, s);
         return cudaGetLastError();
@@ -839,8 +1000,8 @@ cudaError_t ms_connect_k(const DevScene &sc, const SolverCfg &cfg, const float *
         cudaError_t e = cudaMemsetAsync(&ctr->trial_count, 0, 2 * sizeof(unsigned), s);
         if (e != cudaSuccess) return e;
         phase_begin(tm, kPhaseMs, s);
-        auto first = ms_first_kernel<K, kNM>;
-        auto trials = ms_trials_kernel<K, kNM>;
+        auto first = ms_first_kernel<K, kNM, kRough>;
+        auto trials = ms_trials_kernel<K, kNM, kRough>;
         first<<<(n + 127) / 128, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, tmpl, ctr);
         trials<<<num_sms * bps, 128, 0, s>>>(sc, cfg, c, q, n, seed, stream_off, value, count, walks, scr, tmpl,
                                               ctr);

@@ -234,11 +234,12 @@ def slab_waves(seed: int, n_waves: int = 8):
     return waves
 
 
-def slab_scene(res: int = 256) -> SceneDesc:
+def slab_scene(res: int = 256, alpha: float = 0.0) -> SceneDesc:
     """Glass slab: top face caustic_caster_multi (normals up), bottom face
-    caustic_bouncer (normals down, i.e. outward), IOR 1.5; point light."""
+    caustic_bouncer (normals down, i.e. outward), IOR 1.5; point light.
+    alpha > 0: both faces rough (Beckmann roughdielectric)."""
     d = SceneDesc()
-    glass = Bsdf(BSDF_DIELECTRIC, 1.5)
+    glass = Bsdf(BSDF_DIELECTRIC, 1.5, alpha=alpha)
     P, N, UV, F = heightfield_mesh(res, 1.0, 1.3, slab_waves(4))
     d.add_mesh(P, F, glass, SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
     P, N, UV, F = heightfield_mesh(res, 1.0, 1.0, slab_waves(5), flip_normals=True)
@@ -321,12 +322,13 @@ def glint_camera():
 
 
 def glint_scene(map_res: int = 8192, slopes: np.ndarray | None = None, intensity: float = 50.0,
-                conductor=(1.0, 6.0)) -> SceneDesc:
+                conductor=(1.0, 6.0), alpha: float = 0.0) -> SceneDesc:
+    """alpha > 0: a rough (Beckmann) conductor under the slope map."""
     d = SceneDesc()
     P = np.array([[-0.5, -0.5, 0.0], [0.5, -0.5, 0.0], [0.5, 0.5, 0.0], [-0.5, 0.5, 0.0]], np.float32)
     UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
     F = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
-    sid = d.add_mesh(P, F, Bsdf(BSDF_CONDUCTOR, conductor[0], conductor[1]), SHAPE_GLINTY, UV=UV)
+    sid = d.add_mesh(P, F, Bsdf(BSDF_CONDUCTOR, conductor[0], conductor[1], alpha=alpha), SHAPE_GLINTY, UV=UV)
     d.normalmap = (sid, glint_slopes(map_res) if slopes is None else slopes, 1.0)
     _, light = glint_camera()
     d.add_point_emitter(tuple(light), (intensity,) * 3, EMITTER_CAUSTIC_SINGLE)

@@ -91,3 +91,34 @@ def test_glint_full_size(sms, workloads, gpu_lib):
     assert np.all(v[:, c == 0] == 0)
     assert st["walks"] == w.sum() and st["connections"] == q.shape[1]
     assert (c > 0).mean() > 0.01
+
+
+@pytest.mark.parametrize("biased", [True, False])
+def test_rough_glint_connect(sms, workloads, oracle, gpu_lib, biased):
+    """Rough glinty surface (manifold_glints.cpp:56-64, :141, :383-393): a
+    visible-normal Beckmann offset drawn after the emitter sample shifts the
+    target slope, the glossy BSDF value of the normal-mapped rough conductor
+    replaces the Fresnel factor, and the estimate is divided by the offset's
+    density.  GPU vs oracle on the same random streams, against the
+    oracle-vs-FMA floor; the offsets' inverse error function differs in the
+    last bits between the two (CUDA's erfinvf, the oracle's own)."""
+    W = workloads
+    desc = W.glint_scene(slopes=_slopes(W, 1024), alpha=0.05)
+    cfg = W.glint_config() if biased else sms.SMSConfig(max_iterations=10, max_trials=64)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    gl = sms.SpecularManifoldGlints(ctx)
+    q = W.glint_queries(256)
+    vg, cg, wg = gl.specular_manifold_sampling(q, seed=3)
+    vo, co, wo, st_o = oracle.OracleScene(desc).connect_batch(cfg, q, seed=3, glints=True)
+    vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=3, glints=True)
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    print(f"rough glints {'biased' if biased else 'unbiased'}: count mismatch {g_cm:.4f} differs {g_diff:.4f} "
+          f"(floor {f_cm:.4f}/{f_diff:.4f}) median rel {g_med:.1e} nonzero {(vo[0] > 0).mean():.3f}")
+    assert (co != 0).sum() > 50
+    assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+    assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+    assert g_med < 1e-3
+    st = ctx.stats()
+    assert st["connections"] == st_o["connections"] and st["walks"] == wg.sum()
+    ctx.close()

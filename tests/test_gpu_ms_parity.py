@@ -121,3 +121,36 @@ def test_slab_mnee_init_walks(sms, workloads, oracle, gpu_lib):
     print(f"slab mnee walks: gpu mismatch {g_m:.4f} (floor {f_m:.4f}) both {nboth}")
     assert nboth > n // 4
     assert g_m <= FLOOR_FACTOR * f_m + FLOOR_SLACK and g_c <= FLOOR_FACTOR * f_c + FLOOR_SLACK
+
+
+@pytest.mark.parametrize("biased", [True, False])
+def test_rough_slab_connect(sms, workloads, oracle, gpu_lib, biased):
+    """Rough chain shapes (manifold_ms.cpp:356-375): the first complete seed
+    path samples a Beckmann offset normal at every rough vertex, later walks
+    scatter about those offsets and must hit the same shapes, the Newton steps
+    solve the offset constraints (:618-621, :707-717) and the estimate is
+    divided by the offsets' density (:198).  Both slab faces rough (alpha 0.1);
+    GPU vs oracle on the same random streams, against the oracle-vs-FMA floor."""
+    W = workloads
+    desc = W.slab_scene(alpha=0.1)
+    cfg = W.slab_config() if biased else sms.SMSConfig(bounces=2, max_iterations=30, max_trials=64)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    ms = sms.SpecularManifoldMultiScatter(ctx)
+    n = 4096 if biased else 8192
+    q = W.slab_queries(n)
+    vg, cg, wg = ms.specular_manifold_sampling(q, seed=2)
+    vo, co, wo, st_o = oracle.OracleScene(desc).connect_batch(cfg, q, seed=2, multi=True)
+    vf, cf, wf, _ = oracle.OracleScene(desc, fma=True).connect_batch(cfg, q, seed=2, multi=True)
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    print(f"rough slab {'biased' if biased else 'unbiased'}: count mismatch {g_cm:.4f} differs {g_diff:.4f} "
+          f"(floor {f_cm:.4f}/{f_diff:.4f}) median rel {g_med:.1e} nonzero {np.mean(vo[0] > 0):.3f}")
+    assert np.mean(vo[0] > 0) > 0.3
+    assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+    assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+    assert g_med < 1e-4
+    st = ctx.stats()
+    assert st["connections"] == n and st["walks"] == wg.sum()
+    if biased:
+        assert np.all(wg == cfg.max_trials)
+    ctx.close()

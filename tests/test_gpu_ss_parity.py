@@ -299,11 +299,14 @@ def test_rough_caster_connect(sms, workloads, oracle, gpu_lib, biased, conductor
     ctx.close()
 
 
-def test_rough_multi_scatter_and_glints_are_refused(sms, workloads, gpu_lib):
+def test_rough_normal_mapped_chain_is_refused(sms, workloads, gpu_lib):
+    """Rough chain shapes are supported (tests/test_gpu_ms_parity.py), rough
+    normal-mapped chain shapes are not: SMS_ERR_UNSUPPORTED."""
     W = workloads
     d = sms.SceneDesc()
     P, N, UV, F = W.heightfield_mesh(8, 1.0, 1.3, [])
-    d.add_mesh(P, F, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5, alpha=0.1), sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    sid = d.add_mesh(P, F, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5, alpha=0.1), sms.SHAPE_CAUSTIC_CASTER_MULTI, N=N, UV=UV)
+    d.normalmap = (sid, W.nm_plane_slopes(64), 1.0)
     d.add_point_emitter((0.0, 0.0, 4.0), (40.0,) * 3, sms.EMITTER_CAUSTIC_MULTI)
     ctx = sms.Context(sms.Scene(d), sms.SMSConfig(bounces=1, biased=True, max_trials=4))
     with pytest.raises(sms.SMSError) as e:

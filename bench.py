@@ -280,11 +280,12 @@ def connect_timed(torch, sms, ctx, kind, q_dev, n, seed, stream_offset=0):
     return val, t.ms
 
 
-def secondary_configs(torch, sms, W, dev, only=None, calls=5):
+def secondary_configs(torch, sms, W, dev, only=None, calls=5, max_queries=None):
     """Throughput of the other solver configurations (one GPU): sphere
     (biased, 16 walks), two-bounce slab (biased, 32 walks, 512k queries) and
     glints (8192^2 FP16 slope map, 1024^2 pixels, 64 seeds, vectorized).
-    only: run just that configuration (for profiling one kernel)."""
+    only: run just that configuration (for profiling one kernel), on its first
+    max_queries queries if given."""
     out = {}
     cases = [
         ("sphere_biased_m16", "ss", W.sphere_scene, W.sphere_config, lambda: W.sphere_queries(64), 16),
@@ -295,8 +296,20 @@ def secondary_configs(torch, sms, W, dev, only=None, calls=5):
         if only and name != only:
             continue
         ctx = sms.Context(sms.Scene(scene()), config(), device=dev)
-        q = torch.from_numpy(np.ascontiguousarray(queries(), np.float32)).to(f"cuda:{dev}")
+        qh = queries()
+        if max_queries:
+            qh = qh[:, :max_queries]
+        q = torch.from_numpy(np.ascontiguousarray(qh, np.float32)).to(f"cuda:{dev}")
         n = q.shape[1]
+        tuned = None
+        if kind in ("ms", "glints"):
+            # blocks per SM of the persistent kernels, picked on the same queries
+            from sms_gb300.autotune import autotune_blocks
+            bufs = [torch.empty((3, n), dtype=torch.float32, device=f"cuda:{dev}"),
+                    torch.empty(n, dtype=torch.int32, device=f"cuda:{dev}"),
+                    torch.empty(n, dtype=torch.int32, device=f"cuda:{dev}")]
+            torch.cuda.synchronize()
+            tuned = autotune_blocks(sms, ctx, kind, q.data_ptr(), n, *(b.data_ptr() for b in bufs), repeats=1)
         for i in range(3):
             connect_timed(torch, sms, ctx, kind, q, n, seed=50 + i)
         ctx.reset_stats()
@@ -308,6 +321,8 @@ def secondary_configs(torch, sms, W, dev, only=None, calls=5):
                      "walks_per_s": st["walks"] / (calls * t / 1e3), "walks_per_connection": walks,
                      "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),
                      "newton_iterations_per_s": its_per_s}
+        if tuned:
+            out[name]["launch"] = {"blocks_per_sm": tuned["best"], "autotune_ms": tuned["ms"]}
         units = flops_per_unit().get(name)
         if units:
             if kind == "glints":
@@ -456,7 +471,7 @@ def learned_study(torch, sms, W, ctx, dev, pairs=4 << 20, steps=20000, batch=819
     ws = torch.empty(ns, dtype=torch.int32, device=f"cuda:{dev}")
     torch.cuda.synchronize()
     tune = autotune_ss(sms, ctx, qs.data_ptr(), ns, vs.data_ptr(), cs.data_ptr(), ws.data_ptr(),
-                       blocks_per_sm=(16,), trial_groups=(8, 16, 32), treelets=(0,), seed=99)
+                       blocks_per_sm=(16,), trial_groups=(8, 16, 32), treelets=(0,), chunks=(1,), seed=99)
     learned_group = tune["best"][1]
     ctx.set_proposal(None)
     ctx.set_launch(0, 0)
@@ -706,7 +721,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "queries_per_step": n, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}",
                    "launch": ({"blocks_per_sm": tuned["best"][0], "trial_group": tuned["best"][1],
-                               "treelet_nodes": tuned["best"][2],
+                               "treelet_nodes": tuned["best"][2], "queue_chunk": tuned["best"][3],
                                "autotune_ms": tuned["ms"]} if tuned else "library default")},
         "walks_per_s": world * st["walks"] / total_s,
         "newton_iterations_per_walk": st["newton_iterations"] / max(1, st["walks"]),
@@ -797,8 +812,9 @@ def main():
         import torch
         sms = load_package()
         from sms_gb300 import workloads as W
+        mq = args.queries if args.queries != N_QUERIES else None
         print(json.dumps({"configs": secondary_configs(torch, sms, W, 0, only=args.secondary_only,
-                                                       calls=args.steps)}), flush=True)
+                                                       calls=args.steps, max_queries=mq)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

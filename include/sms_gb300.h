@@ -208,6 +208,10 @@ sms_status sms_ctx_set_trial_group(sms_ctx *ctx, int32_t group);
  * L1 for the top levels; results do not depend on it.  No counterpart in the
  * reference (a staging knob of the batched solver, set by the autotuner). */
 sms_status sms_ctx_set_treelet(sms_ctx *ctx, int32_t nodes);
+/* Queries a lane group of the Bernoulli-trial kernel claims from the work queue
+ * per atomic, 1..64 (default 1).  Results do not depend on it.  No counterpart
+ * in the reference (a tuning knob of the batched solver, set by the autotuner). */
+sms_status sms_ctx_set_queue_chunk(sms_ctx *ctx, int32_t chunk);
 
 /* ---------------------------------------------------------------- queries */
 /* Shading-point query, SoA with SMS_QUERY_FIELDS rows of n floats each:

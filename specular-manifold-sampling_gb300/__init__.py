@@ -148,6 +148,7 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ctx_set_launch": (i32, [vp, i32, i32]),
         "sms_ctx_set_trial_group": (i32, [vp, i32]),
         "sms_ctx_set_treelet": (i32, [vp, i32]),
+        "sms_ctx_set_queue_chunk": (i32, [vp, i32]),
         "sms_stats_read": (i32, [vp, C.POINTER(_Stats)]),
         "sms_stats_reset": (i32, [vp]),
         "sms_ctx_set_profiling": (i32, [vp, i32]),
@@ -422,6 +423,10 @@ class Context:
         """Top node records of the tree the Bernoulli-trial kernel stages in
         shared memory (0..384, 0 = none)."""
         _check(_LIB.sms_ctx_set_treelet(self._h, nodes))
+
+    def set_queue_chunk(self, chunk: int = 1):
+        """Queries a Bernoulli-trial lane group claims per atomic (1..64)."""
+        _check(_LIB.sms_ctx_set_queue_chunk(self._h, chunk))
 
     def stats(self) -> dict:
         s = _Stats()

@@ -336,7 +336,10 @@ SMS_HD bool box2(float lox, float loy, float loz, float hix, float hiy, float hi
 
 // Closest hit (any_hit = false) or occlusion test (any_hit = true) against the
 // whole scene; one traversal loop serves both so that lanes of a warp casting
-// different kinds of rays still traverse together.  Returns false and sets *err on stack overflow (treated as miss).
+// different kinds of rays still traverse together.  kTree: the launching
+// kernel holds the top sc.n_tnodes node records in shared memory (a separate
+// instantiation, so that kernels without it keep the plain fetch).  Returns false and sets *err on stack overflow (treated as miss).
+template <bool kTree = false>
 SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool any_hit, Hit &hit,
                   uint32_t &err) {
     hit.t = maxt; hit.shape = -1; hit.prim = 0; hit.u = hit.v = 0.f;
@@ -374,7 +377,7 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
         float4 n0, n1, n2;
         int4 n3;
 #ifdef __CUDA_ARCH__
-        if ((uint32_t)node < sc.n_tnodes) {
+        if (kTree && (uint32_t)node < sc.n_tnodes) {
             const float4 *sp = sms_tree_smem + 4 * node;
             n0 = sp[0]; n1 = sp[1]; n2 = sp[2];
             n3 = *reinterpret_cast<const int4 *>(sp + 3);

@@ -194,7 +194,7 @@ SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
 // the accepted solution and, with kTrack, (h_acc, d_acc) the hit that
 // produced it; true = converged there and admissible
 // (reflection vs refraction, :391-402).
-template <bool kTrack, bool kNM>
+template <bool kTrack, bool kNM, bool kTree = false>
 SMS_D bool ss_newton(const DevScene &sc, const SolverCfg &cfg, f3 x, f3 lp, Vtx &v, Hit &h, Hit &h_acc, f3 &d_acc,
                      int &it, uint32_t &err, LaneStats &st, f3 no, bool coarse) {
     float beta = 1.f;
@@ -208,7 +208,7 @@ SMS_D bool ss_newton(const DevScene &sc, const SolverCfg &cfg, f3 x, f3 lp, Vtx 
         if (sqrtf(c0 * c0 + c1 * c1) < cfg.solver_threshold) { conv = true; break; }
         f3 pp = v.p - (v.dp_du * dx0 + v.dp_dv * dx1) * (cfg.step_scale * beta);
         f3 dd = normalize(pp - x);
-        trace(sc, x, dd, kRayEps, INFINITY, false, h, err);
+        trace<kTree>(sc, x, dd, kRayEps, INFINITY, false, h, err);
         st.ray(h);
         it++;
         if (h.shape < 0 || h.shape != v.shape) {
@@ -253,14 +253,14 @@ SMS_D float2 sample_slope_gaussian(float mx, float my, float sa, float sb, float
 // two numbers), then the solve on the full normal map from its solution.
 // Returns ok; v holds the solution vertex; it counts all iterations.
 // kNM: the caster may be normal-mapped (its manifold vertices read the map).
-template <bool kOffset = false, bool kTwoStage = false, bool kNM = false>
+template <bool kOffset = false, bool kTwoStage = false, bool kNM = false, bool kTree = false>
 SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f3 lp, f3 seed, Vtx &v, int &it,
                    uint32_t &err, LaneStats &st, f3 *p_init = nullptr, f3 no_in = f3{0.f, 0.f, 1.f}, float g0 = 0.f,
                    float g1 = 0.f) {
     const f3 no = kOffset ? no_in : f3{0.f, 0.f, 1.f};
     f3 d = normalize((cfg.mnee_init ? mnee_target(sc.shapes[caster], lp) : seed) - x);
     Hit h;
-    trace(sc, x, d, kRayEps, INFINITY, false, h, err);
+    trace<kTree>(sc, x, d, kRayEps, INFINITY, false, h, err);
     st.ray(h);
     it = 0;
     if (h.shape < 0) return false;
@@ -276,13 +276,13 @@ SMS_D bool ss_walk(const DevScene &sc, const SolverCfg &cfg, int caster, f3 x, f
                                                 g0, g1);
         const f3 ln = normalize(mk(-sl.x, -sl.y, 1.f));
         int it1;
-        const bool ok1 = ss_newton<true, kNM>(sc, cfg, x, lp, v, h, h_acc, d_acc, it1, err, st, ln, true);
+        const bool ok1 = ss_newton<true, kNM, kTree>(sc, cfg, x, lp, v, h, h_acc, d_acc, it1, err, st, ln, true);
         it = it1;
         if (!ok1) return false;
         vertex_from_hit<kNM>(sc, x, d_acc, h_acc, v, nullptr, false);   // ManifoldVertex(si_smooth, 0)
     }
     int it2;
-    const bool ok = ss_newton<false, kNM>(sc, cfg, x, lp, v, h, h, d, it2, err, st, no, false);
+    const bool ok = ss_newton<false, kNM, kTree>(sc, cfg, x, lp, v, h, h, d, it2, err, st, no, false);
     it += it2;
     return ok;
 }

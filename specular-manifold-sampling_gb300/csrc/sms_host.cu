@@ -351,6 +351,7 @@ struct sms_ctx {
     int threads = 128;
     int trial_group = 0;          // lanes per query of the Bernoulli-trial kernel (0: auto)
     uint32_t treelet = 0;         // node records the trial kernel stages in shared memory
+    int queue_chunk = 1;          // queries a trial-kernel lane group claims per atomic
     // device staging for the host-pointer entry points
     void *io = nullptr;
     size_t io_bytes = 0;
@@ -402,6 +403,7 @@ static SolverCfg solver_cfg(const sms_config &c) {
     s.mnee_init = c.mnee_init;
     s.twostage = c.twostage;
     s.streams = nullptr;
+    s.queue_chunk = 1;
     return s;
 }
 
@@ -683,6 +685,13 @@ extern "C" sms_status sms_ctx_set_treelet(sms_ctx *c, int32_t nodes) {
     return SMS_OK;
 }
 
+extern "C" sms_status sms_ctx_set_queue_chunk(sms_ctx *c, int32_t chunk) {
+    if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
+    if (chunk < 1 || chunk > 64) return fail(SMS_ERR_INVALID_ARG, "queue chunk must be in [1, 64]");
+    c->queue_chunk = chunk;
+    return SMS_OK;
+}
+
 extern "C" sms_status sms_ctx_set_launch(sms_ctx *c, int32_t bps, int32_t tpb) {
     if (!c) return fail(SMS_ERR_INVALID_ARG, "null context");
     if (bps < 0 || tpb < 0) return fail(SMS_ERR_INVALID_ARG, "negative launch parameter");
@@ -855,6 +864,7 @@ sms_status ctx_ss_connect(sms_ctx *c, const float *q, uint32_t n, uint64_t seed,
     }
     SolverCfg sc = solver_cfg(c->cfg);
     sc.streams = streams;
+    sc.queue_chunk = c->queue_chunk;
     CUDA_TRY(launch_ss_connect(c->dsc, sc, q, n, seed, stream_off, out->value, out->count, out->walks, c->ctr, scr,
                                c->num_sms, c->blocks_per_sm, &c->timer, c->stream, c->prop ? &pr : nullptr,
                                c->trial_group, c->treelet));

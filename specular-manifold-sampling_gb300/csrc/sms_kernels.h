@@ -34,6 +34,9 @@ struct SolverCfg {
     // its path and bounce, so that results do not depend on which paths of a
     // wavefront reached a receiver or on how the queries were batched).
     const uint64_t *streams;
+    // Queries a lane group of the Bernoulli-trial kernel claims from the work
+    // queue per atomic (1: one at a time).
+    int queue_chunk;
 };
 
 // Unique-solution capacity per query of the biased estimator (shared memory

@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_first_kernel(D
 //
 // All lanes run one warp-uniform loop: groups whose query finished fetch the
 // next one at the top, so every ballot and shuffle has the whole warp.
-template <bool kLearned, int G, int kVar>
+template <bool kLearned, int G, int kVar, bool kTree = false>
 __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_trials_kernel(DevScene sc, SolverCfg cfg, int c, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,
                                                         float *__restrict__ value, int *__restrict__ count,
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_trials_kernel(
                                                         mlp::SeedProposal pr) {
     static_assert(G == 8 || G == 16 || G == 32, "group size");
     constexpr bool kRough = (kVar & 1) != 0, kTwo = (kVar & 2) != 0, kNM = (kVar & 4) != 0;
-    tree_smem_fill(sc);
+    if (kTree) tree_smem_fill(sc);
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31;
     const unsigned gbase = lane & ~(unsigned)(G - 1), gl = lane - gbase;
@@ -289,6 +289,8 @@ __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_trials_kernel(
     const unsigned n_list = *(volatile unsigned *)&ctr->trial_count;
     // per-group state (replicated on the group's lanes)
     bool have = false, drained = false;
+    const unsigned chunk = cfg.queue_chunk > 1 ? (unsigned)cfg.queue_chunk : 1u;
+    unsigned cnext = 0, cend = 0;   // the group's claimed range of the queue
     uint32_t qi = 0, pos = 0;
     int t0 = 1;
     Query Q;
@@ -298,12 +300,17 @@ __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_trials_kernel(
     f3 no = mk(0.f, 0.f, 1.f);
     const DevShape &cshape = sc.shapes[caster];
     while (true) {
-        // groups without a query take the next one
+        // groups without a query take the next one, claiming `chunk` queue
+        // entries per atomic
         const bool need = !have && !drained;
-        unsigned idx = 0;
-        if (need && gl == 0) idx = atomicAdd(&ctr->trial_head, 1u);
-        idx = __shfl_sync(full, idx, gbase);
+        const bool claim = need && cnext == cend;
+        unsigned got = 0;
+        if (claim && gl == 0) got = atomicAdd(&ctr->trial_head, chunk);
+        got = __shfl_sync(full, got, gbase);
+        if (claim) { cnext = got; cend = got + chunk; }
+        const unsigned idx = cnext;
         if (need) {
+            ++cnext;
             if (idx < n_list) {
                 have = true;
                 qi = scr.list[idx];
@@ -342,7 +349,8 @@ __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_trials_kernel(
             float g0 = 0.f, g1 = 0.f;
             if (kTwo) { g0 = rng.next_f32(); g1 = rng.next_f32(); }
             Vtx v;
-            succ = ss_walk<kRough, kTwo, kNM>(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no, g0, g1) &&
+            succ = ss_walk<kRough, kTwo, kNM, kTree>(sc, cfg, caster, Q.x, L.p, sp, v, it, err, st, nullptr, no, g0,
+                                                     g1) &&
                    fabsf(dot(dir0, normalize(v.p - Q.x)) - 1.f) < cfg.uniqueness_threshold;
         }
         const unsigned b = (__ballot_sync(full, succ) & gmask) >> gbase;
@@ -412,8 +420,9 @@ cudaError_t ss_caster_launch(const DevScene &sc, const SolverCfg &cfg, int c, co
                              cudaStream_t s, const mlp::SeedProposal *prop, int trial_group, uint32_t treelet = 0) {
     const bool learned = kLearnedOk && prop && prop->shape == sc.casters_ss[c];
     // the trial kernel holds the top `treelet` node records in shared memory
+    // (plain and rough casters)
     DevScene st = sc;
-    st.n_tnodes = std::min<uint32_t>(treelet, sc.n_nodes);
+    st.n_tnodes = (kVar & 4) ? 0u : std::min<uint32_t>(treelet, sc.n_nodes);
     const size_t tsmem = (size_t)st.n_tnodes * 4 * sizeof(float4);
     const mlp::SeedProposal pr = learned ? *prop : mlp::SeedProposal{};
     phase_begin(tm, kPhaseSsFirst, s);
@@ -438,6 +447,12 @@ cudaError_t ss_caster_launch(const DevScene &sc, const SolverCfg &cfg, int c, co
         if (learned) {
             auto trials = group == 8 ? ss_trials_kernel<true, 8, kVar>
                           : group == 16 ? ss_trials_kernel<true, 16, kVar> : ss_trials_kernel<true, 32, kVar>;
+            if constexpr ((kVar & 4) == 0) {   // the treelet serves the plain and rough casters
+                if (st.n_tnodes)
+                    trials = group == 8 ? ss_trials_kernel<true, 8, kVar, true>
+                             : group == 16 ? ss_trials_kernel<true, 16, kVar, true>
+                                           : ss_trials_kernel<true, 32, kVar, true>;
+            }
             trials<<<num_sms * bps, 128, tsmem, s>>>(st, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr,
                                                      pr);
         }
@@ -445,6 +460,12 @@ cudaError_t ss_caster_launch(const DevScene &sc, const SolverCfg &cfg, int c, co
     if (!learned) {
         auto trials = group == 8 ? ss_trials_kernel<false, 8, kVar>
                       : group == 16 ? ss_trials_kernel<false, 16, kVar> : ss_trials_kernel<false, 32, kVar>;
+        if constexpr ((kVar & 4) == 0) {
+            if (st.n_tnodes)
+                trials = group == 8 ? ss_trials_kernel<false, 8, kVar, true>
+                         : group == 16 ? ss_trials_kernel<false, 16, kVar, true>
+                                       : ss_trials_kernel<false, 32, kVar, true>;
+        }
         trials<<<num_sms * bps, 128, tsmem, s>>>(st, cfg, c, q, n, seed, stream_off, value, count, walks, scr, ctr,
                                                  pr);
     }

@@ -98,11 +98,43 @@ def test_autotuner_picks_a_shape_and_keeps_results(sms, workloads, gpu_lib):
     ss = sms.SpecularManifoldSingleScatter(ctx)
     ref = ss.specular_manifold_sampling(W.water_queries(n), seed=4)
     r = autotune_ss(sms, ctx, q.data_ptr(), n, out.data_ptr(), cnt.data_ptr(), wlk.data_ptr(),
-                    blocks_per_sm=(2, 8), trial_groups=(8, 32), repeats=1)
+                    blocks_per_sm=(2, 8), trial_groups=(8, 32), treelets=(0, 128), chunks=(1, 4), repeats=1)
     print("autotune:", r)
-    assert r["best"] in {(2, 8), (2, 32), (8, 8), (8, 32)} and len(r["ms"]) == 4
+    assert r["best"][:2] in {(2, 8), (2, 32), (8, 8), (8, 32)} and r["best"][2] in (0, 128)
+    assert r["best"][3] in (1, 4) and len(r["ms"]) == 6
     assert all(t > 0 for t in r["ms"].values())
     again = ss.specular_manifold_sampling(W.water_queries(n), seed=4)
     for a, b in zip(ref, again):
         np.testing.assert_array_equal(a, b)
+    # every treelet size and queue chunk gives the same results
+    for t, ch in ((384, 1), (64, 3)):
+        ctx.set_treelet(t)
+        ctx.set_queue_chunk(ch)
+        again = ss.specular_manifold_sampling(W.water_queries(n), seed=4)
+        for a, b in zip(ref, again):
+            np.testing.assert_array_equal(a, b)
     ctx.close()
+
+
+def test_block_tuner_for_chains_and_glints_keeps_results(sms, workloads, gpu_lib):
+    import torch
+    from sms_gb300.autotune import autotune_blocks
+    W = workloads
+    for kind, desc, cfg, qh in (("ms", W.slab_scene(res=64), W.slab_config(), W.slab_queries(2048)),
+                                ("glints", W.glint_scene(map_res=256), W.glint_config(), W.glint_queries(64))):
+        ctx = sms.Context(sms.Scene(desc), cfg)
+        est = (sms.SpecularManifoldMultiScatter if kind == "ms" else sms.SpecularManifoldGlints)(ctx)
+        ref = est.specular_manifold_sampling(qh, seed=4)
+        n = qh.shape[1]
+        q = torch.from_numpy(qh).cuda()
+        bufs = [torch.zeros((3, n), device="cuda"), torch.zeros(n, dtype=torch.int32, device="cuda"),
+                torch.zeros(n, dtype=torch.int32, device="cuda")]
+        torch.cuda.synchronize()
+        r = autotune_blocks(sms, ctx, kind, q.data_ptr(), n, *(b.data_ptr() for b in bufs), blocks_per_sm=(2, 8),
+                            repeats=1)
+        print(kind, "blocks tuner:", r)
+        assert r["best"] in (2, 8) and all(t > 0 for t in r["ms"].values())
+        again = est.specular_manifold_sampling(qh, seed=4)
+        for a, b in zip(ref, again):
+            np.testing.assert_array_equal(a, b)
+        ctx.close()

@@ -280,7 +280,7 @@ def connect_timed(torch, sms, ctx, kind, q_dev, n, seed, stream_offset=0):
     return val, t.ms
 
 
-def secondary_configs(torch, sms, W, dev, only=None, calls=5, max_queries=None):
+def secondary_configs(torch, sms, W, dev, only=None, calls=5, max_queries=None, tune=True):
     """Throughput of the other solver configurations (one GPU): sphere
     (biased, 16 walks), two-bounce slab (biased, 32 walks, 512k queries) and
     glints (8192^2 FP16 slope map, 1024^2 pixels, 64 seeds, vectorized).
@@ -302,7 +302,7 @@ def secondary_configs(torch, sms, W, dev, only=None, calls=5, max_queries=None):
         q = torch.from_numpy(np.ascontiguousarray(qh, np.float32)).to(f"cuda:{dev}")
         n = q.shape[1]
         tuned = None
-        if kind in ("ms", "glints"):
+        if tune and kind in ("ms", "glints"):
             # blocks per SM of the persistent kernels, picked on the same queries
             from sms_gb300.autotune import autotune_blocks
             bufs = [torch.empty((3, n), dtype=torch.float32, device=f"cuda:{dev}"),
@@ -814,7 +814,8 @@ def main():
         from sms_gb300 import workloads as W
         mq = args.queries if args.queries != N_QUERIES else None
         print(json.dumps({"configs": secondary_configs(torch, sms, W, 0, only=args.secondary_only,
-                                                       calls=args.steps, max_queries=mq)}), flush=True)
+                                                       calls=args.steps, max_queries=mq,
+                                                       tune=not args.no_autotune)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -539,6 +539,12 @@ typedef struct sms_camera {
  * = the context's cfg.bounces). */
 #define SMS_INTEGRATOR_PATH_FILTERED_SS 4
 #define SMS_INTEGRATOR_PATH_FILTERED_MS 5
+/* The paper's combined integrator (src/integrators/path_sms_teaser.cpp:60-81,
+ * 120-320): single- and multi-scatter caustics at receivers with the
+ * context's config (the "caustics_*" block), biased glints at glinty shapes
+ * seen from the camera with options.glints (the "glints_*" block), and path
+ * tracing filtered to the paths SMS does not handle (non_sms_paths_enabled). */
+#define SMS_INTEGRATOR_PATH_SMS_TEASER 6
 typedef struct sms_render_options {
     int32_t  integrator;                 /* SMS_INTEGRATOR_*                        */
     int32_t  max_depth;                  /* -1 = unbounded                          */
@@ -559,6 +565,13 @@ typedef struct sms_render_options {
                                             of the passes done (integrator.cpp:36,
                                             143-146: the reference stops at the
                                             block, here at the pass) */
+    /* path_sms_teaser only (path_sms_teaser.cpp:60-81) */
+    int32_t  caustics_enabled;           /* true                                    */
+    int32_t  glints_enabled;             /* true                                    */
+    int32_t  non_sms_paths_enabled;      /* true                                    */
+    sms_config glints;                   /* glints_* (SMSConfig defaults); the
+                                            glints always run the biased estimator
+                                            (path_sms_teaser.cpp:347-350)          */
 } sms_render_options;
 void sms_render_options_default(sms_render_options *opt);
 

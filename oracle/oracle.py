@@ -53,11 +53,12 @@ class _RenderOptions(C.Structure):
                 ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
                 ("seed", C.c_uint64), ("max_paths", C.c_uint32),
                 ("glint_diff_scale_factor_clamp", C.c_float), ("samples_per_pass", C.c_uint32),
-                ("timeout", C.c_float)]
+                ("timeout", C.c_float), ("caustics_enabled", C.c_int32), ("glints_enabled", C.c_int32),
+                ("non_sms_paths_enabled", C.c_int32), ("glints", _Config)]
 
 
 _INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
-                "path_filtered_ms": 5}
+                "path_filtered_ms": 5, "path_sms_teaser": 6}
 _FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 
@@ -327,6 +328,15 @@ class OracleScene:
         o.disable_reflected_emitters = int(options.disable_reflected_emitters)
         o.biased_mnee, o.seed, o.max_paths = int(options.biased_mnee), options.seed, options.max_paths
         o.glint_diff_scale_factor_clamp = float(getattr(options, "glint_diff_scale_factor_clamp", 0.0))
+        o.caustics_enabled = int(getattr(options, "caustics_enabled", True))
+        o.glints_enabled = int(getattr(options, "glints_enabled", True))
+        o.non_sms_paths_enabled = int(getattr(options, "non_sms_paths_enabled", True))
+        gcfg = getattr(options, "glints", None)
+        if gcfg is not None:
+            o.glints = _cfg(gcfg)
+        else:   # SMSConfig defaults (manifold.h:11-45)
+            o.glints.step_scale, o.glints.max_iterations, o.glints.solver_threshold = 1.0, 20, 1e-5
+            o.glints.uniqueness_threshold, o.glints.max_trials, o.glints.bounces = 1e-4, -1, 2
         img = np.zeros((camera.height, camera.width, 3), np.float32)
         nt = nthreads or os.cpu_count() or 1
         self._lib.oracle_render(self._h, C.byref(_cfg(config)), C.byref(cam), C.byref(o), img.ctypes.data, nt)

@@ -2911,6 +2911,13 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
     V3 prev_p;
     const int integ = opt.integrator;
     const bool filtered_ss = integ == SMS_INTEGRATOR_PATH_FILTERED_SS, filtered_ms = integ == SMS_INTEGRATOR_PATH_FILTERED_MS;
+    /* path_sms_teaser (path_sms_teaser.cpp:120-320): caustics with cfg, glints
+       with opt.glints run biased (:347-350); its SMS calls draw from their own
+       state seeds: single scatter sms_seed(seed), multi scatter sms_seed(seed + 1),
+       glints sms_seed(seed + 2) */
+    const bool teaser = integ == SMS_INTEGRATOR_PATH_SMS_TEASER;
+    sms_config gcfg = opt.glints;
+    gcfg.biased = 1;
     const int bounces = (integ == SMS_INTEGRATOR_PATH_SMS_MS || filtered_ms) ? cfg.bounces : 1;
     /* PathRecord of path_filtered_ms.cpp:219-301 (state 0 default, 1 receiver,
        2 caster, 3 emitter; chain bounce count), after the camera ray */
@@ -2937,7 +2944,10 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         V3 wi(dot(wiw, fs), dot(wiw, ft), dot(wiw, n_sh));
         const bool receiver = (s.flags & SMS_SHAPE_CAUSTIC_RECEIVER) != 0;
         bool on_caster = false;
-        if (integ == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) != 0;
+        if (teaser)
+            on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI |
+                                    SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
+        else if (integ == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & SMS_SHAPE_CAUSTIC_CASTER_SINGLE) != 0;
         else if (integ == SMS_INTEGRATOR_PATH_SMS_MS || filtered_ms)
             on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
         else if (filtered_ss)
@@ -2952,8 +2962,9 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
            normalmap BSDF around its smooth conductor or dielectric */
         const bool nmapped = si.shape == sc.glinty_shape && sc.nmap.res > 0;
         const bool smooth = !nmapped && (diffuse || is_rough(s.bsdf));   /* BSDFFlags::Smooth */
-        const bool on_glinty = integ == SMS_INTEGRATOR_PATH_SMS_GLINTS && depth == 1 && nmapped &&
-                               (s.flags & SMS_SHAPE_GLINTY);
+        const bool on_glinty = (integ == SMS_INTEGRATOR_PATH_SMS_GLINTS || (teaser && opt.glints_enabled)) &&
+                               depth == 1 && nmapped && (s.flags & SMS_SHAPE_GLINTY);
+        const sms_config &glint_cfg = teaser ? gcfg : cfg;
         if (on_glinty) {
             /* SurfaceInteraction::compute_partials (interaction.h:216-248) */
             Float dn = dot(si.n, si.p);
@@ -2972,13 +2983,14 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             auto local = [&](V3 w) { return V3(dot(w, fs0), dot(w, ft0), dot(w, si.shn)); };
             const V3 wi_l = local(-ray.d);
             /* SMS strategy (manifold_glints.cpp:40-176) */
+            const uint64_t gseed = sms_seed(opt.seed + (teaser ? 2 : 0));
             PCG32 grng;
-            grng.seed(sms_seed(opt.seed), g + (1ull << 48));
+            grng.seed(gseed, g + (1ull << 48));
             int gc = 0, gw = 0;
-            V3 gv = glint_connect(sc, cfg, gq, grng, gc, gw, st);
+            V3 gv = glint_connect(sc, glint_cfg, gq, grng, gc, gw, st);
             if (gv.x != 0.f || gv.y != 0.f || gv.z != 0.f) {
                 PCG32 r2;
-                r2.seed(sms_seed(opt.seed), g + (1ull << 48));
+                r2.seed(gseed, g + (1ull << 48));
                 Query qq; qq.p = si.p;
                 EI ei = sample_emitter_interaction(sc, sc.emitters_all, qq, r2);
                 V3 ed = ei.p - si.p;
@@ -2988,7 +3000,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 if (!ei.is_point) p_sms = pt_emitter_pdf(sc, sc.shapes[sc.emitters[ei.emitter].shape], si.p, ei.p, ed, edist);
                 Float p_bsdf = glint_lean_pdf(sc.nmap, gq.uv, gq.duv_dx, gq.duv_dy, local(normalize(gq.sensor - si.p)),
                                               local(ed)) + 1.f;
-                Float mis = cfg.bsdf_strategy_only ? Float(0.f) : mis_weight(p_sms, p_bsdf);
+                Float mis = (cfg.bsdf_strategy_only && !teaser) ? Float(0.f) : mis_weight(p_sms, p_bsdf);
                 Float We = pt_importance(cam, tm, normalize(si.p - ray.o));
                 L += thr * gv * (mis * We);
             }
@@ -3008,14 +3020,32 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                     V3 Le = pt_emitted(sc, es, ep, br.d);
                     Float p_bsdf = glint_lean_pdf(sc.nmap, uvo, gq.duv_dx, gq.duv_dy, wi_l, local(bwo)) + 1.f;
                     Float p_sms = pt_emitter_pdf(sc, es, si.p, ep, bwo, sb.t);
-                    Float mis = cfg.sms_strategy_only ? Float(0.f) : mis_weight(p_bsdf, p_sms);
+                    Float mis = (cfg.sms_strategy_only && !teaser) ? Float(0.f) : mis_weight(p_bsdf, p_sms);
                     L += thr * Le * (mis * bw);
                 }
             }
         }
         V3 albedo(s.bsdf.albedo[0], s.bsdf.albedo[1], s.bsdf.albedo[2]);
+        /* the teaser's caustics at a receiver (path_sms_teaser.cpp:152-162):
+           single scatter if depth + 1 < max_depth, multi scatter if depth +
+           bounces < max_depth, both with cfg */
+        if (teaser && opt.caustics_enabled && receiver && diffuse) {
+            Query q;
+            q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
+            int c = 0, w = 0;
+            if (opt.max_depth < 0 || depth + 1 < opt.max_depth) {
+                PCG32 srng;
+                srng.seed(sms_seed(opt.seed), g + ((uint64_t)depth << 48));
+                L += thr * ss_connect(sc, cfg, q, srng, c, w, st);
+            }
+            if (opt.max_depth < 0 || depth + cfg.bounces < opt.max_depth) {
+                PCG32 srng;
+                srng.seed(sms_seed(opt.seed + 1), g + ((uint64_t)depth << 48));
+                L += thr * ms_connect(sc, cfg, q, srng, c, w, st);
+            }
+        }
         /* SMS at a receiver (path_sms_ss.cpp:115-121, path_sms_ms.cpp:226-232) */
-        if (integ != SMS_INTEGRATOR_PATH && !filtered_ss && !filtered_ms && receiver && !on_caster && diffuse &&
+        if (integ != SMS_INTEGRATOR_PATH && !teaser && !filtered_ss && !filtered_ms && receiver && !on_caster && diffuse &&
             (opt.max_depth < 0 || depth + bounces < opt.max_depth)) {
             Query q;
             q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
@@ -3029,6 +3059,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         /* emitter sampling */
         bool nee = smooth && !on_caster && !on_glinty;
         if (integ == SMS_INTEGRATOR_PATH_SMS_SS) nee = nee || (depth == 1 && !opt.disable_reflected_emitters);
+        if (teaser) nee = smooth && !on_caster && opt.non_sms_paths_enabled;   /* :185 */
         if (filtered_ss || filtered_ms) nee = smooth && (!on_caster || valid_conn);
         if (nee) {
             Float ex = rng.next_f32(), ey = rng.next_f32();
@@ -3117,6 +3148,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             if (integ == SMS_INTEGRATOR_PATH_SMS_SS) allow = !on_caster || (depth == 1 && !opt.disable_reflected_emitters);
             else if (integ == SMS_INTEGRATOR_PATH_SMS_MS) allow = !on_caster || spec_cam;
             else if (integ == SMS_INTEGRATOR_PATH_SMS_GLINTS) allow = !on_glinty;
+            else if (teaser) allow = !on_caster && opt.non_sms_paths_enabled && !on_glinty;   /* :276 */
             else if (filtered_ss)   /* path_filtered_ss.cpp:166-172 */
                 allow = !on_caster || (prev_receiver && (caustic_eta == 1.f ? !bs.transmit : bs.transmit)) || glint_case;
             else if (filtered_ms)   /* light_hit_valid (path_filtered_ms.cpp:191) */
@@ -3672,7 +3704,8 @@ int oracle_render(void *s, const sms_config *cfg, const sms_camera *cam, const s
                   float *image, int nthreads) {
     Scene *sc = as_scene(s);
     if (!sc->finalized) oracle_scene_finalize(s);
-    if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS) build_lean(sc->nmap);
+    if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS || (opt->integrator == SMS_INTEGRATOR_PATH_SMS_TEASER && opt->glints_enabled && sc->nmap.res > 0))
+        build_lean(sc->nmap);
     const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
     const double aspect = (double)cam->width / (double)cam->height;
     const double t = std::tan(0.5 * (double)cam->fov * 3.14159265358979323846 / 180.0);

@@ -51,7 +51,7 @@ PROPOSAL_OUTPUTS = 40
 PROPOSAL_PARAMS = 21808
 
 INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
-               "path_filtered_ms": 5}
+               "path_filtered_ms": 5, "path_sms_teaser": 6}
 FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device limit",
@@ -110,7 +110,8 @@ class _RenderOptions(C.Structure):
                 ("spp", C.c_int32), ("disable_reflected_emitters", C.c_int32), ("biased_mnee", C.c_int32),
                 ("seed", C.c_uint64), ("max_paths", C.c_uint32),
                 ("glint_diff_scale_factor_clamp", C.c_float), ("samples_per_pass", C.c_uint32),
-                ("timeout", C.c_float)]
+                ("timeout", C.c_float), ("caustics_enabled", C.c_int32), ("glints_enabled", C.c_int32),
+                ("non_sms_paths_enabled", C.c_int32), ("glints", _Config)]
 
 
 class _Profile(C.Structure):
@@ -631,7 +632,7 @@ class Camera:
 @dataclass
 class RenderOptions:
     """Integrator parameters: path, path_sms_ss, path_sms_ms, path_sms_glints,
-    path_filtered_ss or path_filtered_ms with the MonteCarloIntegrator fields
+    path_filtered_ss, path_filtered_ms or path_sms_teaser with the MonteCarloIntegrator fields
     (src/librender/integrator.cpp:300-320), the sampling integrator's passes,
     timeout and glint ray-differential clamp (:35-41) and the SMS integrators'
     switches (path_sms_ss.cpp:59-60)."""
@@ -646,6 +647,12 @@ class RenderOptions:
     glint_diff_scale_factor_clamp: float = 0.0
     samples_per_pass: int = 0         # 0 = spp (integrator.cpp:35)
     timeout: float = -1.0             # seconds, <= 0: none (integrator.cpp:36)
+    # path_sms_teaser (path_sms_teaser.cpp:60-81): the context's config is the
+    # caustics_* block, glints the glints_* block
+    caustics_enabled: bool = True
+    glints_enabled: bool = True
+    non_sms_paths_enabled: bool = True
+    glints: "SMSConfig | None" = None
 
     def to_c(self) -> _RenderOptions:
         o = _RenderOptions()
@@ -656,6 +663,9 @@ class RenderOptions:
         o.seed, o.max_paths = self.seed, self.max_paths
         o.glint_diff_scale_factor_clamp = self.glint_diff_scale_factor_clamp
         o.samples_per_pass, o.timeout = self.samples_per_pass, self.timeout
+        o.caustics_enabled, o.glints_enabled = int(self.caustics_enabled), int(self.glints_enabled)
+        o.non_sms_paths_enabled = int(self.non_sms_paths_enabled)
+        o.glints = (self.glints or SMSConfig()).to_c()
         return o
 
 

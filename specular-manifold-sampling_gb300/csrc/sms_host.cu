@@ -96,6 +96,11 @@ extern "C" sms_status sms_config_parse_xml(const char *xml, sms_config *cfg, cha
     sms_config c;
     sms_config_default(&c);
     if (type == "path_sms_ms" || type == "path_filtered_ms") c.bounces = 2;   // path_sms_ms.cpp:152, path_filtered_ms.cpp:58
+    // path_sms_teaser: the context config is its caustics_* block (bounces
+    // default 2, path_sms_teaser.cpp:60-70); glints_* and the switches are
+    // render options
+    const bool teaser = type == "path_sms_teaser";
+    if (teaser) c.bounces = 2;
     size_t end = s.find("</integrator>", ie);
     if (end == std::string::npos) end = s.size();
     size_t pos = ie + 1;
@@ -114,6 +119,10 @@ extern "C" sms_status sms_config_parse_xml(const char *xml, sms_config *cfg, cha
         std::string name, value;
         if (!attr(tag, "name", name) || !attr(tag, "value", value))
             return fail(SMS_ERR_PARSE, "parameter without name/value: " + tag);
+        if (teaser) {
+            if (name.compare(0, 9, "caustics_") != 0) continue;
+            name = name.substr(9);
+        }
         char *ep = nullptr;
         if (kind == "boolean") {
             bool ok;
@@ -984,6 +993,13 @@ extern "C" sms_status sms_ss_walk_batch(sms_ctx *c, int32_t caster, const float 
 }
 
 // ------------------------------------------------- accessors for other TUs
+bool ctx_swap_config(sms_ctx *c, const sms_config *in, sms_config *old) {
+    if (!c || !in || validate_cfg(in) != SMS_OK) return false;
+    if (old) *old = c->cfg;
+    c->cfg = *in;
+    return true;
+}
+
 bool ctx_view(sms_ctx *c, CtxView &out) {
     if (!c) return false;
     out.device = c->device;

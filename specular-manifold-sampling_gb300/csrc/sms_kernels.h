@@ -139,6 +139,9 @@ struct CtxView {
 // Context accessors implemented in sms_host.cu.
 struct sms_ctx;
 bool ctx_view(sms_ctx *c, sms::CtxView &out);
+// Replace the context's config by *in (validated), returning the old one in
+// *old when old is not null; false if *in is invalid.
+bool ctx_swap_config(sms_ctx *c, const sms_config *in, sms_config *old);
 // Connection entry points shared with the path tracer (sms_render.cu): as
 // sms_ss_connect_batch_device / sms_ms_connect_batch_device, with an optional
 // per-query stream table (SolverCfg::streams).

@@ -591,7 +591,7 @@ SMS_D float *ms_offset_rows(int *tmpl, uint32_t n) { return reinterpret_cast<flo
 // seed paths about them (:160, :372-375).
 template <int K, int G, bool kNM, bool kRough = false>
 #ifndef SMS_MS_BIASED_MIN_BLOCKS
-#define SMS_MS_BIASED_MIN_BLOCKS 4
+#define SMS_MS_BIASED_MIN_BLOCKS 8
 #endif
 __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kernel(DevScene sc, SolverCfg cfg, const float *__restrict__ qs,
                                                         uint32_t n, uint64_t seed, uint64_t stream_off,

@@ -79,6 +79,11 @@ struct PtParams {
     SolverCfg solver;     // for the MNEE check walk
     float diff_scale;     // ray-differential scale (glints)
     int bsdf_strategy_only, sms_strategy_only;
+    // path_sms_teaser: the pass being rendered (0 single-scatter caustics and
+    // the paths SMS does not handle, 1 multi-scatter caustics, 2 glints) and
+    // its switches
+    int teaser_pass;
+    int caustics_enabled, glints_enabled, non_sms_paths;
 };
 
 struct PtState {
@@ -471,7 +476,7 @@ SMS_D void store_rng(const PtState &S, uint32_t i, const Pcg32 &r) {
 // Perspective sensor (perspective.cpp sample_ray) through a box-filtered pixel
 // sample; first intersection and directly visible emitters.
 __global__ void __launch_bounds__(kPtBlock) pt_camera_kernel(DevScene sc, PtCam cam, PtState S, uint64_t base,
-                                                             uint32_t n, uint64_t seed) {
+                                                             uint32_t n, uint64_t seed, int add_emitted) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t g = base + i;
@@ -495,7 +500,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_camera_kernel(DevScene sc, PtCam 
     f3 L = splat(0.f);
     if (h.shape >= 0) {
         const DevShape &s = sc.shapes[h.shape];
-        if (s.emitter >= 0) L = emitted(sc, s, o + d * h.t, d);
+        if (s.emitter >= 0 && add_emitted) L = emitted(sc, s, o + d * h.t, d);
     }
     st3s(S.o, S.cap, i, o);
     st3s(S.d, S.cap, i, d);
@@ -568,8 +573,14 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             const f3 wiw = -d;
             const f3 wi = mk(dot(wiw, fs), dot(wiw, ft), dot(wiw, n_sh));
             const bool receiver = (s.flags & kShapeFlagReceiver) != 0;
+            const bool teaser = P.integrator == SMS_INTEGRATOR_PATH_SMS_TEASER;
+            // the teaser's passes trace the same paths (every draw below is
+            // made in each pass); only pass 0 adds the non-SMS contributions
+            const bool add_paths = !teaser || P.teaser_pass == 0;
             bool on_caster = false;
-            if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & kShapeFlagCasterSingle) != 0;
+            if (teaser)
+                on_caster = (s.flags & (kShapeFlagCasterSingle | kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
+            else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS) on_caster = (s.flags & kShapeFlagCasterSingle) != 0;
             else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS || P.integrator == SMS_INTEGRATOR_PATH_FILTERED_MS)
                 on_caster = (s.flags & (kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
             else if (P.integrator == SMS_INTEGRATOR_PATH_FILTERED_SS)
@@ -589,8 +600,9 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             // normalmap BSDF around its smooth conductor or dielectric
             const bool nmapped = shape == sc.glinty_shape && sc.nmap_res > 0;
             const bool smooth = !nmapped && (diffuse || s.alpha > 0.f);   // BSDFFlags::Smooth
-            const bool on_glinty = P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS && depth == 1 && nmapped &&
-                                   (s.flags & kShapeFlagGlinty);
+            const bool on_glinty = (P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS || (teaser && P.glints_enabled)) &&
+                                   depth == 1 && nmapped && (s.flags & kShapeFlagGlinty);
+            const bool glint_pass = !teaser || P.teaser_pass == 2;
             const f3 albedo = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
             if (on_glinty) {
                 // ray differentials of the camera ray (perspective.cpp:198-220),
@@ -614,9 +626,11 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                 const float row[kStageRows] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
                                                si.dp_du.x, si.dp_du.y, si.dp_du.z, si.dp_dv.x, si.dp_dv.y, si.dp_dv.z,
                                                si.u, si.v, dxu, dxv, dyu, dyv, o.x, o.y, o.z, thr.x, thr.y, thr.z};
-                #pragma unroll
-                for (int k = 0; k < kStageRows; ++k) S.stage[(size_t)k * S.cap + i] = row[k];
-                want = 1;
+                if (glint_pass) {
+                    #pragma unroll
+                    for (int k = 0; k < kStageRows; ++k) S.stage[(size_t)k * S.cap + i] = row[k];
+                    want = 1;
+                }
                 // BSDF strategy inside the footprint (manifold_glints.cpp:178-220)
                 const float fpx = rng.next_f32(), fpy = rng.next_f32();
                 (void)rng.next_f32(); (void)rng.next_f32(); (void)rng.next_f32();
@@ -635,13 +649,21 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                         const float p_bsdf = glint_lean_pdf(sc, uo, vo, dxu, dxv, dyu, dyv, wi, bwo_l) + 1.f;
                         const float p_sms = emitter_pdf(sc, es, si.p, ep, bwo, hb.t);
                         const float mis = P.sms_strategy_only ? 0.f : mis_weight(p_bsdf, p_sms);
-                        L = L + thr * Le * (mis * bw);
+                        if (glint_pass) L = L + thr * Le * (mis * bw);
                     }
                 }
             }
-            // ---- SMS query of a receiver vertex (solved after this launch)
-            if (P.integrator != SMS_INTEGRATOR_PATH && !filtered && receiver && !on_caster && diffuse &&
-                (P.max_depth < 0 || depth + P.bounces < P.max_depth)) {
+            // ---- SMS query of a receiver vertex (solved after this launch); the
+            // teaser's caustics (path_sms_teaser.cpp:152-162): single scatter
+            // if depth + 1 < max_depth (pass 0), multi scatter if depth +
+            // bounces < max_depth (pass 1)
+            const bool teaser_caustic =
+                teaser && P.caustics_enabled && receiver && diffuse &&
+                ((P.teaser_pass == 0 && (P.max_depth < 0 || depth + 1 < P.max_depth)) ||
+                 (P.teaser_pass == 1 && (P.max_depth < 0 || depth + P.bounces < P.max_depth)));
+            if (teaser_caustic ||
+                (!teaser && P.integrator != SMS_INTEGRATOR_PATH && !filtered && receiver && !on_caster && diffuse &&
+                 (P.max_depth < 0 || depth + P.bounces < P.max_depth))) {
                 const float row[SMS_QUERY_FIELDS] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
                                                      si.dp_du.x, si.dp_du.y, si.dp_du.z,
                                                      si.dp_dv.x, si.dp_dv.y, si.dp_dv.z,
@@ -657,6 +679,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             bool nee = smooth && !on_caster && !on_glinty;
             if (P.integrator == SMS_INTEGRATOR_PATH_SMS_SS)
                 nee = nee || (depth == 1 && !P.disable_reflected_emitters);
+            if (teaser) nee = smooth && !on_caster && P.non_sms_paths;   // path_sms_teaser.cpp:185
             if (filtered) nee = smooth && (!on_caster || valid_conn);
             if (nee) {
                 float ux = rng.next_f32(), uy = rng.next_f32();
@@ -677,7 +700,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                                 const bool refraction = wo.z * wi.z < 0.f;
                                 if (s.spec_eta == 1.f ? refraction : !refraction) w = 0.f;
                             }
-                            L = L + thr * bv * ds.spec * w;
+                            if (add_paths) L = L + thr * bv * ds.spec * w;
                         }
                     }
                 }
@@ -773,6 +796,8 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                         allow = !on_caster || (flags & kSpecularCamera);
                     else if (P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS)
                         allow = !on_glinty;
+                    else if (teaser)   // path_sms_teaser.cpp:276
+                        allow = !on_caster && P.non_sms_paths && !on_glinty;
                     else if (filtered_ss)   // path_filtered_ss.cpp:166-172
                         allow = !on_caster || ((flags & kPrevReceiver) && (s.spec_eta == 1.f ? !bs.transmit : bs.transmit)) ||
                                 glint_case;
@@ -780,7 +805,7 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                         allow = !on_caster || (rec == kRecEmitter && rec_b == P.bounces) || (flags & kSpecularCamera);
                     if (allow) {
                         float epdf = bs.delta ? 0.f : emitter_pdf(sc, es, si.p, ep, d2, h2.t);
-                        L = L + thr * Le * mis_weight(bs.pdf, epdf);
+                        if (add_paths) L = L + thr * Le * mis_weight(bs.pdf, epdf);
                     } else if (P.mnee_ms && rec == kRecEmitter && rec_b == P.bounces) {
                         // path_sms_ms.cpp:323-360: the MNEE test runs after this
                         // launch (ms_mnee_check_kernel); stage the light point and
@@ -998,6 +1023,8 @@ extern "C" void sms_render_options_default(sms_render_options *o) {
     o->max_depth = -1;
     o->rr_depth = 5;
     o->spp = 1;
+    o->caustics_enabled = o->glints_enabled = o->non_sms_paths_enabled = 1;
+    sms_config_default(&o->glints);
 }
 
 extern "C" uint64_t sms_render_sms_seed(uint64_t seed) {
@@ -1046,13 +1073,21 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
                                                          : std::min<uint32_t>(opt->samples_per_pass, (uint32_t)opt->spp);
     if ((uint32_t)opt->spp % spp_pass != 0)
         return rfail(SMS_ERR_INVALID_ARG, "sms_render: spp must be a multiple of samples_per_pass");
-    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_FILTERED_MS)
+    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_SMS_TEASER)
         return rfail(SMS_ERR_INVALID_ARG, "sms_render: unknown integrator");
-    const bool glints = opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS;
-    if (glints) {
+    const bool teaser = opt->integrator == SMS_INTEGRATOR_PATH_SMS_TEASER;
+    // the teaser's glints need a glinty shape with a slope map
+    const bool teaser_glints = teaser && opt->glints_enabled && v.scene->glinty_shape >= 0 && v.scene->nmap_res > 0;
+    bool glints = opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS;
+    if (glints || teaser_glints) {
         // the footprint MIS needs the LEAN pyramid of the slope map
         if (sms_status est = ctx_ensure_lean(c)) return est;
     }
+    if (teaser && opt->timeout > 0.f)
+        return rfail(SMS_ERR_UNSUPPORTED, "path_sms_teaser: a timeout is not supported (the image is rendered in "
+                                          "three passes over the same paths)");
+    if (teaser && opt->caustics_enabled && (v.bounces < 1 || v.bounces > kMaxBounces))
+        return rfail(SMS_ERR_UNSUPPORTED, "path_sms_teaser: caustics_bounces must be between 1 and 4");
     if (opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee &&
         v.solver.twostage)
         return rfail(SMS_ERR_UNSUPPORTED, "path_sms_ss: unbiased MNEE with the twostage solver is not supported");
@@ -1068,15 +1103,31 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     P.rr_depth = opt->rr_depth;
     P.disable_reflected_emitters = opt->disable_reflected_emitters;
     P.biased_mnee = opt->biased_mnee;
-    P.bounces = (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS || opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS)
+    P.bounces = (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS || opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS ||
+                 teaser)
                     ? v.bounces : 1;
     P.mnee_check = opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee;
     P.mnee_ms = opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee;
     P.seed = opt->seed;
     P.solver = v.solver;
     P.diff_scale = std::max(1.f / std::sqrt((float)opt->spp), opt->glint_diff_scale_factor_clamp);
-    P.bsdf_strategy_only = v.bsdf_strategy_only;
-    P.sms_strategy_only = v.sms_strategy_only;
+    P.bsdf_strategy_only = teaser ? 0 : v.bsdf_strategy_only;
+    P.sms_strategy_only = teaser ? 0 : v.sms_strategy_only;
+    P.caustics_enabled = opt->caustics_enabled;
+    P.glints_enabled = teaser_glints ? 1 : 0;
+    P.non_sms_paths = opt->non_sms_paths_enabled;
+    // the teaser's passes; -1: any other integrator (one pass)
+    std::vector<int> passes;
+    if (teaser) {
+        if (opt->caustics_enabled || opt->non_sms_paths_enabled) passes.push_back(0);
+        if (opt->caustics_enabled) passes.push_back(1);
+        if (teaser_glints) passes.push_back(2);
+        if (passes.empty()) passes.push_back(0);
+    } else {
+        passes.push_back(-1);
+    }
+    sms_config glint_cfg = opt->glints;
+    glint_cfg.biased = 1;   // path_sms_teaser.cpp:347-350
 
     const uint64_t wh = (uint64_t)cam->width * (uint64_t)cam->height;
     const uint64_t total = wh * (uint64_t)opt->spp;
@@ -1112,7 +1163,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     PtState S{};
     uint64_t g0 = 0;
     const size_t img_n = 3 * (size_t)wh;
-    const uint64_t sseed = sms_render_sms_seed(P.seed);
+    uint64_t sseed = sms_render_sms_seed(P.seed);
     std::vector<uint32_t> seg_base, seg_cnt;   // pending batch: one segment per bounce
     uint32_t pending = 0;
     // Solves the pending batch and adds it to the paths' radiance.
@@ -1122,10 +1173,20 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return rfail(SMS_ERR_CUDA, std::string("pt_pack_kernel: ") + cudaGetErrorString(e));
         sms_result r{S.value, S.count, S.walks};
-        sms_status fs = glints ? ctx_glint_connect(c, S.q, pending, sseed, 0, S.qstream, &r)
-                        : P.integrator == SMS_INTEGRATOR_PATH_SMS_MS
-                            ? ctx_ms_connect(c, S.q, pending, sseed, 0, S.qstream, &r)
-                            : ctx_ss_connect(c, S.q, pending, sseed, 0, S.qstream, &r);
+        sms_status fs;
+        if (glints && teaser) {
+            // the teaser's glints run with their own config
+            sms_config caustics_cfg;
+            if (!ctx_swap_config(c, &glint_cfg, &caustics_cfg))
+                return rfail(SMS_ERR_INVALID_ARG, "path_sms_teaser: invalid glints config");
+            fs = ctx_glint_connect(c, S.q, pending, sseed, 0, S.qstream, &r);
+            ctx_swap_config(c, &caustics_cfg, nullptr);
+        } else {
+            fs = glints ? ctx_glint_connect(c, S.q, pending, sseed, 0, S.qstream, &r)
+                 : (P.integrator == SMS_INTEGRATOR_PATH_SMS_MS || P.teaser_pass == 1)
+                     ? ctx_ms_connect(c, S.q, pending, sseed, 0, S.qstream, &r)
+                     : ctx_ss_connect(c, S.q, pending, sseed, 0, S.qstream, &r);
+        }
         if (fs) return fs;
         for (size_t k = 0; k < seg_base.size(); ++k) {
             const uint32_t g = (seg_cnt[k] + kPtBlock - 1) / kPtBlock;
@@ -1177,9 +1238,16 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     S.mnee_want = P.mnee_ms ? reinterpret_cast<int *>(blk + o_mw) : nullptr;
     S.cap = cap;
     S.qcap = qcap;
-    S.qrows = glints ? kQueryRowsMax : SMS_QUERY_FIELDS;
     PT_TRY(cudaMemsetAsync(image, 0, img_n * sizeof(float), s));
     ctx_set_render_spp(c, 0);
+    for (const int tp : passes) {
+    if (teaser) {
+        P.teaser_pass = tp;
+        glints = tp == 2;
+        sseed = sms_render_sms_seed(P.seed + (uint64_t)tp);
+        g0 = 0;
+    }
+    S.qrows = glints ? kQueryRowsMax : SMS_QUERY_FIELDS;
     t_start = std::chrono::steady_clock::now();
     while (g0 < total) {
         // timeout: stop at a pass boundary once the time is up
@@ -1191,7 +1259,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         else n = (uint32_t)std::min<uint64_t>(cap, wh - g0 % wh);
         n = (uint32_t)std::min<uint64_t>(n, pass - g0 % pass);
         const uint32_t nb = (n + kPtBlock - 1) / kPtBlock;
-        pt_camera_kernel<<<nb, kPtBlock, 0, s>>>(*v.scene, pc, S, g0, n, P.seed);
+        pt_camera_kernel<<<nb, kPtBlock, 0, s>>>(*v.scene, pc, S, g0, n, P.seed, teaser ? (tp == 0 ? 1 : 0) : 1);
         PT_TRY(cudaGetLastError());
         uint32_t alive_bound = n;   // paths that can stage a query at the next bounce
         for (int depth = 1;; ++depth) {
@@ -1239,6 +1307,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         }
         g0 += n;
     }
+    }   // passes
     {
         const uint32_t spp_done = (uint32_t)(g0 / wh);
         pt_scale_kernel<<<(unsigned)((img_n + 255) / 256), 256, 0, s>>>(image, img_n, 1.f / (float)spp_done);

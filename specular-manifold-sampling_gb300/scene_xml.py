@@ -34,10 +34,13 @@ load_render_setup reads the rendering side of the same file:
       <transform name="to_world"> (lookat / translate / scale / rotate / matrix),
       <film> width, height (hdrfilm defaults 768 x 576), <sampler> sample_count
       (independent sampler default 4)   (src/sensors/perspective.cpp)
-  <integrator type="path|path_sms_ss|path_sms_ms|path_filtered_ss|path_filtered_ms">  max_depth, rr_depth
+  <integrator type="path|path_sms_ss|path_sms_ms|path_sms_glints|path_filtered_ss|path_filtered_ms|
+                    path_sms_teaser">  max_depth, rr_depth
       (src/librender/integrator.cpp:300-320), samples_per_pass, timeout,
       glint_diff_scale_factor_clamp (:35-41), disable_reflected_emitters,
-      biased_mnee (path_sms_ss.cpp:59-60)
+      biased_mnee (path_sms_ss.cpp:59-60); path_sms_teaser's caustics_enabled,
+      glints_enabled, non_sms_paths_enabled and glints_* block
+      (path_sms_teaser.cpp:60-81; its caustics_* block is the SMSConfig)
 and returns (Camera, RenderOptions).
 """
 from __future__ import annotations
@@ -56,7 +59,8 @@ IOR = {"vacuum": 1.0, "helium": 1.000036, "hydrogen": 1.000132, "air": 1.000277,
        "amber": 1.55, "pet": 1.5750, "diamond": 2.419}
 
 _IGNORED = {"sensor", "film", "sampler", "default"}
-_INTEGRATOR_TYPES = {"path", "path_sms_ss", "path_sms_ms", "path_filtered_ss", "path_filtered_ms"}
+_INTEGRATOR_TYPES = {"path", "path_sms_ss", "path_sms_ms", "path_filtered_ss", "path_filtered_ms", "path_sms_glints",
+                     "path_sms_teaser"}
 
 
 def _props(el):
@@ -365,4 +369,17 @@ def load_render_setup(sms, path):
         opt.samples_per_pass = _int(ip, "samples_per_pass", 0)
         opt.timeout = _float(ip, "timeout", -1.0)
         opt.glint_diff_scale_factor_clamp = _float(ip, "glint_diff_scale_factor_clamp", 0.0)
+        if t == "path_sms_teaser":
+            # path_sms_teaser.cpp:60-81: the switches and the glints_* block
+            opt.caustics_enabled = _bool(ip, "caustics_enabled", True)
+            opt.glints_enabled = _bool(ip, "glints_enabled", True)
+            opt.non_sms_paths_enabled = _bool(ip, "non_sms_paths_enabled", True)
+            g = sms.SMSConfig()
+            g.biased = _bool(ip, "glints_biased")
+            g.step_scale = _float(ip, "glints_step_scale", 1.0)
+            g.max_iterations = _int(ip, "glints_max_iterations", 20)
+            g.solver_threshold = _float(ip, "glints_solver_threshold", 1e-5)
+            g.uniqueness_threshold = _float(ip, "glints_uniqueness_threshold", 1e-4)
+            g.max_trials = _int(ip, "glints_max_trials", -1)
+            opt.glints = g
     return cam, opt

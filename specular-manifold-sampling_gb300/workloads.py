@@ -221,6 +221,51 @@ def pool_camera(width: int = 64, height: int = 64, fov: float = 40.0):
     return Camera.look_at((0.0, -3.2, 3.6), (0.0, 0.0, 0.4), (0.0, 0.0, 1.0), fov, width, height)
 
 
+def teaser_scene(sphere_res: int = 24, map_res: int = 256) -> SceneDesc:
+    """A small stand-in for the combined integrator's scene (path_sms_teaser):
+    a diffuse floor z = 0 on [-2, 2]^2 (caustic_receiver), a mirror sphere r =
+    0.35 at (-0.7, 0, 0.8) (caustic_caster_single: a reflection caustic), a
+    glass sphere r = 0.4 at (0.6, 0, 0.9) tessellated to a mesh
+    (caustic_caster_multi: the two refractions of the multi-scatter chain), a
+    normal-mapped conductor tile z = 0.01 on [-1.5, 1.5] x [-1.9, -1.1] (glinty,
+    FP16 slope map map_res^2), and a point light at (0, 0.5, 4) flagged for both
+    caustic estimators."""
+    d = SceneDesc()
+    fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
+    fuv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    quad = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    d.add_mesh(fl, quad, Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.5, 0.5, 0.5)), SHAPE_CAUSTIC_RECEIVER, UV=fuv)
+    d.add_sphere((-0.7, 0.0, 0.8), 0.35, Bsdf(BSDF_CONDUCTOR, 0.2, 3.0), SHAPE_CAUSTIC_CASTER_SINGLE)
+    # glass sphere as a UV-sphere mesh with analytic normals
+    nt, nph = sphere_res, 2 * sphere_res
+    th = np.linspace(0.0, math.pi, nt + 1)
+    ph = np.linspace(0.0, 2.0 * math.pi, nph + 1)
+    T, PH = np.meshgrid(th, ph, indexing="ij")
+    nrm = np.stack([np.sin(T) * np.cos(PH), np.sin(T) * np.sin(PH), np.cos(T)], axis=-1).reshape(-1, 3)
+    P = (np.array([0.6, 0.0, 0.9]) + 0.4 * nrm).astype(np.float32)
+    UV = np.stack([PH / (2.0 * math.pi), T / math.pi], axis=-1).reshape(-1, 2).astype(np.float32)
+    F = []
+    for i in range(nt):
+        for j in range(nph):
+            a0, a1, b0, b1 = i * (nph + 1) + j, i * (nph + 1) + j + 1, (i + 1) * (nph + 1) + j, (i + 1) * (nph + 1) + j + 1
+            if i > 0:
+                F.append((a0, b0, a1))
+            if i < nt - 1:
+                F.append((a1, b0, b1))
+    d.add_mesh(P, np.array(F, np.uint32), Bsdf(BSDF_DIELECTRIC, 1.5), SHAPE_CAUSTIC_CASTER_MULTI,
+               N=nrm.astype(np.float32), UV=UV)
+    tile = np.array([[-1.5, -1.9, 0.01], [1.5, -1.9, 0.01], [1.5, -1.1, 0.01], [-1.5, -1.1, 0.01]], np.float32)
+    sid = d.add_mesh(tile, quad, Bsdf(BSDF_CONDUCTOR, 1.0, 6.0), SHAPE_GLINTY, UV=fuv)
+    d.normalmap = (sid, glint_slopes(map_res), 1.0)
+    d.add_point_emitter((0.0, 0.5, 4.0), (60.0, 60.0, 60.0), EMITTER_CAUSTIC_SINGLE | EMITTER_CAUSTIC_MULTI)
+    return d
+
+
+def teaser_camera(width: int = 32, height: int = 32, fov: float = 45.0):
+    from . import Camera
+    return Camera.look_at((0.0, -3.4, 2.6), (0.0, -0.3, 0.3), (0.0, 0.0, 1.0), fov, width, height)
+
+
 # ------------------------------------------------------------------- slab
 def slab_waves(seed: int, n_waves: int = 8):
     r = Pcg32(seed, 0)

@@ -169,6 +169,43 @@ def test_render_setup_from_xml(sms, workloads, tmp_path):
     assert (opt.timeout, opt.samples_per_pass) == (2.5, 4)
 
 
+TEASER_INTEGRATOR = """<integrator type="path_sms_teaser">
+    <integer name="max_depth" value="6"/>
+    <boolean name="caustics_biased" value="true"/>
+    <integer name="caustics_max_trials" value="24"/>
+    <integer name="caustics_bounces" value="3"/>
+    <float name="caustics_solver_threshold" value="2e-5"/>
+    <boolean name="glints_biased" value="false"/>
+    <integer name="glints_max_trials" value="48"/>
+    <integer name="glints_max_iterations" value="12"/>
+    <boolean name="non_sms_paths_enabled" value="false"/>
+    <boolean name="glints_enabled" value="false"/>
+  </integrator>"""
+
+
+def test_teaser_integrator_from_xml(sms, tmp_path):
+    """path_sms_teaser (path_sms_teaser.cpp:60-81): the caustics_* block is the
+    context's SMSConfig (bounces default 2), the glints_* block and the
+    switches are render options."""
+    path = tmp_path / "teaser.xml"
+    i0, i1 = RENDER_XML.index("<integrator"), RENDER_XML.index("</integrator>") + len("</integrator>")
+    path.write_text(RENDER_XML[:i0] + TEASER_INTEGRATOR + RENDER_XML[i1:])
+    _, cfg, kind = sms.load_scene(path)
+    assert kind == "path_sms_teaser"
+    assert cfg.biased and cfg.max_trials == 24 and cfg.bounces == 3 and abs(cfg.solver_threshold - 2e-5) < 1e-12
+    assert cfg.max_iterations == 20     # glints_max_iterations is not a caustics parameter
+    cam, opt = sms.load_render_setup(path)
+    assert opt.integrator == "path_sms_teaser" and opt.max_depth == 6
+    assert opt.caustics_enabled and not opt.glints_enabled and not opt.non_sms_paths_enabled
+    assert opt.glints.max_trials == 48 and opt.glints.max_iterations == 12 and not opt.glints.biased
+    c = opt.to_c()
+    assert c.integrator == 6 and c.glints.max_trials == 48 and c.non_sms_paths_enabled == 0
+    # defaults: bounces 2 for the caustics block
+    path.write_text(RENDER_XML[:i0] + '<integrator type="path_sms_teaser"/>' + RENDER_XML[i1:])
+    _, cfg, _ = sms.load_scene(path)
+    assert cfg.bounces == 2 and not cfg.biased and cfg.max_trials == -1
+
+
 def test_rough_bsdfs_from_xml(sms, tmp_path):
     body = """<scene version="2.0.0">
       <shape type="sphere"><float name="radius" value="1"/>

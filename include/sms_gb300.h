@@ -302,8 +302,8 @@ sms_status sms_ss_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
 
 /* Allocation-free variant of sms_ss_connect_batch_device.  No counterpart in
  * the reference: it exists for callers that must not allocate device memory
- * while rendering (work issued inside CUDA stream capture, fixed-budget
- * real-time loops, hosts that own every allocation).  It runs the same kernels
+ * while rendering (fixed-budget real-time loops, hosts that own every device
+ * allocation and forbid libraries from calling cudaMalloc).  It runs the same kernels
  * and gives bit-identical results, but takes the unbiased estimator's
  * per-query scratch from a fixed device array inside the library instead of
  * growing the context's scratch with cudaMalloc, and calls no allocating CUDA

@@ -1,9 +1,8 @@
 // sms_noalloc.cu -- allocation-free variant of the single-scatter connection call.
 //
-// Some callers cannot allocate device memory while they render: a host that
-// issues work from inside CUDA stream capture, a real-time loop with a fixed
-// memory budget, or an embedding that owns every allocation itself and forbids
-// libraries from calling cudaMalloc.  sms_ss_connect_batch_device may allocate:
+// Some callers cannot allocate device memory while they render: a real-time
+// loop with a fixed memory budget, or an embedding that owns every allocation
+// itself and forbids libraries from calling cudaMalloc.  sms_ss_connect_batch_device may allocate:
 // it grows the context's per-query scratch of the unbiased estimator on demand.
 // sms_ss_connect_batch_noalloc runs the same kernels, but takes that scratch
 // from the fixed device array below and makes no allocating call at all.

@@ -183,6 +183,17 @@ sms_status sms_scene_add_area_emitter(sms_scene *scene, int32_t shape_id,
 sms_status sms_scene_set_normalmap(sms_scene *scene, int32_t shape_id,
                                    const uint16_t *slopes, uint32_t res, float tiles);
 
+/* The normal map's LEAN fallback (NormalmapBSDF's lean_fallback,
+ * src/bsdfs/normalmap.cpp:46-55, 80-112, 142-170, 187-203): at path vertices
+ * without uv partials -- every vertex after the camera's first hit -- the
+ * normal-mapped shape reflects like the glossy LEAN distribution of the map's
+ * top mip level widened by the base roughness alpha (lean_fallback_alpha,
+ * 1e-4 in the reference), with the Fresnel factor of the IOR eta + i k
+ * (dielectric Fresnel when k = 0; the reference's defaults are eta 0, k 1).
+ * The surface then also takes emitter samples (the BSDF is glossy).  Call
+ * after sms_scene_set_normalmap. */
+sms_status sms_scene_set_lean_fallback(sms_scene *scene, float alpha, float eta, float k);
+
 /* --------------------------------------------------------------- context */
 typedef struct sms_ctx sms_ctx;   /* device copy of a scene + config + scratch */
 

@@ -97,6 +97,9 @@ def load(fma: bool = False, variant: str | None = None):
         "oracle_ms_walk_batch": (i32, [vp, C.POINTER(_Config), i32, vp, vp, u32, vp]),
         "oracle_ms_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
         "oracle_scene_set_normalmap": (i32, [vp, i32, vp, u32, f32]),
+        "oracle_scene_set_lean_fallback": (i32, [vp, f32, f32, f32]),
+        "oracle_lean_fb_eval": (i32, [vp, vp, vp, u32, vp]),
+        "oracle_lean_fb_sample": (i32, [vp, vp, vp, u32, vp]),
         "oracle_glint_walk_batch": (i32, [vp, C.POINTER(_Config), vp, vp, u32, vp]),
         "oracle_glint_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
         "oracle_nm_slope": (None, [vp, f32, f32, vp]),
@@ -206,7 +209,31 @@ class OracleScene:
             sl = np.ascontiguousarray(slopes, np.float16)
             self._keep.append(sl)
             lib.oracle_scene_set_normalmap(self._h, sid, sl.ctypes.data, sl.shape[0], tiles)
+            if getattr(desc, "lean_fallback", None) is not None:
+                a, e, k = desc.lean_fallback
+                if lib.oracle_scene_set_lean_fallback(self._h, float(a), float(e), float(k)) != 0:
+                    raise ValueError("lean fallback without a normal map")
         lib.oracle_scene_finalize(self._h)
+
+    def lean_fb_eval(self, wi: np.ndarray, wo: np.ndarray) -> np.ndarray:
+        """The normal map's LEAN fallback BSDF for local-frame pairs (3, n):
+        rows eval (BSDF x cos_o), pdf."""
+        a = np.ascontiguousarray(wi, np.float32)
+        b = np.ascontiguousarray(wo, np.float32)
+        out = np.zeros((2, a.shape[1]), np.float32)
+        if self._lib.oracle_lean_fb_eval(self._h, a.ctypes.data, b.ctypes.data, a.shape[1], out.ctypes.data) != 0:
+            raise ValueError("the scene has no LEAN fallback")
+        return out
+
+    def lean_fb_sample(self, wi: np.ndarray, u: np.ndarray) -> np.ndarray:
+        """Sampling of the LEAN fallback from local wi (3, n) with numbers u
+        (2, n): rows ok, wo (3), weight, pdf."""
+        a = np.ascontiguousarray(wi, np.float32)
+        uu = np.ascontiguousarray(u, np.float32)
+        out = np.zeros((6, a.shape[1]), np.float32)
+        if self._lib.oracle_lean_fb_sample(self._h, a.ctypes.data, uu.ctypes.data, a.shape[1], out.ctypes.data) != 0:
+            raise ValueError("the scene has no LEAN fallback")
+        return out
 
     def walk_batch(self, config, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:
         n = queries.shape[1]

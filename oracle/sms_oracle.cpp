@@ -209,11 +209,18 @@ struct NormalMap {
     std::vector<std::vector<Float>> lean;
 };
 
+/* The normal map's LEAN fallback BSDF (normalmap.cpp:46-55), off by default. */
+struct LeanFallback {
+    bool on = false;
+    Float alpha = 1e-4f, eta = 0.f, k = 1.f;
+};
+
 struct Scene {
     std::vector<Shape> shapes;
     std::vector<Emitter> emitters;
     std::vector<int> emitters_all;
     NormalMap nmap;
+    LeanFallback lean_fb;
     int glinty_shape = -1;
     /* triangle BVH over all mesh shapes: primitive = (shape, face) */
     std::vector<uint32_t> tri_shape, tri_face;
@@ -2811,6 +2818,96 @@ static Float glint_lean_pdf(const NormalMap &m, V2 uv, V2 duv_dx, V2 duv_dy, V3 
     return vndf / (4.f * dot(wi, h));
 }
 
+/* NormalmapBSDF's LEAN fallback (normalmap.cpp:80-112, 142-170, 187-203):
+ * the glossy LEAN distribution of the top pyramid level widened by the base
+ * roughness alpha, Fresnel of eta + i k (dielectric when k = 0).  Visible
+ * slopes by LEAN::sample_vndf (include/mitsuba/render/lean.h): qf2 inverts the
+ * standard distribution's visible-slope CDF by Newton steps kept inside a
+ * bisection bracket in the erf domain, qf1 = erfinv(2u - 1), then the
+ * Cholesky map to the surface's slope distribution. */
+static Float lean_qf2(Float u, Float ct, Float st) {
+    const Float kInvSqrtPi = 0.56418958354775628695f;
+    const Float cot = ct / st, tan_t = st / ct;
+    Float a = -1.f, c = std::erf(cot);
+    u = omax(u, Float(1e-6f));
+    const Float fit = 1.f + ct * (-0.876f + ct * (0.4265f - 0.0594f * ct));
+    Float b = c - (1.f + c) * std::pow(1.f - u, fit);
+    const Float norm_cdf = 1.f / (1.f + c + kInvSqrtPi * tan_t * std::exp(-cot * cot));
+    int it = 0;
+    while (++it < 10) {
+        if (!(b >= a && b <= c)) b = 0.5f * (a + c);
+        const Float ie = erfinv_f(b);
+        const Float value = norm_cdf * (1.f + b + kInvSqrtPi * tan_t * std::exp(-ie * ie)) - u;
+        const Float deriv = norm_cdf * (1.f - ie * tan_t);
+        if (std::fabs(value) < 1e-5f) break;
+        if (value > 0.f) c = b;
+        else a = b;
+        b -= value / deriv;
+    }
+    return erfinv_f(omax(Float(-0.9999f), b));
+}
+static V2 lean_sample_vp22_std(V3 wi, Float u0, Float u1) {
+    const Float ct = wi.z;
+    const Float st = ct < 1.f ? std::sqrt(1.f - ct * ct) : Float(0.f);
+    const Float tx = lean_qf2(u0, ct, st);
+    const Float ty = erfinv_f(2.f * u1 - 1.f);
+    if (st == 0.f) return V2{tx, ty};
+    const Float nrm = 1.f / std::sqrt(wi.x * wi.x + wi.y * wi.y);
+    const Float cp = wi.x * nrm, sp = wi.y * nrm;
+    return V2{cp * tx - sp * ty, sp * tx + cp * ty};
+}
+static V3 lean_sample_vndf(V3 wi, Float u0, Float u1, const LeanP &p) {
+    const Float a = wi.x * p.ax + wi.y * p.ay * p.rho, b = wi.y * p.ay * p.srho;
+    const Float c = wi.z - wi.x * p.tx - wi.y * p.ty;
+    const V3 ws = normalize(V3(a, b, c));
+    if (!(ws.z > 0.f)) return V3(0.f, 0.f, 1.f);
+    const V2 t = lean_sample_vp22_std(ws, u0, u1);
+    const Float txh = p.ax * t.x + p.tx;
+    const Float chol = p.rho * t.x + p.srho * t.y;
+    const Float tyh = p.ay * chol + p.ty;
+    return normalize(V3(-txh, -tyh, 1.f));
+}
+static Float lean_vndf(V3 h, V3 wi, const LeanP &p) {
+    const Float dp = dot(wi, h);
+    return dp > 0.f ? dp * lean_ndf(h, p) / lean_sigma(wi, p) : Float(0.f);
+}
+static Float lean_gaf(V3 a, V3 b, const LeanP &p) {   /* LEAN::gaf: the product of the two G1 */
+    const Float g = lean_g1(a, p) * lean_g1(b, p);
+    return g > 0.f ? g : Float(0.f);
+}
+static LeanP lean_fb_params(const NormalMap &m, const LeanFallback &f) {
+    V2 mu; Float sa, sb, sc;
+    lean_lookup(m, V2{0.f, 0.f}, (int)m.lean.size() - 1, mu, sa, sb, sc);
+    return lean_params(mu, sa, sb, sc, f.alpha);
+}
+static Float lean_fb_fresnel(const LeanFallback &f, Float c) {
+    return f.k == 0.f ? fresnel(c, f.eta) : fresnel_conductor(c, f.eta, f.k);
+}
+static bool lean_fb_sample(const NormalMap &m, const LeanFallback &f, V3 wi, Float u0, Float u1, V3 &wo,
+                           Float &weight, Float &pdf) {
+    if (!(wi.z > 0.f)) return false;
+    const LeanP p = lean_fb_params(m, f);
+    const V3 mm = lean_sample_vndf(wi, u0, u1, p);
+    const Float dm = dot(wi, mm);
+    wo = mm * (2.f * dm) - wi;
+    const Float G = lean_gaf(wo, wi, p);
+    if (!(G > 0.f && wo.z > 0.f)) return false;
+    pdf = lean_vndf(mm, wi, p) / (4.f * dm);
+    weight = lean_fb_fresnel(f, dm) * G / lean_g1(wi, p);
+    return true;
+}
+static Float lean_fb_eval(const NormalMap &m, const LeanFallback &f, V3 wi, V3 wo) {
+    if (!(wi.z > 0.f && wo.z > 0.f)) return 0.f;
+    const LeanP p = lean_fb_params(m, f);
+    const V3 h = normalize(wo + wi);
+    return lean_fb_fresnel(f, dot(wi, h)) * lean_ndf(h, p) * lean_gaf(wi, wo, p) / (4.f * wi.z);
+}
+static Float lean_fb_pdf(const NormalMap &m, const LeanFallback &f, V3 wi, V3 wo) {
+    const LeanP p = lean_fb_params(m, f);
+    const V3 h = normalize(wo + wi);
+    return lean_gaf(wo, wi, p) > 0.f ? lean_vndf(h, wi, p) / (4.f * dot(wi, h)) : Float(0.f);
+}
+
 /* NormalmapBSDF::frame (normalmap.cpp:236-257) at level 0: the base shading
  * frame (n, tangent from dp_du) tilted to the bilinear slope normal */
 static void nm_frame(const NormalMap &m, V3 n, V3 dp_du, V2 uv, V3 &pn, V3 &ps, V3 &pt) {
@@ -2961,7 +3058,12 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         /* the normal-mapped shape (glinty, or a caster / bouncer) carries the
            normalmap BSDF around its smooth conductor or dielectric */
         const bool nmapped = si.shape == sc.glinty_shape && sc.nmap.res > 0;
-        const bool smooth = !nmapped && (diffuse || is_rough(s.bsdf));   /* BSDFFlags::Smooth */
+        /* with the LEAN fallback the normalmap BSDF is also glossy; it takes
+           the fallback where the interaction has no uv partials, i.e. after
+           the camera's first hit (normalmap.cpp:80, 142, 187) */
+        const bool lean_fb = nmapped && sc.lean_fb.on;
+        const bool lean_now = lean_fb && depth > 1;
+        const bool smooth = (!nmapped && (diffuse || is_rough(s.bsdf))) || lean_fb;   /* BSDFFlags::Smooth */
         const bool on_glinty = (integ == SMS_INTEGRATOR_PATH_SMS_GLINTS || (teaser && opt.glints_enabled)) &&
                                depth == 1 && nmapped && (s.flags & SMS_SHAPE_GLINTY);
         const sms_config &glint_cfg = teaser ? gcfg : cfg;
@@ -3069,9 +3171,14 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 sr.mint = kRayEps * (1.f + hmax_abs(si.p)); sr.maxt = ds.dist * (1.f - kShadowEps);
                 if (!ray_test(sc, sr) && smooth) {
                     V3 wo(dot(ds.d, fs), dot(ds.d, ft), dot(ds.d, n_sh));
-                    V3 bv = pt_bsdf_eval(s.bsdf, wi, wo);
+                    /* with uv partials the normalmap BSDF evaluates its smooth
+                       nested BSDF: nothing */
+                    V3 bv = lean_now  ? V3(lean_fb_eval(sc.nmap, sc.lean_fb, wi, wo))
+                            : nmapped ? V3(0.f)
+                                      : pt_bsdf_eval(s.bsdf, wi, wo);
                     if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
-                        Float w = ds.delta ? Float(1.f) : mis_weight(ds.pdf, pt_bsdf_pdf(s.bsdf, wi, wo));
+                        const Float bp = lean_now ? lean_fb_pdf(sc.nmap, sc.lean_fb, wi, wo) : pt_bsdf_pdf(s.bsdf, wi, wo);
+                        Float w = ds.delta ? Float(1.f) : mis_weight(ds.pdf, bp);
                         /* path_filtered_ss.cpp:127-142 / path_filtered_ms.cpp:137-150 */
                         if (valid_conn && (filtered_ms || depth > 1)) {
                             const bool refraction = wo.z * wi.z < 0.f;
@@ -3085,7 +3192,18 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         /* BSDF sampling */
         Float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
         PtBsdf bs;
-        if (nmapped) {
+        if (lean_now) {
+            /* the LEAN fallback (normalmap.cpp:80-112): glossy reflection */
+            V3 lwo;
+            Float lw, lpdf;
+            if (!lean_fb_sample(sc.nmap, sc.lean_fb, wi, u2, u3, lwo, lw, lpdf)) break;
+            bs.wo = lwo;
+            bs.weight = V3(lw);
+            bs.pdf = lpdf;
+            bs.eta = 1.f;
+            bs.delta = false;
+            bs.transmit = false;
+        } else if (nmapped) {
             /* the normal-mapped BSDF at the hit's own uv */
             if (!nm_bsdf_sample(sc.nmap, s.bsdf, fs, ft, n_sh, si.dp_du, si.uv, wiw, u1, u2, u3, bs)) break;
         } else {
@@ -3632,6 +3750,47 @@ int oracle_scene_set_normalmap(void *s, int shape, const uint16_t *slopes_half, 
     const uint32_t chain = SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER;
     if (!(sc->shapes[shape].flags & chain)) sc->shapes[shape].flags |= SMS_SHAPE_GLINTY;
     else build_lean(sc->nmap);   /* the two-stage solver's smoothed frames read its top level */
+    return 0;
+}
+
+int oracle_scene_set_lean_fallback(void *s, float alpha, float eta, float k) {
+    Scene *sc = as_scene(s);
+    if (sc->nmap.res == 0) return -1;
+    sc->lean_fb.on = true;
+    sc->lean_fb.alpha = alpha;
+    sc->lean_fb.eta = eta;
+    sc->lean_fb.k = k;
+    build_lean(sc->nmap);
+    return 0;
+}
+
+/* The LEAN fallback BSDF of the scene's normal map, for n local-frame pairs
+ * (SoA, 3 x n each): out rows eval, pdf. */
+int oracle_lean_fb_eval(void *s, const float *wi, const float *wo, uint32_t n, float *out) {
+    Scene *sc = as_scene(s);
+    if (!sc->lean_fb.on) return -1;
+    for (uint32_t i = 0; i < n; ++i) {
+        const V3 a(wi[i], wi[n + i], wi[2 * n + i]), b(wo[i], wo[n + i], wo[2 * n + i]);
+        out[i] = (float)lean_fb_eval(sc->nmap, sc->lean_fb, a, b);
+        out[n + i] = (float)lean_fb_pdf(sc->nmap, sc->lean_fb, a, b);
+    }
+    return 0;
+}
+
+/* ... and its sampling from local wi (3 x n) with numbers u (2 x n): out rows
+ * ok, wo (3), weight, pdf. */
+int oracle_lean_fb_sample(void *s, const float *wi, const float *u, uint32_t n, float *out) {
+    Scene *sc = as_scene(s);
+    if (!sc->lean_fb.on) return -1;
+    for (uint32_t i = 0; i < n; ++i) {
+        const V3 a(wi[i], wi[n + i], wi[2 * n + i]);
+        V3 wo(0.f);
+        Float w = 0.f, pdf = 0.f;
+        const bool ok = lean_fb_sample(sc->nmap, sc->lean_fb, a, u[i], u[n + i], wo, w, pdf);
+        out[i] = ok ? 1.f : 0.f;
+        out[n + i] = (float)wo.x; out[2 * n + i] = (float)wo.y; out[3 * n + i] = (float)wo.z;
+        out[4 * n + i] = (float)w; out[5 * n + i] = (float)pdf;
+    }
     return 0;
 }
 

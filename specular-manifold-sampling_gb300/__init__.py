@@ -162,6 +162,7 @@ def load_library(path: str | os.PathLike | None = None):
         "sms_ms_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_ms_walk_batch": (i32, [vp, i32, vp, vp, u32, vp]),
         "sms_scene_set_normalmap": (i32, [vp, i32, vp, u32, f32]),
+        "sms_scene_set_lean_fallback": (i32, [vp, f32, f32, f32]),
         "sms_glint_connect_batch": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_glint_connect_batch_device": (i32, [vp, vp, u32, u64, u64, C.POINTER(_Result)]),
         "sms_glint_walk_batch": (i32, [vp, vp, vp, u32, vp]),
@@ -286,6 +287,7 @@ class SceneDesc:
     order: list = field(default_factory=list)     # ("sphere"|"mesh", index) in shape-id order
     point_emitters: list = field(default_factory=list)  # (pos, I, flags)
     normalmap: tuple | None = None   # (shape_id, (res, res, 2) float16 slopes, tiles)
+    lean_fallback: tuple | None = None   # the normal map's LEAN fallback BSDF: (alpha, eta, k)
     area_emitters: list = field(default_factory=list)   # (shape_id, L, flags)
 
     def add_sphere(self, center, radius, bsdf: Bsdf, flags: int = 0, flip: bool = False) -> int:
@@ -380,6 +382,9 @@ class Scene:
                 raise ValueError("slopes must have shape (res, res, 2)")
             self._keep.append(sl)
             _check(lib.sms_scene_set_normalmap(h, sid, _ptr(sl), sl.shape[0], float(tiles)))
+        if desc.lean_fallback is not None:
+            a, e, k = desc.lean_fallback
+            _check(lib.sms_scene_set_lean_fallback(h, float(a), float(e), float(k)))
 
     @property
     def handle(self):

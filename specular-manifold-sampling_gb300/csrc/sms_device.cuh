@@ -240,6 +240,11 @@ struct DevScene {
     const float *lean;
     uint32_t lean_off[kMaxLeanLevels];
     int lean_levels;
+    // the normal map's LEAN fallback BSDF (glossy reflection of the top LEAN
+    // level widened by lf_alpha, Fresnel of lf_eta + i lf_k) at vertices
+    // without uv partials; 0 = off
+    int lean_fb;
+    float lf_alpha, lf_eta, lf_k;
     const DevEmitter *emitters;
     // The first n_tnodes node records (the top levels of the tree: records are
     // stored breadth first) are also held in the launching kernel's dynamic

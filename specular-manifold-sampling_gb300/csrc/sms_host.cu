@@ -186,6 +186,9 @@ struct sms_scene {
     uint32_t nmap_res = 0;
     float nmap_tiles = 1.f;
     std::vector<uint16_t> nmap;   // res * res * 2 FP16 (sx, sy)
+    // the normal map's LEAN fallback BSDF (normalmap.cpp:46-55), off by default
+    bool lean_fb = false;
+    float lf_alpha = 1e-4f, lf_eta = 0.f, lf_k = 1.f;
 };
 
 extern "C" sms_status sms_scene_create(sms_scene **out) {
@@ -293,6 +296,21 @@ extern "C" sms_status sms_scene_set_normalmap(sms_scene *s, int32_t shape, const
     // keeps its role and its manifold vertices take the normal-mapped frame
     const uint32_t chain = SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER;
     if (!(s->shapes[shape].flags & chain)) s->shapes[shape].flags |= SMS_SHAPE_GLINTY;
+    return SMS_OK;
+}
+
+extern "C" sms_status sms_scene_set_lean_fallback(sms_scene *s, float alpha, float eta, float k) {
+    if (!s) return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_lean_fallback: null scene");
+    if (s->nmap_res == 0)
+        return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_lean_fallback: the scene has no normal map");
+    if (!(alpha >= 0.f && alpha < 1e3f) || !(eta >= 0.f && eta < 1e3f) || !(k >= 0.f && k < 1e3f))
+        return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_lean_fallback: alpha, eta and k must be finite and >= 0");
+    if (eta == 0.f && k == 0.f)
+        return fail(SMS_ERR_INVALID_ARG, "sms_scene_set_lean_fallback: eta and k cannot both be 0");
+    s->lean_fb = true;
+    s->lf_alpha = alpha;
+    s->lf_eta = eta;
+    s->lf_k = k;
     return SMS_OK;
 }
 
@@ -578,6 +596,10 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
     d.ms_rough = c->ms_rough ? 1 : 0;
     d.nmap_res = s->nmap_res;
     d.nmap_tiles = s->nmap_tiles;
+    d.lean_fb = s->lean_fb && s->nmap_res > 0 ? 1 : 0;
+    d.lf_alpha = s->lf_alpha;
+    d.lf_eta = s->lf_eta;
+    d.lf_k = s->lf_k;
     for (size_t i = 0; i < s->emitters.size(); ++i) {
         if (d.n_emitters_all >= kMaxEmitters) return fail(SMS_ERR_UNSUPPORTED, "too many emitters");
         d.emitters_all[d.n_emitters_all++] = (int)i;

@@ -120,6 +120,122 @@ SMS_D float glint_lean_pdf(const DevScene &sc, float u, float v, float dxu, floa
     return vndf / (4.f * dot(wi, h));
 }
 
+// ------------------------------------------------------- LEAN fallback BSDF
+// NormalmapBSDF with lean_fallback (src/bsdfs/normalmap.cpp:46-55, 80-112,
+// 142-170, 187-203): where the interaction has no uv partials -- every path
+// vertex after the camera's first hit -- the normal-mapped surface reflects
+// like the glossy LEAN/LEADR distribution of the map's top pyramid level (the
+// whole map's mean slope and covariance), widened by the base roughness
+// lean_fallback_alpha, times the Fresnel factor of (eta, k).  The visible-
+// slope sampling is LEAN::sample_vndf (include/mitsuba/render/lean.h): the
+// standard distribution's visible slopes by a Newton/bisection inversion of
+// their CDF in the erf domain (qf2) and an erfinv (qf1), then the Cholesky
+// map to the surface's slope distribution.
+
+constexpr float kInvSqrtPi = 0.56418958354775628695f;
+
+SMS_D float lean_qf2(float u, float ct, float st) {
+    const float cot = ct / st, tan_t = st / ct;
+    float a = -1.f, c = erff(cot);
+    u = fmaxf(u, 1e-6f);
+    // initial guess, then at most 9 Newton steps kept inside [a, c]
+    const float fit = 1.f + ct * (-0.876f + ct * (0.4265f - 0.0594f * ct));
+    float b = c - (1.f + c) * powf(1.f - u, fit);
+    const float norm_cdf = 1.f / (1.f + c + kInvSqrtPi * tan_t * expf(-cot * cot));
+    int it = 0;
+    while (++it < 10) {
+        if (!(b >= a && b <= c)) b = 0.5f * (a + c);
+        const float ie = erfinvf(b);
+        const float value = norm_cdf * (1.f + b + kInvSqrtPi * tan_t * expf(-ie * ie)) - u;
+        const float deriv = norm_cdf * (1.f - ie * tan_t);
+        if (fabsf(value) < 1e-5f) break;
+        if (value > 0.f) c = b;
+        else a = b;
+        b -= value / deriv;
+    }
+    return erfinvf(fmaxf(-0.9999f, b));
+}
+
+// A visible slope of the standard distribution for direction wi (z up).
+SMS_D float2 lean_sample_vp22_std(f3 wi, float u0, float u1) {
+    const float ct = wi.z;
+    const float st = ct < 1.f ? sqrtf(1.f - ct * ct) : 0.f;
+    const float tx = lean_qf2(u0, ct, st);
+    const float ty = erfinvf(2.f * u1 - 1.f);
+    if (st == 0.f) return make_float2(tx, ty);
+    const float nrm = 1.f / sqrtf(wi.x * wi.x + wi.y * wi.y);
+    const float cp = wi.x * nrm, sp = wi.y * nrm;
+    return make_float2(cp * tx - sp * ty, sp * tx + cp * ty);
+}
+
+// A visible microfacet normal of the LEAN distribution p for wi.
+SMS_D f3 lean_sample_vndf(f3 wi, float u0, float u1, const LeanP &p) {
+    const float a = wi.x * p.ax + wi.y * p.ay * p.rho, b = wi.y * p.ay * p.srho;
+    const float c = wi.z - wi.x * p.tx - wi.y * p.ty;
+    const f3 ws = normalize(mk(a, b, c));
+    if (!(ws.z > 0.f)) return mk(0.f, 0.f, 1.f);
+    const float2 t = lean_sample_vp22_std(ws, u0, u1);
+    const float txh = p.ax * t.x + p.tx;
+    const float chol = p.rho * t.x + p.srho * t.y;
+    const float tyh = p.ay * chol + p.ty;
+    return normalize(mk(-txh, -tyh, 1.f));
+}
+
+SMS_D float lean_vndf(f3 h, f3 wi, const LeanP &p) {
+    const float dp = dot(wi, h);
+    return dp > 0.f ? dp * lean_ndf(h, p) / lean_sigma(wi, p) : 0.f;
+}
+
+// LEAN::gaf as the reference computes it: the product of the two G1 (its
+// height-correlated form is unreachable code there).
+SMS_D float lean_gaf(f3 a, f3 b, const LeanP &p) {
+    const float g = lean_g1(a, p) * lean_g1(b, p);
+    return g > 0.f ? g : 0.f;
+}
+
+// The fallback's distribution: the top pyramid level and the base roughness.
+SMS_D LeanP lean_fb_params(const DevScene &sc) {
+    float mx, my, sa, sb, scv;
+    lean_lookup(sc, 0.f, 0.f, sc.lean_levels - 1, mx, my, sa, sb, scv);
+    return lean_params(mx, my, sa, sb, scv, sc.lf_alpha);
+}
+
+SMS_D float lean_fb_fresnel(const DevScene &sc, float c) {
+    return sc.lf_k == 0.f ? fresnel_dielectric(c, sc.lf_eta) : fresnel_conductor(c, sc.lf_eta, sc.lf_k);
+}
+
+// NormalmapBSDF::sample, lean_fallback branch (normalmap.cpp:80-112), local
+// shading frame: reflected direction, weight F G / G1 and the density.
+SMS_D bool lean_fb_sample(const DevScene &sc, f3 wi, float u0, float u1, f3 &wo, float &weight, float &pdf) {
+    if (!(wi.z > 0.f)) return false;
+    const LeanP p = lean_fb_params(sc);
+    const f3 m = lean_sample_vndf(wi, u0, u1, p);
+    const float dm = dot(wi, m);
+    wo = m * (2.f * dm) - wi;
+    const float G = lean_gaf(wo, wi, p);   // LEAN::gaf(m, wo, wi): G1 ignores m
+    if (!(G > 0.f && wo.z > 0.f)) return false;
+    const float F = lean_fb_fresnel(sc, dm);
+    pdf = lean_vndf(m, wi, p) / (4.f * dm);
+    weight = F * G / lean_g1(wi, p);
+    return true;
+}
+
+// NormalmapBSDF::eval, lean_fallback branch (normalmap.cpp:142-170).
+SMS_D float lean_fb_eval(const DevScene &sc, f3 wi, f3 wo) {
+    if (!(wi.z > 0.f && wo.z > 0.f)) return 0.f;
+    const LeanP p = lean_fb_params(sc);
+    const f3 h = normalize(wo + wi);
+    return lean_fb_fresnel(sc, dot(wi, h)) * lean_ndf(h, p) * lean_gaf(wi, wo, p) / (4.f * wi.z);
+}
+
+// NormalmapBSDF::pdf, lean_fallback branch (normalmap.cpp:187-203): the
+// reference returns the density wherever G > 0, whatever the cosines.
+SMS_D float lean_fb_pdf(const DevScene &sc, f3 wi, f3 wo) {
+    const LeanP p = lean_fb_params(sc);
+    const f3 h = normalize(wo + wi);
+    return lean_gaf(wo, wi, p) > 0.f ? lean_vndf(h, wi, p) / (4.f * dot(wi, h)) : 0.f;
+}
+
 // Normal-mapped smooth conductor: reflection about the bilinear slope normal
 // of level 0 at uv; world-space directions; weight = Fresnel.
 SMS_D bool nm_conductor_sample(const DevScene &sc, const DevShape &s, f3 n, f3 dp_du, float u, float v, f3 wi_w,

@@ -599,7 +599,12 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             // the normal-mapped shape (glinty, or a caster / bouncer) carries the
             // normalmap BSDF around its smooth conductor or dielectric
             const bool nmapped = shape == sc.glinty_shape && sc.nmap_res > 0;
-            const bool smooth = !nmapped && (diffuse || s.alpha > 0.f);   // BSDFFlags::Smooth
+            // with the LEAN fallback the normalmap BSDF is also glossy; it
+            // takes the fallback where the interaction has no uv partials,
+            // i.e. after the camera's first hit (normalmap.cpp:80, 142, 187)
+            const bool lean_fb = nmapped && sc.lean_fb;
+            const bool lean_now = lean_fb && depth > 1;
+            const bool smooth = (!nmapped && (diffuse || s.alpha > 0.f)) || lean_fb;   // BSDFFlags::Smooth
             const bool on_glinty = (P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS || (teaser && P.glints_enabled)) &&
                                    depth == 1 && nmapped && (s.flags & kShapeFlagGlinty);
             const bool glint_pass = !teaser || P.teaser_pass == 2;
@@ -690,9 +695,14 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                     bool occ = trace(sc, si.p, ds.d, mint, ds.dist * (1.f - kShadowEps), true, hs, err);
                     if (!occ && smooth) {
                         const f3 wo = mk(dot(ds.d, fs), dot(ds.d, ft), dot(ds.d, n_sh));
-                        const f3 bv = bsdf_eval(s, wi, wo);
+                        // the normalmap BSDF with uv partials evaluates its
+                        // smooth nested BSDF: nothing
+                        const f3 bv = lean_now  ? splat(lean_fb_eval(sc, wi, wo))
+                                      : nmapped ? splat(0.f)
+                                                : bsdf_eval(s, wi, wo);
                         if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
-                            float w = ds.delta ? 1.f : mis_weight(ds.pdf, bsdf_pdf(s, wi, wo));
+                            const float bp = lean_now ? lean_fb_pdf(sc, wi, wo) : bsdf_pdf(s, wi, wo);
+                            float w = ds.delta ? 1.f : mis_weight(ds.pdf, bp);
                             // a filtered caustic connection must scatter the way
                             // SMS solves it: reflection on conductors, refraction
                             // on dielectrics (path_filtered_ss.cpp:127-142)
@@ -709,7 +719,20 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             float u1 = rng.next_f32(), u2 = rng.next_f32(), u3 = rng.next_f32();
             BsdfSample bs;
             bool ok;
-            if (nmapped) {
+            if (lean_now) {
+                // the LEAN fallback (normalmap.cpp:80-112): glossy reflection
+                f3 lwo;
+                float lw, lpdf;
+                ok = lean_fb_sample(sc, wi, u2, u3, lwo, lw, lpdf);
+                if (ok) {
+                    bs.wo = lwo;
+                    bs.weight = splat(lw);
+                    bs.pdf = lpdf;
+                    bs.eta = 1.f;
+                    bs.delta = false;
+                    bs.transmit = false;
+                }
+            } else if (nmapped) {
                 // the normal-mapped BSDF at the hit's own uv
                 ok = nm_bsdf_sample(sc, s, fs, ft, n_sh, si.dp_du, si.u, si.v, wiw, u1, u2, u3, bs);
             } else {
@@ -1079,8 +1102,8 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     // the teaser's glints need a glinty shape with a slope map
     const bool teaser_glints = teaser && opt->glints_enabled && v.scene->glinty_shape >= 0 && v.scene->nmap_res > 0;
     bool glints = opt->integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS;
-    if (glints || teaser_glints) {
-        // the footprint MIS needs the LEAN pyramid of the slope map
+    if (glints || teaser_glints || v.scene->lean_fb) {
+        // the footprint MIS and the LEAN fallback BSDF read the LEAN pyramid
         if (sms_status est = ctx_ensure_lean(c)) return est;
     }
     if (teaser && opt->timeout > 0.f)

@@ -17,8 +17,9 @@ silently half-loaded):
       include/mitsuba/render/ior.h), conductor (eta, k), diffuse (reflectance),
       roughdielectric / roughconductor (isotropic Beckmann alpha),
       normalmap around any of these (filename of an OpenEXR or PNG RGB normal
-      map, tiles; src/bsdfs/normalmap.cpp:24-58; one normal-mapped shape per
-      scene); a top-level <bsdf id="..."> referenced by <ref id="..."/>;
+      map, tiles, lean_fallback with lean_fallback_alpha and grey eta / k;
+      src/bsdfs/normalmap.cpp:24-58; one normal-mapped shape per scene); a
+      top-level <bsdf id="..."> referenced by <ref id="..."/>;
       no bsdf -> diffuse (shape.cpp:73-74);
       nested <emitter type="area"> with radiance (spheres only)
   <emitter type="point">  position (point), intensity (spectrum / rgb / float)
@@ -169,8 +170,16 @@ def _bsdf_nm(sms, el, refs, base):
         p = _props(el)
         if not _bool(p, "use_slopes", True):
             raise ValueError("normalmap with use_slopes = false is not supported")
+        lean_fb = None
         if _bool(p, "lean_fallback"):
-            raise ValueError("normalmap lean_fallback is not supported")
+            # normalmap.cpp:46-55: base roughness and the fallback's complex IOR
+            mat = p.get("lean_fallback_material", (None, None))[1]
+            if mat is not None and mat.get("value", "none").lower() != "none":
+                raise ValueError("named lean_fallback_material is not supported; give eta and k")
+            eta, k = _spectrum(p, "eta", (0.0,) * 3), _spectrum(p, "k", (1.0,) * 3)
+            if len(set(eta)) != 1 or len(set(k)) != 1:
+                raise ValueError("lean_fallback: eta and k must be grey (one value)")
+            lean_fb = (_float(p, "lean_fallback_alpha", 0.0001), eta[0], k[0])
         if "filename" not in p:
             raise ValueError("normalmap without a filename")
         from .image_io import normalmap_slopes
@@ -180,7 +189,7 @@ def _bsdf_nm(sms, el, refs, base):
         b, nm = _bsdf_nm(sms, _deref(inner[0], refs), refs, base)
         if nm is not None:
             raise ValueError("nested normal maps are not supported")
-        return b, (normalmap_slopes(base / p["filename"][1].get("value")), _float(p, "tiles", 1.0))
+        return b, (normalmap_slopes(base / p["filename"][1].get("value")), _float(p, "tiles", 1.0), lean_fb)
     return _bsdf(sms, el, refs), None
 
 
@@ -316,6 +325,7 @@ def load_scene_xml(sms, path):
             if desc.normalmap is not None:
                 raise ValueError("more than one normal-mapped shape (one normal map per scene)")
             desc.normalmap = (sid, nm[0], nm[1])
+            desc.lean_fallback = nm[2]
         for em in (c for c in el if c.tag == "emitter"):
             if em.get("type") != "area":
                 raise ValueError("only area emitters may be nested in a shape")

@@ -428,6 +428,31 @@ def glint_queries(width: int = 1024, fov_deg: float = 30.0, diff_scale: float = 
     return q
 
 
+def lean_fallback_scene(map_res: int = 256, fallback=(0.05, 0.2, 3.0), radiance: float = 30.0) -> SceneDesc:
+    """The normal map's LEAN fallback BSDF at work: the normal-mapped conductor
+    plane of glint_scene (z = 0, [-0.5, 0.5]^2, map glint_slopes) with the
+    fallback (alpha, eta, k), a diffuse wall facing it (y = -0.6, normal +y),
+    and a sphere area light above.  Camera rays (lean_fallback_camera) hit the
+    wall first; paths that bounce from the wall to the plane meet it without
+    uv partials, where the plane reflects like its LEAN distribution."""
+    d = glint_scene(map_res=map_res, conductor=(0.2, 3.0))
+    d.point_emitters.clear()
+    d.lean_fallback = tuple(float(x) for x in fallback)
+    W = np.array([[-0.6, -0.6, 0.0], [0.6, -0.6, 0.0], [0.6, -0.6, 1.0], [-0.6, -0.6, 1.0]], np.float32)
+    F = np.array([[0, 2, 1], [0, 3, 2]], np.uint32)
+    UV = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    d.add_mesh(W, F, Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.6, 0.6, 0.6)), SHAPE_CAUSTIC_RECEIVER, UV=UV)
+    light = d.add_sphere((0.0, 0.6, 1.4), 0.25, Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+    d.add_area_emitter(light, (radiance,) * 3, EMITTER_CAUSTIC_SINGLE)
+    return d
+
+
+def lean_fallback_camera(width: int = 32, height: int = 32):
+    """Looks at the wall of lean_fallback_scene from in front of the plane."""
+    from . import Camera
+    return Camera.look_at((0.0, 1.2, 0.6), (0.0, -0.6, 0.4), (0.0, 0.0, 1.0), 45.0, width, height)
+
+
 def glint_render_camera(width: int = 64, height: int = 64, fov: float = 30.0):
     """The glint benchmark's camera (60 degrees from the normal, looking at the
     plane's centre) as a Camera for the path tracer."""

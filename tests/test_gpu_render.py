@@ -233,6 +233,28 @@ def test_glints_integrator_matches_oracle(sms, workloads, oracle, gpu_lib, biase
     assert abs(g.mean() - o.mean()) <= 3.0 * abs(f.mean() - o.mean()) + 0.02 * o.mean()
 
 
+@pytest.mark.parametrize("integrator", ["path", "path_sms_glints"])
+def test_lean_fallback_matches_oracle(sms, workloads, oracle, gpu_lib, integrator):
+    """The normal map's LEAN fallback BSDF (normalmap.cpp:80-112, 142-170,
+    187-203): paths that reach the normal-mapped plane after a bounce off the
+    diffuse wall reflect like the map's top LEAN level (emitter sampling with
+    the LEAN eval and density, BSDF sampling of visible normals); GPU vs the
+    oracle within the oracle-vs-FMA floor, and the fallback changes the
+    image."""
+    W = workloads
+    desc = W.lean_fallback_scene(map_res=256)
+    cfg = W.glint_config()
+    cam = W.lean_fallback_camera(24, 24)
+    opt = sms.RenderOptions(integrator=integrator, spp=8, seed=3)
+    g, o, f = _check_against_oracle(sms, oracle, desc, cfg, cam, opt)
+    assert abs(g.mean() - o.mean()) <= 3.0 * abs(f.mean() - o.mean()) + 0.01 * o.mean()
+    desc.lean_fallback = None
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    plain = ctx.render(cam, opt)
+    ctx.close()
+    assert abs(plain.mean() - g.mean()) > 0.005 * g.mean()
+
+
 @pytest.mark.parametrize("integrator", ["path_filtered_ss", "path_filtered_ms"])
 def test_filtered_integrators_match_oracle(sms, workloads, oracle, gpu_lib, integrator):
     """path_filtered_ss / path_filtered_ms (plain path tracing restricted to

@@ -222,6 +222,31 @@ def test_scene_xml_normalmap_bsdf(sms, io, oracle, tmp_path):
         sms.load_scene(tmp_path / "two.xml")
 
 
+def test_scene_xml_normalmap_lean_fallback(sms, io, oracle, tmp_path):
+    """lean_fallback, lean_fallback_alpha and the fallback's eta / k of a
+    normalmap BSDF (normalmap.cpp:46-55) reach the scene description; a named
+    lean_fallback_material is refused."""
+    (tmp_path / "textures").mkdir()
+    n, rgb = _normals_rgb(32)
+    _write_exr(tmp_path / "textures" / "n.exr",
+               {"R": (rgb[..., 0], 1), "G": (rgb[..., 1], 1), "B": (rgb[..., 2], 1)}, 3)
+    xml = NM_XML.replace('<float name="tiles" value="3"/>', '''<float name="tiles" value="3"/>
+    <boolean name="lean_fallback" value="true"/>
+    <float name="lean_fallback_alpha" value="0.02"/>
+    <float name="eta" value="0.2"/><float name="k" value="3"/>''')
+    (tmp_path / "s.xml").write_text(xml)
+    desc, _, _ = sms.load_scene(tmp_path / "s.xml")
+    assert desc.lean_fallback == (0.02, 0.2, 3.0)
+    oracle.OracleScene(desc)
+    sms.Scene(desc)
+    (tmp_path / "m.xml").write_text(NM_XML.replace('<float name="tiles" value="3"/>', '''<float name="tiles" value="3"/>
+    <boolean name="lean_fallback" value="true"/><string name="lean_fallback_material" value="Au"/>'''))
+    with pytest.raises(ValueError, match="lean_fallback_material"):
+        sms.load_scene(tmp_path / "m.xml")
+    (tmp_path / "d.xml").write_text(NM_XML)
+    assert sms.load_scene(tmp_path / "d.xml")[0].lean_fallback is None
+
+
 def test_exr_data_window_and_uint(io, tmp_path):
     """A data window that does not start at the origin (chunks addressed by
     their absolute first scanline) and UINT channels."""

@@ -77,7 +77,6 @@ constexpr int kMaxLeanLevels = 20;
 constexpr uint32_t kErrStackOverflow = 1u;
 constexpr uint32_t kErrTrialLimit = 2u;
 constexpr uint32_t kErrSolutionOverflow = 4u;
-constexpr uint32_t kErrTraversalLimit = 8u;
 
 // ------------------------------------------------------------------- vectors
 struct f3 { float x, y, z; };
@@ -374,10 +373,10 @@ SMS_HD bool trace(const DevScene &sc, f3 o, f3 d, float mint, float maxt, bool a
     int stack[kStackDepth];
     int sp = 0;
     int node = 0;
-    // Every node is visited at most once per ray in a well-formed tree.
-    uint32_t budget = sc.n_nodes + 1;
+    // The loop ends: the host accepts only trees whose inner children come
+    // after their parents (validate_bvh), and a node is reached only from its
+    // parent's single visit, so every node is visited at most once.
     while (true) {
-        if (budget-- == 0) { err |= kErrTraversalLimit; return false; }
         hit.nodes++;
         float4 n0, n1, n2;
         int4 n3;

@@ -744,7 +744,6 @@ sms_status ctx_check_device_error(sms_ctx *c) {
         if (err & kErrStackOverflow) m += " BVH traversal stack overflow;";
         if (err & kErrTrialLimit) m += " Bernoulli trials exceeded the hard limit;";
         if (err & kErrSolutionOverflow) m += " more unique solutions than the per-query capacity;";
-        if (err & kErrTraversalLimit) m += " BVH traversal step limit (malformed tree);";
         return fail(SMS_ERR_DEVICE_LIMIT, m);
     }
     return SMS_OK;

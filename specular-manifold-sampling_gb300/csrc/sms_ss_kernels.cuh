@@ -21,11 +21,12 @@
 namespace sms {
 
 // Resident blocks per SM the first-walk and trial kernels are compiled for
-// (128 threads each): 8 gives 64 registers per thread, the measured optimum of
+// (128 threads each): 9 gives 56 registers per thread, the measured optimum of
 // the latency-bound walks (the headline step at 4 / 6 / 7 / 8 / 10 blocks:
-// 62.4 / 53.3 / 50.6 / 49.7 / 57.8 ms).
+// 62.4 / 53.3 / 50.6 / 49.7 / 57.8 ms; with the current traversal loop 8 and
+// 9 blocks: 42.9 and 42.1 ms).
 #ifndef SMS_SS_WALK_MIN_BLOCKS
-#define SMS_SS_WALK_MIN_BLOCKS 8
+#define SMS_SS_WALK_MIN_BLOCKS 9
 #endif
 
 // ------------------------------------------------------ biased estimator

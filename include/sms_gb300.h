@@ -556,6 +556,15 @@ typedef struct sms_camera {
  * seen from the camera with options.glints (the "glints_*" block), and path
  * tracing filtered to the paths SMS does not handle (non_sms_paths_enabled). */
 #define SMS_INTEGRATOR_PATH_SMS_TEASER 6
+/* Its comparison integrator (src/integrators/path_filtered_teaser.cpp): path
+ * tracing restricted like path_sms_teaser's caustics -- on a caster, emitter
+ * samples and emitter hits count only when they complete the single-scatter
+ * chain (caster, then a caustic single-scatter emitter) or the multi-scatter
+ * chain of the context's cfg.bounces (multi_caustic_bounces) vertices, with
+ * the scattering SMS solves; elsewhere only with non_sms_paths_enabled.  As
+ * in the reference, an emitter hit completes either chain only when the
+ * emitter is flagged caustic_emitter_multi_scatter (:380-393).  No glints. */
+#define SMS_INTEGRATOR_PATH_FILTERED_TEASER 7
 typedef struct sms_render_options {
     int32_t  integrator;                 /* SMS_INTEGRATOR_*                        */
     int32_t  max_depth;                  /* -1 = unbounded                          */

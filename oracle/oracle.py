@@ -58,7 +58,7 @@ class _RenderOptions(C.Structure):
 
 
 _INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
-                "path_filtered_ms": 5, "path_sms_teaser": 6}
+                "path_filtered_ms": 5, "path_sms_teaser": 6, "path_filtered_teaser": 7}
 _FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 

@@ -2513,8 +2513,11 @@ struct PtDir { V3 d, spec; Float dist = 0.f, pdf = 0.f; bool delta = false; };
 
 /* Scene::sample_emitter_direction (scene.cpp:156-196), point.cpp and
  * area.cpp + Sphere::sample_direction (sphere.cpp) */
-static bool pt_sample_emitter(const Scene &sc, V3 x, Float ux, Float uy, PtDir &ds) {
-    const int ne = (int)sc.emitters_all.size();
+/* Scene::sample_emitter_direction over an emitter list (all emitters, or a
+ * caustic list as path_filtered_teaser.cpp:331-378 picks them) */
+static bool pt_sample_emitter_from(const Scene &sc, const std::vector<int> &list, V3 x, Float ux, Float uy,
+                                   PtDir &ds) {
+    const int ne = (int)list.size();
     if (ne == 0) return false;
     int idx = 0;
     if (ne > 1) {
@@ -2522,7 +2525,7 @@ static bool pt_sample_emitter(const Scene &sc, V3 x, Float ux, Float uy, PtDir &
         idx = (int)omin((uint32_t)(ux * (Float)ne), (uint32_t)ne - 1);
         ux = (ux - (Float)idx * epdf) * (Float)ne;
     }
-    const Emitter &e = sc.emitters[sc.emitters_all[idx]];
+    const Emitter &e = sc.emitters[list[idx]];
     if (e.kind == 0) {
         V3 d = e.p - x;
         ds.dist = norm(d);
@@ -2570,6 +2573,9 @@ static bool pt_sample_emitter(const Scene &sc, V3 x, Float ux, Float uy, PtDir &
     }
     if (ne > 1) { ds.pdf *= 1.f / (Float)ne; ds.spec = ds.spec * (Float)ne; }
     return ds.pdf != 0.f;
+}
+static bool pt_sample_emitter(const Scene &sc, V3 x, Float ux, Float uy, PtDir &ds) {
+    return pt_sample_emitter_from(sc, sc.emitters_all, x, ux, uy, ds);
 }
 
 /* warp.h:54-90 concentric disk, lifted to the cosine hemisphere (warp.h:332-340) */
@@ -3015,10 +3021,16 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
     const bool teaser = integ == SMS_INTEGRATOR_PATH_SMS_TEASER;
     sms_config gcfg = opt.glints;
     gcfg.biased = 1;
-    const int bounces = (integ == SMS_INTEGRATOR_PATH_SMS_MS || filtered_ms) ? cfg.bounces : 1;
+    const int bounces = (integ == SMS_INTEGRATOR_PATH_SMS_MS || filtered_ms || integ == SMS_INTEGRATOR_PATH_FILTERED_TEASER)
+                            ? cfg.bounces : 1;
     /* PathRecord of path_filtered_ms.cpp:219-301 (state 0 default, 1 receiver,
        2 caster, 3 emitter; chain bounce count), after the camera ray */
     int rec = (si.valid() && (sc.shapes[si.shape].flags & SMS_SHAPE_CAUSTIC_RECEIVER)) ? 1 : 0, rec_b = 0;
+    /* PathRecord of path_filtered_teaser.cpp:36-43, 334-410 (state 0 default,
+       1 receiver, 2 single caster, 3 single emitter, 4 multi caster, 5 multi
+       emitter; chain bounce count in rec_b), after the camera ray */
+    const bool filtered_teaser = integ == SMS_INTEGRATOR_PATH_FILTERED_TEASER;
+    int tf = rec == 1 ? 1 : 0;
     /* MNEEHelper of path_sms_ms.cpp:54-142 for unbiased MNEE: the same states
        in rec / rec_b, plus the receiver point and the specular vertices */
     const bool mnee_ms = integ == SMS_INTEGRATOR_PATH_SMS_MS && cfg.mnee_init && !opt.biased_mnee;
@@ -3049,6 +3061,9 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
         else if (filtered_ss)
             on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI)) != 0;
+        else if (filtered_teaser)
+            on_caster = (s.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI |
+                                    SMS_SHAPE_CAUSTIC_BOUNCER)) != 0;
         const bool glint_case = depth == 1 && !opt.disable_reflected_emitters;
         /* path_filtered_ss.cpp:109-110; light_connection_valid (path_filtered_ms.cpp:240-242) */
         const bool valid_conn = filtered_ss ? on_caster && (prev_receiver || glint_case)
@@ -3147,7 +3162,8 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             }
         }
         /* SMS at a receiver (path_sms_ss.cpp:115-121, path_sms_ms.cpp:226-232) */
-        if (integ != SMS_INTEGRATOR_PATH && !teaser && !filtered_ss && !filtered_ms && receiver && !on_caster && diffuse &&
+        if (integ != SMS_INTEGRATOR_PATH && !teaser && !filtered_ss && !filtered_ms && !filtered_teaser && receiver &&
+            !on_caster && diffuse &&
             (opt.max_depth < 0 || depth + bounces < opt.max_depth)) {
             Query q;
             q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
@@ -3163,10 +3179,20 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         if (integ == SMS_INTEGRATOR_PATH_SMS_SS) nee = nee || (depth == 1 && !opt.disable_reflected_emitters);
         if (teaser) nee = smooth && !on_caster && opt.non_sms_paths_enabled;   /* :185 */
         if (filtered_ss || filtered_ms) nee = smooth && (!on_caster || valid_conn);
+        if (filtered_teaser) nee = smooth;   /* path_filtered_teaser.cpp:108 */
         if (nee) {
             Float ex = rng.next_f32(), ey = rng.next_f32();
             PtDir ds;
-            if (pt_sample_emitter(sc, si.p, ex, ey, ds)) {
+            bool got;
+            if (filtered_teaser && on_caster) {
+                /* sample_filtered_emitter_direction (:331-378) */
+                const bool single_em = tf == 2 && rec_b == 1, multi_em = tf == 4 && rec_b == bounces;
+                got = (single_em || multi_em) &&
+                      pt_sample_emitter_from(sc, single_em ? sc.emitters_ss : sc.emitters_ms, si.p, ex, ey, ds);
+            } else {
+                got = pt_sample_emitter(sc, si.p, ex, ey, ds);
+            }
+            if (got) {
                 Ray sr; sr.o = si.p; sr.d = ds.d;
                 sr.mint = kRayEps * (1.f + hmax_abs(si.p)); sr.maxt = ds.dist * (1.f - kShadowEps);
                 if (!ray_test(sc, sr) && smooth) {
@@ -3183,6 +3209,12 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                         if (valid_conn && (filtered_ms || depth > 1)) {
                             const bool refraction = wo.z * wi.z < 0.f;
                             if (caustic_eta == 1.f ? refraction : !refraction) w = 0.f;
+                        }
+                        /* path_filtered_teaser.cpp:131-150 */
+                        if (filtered_teaser) {
+                            const bool refraction = wo.z * wi.z < 0.f;
+                            if (on_caster ? (caustic_eta == 1.f ? refraction : !refraction) : !opt.non_sms_paths_enabled)
+                                w = 0.f;
                         }
                         L += thr * bv * ds.spec * w;
                     }
@@ -3237,6 +3269,28 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 } else { rec = 0; rec_b = 0; }
             } else { rec = 0; rec_b = 0; }
         }
+        if (filtered_teaser) {
+            /* PathRecord::state_transition (path_filtered_teaser.cpp:334-410) */
+            const bool nv = si2.valid();
+            const uint32_t nf = nv ? sc.shapes[si2.shape].flags : 0u;
+            const int em = nv ? sc.shapes[si2.shape].emitter : -1;
+            auto in = [&](const std::vector<int> &l) { return em >= 0 && std::find(l.begin(), l.end(), em) != l.end(); };
+            const bool wrong = caustic_eta == 1.f ? bs.transmit : !bs.transmit;
+            if (nv && (nf & SMS_SHAPE_CAUSTIC_RECEIVER)) { tf = 1; rec_b = 0; }
+            else if (tf == 1) {
+                if (nv && (nf & SMS_SHAPE_CAUSTIC_CASTER_SINGLE)) { tf = 2; rec_b = 1; }
+                else if (nv && (nf & SMS_SHAPE_CAUSTIC_CASTER_MULTI)) { tf = 4; rec_b = 1; }
+                else { tf = 0; rec_b = 0; }
+            } else if (tf == 2) {
+                if (!wrong && rec_b == 1 && in(sc.emitters_ss)) tf = 3;
+                else { tf = 0; rec_b = 0; }
+            } else if (tf == 4) {
+                if (wrong) { tf = 0; rec_b = 0; }
+                else if (rec_b < bounces && nv && (nf & (SMS_SHAPE_CAUSTIC_CASTER_MULTI | SMS_SHAPE_CAUSTIC_BOUNCER))) rec_b++;
+                else if (rec_b == bounces && in(sc.emitters_ms)) tf = 5;
+                else { tf = 0; rec_b = 0; }
+            } else { tf = 0; rec_b = 0; }
+        }
         if (mnee_ms) {
             /* MNEEHelper::state_transition (path_sms_ms.cpp:84-140) */
             const bool nv = si2.valid();
@@ -3271,6 +3325,11 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                 allow = !on_caster || (prev_receiver && (caustic_eta == 1.f ? !bs.transmit : bs.transmit)) || glint_case;
             else if (filtered_ms)   /* light_hit_valid (path_filtered_ms.cpp:191) */
                 allow = !on_caster || (rec == 3 && rec_b == bounces) || spec_cam;
+            else if (filtered_teaser)   /* filtered_emitter_hit_valid (:380-393), :186-195 */
+                allow = on_caster ? (((tf == 3 && rec_b == 1) || (tf == 5 && rec_b == bounces)) &&
+                                     std::find(sc.emitters_ms.begin(), sc.emitters_ms.end(), es.emitter) !=
+                                         sc.emitters_ms.end())
+                                  : opt.non_sms_paths_enabled != 0;
             if (allow) {
                 Float epdf = bs.delta ? Float(0.f) : pt_emitter_pdf(sc, es, si.p, ep, nr.d, si2.t);
                 L += thr * Le * mis_weight(bs.pdf, epdf);

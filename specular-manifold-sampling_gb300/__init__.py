@@ -51,7 +51,7 @@ PROPOSAL_OUTPUTS = 40
 PROPOSAL_PARAMS = 21808
 
 INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
-               "path_filtered_ms": 5, "path_sms_teaser": 6}
+               "path_filtered_ms": 5, "path_sms_teaser": 6, "path_filtered_teaser": 7}
 FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
 
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device limit",
@@ -637,7 +637,8 @@ class Camera:
 @dataclass
 class RenderOptions:
     """Integrator parameters: path, path_sms_ss, path_sms_ms, path_sms_glints,
-    path_filtered_ss, path_filtered_ms or path_sms_teaser with the MonteCarloIntegrator fields
+    path_filtered_ss, path_filtered_ms, path_sms_teaser or path_filtered_teaser
+    with the MonteCarloIntegrator fields
     (src/librender/integrator.cpp:300-320), the sampling integrator's passes,
     timeout and glint ray-differential clamp (:35-41) and the SMS integrators'
     switches (path_sms_ss.cpp:59-60)."""

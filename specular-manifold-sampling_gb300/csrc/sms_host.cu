@@ -101,6 +101,10 @@ extern "C" sms_status sms_config_parse_xml(const char *xml, sms_config *cfg, cha
     // render options
     const bool teaser = type == "path_sms_teaser";
     if (teaser) c.bounces = 2;
+    // path_filtered_teaser: multi_caustic_bounces (default 2,
+    // path_filtered_teaser.cpp:46) is the chain length of its filter
+    const bool filtered_teaser = type == "path_filtered_teaser";
+    if (filtered_teaser) c.bounces = 2;
     size_t end = s.find("</integrator>", ie);
     if (end == std::string::npos) end = s.size();
     size_t pos = ie + 1;
@@ -142,6 +146,7 @@ extern "C" sms_status sms_config_parse_xml(const char *xml, sms_config *cfg, cha
             if (name == "max_iterations") c.max_iterations = (int32_t)v;
             else if (name == "max_trials") c.max_trials = (int32_t)v;
             else if (name == "bounces") c.bounces = (int32_t)v;
+            else if (filtered_teaser && name == "multi_caustic_bounces") c.bounces = (int32_t)v;
         } else {
             float v = std::strtof(value.c_str(), &ep);
             if (ep == value.c_str() || *ep) return fail(SMS_ERR_PARSE, "bad float for " + name);

@@ -57,6 +57,11 @@ constexpr int kStageRows = 24;            // query rows, then 3 throughput rows 
 constexpr int kAlive = 1, kPrevReceiver = 2, kSpecularCamera = 4;
 constexpr int kRecShift = 3, kRecBounceShift = 5;
 constexpr int kRecDefault = 0, kRecReceiver = 1, kRecCaster = 2, kRecEmitter = 3;
+// path_filtered_teaser's path record (path_filtered_teaser.cpp:36-43,
+// 334-410): its state in bits 8-10, its chain bounce count in bits 5-7
+constexpr int kTfShift = 8;
+constexpr int kTfDefault = 0, kTfReceiver = 1, kTfSingleCaster = 2, kTfSingleEmitter = 3, kTfMultiCaster = 4,
+              kTfMultiEmitter = 5;
 // rows of the MNEE record: receiver point (3), first specular shape (int
 // bits), specular vertices (3 per bounce)
 constexpr int kMneeRows = 4 + 3 * kMaxBounces;
@@ -192,12 +197,13 @@ struct DirSample {
     bool delta;
 };
 
-// Scene::sample_emitter_direction over all emitters (scene.cpp:156-196):
-// point.cpp sample_direction; area.cpp + Sphere::sample_direction (cone
-// sampling from outside, uniform sphere from inside).  Visibility is tested
-// by the caller.
-SMS_D bool sample_emitter_direction(const DevScene &sc, f3 x, float ux, float uy, DirSample &ds) {
-    const int ne = sc.n_emitters_all;
+// Scene::sample_emitter_direction over an emitter list (scene.cpp:156-196;
+// all emitters, or a caustic list as path_filtered_teaser.cpp:331-378 picks
+// them): point.cpp sample_direction; area.cpp + Sphere::sample_direction
+// (cone sampling from outside, uniform sphere from inside).  Visibility is
+// tested by the caller.
+SMS_D bool sample_emitter_direction_from(const DevScene &sc, const int *list, int ne, f3 x, float ux, float uy,
+                                         DirSample &ds) {
     if (ne == 0) return false;
     int idx = 0;
     if (ne > 1) {
@@ -205,7 +211,7 @@ SMS_D bool sample_emitter_direction(const DevScene &sc, f3 x, float ux, float uy
         idx = (int)min((uint32_t)(ux * (float)ne), (uint32_t)ne - 1);
         ux = (ux - (float)idx * epdf) * (float)ne;
     }
-    const DevEmitter &e = sc.emitters[sc.emitters_all[idx]];
+    const DevEmitter &e = sc.emitters[list[idx]];
     if (e.kind == 0) {
         f3 d = mk(e.px, e.py, e.pz) - x;
         ds.dist = length(d);
@@ -267,6 +273,10 @@ SMS_D bool sample_emitter_direction(const DevScene &sc, f3 x, float ux, float uy
         ds.spec = ds.spec * (float)ne;
     }
     return ds.pdf != 0.f;
+}
+
+SMS_D bool sample_emitter_direction(const DevScene &sc, f3 x, float ux, float uy, DirSample &ds) {
+    return sample_emitter_direction_from(sc, sc.emitters_all, sc.n_emitters_all, x, ux, uy, ds);
 }
 
 // Fresnel equations for a dielectric (fresnel.h:34-80): reflectance, signed
@@ -513,7 +523,8 @@ __global__ void __launch_bounds__(kPtBlock) pt_camera_kernel(DevScene sc, PtCam 
     // (state_transition(si, si, ...) of path_filtered_ms.cpp:79)
     const int rec = (h.shape >= 0 && (sc.shapes[h.shape].flags & kShapeFlagReceiver)) ? kRecReceiver : kRecDefault;
     if (S.mnee && rec == kRecReceiver) st3s(S.mnee, S.cap, i, o + d * h.t);
-    S.flags[i] = (h.shape >= 0 ? kAlive : 0) | kSpecularCamera | (rec << kRecShift);
+    const int tf = rec == kRecReceiver ? kTfReceiver : kTfDefault;
+    S.flags[i] = (h.shape >= 0 ? kAlive : 0) | kSpecularCamera | (rec << kRecShift) | (tf << kTfShift);
     S.cam_s[i] = sx;
     S.cam_s[(size_t)S.cap + i] = sy;
     store_rng(S, i, rng);
@@ -585,6 +596,10 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                 on_caster = (s.flags & (kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
             else if (P.integrator == SMS_INTEGRATOR_PATH_FILTERED_SS)
                 on_caster = (s.flags & (kShapeFlagCasterSingle | kShapeFlagCasterMulti)) != 0;
+            const bool filtered_teaser = P.integrator == SMS_INTEGRATOR_PATH_FILTERED_TEASER;
+            if (filtered_teaser)
+                on_caster = (s.flags & (kShapeFlagCasterSingle | kShapeFlagCasterMulti | kShapeFlagBouncer)) != 0;
+            int tf = (flags >> kTfShift) & 7;
             const bool filtered_ss = P.integrator == SMS_INTEGRATOR_PATH_FILTERED_SS;
             const bool filtered_ms = P.integrator == SMS_INTEGRATOR_PATH_FILTERED_MS;
             const bool filtered = filtered_ss || filtered_ms;
@@ -667,7 +682,8 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                 ((P.teaser_pass == 0 && (P.max_depth < 0 || depth + 1 < P.max_depth)) ||
                  (P.teaser_pass == 1 && (P.max_depth < 0 || depth + P.bounces < P.max_depth)));
             if (teaser_caustic ||
-                (!teaser && P.integrator != SMS_INTEGRATOR_PATH && !filtered && receiver && !on_caster && diffuse &&
+                (!teaser && P.integrator != SMS_INTEGRATOR_PATH && !filtered && !filtered_teaser && receiver &&
+                 !on_caster && diffuse &&
                  (P.max_depth < 0 || depth + P.bounces < P.max_depth))) {
                 const float row[SMS_QUERY_FIELDS] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
                                                      si.dp_du.x, si.dp_du.y, si.dp_du.z,
@@ -686,10 +702,24 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                 nee = nee || (depth == 1 && !P.disable_reflected_emitters);
             if (teaser) nee = smooth && !on_caster && P.non_sms_paths;   // path_sms_teaser.cpp:185
             if (filtered) nee = smooth && (!on_caster || valid_conn);
+            if (filtered_teaser) nee = smooth;   // path_filtered_teaser.cpp:108
             if (nee) {
                 float ux = rng.next_f32(), uy = rng.next_f32();
                 DirSample ds;
-                if (sample_emitter_direction(sc, si.p, ux, uy, ds)) {
+                bool got;
+                if (filtered_teaser && on_caster) {
+                    // sample_filtered_emitter_direction (:331-378): only the
+                    // caustic emitters that end the caster's chain here
+                    const bool single_em = tf == kTfSingleCaster && rec_b == 1;
+                    const bool multi_em = tf == kTfMultiCaster && rec_b == P.bounces;
+                    got = (single_em || multi_em) &&
+                          sample_emitter_direction_from(sc, single_em ? sc.emitters_ss : sc.emitters_ms,
+                                                        single_em ? sc.n_emitters_ss : sc.n_emitters_ms, si.p, ux,
+                                                        uy, ds);
+                } else {
+                    got = sample_emitter_direction(sc, si.p, ux, uy, ds);
+                }
+                if (got) {
                     Hit hs;
                     float mint = kRayEps * (1.f + max_abs(si.p));
                     bool occ = trace(sc, si.p, ds.d, mint, ds.dist * (1.f - kShadowEps), true, hs, err);
@@ -709,6 +739,14 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                             if (valid_conn && (filtered_ms || depth > 1)) {
                                 const bool refraction = wo.z * wi.z < 0.f;
                                 if (s.spec_eta == 1.f ? refraction : !refraction) w = 0.f;
+                            }
+                            // path_filtered_teaser.cpp:131-150: on a caster only
+                            // the scattering SMS solves, elsewhere only with
+                            // the non-SMS paths
+                            if (filtered_teaser) {
+                                const bool refraction = wo.z * wi.z < 0.f;
+                                if (on_caster ? (s.spec_eta == 1.f ? refraction : !refraction) : !P.non_sms_paths)
+                                    w = 0.f;
                             }
                             if (add_paths) L = L + thr * bv * ds.spec * w;
                         }
@@ -775,6 +813,34 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                     }
                     flags = (flags & ~(0x1F << kRecShift)) | (rec << kRecShift) | (rec_b << kRecBounceShift);
                 }
+                if (filtered_teaser) {
+                    // PathRecord::state_transition (path_filtered_teaser.cpp:334-410)
+                    const bool nv = h2.shape >= 0;
+                    const uint32_t nf = nv ? sc.shapes[h2.shape].flags : 0u;
+                    const int em = nv ? sc.shapes[h2.shape].emitter : -1;
+                    // the scattering SMS solves: reflection off a conductor,
+                    // refraction through a dielectric
+                    const bool wrong = s.spec_eta == 1.f ? bs.transmit : !bs.transmit;
+                    if (nv && (nf & kShapeFlagReceiver)) {
+                        tf = kTfReceiver; rec_b = 0;
+                    } else if (tf == kTfReceiver) {
+                        if (nv && (nf & kShapeFlagCasterSingle)) { tf = kTfSingleCaster; rec_b = 1; }
+                        else if (nv && (nf & kShapeFlagCasterMulti)) { tf = kTfMultiCaster; rec_b = 1; }
+                        else { tf = kTfDefault; rec_b = 0; }
+                    } else if (tf == kTfSingleCaster) {
+                        if (!wrong && rec_b == 1 && em >= 0 && emitter_is_caustic_ss(sc, em)) tf = kTfSingleEmitter;
+                        else { tf = kTfDefault; rec_b = 0; }
+                    } else if (tf == kTfMultiCaster) {
+                        if (wrong) { tf = kTfDefault; rec_b = 0; }
+                        else if (rec_b < P.bounces && nv && (nf & (kShapeFlagCasterMulti | kShapeFlagBouncer))) rec_b++;
+                        else if (rec_b == P.bounces && em >= 0 && emitter_is_caustic_ms(sc, em)) tf = kTfMultiEmitter;
+                        else { tf = kTfDefault; rec_b = 0; }
+                    } else {
+                        tf = kTfDefault; rec_b = 0;
+                    }
+                    flags = (flags & ~((7 << kTfShift) | (7 << kRecBounceShift))) | (tf << kTfShift) |
+                            (rec_b << kRecBounceShift);
+                }
                 if (P.mnee_ms) {
                     // MNEEHelper::state_transition (path_sms_ms.cpp:84-140): like
                     // the filter's record, without its scattering-type test, and
@@ -826,6 +892,11 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
                                 glint_case;
                     else if (filtered_ms)   // light_hit_valid, path_filtered_ms.cpp:191
                         allow = !on_caster || (rec == kRecEmitter && rec_b == P.bounces) || (flags & kSpecularCamera);
+                    else if (filtered_teaser)   // filtered_emitter_hit_valid (:380-393), :186-195
+                        allow = on_caster ? (((tf == kTfSingleEmitter && rec_b == 1) ||
+                                              (tf == kTfMultiEmitter && rec_b == P.bounces)) &&
+                                             emitter_is_caustic_ms(sc, es.emitter))
+                                          : P.non_sms_paths != 0;
                     if (allow) {
                         float epdf = bs.delta ? 0.f : emitter_pdf(sc, es, si.p, ep, d2, h2.t);
                         if (add_paths) L = L + thr * Le * mis_weight(bs.pdf, epdf);
@@ -1096,7 +1167,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
                                                          : std::min<uint32_t>(opt->samples_per_pass, (uint32_t)opt->spp);
     if ((uint32_t)opt->spp % spp_pass != 0)
         return rfail(SMS_ERR_INVALID_ARG, "sms_render: spp must be a multiple of samples_per_pass");
-    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_SMS_TEASER)
+    if (opt->integrator < SMS_INTEGRATOR_PATH || opt->integrator > SMS_INTEGRATOR_PATH_FILTERED_TEASER)
         return rfail(SMS_ERR_INVALID_ARG, "sms_render: unknown integrator");
     const bool teaser = opt->integrator == SMS_INTEGRATOR_PATH_SMS_TEASER;
     // the teaser's glints need a glinty shape with a slope map
@@ -1120,6 +1191,8 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     if (opt->max_depth < -1) return rfail(SMS_ERR_INVALID_ARG, "sms_render: max_depth must be -1 or >= 0");
     if (opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS && (v.bounces < 1 || v.bounces > kMaxBounces))
         return rfail(SMS_ERR_UNSUPPORTED, "path_filtered_ms: bounces must be between 1 and 4");
+    if (opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_TEASER && (v.bounces < 1 || v.bounces > kMaxBounces))
+        return rfail(SMS_ERR_UNSUPPORTED, "path_filtered_teaser: multi_caustic_bounces must be between 1 and 4");
     PtParams P{};
     P.integrator = opt->integrator;
     P.max_depth = opt->max_depth;
@@ -1127,7 +1200,7 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     P.disable_reflected_emitters = opt->disable_reflected_emitters;
     P.biased_mnee = opt->biased_mnee;
     P.bounces = (opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS || opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_MS ||
-                 teaser)
+                 opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_TEASER || teaser)
                     ? v.bounces : 1;
     P.mnee_check = opt->integrator == SMS_INTEGRATOR_PATH_SMS_SS && v.solver.mnee_init && !opt->biased_mnee;
     P.mnee_ms = opt->integrator == SMS_INTEGRATOR_PATH_SMS_MS && v.solver.mnee_init && !opt->biased_mnee;

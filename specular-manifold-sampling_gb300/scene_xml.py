@@ -36,12 +36,14 @@ load_render_setup reads the rendering side of the same file:
       <film> width, height (hdrfilm defaults 768 x 576), <sampler> sample_count
       (independent sampler default 4)   (src/sensors/perspective.cpp)
   <integrator type="path|path_sms_ss|path_sms_ms|path_sms_glints|path_filtered_ss|path_filtered_ms|
-                    path_sms_teaser">  max_depth, rr_depth
+                    path_sms_teaser|path_filtered_teaser">  max_depth, rr_depth
       (src/librender/integrator.cpp:300-320), samples_per_pass, timeout,
       glint_diff_scale_factor_clamp (:35-41), disable_reflected_emitters,
       biased_mnee (path_sms_ss.cpp:59-60); path_sms_teaser's caustics_enabled,
       glints_enabled, non_sms_paths_enabled and glints_* block
-      (path_sms_teaser.cpp:60-81; its caustics_* block is the SMSConfig)
+      (path_sms_teaser.cpp:60-81; its caustics_* block is the SMSConfig);
+      path_filtered_teaser's non_sms_paths_enabled and multi_caustic_bounces
+      (the SMSConfig's bounces; path_filtered_teaser.cpp:45-48)
 and returns (Camera, RenderOptions).
 """
 from __future__ import annotations
@@ -61,7 +63,7 @@ IOR = {"vacuum": 1.0, "helium": 1.000036, "hydrogen": 1.000132, "air": 1.000277,
 
 _IGNORED = {"sensor", "film", "sampler", "default"}
 _INTEGRATOR_TYPES = {"path", "path_sms_ss", "path_sms_ms", "path_filtered_ss", "path_filtered_ms", "path_sms_glints",
-                     "path_sms_teaser"}
+                     "path_sms_teaser", "path_filtered_teaser"}
 
 
 def _props(el):
@@ -379,6 +381,8 @@ def load_render_setup(sms, path):
         opt.samples_per_pass = _int(ip, "samples_per_pass", 0)
         opt.timeout = _float(ip, "timeout", -1.0)
         opt.glint_diff_scale_factor_clamp = _float(ip, "glint_diff_scale_factor_clamp", 0.0)
+        if t == "path_filtered_teaser":
+            opt.non_sms_paths_enabled = _bool(ip, "non_sms_paths_enabled", True)
         if t == "path_sms_teaser":
             # path_sms_teaser.cpp:60-81: the switches and the glints_* block
             opt.caustics_enabled = _bool(ip, "caustics_enabled", True)

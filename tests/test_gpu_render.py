@@ -255,6 +255,62 @@ def test_lean_fallback_matches_oracle(sms, workloads, oracle, gpu_lib, integrato
     assert abs(plain.mean() - g.mean()) > 0.005 * g.mean()
 
 
+def _teaser_area_light(sms, W):
+    """The teaser stand-in with its point light replaced by a sphere area light
+    flagged for single- and multi-scatter caustics, so that path tracing can
+    reach the caustics it filters."""
+    desc = W.teaser_scene()
+    desc.point_emitters.clear()
+    light = desc.add_sphere((0.0, 0.5, 4.0), 0.4, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0)
+    desc.add_area_emitter(light, (40.0, 40.0, 40.0), sms.EMITTER_CAUSTIC_SINGLE | sms.EMITTER_CAUSTIC_MULTI)
+    return desc
+
+
+def test_filtered_teaser_matches_oracle(sms, workloads, oracle, gpu_lib):
+    """path_filtered_teaser (path_filtered_teaser.cpp:56-226, 331-410): path
+    tracing with the teaser's caustic filter (single- and multi-scatter chains
+    tracked by the path record, caustic-only emitter samples on casters) on the
+    teaser stand-in with an area light, GPU vs the oracle within the
+    oracle-vs-FMA floor."""
+    W = workloads
+    desc = _teaser_area_light(sms, W)
+    cfg = sms.SMSConfig(bounces=2)
+    cam = W.teaser_camera(16, 16)
+    opt = sms.RenderOptions(integrator="path_filtered_teaser", spp=8, seed=5)
+    g, o, f = _check_against_oracle(sms, oracle, desc, cfg, cam, opt)
+    assert abs(g.mean() - o.mean()) <= 3.0 * abs(f.mean() - o.mean()) + 0.02 * o.mean()
+
+
+def test_filtered_teaser_caustics_only(sms, workloads, oracle, gpu_lib):
+    """Without the non-SMS paths only the filtered caustics remain.  With the
+    teaser's point light none can be found by path tracing (its casters are
+    smooth, so they take no emitter samples, and no ray hits a point light):
+    the image is zero, and no SMS query is made.  With an area light the
+    sparse caustic image (a few paths per pixel that reach the light through
+    the chains) matches the oracle's."""
+    W = workloads
+    cfg = sms.SMSConfig(bounces=2)
+    ctx = sms.Context(sms.Scene(W.teaser_scene()), cfg)
+    img = ctx.render(W.teaser_camera(16, 16), sms.RenderOptions(integrator="path_filtered_teaser", spp=8, seed=5,
+                                                                non_sms_paths_enabled=False))
+    assert ctx.stats()["connections"] == 0
+    ctx.close()
+    assert not img.any()
+    desc = _teaser_area_light(sms, W)
+    cam = W.teaser_camera(24, 24)
+    opt = sms.RenderOptions(integrator="path_filtered_teaser", spp=256, seed=5, non_sms_paths_enabled=False)
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    g = ctx.render(cam, opt)
+    ctx.close()
+    o = oracle.OracleScene(desc).render(cfg, cam, opt)
+    nz_g, nz_o = g[..., 0] > 0, o[..., 0] > 0
+    print(f"filtered teaser caustics: mean gpu {g.mean():.5g} oracle {o.mean():.5g}, "
+          f"pixels {nz_g.sum()} / {nz_o.sum()}, shared {(nz_g & nz_o).sum()}")
+    assert nz_o.sum() > 10
+    assert (nz_g & nz_o).sum() >= 0.7 * nz_o.sum()
+    assert abs(g.mean() - o.mean()) <= 0.25 * o.mean()
+
+
 @pytest.mark.parametrize("integrator", ["path_filtered_ss", "path_filtered_ms"])
 def test_filtered_integrators_match_oracle(sms, workloads, oracle, gpu_lib, integrator):
     """path_filtered_ss / path_filtered_ms (plain path tracing restricted to

@@ -206,6 +206,29 @@ def test_teaser_integrator_from_xml(sms, tmp_path):
     assert cfg.bounces == 2 and not cfg.biased and cfg.max_trials == -1
 
 
+def test_filtered_teaser_integrator_from_xml(sms, tmp_path):
+    """path_filtered_teaser (path_filtered_teaser.cpp:45-48): the filter's
+    chain length multi_caustic_bounces (default 2) is the SMSConfig's bounces;
+    non_sms_paths_enabled is a render option."""
+    path = tmp_path / "ft.xml"
+    i0, i1 = RENDER_XML.index("<integrator"), RENDER_XML.index("</integrator>") + len("</integrator>")
+    body = """<integrator type="path_filtered_teaser">
+    <integer name="max_depth" value="7"/>
+    <integer name="multi_caustic_bounces" value="3"/>
+    <boolean name="non_sms_paths_enabled" value="false"/>
+  </integrator>"""
+    path.write_text(RENDER_XML[:i0] + body + RENDER_XML[i1:])
+    _, cfg, kind = sms.load_scene(path)
+    assert kind == "path_filtered_teaser" and cfg.bounces == 3
+    cam, opt = sms.load_render_setup(path)
+    assert opt.integrator == "path_filtered_teaser" and opt.max_depth == 7 and not opt.non_sms_paths_enabled
+    assert opt.to_c().integrator == 7
+    path.write_text(RENDER_XML[:i0] + '<integrator type="path_filtered_teaser"/>' + RENDER_XML[i1:])
+    _, cfg, _ = sms.load_scene(path)
+    assert cfg.bounces == 2
+    assert sms.load_render_setup(path)[1].non_sms_paths_enabled
+
+
 def test_rough_bsdfs_from_xml(sms, tmp_path):
     body = """<scene version="2.0.0">
       <shape type="sphere"><float name="radius" value="1"/>

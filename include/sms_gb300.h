@@ -592,7 +592,17 @@ typedef struct sms_render_options {
     sms_config glints;                   /* glints_* (SMSConfig defaults); the
                                             glints always run the biased estimator
                                             (path_sms_teaser.cpp:347-350)          */
+    /* the film's reconstruction filter: SMS_RFILTER_BOX (this struct's default;
+       each pixel the mean of its samples) or SMS_RFILTER_GAUSSIAN (the
+       reference film's default, src/rfilters/gaussian.cpp: stddev, radius
+       4 stddev, tabulated like rfilter.cpp:9-20; every sample splats onto the
+       pixels within the radius, imageblock.cpp:111-160, and each pixel is its
+       weighted mean)                                                         */
+    int32_t  rfilter;
+    float    rfilter_stddev;             /* 0.5; Gaussian only, (0, 2]             */
 } sms_render_options;
+#define SMS_RFILTER_BOX      0
+#define SMS_RFILTER_GAUSSIAN 1
 void sms_render_options_default(sms_render_options *opt);
 
 /* Samples per pixel of the context's last render (spp, or fewer after a

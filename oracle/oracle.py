@@ -54,7 +54,8 @@ class _RenderOptions(C.Structure):
                 ("seed", C.c_uint64), ("max_paths", C.c_uint32),
                 ("glint_diff_scale_factor_clamp", C.c_float), ("samples_per_pass", C.c_uint32),
                 ("timeout", C.c_float), ("caustics_enabled", C.c_int32), ("glints_enabled", C.c_int32),
-                ("non_sms_paths_enabled", C.c_int32), ("glints", _Config)]
+                ("non_sms_paths_enabled", C.c_int32), ("glints", _Config),
+                ("rfilter", C.c_int32), ("rfilter_stddev", C.c_float)]
 
 
 _INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
@@ -358,6 +359,8 @@ class OracleScene:
         o.caustics_enabled = int(getattr(options, "caustics_enabled", True))
         o.glints_enabled = int(getattr(options, "glints_enabled", True))
         o.non_sms_paths_enabled = int(getattr(options, "non_sms_paths_enabled", True))
+        o.rfilter = {"box": 0, "gaussian": 1}[getattr(options, "rfilter", "box")]
+        o.rfilter_stddev = float(getattr(options, "rfilter_stddev", 0.5))
         gcfg = getattr(options, "glints", None)
         if gcfg is not None:
             o.glints = _cfg(gcfg)

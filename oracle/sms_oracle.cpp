@@ -3952,6 +3952,62 @@ int oracle_render(void *s, const sms_config *cfg, const sms_camera *cam, const s
     for (int k = 1; k < nthreads; ++k) th.emplace_back(worker);
     worker();
     for (auto &x : th) x.join();
+    if (opt->rfilter == SMS_RFILTER_GAUSSIAN) {
+        /* the Gaussian reconstruction filter (gaussian.cpp; radius 4 stddev),
+           tabulated at 32 points (rfilter.cpp:9-20); every sample splats onto
+           n pixels per axis (ImageBlock::put, imageblock.cpp:111-160) and each
+           pixel is its weighted mean */
+        const int R = 31;
+        const float sd = opt->rfilter_stddev, r = 4.f * sd, alpha = -1.f / (2.f * sd * sd);
+        const float bias = std::exp(alpha * r * r);
+        float table[32];
+        for (int i = 0; i < R; ++i) {
+            const float x = (r * (float)i) / (float)R;
+            table[i] = std::max(0.f, std::exp(alpha * (x * x)) - bias);
+        }
+        table[R] = 0.f;
+        const float scale = (float)R / r;
+        const int n = (int)std::ceil((r - 2.f * (float)kRayEps) * 2.f);
+        std::vector<float> img(3 * wh, 0.f), wsum(wh, 0.f);
+        const int W = cam->width, H = cam->height;
+        for (uint64_t g = 0; g < total; ++g) {
+            const uint64_t p = g % wh;
+            const int px = (int)(p % (uint64_t)W), py = (int)(p / (uint64_t)W);
+            PCG32 rng;
+            rng.seed(opt->seed, g);   /* the camera sample's position (pt_sample) */
+            const float ux = (float)rng.next_f32(), uy = (float)rng.next_f32();
+            const float sx = ((float)px + ux) / (float)W, sy = ((float)py + uy) / (float)H;
+            const float pos[2] = {sx * (float)W - 0.5f, sy * (float)H - 0.5f};
+            int lo[2];
+            float w[2][64];
+            int cnt[2];
+            for (int a = 0; a < 2; ++a) {
+                lo[a] = (int)std::ceil(pos[a] - r);
+                const int hi = (int)std::floor(pos[a] + r);
+                cnt[a] = std::min(n, hi - lo[a] + 1);
+                const float base = (float)lo[a] - pos[a];
+                for (int i = 0; i < cnt[a]; ++i)
+                    w[a][i] = table[std::min((int)std::fabs((base + (float)i) * scale), R)];
+            }
+            for (int yr = 0; yr < cnt[1]; ++yr) {
+                const int y = lo[1] + yr;
+                if (y < 0 || y >= H) continue;
+                for (int xr = 0; xr < cnt[0]; ++xr) {
+                    const int x = lo[0] + xr;
+                    if (x < 0 || x >= W) continue;
+                    const float wt = w[1][yr] * w[0][xr];
+                    const uint64_t d = (uint64_t)y * W + x;
+                    for (int c = 0; c < 3; ++c) img[3 * d + c] += Ls[3 * g + c] * wt;
+                    wsum[d] += wt;
+                }
+            }
+        }
+        for (uint64_t p = 0; p < wh; ++p) {
+            const float sc = wsum[p] != 0.f ? 1.f / wsum[p] : 0.f;
+            for (int c = 0; c < 3; ++c) image[3 * p + c] = img[3 * p + c] * sc;
+        }
+        return 0;
+    }
     for (uint64_t p = 0; p < wh; ++p) {
         float acc[3] = {0.f, 0.f, 0.f};
         for (int k = 0; k < opt->spp; ++k)

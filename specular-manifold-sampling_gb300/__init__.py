@@ -50,6 +50,7 @@ PROPOSAL_FEATURES = 9
 PROPOSAL_OUTPUTS = 40
 PROPOSAL_PARAMS = 21808
 
+RFILTERS = {"box": 0, "gaussian": 1}
 INTEGRATORS = {"path": 0, "path_sms_ss": 1, "path_sms_ms": 2, "path_sms_glints": 3, "path_filtered_ss": 4,
                "path_filtered_ms": 5, "path_sms_teaser": 6, "path_filtered_teaser": 7}
 FOV_AXES = {"x": 0, "y": 1, "diagonal": 2, "smaller": 3, "larger": 4}
@@ -111,7 +112,8 @@ class _RenderOptions(C.Structure):
                 ("seed", C.c_uint64), ("max_paths", C.c_uint32),
                 ("glint_diff_scale_factor_clamp", C.c_float), ("samples_per_pass", C.c_uint32),
                 ("timeout", C.c_float), ("caustics_enabled", C.c_int32), ("glints_enabled", C.c_int32),
-                ("non_sms_paths_enabled", C.c_int32), ("glints", _Config)]
+                ("non_sms_paths_enabled", C.c_int32), ("glints", _Config),
+                ("rfilter", C.c_int32), ("rfilter_stddev", C.c_float)]
 
 
 class _Profile(C.Structure):
@@ -659,6 +661,10 @@ class RenderOptions:
     glints_enabled: bool = True
     non_sms_paths_enabled: bool = True
     glints: "SMSConfig | None" = None
+    # the film's reconstruction filter: "box" or "gaussian" (the reference
+    # film's default, stddev 0.5; src/rfilters/gaussian.cpp)
+    rfilter: str = "box"
+    rfilter_stddev: float = 0.5
 
     def to_c(self) -> _RenderOptions:
         o = _RenderOptions()
@@ -672,6 +678,8 @@ class RenderOptions:
         o.caustics_enabled, o.glints_enabled = int(self.caustics_enabled), int(self.glints_enabled)
         o.non_sms_paths_enabled = int(self.non_sms_paths_enabled)
         o.glints = (self.glints or SMSConfig()).to_c()
+        o.rfilter = RFILTERS[self.rfilter]
+        o.rfilter_stddev = float(self.rfilter_stddev)
         return o
 
 

@@ -1091,6 +1091,78 @@ __global__ void pt_scale_kernel(float *image, size_t n, float s) {
     if (i < n) image[i] *= s;
 }
 
+// The Gaussian reconstruction filter as the reference film applies it: the
+// filter tabulated at kFilterRes + 1 points (rfilter.cpp:9-20), n weights per
+// axis around each sample (imageblock.cpp:111-135).
+constexpr int kFilterRes = 31;
+struct PtFilter {
+    float table[kFilterRes + 1];
+    float radius, scale;
+    int n;       // weights per axis of one sample
+    int reach;   // source pixels a destination pixel gathers from, each side
+};
+
+// Weight of a sample at pixel coordinate pos (the sample position minus 0.5)
+// on pixel x of one axis; false when x is not among its n pixels.
+SMS_D bool filter_weight(const PtFilter &F, float pos, int x, float &w) {
+    const int lo = (int)ceilf(pos - F.radius), hi = (int)floorf(pos + F.radius);
+    const int i = x - lo;
+    if (i < 0 || i >= F.n || x > hi) return false;
+    const float p = ((float)lo - pos) + (float)i;
+    w = F.table[min((int)fabsf(p * F.scale), kFilterRes)];
+    return true;
+}
+
+// ImageBlock::put of one chunk's samples (imageblock.cpp:111-160) as a
+// gather: each destination pixel of rows [y0, y0 + rows) sums w L and w over
+// the chunk's samples that splat onto it, source pixel by source pixel in
+// sample order, so the image is reproducible; chunks add in order.  The
+// weight sum is kept only when `weights` (the teaser's later passes trace
+// the same samples).
+__global__ void __launch_bounds__(kPtBlock) pt_splat_kernel(PtState S, PtFilter F, float *image, float *wsum,
+                                                            uint32_t width, uint32_t height, uint32_t pix0,
+                                                            uint32_t n_pix, uint32_t n_samples, uint32_t y0,
+                                                            uint32_t rows, int weights) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= rows * width) return;
+    const int x = (int)(j % width), y = (int)(y0 + j / width);
+    f3 acc = splat(0.f);
+    float wacc = 0.f;
+    for (int dy = -F.reach; dy <= F.reach; ++dy) {
+        const int sy = y + dy;
+        if (sy < 0 || sy >= (int)height) continue;
+        for (int dx = -F.reach; dx <= F.reach; ++dx) {
+            const int sx = x + dx;
+            if (sx < 0 || sx >= (int)width) continue;
+            const uint32_t src = (uint32_t)sy * width + (uint32_t)sx;
+            if (src < pix0 || src >= pix0 + n_pix) continue;
+            for (uint32_t k = 0; k < n_samples; ++k) {
+                const uint32_t i = k * n_pix + (src - pix0);
+                const float px = S.cam_s[i] * (float)width - 0.5f;
+                const float py = S.cam_s[(size_t)S.cap + i] * (float)height - 0.5f;
+                float wx, wy;
+                if (!filter_weight(F, px, x, wx) || !filter_weight(F, py, y, wy)) continue;
+                const float w = wy * wx;
+                acc = acc + ld3s(S.L, S.cap, i) * w;
+                wacc += w;
+            }
+        }
+    }
+    const size_t d = (size_t)y * width + (size_t)x;
+    float *px = image + 3 * d;
+    px[0] += acc.x; px[1] += acc.y; px[2] += acc.z;
+    if (weights) wsum[d] += wacc;
+}
+
+// The film's weighted mean: pixels without weight stay 0.
+__global__ void pt_normalize_kernel(float *image, const float *wsum, size_t n_pix) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pix) return;
+    const float w = wsum[i];
+    const float s = w != 0.f ? 1.f / w : 0.f;
+    image[3 * i] *= s; image[3 * i + 1] *= s; image[3 * i + 2] *= s;
+}
+
 sms_status rfail(sms_status st, const std::string &msg) {
     return (sms_status)set_last_error_impl((int)st, msg.c_str());
 }
@@ -1119,6 +1191,8 @@ extern "C" void sms_render_options_default(sms_render_options *o) {
     o->spp = 1;
     o->caustics_enabled = o->glints_enabled = o->non_sms_paths_enabled = 1;
     sms_config_default(&o->glints);
+    o->rfilter = SMS_RFILTER_BOX;
+    o->rfilter_stddev = 0.5f;
 }
 
 extern "C" uint64_t sms_render_sms_seed(uint64_t seed) {
@@ -1193,6 +1267,25 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         return rfail(SMS_ERR_UNSUPPORTED, "path_filtered_ms: bounces must be between 1 and 4");
     if (opt->integrator == SMS_INTEGRATOR_PATH_FILTERED_TEASER && (v.bounces < 1 || v.bounces > kMaxBounces))
         return rfail(SMS_ERR_UNSUPPORTED, "path_filtered_teaser: multi_caustic_bounces must be between 1 and 4");
+    const bool gauss = opt->rfilter == SMS_RFILTER_GAUSSIAN;
+    if (opt->rfilter != SMS_RFILTER_BOX && !gauss) return rfail(SMS_ERR_INVALID_ARG, "sms_render: unknown rfilter");
+    PtFilter F{};
+    if (gauss) {
+        if (!(opt->rfilter_stddev > 0.f && opt->rfilter_stddev <= 2.f))
+            return rfail(SMS_ERR_INVALID_ARG, "sms_render: rfilter_stddev must lie in (0, 2]");
+        // gaussian.cpp: radius 4 stddev, max(0, exp(alpha x^2) - exp(alpha r^2))
+        const float sd = opt->rfilter_stddev, r = 4.f * sd, alpha = -1.f / (2.f * sd * sd);
+        const float bias = std::exp(alpha * r * r);
+        for (int i = 0; i < kFilterRes; ++i) {
+            const float x = (r * (float)i) / (float)kFilterRes;
+            F.table[i] = std::max(0.f, std::exp(alpha * (x * x)) - bias);
+        }
+        F.table[kFilterRes] = 0.f;
+        F.radius = r;
+        F.scale = (float)kFilterRes / r;
+        F.n = (int)std::ceil((r - 2.f * kRayEps) * 2.f);
+        F.reach = (int)std::ceil(r + 0.5f);
+    }
     PtParams P{};
     P.integrator = opt->integrator;
     P.max_depth = opt->max_depth;
@@ -1251,8 +1344,9 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
                  o_q = take(4 * (size_t)kQueryRowsMax * qcap), o_val = take(12 * (size_t)qcap),
                  o_cnt = take(4 * (size_t)qcap), o_wk = take(4 * (size_t)qcap),
                  o_mn = take(P.mnee_ms ? 4 * (size_t)kMneeRows * cap : 0),
-                 o_mw = take(P.mnee_ms ? 4 * (size_t)cap : 0);
+                 o_mw = take(P.mnee_ms ? 4 * (size_t)cap : 0), o_ws = take(gauss ? 4 * (size_t)wh : 0);
     char *blk = nullptr;
+    float *wsum = nullptr;   // the Gaussian filter's weight per pixel
     uint32_t *host_tot = nullptr;
     sms_status st = SMS_OK;
     cudaStream_t s = v.stream;
@@ -1334,7 +1428,9 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     S.mnee_want = P.mnee_ms ? reinterpret_cast<int *>(blk + o_mw) : nullptr;
     S.cap = cap;
     S.qcap = qcap;
+    wsum = gauss ? reinterpret_cast<float *>(blk + o_ws) : nullptr;
     PT_TRY(cudaMemsetAsync(image, 0, img_n * sizeof(float), s));
+    if (gauss) PT_TRY(cudaMemsetAsync(wsum, 0, (size_t)wh * sizeof(float), s));
     ctx_set_render_spp(c, 0);
     for (const int tp : passes) {
     if (teaser) {
@@ -1397,8 +1493,19 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
         {
             const uint32_t n_pix = (uint32_t)std::min<uint64_t>(n, wh);
             const uint32_t pix0 = (uint32_t)(g0 % wh);
-            pt_resolve_kernel<<<(n_pix + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, image, pix0, n_pix,
-                                                                                     n / n_pix);
+            if (gauss) {
+                // destination rows: the chunk's rows and `reach` rows either side
+                const uint32_t W = (uint32_t)cam->width, H = (uint32_t)cam->height;
+                const int r0 = (int)(pix0 / W) - F.reach, r1 = (int)((pix0 + n_pix - 1) / W) + F.reach;
+                const uint32_t y0 = (uint32_t)std::max(r0, 0), y1 = (uint32_t)std::min(r1, (int)H - 1);
+                const uint32_t rows = y1 - y0 + 1;
+                const int weights = !teaser || tp == passes.front();
+                pt_splat_kernel<<<(rows * W + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(
+                    S, F, image, wsum, W, H, pix0, n_pix, n / n_pix, y0, rows, weights);
+            } else {
+                pt_resolve_kernel<<<(n_pix + kPtBlock - 1) / kPtBlock, kPtBlock, 0, s>>>(S, image, pix0, n_pix,
+                                                                                         n / n_pix);
+            }
             PT_TRY(cudaGetLastError());
         }
         g0 += n;
@@ -1406,7 +1513,10 @@ extern "C" sms_status sms_render_device(sms_ctx *c, const sms_camera *cam, const
     }   // passes
     {
         const uint32_t spp_done = (uint32_t)(g0 / wh);
-        pt_scale_kernel<<<(unsigned)((img_n + 255) / 256), 256, 0, s>>>(image, img_n, 1.f / (float)spp_done);
+        if (gauss)
+            pt_normalize_kernel<<<(unsigned)((wh + 255) / 256), 256, 0, s>>>(image, wsum, (size_t)wh);
+        else
+            pt_scale_kernel<<<(unsigned)((img_n + 255) / 256), 256, 0, s>>>(image, img_n, 1.f / (float)spp_done);
         PT_TRY(cudaGetLastError());
         ctx_set_render_spp(c, spp_done);
     }

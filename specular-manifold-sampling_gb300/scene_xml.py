@@ -33,7 +33,8 @@ Returns (SceneDesc, SMSConfig or None, integrator type or None).
 load_render_setup reads the rendering side of the same file:
   <sensor type="perspective">  fov, fov_axis, near_clip, far_clip,
       <transform name="to_world"> (lookat / translate / scale / rotate / matrix),
-      <film> width, height (hdrfilm defaults 768 x 576), <sampler> sample_count
+      <film> width, height (hdrfilm defaults 768 x 576) and its <rfilter> (box,
+      or gaussian with stddev: the default), <sampler> sample_count
       (independent sampler default 4)   (src/sensors/perspective.cpp)
   <integrator type="path|path_sms_ss|path_sms_ms|path_sms_glints|path_filtered_ss|path_filtered_ms|
                     path_sms_teaser|path_filtered_teaser">  max_depth, rr_depth
@@ -359,14 +360,17 @@ def load_render_setup(sms, path):
     fp = _props(film) if film is not None else {}
     smp = next((c for c in sensor if c.tag == "sampler"), None)
     sp = _props(smp) if smp is not None else {}
-    if film is not None:
-        rf = next((c for c in film if c.tag == "rfilter"), None)
-        if rf is not None and rf.get("type") != "box":
-            raise ValueError(f"reconstruction filter '{rf.get('type')}' is not supported (box only)")
+    # the film's reconstruction filter: gaussian (stddev 0.5) unless the film
+    # names one (src/rfilters/gaussian.cpp: the reference's default), or box
+    rf = next((c for c in film if c.tag == "rfilter"), None) if film is not None else None
+    rf_type = "gaussian" if rf is None else rf.get("type")
+    if rf_type not in ("box", "gaussian"):
+        raise ValueError(f"reconstruction filter '{rf_type}' is not supported (box or gaussian)")
+    rf_stddev = _float(_props(rf), "stddev", 0.5) if rf is not None else 0.5
     axis = p["fov_axis"][1].get("value").lower() if "fov_axis" in p else "x"
     cam = sms.Camera(M.astype(np.float32), _float(p, "fov", 45.0), _int(fp, "width", 768), _int(fp, "height", 576),
                      axis, _float(p, "near_clip", 1e-2), _float(p, "far_clip", 1e4))
-    opt = sms.RenderOptions(spp=_int(sp, "sample_count", 4))
+    opt = sms.RenderOptions(spp=_int(sp, "sample_count", 4), rfilter=rf_type, rfilter_stddev=rf_stddev)
     integ = next((c for c in root if c.tag == "integrator"), None)
     if integ is not None:
         t = integ.get("type")

@@ -255,6 +255,28 @@ def test_lean_fallback_matches_oracle(sms, workloads, oracle, gpu_lib, integrato
     assert abs(plain.mean() - g.mean()) > 0.005 * g.mean()
 
 
+def test_gaussian_film_filter_matches_oracle(sms, workloads, oracle, gpu_lib):
+    """The film's Gaussian reconstruction filter (gaussian.cpp; ImageBlock::put,
+    imageblock.cpp:111-160): the GPU gathers each pixel's weighted samples in a
+    fixed order, chunk by chunk; the oracle splats sample by sample.  Checked
+    with the whole image in one wavefront and with wavefronts smaller than the
+    image (the splat crosses chunk boundaries)."""
+    W = workloads
+    desc, cfg = W.pool_scene(res=32), W.water_config()
+    cam = W.pool_camera(20, 16)
+    for max_paths in (0, 97):
+        opt = sms.RenderOptions(integrator="path_sms_ss", spp=4, seed=11, rfilter="gaussian", max_paths=max_paths)
+        g, o, f = _check_against_oracle(sms, oracle, desc, cfg, cam, opt)
+        assert abs(g.mean() - o.mean()) <= 3.0 * abs(f.mean() - o.mean()) + 0.01 * o.mean()
+    ctx = sms.Context(sms.Scene(desc), cfg)
+    box = ctx.render(cam, sms.RenderOptions(integrator="path_sms_ss", spp=4, seed=11))
+    with pytest.raises(sms.SMSError):
+        ctx.render(cam, sms.RenderOptions(integrator="path_sms_ss", spp=4, seed=11, rfilter="gaussian",
+                                          rfilter_stddev=0.0))
+    ctx.close()
+    assert not np.array_equal(box, g)
+
+
 def _teaser_area_light(sms, W):
     """The teaser stand-in with its point light replaced by a sphere area light
     flagged for single- and multi-scatter caustics, so that path tracing can

@@ -191,3 +191,38 @@ def test_path_filtered_ss_matches_path_sms_ss_on_flat_water(sms, workloads, O):
     se = np.sqrt(a.var(0, ddof=1) / 4 + b.var(0, ddof=1) / 4)
     assert np.all(np.abs(a.mean(0) - b.mean(0)) < 5.0 * se + 0.01 * a.mean(0) + 1e-3), (a.mean(0), b.mean(0), se)
     assert abs(a.mean() - b.mean()) < 0.03 * a.mean()
+
+
+def test_gaussian_film_filter(sms, workloads, O):
+    """The film's Gaussian reconstruction filter (gaussian.cpp, ImageBlock::put
+    at imageblock.cpp:111-160): a pixel is the weighted mean of the samples
+    within 2 pixels, so a constant image stays constant; an edge is blurred over
+    about two pixels either side; stddev 0 is refused by the library."""
+    cfg = sms.SMSConfig()
+
+    def sphere_light(flip):
+        d = sms.SceneDesc()
+        light = d.add_sphere((0.0, 0.0, 0.0), 1.0, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0, 0.0, 0.0)), 0,
+                             flip=flip)
+        d.add_area_emitter(light, (3.0, 2.0, 1.0), 0)
+        return O.OracleScene(d)
+
+    # inside an inward-facing sphere light: every camera ray sees the emitter
+    inside = sms.Camera.look_at((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), (0.0, 1.0, 0.0), 60.0, 12, 10)
+    g = sphere_light(True).render(cfg, inside, sms.RenderOptions(integrator="path", spp=4, seed=1,
+                                                                  rfilter="gaussian"))
+    np.testing.assert_allclose(g.reshape(-1, 3), np.tile([3.0, 2.0, 1.0], (120, 1)), rtol=1e-5)
+    osc = sphere_light(False)
+    # from outside: the sphere's silhouette, box vs Gaussian
+    cam = sms.Camera.look_at((0.0, 0.0, 6.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 30.0, 24, 24)
+    box = osc.render(cfg, cam, sms.RenderOptions(integrator="path", spp=16, seed=2))
+    gau = osc.render(cfg, cam, sms.RenderOptions(integrator="path", spp=16, seed=2, rfilter="gaussian"))
+    assert abs(gau[..., 0].sum() - box[..., 0].sum()) < 0.02 * box[..., 0].sum()
+    # the silhouette's interior keeps the emitter's radiance
+    assert abs(gau[12, 12, 0] - 3.0) < 1e-4 and abs(box[12, 12, 0] - 3.0) < 1e-4
+    # the Gaussian image varies more smoothly across the silhouette
+    assert np.abs(np.diff(gau[..., 0], axis=1)).max() < np.abs(np.diff(box[..., 0], axis=1)).max()
+    # a wider filter blurs more
+    wide = osc.render(cfg, cam, sms.RenderOptions(integrator="path", spp=16, seed=2, rfilter="gaussian",
+                                                  rfilter_stddev=1.0))
+    assert np.abs(np.diff(wide[..., 0], axis=1)).max() < np.abs(np.diff(gau[..., 0], axis=1)).max()

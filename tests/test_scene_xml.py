@@ -148,8 +148,16 @@ def test_render_setup_from_xml(sms, workloads, tmp_path):
     assert (cam.width, cam.height, cam.fov, cam.fov_axis) == (40, 30, 40.0, "y")
     assert (opt.integrator, opt.max_depth, opt.rr_depth, opt.spp) == ("path_sms_ss", 8, 3, 32)
     assert opt.biased_mnee and opt.disable_reflected_emitters
-    bad = RENDER_XML.replace('<rfilter type="box"/>', '<rfilter type="gaussian"/>')
-    path.write_text(bad)
+    assert opt.rfilter == "box"
+    # the film's filter: gaussian by default (the reference's), with its stddev
+    path.write_text(RENDER_XML.replace('<rfilter type="box"/>', ''))
+    assert sms.load_render_setup(path)[1].rfilter == "gaussian"
+    path.write_text(RENDER_XML.replace('<rfilter type="box"/>',
+                                       '<rfilter type="gaussian"><float name="stddev" value="0.3"/></rfilter>'))
+    opt = sms.load_render_setup(path)[1]
+    assert opt.rfilter == "gaussian" and abs(opt.rfilter_stddev - 0.3) < 1e-7
+    assert opt.to_c().rfilter == 1
+    path.write_text(RENDER_XML.replace('<rfilter type="box"/>', '<rfilter type="tent"/>'))
     with pytest.raises(ValueError):
         sms.load_render_setup(path)
     path.write_text(RENDER_XML.replace('type="path_sms_ss"', 'type="bdpt"'))

@@ -118,6 +118,9 @@ typedef struct sms_bsdf {
     float   k;          /* conductor imaginary part                             */
     float   albedo[3];  /* diffuse reflectance (receivers)                      */
     float   alpha;      /* Beckmann roughness, 0 = smooth                       */
+    int32_t twosided;   /* the BSDF acts on both sides (src/bsdfs/twosided.cpp):
+                           seen from the back, the local frame's normal is
+                           reflected; diffuse and conductor only, as there   */
 } sms_bsdf;
 
 typedef struct sms_scene sms_scene;  /* host-side scene builder (owned by caller) */

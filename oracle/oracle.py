@@ -40,7 +40,7 @@ class _Config(C.Structure):
 
 class _Bsdf(C.Structure):
     _fields_ = [("type", C.c_int32), ("eta", C.c_float), ("k", C.c_float),
-                ("albedo", C.c_float * 3), ("alpha", C.c_float)]
+                ("albedo", C.c_float * 3), ("alpha", C.c_float), ("twosided", C.c_int32)]
 
 
 class _Camera(C.Structure):
@@ -180,6 +180,7 @@ def _bsdf(b) -> _Bsdf:
     r.type, r.eta, r.k = b.type, b.eta, b.k
     r.albedo[:] = [float(x) for x in b.albedo]
     r.alpha = float(getattr(b, "alpha", 0.0))
+    r.twosided = int(getattr(b, "twosided", False))
     return r
 
 

@@ -3049,7 +3049,10 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         const Shape &s = sc.shapes[si.shape];
         V3 fs, ft;
         pt_frame(si, fs, ft);
-        V3 n_sh = si.shn, wiw = -ray.d;
+        V3 wiw = -ray.d;
+        /* a twosided BSDF seen from the back (cos_theta(wi) <= 0) works in the
+           local frame with its normal reflected (twosided.cpp) */
+        V3 n_sh = (s.bsdf.twosided && !(dot(wiw, si.shn) > 0.f)) ? -si.shn : si.shn;
         V3 wi(dot(wiw, fs), dot(wiw, ft), dot(wiw, n_sh));
         const bool receiver = (s.flags & SMS_SHAPE_CAUSTIC_RECEIVER) != 0;
         bool on_caster = false;

@@ -77,7 +77,7 @@ class _Config(C.Structure):
 
 class _Bsdf(C.Structure):
     _fields_ = [("type", C.c_int32), ("eta", C.c_float), ("k", C.c_float),
-                ("albedo", C.c_float * 3), ("alpha", C.c_float)]
+                ("albedo", C.c_float * 3), ("alpha", C.c_float), ("twosided", C.c_int32)]
 
 
 class _Result(C.Structure):
@@ -271,12 +271,14 @@ class Bsdf:
     k: float = 0.0
     albedo: tuple = (0.5, 0.5, 0.5)
     alpha: float = 0.0       # Beckmann roughness (rough dielectric / conductor), 0 = smooth
+    twosided: bool = False   # the BSDF acts on both sides (twosided.cpp); diffuse / conductor
 
     def to_c(self) -> _Bsdf:
         b = _Bsdf()
         b.type, b.eta, b.k = self.type, self.eta, self.k
         b.albedo[:] = [float(x) for x in self.albedo]
         b.alpha = self.alpha
+        b.twosided = int(self.twosided)
         return b
 
 

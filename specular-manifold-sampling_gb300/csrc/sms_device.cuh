@@ -182,6 +182,7 @@ struct DevShape {
     float albedo[3];       // diffuse reflectance (path tracer)
     float alpha;           // Beckmann roughness of a rough dielectric / conductor (0: smooth)
     int nmap_frames;       // manifold vertices on this shape use its normal map (a caster / bouncer)
+    int twosided;          // the path tracer reflects the local frame at back-side hits (twosided.cpp)
 };
 
 // Target of the MNEE initialisation (manifold_ss.cpp:229-241,

@@ -212,6 +212,9 @@ static sms_status check_bsdf(const sms_bsdf *b) {
         return fail(SMS_ERR_INVALID_ARG, "dielectric eta must be positive");
     if (!(b->alpha >= 0.f) || !std::isfinite(b->alpha))
         return fail(SMS_ERR_INVALID_ARG, "bsdf roughness alpha must be finite and >= 0");
+    // twosided.cpp: only BSDFs without transmission may be nested
+    if (b->twosided && b->type == SMS_BSDF_DIELECTRIC)
+        return fail(SMS_ERR_UNSUPPORTED, "a twosided bsdf cannot wrap a dielectric (transmission)");
     return SMS_OK;
 }
 
@@ -509,6 +512,7 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         ds.k = h.bsdf.k;
         ds.albedo[0] = h.bsdf.albedo[0]; ds.albedo[1] = h.bsdf.albedo[1]; ds.albedo[2] = h.bsdf.albedo[2];
         ds.alpha = h.bsdf.type == SMS_BSDF_DIFFUSE ? 0.f : h.bsdf.alpha;
+        ds.twosided = h.bsdf.twosided ? 1 : 0;
         ds.nmap_frames = ((int)i == s->nmap_shape && s->nmap_res > 0 &&
                           (h.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI |
                                       SMS_SHAPE_CAUSTIC_BOUNCER))) ? 1 : 0;

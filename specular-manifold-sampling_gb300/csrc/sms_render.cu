@@ -580,7 +580,9 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
         if (alive) {
             f3 fs, ft;
             shading_frame(si, fs, ft);
-            const f3 n_sh = si.shn;
+            // a twosided BSDF seen from the back (cos_theta(wi) <= 0) works in
+            // the local frame with its normal reflected (twosided.cpp)
+            const f3 n_sh = (s.twosided && !(dot(-d, si.shn) > 0.f)) ? -si.shn : si.shn;
             const f3 wiw = -d;
             const f3 wi = mk(dot(wiw, fs), dot(wiw, ft), dot(wiw, n_sh));
             const bool receiver = (s.flags & kShapeFlagReceiver) != 0;

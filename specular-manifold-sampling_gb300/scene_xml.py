@@ -16,6 +16,7 @@ silently half-loaded):
       nested <bsdf>: dielectric (int_ior / ext_ior, names from
       include/mitsuba/render/ior.h), conductor (eta, k), diffuse (reflectance),
       roughdielectric / roughconductor (isotropic Beckmann alpha),
+      twosided around one diffuse or conductor bsdf (src/bsdfs/twosided.cpp),
       normalmap around any of these (filename of an OpenEXR or PNG RGB normal
       map, tiles, lean_fallback with lean_fallback_alpha and grey eta / k;
       src/bsdfs/normalmap.cpp:24-58; one normal-mapped shape per scene); a
@@ -214,8 +215,16 @@ def _bsdf(sms, el, refs=None):
     if t == "normalmap":
         raise ValueError("a normalmap bsdf is only supported directly on a shape")
     if t == "twosided":
+        # twosided.cpp: one nested BSDF for both sides (two different ones are
+        # not supported), no transmission
         inner = [c for c in el if c.tag in ("bsdf", "ref")]
-        return _bsdf(sms, inner[0] if inner else None, refs)
+        if len(inner) > 1:
+            raise ValueError("twosided with two different nested bsdfs is not supported")
+        b = _bsdf(sms, inner[0] if inner else None, refs)
+        if b.type == sms.BSDF_DIELECTRIC:
+            raise ValueError("twosided cannot wrap a dielectric (transmission)")
+        b.twosided = True
+        return b
     if t == "dielectric":
         # dielectric.cpp:177-186: eta = int_ior / ext_ior, defaults bk7 / air
         return sms.Bsdf(sms.BSDF_DIELECTRIC, _float(p, "int_ior", 1.5046) / _float(p, "ext_ior", 1.000277))

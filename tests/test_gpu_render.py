@@ -277,6 +277,22 @@ def test_gaussian_film_filter_matches_oracle(sms, workloads, oracle, gpu_lib):
     assert not np.array_equal(box, g)
 
 
+def test_twosided_matches_oracle(sms, workloads, oracle, gpu_lib):
+    """A twosided diffuse plane lit and seen from its back (twosided.cpp: the
+    local frame's normal reflected), GPU vs the oracle; one-sided it is black
+    on the GPU too."""
+    W = workloads
+    cfg = sms.SMSConfig()
+    opt = sms.RenderOptions(integrator="path", spp=16, seed=4)
+    d, cam = W.plane_light_scene(below=True, twosided=True)
+    g, o, f = _check_against_oracle(sms, oracle, d, cfg, cam, opt)
+    assert o.mean() > 0.01
+    d, cam = W.plane_light_scene(below=True, twosided=False)
+    ctx = sms.Context(sms.Scene(d), cfg)
+    assert not ctx.render(cam, opt).any()
+    ctx.close()
+
+
 def _teaser_area_light(sms, W):
     """The teaser stand-in with its point light replaced by a sphere area light
     flagged for single- and multi-scatter caustics, so that path tracing can

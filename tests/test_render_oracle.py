@@ -226,3 +226,20 @@ def test_gaussian_film_filter(sms, workloads, O):
     wide = osc.render(cfg, cam, sms.RenderOptions(integrator="path", spp=16, seed=2, rfilter="gaussian",
                                                   rfilter_stddev=1.0))
     assert np.abs(np.diff(wide[..., 0], axis=1)).max() < np.abs(np.diff(gau[..., 0], axis=1)).max()
+
+
+def test_twosided_diffuse(sms, workloads, O):
+    """twosided.cpp: a twosided diffuse plane lit and seen from its back
+    renders like the same plane lit and seen from its front; one-sided, its
+    back is black."""
+    cfg = sms.SMSConfig()
+    opt = sms.RenderOptions(integrator="path", spp=64, seed=4)
+    d, cam = workloads.plane_light_scene(below=False, twosided=False)
+    front = O.OracleScene(d).render(cfg, cam, opt)
+    d, cam = workloads.plane_light_scene(below=True, twosided=True)
+    back = O.OracleScene(d).render(cfg, cam, opt)
+    d, cam = workloads.plane_light_scene(below=True, twosided=False)
+    dark = O.OracleScene(d).render(cfg, cam, opt)
+    assert front.mean() > 0.01
+    assert abs(back.mean() - front.mean()) < 0.03 * front.mean()
+    assert not dark.any()

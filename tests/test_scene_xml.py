@@ -237,6 +237,30 @@ def test_filtered_teaser_integrator_from_xml(sms, tmp_path):
     assert sms.load_render_setup(path)[1].non_sms_paths_enabled
 
 
+def test_twosided_bsdf_from_xml(sms, tmp_path):
+    """<bsdf type="twosided"> around a diffuse or conductor bsdf sets the
+    twosided flag (twosided.cpp); around a dielectric it is refused."""
+    body = '''<scene version="2.0.0">
+      <shape type="rectangle"><bsdf type="twosided"><bsdf type="diffuse">
+        <rgb name="reflectance" value="0.2, 0.3, 0.4"/></bsdf></bsdf></shape>
+      <shape type="rectangle"><bsdf type="conductor"/></shape>
+    </scene>'''
+    (tmp_path / "t.xml").write_text(body)
+    desc, _, _ = sms.load_scene(tmp_path / "t.xml")
+    b0, b1 = desc.meshes[0][4], desc.meshes[1][4]
+    assert b0.twosided and b0.type == sms.BSDF_DIFFUSE and b0.albedo == (0.2, 0.3, 0.4)
+    assert not b1.twosided
+    assert b0.to_c().twosided == 1
+    sms.Scene(desc)
+    (tmp_path / "d.xml").write_text(body.replace('<bsdf type="diffuse">', '<bsdf type="dielectric">'))
+    with pytest.raises(ValueError, match="dielectric"):
+        sms.load_scene(tmp_path / "d.xml")
+    d = sms.SceneDesc()
+    d.add_sphere((0, 0, 0), 1.0, sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5, twosided=True))
+    with pytest.raises(sms.SMSError):
+        sms.Scene(d)
+
+
 def test_rough_bsdfs_from_xml(sms, tmp_path):
     body = """<scene version="2.0.0">
       <shape type="sphere"><float name="radius" value="1"/>

@@ -104,7 +104,11 @@ sms_status sms_config_parse_xml(const char *xml, sms_config *cfg,
 typedef enum sms_bsdf_type {
     SMS_BSDF_DIFFUSE = 0,     /* ior() = (0, 1): treated as eta = 1            */
     SMS_BSDF_DIELECTRIC = 1,  /* dielectric, eta = int_ior / ext_ior            */
-    SMS_BSDF_CONDUCTOR = 2    /* conductor, complex ior (eta, k)                */
+    SMS_BSDF_CONDUCTOR = 2,   /* conductor, complex ior (eta, k)                */
+    SMS_BSDF_ROUGHPLASTIC = 3 /* src/bsdfs/roughplastic.cpp: diffuse base
+                                 (albedo) under a rough dielectric coating
+                                 (eta = int_ior / ext_ior, Beckmann alpha > 0);
+                                 for the path tracer only (no SMS caster)      */
 } sms_bsdf_type;
 
 /* alpha > 0 makes a dielectric / conductor the reference's roughdielectric /
@@ -120,7 +124,9 @@ typedef struct sms_bsdf {
     float   alpha;      /* Beckmann roughness, 0 = smooth                       */
     int32_t twosided;   /* the BSDF acts on both sides (src/bsdfs/twosided.cpp):
                            seen from the back, the local frame's normal is
-                           reflected; diffuse and conductor only, as there   */
+                           reflected; not around a dielectric, as there      */
+    int32_t nonlinear;  /* roughplastic: the base's internal scattering with the
+                           nonlinear colour model (roughplastic.cpp:166, 290) */
 } sms_bsdf;
 
 typedef struct sms_scene sms_scene;  /* host-side scene builder (owned by caller) */

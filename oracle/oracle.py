@@ -40,7 +40,8 @@ class _Config(C.Structure):
 
 class _Bsdf(C.Structure):
     _fields_ = [("type", C.c_int32), ("eta", C.c_float), ("k", C.c_float),
-                ("albedo", C.c_float * 3), ("alpha", C.c_float), ("twosided", C.c_int32)]
+                ("albedo", C.c_float * 3), ("alpha", C.c_float), ("twosided", C.c_int32),
+                ("nonlinear", C.c_int32)]
 
 
 class _Camera(C.Structure):
@@ -101,6 +102,9 @@ def load(fma: bool = False, variant: str | None = None):
         "oracle_scene_set_lean_fallback": (i32, [vp, f32, f32, f32]),
         "oracle_lean_fb_eval": (i32, [vp, vp, vp, u32, vp]),
         "oracle_lean_fb_sample": (i32, [vp, vp, vp, u32, vp]),
+        "oracle_shape_bsdf_eval": (i32, [vp, i32, vp, vp, u32, vp]),
+        "oracle_shape_bsdf_sample": (i32, [vp, i32, vp, vp, u32, vp]),
+        "oracle_roughplastic_tables": (i32, [vp, i32, vp]),
         "oracle_glint_walk_batch": (i32, [vp, C.POINTER(_Config), vp, vp, u32, vp]),
         "oracle_glint_connect_batch": (i32, [vp, C.POINTER(_Config), vp, u32, u64, u64, vp, vp, vp, C.c_int, vp]),
         "oracle_nm_slope": (None, [vp, f32, f32, vp]),
@@ -181,6 +185,7 @@ def _bsdf(b) -> _Bsdf:
     r.albedo[:] = [float(x) for x in b.albedo]
     r.alpha = float(getattr(b, "alpha", 0.0))
     r.twosided = int(getattr(b, "twosided", False))
+    r.nonlinear = int(getattr(b, "nonlinear", False))
     return r
 
 
@@ -235,6 +240,36 @@ class OracleScene:
         out = np.zeros((6, a.shape[1]), np.float32)
         if self._lib.oracle_lean_fb_sample(self._h, a.ctypes.data, uu.ctypes.data, a.shape[1], out.ctypes.data) != 0:
             raise ValueError("the scene has no LEAN fallback")
+        return out
+
+    def shape_bsdf_eval(self, shape: int, wi: np.ndarray, wo: np.ndarray) -> np.ndarray:
+        """A shape's BSDF for local-frame pairs (3, n): rows eval (BSDF x
+        cos_o, 3), pdf."""
+        a = np.ascontiguousarray(wi, np.float32)
+        b = np.ascontiguousarray(wo, np.float32)
+        out = np.zeros((4, a.shape[1]), np.float32)
+        if self._lib.oracle_shape_bsdf_eval(self._h, shape, a.ctypes.data, b.ctypes.data, a.shape[1],
+                                            out.ctypes.data) != 0:
+            raise ValueError(f"no shape {shape}")
+        return out
+
+    def shape_bsdf_sample(self, shape: int, wi: np.ndarray, u: np.ndarray) -> np.ndarray:
+        """Sampling of a shape's BSDF from local wi (3, n) with numbers u (3,
+        n): rows ok, wo (3), weight (3), pdf."""
+        a = np.ascontiguousarray(wi, np.float32)
+        uu = np.ascontiguousarray(u, np.float32)
+        out = np.zeros((8, a.shape[1]), np.float32)
+        if self._lib.oracle_shape_bsdf_sample(self._h, shape, a.ctypes.data, uu.ctypes.data, a.shape[1],
+                                              out.ctypes.data) != 0:
+            raise ValueError(f"no shape {shape}")
+        return out
+
+    def roughplastic_tables(self, shape: int) -> np.ndarray:
+        """A roughplastic shape's transmittance table (64), internal
+        reflectance and specular sampling weight."""
+        out = np.zeros(66, np.float32)
+        if self._lib.oracle_roughplastic_tables(self._h, shape, out.ctypes.data) != 0:
+            raise ValueError(f"shape {shape} is not roughplastic")
         return out
 
     def walk_batch(self, config, caster: int, queries: np.ndarray, walk_in: np.ndarray) -> np.ndarray:

@@ -175,6 +175,15 @@ struct PCG32 {
 };
 
 /* ------------------------------------------------------------------ scene */
+/* roughplastic's precomputed coating terms (roughplastic.cpp:364-396):
+ * external transmittance at 64 cosines, internal diffuse reflectance,
+ * specular sampling weight */
+constexpr int kRoughPlasticRes = 64;   /* MTS_ROUGH_TRANSMITTANCE_RES */
+struct RoughPlastic {
+    Float t[kRoughPlasticRes] = {};
+    Float fdr = 0.f, ws = 0.f;
+};
+
 struct Shape {
     int kind = 0; /* 0 sphere, 1 mesh */
     V3 center; Float radius = 1.f; bool flip = false;
@@ -185,6 +194,7 @@ struct Shape {
     Float area_sum = 0.f, area_norm = 0.f;
     uint32_t valid_lo = 0, valid_hi = 0;
     sms_bsdf bsdf{};
+    RoughPlastic rp;  /* set for SMS_BSDF_ROUGHPLASTIC */
     uint32_t flags = 0;
     int emitter = -1;
     V3 bbox_center;   /* Shape::bbox().center(), for the MNEE initialisation */
@@ -2939,6 +2949,145 @@ static bool nm_conductor_sample(const NormalMap &m, const sms_bsdf &b, V3 n, V3 
     return true;
 }
 
+/* ---- roughplastic (src/bsdfs/roughplastic.cpp) */
+
+/* Gauss-Legendre nodes and weights on [-1, 1] (quad::gauss_legendre): the
+ * roots of P_n by Newton's method from the Tricomi initial guesses */
+static void gauss_legendre_nodes(int n, std::vector<double> &x, std::vector<double> &w) {
+    x.assign(n, 0.0); w.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        double z = std::cos(3.14159265358979323846 * (i + 0.75) / (n + 0.5)), dp = 1.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; ++k) { const double p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k; p0 = p1; p1 = p2; }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+            const double dz = p1 / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-15) break;
+        }
+        x[n - 1 - i] = z;
+        w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+/* eval_transmittance / eval_reflectance (microfacet.h:454-551): visible
+ * normals drawn at the Gauss-Legendre nodes mapped to [0, 1]^2 (32 x 32 when
+ * eta > 1, else 128 x 128), weighted by G1 of the refracted / reflected
+ * direction and by 1 - F / F; the weight sum of 4 is divided out */
+static Float rp_eval_coating(Float alpha, Float eta, V3 wi, bool transmit) {
+    const int res = eta > 1.f ? 32 : 128;
+    std::vector<double> gx, gw;
+    gauss_legendre_nodes(res, gx, gw);
+    Float acc = 0.f;
+    for (int j = 0; j < res; ++j)
+        for (int k = 0; k < res; ++k) {
+            V2 u; u.x = Float(gx[j] * 0.5 + 0.5); u.y = Float(gx[k] * 0.5 + 0.5);
+            Float pdf;
+            const V3 m = beckmann_sample_visible(alpha, wi, u, pdf);
+            Float cos_t;
+            const Float dm = dot(wi, m);
+            const Float F = fresnel(dm, eta, &cos_t);
+            Float val;
+            if (transmit) {
+                const Float eta_ti = dm >= 0.f ? 1.f / eta : eta;
+                const V3 wo = m * (dm * eta_ti + cos_t) - wi * eta_ti;
+                val = wo.z * wi.z >= 0.f ? Float(0.f) : beckmann_G1(wo, m, alpha) * (1.f - F);
+            } else {
+                const V3 wo = m * (2.f * dm) - wi;
+                val = (wo.z <= 0.f || wi.z <= 0.f) ? Float(0.f) : beckmann_G1(wo, m, alpha) * F;
+            }
+            acc += val * Float(gw[j] * gw[k]);
+        }
+    return acc * 0.25f;
+}
+
+/* parameters_changed (roughplastic.cpp:364-396) */
+static void rp_init(Shape &sh) {
+    if (sh.bsdf.type != SMS_BSDF_ROUGHPLASTIC) return;
+    const sms_bsdf &b = sh.bsdf;
+    Float rsum = 0.f;
+    for (int i = 0; i < kRoughPlasticRes; ++i) {
+        const Float mu = omax(Float(1e-6f), Float(i) / Float(kRoughPlasticRes - 1));
+        const V3 wi(std::sqrt(1.f - mu * mu), 0.f, mu);
+        sh.rp.t[i] = rp_eval_coating(b.alpha, b.eta, wi, true);
+        rsum += rp_eval_coating(b.alpha, 1.f / b.eta, wi, false) * mu;
+    }
+    sh.rp.fdr = rsum / Float(kRoughPlasticRes) * 2.f;
+    const Float d_mean = (b.albedo[0] + b.albedo[1] + b.albedo[2]) / 3.f;
+    sh.rp.ws = 1.f / (d_mean + 1.f);
+}
+
+/* lerp_gather (roughplastic.cpp:299-310) */
+static Float rp_transmittance(const RoughPlastic &rp, Float c) {
+    const Float x = c * Float(kRoughPlasticRes - 1);
+    const int i = std::min((int)x, kRoughPlasticRes - 2);
+    return rp.t[i] + (rp.t[i + 1] - rp.t[i]) * (x - Float(i));
+}
+static Float rp_prob_specular(const RoughPlastic &rp, Float ci) {
+    const Float t_i = rp_transmittance(rp, ci);
+    const Float ps = (1.f - t_i) * rp.ws, pd = t_i * (1.f - rp.ws);
+    return ps / (ps + pd);
+}
+
+/* eval (roughplastic.cpp:245-297), value x cos_theta_o */
+static V3 rp_eval(const Shape &sh, V3 wi, V3 wo) {
+    const sms_bsdf &b = sh.bsdf;
+    const Float ci = wi.z, co = wo.z;
+    if (!(ci > 0.f && co > 0.f)) return V3(0.f);
+    const V3 h = normalize(wo + wi);
+    const Float F = fresnel(dot(wi, h), b.eta);
+    const Float G = beckmann_G1(wi, h, b.alpha) * beckmann_G1(wo, h, b.alpha);
+    const Float spec = F * beckmann_D(h, b.alpha) * G / (4.f * ci);
+    const Float t_i = rp_transmittance(sh.rp, ci), t_o = rp_transmittance(sh.rp, co);
+    V3 diff(b.albedo[0], b.albedo[1], b.albedo[2]);
+    if (b.nonlinear)
+        diff = V3(diff.x / (1.f - diff.x * sh.rp.fdr), diff.y / (1.f - diff.y * sh.rp.fdr),
+                  diff.z / (1.f - diff.z * sh.rp.fdr));
+    else
+        diff = diff * (1.f / (1.f - sh.rp.fdr));
+    return V3(spec) + diff * (kInvPi * (1.f / (b.eta * b.eta)) * co * t_i * t_o);
+}
+
+/* pdf (roughplastic.cpp:312-353), microfacet normals drawn from D cos */
+static Float rp_pdf(const Shape &sh, V3 wi, V3 wo) {
+    const Float ci = wi.z, co = wo.z;
+    if (!(ci > 0.f && co > 0.f)) return 0.f;
+    const Float ps = rp_prob_specular(sh.rp, ci);
+    const V3 h = normalize(wo + wi);
+    return beckmann_D(h, sh.bsdf.alpha) * h.z / (4.f * dot(wo, h)) * ps + (1.f - ps) * kInvPi * co;
+}
+
+/* sample (roughplastic.cpp:185-243) */
+static bool rp_sample(const Shape &sh, V3 wi, Float u1, Float u2, Float u3, PtBsdf &bs) {
+    const Float ci = wi.z;
+    if (!(ci > 0.f)) return false;
+    if (u1 < rp_prob_specular(sh.rp, ci)) {
+        Float pm;
+        const V3 m = beckmann_sample(sh.bsdf.alpha, u2, u3, pm);
+        bs.wo = m * (2.f * dot(wi, m)) - wi;
+    } else {
+        bs.wo = pt_cosine_hemisphere(u2, u3);
+    }
+    bs.delta = false;
+    bs.eta = 1.f;
+    bs.pdf = rp_pdf(sh, wi, bs.wo);
+    if (!(bs.pdf > 0.f)) return false;
+    bs.weight = rp_eval(sh, wi, bs.wo) * (1.f / bs.pdf);
+    return true;
+}
+
+/* the path tracers' BSDF of a shape: roughplastic or the plain BSDFs */
+static V3 shape_bsdf_eval(const Shape &sh, V3 wi, V3 wo) {
+    return sh.bsdf.type == SMS_BSDF_ROUGHPLASTIC ? rp_eval(sh, wi, wo) : pt_bsdf_eval(sh.bsdf, wi, wo);
+}
+static Float shape_bsdf_pdf(const Shape &sh, V3 wi, V3 wo) {
+    return sh.bsdf.type == SMS_BSDF_ROUGHPLASTIC ? rp_pdf(sh, wi, wo) : pt_bsdf_pdf(sh.bsdf, wi, wo);
+}
+static bool shape_bsdf_sample(const Shape &sh, V3 wi, Float u1, Float u2, Float u3, PtBsdf &bs) {
+    return sh.bsdf.type == SMS_BSDF_ROUGHPLASTIC ? rp_sample(sh, wi, u1, u2, u3, bs)
+                                                 : pt_bsdf_sample(sh.bsdf, wi, u1, u2, u3, bs);
+}
+
 /* NormalmapBSDF::sample (normalmap.cpp:118-135) around any smooth nested BSDF:
  * sampled in the perturbed frame at uv, the direction taken back to the
  * shading frame (fs, ft, n) and kept when it lies on the same side of both
@@ -3204,9 +3353,9 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
                        nested BSDF: nothing */
                     V3 bv = lean_now  ? V3(lean_fb_eval(sc.nmap, sc.lean_fb, wi, wo))
                             : nmapped ? V3(0.f)
-                                      : pt_bsdf_eval(s.bsdf, wi, wo);
+                                      : shape_bsdf_eval(s, wi, wo);
                     if (bv.x != 0.f || bv.y != 0.f || bv.z != 0.f) {
-                        const Float bp = lean_now ? lean_fb_pdf(sc.nmap, sc.lean_fb, wi, wo) : pt_bsdf_pdf(s.bsdf, wi, wo);
+                        const Float bp = lean_now ? lean_fb_pdf(sc.nmap, sc.lean_fb, wi, wo) : shape_bsdf_pdf(s, wi, wo);
                         Float w = ds.delta ? Float(1.f) : mis_weight(ds.pdf, bp);
                         /* path_filtered_ss.cpp:127-142 / path_filtered_ms.cpp:137-150 */
                         if (valid_conn && (filtered_ms || depth > 1)) {
@@ -3242,7 +3391,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
             /* the normal-mapped BSDF at the hit's own uv */
             if (!nm_bsdf_sample(sc.nmap, s.bsdf, fs, ft, n_sh, si.dp_du, si.uv, wiw, u1, u2, u3, bs)) break;
         } else {
-            if (!pt_bsdf_sample(s.bsdf, wi, u1, u2, u3, bs)) break;
+            if (!shape_bsdf_sample(s, wi, u1, u2, u3, bs)) break;
             bs.transmit = bs.wo.z * wi.z < 0.f;
         }
         thr = thr * bs.weight;
@@ -3422,6 +3571,7 @@ int oracle_scene_add_sphere(void *s, const float *c, float r, int flip, const sm
     sh.kind = 0; sh.center = V3(c[0], c[1], c[2]); sh.radius = std::fabs(r);
     sh.flip = (flip != 0) != (r <= 0.f);
     sh.bsdf = *b; sh.flags = flags;
+    rp_init(sh);
     sh.bbox_center = sh.center;
     sc->shapes.push_back(sh);
     sc->finalized = false;
@@ -3461,6 +3611,7 @@ int oracle_scene_add_mesh(void *s, const float *P, const float *N, const float *
     sh.area_sum = (float)sum;
     sh.area_norm = (float)(1.0 / sum);
     sh.bsdf = *b; sh.flags = flags;
+    rp_init(sh);
     sc->shapes.push_back(sh);
     sc->finalized = false;
     return (int)sc->shapes.size() - 1;
@@ -3853,6 +4004,53 @@ int oracle_lean_fb_sample(void *s, const float *wi, const float *u, uint32_t n, 
         out[n + i] = (float)wo.x; out[2 * n + i] = (float)wo.y; out[3 * n + i] = (float)wo.z;
         out[4 * n + i] = (float)w; out[5 * n + i] = (float)pdf;
     }
+    return 0;
+}
+
+/* A shape's BSDF as the path tracers see it, for local-frame pairs wi, wo
+ * (3 x n): out rows eval (BSDF x cos_o, 3), pdf. */
+int oracle_shape_bsdf_eval(void *s, int shape, const float *wi, const float *wo, uint32_t n, float *out) {
+    Scene *sc = as_scene(s);
+    if (shape < 0 || shape >= (int)sc->shapes.size()) return -1;
+    const Shape &sh = sc->shapes[shape];
+    for (uint32_t i = 0; i < n; ++i) {
+        const V3 a(wi[i], wi[n + i], wi[2 * n + i]), b(wo[i], wo[n + i], wo[2 * n + i]);
+        const V3 f = shape_bsdf_eval(sh, a, b);
+        out[i] = (float)f.x; out[n + i] = (float)f.y; out[2 * n + i] = (float)f.z;
+        out[3 * n + i] = (float)shape_bsdf_pdf(sh, a, b);
+    }
+    return 0;
+}
+
+/* ... and its sampling from local wi (3 x n) with numbers u (3 x n): out rows
+ * ok, wo (3), weight (3), pdf. */
+int oracle_shape_bsdf_sample(void *s, int shape, const float *wi, const float *u, uint32_t n, float *out) {
+    Scene *sc = as_scene(s);
+    if (shape < 0 || shape >= (int)sc->shapes.size()) return -1;
+    const Shape &sh = sc->shapes[shape];
+    for (uint32_t i = 0; i < n; ++i) {
+        const V3 a(wi[i], wi[n + i], wi[2 * n + i]);
+        PtBsdf bs;
+        const bool ok = shape_bsdf_sample(sh, a, u[i], u[n + i], u[2 * n + i], bs);
+        out[i] = ok ? 1.f : 0.f;
+        out[n + i] = ok ? (float)bs.wo.x : 0.f; out[2 * n + i] = ok ? (float)bs.wo.y : 0.f;
+        out[3 * n + i] = ok ? (float)bs.wo.z : 0.f;
+        out[4 * n + i] = ok ? (float)bs.weight.x : 0.f; out[5 * n + i] = ok ? (float)bs.weight.y : 0.f;
+        out[6 * n + i] = ok ? (float)bs.weight.z : 0.f; out[7 * n + i] = ok ? (float)bs.pdf : 0.f;
+    }
+    return 0;
+}
+
+/* A roughplastic shape's precomputed terms: out = transmittance (64),
+ * internal reflectance, specular sampling weight. */
+int oracle_roughplastic_tables(void *s, int shape, float *out) {
+    Scene *sc = as_scene(s);
+    if (shape < 0 || shape >= (int)sc->shapes.size()) return -1;
+    const Shape &sh = sc->shapes[shape];
+    if (sh.bsdf.type != SMS_BSDF_ROUGHPLASTIC) return -1;
+    for (int i = 0; i < kRoughPlasticRes; ++i) out[i] = (float)sh.rp.t[i];
+    out[kRoughPlasticRes] = (float)sh.rp.fdr;
+    out[kRoughPlasticRes + 1] = (float)sh.rp.ws;
     return 0;
 }
 

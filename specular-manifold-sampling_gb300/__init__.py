@@ -44,7 +44,7 @@ SHAPE_GLINTY = 1 << 4
 EMITTER_CAUSTIC_SINGLE = 1 << 0
 EMITTER_CAUSTIC_MULTI = 1 << 1
 
-BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_CONDUCTOR = 0, 1, 2
+BSDF_DIFFUSE, BSDF_DIELECTRIC, BSDF_CONDUCTOR, BSDF_ROUGHPLASTIC = 0, 1, 2, 3
 
 PROPOSAL_FEATURES = 9
 PROPOSAL_OUTPUTS = 40
@@ -77,7 +77,8 @@ class _Config(C.Structure):
 
 class _Bsdf(C.Structure):
     _fields_ = [("type", C.c_int32), ("eta", C.c_float), ("k", C.c_float),
-                ("albedo", C.c_float * 3), ("alpha", C.c_float), ("twosided", C.c_int32)]
+                ("albedo", C.c_float * 3), ("alpha", C.c_float), ("twosided", C.c_int32),
+                ("nonlinear", C.c_int32)]
 
 
 class _Result(C.Structure):
@@ -271,7 +272,8 @@ class Bsdf:
     k: float = 0.0
     albedo: tuple = (0.5, 0.5, 0.5)
     alpha: float = 0.0       # Beckmann roughness (rough dielectric / conductor), 0 = smooth
-    twosided: bool = False   # the BSDF acts on both sides (twosided.cpp); diffuse / conductor
+    twosided: bool = False   # the BSDF acts on both sides (twosided.cpp); not a dielectric
+    nonlinear: bool = False  # roughplastic's nonlinear internal scattering
 
     def to_c(self) -> _Bsdf:
         b = _Bsdf()
@@ -279,6 +281,7 @@ class Bsdf:
         b.albedo[:] = [float(x) for x in self.albedo]
         b.alpha = self.alpha
         b.twosided = int(self.twosided)
+        b.nonlinear = int(self.nonlinear)
         return b
 
 

@@ -159,7 +159,8 @@ constexpr uint32_t kShapeFlagCasterSingle = 1u << 1;
 constexpr uint32_t kShapeFlagCasterMulti = 1u << 2;
 constexpr uint32_t kShapeFlagBouncer = 1u << 3;
 constexpr uint32_t kShapeFlagGlinty = 1u << 4;
-enum : int { kBsdfDiffuse = 0, kBsdfDielectric = 1, kBsdfConductor = 2 };
+enum : int { kBsdfDiffuse = 0, kBsdfDielectric = 1, kBsdfConductor = 2, kBsdfRoughPlastic = 3 };
+constexpr int kRoughPlasticRes = 64;   // MTS_ROUGH_TRANSMITTANCE_RES (roughplastic.cpp)
 
 struct DevShape {
     int kind;
@@ -183,6 +184,12 @@ struct DevShape {
     float alpha;           // Beckmann roughness of a rough dielectric / conductor (0: smooth)
     int nmap_frames;       // manifold vertices on this shape use its normal map (a caster / bouncer)
     int twosided;          // the path tracer reflects the local frame at back-side hits (twosided.cpp)
+    // roughplastic: the coating's external transmittance at kRoughPlasticRes
+    // cosines, the base's internal diffuse reflectance, the specular
+    // sampling weight and the nonlinear switch (roughplastic.cpp:355-399)
+    float rp_t[kRoughPlasticRes];
+    float rp_fdr, rp_ws;
+    int rp_nonlinear;
 };
 
 // Target of the MNEE initialisation (manifold_ss.cpp:229-241,

@@ -204,10 +204,112 @@ extern "C" sms_status sms_scene_create(sms_scene **out) {
 
 extern "C" void sms_scene_destroy(sms_scene *s) { delete s; }
 
+// roughplastic.cpp:355-399 (parameters_changed): the coating's external
+// transmittance T at the 64 cosines mu_i = max(1e-6, i / 63) and the base's
+// internal diffuse reflectance 2 mean_i(mu_i R_int(mu_i)).  T and R are the
+// integrals of microfacet.h:454-550 (eval_transmittance / eval_reflectance)
+// over the Beckmann visible normals of wi; here by Gauss-Legendre quadrature
+// in the normal's polar angle on [0, atan(6 alpha)] (where the density lives)
+// and the midpoint rule in its azimuth, in double precision.
+namespace {
+double rp_g1(const double v[3], const double m[3], double alpha) {   // microfacet.h smith_g1 (Beckmann)
+    if ((v[0] * m[0] + v[1] * m[1] + v[2] * m[2]) * v[2] <= 0.0) return 0.0;
+    const double xy = alpha * alpha * (v[0] * v[0] + v[1] * v[1]);
+    if (xy == 0.0) return 1.0;
+    const double a = 1.0 / std::sqrt(xy / (v[2] * v[2])), a2 = a * a;
+    return a >= 1.6 ? 1.0 : (3.535 * a + 2.181 * a2) / (1.0 + 2.276 * a + 2.577 * a2);
+}
+// dielectric Fresnel (fresnel.h:34-80): reflectance, cos of the transmitted
+// direction, eta_ti
+double rp_fresnel(double ci, double eta, double &ct, double &eta_ti) {
+    const double eta_it = ci >= 0.0 ? eta : 1.0 / eta;
+    eta_ti = ci >= 0.0 ? 1.0 / eta : eta;
+    const double ct2 = 1.0 - (1.0 - ci * ci) * eta_ti * eta_ti;
+    const double aci = std::fabs(ci), act = std::sqrt(std::max(0.0, ct2));
+    const double as = (aci - eta_it * act) / (aci + eta_it * act), ap = (act - eta_it * aci) / (act + eta_it * aci);
+    ct = ci >= 0.0 ? -act : act;
+    if (ct2 <= 0.0) return 1.0;
+    return aci == 0.0 ? 1.0 : 0.5 * (as * as + ap * ap);
+}
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
+    x.resize(n);
+    w.resize(n);
+    for (int i = 0; i < n; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; ++k) {
+                const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+            const double dz = p1 / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-15) break;
+        }
+        x[i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+// the visible-normal integral of g over m for direction wi (wi.z > 0)
+template <typename G>
+double rp_visible_integral(const double wi[3], double alpha, const std::vector<double> &gx,
+                           const std::vector<double> &gw, int n_phi, G g) {
+    const double tmax = std::atan(6.0 * alpha);
+    double sum = 0.0;
+    for (size_t i = 0; i < gx.size(); ++i) {
+        const double th = 0.5 * tmax * (gx[i] + 1.0), wth = 0.5 * tmax * gw[i];
+        const double st = std::sin(th), ct = std::cos(th), t = st / ct;
+        const double D = std::exp(-(t * t) / (alpha * alpha)) / (M_PI * alpha * alpha * ct * ct * ct * ct);
+        for (int j = 0; j < n_phi; ++j) {
+            const double ph = 2.0 * M_PI * (j + 0.5) / n_phi;
+            const double m[3] = {st * std::cos(ph), st * std::sin(ph), ct};
+            const double dm = wi[0] * m[0] + wi[1] * m[1] + wi[2] * m[2];
+            if (dm <= 0.0) continue;
+            const double dvis = rp_g1(wi, m, alpha) * dm * D / wi[2];
+            sum += dvis * g(m, dm) * st * wth * (2.0 * M_PI / n_phi);
+        }
+    }
+    return sum;
+}
+}  // namespace
+
+static void roughplastic_tables(double eta, double alpha, float table[kRoughPlasticRes], float &fdr) {
+    std::vector<double> gx, gw;
+    gauss_legendre(128, gx, gw);
+    const int n_phi = 128;
+    double rsum = 0.0;
+    for (int i = 0; i < kRoughPlasticRes; ++i) {
+        const double mu = std::max(1e-6, (double)i / (kRoughPlasticRes - 1));
+        const double wi[3] = {std::sqrt(1.0 - mu * mu), 0.0, mu};
+        // external transmittance: refraction into the coating, G1 of the refracted direction
+        const double T = rp_visible_integral(wi, alpha, gx, gw, n_phi, [&](const double m[3], double dm) {
+            double ct, eta_ti;
+            const double F = rp_fresnel(dm, eta, ct, eta_ti);
+            const double k = dm * eta_ti + ct;
+            const double wt[3] = {m[0] * k - wi[0] * eta_ti, m[1] * k - wi[1] * eta_ti, m[2] * k - wi[2] * eta_ti};
+            return wt[2] * wi[2] >= 0.0 ? 0.0 : rp_g1(wt, m, alpha) * (1.0 - F);
+        });
+        // internal reflectance (eta inverted), G1 of the reflected direction
+        const double R = rp_visible_integral(wi, alpha, gx, gw, n_phi, [&](const double m[3], double dm) {
+            double ct, eta_ti;
+            const double F = rp_fresnel(dm, 1.0 / eta, ct, eta_ti);
+            const double wo[3] = {2.0 * dm * m[0] - wi[0], 2.0 * dm * m[1] - wi[1], 2.0 * dm * m[2] - wi[2]};
+            return wo[2] <= 0.0 ? 0.0 : rp_g1(wo, m, alpha) * F;
+        });
+        table[i] = (float)T;
+        rsum += R * mu;
+    }
+    fdr = (float)(rsum / kRoughPlasticRes * 2.0);
+}
+
 static sms_status check_bsdf(const sms_bsdf *b) {
     if (!b) return fail(SMS_ERR_INVALID_ARG, "null bsdf");
-    if (b->type < SMS_BSDF_DIFFUSE || b->type > SMS_BSDF_CONDUCTOR)
+    if (b->type < SMS_BSDF_DIFFUSE || b->type > SMS_BSDF_ROUGHPLASTIC)
         return fail(SMS_ERR_INVALID_ARG, "unknown bsdf type");
+    if (b->type == SMS_BSDF_ROUGHPLASTIC && !(b->eta > 0.f && b->eta != 1.f && b->alpha > 0.f))
+        return fail(SMS_ERR_INVALID_ARG, "roughplastic needs eta > 0, eta != 1 and alpha > 0");
     if (b->type == SMS_BSDF_DIELECTRIC && !(b->eta > 0.f))
         return fail(SMS_ERR_INVALID_ARG, "dielectric eta must be positive");
     if (!(b->alpha >= 0.f) || !std::isfinite(b->alpha))
@@ -513,6 +615,16 @@ static sms_status ctx_build(sms_ctx *c, const sms_scene *s) {
         ds.albedo[0] = h.bsdf.albedo[0]; ds.albedo[1] = h.bsdf.albedo[1]; ds.albedo[2] = h.bsdf.albedo[2];
         ds.alpha = h.bsdf.type == SMS_BSDF_DIFFUSE ? 0.f : h.bsdf.alpha;
         ds.twosided = h.bsdf.twosided ? 1 : 0;
+        if (h.bsdf.type == SMS_BSDF_ROUGHPLASTIC) {
+            if (h.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI |
+                           SMS_SHAPE_CAUSTIC_BOUNCER | SMS_SHAPE_GLINTY))
+                return fail(SMS_ERR_UNSUPPORTED, "a roughplastic shape cannot be a caustic caster, bouncer or glinty");
+            roughplastic_tables(h.bsdf.eta, h.bsdf.alpha, ds.rp_t, ds.rp_fdr);
+            // specular sampling weight: s_mean / (d_mean + s_mean), s_mean = 1
+            const float d_mean = (h.bsdf.albedo[0] + h.bsdf.albedo[1] + h.bsdf.albedo[2]) / 3.f;
+            ds.rp_ws = 1.f / (d_mean + 1.f);
+            ds.rp_nonlinear = h.bsdf.nonlinear ? 1 : 0;
+        }
         ds.nmap_frames = ((int)i == s->nmap_shape && s->nmap_res > 0 &&
                           (h.flags & (SMS_SHAPE_CAUSTIC_CASTER_SINGLE | SMS_SHAPE_CAUSTIC_CASTER_MULTI |
                                       SMS_SHAPE_CAUSTIC_BOUNCER))) ? 1 : 0;

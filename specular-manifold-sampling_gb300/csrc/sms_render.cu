@@ -346,10 +346,57 @@ SMS_D float rough_pdf(const DevShape &s, f3 wi, f3 wo) {
     return (1.f - F) * pm * eta * eta * fabsf(dot(wo, m)) / (den * den);
 }
 
+// ------------------------------------------------------------ roughplastic
+// roughplastic.cpp:185-353: a Beckmann-rough dielectric coating (eta) over a
+// diffuse base.  The external transmittance t(cos) is the tabulated integral
+// (lerp_gather, :301-310); the base's internal scattering divides its albedo
+// by 1 - Fdr (or 1 - albedo Fdr, nonlinear).  The coating's normals are drawn
+// with density D(m) cos(theta_m) like the other rough BSDFs here (the
+// reference's sample_visible = false branch of pdf, :346-348).
+SMS_D float rp_transmittance(const DevShape &s, float c) {
+    float x = c * (float)(kRoughPlasticRes - 1);
+    const int i = min((int)x, kRoughPlasticRes - 2);
+    const float v0 = s.rp_t[i], v1 = s.rp_t[i + 1];
+    return v0 + (v1 - v0) * (x - (float)i);
+}
+
+// the probability of sampling the coating's specular lobe at cos theta_i
+SMS_D float rp_prob_specular(const DevShape &s, float ci) {
+    const float t_i = rp_transmittance(s, ci);
+    const float ps = (1.f - t_i) * s.rp_ws, pd = t_i * (1.f - s.rp_ws);
+    return ps / (ps + pd);
+}
+
+SMS_D f3 roughplastic_eval(const DevShape &s, f3 wi, f3 wo) {
+    const float ci = wi.z, co = wo.z;
+    if (!(ci > 0.f && co > 0.f)) return splat(0.f);
+    const f3 h = normalize(wo + wi);
+    const float F = fresnel_dielectric(dot(wi, h), s.eta);
+    const float G = beckmann_G1(wi, h, s.alpha) * beckmann_G1(wo, h, s.alpha);
+    const float spec = F * beckmann_D(h, s.alpha) * G / (4.f * ci);
+    const float t_i = rp_transmittance(s, ci), t_o = rp_transmittance(s, co);
+    f3 diff = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
+    if (s.rp_nonlinear)
+        diff = mk(diff.x / (1.f - diff.x * s.rp_fdr), diff.y / (1.f - diff.y * s.rp_fdr),
+                  diff.z / (1.f - diff.z * s.rp_fdr));
+    else
+        diff = diff * (1.f / (1.f - s.rp_fdr));
+    return splat(spec) + diff * (kInvPi * (1.f / (s.eta * s.eta)) * co * t_i * t_o);
+}
+
+SMS_D float roughplastic_pdf(const DevShape &s, f3 wi, f3 wo) {
+    const float ci = wi.z, co = wo.z;
+    if (!(ci > 0.f && co > 0.f)) return 0.f;
+    const float ps = rp_prob_specular(s, ci);
+    const f3 h = normalize(wo + wi);
+    return beckmann_D(h, s.alpha) * h.z / (4.f * dot(wo, h)) * ps + (1.f - ps) * kInvPi * co;
+}
+
 // BSDF value x |cos(theta_o)| of the BSDFs emitter sampling evaluates:
 // diffuse (diffuse.cpp eval) and rough (roughconductor.cpp,
 // roughdielectric.cpp eval); delta BSDFs give 0.
 SMS_D f3 bsdf_eval(const DevShape &s, f3 wi, f3 wo) {
+    if (s.bsdf_type == kBsdfRoughPlastic) return roughplastic_eval(s, wi, wo);
     if (s.bsdf_type == kBsdfDiffuse) {
         if (!(wi.z > 0.f && wo.z > 0.f)) return splat(0.f);
         return mk(s.albedo[0], s.albedo[1], s.albedo[2]) * (kInvPi * wo.z);
@@ -360,6 +407,7 @@ SMS_D f3 bsdf_eval(const DevShape &s, f3 wi, f3 wo) {
 }
 
 SMS_D float bsdf_pdf(const DevShape &s, f3 wi, f3 wo) {
+    if (s.bsdf_type == kBsdfRoughPlastic) return roughplastic_pdf(s, wi, wo);
     if (s.bsdf_type == kBsdfDiffuse) return (wi.z > 0.f && wo.z > 0.f) ? kInvPi * wo.z : 0.f;
     return s.alpha > 0.f ? rough_pdf(s, wi, wo) : 0.f;
 }
@@ -401,6 +449,23 @@ SMS_D bool rough_sample(const DevShape &s, f3 wi, float u1, float u2, float u3, 
 // zero weight.
 SMS_D bool bsdf_sample(const DevShape &s, f3 wi, float u1, float u2, float u3, BsdfSample &bs) {
     const float ci = wi.z;
+    if (s.bsdf_type == kBsdfRoughPlastic) {
+        // roughplastic.cpp:185-241: the coating's lobe or the base's cosine lobe
+        if (!(ci > 0.f)) return false;
+        if (u1 < rp_prob_specular(s, ci)) {
+            float pm;
+            const f3 m = beckmann_sample(s.alpha, u2, u3, pm);
+            bs.wo = m * (2.f * dot(wi, m)) - wi;
+        } else {
+            bs.wo = cosine_hemisphere(u2, u3);
+        }
+        bs.delta = false;
+        bs.eta = 1.f;
+        bs.pdf = roughplastic_pdf(s, wi, bs.wo);
+        if (!(bs.pdf > 0.f)) return false;
+        bs.weight = roughplastic_eval(s, wi, bs.wo) * (1.f / bs.pdf);
+        return true;
+    }
     if (s.bsdf_type != kBsdfDiffuse && s.alpha > 0.f) return rough_sample(s, wi, u1, u2, u3, bs);
     if (s.bsdf_type == kBsdfDiffuse) {
         if (!(ci > 0.f)) return false;
@@ -621,7 +686,8 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             // i.e. after the camera's first hit (normalmap.cpp:80, 142, 187)
             const bool lean_fb = nmapped && sc.lean_fb;
             const bool lean_now = lean_fb && depth > 1;
-            const bool smooth = (!nmapped && (diffuse || s.alpha > 0.f)) || lean_fb;   // BSDFFlags::Smooth
+            const bool smooth =
+                (!nmapped && (diffuse || s.alpha > 0.f || s.bsdf_type == kBsdfRoughPlastic)) || lean_fb;   // BSDFFlags::Smooth
             const bool on_glinty = (P.integrator == SMS_INTEGRATOR_PATH_SMS_GLINTS || (teaser && P.glints_enabled)) &&
                                    depth == 1 && nmapped && (s.flags & kShapeFlagGlinty);
             const bool glint_pass = !teaser || P.teaser_pass == 2;

@@ -16,7 +16,9 @@ silently half-loaded):
       nested <bsdf>: dielectric (int_ior / ext_ior, names from
       include/mitsuba/render/ior.h), conductor (eta, k), diffuse (reflectance),
       roughdielectric / roughconductor (isotropic Beckmann alpha),
-      twosided around one diffuse or conductor bsdf (src/bsdfs/twosided.cpp),
+      roughplastic (int_ior / ext_ior, diffuse_reflectance, Beckmann alpha,
+      nonlinear), twosided around one diffuse, conductor or roughplastic bsdf
+      (src/bsdfs/twosided.cpp),
       normalmap around any of these (filename of an OpenEXR or PNG RGB normal
       map, tiles, lean_fallback with lean_fallback_alpha and grey eta / k;
       src/bsdfs/normalmap.cpp:24-58; one normal-mapped shape per scene); a
@@ -249,6 +251,18 @@ def _bsdf(sms, el, refs=None):
         return sms.Bsdf(sms.BSDF_CONDUCTOR, float(np.mean(eta)), float(np.mean(k)), alpha=alpha)
     if t == "diffuse":
         return sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, _spectrum(p, "reflectance", (0.5,) * 3))
+    if t == "roughplastic":
+        # roughplastic.cpp:148-183: isotropic Beckmann coating over a diffuse base
+        dist = p["distribution"][1].get("value").lower() if "distribution" in p else "beckmann"
+        if dist != "beckmann":
+            raise ValueError(f"microfacet distribution '{dist}' is not supported (beckmann only)")
+        if "alpha_u" in p or "alpha_v" in p:
+            raise ValueError("anisotropic roughness (alpha_u / alpha_v) is not supported")
+        if "specular_reflectance" in p and _spectrum(p, "specular_reflectance", (1.0,) * 3) != (1.0, 1.0, 1.0):
+            raise ValueError("roughplastic specular_reflectance other than 1 is not supported")
+        eta = _float(p, "int_ior", 1.49) / _float(p, "ext_ior", 1.000277)
+        return sms.Bsdf(sms.BSDF_ROUGHPLASTIC, eta, 0.0, _spectrum(p, "diffuse_reflectance", (0.5,) * 3),
+                        alpha=_float(p, "alpha", 0.1), nonlinear=_bool(p, "nonlinear"))
     raise ValueError(f"unsupported bsdf type '{t}'")
 
 

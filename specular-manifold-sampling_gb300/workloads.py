@@ -453,15 +453,16 @@ def lean_fallback_camera(width: int = 32, height: int = 32):
     return Camera.look_at((0.0, 1.2, 0.6), (0.0, -0.6, 0.4), (0.0, 0.0, 1.0), 45.0, width, height)
 
 
-def plane_light_scene(below: bool, twosided: bool, width: int = 16, height: int = 16):
-    """(SceneDesc, Camera): a diffuse plane z = 0 (normal +z, twosided or not)
-    lit by a sphere light outside the camera's view, light and camera both
-    above the plane or both below it (looking at its back)."""
+def plane_light_scene(below: bool, twosided: bool, width: int = 16, height: int = 16, bsdf=None):
+    """(SceneDesc, Camera): a plane z = 0 (normal +z, twosided or not; diffuse
+    unless a Bsdf is given) lit by a sphere light outside the camera's view,
+    light and camera both above the plane or both below it (looking at its
+    back)."""
     from . import Camera
     d = SceneDesc()
     fl = np.array([[-3, -3, 0], [3, -3, 0], [3, 3, 0], [-3, 3, 0]], np.float32)
     d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32),
-               Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.6,) * 3, twosided=twosided))
+               bsdf if bsdf is not None else Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.6,) * 3, twosided=twosided))
     z = -2.0 if below else 2.0
     light = d.add_sphere((1.5, 0.0, z), 0.3, Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (0.0,) * 3), 0)
     d.add_area_emitter(light, (30.0,) * 3, 0)

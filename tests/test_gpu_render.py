@@ -293,6 +293,38 @@ def test_twosided_matches_oracle(sms, workloads, oracle, gpu_lib):
     ctx.close()
 
 
+@pytest.mark.parametrize("nonlinear", [False, True])
+def test_roughplastic_matches_oracle(sms, workloads, oracle, gpu_lib, nonlinear):
+    """A roughplastic plane (roughplastic.cpp: Beckmann coating over a diffuse
+    base) lit by a sphere light in view of its glossy lobe, GPU vs the oracle.
+    The library tabulates the coating's transmittance by its own quadrature,
+    the oracle by the reference's; they agree to about 1e-3."""
+    b = sms.Bsdf(sms.BSDF_ROUGHPLASTIC, 1.49 / 1.000277, 0.0, (0.2, 0.5, 0.8), alpha=0.15, nonlinear=nonlinear)
+    d, cam = workloads.plane_light_scene(below=False, twosided=False, width=24, height=24, bsdf=b)
+    g, o, f = _check_against_oracle(sms, oracle, d, sms.SMSConfig(), cam,
+                                    sms.RenderOptions(integrator="path", spp=16, seed=6))
+    assert o.mean() > 0.01
+    assert abs(g.mean() - o.mean()) < 0.02 * o.mean()
+
+
+def test_roughplastic_refused_on_the_caustic_path(sms, gpu_lib):
+    """A roughplastic shape cannot be a caustic caster (the manifold walks
+    need a smooth dielectric or conductor)."""
+    def scene(caster_bsdf):
+        d = sms.SceneDesc()
+        q = np.array([[-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], np.float32)
+        d.add_mesh(q, np.array([[0, 1, 2], [0, 2, 3]], np.uint32), caster_bsdf, sms.SHAPE_CAUSTIC_CASTER_SINGLE)
+        d.add_mesh(q * np.float32([3, 3, 0]), np.array([[0, 1, 2], [0, 2, 3]], np.uint32),
+                   sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5,) * 3), sms.SHAPE_CAUSTIC_RECEIVER)
+        light = d.add_sphere((0, 0, 5), 0.3, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.0,) * 3), 0)
+        d.add_area_emitter(light, (10.0,) * 3, sms.EMITTER_CAUSTIC_SINGLE)
+        return sms.Scene(d)
+
+    sms.Context(scene(sms.Bsdf(sms.BSDF_DIELECTRIC, 1.5)), sms.SMSConfig()).close()
+    with pytest.raises(sms.SMSError, match="roughplastic"):
+        sms.Context(scene(sms.Bsdf(sms.BSDF_ROUGHPLASTIC, 1.5, 0.0, (0.5,) * 3, alpha=0.1)), sms.SMSConfig())
+
+
 def _teaser_area_light(sms, W):
     """The teaser stand-in with its point light replaced by a sphere area light
     flagged for single- and multi-scatter caustics, so that path tracing can

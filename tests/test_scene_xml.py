@@ -274,3 +274,29 @@ def test_rough_bsdfs_from_xml(sms, tmp_path):
     b0, b1 = desc.spheres[0][3], desc.spheres[1][3]
     assert b0.type == sms.BSDF_DIELECTRIC and b0.alpha == pytest.approx(0.3) and b0.eta == pytest.approx(1.5)
     assert b1.type == sms.BSDF_CONDUCTOR and b1.alpha == pytest.approx(0.05)
+
+
+def test_roughplastic_bsdf_from_xml(sms, tmp_path):
+    """<bsdf type="roughplastic"> (roughplastic.cpp:148-183): defaults
+    polypropylene in air, alpha 0.1, diffuse_reflectance 0.5; Beckmann only;
+    twosided may wrap it."""
+    body = '''<scene version="2.0.0">
+      <shape type="rectangle"><bsdf type="roughplastic"/></shape>
+      <shape type="rectangle"><bsdf type="twosided"><bsdf type="roughplastic">
+        <float name="alpha" value="0.3"/><float name="int_ior" value="1.5"/><float name="ext_ior" value="1.0"/>
+        <rgb name="diffuse_reflectance" value="0.1, 0.2, 0.3"/><boolean name="nonlinear" value="true"/>
+      </bsdf></bsdf></shape>
+    </scene>'''
+    (tmp_path / "t.xml").write_text(body)
+    desc, _, _ = sms.load_scene(tmp_path / "t.xml")
+    b0, b1 = desc.meshes[0][4], desc.meshes[1][4]
+    assert b0.type == sms.BSDF_ROUGHPLASTIC and b0.alpha == pytest.approx(0.1)
+    assert b0.eta == pytest.approx(1.49 / 1.000277) and b0.albedo == (0.5, 0.5, 0.5) and not b0.nonlinear
+    assert b1.twosided and b1.nonlinear and b1.alpha == pytest.approx(0.3) and b1.eta == pytest.approx(1.5)
+    assert b1.albedo == (0.1, 0.2, 0.3)
+    sms.Scene(desc)
+    (tmp_path / "g.xml").write_text(body.replace('<bsdf type="roughplastic"/>',
+                                                 '<bsdf type="roughplastic"><string name="distribution" '
+                                                 'value="ggx"/></bsdf>'))
+    with pytest.raises(ValueError, match="beckmann"):
+        sms.load_scene(tmp_path / "g.xml")

@@ -239,7 +239,16 @@ sms_status sms_ctx_set_queue_chunk(sms_ctx *ctx, int32_t chunk);
  *   row 3-5   n        shading normal (= geometric normal of the receiver)
  *   row 6-8   dp_du    position partial
  *   row 9-11  dp_dv    position partial
- *   row 12-14 albedo   diffuse reflectance of the receiver (RGB)
+ *   row 12-14 albedo   diffuse reflectance of the receiver (RGB, >= 0), or,
+ *                      for a receiver with any other BSDF: row 12 =
+ *                      -(1 + shape id) of the receiver shape (its index among
+ *                      the scene's shapes), rows 13-14 = x, y of the incident
+ *                      (camera) direction in the frame built from n by the
+ *                      branchless orthonormal basis of Duff et al. 2017; the
+ *                      library then evaluates that shape's BSDF toward the
+ *                      caster (manifold_ss.cpp:109, 191); an id outside the
+ *                      scene contributes 0 and the call returns
+ *                      SMS_ERR_DEVICE_LIMIT
  *   row 15    cos_i    cosine of the incident (camera) direction in the local
  *                      frame; the diffuse BSDF returns 0 when it is <= 0
  * The receiver is taken as locally flat (dn/du = dn/dv = 0), as for the

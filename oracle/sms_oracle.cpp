@@ -1319,6 +1319,21 @@ static V3 diffuse_eval(const Query &q, V3 dir) {
     return (q.albedo * kInvPi) * co;
 }
 
+/* The receiver's BSDF toward the first specular vertex (manifold_ss.cpp:109,
+ * 191; manifold_ms.cpp:113, 190): a query with albedo.x >= 0 is a diffuse
+ * receiver; albedo.x = -(1 + shape id) names a receiver shape whose BSDF is
+ * evaluated in the frame coordinate_system(n) with the incident direction
+ * (albedo.y, albedo.z, cos_i). */
+static V3 shape_bsdf_eval(const Shape &sh, V3 wi, V3 wo);
+static V3 receiver_eval(const Scene &sc, const Query &q, V3 dir) {
+    if (q.albedo.x >= 0.f) return diffuse_eval(q, dir);
+    const int id = (int)(-q.albedo.x) - 1;
+    if (id < 0 || id >= (int)sc.shapes.size()) return V3(0.f);
+    V3 s, t;
+    coordinate_system(q.n, s, t);
+    return shape_bsdf_eval(sc.shapes[id], V3(q.albedo.y, q.albedo.z, q.cos_i), V3(dot(dir, s), dot(dir, t), dot(dir, q.n)));
+}
+
 static bool visible(const Scene &sc, const EI &ei, V3 p) {
     V3 d = p - ei.p;
     Float dist = norm(d);
@@ -1419,7 +1434,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             V3 direction = normalize(si_final.p - q.p);
             if (!visible(sc, ei, si_final.p)) continue;
             V3 spec = evaluate_path_contribution(sc, q, ei, si_final);
-            V3 bsdf = diffuse_eval(q, direction);
+            V3 bsdf = receiver_eval(sc, q, direction);
             Float inv_prob = 1.f;
             int iterations = 1;
             st.calls++;
@@ -1459,7 +1474,7 @@ static V3 ss_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
                     if (std::fabs(dot(direction, s) - 1.f) < cfg.uniqueness_threshold) { dup = true; break; }
                 if (dup) continue;
                 solutions.push_back(direction);
-                V3 bsdf = diffuse_eval(q, direction);
+                V3 bsdf = receiver_eval(sc, q, direction);
                 V3 spec = evaluate_path_contribution(sc, q, ei, si_final);
                 value += bsdf * spec;
             }
@@ -2005,7 +2020,7 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
             st.succeeded++;
             V3 direction = normalize(path[0].p - q.p);
             V3 spec = ms_contribution(sc, q, ei, path);
-            V3 bsdf = diffuse_eval(q, direction);
+            V3 bsdf = receiver_eval(sc, q, direction);
             Float inv_prob = 1.f;
             int iterations = 1;
             st.calls++;
@@ -2042,7 +2057,7 @@ static V3 ms_connect(const Scene &sc, const sms_config &cfg, const Query &q, PCG
                     if (std::fabs(dot(direction, s) - 1.f) < cfg.uniqueness_threshold) { dup = true; break; }
                 if (dup) continue;
                 solutions.push_back(direction);
-                V3 bsdf = diffuse_eval(q, direction);
+                V3 bsdf = receiver_eval(sc, q, direction);
                 V3 spec = ms_contribution(sc, q, ei, path);
                 value += bsdf * spec;
             }
@@ -3298,7 +3313,17 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         /* the teaser's caustics at a receiver (path_sms_teaser.cpp:152-162):
            single scatter if depth + 1 < max_depth, multi scatter if depth +
            bounces < max_depth, both with cfg */
-        if (teaser && opt.caustics_enabled && receiver && diffuse) {
+        /* any receiver whose BSDF has a non-delta lobe takes SMS queries
+           (path_sms_ss.cpp:120-124; a delta BSDF's eval toward the chain is
+           zero); a diffuse one passes its albedo, any other its shape and
+           the incident direction in the frame coordinate_system(n_sh) */
+        const bool sms_receiver = receiver && smooth && !nmapped;
+        if (!diffuse) {
+            V3 os, ot;
+            coordinate_system(n_sh, os, ot);
+            albedo = V3(-1.f - (Float)si.shape, dot(wiw, os), dot(wiw, ot));
+        }
+        if (teaser && opt.caustics_enabled && sms_receiver) {
             Query q;
             q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;
             int c = 0, w = 0;
@@ -3315,7 +3340,7 @@ static V3 pt_sample(const Scene &sc, const sms_config &cfg, const sms_camera &ca
         }
         /* SMS at a receiver (path_sms_ss.cpp:115-121, path_sms_ms.cpp:226-232) */
         if (integ != SMS_INTEGRATOR_PATH && !teaser && !filtered_ss && !filtered_ms && !filtered_teaser && receiver &&
-            !on_caster && diffuse &&
+            !on_caster && sms_receiver &&
             (opt.max_depth < 0 || depth + bounces < opt.max_depth)) {
             Query q;
             q.p = si.p; q.n = n_sh; q.dp_du = si.dp_du; q.dp_dv = si.dp_dv; q.albedo = albedo; q.cos_i = wi.z;

@@ -77,6 +77,7 @@ constexpr int kMaxLeanLevels = 20;
 constexpr uint32_t kErrStackOverflow = 1u;
 constexpr uint32_t kErrTrialLimit = 2u;
 constexpr uint32_t kErrSolutionOverflow = 4u;
+constexpr uint32_t kErrBadQuery = 8u;   // a query names a receiver shape outside the scene
 
 // ------------------------------------------------------------------- vectors
 struct f3 { float x, y, z; };

@@ -183,6 +183,70 @@ SMS_D f3 diffuse_eval(const Query &Q, f3 dir) {
     return (Q.albedo * kInvPi) * co;
 }
 
+// ------------------------------------------------------------ roughplastic
+// roughplastic.cpp:185-353: a Beckmann-rough dielectric coating (eta) over a
+// diffuse base.  The external transmittance t(cos) is the tabulated integral
+// (lerp_gather, :301-310); the base's internal scattering divides its albedo
+// by 1 - Fdr (or 1 - albedo Fdr, nonlinear).  The coating's normals are drawn
+// with density D(m) cos(theta_m) like the other rough BSDFs here (the
+// reference's sample_visible = false branch of pdf, :346-348).
+SMS_D float rp_transmittance(const DevShape &s, float c) {
+    float x = c * (float)(kRoughPlasticRes - 1);
+    const int i = min((int)x, kRoughPlasticRes - 2);
+    const float v0 = s.rp_t[i], v1 = s.rp_t[i + 1];
+    return v0 + (v1 - v0) * (x - (float)i);
+}
+
+SMS_D f3 roughplastic_eval(const DevShape &s, f3 wi, f3 wo) {
+    const float ci = wi.z, co = wo.z;
+    if (!(ci > 0.f && co > 0.f)) return splat(0.f);
+    const f3 h = normalize(wo + wi);
+    const float F = fresnel_dielectric(dot(wi, h), s.eta);
+    const float G = beckmann_G1(wi, h, s.alpha) * beckmann_G1(wo, h, s.alpha);
+    const float spec = F * beckmann_D(h, s.alpha) * G / (4.f * ci);
+    const float t_i = rp_transmittance(s, ci), t_o = rp_transmittance(s, co);
+    f3 diff = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
+    if (s.rp_nonlinear)
+        diff = mk(diff.x / (1.f - diff.x * s.rp_fdr), diff.y / (1.f - diff.y * s.rp_fdr),
+                  diff.z / (1.f - diff.z * s.rp_fdr));
+    else
+        diff = diff * (1.f / (1.f - s.rp_fdr));
+    return splat(spec) + diff * (kInvPi * (1.f / (s.eta * s.eta)) * co * t_i * t_o);
+}
+
+// BSDF value x |cos(theta_o)| of the BSDFs emitter sampling and receivers
+// evaluate: diffuse (diffuse.cpp eval), rough (roughconductor.cpp,
+// roughdielectric.cpp eval) and roughplastic; delta BSDFs give 0.
+SMS_D f3 bsdf_eval(const DevShape &s, f3 wi, f3 wo) {
+    if (s.bsdf_type == kBsdfRoughPlastic) return roughplastic_eval(s, wi, wo);
+    if (s.bsdf_type == kBsdfDiffuse) {
+        if (!(wi.z > 0.f && wo.z > 0.f)) return splat(0.f);
+        return mk(s.albedo[0], s.albedo[1], s.albedo[2]) * (kInvPi * wo.z);
+    }
+    if (!(s.alpha > 0.f)) return splat(0.f);
+    return splat(s.bsdf_type == kBsdfConductor ? roughconductor_eval(s.alpha, s.eta, s.k, wi, wo)
+                                               : roughdielectric_eval(s.alpha, s.eta, wi, wo));
+}
+
+// The receiver's BSDF toward the first specular vertex (manifold_ss.cpp:109,
+// 191; manifold_ms.cpp:113, 190).  A query whose row 12 is >= 0 is a diffuse
+// receiver with that albedo (diffuse_eval, unchanged).  A negative row 12 is
+// -(1 + shape id) of the receiver shape, whose BSDF is evaluated in the frame
+// onb(n) with the incident direction (row 13, row 14, cos_i); the isotropic
+// BSDFs here depend on the frame's normal only.  An id outside the scene
+// contributes nothing and raises the invalid-query error bit.
+SMS_D f3 receiver_eval(const DevScene &sc, const Query &Q, f3 dir, uint32_t &err) {
+    if (Q.albedo.x >= 0.f) return diffuse_eval(Q, dir);
+    const int id = (int)(-Q.albedo.x) - 1;
+    if (!(id >= 0 && id < sc.n_shapes)) {
+        err |= kErrBadQuery;
+        return splat(0.f);
+    }
+    f3 s, t;
+    onb(Q.n, s, t);
+    return bsdf_eval(sc.shapes[id], mk(Q.albedo.y, Q.albedo.z, Q.cos_i), mk(dot(dir, s), dot(dir, t), dot(dir, Q.n)));
+}
+
 // ------------------------------------------------------------------- walk
 // sample_path + newton_solver (manifold_ss.cpp:206-279, 331-405) from an
 // explicit seed point.  Returns ok; v holds the solution vertex.

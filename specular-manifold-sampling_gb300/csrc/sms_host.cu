@@ -865,6 +865,7 @@ sms_status ctx_check_device_error(sms_ctx *c) {
         if (err & kErrStackOverflow) m += " BVH traversal stack overflow;";
         if (err & kErrTrialLimit) m += " Bernoulli trials exceeded the hard limit;";
         if (err & kErrSolutionOverflow) m += " more unique solutions than the per-query capacity;";
+        if (err & kErrBadQuery) m += " a query names a receiver shape outside the scene;";
         return fail(SMS_ERR_DEVICE_LIMIT, m);
     }
     return SMS_OK;

@@ -752,7 +752,7 @@ __global__ void __launch_bounds__(128, SMS_MS_BIASED_MIN_BLOCKS) ms_biased_kerne
                 }
                 f3 contrib = splat(0.f);
                 if (keep)
-                    contrib = diffuse_eval(Q, dir) * chain_contribution<K, kNM, kRough>(sc, Q.x, L, c, err, st);
+                    contrib = receiver_eval(sc, Q, dir, err) * chain_contribution<K, kNM, kRough>(sc, Q.x, L, c, err, st);
                 // sum in walk order
                 for (int k = 0; k < G; ++k) {
                     const int src = gbase + k;
@@ -835,7 +835,7 @@ __global__ void __launch_bounds__(128) ms_first_kernel(DevScene sc, SolverCfg cf
                 st.succ++;
                 f3 dir = normalize(c.v[0].p - Q.x);
                 f3 spec = chain_contribution<K, kNM, kRough>(sc, Q.x, L, c, err, st);
-                f3 val = diffuse_eval(Q, dir) * spec;
+                f3 val = receiver_eval(sc, Q, dir, err) * spec;
                 scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;
                 scr.val[qi] = val.x; scr.val[(size_t)n + qi] = val.y; scr.val[2 * (size_t)n + qi] = val.z;
                 #pragma unroll

@@ -347,41 +347,13 @@ SMS_D float rough_pdf(const DevShape &s, f3 wi, f3 wo) {
 }
 
 // ------------------------------------------------------------ roughplastic
-// roughplastic.cpp:185-353: a Beckmann-rough dielectric coating (eta) over a
-// diffuse base.  The external transmittance t(cos) is the tabulated integral
-// (lerp_gather, :301-310); the base's internal scattering divides its albedo
-// by 1 - Fdr (or 1 - albedo Fdr, nonlinear).  The coating's normals are drawn
-// with density D(m) cos(theta_m) like the other rough BSDFs here (the
-// reference's sample_visible = false branch of pdf, :346-348).
-SMS_D float rp_transmittance(const DevShape &s, float c) {
-    float x = c * (float)(kRoughPlasticRes - 1);
-    const int i = min((int)x, kRoughPlasticRes - 2);
-    const float v0 = s.rp_t[i], v1 = s.rp_t[i + 1];
-    return v0 + (v1 - v0) * (x - (float)i);
-}
-
+// roughplastic_eval, its transmittance table and bsdf_eval are shared with the
+// estimators' receiver evaluation (sms_estimator.cuh).
 // the probability of sampling the coating's specular lobe at cos theta_i
 SMS_D float rp_prob_specular(const DevShape &s, float ci) {
     const float t_i = rp_transmittance(s, ci);
     const float ps = (1.f - t_i) * s.rp_ws, pd = t_i * (1.f - s.rp_ws);
     return ps / (ps + pd);
-}
-
-SMS_D f3 roughplastic_eval(const DevShape &s, f3 wi, f3 wo) {
-    const float ci = wi.z, co = wo.z;
-    if (!(ci > 0.f && co > 0.f)) return splat(0.f);
-    const f3 h = normalize(wo + wi);
-    const float F = fresnel_dielectric(dot(wi, h), s.eta);
-    const float G = beckmann_G1(wi, h, s.alpha) * beckmann_G1(wo, h, s.alpha);
-    const float spec = F * beckmann_D(h, s.alpha) * G / (4.f * ci);
-    const float t_i = rp_transmittance(s, ci), t_o = rp_transmittance(s, co);
-    f3 diff = mk(s.albedo[0], s.albedo[1], s.albedo[2]);
-    if (s.rp_nonlinear)
-        diff = mk(diff.x / (1.f - diff.x * s.rp_fdr), diff.y / (1.f - diff.y * s.rp_fdr),
-                  diff.z / (1.f - diff.z * s.rp_fdr));
-    else
-        diff = diff * (1.f / (1.f - s.rp_fdr));
-    return splat(spec) + diff * (kInvPi * (1.f / (s.eta * s.eta)) * co * t_i * t_o);
 }
 
 SMS_D float roughplastic_pdf(const DevShape &s, f3 wi, f3 wo) {
@@ -390,20 +362,6 @@ SMS_D float roughplastic_pdf(const DevShape &s, f3 wi, f3 wo) {
     const float ps = rp_prob_specular(s, ci);
     const f3 h = normalize(wo + wi);
     return beckmann_D(h, s.alpha) * h.z / (4.f * dot(wo, h)) * ps + (1.f - ps) * kInvPi * co;
-}
-
-// BSDF value x |cos(theta_o)| of the BSDFs emitter sampling evaluates:
-// diffuse (diffuse.cpp eval) and rough (roughconductor.cpp,
-// roughdielectric.cpp eval); delta BSDFs give 0.
-SMS_D f3 bsdf_eval(const DevShape &s, f3 wi, f3 wo) {
-    if (s.bsdf_type == kBsdfRoughPlastic) return roughplastic_eval(s, wi, wo);
-    if (s.bsdf_type == kBsdfDiffuse) {
-        if (!(wi.z > 0.f && wo.z > 0.f)) return splat(0.f);
-        return mk(s.albedo[0], s.albedo[1], s.albedo[2]) * (kInvPi * wo.z);
-    }
-    if (!(s.alpha > 0.f)) return splat(0.f);
-    return splat(s.bsdf_type == kBsdfConductor ? roughconductor_eval(s.alpha, s.eta, s.k, wi, wo)
-                                               : roughdielectric_eval(s.alpha, s.eta, wi, wo));
 }
 
 SMS_D float bsdf_pdf(const DevShape &s, f3 wi, f3 wo) {
@@ -745,18 +703,30 @@ __global__ void __launch_bounds__(kPtBlock) pt_bounce_kernel(DevScene sc, PtPara
             // teaser's caustics (path_sms_teaser.cpp:152-162): single scatter
             // if depth + 1 < max_depth (pass 0), multi scatter if depth +
             // bounces < max_depth (pass 1)
+            // any receiver whose BSDF has a non-delta lobe takes SMS queries
+            // (path_sms_ss.cpp:120-124 calls the solver at every receiver;
+            // a delta BSDF's eval toward the chain is zero)
+            const bool sms_receiver = receiver && smooth && !nmapped;
             const bool teaser_caustic =
-                teaser && P.caustics_enabled && receiver && diffuse &&
+                teaser && P.caustics_enabled && sms_receiver &&
                 ((P.teaser_pass == 0 && (P.max_depth < 0 || depth + 1 < P.max_depth)) ||
                  (P.teaser_pass == 1 && (P.max_depth < 0 || depth + P.bounces < P.max_depth)));
             if (teaser_caustic ||
                 (!teaser && P.integrator != SMS_INTEGRATOR_PATH && !filtered && !filtered_teaser && receiver &&
-                 !on_caster && diffuse &&
+                 !on_caster && sms_receiver &&
                  (P.max_depth < 0 || depth + P.bounces < P.max_depth))) {
+                // a diffuse receiver passes its albedo; any other names its
+                // shape and the incident direction in the frame onb(n_sh)
+                f3 rx = albedo;
+                if (!diffuse) {
+                    f3 os, ot;
+                    onb(n_sh, os, ot);
+                    rx = mk(-1.f - (float)shape, dot(wiw, os), dot(wiw, ot));
+                }
                 const float row[SMS_QUERY_FIELDS] = {si.p.x, si.p.y, si.p.z, n_sh.x, n_sh.y, n_sh.z,
                                                      si.dp_du.x, si.dp_du.y, si.dp_du.z,
                                                      si.dp_dv.x, si.dp_dv.y, si.dp_dv.z,
-                                                     albedo.x, albedo.y, albedo.z, wi.z};
+                                                     rx.x, rx.y, rx.z, wi.z};
                 #pragma unroll
                 for (int k = 0; k < SMS_QUERY_FIELDS; ++k) S.stage[(size_t)k * S.cap + i] = row[k];
                 S.stage[(size_t)21 * S.cap + i] = thr.x;

@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(128) ss_collect_kernel(DevScene sc, SolverCfg 
         for (int j = 0; j < n_seen; ++j)
             if (fabsf(dot(dir, seen[j]) - 1.f) < cfg.uniqueness_threshold) dup = true;
         if (dup || !visible(sc, L.p, v.p, err, st)) continue;
-        const f3 c = diffuse_eval(Q, dir) * contribution(sc, Q.x, L, v, err, st);
+        const f3 c = receiver_eval(sc, Q, dir, err) * contribution(sc, Q.x, L, v, err, st);
         seen[n_seen] = dir;
         mlp::frame_uv(fr, v.p, kuv[n_seen][0], kuv[n_seen][1]);
         kf[n_seen] = fmaxf(0.f, (c.x + c.y + c.z) * (1.f / 3.f));

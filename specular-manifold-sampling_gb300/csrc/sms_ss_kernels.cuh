@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(128, 4) ss_biased_kernel(DevScene sc, SolverCf
                             dir = normalize(v.p - Q.x);
                             // evaluated for every visible solution; only first
                             // occurrences are kept below
-                            contrib = diffuse_eval(Q, dir) * contribution<kNM>(sc, Q.x, L, v, err, st);
+                            contrib = receiver_eval(sc, Q, dir, err) * contribution<kNM>(sc, Q.x, L, v, err, st);
                         }
                     } else {
                         st.fail++;
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(128, SMS_SS_WALK_MIN_BLOCKS) ss_first_kernel(D
                     f3 dir = normalize(v.p - Q.x);
                     f3 spec = contribution<kNM>(sc, Q.x, L, v, err, st);
                     // the caster's estimate is divided by the offset density (manifold_ss.cpp:199)
-                    f3 val = kRough ? diffuse_eval(Q, dir) * spec * (1.f / p_off) : diffuse_eval(Q, dir) * spec;
+                    f3 val = kRough ? receiver_eval(sc, Q, dir, err) * spec * (1.f / p_off) : receiver_eval(sc, Q, dir, err) * spec;
                     scr.dir0[qi] = dir.x; scr.dir0[(size_t)n + qi] = dir.y; scr.dir0[2 * (size_t)n + qi] = dir.z;
                     scr.val[qi] = val.x; scr.val[(size_t)n + qi] = val.y; scr.val[2 * (size_t)n + qi] = val.z;
                     enqueue = true;

@@ -192,18 +192,21 @@ def water_config() -> SMSConfig:
 
 # ------------------------------------------------------------------- pool
 def pool_scene(res: int = 128, light_radius: float = 0.5, light_z: float = 4.0, radiance: float = 40.0,
-               point_light: bool = False, floor_albedo: float = 0.5, wave_scale: float = 1.0) -> SceneDesc:
+               point_light: bool = False, floor_albedo: float = 0.5, wave_scale: float = 1.0,
+               floor_bsdf=None) -> SceneDesc:
     """Rendering scene: the water heightfield of water_scene with its wave
     amplitudes scaled by wave_scale (0: flat; res x res grid over [-1, 1]^2
     around z = 1, dielectric 1.33, caustic_caster_single) over a
     diffuse floor z = 0 on [-2, 2]^2 (caustic_receiver), lit by a sphere area
     light (or a point light of intensity radiance * light_radius^2 * pi at the
-    same place), flagged caustic_emitter_single."""
+    same place), flagged caustic_emitter_single.  floor_bsdf replaces the
+    floor's diffuse BSDF."""
     d = SceneDesc()
     fl = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)
     fuv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
     d.add_mesh(fl, np.array([[0, 1, 2], [0, 2, 3]], np.uint32),
-               Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (floor_albedo,) * 3), SHAPE_CAUSTIC_RECEIVER, UV=fuv)
+               floor_bsdf if floor_bsdf is not None else Bsdf(BSDF_DIFFUSE, 1.0, 0.0, (floor_albedo,) * 3),
+               SHAPE_CAUSTIC_RECEIVER, UV=fuv)
     waves = [(a * wave_scale, kx, ky, ph) for (a, kx, ky, ph) in water_params()] if wave_scale > 0 else []
     P, N, UV, F = heightfield_mesh(res, 1.0, 1.0, waves)
     d.add_mesh(P, F, Bsdf(BSDF_DIELECTRIC, 1.33), SHAPE_CAUSTIC_CASTER_SINGLE, N=N, UV=UV)

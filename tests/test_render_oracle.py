@@ -49,12 +49,18 @@ def test_unflagged_scene_sms_integrator_equals_path(sms, workloads, O):
     assert a.mean() > 0.0
 
 
-def test_path_sms_ss_matches_path_on_flat_water(sms, workloads, O):
+@pytest.mark.parametrize("floor", ["diffuse", "roughplastic", "roughconductor"])
+def test_path_sms_ss_matches_path_on_flat_water(sms, workloads, O, floor):
     """Flat water: SMS finds the one refraction solution of every receiver
     point, so path_sms_ss (unbiased) and plain path tracing estimate the same
-    image; compare 3x3-pixel blocks against the sample spread of 4 runs."""
+    image; compare 3x3-pixel blocks against the sample spread of 4 runs.  A
+    glossy floor evaluates its own BSDF toward the caster
+    (manifold_ss.cpp:109, 191)."""
     W = workloads
-    osc = O.OracleScene(W.pool_scene(res=16, wave_scale=0.0))
+    fb = {"diffuse": None,
+          "roughplastic": sms.Bsdf(sms.BSDF_ROUGHPLASTIC, 1.5, 0.0, (0.4, 0.5, 0.6), alpha=0.3),
+          "roughconductor": sms.Bsdf(sms.BSDF_CONDUCTOR, 0.2, 3.0, alpha=0.4)}[floor]
+    osc = O.OracleScene(W.pool_scene(res=16, wave_scale=0.0, floor_bsdf=fb))
     cam = W.pool_camera(12, 12)
     cfg = W.water_config()
     cfg.max_trials = -1
@@ -243,3 +249,33 @@ def test_twosided_diffuse(sms, workloads, O):
     assert front.mean() > 0.01
     assert abs(back.mean() - front.mean()) < 0.03 * front.mean()
     assert not dark.any()
+
+
+def test_tagged_receiver_query(sms, workloads, O):
+    """A query naming its receiver shape (row 12 = -(1 + id), rows 13-14 the
+    incident direction in the frame of its normal) evaluates that shape's
+    BSDF: a diffuse shape gives the albedo query's estimate, a rough
+    conductor its own glossy value, an id outside the scene nothing."""
+    W = workloads
+    far = np.array([[-1, -1, -10], [1, -1, -10], [1, 1, -10], [-1, 1, -10]], np.float32)
+    tri = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    cfg = W.sphere_config()
+    q = W.sphere_queries(16)
+    t = q.copy()
+    t[12], t[13], t[14] = -2.0, 0.0, 0.0
+    d = W.sphere_scene(conductor=True)
+    d.add_mesh(far, tri, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5, 0.5, 0.5)))
+    osc = O.OracleScene(d)
+    va, ca, _ = osc.connect_batch(cfg, q, seed=4)[:3]
+    vt, ct, _ = osc.connect_batch(cfg, t, seed=4)[:3]
+    assert va.sum() > 0
+    np.testing.assert_array_equal(ca, ct)
+    np.testing.assert_allclose(vt, va, rtol=1e-5, atol=1e-7)
+    d = W.sphere_scene(conductor=True)
+    d.add_mesh(far, tri, sms.Bsdf(sms.BSDF_CONDUCTOR, 0.2, 3.0, alpha=0.3))
+    osc = O.OracleScene(d)
+    vg = osc.connect_batch(cfg, t, seed=4)[0]
+    np.testing.assert_array_equal(osc.connect_batch(cfg, t, seed=4)[1], ca)
+    assert vg.sum() > 0 and not np.allclose(vg, va)
+    t[12] = -9.0
+    assert not osc.connect_batch(cfg, t, seed=4)[0].any()

@@ -63,6 +63,30 @@ def test_glossy_receiver_connections_match_oracle(sms, workloads, oracle, gpu_li
     assert abs(vg.sum() - vo.sum()) < 0.02 * vo.sum()
 
 
+def test_glossy_receiver_chains_match_oracle(sms, workloads, oracle, gpu_lib):
+    """Two-bounce chains through the slab ending at a rough-conductor
+    receiver (manifold_ms.cpp:113, 190), biased, GPU vs the oracle with the
+    oracle's FMA build as the floor."""
+    from test_gpu_ss_parity import FLOOR_FACTOR, FLOOR_SLACK, _connect_diff
+    W = workloads
+    d = W.slab_scene()
+    rid = d.add_mesh(_FAR, _TRI, sms.Bsdf(sms.BSDF_CONDUCTOR, 0.2, 3.0, alpha=0.3))
+    cfg = W.slab_config()
+    q = _tagged(W.slab_queries(2048), rid, (0.0, 0.6))
+    q[15] = 0.8
+    ms = sms.SpecularManifoldMultiScatter(sms.Context(sms.Scene(d), cfg))
+    vg, cg, wg = ms.specular_manifold_sampling(q, seed=2)
+    vo, co, wo, _ = oracle.OracleScene(d).connect_batch(cfg, q, seed=2, multi=True)
+    vf, cf, wf, _ = oracle.OracleScene(d, fma=True).connect_batch(cfg, q, seed=2, multi=True)
+    assert vo.sum() > 0
+    g_cm, g_diff, g_med = _connect_diff(vg, cg, wg, vo, co, wo)
+    f_cm, f_diff, _ = _connect_diff(vf, cf, wf, vo, co, wo)
+    assert g_cm <= FLOOR_FACTOR * f_cm + FLOOR_SLACK
+    assert g_diff <= FLOOR_FACTOR * f_diff + FLOOR_SLACK
+    assert g_med < 1e-4
+    assert abs(vg.mean() - vo.mean()) <= 0.01 * vo.mean()
+
+
 def test_receiver_outside_the_scene_is_an_error(sms, workloads, gpu_lib):
     W = workloads
     d = _scene(sms, W, sms.Bsdf(sms.BSDF_DIFFUSE, 1.0, 0.0, (0.5, 0.5, 0.5)))

@@ -349,6 +349,10 @@ sms_status sms_ss_connect_batch_device(sms_ctx *ctx, const float *queries_dev,
  *     up the array's device address and lets the CUDA runtime load the module
  *     that holds it; make that first call before any stream capture.
  *   - Its kernels are not included in sms_profile_read's phase times.
+ *   - It does not synchronize, so it cannot return SMS_ERR_DEVICE_LIMIT: a
+ *     device limit its kernels hit (traversal stack, trial cap, solution
+ *     capacity, a receiver shape outside the scene) is reported by the
+ *     context's next synchronous call.
  *   - All calls, from every context on a device, share the one array: calls
  *     whose kernels overlap on the GPU (different streams, or different
  *     contexts) race on it.  Calls issued on one stream are safe.

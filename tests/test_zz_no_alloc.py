@@ -89,3 +89,24 @@ def test_noalloc_biased_matches_device_and_shares_its_checks(sms, workloads, gpu
             fn(q_dev.data_ptr(), n, out[0].data_ptr(), out[3].data_ptr(), out[4].data_ptr(), seed=1)
         assert e.value.status == 1 and "max_trials" in str(e.value)
     ctx.close()
+
+
+def test_noalloc_device_limit_reported_by_next_call(sms, workloads, gpu_lib):
+    """A device limit hit inside an allocation-free call (here a query naming
+    a receiver shape outside the scene) is not returned by that asynchronous
+    call; the context's next synchronous call reports it, and the one after
+    that runs clean."""
+    import torch
+    W = workloads
+    ctx = sms.Context(sms.Scene(W.sphere_scene(conductor=True)), W.sphere_config())
+    ss = sms.SpecularManifoldSingleScatter(ctx)
+    q = W.sphere_queries(16)
+    bad = q.copy()
+    bad[12] = -9.0
+    n = q.shape[1]
+    _run(ss.specular_manifold_sampling_noalloc, ctx, torch.from_numpy(bad).cuda(), n, 1)
+    with pytest.raises(sms.SMSError, match="receiver shape"):
+        ss.specular_manifold_sampling(q, seed=1)
+    v, c, _ = ss.specular_manifold_sampling(q, seed=1)
+    assert c.sum() > 0
+    ctx.close()
